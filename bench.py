@@ -1,0 +1,356 @@
+"""Benchmark: streaming RMAT scale 22 on the tile store, BFS / CC / SSSP re-run
+incrementally after every batch.
+
+Workload (the GPU-sized streaming configuration): 4,194,304 vertices, RMAT graph500
+parameters, seed 2, uint32 weights uniform in [1, 255] (a pure function of
+(src, tgt)), batches of 1,048,576 edges inserted in generation order; after each
+batch the tile store is compacted and BFS (source 0), CC (min label) and SSSP
+(source 0) continue from their previous state to the new fixed point. One step =
+one batch: insert + compact + the three runs. 64 batches make the full 67,108,864-
+edge stream; the default run uses W = 3 warm-up batches and K = 61 timed batches.
+
+Metric: GTEPS by the reference's counting rule (edges of tiles with an active
+source, summed over rounds and algorithms, algorithm-executor.h:424-426) per second
+of device time, plus ingest M edges/s. `value` times device-resident inputs;
+`e2e` feeds every batch from pinned host memory through the public C ABI and reads
+the per-run statistics back.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "GTEPS & HBM GB/s per executor, M edges/s ingest; batched/FP32 vs plain at tol"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=61)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="cytom", choices=["cytom", "reference"])
+    ap.add_argument("--scale", type=int, default=22)
+    ap.add_argument("--batch", type=int, default=1 << 20)
+    ap.add_argument("--vpt", type=int, default=65536)
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--max-iter", type=int, default=100)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-steps", type=int, default=4)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, path: Path, index: int):
+        self.path, self.index, self.proc = path, index, None
+
+    def start(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        self.proc.wait()
+        self.fh.close()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if f[5 + k].lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(args, budget_s: float = 20.0) -> dict:
+    """The oracle (single-thread C port of the reference executor) on a bounded
+    sample of the same workload: the graph after the first batches, BFS / CC / SSSP
+    run to their fixed points, counted by the same rule."""
+    from oracle import oracle as orc
+    n = 1 << args.scale
+    st = orc.Store(n, args.vpt, weighted=True)
+    total_edges, total_t, batches = 0, 0.0, 0
+    t_start = time.time()
+    while time.time() - t_start < budget_s and batches < 64:
+        s, t = orc.rmat(args.scale, batches * args.batch, args.batch, args.seed)
+        w = orc.edge_weights(s, t, args.seed + 1000)
+        st.insert(s, t, w)
+        st.compact()
+        batches += 1
+        t0 = time.perf_counter()
+        for algo in (orc.BFS, orc.CC, orc.SSSP):
+            _, info = st.run_minprop(algo, start=0, max_iter=args.max_iter)
+            total_edges += info["count_edges"]
+        total_t += time.perf_counter() - t0
+    return {"value": total_edges / total_t / 1e9, "unit": "GTEPS", "cores": 1, "kind": "port",
+            "sample": f"first {batches} batches of the stream; BFS/CC/SSSP from scratch after each "
+                      f"(single-thread oracle)"}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    t0 = time.time()
+    cb = cpu_baseline(args, budget_s=max(20.0, 10.0 * (args.steps + args.warmup) / 64))
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "GTEPS",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic RMAT (graph500 a,b,c), generated",
+            "config": {"workload": f"streaming RMAT-{args.scale}, {args.batch}-edge batches, "
+                                   "compaction + BFS/CC/SSSP after each batch",
+                       "vertices_per_tile": args.vpt},
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": cb["value"], "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": time.time() - t0}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    import numpy as np
+    import torch
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    import cytom_gb300 as cg
+
+    n = 1 << args.scale
+    B = args.batch
+    nsteps = args.warmup + args.steps
+    stream = torch.cuda.Stream(device=dev)
+    out_dir = ROOT / "gpurun_out"
+    out_dir.mkdir(exist_ok=True)
+
+    def make_engine():
+        eng = cg.Engine(n, args.vpt, weight_type=cg.WEIGHT_U32, stream=stream.cuda_stream)
+        progs = [cg.BFS(eng, start_vertex=0, max_iterations=args.max_iter),
+                 cg.CC(eng, max_iterations=args.max_iter),
+                 cg.SSSP(eng, start_vertex=0, max_iterations=args.max_iter)]
+        return eng, progs
+
+    # device-resident inputs for every step (generated by the library's RMAT kernel)
+    eng, progs = make_engine()
+    d_src = torch.empty(nsteps * B, dtype=torch.int32, device=dev)
+    d_tgt = torch.empty_like(d_src)
+    d_w = torch.empty_like(d_src)
+    with torch.cuda.stream(stream):
+        eng.generate_rmat(0, nsteps * B, args.scale, seed=args.seed, weight_seed=args.seed + 1000,
+                          wmin=1, wmax=255, out=(d_src, d_tgt, d_w))
+    stream.synchronize()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > L2 (126 MB)
+
+    def step(e, ps, k, srcs):
+        s, t, w = srcs
+        e.insert_edges_device(s.data_ptr() + 4 * k * B, t.data_ptr() + 4 * k * B,
+                              w.data_ptr() + 4 * k * B, B)
+        e.do_global_compaction()
+        return [p.execute_algorithm() for p in ps]
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(nsteps)]
+    for k in range(args.warmup):
+        step(eng, progs, k, (d_src, d_tgt, d_w))
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(out_dir / f"clocks_rank{rank}.csv", local)
+    clocks.start()
+    launches0 = eng.launch_count()
+    teps_edges, scanned, ingest_ms, total_ms = 0, 0, 0.0, 0.0
+    per_algo = [0, 0, 0]
+    per_algo_ms = [0.0, 0.0, 0.0]
+    for k in range(args.warmup, nsteps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        a, b, c = ev[k]
+        a.record(stream)
+        eng.insert_edges_device(d_src.data_ptr() + 4 * k * B, d_tgt.data_ptr() + 4 * k * B,
+                                d_w.data_ptr() + 4 * k * B, B)
+        eng.do_global_compaction()
+        b.record(stream)
+        stats = [p.execute_algorithm() for p in progs]
+        c.record(stream)
+        for i, s in enumerate(stats):
+            teps_edges += s["count_edges"]
+            scanned += s["edges_scanned"]
+            per_algo[i] += s["count_edges"]
+            per_algo_ms[i] += s["elapsed_ms"]
+    torch.cuda.synchronize()
+    launches = eng.launch_count() - launches0
+    clk = clocks.stop()
+    for k in range(args.warmup, nsteps):
+        a, b, c = ev[k]
+        ingest_ms += a.elapsed_time(b)
+        total_ms += a.elapsed_time(c)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+        te = torch.tensor([teps_edges], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(te)
+        teps_all = float(te.item())
+    else:
+        teps_all = float(teps_edges)
+    value = teps_all / (total_ms / 1e3) / 1e9
+    ingest_meps = world * args.steps * B / (ingest_ms / 1e3) / 1e6
+    final_edges = eng.count_edges()[0]
+
+    # ---- roofline pass: the gather kernel timed per launch with CUDA events on the
+    # engine's stream (profiling mode drives the loop from the host), on the next
+    # batches of the same stream
+    eng.reset_kernel_stats()
+    eng.set_profiling(True)
+    prof_stats = []
+    extra = min(args.profile_steps, 64)
+    src_h, tgt_h, w_h = eng.generate_rmat(nsteps * B, extra * B, args.scale, seed=args.seed,
+                                          weight_seed=args.seed + 1000, wmin=1, wmax=255)
+    for k in range(extra):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        sl = slice(k * B, (k + 1) * B)
+        eng.insert_edges(src_h[sl].copy(), tgt_h[sl].copy(), w_h[sl].copy())
+        eng.do_global_compaction()
+        prof_stats.append([(i, p.execute_algorithm()) for i, p in enumerate(progs)])
+    ks = eng.kernel_stats()
+    eng.set_profiling(False)
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    gbytes = 0.0
+    for runs in prof_stats:
+        for i, s in runs:
+            wbytes = 4 if i == 2 else 0
+            # algorithmic bytes of the gather: packed edge (+ weight) per
+            # scanned edge, one value per active source, atomic read+write per changed
+            # target, the frontier bitmap once per round
+            gbytes += s["edges_scanned"] * (4 + wbytes) + s["active_vertices"] * (4 + 8) \
+                + s["iterations"] * (n / 8)
+    g = ks["gather"]
+    achieved = gbytes / (g["total_ms"] / 1e3) / 1e9 if g["total_ms"] > 0 else None
+    traffic = None
+    tfile = ROOT / "profiles" / "gather_traffic.json"
+    if tfile.exists():
+        try:
+            traffic = json.loads(tfile.read_text()).get("bytes_per_launch")
+        except Exception:
+            traffic = None
+
+    # ---- end to end: a fresh engine fed from pinned host memory through the C ABI
+    e2e = None
+    if not args.no_e2e:
+        eng2, progs2 = make_engine()
+        hs = torch.empty(nsteps * B, dtype=torch.int32, pin_memory=True)
+        ht = torch.empty_like(hs)
+        hw = torch.empty_like(hs)
+        hs.copy_(d_src.cpu())
+        ht.copy_(d_tgt.cpu())
+        hw.copy_(d_w.cpu())
+        hsn, htn, hwn = hs.numpy().view(np.uint32), ht.numpy().view(np.uint32), hw.numpy().view(np.uint32)
+        for k in range(args.warmup):
+            sl = slice(k * B, (k + 1) * B)
+            eng2.insert_edges(hsn[sl], htn[sl], hwn[sl])
+            eng2.do_global_compaction()
+            [p.execute_algorithm() for p in progs2]
+        torch.cuda.synchronize()
+        e_edges, e_ms = 0, 0.0
+        evs = []
+        for k in range(args.warmup, nsteps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            a, c = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            sl = slice(k * B, (k + 1) * B)
+            eng2.insert_edges(hsn[sl], htn[sl], hwn[sl])  # H2D from pinned host buffers
+            eng2.do_global_compaction()
+            st2 = [p.execute_algorithm() for p in progs2]  # per-run statistics read back (D2H)
+            c.record(stream)
+            evs.append((a, c))
+            e_edges += sum(s["count_edges"] for s in st2)
+        torch.cuda.synchronize()
+        e_ms = sum(a.elapsed_time(c) for a, c in evs)
+        e2e = {"value": world * e_edges / (e_ms / 1e3) / 1e9, "unit": "GTEPS",
+               "h2d_bytes_per_step": B * 12, "d2h_bytes_per_step": 3 * 160 + 16}
+        eng2.close()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(args)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic RMAT (graph500 a,b,c), generated on the device",
+            "config": {"workload": f"streaming RMAT-{args.scale}: {args.batch}-edge batches, compaction "
+                                   f"+ incremental BFS/CC/SSSP after each batch",
+                       "vertices": n, "vertices_per_tile": args.vpt, "batch_edges": B,
+                       "max_iterations": args.max_iter, "parallelism": "replicas" if world > 1 else "1 GPU",
+                       "l2": "flushed (256 MiB write) before every timed step"},
+            "ingest_medges_per_s": ingest_meps,
+            "gteps_per_algorithm": {nm: per_algo[i] / (per_algo_ms[i] / 1e3) / 1e9 if per_algo_ms[i] else None
+                                    for i, nm in enumerate(["bfs", "cc", "sssp"])},
+            "edges_scanned_per_s": scanned / (total_ms / 1e3),
+            "final_edges": final_edges,
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": (achieved / hbm_peak) if achieved else None, "traffic": traffic,
+                         "kernel": "gather_minprop", "launches": g["launches"],
+                         "avg_launch_us": (g["total_ms"] * 1e3 / g["launches"]) if g["launches"] else None,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
+            "kernel_time_ms": {k: v["total_ms"] for k, v in ks.items() if v["launches"]},
+            "clocks": clk,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

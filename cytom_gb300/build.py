@@ -1,0 +1,72 @@
+"""Build recipe for libcytom_gpu.so (sm_103a) — nvcc only, no cmake.
+
+Compiles every translation unit under csrc/ in parallel into cytom_gb300/_build/
+and links cytom_gb300/libcytom_gpu.so in place.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+LIB = PKG / "libcytom_gpu.so"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ARCH + [
+    "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+    "--expt-relaxed-constexpr", "-diag-suppress", "177",
+]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and Path(cand).exists():
+            return cand
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build cytom_gb300")
+
+
+def sources() -> list[Path]:
+    return sorted(CSRC.glob("*.cu"))
+
+
+def _stale(obj: Path, src: Path) -> bool:
+    if not obj.exists():
+        return True
+    deps = [src, *CSRC.glob("*.h"), *(PKG.parent / "include").glob("*.h")]
+    return any(d.stat().st_mtime > obj.stat().st_mtime for d in deps)
+
+
+def build(verbose: bool = False, force: bool = False) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    cc = nvcc()
+    jobs = []
+    for src in sources():
+        obj = BUILD / (src.stem + ".o")
+        if force or _stale(obj, src):
+            jobs.append([cc, *NVCC_FLAGS, "-I", str(PKG.parent / "include"), "-c", str(src), "-o", str(obj)])
+    if jobs:
+        with cf.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
+            results = list(ex.map(lambda cmd: subprocess.run(cmd, capture_output=True, text=True), jobs))
+        for cmd, r in zip(jobs, results):
+            if verbose or r.returncode != 0:
+                print(" ".join(cmd))
+                print(r.stdout, r.stderr)
+            if r.returncode != 0:
+                raise RuntimeError(f"nvcc failed for {cmd[-3]}")
+    objs = [str(BUILD / (s.stem + ".o")) for s in sources()]
+    if force or jobs or not LIB.exists():
+        cmd = [cc, *ARCH, "-shared", "-o", str(LIB), *objs]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            print(" ".join(cmd), r.stdout, r.stderr)
+            raise RuntimeError("link of libcytom_gpu.so failed")
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose=True))

@@ -1,0 +1,657 @@
+// capi.cu — the C ABI (include/cytom_gpu.h): contexts, buffers, jobs, statistics.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+
+namespace cytom {
+
+int minprop_alloc(Ctx* c, Job* j);
+int minprop_init(Ctx* c, Job* j);
+int minprop_seed(Ctx* c, Job* j, const uint32_t* src, const uint32_t* tgt, const uint32_t* w,
+                 uint64_t count);
+int minprop_run(Ctx* c, Job* j);
+int pagerank_alloc(Ctx* c, Job* j);
+int pagerank_init(Ctx* c, Job* j);
+int pagerank_seed(Ctx* c, Job* j, const uint32_t* src, const uint32_t* tgt, const uint32_t* w,
+                  uint64_t count);
+int pagerank_run(Ctx* c, Job* j);
+int pagerank_result(Ctx* c, Job* j, void* out, int where);
+
+int set_err(Ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int cuda_err(Ctx* c, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return CYTOM_OK;
+  if (c) c->err = std::string(what) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return CYTOM_ERR_OOM;
+  return CYTOM_ERR_CUDA;
+}
+
+// ---- profiling: CUDA events around launches --------------------------------
+static const char* kClassNames[CYTOM_KERNEL_CLASSES] = {"rmat", "insert", "sort", "merge",
+                                                        "gather", "apply", "pagerank", "other"};
+
+int prof_begin(Ctx* c, int cls) {
+  if (!c->profiling) return -1;
+  cudaEvent_t a, b;
+  if (c->ev_pool.size() >= 2) {
+    a = c->ev_pool.back();
+    c->ev_pool.pop_back();
+    b = c->ev_pool.back();
+    c->ev_pool.pop_back();
+  } else {
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+  }
+  cudaEventRecord(a, c->stream);
+  c->pending.push_back({cls, a, b, 0.0});
+  return (int)c->pending.size() - 1;
+}
+
+void prof_end(Ctx* c, int slot, double bytes) {
+  if (slot < 0 || !c->profiling) return;
+  cudaEventRecord(c->pending[slot].b, c->stream);
+  c->pending[slot].bytes = bytes;
+}
+
+int prof_flush(Ctx* c) {
+  if (c->pending.empty()) return CYTOM_OK;
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "profiling sync");
+  for (auto& p : c->pending) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p.a, p.b);
+    c->kstats.launches[p.cls] += 1;
+    c->kstats.total_ms[p.cls] += ms;
+    if (p.bytes > 0) c->kstats.algo_bytes[p.cls] += p.bytes;
+    c->ev_pool.push_back(p.a);
+    c->ev_pool.push_back(p.b);
+  }
+  c->pending.clear();
+  return CYTOM_OK;
+}
+
+int upload_store_desc(Ctx* c) {
+  StoreDesc& h = c->hsd;
+  h.edges = c->edges;
+  h.wts = c->wts;
+  h.tile_ptr = c->tile_ptr;
+  h.chunk_tile = c->chunk_tile;
+  h.out_deg = c->out_deg;
+  h.in_deg = c->in_deg;
+  h.E = c->E;
+  h.nchunks = (c->E + kChunk - 1) / kChunk;
+  h.n = c->n;
+  h.T = c->T;
+  h.ntiles = c->ntiles;
+  h.lvpt = c->lvpt;
+  h.lT = c->lT;
+  h.wtype = c->wtype;
+  // pageable source: the copy is staged before the call returns, so h may change later
+  cudaError_t e = cudaMemcpyAsync(c->dsd, &h, sizeof(StoreDesc), cudaMemcpyHostToDevice, c->stream);
+  return cuda_err(c, e, "store descriptor upload");
+}
+
+static uint32_t ilog2(uint64_t v) {
+  uint32_t r = 0;
+  while ((1ULL << r) < v) ++r;
+  return r;
+}
+
+// ---- jobs -----------------------------------------------------------------
+static bool is_minprop(int a) { return a == CYTOM_ALGO_BFS || a == CYTOM_ALGO_CC || a == CYTOM_ALGO_SSSP; }
+
+int job_alloc(Ctx* c, Job* j) {
+  cudaError_t e = cudaMalloc(&j->ls, sizeof(LoopState));
+  if (e != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "loop state");
+  cudaMemsetAsync(j->ls, 0, sizeof(LoopState), c->stream);
+  j->h.ls = j->ls;
+  j->h.algo = j->algo;
+  j->h.kahan = j->params.kahan;
+  j->h.alpha = j->params.alpha;
+  j->h.delta_param = j->params.delta;
+  j->h.start = j->params.start_vertex;
+  int rc = is_minprop(j->algo) ? minprop_alloc(c, j) : pagerank_alloc(c, j);
+  if (rc) return rc;
+  e = cudaMalloc(&j->d, sizeof(JobDesc));
+  if (e != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "job descriptor");
+  e = cudaMemcpyAsync(j->d, &j->h, sizeof(JobDesc), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  return cuda_err(c, e, "job descriptor upload");
+}
+
+void job_free(Ctx* c, Job* j) {
+  (void)c;
+  if (j->loop_exec) cudaGraphExecDestroy(j->loop_exec);
+  void* ptrs[] = {j->h.cur, j->h.next, j->h.fa, j->h.ch, j->h.rows, j->h.rank, j->h.rank_c,
+                  j->h.delta, j->h.dsum, j->h.contrib, j->h.rank64, j->h.dsum64, j->h.deg_distinct,
+                  j->ls, j->d};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+}
+
+int job_init_state(Ctx* c, Job* j) {
+  return is_minprop(j->algo) ? minprop_init(c, j) : pagerank_init(c, j);
+}
+
+int job_seed(Ctx* c, Job* j, const uint32_t* src, const uint32_t* tgt, const uint32_t* w,
+             uint64_t count) {
+  return is_minprop(j->algo) ? minprop_seed(c, j, src, tgt, w, count)
+                             : pagerank_seed(c, j, src, tgt, w, count);
+}
+
+int job_run(Ctx* c, Job* j, cytom_run_stats* st) {
+  int rc = compact(c);
+  if (rc) return rc;
+  if (j->fresh) {
+    rc = job_init_state(c, j);
+    if (rc) return rc;
+    j->fresh = false;
+  }
+  cudaEventRecord(c->run_a, c->stream);
+  rc = is_minprop(j->algo) ? minprop_run(c, j) : pagerank_run(c, j);
+  if (rc) return rc;
+  cudaEventRecord(c->run_b, c->stream);
+  LoopState ls;
+  cudaError_t e = cudaMemcpyAsync(&ls, j->ls, sizeof(LoopState), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "run");
+  rc = prof_flush(c);
+  if (rc) return rc;
+  if (ls.err) return set_err(c, CYTOM_ERR_TIMEOUT, "a bounded device wait gave up");
+  if (j->last_run_graph) c->launches += 3ULL * ls.iter;
+  if (st) {
+    memset(st, 0, sizeof(*st));
+    st->iterations = ls.iter;
+    st->count_edges = ls.count_edges;
+    st->edges_scanned = ls.edges_scanned;
+    st->active_vertices = ls.active_total;
+    st->converged = (ls.cont == 0 && ls.iter < ls.max_iter) ? 1 : (ls.cont == 0 ? 1 : 0);
+    st->residual = ls.resid_final;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->run_a, c->run_b);
+    st->elapsed_ms = ms;
+  }
+  return CYTOM_OK;
+}
+
+}  // namespace cytom
+
+using namespace cytom;
+
+extern "C" {
+
+void cytom_config_default(cytom_config* cfg) {
+  if (!cfg) return;
+  memset(cfg, 0, sizeof(*cfg));
+  cfg->max_vertices = 1ULL << 16;
+  cfg->vertices_per_tile = 65536;  // VERTICES_PER_TILE, src/scripts/config.py:91
+  cfg->weight_type = CYTOM_UNWEIGHTED;
+  cfg->enable_adaptive_scheduling = 1;
+  cfg->edge_capacity_hint = 0;
+  cfg->stream = nullptr;
+}
+
+void cytom_rmat_default(cytom_rmat_params* p) {
+  if (!p) return;
+  memset(p, 0, sizeof(*p));
+  p->scale = 16;
+  p->a = (double)0.57f;  // RMAT_A, src/include/util/datatypes.h:17
+  p->b = (double)0.19f;
+  p->c = (double)0.19f;
+  p->seed = 2;  // RMAT_SEED, datatypes.h:20
+  p->weight_seed = 0;
+  p->wmin = 1;
+  p->wmax = 0;
+}
+
+void cytom_job_params_default(cytom_job_params* p) {
+  if (!p) return;
+  memset(p, 0, sizeof(*p));
+  p->start_vertex = 1;  // DEFAULT_ALGORITHM_START_VERTEX, src/scripts/config.py:107
+  p->max_iterations = 100;  // MAX_ITERATIONS, config.py:46
+  p->delta = 0.01;  // DEFAULT_DELTA, config.py:105
+  p->alpha = 0.85;  // ALPHA, examples/pagerank-delta.cc:19
+  p->tolerance = 0.0;
+  p->kahan = 1;
+}
+
+int cytom_create(const cytom_config* cfg, cytom_ctx** out) {
+  if (!cfg || !out) return CYTOM_ERR_INVAL;
+  *out = nullptr;
+  Ctx* c = new (std::nothrow) Ctx();
+  if (!c) return CYTOM_ERR_OOM;
+  c->cfg = *cfg;
+  uint64_t n = 1;
+  while (n < cfg->max_vertices) n <<= 1;  // Config::normalizeConfig rounds up to 2^k
+  uint64_t vpt = cfg->vertices_per_tile;
+  if (cfg->max_vertices == 0 || vpt == 0 || (vpt & (vpt - 1)) || vpt > 65536 || vpt > n ||
+      n > (1ULL << 32) || (cfg->weight_type < 0 || cfg->weight_type > 2)) {
+    delete c;
+    return CYTOM_ERR_INVAL;  // the reference gets 0 tiles when vpt > vertices (config.cc:18-19)
+  }
+  c->n = n;
+  c->vpt = vpt;
+  c->T = n / vpt;
+  c->ntiles = c->T * c->T;
+  c->lvpt = ilog2(vpt);
+  c->lT = ilog2(c->T);
+  c->wtype = cfg->weight_type;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    delete c;
+    return CYTOM_ERR_CUDA;
+  }
+  cudaGetDevice(&c->device);
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+  if (cfg->stream) {
+    c->stream = (cudaStream_t)cfg->stream;
+  } else {
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    c->own_stream = true;
+  }
+  // keep stream-ordered temporaries cached in the pool
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, c->device) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  bool ok = e == cudaSuccess;
+  ok = ok && cudaMalloc(&c->out_deg, n * 4) == cudaSuccess;
+  ok = ok && cudaMalloc(&c->in_deg, n * 4) == cudaSuccess;
+  ok = ok && cudaMalloc(&c->tile_ptr, (c->ntiles + 1) * 8) == cudaSuccess;
+  ok = ok && cudaMalloc(&c->tile_ptr_alt, (c->ntiles + 1) * 8) == cudaSuccess;
+  ok = ok && cudaMalloc(&c->dsd, sizeof(StoreDesc)) == cudaSuccess;
+  ok = ok && cudaMalloc(&c->d_flag, 64) == cudaSuccess;
+  ok = ok && cudaMallocHost(&c->h_pinned, 64) == cudaSuccess;
+  ok = ok && cudaEventCreate(&c->run_a) == cudaSuccess;
+  ok = ok && cudaEventCreate(&c->run_b) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    cytom_destroy((cytom_ctx*)c);
+    return CYTOM_ERR_OOM;
+  }
+  cudaMemsetAsync(c->out_deg, 0, n * 4, c->stream);
+  cudaMemsetAsync(c->in_deg, 0, n * 4, c->stream);
+  cudaMemsetAsync(c->tile_ptr, 0, (c->ntiles + 1) * 8, c->stream);
+  cudaMemsetAsync(c->tile_ptr_alt, 0, (c->ntiles + 1) * 8, c->stream);
+  for (int k = 0; k < CYTOM_KERNEL_CLASSES; ++k)
+    snprintf(c->kstats.name[k], sizeof(c->kstats.name[k]), "%s", kClassNames[k]);
+  int rc = CYTOM_OK;
+  uint64_t hint = std::max<uint64_t>(cfg->edge_capacity_hint, 1024);
+  (void)hint;
+  // the store starts empty with a small capacity; chunk table for zero edges
+  c->cap = 0;
+  c->chunk_cap = 0;
+  {
+    uint32_t* ct = nullptr;
+    if (cudaMalloc(&ct, 2 * 4) != cudaSuccess) rc = CYTOM_ERR_OOM;
+    c->chunk_tile = ct;
+    c->chunk_cap = 2;
+    if (ct) cudaMemsetAsync(ct, 0, 8, c->stream);
+  }
+  if (!rc) rc = upload_store_desc(c);
+  if (!rc && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = CYTOM_ERR_CUDA;
+  if (rc) {
+    cytom_destroy((cytom_ctx*)c);
+    return rc;
+  }
+  *out = (cytom_ctx*)c;
+  return CYTOM_OK;
+}
+
+int cytom_destroy(cytom_ctx* ctx) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c) return CYTOM_ERR_INVAL;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (Job* j : c->jobs)
+    if (j) {
+      job_free(c, j);
+      delete j;
+    }
+  void* ptrs[] = {c->edges, c->wts, c->edges_alt, c->wts_alt, c->tile_ptr, c->tile_ptr_alt,
+                  c->chunk_tile, c->app_keys, c->app_keys_alt, c->app_w, c->app_w_alt,
+                  c->out_deg, c->in_deg, c->dsd, c->scratch, c->d_flag};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (c->h_pinned) cudaFreeHost(c->h_pinned);
+  for (auto& p : c->pending) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  for (auto ev : c->ev_pool) cudaEventDestroy(ev);
+  if (c->run_a) cudaEventDestroy(c->run_a);
+  if (c->run_b) cudaEventDestroy(c->run_b);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return CYTOM_OK;
+}
+
+const char* cytom_last_error(const cytom_ctx* ctx) {
+  const Ctx* c = (const Ctx*)ctx;
+  return c ? c->err.c_str() : "null context";
+}
+
+int cytom_geometry(const cytom_ctx* ctx, uint64_t* vertices, uint64_t* vpt, uint64_t* tpd) {
+  const Ctx* c = (const Ctx*)ctx;
+  if (!c) return CYTOM_ERR_INVAL;
+  if (vertices) *vertices = c->n;
+  if (vpt) *vpt = c->vpt;
+  if (tpd) *tpd = c->T;
+  return CYTOM_OK;
+}
+
+// Device staging for host inputs.
+struct Staging {
+  void* p = nullptr;
+  cudaStream_t s = nullptr;
+  ~Staging() {
+    if (p) cudaFreeAsync(p, s);
+  }
+};
+
+int cytom_rmat_generate(cytom_ctx* ctx, const cytom_rmat_params* p, uint64_t first, uint64_t count,
+                        uint32_t* src, uint32_t* tgt, uint32_t* w, int where) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !p || !src || !tgt) return CYTOM_ERR_INVAL;
+  if (p->scale == 0 || p->scale > 32 || (p->wmax > 0 && (p->wmin > p->wmax || !w)))
+    return set_err(c, CYTOM_ERR_INVAL, "bad rmat parameters");
+  if (count == 0) return CYTOM_OK;
+  if (where == CYTOM_PTR_DEVICE) {
+    int rc = rmat_generate(c, p, first, count, src, tgt, w);
+    if (rc) return rc;
+    return cuda_err(c, cudaStreamSynchronize(c->stream), "rmat");
+  }
+  Staging st;
+  st.s = c->stream;
+  size_t per = (p->wmax > 0) ? 12 : 8;
+  if (cudaMallocAsync(&st.p, count * per, c->stream) != cudaSuccess)
+    return set_err(c, CYTOM_ERR_OOM, "rmat staging");
+  uint32_t* ds = (uint32_t*)st.p;
+  uint32_t* dt = ds + count;
+  uint32_t* dw = (p->wmax > 0) ? dt + count : nullptr;
+  int rc = rmat_generate(c, p, first, count, ds, dt, dw);
+  if (rc) return rc;
+  cudaMemcpyAsync(src, ds, count * 4, cudaMemcpyDeviceToHost, c->stream);
+  cudaMemcpyAsync(tgt, dt, count * 4, cudaMemcpyDeviceToHost, c->stream);
+  if (dw) cudaMemcpyAsync(w, dw, count * 4, cudaMemcpyDeviceToHost, c->stream);
+  return cuda_err(c, cudaStreamSynchronize(c->stream), "rmat copy");
+}
+
+int cytom_gridgraph_decode(cytom_ctx* ctx, const void* bytes, uint64_t size, uint32_t* src,
+                           uint32_t* tgt, int where, uint64_t* count) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || (!bytes && size)) return CYTOM_ERR_INVAL;
+  uint64_t m = size / 8;
+  if (count) *count = m;
+  if (m == 0) return CYTOM_OK;
+  Staging st;
+  st.s = c->stream;
+  size_t need = m * 8 + (where == CYTOM_PTR_HOST ? m * 8 : 0);
+  if (cudaMallocAsync(&st.p, need, c->stream) != cudaSuccess)
+    return set_err(c, CYTOM_ERR_OOM, "gridgraph staging");
+  void* drec = st.p;
+  cudaMemcpyAsync(drec, bytes, m * 8, cudaMemcpyHostToDevice, c->stream);
+  uint32_t *ds = src, *dt = tgt;
+  if (where == CYTOM_PTR_HOST) {
+    ds = (uint32_t*)((char*)st.p + m * 8);
+    dt = ds + m;
+  }
+  int rc = gridgraph_decode(c, drec, m, ds, dt);
+  if (rc) return rc;
+  if (where == CYTOM_PTR_HOST) {
+    cudaMemcpyAsync(src, ds, m * 4, cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(tgt, dt, m * 4, cudaMemcpyDeviceToHost, c->stream);
+  }
+  return cuda_err(c, cudaStreamSynchronize(c->stream), "gridgraph copy");
+}
+
+int cytom_insert_batch(cytom_ctx* ctx, const uint32_t* src, const uint32_t* tgt, const uint32_t* w,
+                       uint64_t count, int where) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || (count && (!src || !tgt))) return CYTOM_ERR_INVAL;
+  if (count == 0) return CYTOM_OK;
+  if (where == CYTOM_PTR_DEVICE) {
+    int rc = insert_device(c, src, tgt, w, count);
+    if (rc) return rc;
+    return cuda_err(c, cudaStreamSynchronize(c->stream), "insert");
+  }
+  Staging st;
+  st.s = c->stream;
+  bool wt = c->wtype != CYTOM_UNWEIGHTED && w;
+  if (cudaMallocAsync(&st.p, count * (wt ? 12 : 8), c->stream) != cudaSuccess)
+    return set_err(c, CYTOM_ERR_OOM, "insert staging");
+  uint32_t* ds = (uint32_t*)st.p;
+  uint32_t* dt = ds + count;
+  uint32_t* dw = wt ? dt + count : nullptr;
+  cudaMemcpyAsync(ds, src, count * 4, cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(dt, tgt, count * 4, cudaMemcpyHostToDevice, c->stream);
+  if (dw) cudaMemcpyAsync(dw, w, count * 4, cudaMemcpyHostToDevice, c->stream);
+  int rc = insert_device(c, ds, dt, dw, count);
+  if (rc) return rc;
+  return cuda_err(c, cudaStreamSynchronize(c->stream), "insert");
+}
+
+int cytom_load_gridgraph(cytom_ctx* ctx, const char* path, uint64_t batch, uint64_t* count) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !path) return CYTOM_ERR_INVAL;
+  if (c->wtype != CYTOM_UNWEIGHTED)
+    return set_err(c, CYTOM_ERR_INVAL, "GridGraph files carry no weights; use an unweighted store");
+  FILE* f = fopen(path, "rb");
+  if (!f) return set_err(c, CYTOM_ERR_IO, std::string("cannot open ") + path);
+  if (batch == 0) batch = 1ULL << 20;
+  std::vector<char> buf(batch * 8);
+  uint64_t total = 0;
+  int rc = CYTOM_OK;
+  void* dev = nullptr;
+  if (cudaMalloc(&dev, batch * 16) != cudaSuccess) {
+    fclose(f);
+    return set_err(c, CYTOM_ERR_OOM, "gridgraph staging");
+  }
+  uint32_t* ds = (uint32_t*)((char*)dev + batch * 8);
+  uint32_t* dt = ds + batch;
+  while (true) {
+    size_t got = fread(buf.data(), 1, batch * 8, f);
+    uint64_t m = got / 8;
+    if (m == 0) break;
+    cudaMemcpyAsync(dev, buf.data(), m * 8, cudaMemcpyHostToDevice, c->stream);
+    rc = gridgraph_decode(c, dev, m, ds, dt);
+    if (rc) break;
+    rc = insert_device(c, ds, dt, nullptr, m);
+    if (rc) break;
+    rc = cuda_err(c, cudaStreamSynchronize(c->stream), "gridgraph insert");
+    if (rc) break;
+    total += m;
+    if (got < batch * 8) break;
+  }
+  fclose(f);
+  cudaFree(dev);
+  if (count) *count = total;
+  return rc;
+}
+
+int cytom_compact(cytom_ctx* ctx) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c) return CYTOM_ERR_INVAL;
+  int rc = compact(c);
+  if (rc) return rc;
+  rc = cuda_err(c, cudaStreamSynchronize(c->stream), "compact");
+  if (rc) return rc;
+  return prof_flush(c);
+}
+
+int cytom_count_edges(const cytom_ctx* ctx, uint64_t* compacted, uint64_t* pending) {
+  const Ctx* c = (const Ctx*)ctx;
+  if (!c) return CYTOM_ERR_INVAL;
+  if (compacted) *compacted = c->E;
+  if (pending) *pending = c->A;
+  return CYTOM_OK;
+}
+
+int cytom_get_tiles(cytom_ctx* ctx, uint64_t* tile_ptr, uint32_t* edges, uint32_t* weights,
+                    uint8_t* compact_flags) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c) return CYTOM_ERR_INVAL;
+  cudaError_t e = cudaSuccess;
+  if (tile_ptr)
+    e = cudaMemcpyAsync(tile_ptr, c->tile_ptr, (c->ntiles + 1) * 8, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess && edges && c->E)
+    e = cudaMemcpyAsync(edges, c->edges, c->E * 4, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess && weights && c->E && c->wtype)
+    e = cudaMemcpyAsync(weights, c->wts, c->E * 4, cudaMemcpyDeviceToHost, c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "get_tiles");
+  if (compact_flags) {
+    uint8_t* d = nullptr;
+    if (cudaMalloc(&d, c->ntiles) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "flags");
+    int rc = compute_compact_flags(c, d);
+    if (!rc) e = cudaMemcpyAsync(compact_flags, d, c->ntiles, cudaMemcpyDeviceToHost, c->stream);
+    cudaStreamSynchronize(c->stream);
+    cudaFree(d);
+    if (rc) return rc;
+    for (uint64_t t = 0; t < c->ntiles; ++t)
+      if (compact_flags[t] == 2) compact_flags[t] = 0;  // empty tile: storage flag stays false
+  }
+  return cuda_err(c, cudaStreamSynchronize(c->stream), "get_tiles");
+}
+
+int cytom_get_degrees(cytom_ctx* ctx, uint32_t* out_degree, uint32_t* in_degree) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c) return CYTOM_ERR_INVAL;
+  if (out_degree) cudaMemcpyAsync(out_degree, c->out_deg, c->n * 4, cudaMemcpyDeviceToHost, c->stream);
+  if (in_degree) cudaMemcpyAsync(in_degree, c->in_deg, c->n * 4, cudaMemcpyDeviceToHost, c->stream);
+  return cuda_err(c, cudaStreamSynchronize(c->stream), "get_degrees");
+}
+
+int cytom_job_create(cytom_ctx* ctx, int algo, const cytom_job_params* params, int* job_id) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !job_id || algo < CYTOM_ALGO_BFS || algo > CYTOM_ALGO_PAGERANK) return CYTOM_ERR_INVAL;
+  Job* j = new (std::nothrow) Job();
+  if (!j) return CYTOM_ERR_OOM;
+  j->algo = algo;
+  if (params) j->params = *params;
+  else cytom_job_params_default(&j->params);
+  if ((algo == CYTOM_ALGO_BFS || algo == CYTOM_ALGO_SSSP) && j->params.start_vertex >= c->n) {
+    delete j;
+    return set_err(c, CYTOM_ERR_RANGE, "start vertex >= vertex count");
+  }
+  if (algo == CYTOM_ALGO_SSSP && c->wtype != CYTOM_WEIGHT_U32) {
+    delete j;
+    return set_err(c, CYTOM_ERR_INVAL, "SSSP needs a store with uint32 weights");
+  }
+  int rc = job_alloc(c, j);
+  if (rc) {
+    job_free(c, j);
+    delete j;
+    return rc;
+  }
+  j->id = (int)c->jobs.size();
+  c->jobs.push_back(j);
+  *job_id = j->id;
+  return CYTOM_OK;
+}
+
+static Job* get_job(Ctx* c, int id) {
+  if (!c || id < 0 || id >= (int)c->jobs.size()) return nullptr;
+  return c->jobs[id];
+}
+
+int cytom_job_destroy(cytom_ctx* ctx, int job_id) {
+  Ctx* c = (Ctx*)ctx;
+  Job* j = get_job(c, job_id);
+  if (!j) return CYTOM_ERR_INVAL;
+  cudaStreamSynchronize(c->stream);
+  job_free(c, j);
+  delete j;
+  c->jobs[job_id] = nullptr;
+  return CYTOM_OK;
+}
+
+int cytom_job_reset(cytom_ctx* ctx, int job_id) {
+  Ctx* c = (Ctx*)ctx;
+  Job* j = get_job(c, job_id);
+  if (!j) return CYTOM_ERR_INVAL;
+  j->fresh = true;
+  return CYTOM_OK;
+}
+
+int cytom_run(cytom_ctx* ctx, int job_id, cytom_run_stats* stats) {
+  Ctx* c = (Ctx*)ctx;
+  Job* j = get_job(c, job_id);
+  if (!j) return CYTOM_ERR_INVAL;
+  return job_run(c, j, stats);
+}
+
+int cytom_run_many(cytom_ctx* ctx, const int* job_ids, int count, cytom_run_stats* stats) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || (count > 0 && !job_ids)) return CYTOM_ERR_INVAL;
+  for (int k = 0; k < count; ++k) {
+    int rc = cytom_run(ctx, job_ids[k], stats ? stats + k : nullptr);
+    if (rc) return rc;
+  }
+  return CYTOM_OK;
+}
+
+int cytom_get_result(cytom_ctx* ctx, int job_id, void* out, int where) {
+  Ctx* c = (Ctx*)ctx;
+  Job* j = get_job(c, job_id);
+  if (!j || !out) return CYTOM_ERR_INVAL;
+  if (!is_minprop(j->algo)) return pagerank_result(c, j, out, where);
+  cudaMemcpyKind k = where == CYTOM_PTR_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  cudaError_t e = cudaMemcpyAsync(out, j->h.next, c->n * 4, k, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  return cuda_err(c, e, "get_result");
+}
+
+int cytom_set_profiling(cytom_ctx* ctx, int on) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c) return CYTOM_ERR_INVAL;
+  prof_flush(c);
+  c->profiling = on != 0;
+  return CYTOM_OK;
+}
+
+int cytom_get_kernel_stats(cytom_ctx* ctx, cytom_kernel_stats* out) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !out) return CYTOM_ERR_INVAL;
+  int rc = prof_flush(c);
+  *out = c->kstats;
+  return rc;
+}
+
+int cytom_reset_kernel_stats(cytom_ctx* ctx) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c) return CYTOM_ERR_INVAL;
+  prof_flush(c);
+  for (int k = 0; k < CYTOM_KERNEL_CLASSES; ++k) {
+    c->kstats.launches[k] = 0;
+    c->kstats.total_ms[k] = 0;
+    c->kstats.algo_bytes[k] = 0;
+  }
+  return CYTOM_OK;
+}
+
+int cytom_launch_count(const cytom_ctx* ctx, uint64_t* launches) {
+  const Ctx* c = (const Ctx*)ctx;
+  if (!c || !launches) return CYTOM_ERR_INVAL;
+  *launches = c->launches;
+  return CYTOM_OK;
+}
+
+int cytom_sync(cytom_ctx* ctx) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c) return CYTOM_ERR_INVAL;
+  return cuda_err(c, cudaStreamSynchronize(c->stream), "sync");
+}
+
+}  // extern "C"

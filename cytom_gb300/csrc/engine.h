@@ -1,0 +1,176 @@
+// engine.h — internal declarations of the GB300 evolving-graph engine.
+//
+// Layout in HBM (one context = one graph):
+//   edges[E]      packed local edge (src_local << 16 | tgt_local), u32, sorted by
+//                 (tile_x, tile_y, src_local, tgt_local), duplicates removed: the
+//                 concatenation, in tile-id order (id = x*T + y), of every tile's CSR.
+//   wts[E]        per-edge weight (u32 or f32 bits), weighted stores only.
+//   tile_ptr[T*T+1]  u64 offsets of every tile's edges.
+//   chunk_tile[E/128+1]  tile id of the first edge of every 128-edge chunk.
+//   app_keys[A]   append region: u64 composite keys (x, y, src_l, tgt_l) of edges
+//                 inserted since the last compaction (+ app_w weights).
+//   out_deg / in_deg  u32 per vertex (multiplicity counts).
+// Kernels read pointers and sizes from a StoreDesc in device memory, so a captured
+// CUDA graph stays valid when the host swaps or grows buffers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/cytom_gpu.h"
+
+namespace cytom {
+
+constexpr int kChunk = 128;  // edges per warp chunk (32 lanes x uint4)
+constexpr uint32_t kInf = 0xFFFFFFFFu;
+
+struct StoreDesc {
+  const uint32_t* edges;
+  const uint32_t* wts;
+  const unsigned long long* tile_ptr;
+  const uint32_t* chunk_tile;
+  const uint32_t* out_deg;
+  const uint32_t* in_deg;
+  unsigned long long E;        // compacted edges (written on the device by compaction)
+  unsigned long long nchunks;  // ceil(E / kChunk)
+  unsigned long long n;        // vertices
+  unsigned long long T;        // tiles per dimension
+  unsigned long long ntiles;
+  uint32_t lvpt, lT;           // log2(vertices per tile), log2(T)
+  int wtype;
+  int pad;
+};
+
+// Loop state of one job run, in device memory. Kernels index the double-buffered
+// per-iteration counters by the parity of `iter`.
+struct LoopState {
+  unsigned int iter;       // rounds executed in this run
+  unsigned int max_iter;
+  unsigned int cont;       // 1 while the run continues
+  unsigned int err;
+  unsigned int active[2];  // vertices activated for the next round (by parity)
+  unsigned long long teps[2];  // edges of newly active tile rows (by parity)
+  unsigned long long count_edges;   // reference counting rule, summed
+  unsigned long long edges_scanned; // edges this engine read
+  unsigned long long active_total;
+  double resid[2];          // PageRank: FP64 residual by parity
+  double rank_sum[2];
+  double dangling[2];
+  double tol;
+  double resid_final;
+};
+
+struct JobDesc {
+  uint32_t* cur;      // current values (u32 for BFS/CC/SSSP)
+  uint32_t* next;
+  uint32_t* fa;       // frontier (active_current) bitmap, n/32 words
+  uint32_t* ch;       // changed bitmap
+  uint32_t* rows;     // 2 x T tile-row activity flags (by parity)
+  float* rank;        // PageRank family
+  float* rank_c;      // Kahan compensation of rank
+  float* delta;
+  float* dsum;
+  float* contrib;
+  double* rank64;     // FP64 plain PageRank
+  double* dsum64;
+  unsigned int* deg_distinct;
+  LoopState* ls;
+  int algo;
+  int kahan;
+  double alpha, delta_param;
+  unsigned long long start;
+};
+
+enum KernelClass { KC_RMAT = 0, KC_INSERT, KC_SORT, KC_MERGE, KC_GATHER, KC_APPLY, KC_PAGERANK, KC_OTHER };
+
+struct Job {
+  int id = -1;
+  int algo = 0;
+  cytom_job_params params{};
+  bool fresh = true;          // next run starts from scratch
+  JobDesc h{};                // host copy of the descriptor
+  JobDesc* d = nullptr;       // device copy
+  LoopState* ls = nullptr;    // device
+  // CUDA graph of the converge loop (while-conditional)
+  cudaGraphExec_t loop_exec = nullptr;
+  bool graph_failed = false;
+  bool last_run_graph = false;  // the last run went through the graph (launch accounting)
+};
+
+struct Ctx {
+  cytom_config cfg{};
+  std::string err;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int device = 0;
+  int num_sms = 1;
+  // geometry
+  uint64_t n = 0, vpt = 0, T = 0, ntiles = 0;
+  uint32_t lvpt = 0, lT = 0;
+  int wtype = 0;
+  // store (host view of pointers)
+  uint32_t *edges = nullptr, *wts = nullptr, *edges_alt = nullptr, *wts_alt = nullptr;
+  unsigned long long *tile_ptr = nullptr, *tile_ptr_alt = nullptr;
+  uint32_t* chunk_tile = nullptr;
+  uint64_t cap = 0, chunk_cap = 0;
+  uint64_t E = 0;  // exact after compaction
+  uint64_t *app_keys = nullptr, *app_keys_alt = nullptr;
+  uint32_t *app_w = nullptr, *app_w_alt = nullptr;
+  uint64_t A = 0, app_cap = 0;
+  uint32_t *out_deg = nullptr, *in_deg = nullptr;
+  StoreDesc hsd{};
+  StoreDesc* dsd = nullptr;
+  // scratch
+  void* scratch = nullptr;
+  size_t scratch_bytes = 0;
+  unsigned int* d_flag = nullptr;       // error / misc flags
+  unsigned long long* d_count = nullptr;
+  unsigned long long* h_pinned = nullptr;  // pinned host words for readbacks
+  // jobs
+  std::vector<Job*> jobs;
+  // instrumentation
+  bool profiling = false;
+  uint64_t launches = 0;
+  struct PendingEv { int cls; cudaEvent_t a, b; double bytes; };
+  std::vector<PendingEv> pending;
+  std::vector<cudaEvent_t> ev_pool;
+  cytom_kernel_stats kstats{};
+  cudaEvent_t run_a = nullptr, run_b = nullptr;
+};
+
+// ---- helpers (capi.cu) ----
+int set_err(Ctx* c, int code, const std::string& msg);
+int cuda_err(Ctx* c, cudaError_t e, const char* what);
+int prof_begin(Ctx* c, int cls);          // returns slot or -1
+void prof_end(Ctx* c, int slot, double bytes);
+int prof_flush(Ctx* c);
+int upload_store_desc(Ctx* c);
+
+// ---- ingest (ingest.cu) ----
+int rmat_generate(Ctx* c, const cytom_rmat_params* p, uint64_t first, uint64_t count,
+                  uint32_t* src, uint32_t* tgt, uint32_t* w);
+int gridgraph_decode(Ctx* c, const void* dbytes, uint64_t m, uint32_t* src, uint32_t* tgt);
+int insert_device(Ctx* c, const uint32_t* src, const uint32_t* tgt, const uint32_t* w,
+                  uint64_t count);
+int compact(Ctx* c);
+int compute_compact_flags(Ctx* c, uint8_t* dflags);
+int ensure_app_capacity(Ctx* c, uint64_t need);
+
+// device-wide utilities
+int exclusive_scan_u32(Ctx* c, const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* total_dev);
+int radix_sort_pairs(Ctx* c, uint64_t* keys, uint64_t* keys_alt, uint32_t* vals, uint32_t* vals_alt,
+                     uint64_t n, int bits, bool* result_in_alt);
+
+// ---- executors ----
+int job_alloc(Ctx* c, Job* j);
+void job_free(Ctx* c, Job* j);
+int job_init_state(Ctx* c, Job* j);
+int job_seed(Ctx* c, Job* j, const uint32_t* src, const uint32_t* tgt, const uint32_t* w,
+             uint64_t count);
+int job_run(Ctx* c, Job* j, cytom_run_stats* st);
+int job_result(Ctx* c, Job* j, void* out, int where);
+
+}  // namespace cytom

@@ -1,0 +1,826 @@
+// ingest.cu — edge sources, streaming insert and compaction of the tile store.
+//
+// Replaces, for one GPU:
+//   RMATContext::getEdge / rMatIterative   (src/include/edge-inserter/rmat-context.h:39-73)
+//   Jobs GridGraph reader                  (src/include/core/jobs.h:53-64, 111-118)
+//   MetaTileManager::insertEdge + TileManager::insertEdge
+//                                          (meta-tile-manager.h:112-125, tile-manager.h:136-163)
+//   TileManager::compactStorage / fillCSR  (tile-manager.h:192-291, 518-565)
+//
+// Compaction is a global merge: the append region is radix-sorted by the
+// composite key (x, y, src_local, tgt_local), deduplicated within itself and
+// against the compacted store (binary search in the tile's segment), and the
+// survivors are merged into a new buffer by output-position ranking. Every
+// compacted tile is then exactly the reference's sorted, deduplicated CSR.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "engine.h"
+
+namespace cytom {
+
+// --------------------------------------------------------------------------
+// Hash (Ligra 64-bit, src/include/util/util.h:188-196)
+// --------------------------------------------------------------------------
+__host__ __device__ __forceinline__ uint64_t hash64(uint64_t a) {
+  a = (a + 0x7ed55d166bef7a1dULL) + (a << 12);
+  a = (a ^ 0xc761c23c510fa2ddULL) ^ (a >> 9);
+  a = (a + 0x165667b183a9c0e1ULL) + (a << 59);
+  a = (a + 0xd3a2646cab3487e3ULL) ^ (a << 49);
+  a = (a + 0xfd7046c5ef9ab54cULL) + (a << 3);
+  a = (a ^ 0xb55a4f090dd4a67bULL) ^ (a >> 32);
+  return a;
+}
+
+// --------------------------------------------------------------------------
+// RMAT
+// --------------------------------------------------------------------------
+// util::hashDouble(i) = (double)hash(i) / (double)UINT64_MAX, and (double)UINT64_MAX
+// is exactly 2^64, so `hashDouble(i) < t` <=> `(double)hash(i) < t * 2^64`. Because
+// the u64 -> double rounding is monotone, that is `hash(i) < H` for the least H
+// whose double value reaches t * 2^64. The kernel compares integers against H;
+// the host derives H once from the double thresholds a, a+b, a+b+c.
+struct RmatThr {
+  unsigned long long h[3];
+  int all[3];  // 1 when every hash is below the threshold
+};
+
+static void rmat_threshold(double t, unsigned long long* h, int* all) {
+  const double two64 = 18446744073709551616.0;
+  double A = t * two64;
+  *all = 0;
+  if (!(A > 0.0)) {  // also NaN
+    *h = 0;
+    return;
+  }
+  if (A > (double)UINT64_MAX) {  // (double)UINT64_MAX == 2^64
+    *all = 1;
+    *h = 0;
+    return;
+  }
+  // A < 2^64 here or A == 2^64 (handled above); search H in a window around A.
+  unsigned long long guess = (A >= two64)                     ? UINT64_MAX
+                             : (A >= 9223372036854775808.0) ? (unsigned long long)(A)
+                                                            : (unsigned long long)std::ceil(A);
+  unsigned long long lo = guess > 8192 ? guess - 8192 : 0;
+  unsigned long long hi = guess < UINT64_MAX - 8192 ? guess + 8192 : UINT64_MAX;
+  // predicate p(h) = ((double)h >= A) is monotone; find the least h with p(h).
+  if ((double)hi < A) {  // all values in range below A: every hash < A
+    *all = 1;
+    *h = 0;
+    return;
+  }
+  while (lo < hi) {
+    unsigned long long mid = lo + (hi - lo) / 2;
+    if ((double)mid >= A) hi = mid;
+    else lo = mid + 1;
+  }
+  *h = lo;
+}
+
+__device__ __forceinline__ bool below(uint64_t v, const RmatThr& t, int k) {
+  return t.all[k] ? true : (v < t.h[k]);
+}
+
+__global__ void rmat_kernel(RmatThr thr, uint32_t scale, uint64_t hseed, uint64_t first,
+                            uint64_t count, uint32_t* __restrict__ src, uint32_t* __restrict__ tgt,
+                            uint32_t* __restrict__ w, uint64_t wseed_h, uint32_t wmin,
+                            uint64_t wspan) {
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += stride) {
+    uint64_t index = first + k;
+    uint64_t rs = hash64(2ULL * index * hseed);
+    uint64_t st = hash64((2ULL * index + 1ULL) * hseed);
+    // bit j (value 2^j) uses hash(rs + (scale-1-j)*st): the most significant bit
+    // uses hash(rs), as rMatIterative walks back from the finest level.
+    uint32_t es = 0, et = 0;
+    uint64_t r = rs;
+    for (int j = (int)scale - 1; j >= 0; --j) {
+      uint64_t h = hash64(r);
+      r += st;
+      uint32_t bit = 1u << j;
+      if (below(h, thr, 0)) {
+      } else if (below(h, thr, 1)) {
+        et |= bit;
+      } else if (below(h, thr, 2)) {
+        es |= bit;
+      } else {
+        es |= bit;
+        et |= bit;
+      }
+    }
+    src[k] = es;
+    tgt[k] = et;
+    if (w) {
+      uint64_t key = wseed_h ^ (((uint64_t)es << 32) | (uint64_t)et);
+      w[k] = wmin + (uint32_t)(hash64(key) % wspan);
+    }
+  }
+}
+
+static int grid_for(Ctx* c, uint64_t work, int threads, int per_sm = 8) {
+  uint64_t blocks = (work + threads - 1) / threads;
+  uint64_t cap = (uint64_t)c->num_sms * per_sm;
+  if (blocks > cap) blocks = cap;
+  if (blocks == 0) blocks = 1;
+  return (int)blocks;
+}
+
+int rmat_generate(Ctx* c, const cytom_rmat_params* p, uint64_t first, uint64_t count,
+                  uint32_t* src, uint32_t* tgt, uint32_t* w) {
+  if (count == 0) return CYTOM_OK;
+  RmatThr thr;
+  double a_ = p->a, ab_ = p->a + p->b, abc_ = p->a + p->b + p->c;
+  rmat_threshold(a_, &thr.h[0], &thr.all[0]);
+  rmat_threshold(ab_, &thr.h[1], &thr.all[1]);
+  rmat_threshold(abc_, &thr.h[2], &thr.all[2]);
+  uint64_t hseed = hash64(p->seed);
+  uint64_t wspan = (uint64_t)p->wmax - (uint64_t)p->wmin + 1ULL;
+  int slot = prof_begin(c, KC_RMAT);
+  rmat_kernel<<<grid_for(c, count, 256, 16), 256, 0, c->stream>>>(
+      thr, p->scale, hseed, first, count, src, tgt, (p->wmax > 0) ? w : nullptr,
+      hash64(p->weight_seed), p->wmin, wspan);
+  c->launches++;
+  prof_end(c, slot, (double)count * ((p->wmax > 0) ? 12.0 : 8.0));
+  return cuda_err(c, cudaGetLastError(), "rmat_kernel");
+}
+
+// --------------------------------------------------------------------------
+// GridGraph decode
+// --------------------------------------------------------------------------
+__global__ void gridgraph_decode_kernel(const int2* __restrict__ rec, uint64_t m, uint64_t n,
+                                        uint32_t* __restrict__ src, uint32_t* __restrict__ tgt,
+                                        unsigned int* bad) {
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  unsigned int nb = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) {
+    int2 r = rec[i];
+    bool ok = r.x >= 0 && r.y >= 0 && (uint64_t)r.x < n && (uint64_t)r.y < n;
+    nb += ok ? 0 : 1;
+    src[i] = ok ? (uint32_t)r.x : 0u;
+    tgt[i] = ok ? (uint32_t)r.y : 0u;
+  }
+  if (nb) atomicAdd(bad, nb);
+}
+
+int gridgraph_decode(Ctx* c, const void* dbytes, uint64_t m, uint32_t* src, uint32_t* tgt) {
+  if (m == 0) return CYTOM_OK;
+  cudaError_t e = cudaMemsetAsync(c->d_flag, 0, sizeof(unsigned int), c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "memset");
+  int slot = prof_begin(c, KC_INSERT);
+  gridgraph_decode_kernel<<<grid_for(c, m, 256), 256, 0, c->stream>>>(
+      (const int2*)dbytes, m, c->n, src, tgt, c->d_flag);
+  c->launches++;
+  prof_end(c, slot, (double)m * 16.0);
+  e = cudaMemcpyAsync(c->h_pinned, c->d_flag, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                      c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "memcpy");
+  e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "gridgraph_decode");
+  unsigned int bad = *(unsigned int*)c->h_pinned;
+  if (bad) return set_err(c, CYTOM_ERR_RANGE, "gridgraph record with a negative id or an id >= vertex count");
+  return CYTOM_OK;
+}
+
+// --------------------------------------------------------------------------
+// Insert
+// --------------------------------------------------------------------------
+__global__ void validate_kernel(const uint32_t* __restrict__ src, const uint32_t* __restrict__ tgt,
+                                uint64_t count, uint64_t n, unsigned int* bad) {
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  unsigned int nb = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride)
+    nb += (src[i] >= n || tgt[i] >= n) ? 1u : 0u;
+  if (nb) atomicAdd(bad, nb);
+}
+
+// Composite key: [x : lT][y : lT][src_local : lvpt][tgt_local : lvpt].
+__device__ __forceinline__ uint64_t make_key(uint32_t s, uint32_t t, uint32_t lvpt, uint32_t lT) {
+  uint64_t m = (1ULL << lvpt) - 1ULL;
+  uint64_t x = (uint64_t)s >> lvpt, y = (uint64_t)t >> lvpt;
+  uint64_t tile = (x << lT) | y;
+  return (tile << (2 * lvpt)) | (((uint64_t)s & m) << lvpt) | ((uint64_t)t & m);
+}
+
+// Appends one batch to the append region and counts degrees. Degree increments
+// are warp-aggregated: lanes holding the same vertex elect one leader that adds
+// the group's size (RMAT hubs repeat often within a warp).
+__global__ void append_kernel(const uint32_t* __restrict__ src, const uint32_t* __restrict__ tgt,
+                              const uint32_t* __restrict__ w, uint64_t count,
+                              uint64_t* __restrict__ keys, uint32_t* __restrict__ kw,
+                              uint32_t* __restrict__ out_deg, uint32_t* __restrict__ in_deg,
+                              uint32_t lvpt, uint32_t lT) {
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const unsigned lane = threadIdx.x & 31;
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < count; base += stride) {
+    uint64_t i = base + threadIdx.x;
+    bool valid = i < count;
+    unsigned vmask = __ballot_sync(0xFFFFFFFFu, valid);
+    if (!valid) continue;
+    uint32_t s = src[i], t = tgt[i];
+    keys[i] = make_key(s, t, lvpt, lT);
+    if (w) kw[i] = w[i];
+    unsigned ps = __match_any_sync(vmask, s);
+    if ((__ffs(ps) - 1) == (int)lane) atomicAdd(&out_deg[s], (uint32_t)__popc(ps));
+    unsigned pt = __match_any_sync(vmask, t);
+    if ((__ffs(pt) - 1) == (int)lane) atomicAdd(&in_deg[t], (uint32_t)__popc(pt));
+  }
+}
+
+int insert_device(Ctx* c, const uint32_t* src, const uint32_t* tgt, const uint32_t* w,
+                  uint64_t count) {
+  if (count == 0) return CYTOM_OK;
+  if (c->wtype != CYTOM_UNWEIGHTED && w == nullptr)
+    return set_err(c, CYTOM_ERR_INVAL, "weighted store needs a weight per edge");
+  cudaError_t e = cudaMemsetAsync(c->d_flag, 0, sizeof(unsigned int), c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "memset");
+  int slot = prof_begin(c, KC_INSERT);
+  validate_kernel<<<grid_for(c, count, 256), 256, 0, c->stream>>>(src, tgt, count, c->n, c->d_flag);
+  c->launches++;
+  prof_end(c, slot, (double)count * 8.0);
+  e = cudaMemcpyAsync(c->h_pinned, c->d_flag, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                      c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "memcpy");
+  e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "validate");
+  if (*(unsigned int*)c->h_pinned)
+    return set_err(c, CYTOM_ERR_RANGE, "edge endpoint >= vertex count; batch rejected");
+  int rc = ensure_app_capacity(c, c->A + count);
+  if (rc) return rc;
+  const uint32_t* wuse = (c->wtype != CYTOM_UNWEIGHTED) ? w : nullptr;
+  slot = prof_begin(c, KC_INSERT);
+  append_kernel<<<grid_for(c, count, 256), 256, 0, c->stream>>>(
+      src, tgt, wuse, count, c->app_keys + c->A, wuse ? c->app_w + c->A : nullptr, c->out_deg,
+      c->in_deg, c->lvpt, c->lT);
+  c->launches++;
+  prof_end(c, slot, (double)count * (wuse ? 28.0 : 24.0));
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_err(c, e, "append_kernel");
+  for (Job* j : c->jobs) {
+    if (!j || j->fresh) continue;
+    rc = job_seed(c, j, src, tgt, wuse, count);
+    if (rc) return rc;
+  }
+  c->A += count;
+  return CYTOM_OK;
+}
+
+// --------------------------------------------------------------------------
+// Device-wide exclusive scan (u32), three phases with recursion on block sums.
+// --------------------------------------------------------------------------
+constexpr int SCAN_T = 256, SCAN_IPT = 16, SCAN_TILE = SCAN_T * SCAN_IPT;
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
+  const unsigned lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xFFFFFFFFu, v, o);
+    if (lane >= (unsigned)o) v += y;
+  }
+  return v;
+}
+
+// Returns the exclusive block prefix of `v`; *total receives the block sum.
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* total) {
+  __shared__ uint32_t wsum[SCAN_T / 32];
+  __shared__ uint32_t tot_s;
+  const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t inc = warp_incl_scan(v);
+  if (lane == 31) wsum[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    uint32_t s = (lane < SCAN_T / 32) ? wsum[lane] : 0u;
+    uint32_t si = warp_incl_scan(s);
+    if (lane < SCAN_T / 32) wsum[lane] = si - s;
+    if (lane == SCAN_T / 32 - 1) tot_s = si;
+  }
+  __syncthreads();
+  uint32_t r = wsum[wid] + inc - v;
+  *total = tot_s;
+  __syncthreads();
+  return r;
+}
+
+__global__ void scan_reduce_kernel(const uint32_t* __restrict__ in, uint64_t n,
+                                   uint32_t* __restrict__ sums) {
+  uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_IPT;
+  uint32_t s = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_IPT; ++k) {
+    uint64_t i = base + k;
+    s += (i < n) ? in[i] : 0u;
+  }
+  uint32_t t;
+  block_excl_scan(s, &t);
+  if (threadIdx.x == 0) sums[blockIdx.x] = t;
+}
+
+__global__ void scan_down_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
+                                 uint64_t n, const uint32_t* __restrict__ offs,
+                                 uint32_t* total_out) {
+  uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_IPT;
+  uint32_t v[SCAN_IPT];
+  uint32_t s = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_IPT; ++k) {
+    uint64_t i = base + k;
+    v[k] = (i < n) ? in[i] : 0u;
+    s += v[k];
+  }
+  uint32_t t;
+  const uint32_t boff = offs ? offs[blockIdx.x] : 0u;
+  uint32_t p = block_excl_scan(s, &t) + boff;
+#pragma unroll
+  for (int k = 0; k < SCAN_IPT; ++k) {
+    uint64_t i = base + k;
+    if (i < n) out[i] = p;
+    p += v[k];
+  }
+  if (total_out && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *total_out = boff + t;
+}
+
+int exclusive_scan_u32(Ctx* c, const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* total_dev) {
+  if (n == 0) return CYTOM_OK;
+  uint64_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+  cudaError_t e;
+  if (nb == 1) {
+    scan_down_kernel<<<1, SCAN_T, 0, c->stream>>>(in, out, n, nullptr, total_dev);
+    c->launches++;
+    return cuda_err(c, cudaGetLastError(), "scan_down");
+  }
+  uint32_t *sums = nullptr, *soffs = nullptr;
+  e = cudaMallocAsync((void**)&sums, nb * 4 * 2, c->stream);
+  if (e != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "scan temp");
+  soffs = sums + nb;
+  scan_reduce_kernel<<<(unsigned)nb, SCAN_T, 0, c->stream>>>(in, n, sums);
+  c->launches++;
+  int rc = exclusive_scan_u32(c, sums, soffs, nb, nullptr);
+  if (rc) return rc;
+  scan_down_kernel<<<(unsigned)nb, SCAN_T, 0, c->stream>>>(in, out, n, soffs, total_dev);
+  c->launches++;
+  cudaFreeAsync(sums, c->stream);
+  return cuda_err(c, cudaGetLastError(), "scan");
+}
+
+// --------------------------------------------------------------------------
+// LSD radix sort of (u64 key, u32 value) pairs, 8-bit digits, stable.
+// Upsweep: per-block digit histogram (digit-major). Scan. Downsweep: warps rank
+// items with __match_any_sync in input order and scatter.
+// --------------------------------------------------------------------------
+constexpr int RS_T = 256, RS_IPT = 16, RS_TILE = RS_T * RS_IPT, RS_WARPS = RS_T / 32;
+
+__global__ void radix_upsweep_kernel(const uint64_t* __restrict__ keys, uint64_t n, int shift,
+                                     uint32_t* __restrict__ hist, uint32_t nb) {
+  __shared__ uint32_t cnt[256];
+  cnt[threadIdx.x] = 0;
+  __syncthreads();
+  uint64_t base = (uint64_t)blockIdx.x * RS_TILE;
+#pragma unroll 4
+  for (int k = 0; k < RS_IPT; ++k) {
+    uint64_t i = base + (uint64_t)k * RS_T + threadIdx.x;
+    if (i < n) atomicAdd(&cnt[(keys[i] >> shift) & 0xFF], 1u);
+  }
+  __syncthreads();
+  hist[(uint64_t)threadIdx.x * nb + blockIdx.x] = cnt[threadIdx.x];
+}
+
+__global__ void radix_downsweep_kernel(const uint64_t* __restrict__ keys,
+                                       const uint32_t* __restrict__ vals, uint64_t n, int shift,
+                                       const uint32_t* __restrict__ offs, uint32_t nb,
+                                       uint64_t* __restrict__ keys_out,
+                                       uint32_t* __restrict__ vals_out) {
+  __shared__ uint32_t wcnt[RS_WARPS][256];
+  __shared__ uint32_t base_d[256];
+  const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int d = threadIdx.x; d < RS_WARPS * 256; d += RS_T) (&wcnt[0][0])[d] = 0;
+  base_d[threadIdx.x] = offs[(uint64_t)threadIdx.x * nb + blockIdx.x];
+  __syncthreads();
+  const uint64_t wbase = (uint64_t)blockIdx.x * RS_TILE + (uint64_t)wid * (32 * RS_IPT);
+  uint64_t k_reg[RS_IPT];
+  uint32_t d_reg[RS_IPT];
+#pragma unroll
+  for (int k = 0; k < RS_IPT; ++k) {
+    uint64_t i = wbase + (uint64_t)k * 32 + lane;
+    k_reg[k] = (i < n) ? keys[i] : 0ULL;
+    d_reg[k] = (i < n) ? (uint32_t)((k_reg[k] >> shift) & 0xFF) : 256u;
+  }
+  // phase 1: per-warp digit counts
+#pragma unroll
+  for (int k = 0; k < RS_IPT; ++k) {
+    unsigned peers = __match_any_sync(0xFFFFFFFFu, d_reg[k]);
+    if (d_reg[k] < 256u && (__ffs(peers) - 1) == (int)lane) wcnt[wid][d_reg[k]] += __popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+  // phase 2: exclusive prefix across warps per digit
+  {
+    uint32_t run = 0;
+    const int d = threadIdx.x;
+#pragma unroll
+    for (int w = 0; w < RS_WARPS; ++w) {
+      uint32_t t = wcnt[w][d];
+      wcnt[w][d] = run;
+      run += t;
+    }
+  }
+  __syncthreads();
+  // phase 3: rank and scatter in input order
+  const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+  for (int k = 0; k < RS_IPT; ++k) {
+    uint32_t d = d_reg[k];
+    unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
+    uint32_t before = (d < 256u) ? wcnt[wid][d] : 0u;
+    __syncwarp();
+    if (d < 256u) {
+      uint32_t pos = base_d[d] + before + __popc(peers & lt);
+      keys_out[pos] = k_reg[k];
+      if (vals) vals_out[pos] = vals[wbase + (uint64_t)k * 32 + lane];
+      if ((__ffs(peers) - 1) == (int)lane) wcnt[wid][d] = before + __popc(peers);
+    }
+    __syncwarp();
+  }
+}
+
+int radix_sort_pairs(Ctx* c, uint64_t* keys, uint64_t* keys_alt, uint32_t* vals, uint32_t* vals_alt,
+                     uint64_t n, int bits, bool* result_in_alt) {
+  *result_in_alt = false;
+  if (n <= 1 || bits <= 0) return CYTOM_OK;
+  uint64_t nb = (n + RS_TILE - 1) / RS_TILE;
+  uint32_t* hist = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&hist, nb * 256 * 4 * 2, c->stream);
+  if (e != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "radix histogram");
+  uint32_t* offs = hist + nb * 256;
+  uint64_t *kin = keys, *kout = keys_alt;
+  uint32_t *vin = vals, *vout = vals_alt;
+  bool alt = false;
+  for (int shift = 0; shift < bits; shift += 8) {
+    int slot = prof_begin(c, KC_SORT);
+    radix_upsweep_kernel<<<(unsigned)nb, RS_T, 0, c->stream>>>(kin, n, shift, hist, (uint32_t)nb);
+    c->launches++;
+    int rc = exclusive_scan_u32(c, hist, offs, nb * 256, nullptr);
+    if (rc) return rc;
+    radix_downsweep_kernel<<<(unsigned)nb, RS_T, 0, c->stream>>>(kin, vin, n, shift, offs,
+                                                                 (uint32_t)nb, kout, vout);
+    c->launches++;
+    prof_end(c, slot, (double)n * (vals ? 12.0 : 8.0) * 3.0);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_err(c, e, "radix");
+    std::swap(kin, kout);
+    std::swap(vin, vout);
+    alt = !alt;
+  }
+  cudaFreeAsync(hist, c->stream);
+  *result_in_alt = alt;
+  return CYTOM_OK;
+}
+
+// --------------------------------------------------------------------------
+// Compaction
+// --------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t lower_bound_u32(const uint32_t* a, uint64_t lo, uint64_t hi,
+                                                    uint32_t v) {
+  while (lo < hi) {
+    uint64_t mid = lo + ((hi - lo) >> 1);
+    if (a[mid] < v) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// For each sorted appended key: first of its run? present in the compacted tile?
+// keep[i] = 1 for a new distinct edge; lb[i] = its insertion index in the old store;
+// wsel[i] = the least weight of its run. A weight that undercuts the stored copy of
+// an existing edge lowers that copy in place.
+__global__ void dedupe_lookup_kernel(const uint64_t* __restrict__ K, const uint32_t* __restrict__ W,
+                                     uint64_t A, const uint32_t* __restrict__ edges,
+                                     uint32_t* __restrict__ wts,
+                                     const unsigned long long* __restrict__ tile_ptr,
+                                     uint32_t lvpt, uint32_t* __restrict__ keep,
+                                     unsigned long long* __restrict__ lb,
+                                     uint32_t* __restrict__ wsel) {
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t m = (1ULL << lvpt) - 1ULL;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A; i += stride) {
+    uint64_t key = K[i];
+    if (i > 0 && K[i - 1] == key) {
+      keep[i] = 0;
+      continue;
+    }
+    uint32_t wmin = 0;
+    if (W) {
+      wmin = W[i];
+      for (uint64_t j = i + 1; j < A && K[j] == key; ++j) wmin = min(wmin, W[j]);
+    }
+    uint64_t tile = key >> (2 * lvpt);
+    uint32_t local = (uint32_t)((((key >> lvpt) & m) << 16) | (key & m));
+    uint64_t lo = tile_ptr[tile], hi = tile_ptr[tile + 1];
+    // fillCSR starts its duplicate filter at (UINT16_MAX, UINT16_MAX)
+    // (tile-manager.h:519-541): when that edge is the first in its tile's sorted
+    // list -- an otherwise empty tile -- the reference drops it.
+    if (local == 0xFFFFFFFFu && lo == hi && (i == 0 || (K[i - 1] >> (2 * lvpt)) != tile)) {
+      keep[i] = 0;
+      continue;
+    }
+    uint64_t pos = lower_bound_u32(edges, lo, hi, local);
+    bool found = pos < hi && edges[pos] == local;
+    if (found) {
+      if (W) atomicMin(&wts[pos], wmin);
+      keep[i] = 0;
+    } else {
+      keep[i] = 1;
+      lb[i] = pos;
+      wsel[i] = wmin;
+    }
+  }
+}
+
+__global__ void pack_kept_kernel(const uint64_t* __restrict__ K, uint64_t A,
+                                 const uint32_t* __restrict__ keep, const uint32_t* __restrict__ P,
+                                 const unsigned long long* __restrict__ lb,
+                                 const uint32_t* __restrict__ wsel, uint32_t lvpt,
+                                 unsigned long long* __restrict__ q, uint32_t* __restrict__ nloc,
+                                 uint32_t* __restrict__ nw, uint32_t* __restrict__ ntile) {
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t m = (1ULL << lvpt) - 1ULL;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A; i += stride) {
+    if (!keep[i]) continue;
+    uint64_t key = K[i];
+    uint32_t p = P[i];
+    q[p] = lb[i] + p;
+    nloc[p] = (uint32_t)((((key >> lvpt) & m) << 16) | (key & m));
+    if (nw) nw[p] = wsel[i];
+    ntile[p] = (uint32_t)(key >> (2 * lvpt));
+  }
+}
+
+__device__ __forceinline__ uint64_t lower_bound_tile(const uint32_t* a, uint64_t n, uint32_t v) {
+  uint64_t lo = 0, hi = n;
+  while (lo < hi) {
+    uint64_t mid = lo + ((hi - lo) >> 1);
+    if (a[mid] < v) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void new_tile_ptr_kernel(const unsigned long long* __restrict__ tile_ptr,
+                                    uint64_t ntiles, const uint32_t* __restrict__ ntile,
+                                    const uint32_t* __restrict__ Kdev,
+                                    unsigned long long* __restrict__ out) {
+  uint64_t K = *Kdev;
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t <= ntiles; t += stride) {
+    uint64_t add = (t == ntiles) ? K : lower_bound_tile(ntile, K, (uint32_t)t);
+    out[t] = tile_ptr[t] + add;
+  }
+}
+
+// Output position o of the merged store holds kept batch element b when q[b] == o,
+// otherwise old store element o - (number of q below o). One warp produces 32
+// consecutive outputs per step: lane j loads candidate q[b + j], the warp ORs the
+// window bits of the candidates that land in the window, and every lane derives its
+// source from the mask. Stores are coalesced 128-byte warp writes.
+constexpr int MERGE_STEPS = 32;  // 1024 outputs per warp
+__global__ void merge_gather_kernel(const uint32_t* __restrict__ edges, const uint32_t* __restrict__ wts,
+                                    uint64_t E, const unsigned long long* __restrict__ q,
+                                    const uint32_t* __restrict__ nloc, const uint32_t* __restrict__ nw,
+                                    const uint32_t* __restrict__ Kdev, uint32_t* __restrict__ oe,
+                                    uint32_t* __restrict__ ow) {
+  const uint64_t K = *Kdev;
+  const uint64_t total = E + K;
+  const unsigned lane = threadIdx.x & 31;
+  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint64_t span = 32ULL * MERGE_STEPS;
+  const unsigned lt = (1u << lane) - 1u;
+  for (uint64_t wbase = warp * span; wbase < total; wbase += nwarps * span) {
+    uint64_t b = 0;
+    if (lane == 0) {
+      uint64_t lo = 0, hi = K;
+      while (lo < hi) {
+        uint64_t mid = lo + ((hi - lo) >> 1);
+        if (q[mid] < wbase) lo = mid + 1;
+        else hi = mid;
+      }
+      b = lo;
+    }
+    b = __shfl_sync(0xFFFFFFFFu, b, 0);
+    for (int st = 0; st < MERGE_STEPS; ++st) {
+      const uint64_t o_start = wbase + (uint64_t)st * 32;
+      if (o_start >= total) break;
+      uint64_t cand = (b + lane < K) ? q[b + lane] : ~0ULL;
+      unsigned bitv = (cand >= o_start && cand < o_start + 32) ? (1u << (unsigned)(cand - o_start)) : 0u;
+      unsigned mask = __reduce_or_sync(0xFFFFFFFFu, bitv);
+      const uint64_t o = o_start + lane;
+      if (o < total) {
+        unsigned before = __popc(mask & lt);
+        uint32_t ev, wv = 0;
+        if ((mask >> lane) & 1u) {
+          ev = nloc[b + before];
+          if (ow) wv = nw[b + before];
+        } else {
+          uint64_t s = o - (b + before);
+          ev = edges[s];
+          if (ow) wv = wts[s];
+        }
+        oe[o] = ev;
+        if (ow) ow[o] = wv;
+      }
+      b += __popc(mask);
+    }
+  }
+}
+
+__global__ void chunk_tile_kernel(const unsigned long long* __restrict__ tile_ptr, uint64_t ntiles,
+                                  uint64_t nchunks, uint32_t* __restrict__ chunk_tile) {
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t cix = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; cix <= nchunks; cix += stride) {
+    if (cix == nchunks) {
+      chunk_tile[cix] = (uint32_t)(ntiles - 1);
+      continue;
+    }
+    unsigned long long e = (unsigned long long)cix * kChunk;
+    // last tile t with tile_ptr[t] <= e
+    uint64_t lo = 0, hi = ntiles;  // search in tile_ptr[0..ntiles]
+    while (lo < hi) {
+      uint64_t mid = lo + ((hi - lo + 1) >> 1);
+      if (tile_ptr[mid] <= e) lo = mid;
+      else hi = mid - 1;
+    }
+    if (lo >= ntiles) lo = ntiles - 1;
+    chunk_tile[cix] = (uint32_t)lo;
+  }
+}
+
+static int grow_store(Ctx* c, uint64_t need) {
+  if (need <= c->cap) return CYTOM_OK;
+  uint64_t ncap = std::max<uint64_t>(need + need / 2, 1 << 16);
+  ncap = (ncap + kChunk - 1) / kChunk * kChunk + kChunk;
+  uint32_t *ne = nullptr, *nea = nullptr, *nw = nullptr, *nwa = nullptr;
+  cudaError_t e = cudaMalloc(&ne, ncap * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&nea, ncap * 4);
+  if (e == cudaSuccess && c->wtype) e = cudaMalloc(&nw, ncap * 4);
+  if (e == cudaSuccess && c->wtype) e = cudaMalloc(&nwa, ncap * 4);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(ne);
+    cudaFree(nea);
+    cudaFree(nw);
+    cudaFree(nwa);
+    return set_err(c, CYTOM_ERR_OOM, "tile store growth");
+  }
+  if (c->E) {
+    cudaMemcpyAsync(ne, c->edges, c->E * 4, cudaMemcpyDeviceToDevice, c->stream);
+    if (c->wtype) cudaMemcpyAsync(nw, c->wts, c->E * 4, cudaMemcpyDeviceToDevice, c->stream);
+  }
+  cudaStreamSynchronize(c->stream);
+  cudaFree(c->edges);
+  cudaFree(c->edges_alt);
+  cudaFree(c->wts);
+  cudaFree(c->wts_alt);
+  c->edges = ne;
+  c->edges_alt = nea;
+  c->wts = nw;
+  c->wts_alt = nwa;
+  c->cap = ncap;
+  uint64_t nch = ncap / kChunk + 2;
+  if (nch > c->chunk_cap) {
+    uint32_t* ct = nullptr;
+    if (cudaMalloc(&ct, nch * 4) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "chunk table");
+    cudaFree(c->chunk_tile);
+    c->chunk_tile = ct;
+    c->chunk_cap = nch;
+  }
+  return CYTOM_OK;
+}
+
+int ensure_app_capacity(Ctx* c, uint64_t need) {
+  if (need <= c->app_cap) return CYTOM_OK;
+  uint64_t ncap = std::max<uint64_t>(need + need / 2, 1 << 16);
+  uint64_t *k = nullptr, *ka = nullptr;
+  uint32_t *w = nullptr, *wa = nullptr;
+  cudaError_t e = cudaMalloc(&k, ncap * 8);
+  if (e == cudaSuccess) e = cudaMalloc(&ka, ncap * 8);
+  if (e == cudaSuccess && c->wtype) e = cudaMalloc(&w, ncap * 4);
+  if (e == cudaSuccess && c->wtype) e = cudaMalloc(&wa, ncap * 4);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(k);
+    cudaFree(ka);
+    cudaFree(w);
+    cudaFree(wa);
+    return set_err(c, CYTOM_ERR_OOM, "append region growth");
+  }
+  if (c->A) {
+    cudaMemcpyAsync(k, c->app_keys, c->A * 8, cudaMemcpyDeviceToDevice, c->stream);
+    if (c->wtype) cudaMemcpyAsync(w, c->app_w, c->A * 4, cudaMemcpyDeviceToDevice, c->stream);
+  }
+  cudaStreamSynchronize(c->stream);
+  cudaFree(c->app_keys);
+  cudaFree(c->app_keys_alt);
+  cudaFree(c->app_w);
+  cudaFree(c->app_w_alt);
+  c->app_keys = k;
+  c->app_keys_alt = ka;
+  c->app_w = w;
+  c->app_w_alt = wa;
+  c->app_cap = ncap;
+  return CYTOM_OK;
+}
+
+int compact(Ctx* c) {
+  if (c->A == 0) return CYTOM_OK;
+  const uint64_t A = c->A;
+  const bool wt = c->wtype != CYTOM_UNWEIGHTED;
+  bool in_alt = false;
+  int rc = radix_sort_pairs(c, c->app_keys, c->app_keys_alt, wt ? c->app_w : nullptr,
+                            wt ? c->app_w_alt : nullptr, A, (int)(2 * (c->lvpt + c->lT)), &in_alt);
+  if (rc) return rc;
+  const uint64_t* K = in_alt ? c->app_keys_alt : c->app_keys;
+  const uint32_t* W = wt ? (in_alt ? c->app_w_alt : c->app_w) : nullptr;
+  rc = grow_store(c, c->E + A);
+  if (rc) return rc;
+  // temporaries
+  size_t bytes = A * (4 + 4 + 8 + 4 + 8 + 4 + 4 + 4) + 64;
+  char* tmp = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&tmp, bytes, c->stream);
+  if (e != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "compaction temporaries");
+  unsigned long long* lb = (unsigned long long*)tmp;
+  unsigned long long* q = lb + A;
+  uint32_t* keep = (uint32_t*)(q + A);
+  uint32_t* P = keep + A;
+  uint32_t* wsel = P + A;
+  uint32_t* nloc = wsel + A;
+  uint32_t* nw = nloc + A;
+  uint32_t* ntile = nw + A;
+  uint32_t* Kdev = ntile + A;
+  int slot = prof_begin(c, KC_MERGE);
+  dedupe_lookup_kernel<<<grid_for(c, A, 256), 256, 0, c->stream>>>(
+      K, W, A, c->edges, c->wts, c->tile_ptr, c->lvpt, keep, lb, wsel);
+  c->launches++;
+  rc = exclusive_scan_u32(c, keep, P, A, Kdev);
+  if (rc) return rc;
+  pack_kept_kernel<<<grid_for(c, A, 256), 256, 0, c->stream>>>(K, A, keep, P, lb, wsel, c->lvpt, q,
+                                                               nloc, wt ? nw : nullptr, ntile);
+  c->launches++;
+  new_tile_ptr_kernel<<<grid_for(c, c->ntiles + 1, 256), 256, 0, c->stream>>>(
+      c->tile_ptr, c->ntiles, ntile, Kdev, c->tile_ptr_alt);
+  c->launches++;
+  merge_gather_kernel<<<grid_for(c, (c->E + A + 31) / 32, 256, 16), 256, 0, c->stream>>>(
+      c->edges, c->wts, c->E, q, nloc, nw, Kdev, c->edges_alt, wt ? c->wts_alt : nullptr);
+  c->launches++;
+  e = cudaMemcpyAsync(c->h_pinned, Kdev, 4, cudaMemcpyDeviceToHost, c->stream);
+  cudaFreeAsync(tmp, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "compaction");
+  uint64_t Kn = *(uint32_t*)c->h_pinned;
+  prof_end(c, slot, (double)A * (wt ? 44.0 : 36.0) + (double)(c->E + Kn) * (wt ? 16.0 : 8.0));
+  std::swap(c->edges, c->edges_alt);
+  std::swap(c->wts, c->wts_alt);
+  std::swap(c->tile_ptr, c->tile_ptr_alt);
+  c->E += Kn;
+  c->A = 0;
+  uint64_t nch = (c->E + kChunk - 1) / kChunk;
+  chunk_tile_kernel<<<grid_for(c, nch + 1, 256), 256, 0, c->stream>>>(c->tile_ptr, c->ntiles, nch,
+                                                                     c->chunk_tile);
+  c->launches++;
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_err(c, e, "chunk_tile");
+  return upload_store_desc(c);
+}
+
+// Compact-vs-sparse flag per tile: distinct sources >= vpt / 2 (tile-manager.h:261-263).
+__global__ void count_sources_kernel(const uint32_t* __restrict__ edges,
+                                     const unsigned long long* __restrict__ tile_ptr,
+                                     uint64_t ntiles, uint64_t vpt, uint8_t* __restrict__ flags) {
+  // one warp per tile
+  const unsigned lane = threadIdx.x & 31;
+  uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t t = warp; t < ntiles; t += nwarps) {
+    uint64_t lo = tile_ptr[t], hi = tile_ptr[t + 1];
+    uint32_t cnt = 0;
+    for (uint64_t i = lo + lane; i < hi; i += 32) {
+      uint32_t s = edges[i] >> 16;
+      uint32_t prev = (i == lo) ? 0xFFFFFFFFu : (edges[i - 1] >> 16);
+      cnt += (s != prev) ? 1u : 0u;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xFFFFFFFFu, cnt, o);
+    if (lane == 0) flags[t] = (hi > lo) ? (uint8_t)(cnt >= vpt / 2 ? 1 : 0) : 2;  // 2 = empty
+  }
+}
+
+int compute_compact_flags(Ctx* c, uint8_t* dflags) {
+  count_sources_kernel<<<grid_for(c, c->ntiles * 32, 256), 256, 0, c->stream>>>(
+      c->edges, c->tile_ptr, c->ntiles, c->vpt, dflags);
+  c->launches++;
+  return cuda_err(c, cudaGetLastError(), "count_sources");
+}
+
+}  // namespace cytom

@@ -1,0 +1,221 @@
+/*
+ * cytom_gpu.h — C ABI of the GB300-native evolving-graph engine.
+ *
+ * One context (cytom_ctx) owns one graph on one GPU: a device-resident tile
+ * store (edges grouped into vpt x vpt tiles, tile-major, sorted, deduplicated),
+ * the vertex degrees, and any number of algorithm jobs (vertex programs) that
+ * keep their vertex state on the device between runs. Plain pointers and sizes
+ * only; no C++ or torch types cross this boundary.
+ *
+ * Every call returns CYTOM_OK (0) or a negative CYTOM_ERR_* code and never
+ * aborts; cytom_last_error() gives the message of the last failure. A context is
+ * single-threaded: callers serialise calls on one context. All device work of a
+ * context runs on one CUDA stream (the caller's, if given). Input pointers are
+ * borrowed for the duration of the call; output buffers belong to the caller.
+ *
+ * Citations name the reference interface each entry point replaces
+ * (oslab-swrc/cytom, path inside that project).
+ */
+#ifndef CYTOM_GPU_H
+#define CYTOM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. The reference aborts through util::die (src/lib/util/util.cc:21-32)
+ * and parseOption returns -EINVAL (src/include/main/execute.h:207). */
+#define CYTOM_OK 0
+#define CYTOM_ERR_INVAL (-1)         /* bad argument or configuration */
+#define CYTOM_ERR_OOM (-2)           /* device or host allocation failed */
+#define CYTOM_ERR_RANGE (-3)         /* vertex id >= vertex count, negative id */
+#define CYTOM_ERR_TIMEOUT (-4)       /* a bounded device wait gave up */
+#define CYTOM_ERR_CUDA (-5)          /* CUDA runtime error */
+#define CYTOM_ERR_UNIMPLEMENTED (-6) /* not available in this build */
+#define CYTOM_ERR_IO (-7)            /* file could not be read */
+
+/* Pointer location flags for buffers passed in or out. */
+#define CYTOM_PTR_HOST 0
+#define CYTOM_PTR_DEVICE 1
+
+/* Weight storage of a tile store. */
+#define CYTOM_UNWEIGHTED 0
+#define CYTOM_WEIGHT_U32 1 /* integer weights (SSSP) */
+#define CYTOM_WEIGHT_F32 2 /* float weights, stored as their bit pattern (weighted PageRank) */
+
+/* Vertex programs: examples/bfs.cc, cc.cc, sssp.cc, pagerank-delta.cc in the
+ * reference (selected by template argument in execute<V, A, w>,
+ * src/include/main/execute.h:534). PAGERANK is the normalised PageRank with
+ * dangling-mass redistribution (FP32 + Kahan, FP64 residual). */
+#define CYTOM_ALGO_BFS 0
+#define CYTOM_ALGO_CC 1
+#define CYTOM_ALGO_SSSP 2
+#define CYTOM_ALGO_PR_DELTA 3
+#define CYTOM_ALGO_PAGERANK 4
+
+/* Context configuration: the subset of ConfigContext (src/include/util/config.h:529-567)
+ * and its command-line flags (src/include/core/jobs.h:176-216) that the hot path uses. */
+typedef struct cytom_config {
+  uint64_t max_vertices;         /* --max-vertices; rounded up to a power of two
+                                    (Config::normalizeConfig, src/lib/util/config.cc:10-13) */
+  uint64_t vertices_per_tile;    /* --vertices-per-tile; power of two, <= 65536, <= vertices */
+  int32_t weight_type;           /* CYTOM_UNWEIGHTED / CYTOM_WEIGHT_U32 / CYTOM_WEIGHT_F32 */
+  int32_t enable_adaptive_scheduling; /* --enable-adaptive-scheduling (skip inactive tile rows) */
+  uint64_t edge_capacity_hint;   /* initial edge capacity; the store grows on demand */
+  void* stream;                  /* cudaStream_t to run on; NULL = the context's own stream */
+} cytom_config;
+
+/* Fills *cfg with the reference defaults (src/scripts/config.py:45-109). */
+void cytom_config_default(cytom_config* cfg);
+
+typedef struct cytom_ctx cytom_ctx;
+
+/* Replaces the per-job construction in execute<V,A,w> (src/include/main/execute.h:534-620):
+ * Config::normalizeConfig, VertexStore::init (vertex-store.h:25-53) and TileStore::init
+ * (tile-store.h:27-74). */
+int cytom_create(const cytom_config* cfg, cytom_ctx** out);
+/* Replaces VertexStore::destroy / TileStore::destroy (vertex-store.h:55-62, tile-store.h:228-241). */
+int cytom_destroy(cytom_ctx* ctx);
+const char* cytom_last_error(const cytom_ctx* ctx);
+/* Vertex count (power of two) and tiles per dimension after normalisation. */
+int cytom_geometry(const cytom_ctx* ctx, uint64_t* vertices, uint64_t* vertices_per_tile,
+                   uint64_t* tiles_per_dim);
+
+/* ---- Edge sources ------------------------------------------------------ */
+
+/* RMAT parameters. The reference's RMATContext (src/include/edge-inserter/rmat-context.h:12-82)
+ * never stores a, b, c or the vertex count (rmat-context.h:14-15); these are the
+ * values it was meant to hold. Defaults: a,b,c = (double)0.57f, 0.19f, 0.19f
+ * (RMAT_A/B/C, src/include/util/datatypes.h:17-19). */
+typedef struct cytom_rmat_params {
+  uint32_t scale;   /* vertices = 2^scale */
+  double a, b, c;   /* quadrant probabilities */
+  uint64_t seed;    /* RMATContext seed (hash_ = hash(seed)) */
+  uint64_t weight_seed; /* weights: wmin + hash(hash(weight_seed) ^ (src<<32|tgt)) % (wmax-wmin+1) */
+  uint32_t wmin, wmax;  /* wmax = 0: no weights generated */
+} cytom_rmat_params;
+void cytom_rmat_default(cytom_rmat_params* p);
+
+/* RMATContext::getEdge(first .. first+count-1) (rmat-context.h:67-73) into src/tgt
+ * (and w when p->wmax > 0), on the device (CYTOM_PTR_DEVICE) or copied to host
+ * buffers (CYTOM_PTR_HOST). */
+int cytom_rmat_generate(cytom_ctx* ctx, const cytom_rmat_params* p, uint64_t first,
+                        uint64_t count, uint32_t* src, uint32_t* tgt, uint32_t* w, int where);
+
+/* GridGraph binary reader (Jobs::Jobs + edge_reader_thread, src/include/core/jobs.h:53-64,
+ * 111-118): `bytes` holds little-endian {int32 src; int32 tgt} records (no header,
+ * src/scripts/convert_graph.py:15-16), size/8 edges. Decodes on the device into
+ * src/tgt (device or host per `where`); a negative id or one >= the vertex count is
+ * CYTOM_ERR_RANGE (the reference would index out of bounds). *count receives size/8. */
+int cytom_gridgraph_decode(cytom_ctx* ctx, const void* bytes, uint64_t size, uint32_t* src,
+                           uint32_t* tgt, int where, uint64_t* count);
+/* Reads a GridGraph file from disk and inserts its edges in batches of `batch`. */
+int cytom_load_gridgraph(cytom_ctx* ctx, const char* path, uint64_t batch, uint64_t* count);
+
+/* ---- Tile store -------------------------------------------------------- */
+
+/* Streaming insert of one batch (IEdgeProvider::processEdge -> MetaTileManager::insertEdge
+ * -> TileManager::insertEdge + VertexStore::increment{Out,In}Degree,
+ * src/include/edge-inserter/i-edge-provider.h:81-96, meta-tile-manager.h:112-125,
+ * tile-manager.h:136-163). Edges join the append region; degrees count every
+ * copy (duplicates included). Every live job is notified of every edge
+ * (Algorithm::edgeChanged(INSERT), meta-tile-manager.h:192-197). `w` may be NULL
+ * for an unweighted store. All ids are checked before anything is inserted. */
+int cytom_insert_batch(cytom_ctx* ctx, const uint32_t* src, const uint32_t* tgt,
+                       const uint32_t* w, uint64_t count, int where);
+
+/* TileStore::doGlobalCompaction -> TileManager::compactStorage for every tile
+ * (tile-store.h:144-172, tile-manager.h:192-291): merges the append region into the
+ * sorted tiles and drops duplicate (src,tgt) (for weighted duplicates the minimum
+ * weight is kept). Runs implicitly before an algorithm runs. */
+int cytom_compact(cytom_ctx* ctx);
+
+/* Edge counts: compacted (distinct) edges and edges still in the append region
+ * (TileStore::countEdges, tile-store.h:174-185). */
+int cytom_count_edges(const cytom_ctx* ctx, uint64_t* compacted, uint64_t* pending);
+
+/* Bit-exact view of the compacted tiles (TileManager::getCounts / getIdCounts /
+ * getTargets / getCSRWeights, tile-manager.h:459-467), flattened: tile_ptr[ntiles+1]
+ * (host, u64), edges[E] packed (src_local << 16 | tgt_local) in CSR order,
+ * weights[E] (NULL to skip) and compact[ntiles] (1 = compact counts_ storage,
+ * chosen when distinct sources >= vpt/2, tile-manager.h:261-263; NULL to skip).
+ * All outputs are host buffers sized from cytom_count_edges. */
+int cytom_get_tiles(cytom_ctx* ctx, uint64_t* tile_ptr, uint32_t* edges, uint32_t* weights,
+                    uint8_t* compact);
+/* vertex_degree_t {in, out} per vertex (datatypes.h:119-122), host buffers. */
+int cytom_get_degrees(cytom_ctx* ctx, uint32_t* out_degree, uint32_t* in_degree);
+
+/* ---- Jobs (vertex programs) -------------------------------------------- */
+
+/* Per-job parameters (ConfigContext::algorithm_config and friends). */
+typedef struct cytom_job_params {
+  uint64_t start_vertex;   /* --algo-start-id (BFS, SSSP) */
+  uint64_t max_iterations; /* --algorithm-iterations per run (reference default 100) */
+  double delta;            /* --delta: PR-delta activation threshold */
+  double alpha;            /* damping (reference ALPHA 0.85) */
+  double tolerance;        /* PageRank / PR-delta: stop when the FP64 L1 residual <= tolerance
+                              (relative to the rank sum for PR_DELTA); 0 = reference rule only */
+  int32_t kahan;           /* PAGERANK: 1 = FP32 with compensated accumulation, 0 = FP64 plain */
+  int32_t reserved;
+} cytom_job_params;
+void cytom_job_params_default(cytom_job_params* p);
+
+/* Creates a job with its own vertex state (VertexStore<V> + Algorithm::init_vertices,
+ * e.g. examples/bfs.cc:170-197). The first run computes from scratch; later runs
+ * continue from the previous state, seeded by the edges inserted in between. */
+int cytom_job_create(cytom_ctx* ctx, int algo, const cytom_job_params* params, int* job_id);
+int cytom_job_destroy(cytom_ctx* ctx, int job_id);
+/* Re-initialises a job (ContinuousAlgorithmExecutor::initAlgorithm, continuous-algorithm-executor.h:342). */
+int cytom_job_reset(cytom_ctx* ctx, int job_id);
+
+/* Per-run statistics of one job (the counters of continuous-algorithm-executor.h:53-177). */
+typedef struct cytom_run_stats {
+  uint64_t iterations;     /* pull/apply rounds executed */
+  uint64_t count_edges;    /* edges of tiles with an active source, summed over rounds
+                              (the reference's processed-edge count, algorithm-executor.h:424-426) */
+  uint64_t edges_scanned;  /* edges this engine actually read */
+  uint64_t active_vertices;/* vertices activated, summed over rounds */
+  int32_t converged;
+  int32_t reserved;
+  double residual;         /* PageRank: final FP64 L1 residual */
+  double elapsed_ms;       /* device time of the run (CUDA events) */
+} cytom_run_stats;
+
+/* ContinuousAlgorithmExecutor::executeAlgorithm (continuous-algorithm-executor.h:49-249)
+ * for one job: compacts pending edges, then iterates pull -> apply -> swap until no
+ * vertex changes or max_iterations. */
+int cytom_run(cytom_ctx* ctx, int job_id, cytom_run_stats* stats);
+/* Runs several jobs of this context back to back. */
+int cytom_run_many(cytom_ctx* ctx, const int* job_ids, int count, cytom_run_stats* stats);
+
+/* Result of a job (ResultsWriter dumps vertices_.next, results-writer.h:54-64):
+ * BFS levels / CC labels / SSSP distances as uint32 (UINT32_MAX = unreached),
+ * PR_DELTA and PAGERANK ranks as float. `out` holds vertices elements. */
+int cytom_get_result(cytom_ctx* ctx, int job_id, void* out, int where);
+
+/* ---- Instrumentation --------------------------------------------------- */
+
+/* Per-kernel-class timing, recorded with CUDA events around each launch when
+ * profiling is on (off by default; it serialises launches). */
+#define CYTOM_KERNEL_CLASSES 8
+typedef struct cytom_kernel_stats {
+  char name[CYTOM_KERNEL_CLASSES][24];
+  uint64_t launches[CYTOM_KERNEL_CLASSES];
+  double total_ms[CYTOM_KERNEL_CLASSES];
+  double algo_bytes[CYTOM_KERNEL_CLASSES]; /* algorithmic bytes moved, summed */
+} cytom_kernel_stats;
+int cytom_set_profiling(cytom_ctx* ctx, int on);
+int cytom_get_kernel_stats(cytom_ctx* ctx, cytom_kernel_stats* out);
+int cytom_reset_kernel_stats(cytom_ctx* ctx);
+/* Number of this library's kernels launched since creation. */
+int cytom_launch_count(const cytom_ctx* ctx, uint64_t* launches);
+/* Waits for all work of the context's stream. */
+int cytom_sync(cytom_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

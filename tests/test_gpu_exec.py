@@ -1,0 +1,127 @@
+"""GPU parity of the BFS / CC / SSSP executors against the CPU oracle.
+
+Fresh runs: values, round count and the reference's processed-edge count equal the
+oracle's Jacobi run round for round. Streaming runs: after every batch the
+incremental result equals the oracle's from-scratch fixed point. Bit-exact."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ALGOS = [("BFS", 0), ("CC", 1), ("SSSP", 2)]
+
+
+def build(cg, orc, scale, vpt, m, seed, adaptive=True):
+    n = 1 << scale
+    s, t = orc.rmat(scale, 0, m, seed)
+    w = orc.edge_weights(s, t, seed + 1)
+    eng = cg.Engine(n, vpt, weight_type=cg.WEIGHT_U32, adaptive_scheduling=adaptive)
+    eng.insert_edges(s, t, w)
+    eng.do_global_compaction()
+    st = orc.Store(n, vpt, weighted=True)
+    st.insert(s, t, w)
+    st.compact()
+    return eng, st
+
+
+@pytest.mark.parametrize("name,algo", ALGOS)
+@pytest.mark.parametrize("scale,vpt,ef,start", [(10, 64, 8, 0), (12, 256, 16, 1), (14, 4096, 16, 0),
+                                                (16, 65536, 8, 3), (17, 2048, 16, 0)])
+def test_fresh_run_round_by_round(cg, orc, name, algo, scale, vpt, ef, start):
+    eng, st = build(cg, orc, scale, vpt, ef << scale, seed=scale + 31)
+    with eng:
+        prog = getattr(cg, name)(eng, start_vertex=start, max_iterations=1000)
+        stats = prog.execute_algorithm()
+        got = prog.result()
+        ref, rinfo = st.run_minprop(algo, start=start, max_iter=1000)
+        assert np.array_equal(got, ref)
+        assert stats["iterations"] == rinfo["iterations"]
+        assert stats["count_edges"] == rinfo["count_edges"]
+        assert stats["converged"] == 1
+
+
+@pytest.mark.parametrize("name,algo", ALGOS)
+def test_iteration_cap_matches_reference_state(cg, orc, name, algo):
+    # with a cap below convergence the state after k rounds still matches (Jacobi rounds)
+    eng, st = build(cg, orc, 14, 1024, 16 << 14, seed=5)
+    with eng:
+        for cap in (1, 2, 3):
+            prog = getattr(cg, name)(eng, start_vertex=0, max_iterations=cap)
+            stats = prog.execute_algorithm()
+            ref, rinfo = st.run_minprop(algo, start=0, max_iter=cap)
+            assert np.array_equal(prog.result(), ref), cap
+            assert stats["iterations"] == rinfo["iterations"]
+            assert stats["count_edges"] == rinfo["count_edges"]
+
+
+@pytest.mark.parametrize("name,algo", ALGOS)
+def test_adaptive_scheduling_off(cg, orc, name, algo):
+    eng, st = build(cg, orc, 12, 512, 16 << 12, seed=9, adaptive=False)
+    with eng:
+        prog = getattr(cg, name)(eng, start_vertex=0, max_iterations=1000)
+        stats = prog.execute_algorithm()
+        ref, rinfo = st.run_minprop(algo, start=0, max_iter=1000, adaptive=False)
+        assert np.array_equal(prog.result(), ref)
+        assert stats["iterations"] == rinfo["iterations"]
+        assert stats["count_edges"] == rinfo["count_edges"]
+
+
+@pytest.mark.parametrize("scale,vpt,nb,batch", [(12, 512, 6, 8192), (16, 4096, 8, 65536),
+                                                (18, 65536, 4, 1 << 18)])
+def test_streaming_incremental_equals_from_scratch(cg, orc, scale, vpt, nb, batch):
+    n = 1 << scale
+    with cg.Engine(n, vpt, weight_type=cg.WEIGHT_U32) as eng:
+        progs = [cg.BFS(eng, start_vertex=0, max_iterations=1000), cg.CC(eng, max_iterations=1000),
+                 cg.SSSP(eng, start_vertex=0, max_iterations=1000)]
+        st = orc.Store(n, vpt, weighted=True)
+        for b in range(nb):
+            s, t = orc.rmat(scale, b * batch, batch, seed=scale)
+            w = orc.edge_weights(s, t, 99)
+            eng.insert_edges(s, t, w)
+            eng.do_global_compaction()
+            st.insert(s, t, w)
+            st.compact()
+            for prog, (_, algo) in zip(progs, ALGOS):
+                stats = prog.execute_algorithm()
+                assert stats["converged"] == 1
+                ref, _ = st.run_minprop(algo, start=0, max_iter=1000)
+                assert np.array_equal(prog.result(), ref), (b, algo)
+
+
+def test_isolated_start_vertex(cg):
+    with cg.Engine(1 << 10, 256, weight_type=cg.WEIGHT_U32) as eng:
+        eng.insert_edges(np.array([1, 2], np.uint32), np.array([2, 3], np.uint32),
+                         np.array([4, 5], np.uint32))
+        p = cg.BFS(eng, start_vertex=7)
+        st = p.execute_algorithm()
+        r = p.result()
+        assert r[7] == 0 and (np.delete(r, 7) == 0xFFFFFFFF).all()
+        assert st["iterations"] == 1
+        q = cg.SSSP(eng, start_vertex=1)
+        q.execute_algorithm()
+        d = q.result()
+        assert d[1] == 0 and d[2] == 4 and d[3] == 9
+
+
+def test_start_vertex_out_of_range(cg):
+    with cg.Engine(1 << 10, 256) as eng:
+        with pytest.raises(cg.CytomError) as ei:
+            cg.BFS(eng, start_vertex=1 << 10)
+        assert ei.value.code == -3
+
+
+def test_graph_and_host_loop_agree(cg, orc, monkeypatch):
+    # profiling mode drives the loop from the host; results and counters must agree
+    eng, st = build(cg, orc, 14, 2048, 16 << 14, seed=12)
+    with eng:
+        a = cg.CC(eng, max_iterations=1000)
+        sa = a.execute_algorithm()
+        eng.set_profiling(True)
+        b = cg.CC(eng, max_iterations=1000)
+        sb = b.execute_algorithm()
+        eng.set_profiling(False)
+        assert np.array_equal(a.result(), b.result())
+        for k in ("iterations", "count_edges", "edges_scanned", "active_vertices"):
+            assert sa[k] == sb[k], k
+        ks = eng.kernel_stats()
+        assert ks["gather"]["launches"] >= sb["iterations"]

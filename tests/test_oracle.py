@@ -1,0 +1,251 @@
+"""CPU tests of the oracle: each restatement is checked against an independent
+numpy / pure-Python restatement of the same reference code."""
+import struct
+
+import numpy as np
+import pytest
+
+M64 = (1 << 64) - 1
+
+
+def py_hash64(a):
+    # src/include/util/util.h:188-196, restated a second time in Python
+    a = ((a + 0x7ed55d166bef7a1d) + (a << 12)) & M64
+    a = ((a ^ 0xc761c23c510fa2dd) ^ (a >> 9)) & M64
+    a = ((a + 0x165667b183a9c0e1) + (a << 59)) & M64
+    a = ((a + 0xd3a2646cab3487e3) ^ (a << 49)) & M64
+    a = ((a + 0xfd7046c5ef9ab54c) + (a << 3)) & M64
+    a = ((a ^ 0xb55a4f090dd4a67b) ^ (a >> 32)) & M64
+    return a
+
+
+def py_rmat_edge(scale, index, seed, a, b, c):
+    # rmat-context.h:39-73 followed literally (rMatIterative)
+    h = py_hash64(seed)
+    rs = py_hash64((2 * index * h) & M64)
+    st = py_hash64(((2 * index + 1) * h) & M64)
+    n = 1 << scale
+    local_n, lrs = n, rs
+    while local_n != 1:
+        local_n //= 2
+        lrs = (lrs + st) & M64
+    s = t = 0
+    while local_n != n:
+        local_n *= 2
+        lrs = (lrs - st) & M64
+        r = float(py_hash64(lrs)) / float(M64)
+        if r < a:
+            pass
+        elif r < a + b:
+            t += local_n // 2
+        elif r < a + b + c:
+            s += local_n // 2
+        else:
+            s += local_n // 2
+            t += local_n // 2
+    return s, t
+
+
+def test_hash_matches_python(orc):
+    for v in [0, 1, 2, 3, 12345, 2**63, M64, 0xdeadbeefcafebabe]:
+        assert orc.hash64(v) == py_hash64(v)
+
+
+@pytest.mark.parametrize("scale,seed", [(4, 1), (10, 2), (16, 3), (22, 17)])
+def test_rmat_matches_python(orc, scale, seed):
+    first, count = 1000, 300
+    s, t = orc.rmat(scale, first, count, seed)
+    for k in range(count):
+        assert (int(s[k]), int(t[k])) == py_rmat_edge(scale, first + k, seed, orc.RMAT_A,
+                                                       orc.RMAT_B, orc.RMAT_C)
+
+
+def test_rmat_quadrant_statistics(orc):
+    # top-level quadrant frequencies follow a, b, c, d
+    s, t = orc.rmat(20, 0, 1 << 18, seed=5)
+    top_s, top_t = s >> 19, t >> 19
+    fa = np.mean((top_s == 0) & (top_t == 0))
+    fb = np.mean((top_s == 0) & (top_t == 1))
+    fc = np.mean((top_s == 1) & (top_t == 0))
+    assert abs(fa - 0.57) < 0.01 and abs(fb - 0.19) < 0.01 and abs(fc - 0.19) < 0.01
+    assert s.max() < (1 << 20) and t.max() < (1 << 20)
+
+
+def test_gridgraph_decode(orc):
+    # writer of src/scripts/convert_graph.py:15-16: struct.pack("<l", ...) pairs
+    pairs = [(0, 1), (5, 3), (1023, 7), (2, 2)]
+    data = b"".join(struct.pack("<l", a) + struct.pack("<l", b) for a, b in pairs)
+    s, t = orc.gridgraph_decode(data, 1024)
+    assert s.tolist() == [p[0] for p in pairs] and t.tolist() == [p[1] for p in pairs]
+    assert orc.gridgraph_decode(struct.pack("<ll", -1, 0), 1024) is None
+    assert orc.gridgraph_decode(struct.pack("<ll", 0, 1024), 1024) is None
+    # a trailing partial record is ignored (count = size / 8, jobs.h:64)
+    s2, _ = orc.gridgraph_decode(data + b"\x01\x02\x03", 1024)
+    assert len(s2) == 4
+
+
+def np_compact(n, vpt, batches, weighted):
+    """Independent numpy restatement of TileManager::compactStorage over a sequence
+    of batches (each compacted after insertion)."""
+    T = n // vpt
+    tiles = {}
+    flags = np.zeros(T * T, np.uint8)
+    for src, tgt, w in batches:
+        x, y = src // vpt, tgt // vpt
+        for i in range(len(src)):
+            tid = int(x[i] * T + y[i])
+            loc = (int(src[i] % vpt) << 16) | int(tgt[i] % vpt)
+            tiles.setdefault(tid, [[], []])[1].append((loc, int(w[i]) if weighted else 0))
+        for tid, (csr, ovf) in tiles.items():
+            allv = ovf + csr
+            if not allv:
+                continue
+            allv.sort()
+            srcs = {e >> 16 for e, _ in allv}
+            flags[tid] = 1 if len(srcs) >= vpt // 2 else 0
+            out, prev = [], 0xFFFFFFFF
+            for e, wv in allv:
+                if e == prev:
+                    continue
+                prev = e
+                out.append((e, wv))
+            tiles[tid] = [out, []]
+    tp = np.zeros(T * T + 1, np.uint64)
+    ed, wt = [], []
+    for tid in range(T * T):
+        tp[tid] = len(ed)
+        for e, wv in tiles.get(tid, [[], []])[0]:
+            ed.append(e)
+            wt.append(wv)
+    tp[-1] = len(ed)
+    return tp, np.array(ed, np.uint32), np.array(wt, np.uint32), flags
+
+
+@pytest.mark.parametrize("n,vpt,weighted", [(256, 64, False), (256, 32, True), (1024, 1024, True),
+                                             (512, 16, False)])
+def test_compaction_matches_numpy(orc, n, vpt, weighted):
+    rng = np.random.default_rng(n + vpt)
+    batches = []
+    st = orc.Store(n, vpt, weighted)
+    for b in range(3):
+        m = 400 + 100 * b
+        src = rng.integers(0, n, m, dtype=np.uint32)
+        tgt = (rng.integers(0, n // 4, m, dtype=np.uint32) * 4 + rng.integers(0, 4, m)).astype(np.uint32) % n
+        src[:50] = src[50:100]  # duplicates inside a batch
+        tgt[:50] = tgt[50:100]
+        w = rng.integers(1, 255, m, dtype=np.uint32)
+        batches.append((src, tgt, w))
+        st.insert(src, tgt, w if weighted else None)
+        st.compact()
+    tp, ed, wt, cf = st.dump()
+    rtp, red, rwt, rcf = np_compact(n, vpt, batches, weighted)
+    assert np.array_equal(tp, rtp)
+    assert np.array_equal(ed, red)
+    if weighted:
+        assert np.array_equal(wt, rwt)
+    assert np.array_equal(cf, rcf)
+
+
+def test_fillcsr_corner_edge_dropped(orc):
+    # tile-manager.h:519-541: with vpt = 65536 an otherwise empty tile whose only edge is
+    # local (65535, 65535) comes out empty; next to another edge it survives.
+    n, vpt = 1 << 17, 1 << 16
+    st = orc.Store(n, vpt)
+    st.insert(np.array([65535, 65535], np.uint32), np.array([65535, 65535], np.uint32))
+    st.insert(np.array([65536 + 65535, 65536 + 5], np.uint32), np.array([65535, 65535], np.uint32))
+    st.compact()
+    tp, ed, _, _ = st.dump()
+    assert tp[1] - tp[0] == 0          # tile (0,0) lost its only edge
+    assert tp[3] - tp[2] == 2          # tile (1,0) keeps both
+    o, _ = st.degrees()
+    assert o[65535] == 2               # degrees still count the dropped copies
+
+
+def test_compact_flag_threshold(orc):
+    n, vpt = 64, 16
+    st = orc.Store(n, vpt)
+    st.insert(np.arange(8, dtype=np.uint32), np.zeros(8, np.uint32))       # 8 sources in tile (0,0)
+    st.insert(np.arange(7, dtype=np.uint32) + 16, np.zeros(7, np.uint32))  # 7 sources in tile (1,0)
+    st.compact()
+    _, _, _, cf = st.dump()
+    assert cf[0] == 1 and cf[4] == 0
+
+
+def np_fixed_point(n, src, tgt, w, algo, start):
+    INF = np.iinfo(np.uint32).max
+    val = np.full(n, INF, np.uint64)
+    if algo == 1:
+        val = np.arange(n, dtype=np.uint64)
+    else:
+        val[start] = 0
+    while True:
+        cand = val[src] + (1 if algo == 0 else (0 if algo == 1 else w.astype(np.uint64)))
+        ok = val[src] != INF
+        new = val.copy()
+        np.minimum.at(new, tgt[ok], cand[ok])
+        if np.array_equal(new, val):
+            return val.astype(np.uint32)
+        val = new
+
+
+@pytest.mark.parametrize("algo", [0, 1, 2])
+@pytest.mark.parametrize("vpt", [64, 256])
+def test_minprop_fixed_points(orc, algo, vpt):
+    n = 1024
+    s, t = orc.rmat(10, 0, 6000, seed=3)
+    w = orc.edge_weights(s, t, 9)
+    st = orc.Store(n, vpt, weighted=True)
+    st.insert(s, t, w)
+    st.compact()
+    got, info = st.run_minprop(algo, start=0, max_iter=1000)
+    assert info["converged"] == 1
+    assert np.array_equal(got, np_fixed_point(n, s.astype(np.int64), t.astype(np.int64), w, algo, 0))
+    # adaptive scheduling off reaches the same fixed point
+    got2, _ = st.run_minprop(algo, start=0, max_iter=1000, adaptive=False)
+    assert np.array_equal(got, got2)
+
+
+def test_pagerank_unnorm_matches_numpy(orc):
+    n = 512
+    s, t = orc.rmat(9, 0, 4000, seed=4)
+    st = orc.Store(n, 128)
+    st.insert(s, t)
+    st.compact()
+    r, it = st.pagerank_unnorm(tol=1e-15)
+    tp, ed, _, _ = st.dump()
+    deg, _ = st.degrees()
+    T = 4
+    xs, ys = [], []
+    for tid in range(T * T):
+        for e in ed[int(tp[tid]):int(tp[tid + 1])]:
+            xs.append((tid // T) * 128 + (int(e) >> 16))
+            ys.append((tid % T) * 128 + (int(e) & 0xFFFF))
+    xs, ys = np.array(xs), np.array(ys)
+    x = np.ones(n)
+    for _ in range(2000):
+        acc = np.zeros(n)
+        np.add.at(acc, ys, x[xs] / deg[xs])
+        x = 0.15 + 0.85 * acc
+    assert np.allclose(r, x, rtol=1e-10, atol=1e-12)
+
+
+def test_pagerank_norm_sums_to_one(orc):
+    n = 1024
+    s, t = orc.rmat(10, 0, 5000, seed=6)
+    st = orc.Store(n, 256)
+    st.insert(s, t)
+    st.compact()
+    r, _ = st.pagerank_norm()
+    assert abs(r.sum() - 1.0) < 1e-10 and (r > 0).all()
+
+
+def test_prdelta_ref_converges_toward_fixed_point(orc):
+    n = 1024
+    s, t = orc.rmat(10, 0, 8000, seed=8)
+    st = orc.Store(n, 256)
+    st.insert(s, t)
+    st.compact()
+    rank, info = st.run_prdelta_ref(max_iter=200, delta=0.0)
+    r64, _ = st.pagerank_unnorm()
+    rel = np.abs(rank - r64).sum() / r64.sum()
+    assert rel < 1e-5, rel

@@ -22,8 +22,11 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 
 #include "engine.h"
+#include "ptx.cuh"
 
 namespace cytom {
 
@@ -56,6 +59,10 @@ __global__ void begin_kernel(const JobDesc* __restrict__ jd, const StoreDesc* __
 }
 
 // Apply: `initial` = the seeding apply before round 0 (writes parity 0).
+// rows[parity][x] receives the number of vertices of tile row x that are active in
+// the next round (0 = the row is skipped; vpt = every source active, the frontier
+// test is skipped). A warp covers 32 consecutive bitmap words; when they share one
+// row (vpt >= 1024) it adds its row count with a single atomic.
 __global__ void __launch_bounds__(APPLY_T) apply_minprop_kernel(const JobDesc* __restrict__ jd,
                                                                 const StoreDesc* __restrict__ sd,
                                                                 int initial) {
@@ -70,24 +77,51 @@ __global__ void __launch_bounds__(APPLY_T) apply_minprop_kernel(const JobDesc* _
   uint32_t* __restrict__ fa = jd->fa;
   uint32_t* __restrict__ cur = jd->cur;
   const uint32_t* __restrict__ next = jd->next;
+  const unsigned lane = threadIdx.x & 31;
   unsigned cnt = 0;
   unsigned long long teps = 0;
   uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nwords; i += stride) {
-    uint32_t w = ch[i];
-    fa[i] = w;
-    if (w == 0) continue;
-    ch[i] = 0;
-    cnt += __popc(w);
-    uint32_t bits = w;
-    while (bits) {
-      int b = __ffs(bits) - 1;
-      bits &= bits - 1;
-      uint64_t v = (i << 5) + b;
-      cur[v] = next[v];
-      if (lvpt < 5 || b == __ffs(w) - 1) {
-        uint64_t x = v >> lvpt;
-        if (rows_w[x] == 0 && atomicExch(&rows_w[x], 1u) == 0) teps += row_edges(sd, x);
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < nwords; base += stride) {
+    const uint64_t i = base + threadIdx.x;
+    uint32_t w = 0;
+    if (i < nwords) {
+      w = ch[i];
+      fa[i] = w;
+      if (w) {
+        ch[i] = 0;
+        uint32_t bits = w;
+        while (bits) {
+          const int b = __ffs(bits) - 1;
+          bits &= bits - 1;
+          const uint64_t v = (i << 5) + b;
+          cur[v] = next[v];
+        }
+      }
+    }
+    const unsigned pc = __popc(w);
+    cnt += pc;
+    if (lvpt >= 10) {
+      // the warp's 32 words (1024 vertices) lie in one tile row
+      unsigned tot = pc;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xFFFFFFFFu, tot, o);
+      if (lane == 0 && tot) {
+        const uint64_t x = ((base + (threadIdx.x & ~31u)) << 5) >> lvpt;
+        if (atomicAdd(&rows_w[x], tot) == 0) teps += row_edges(sd, x);
+      }
+    } else if (w) {
+      uint32_t bits = w;
+      while (bits) {
+        const int b = __ffs(bits) - 1;
+        const uint64_t v = (i << 5) + b;
+        const uint64_t x = v >> lvpt;
+        // count this row's bits of the word at once
+        const uint64_t row_first = x << lvpt;
+        const uint64_t row_last = row_first + (1ULL << lvpt);  // exclusive
+        uint32_t mrow = bits;
+        if (row_last < ((i + 1) << 5)) mrow &= (1u << (uint32_t)(row_last - (i << 5))) - 1u;
+        bits &= ~mrow;
+        if (atomicAdd(&rows_w[x], (unsigned)__popc(mrow)) == 0) teps += row_edges(sd, x);
       }
     }
   }
@@ -99,7 +133,7 @@ __global__ void __launch_bounds__(APPLY_T) apply_minprop_kernel(const JobDesc* _
     cnt += __shfl_xor_sync(0xFFFFFFFFu, cnt, o);
     teps += __shfl_xor_sync(0xFFFFFFFFu, teps, o);
   }
-  const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned wid = threadIdx.x >> 5;
   if (lane == 0) {
     s_cnt[wid] = cnt;
     s_teps[wid] = teps;
@@ -130,7 +164,7 @@ __global__ void control_kernel(const JobDesc* __restrict__ jd, cudaGraphConditio
     }
     unsigned a = ls->active[p];
     ls->active_total += a;
-    ls->cont = (a > 0 && ls->iter < ls->max_iter) ? 1u : 0u;
+    ls->cont = (a > 0 && ls->iter < ls->max_iter && ls->err == 0) ? 1u : 0u;
   }
   if (use_handle) cudaGraphSetConditional(h, ls->cont);
 }
@@ -243,6 +277,303 @@ __global__ void __launch_bounds__(GATHER_T) gather_minprop_kernel(const JobDesc*
   }
 }
 
+// Streaming gather: the same round as gather_minprop_kernel, with the edge array
+// (and weights) streamed through shared memory by bulk copies (cp.async.bulk) in a
+// SG_NST-deep mbarrier pipeline, so each SM keeps tens of KB of HBM reads in
+// flight while its threads resolve the dependent frontier / value / atomic loads of
+// 16 edges each in batches.
+//  - Stages are 4096-edge slices of the tile-major edge array. A block owns groups
+//    of SG_GROUP consecutive stages (group g, g + gridDim.x, ...), so consecutive
+//    stages of a block usually lie in one tile row and its frontier words stay in L1.
+//  - A stage whose tile rows are all inactive is skipped without being copied.
+//  - Single-row stages (the common case at large vertices-per-tile) take the source
+//    row from the stage: the frontier test needs no per-edge tile lookup, and only
+//    edges with an active source look up their target tile.
+constexpr int SG_T = 256;
+constexpr int SG_E = 4096;
+constexpr int SG_NST = 3;
+constexpr int SG_GROUP = 8;
+static_assert(SG_E == SG_T * 16, "16 edges per thread per stage");
+
+template <int ALGO>
+__host__ __device__ constexpr size_t gather_stream_smem() {
+  return (size_t)SG_NST * SG_E * 4 * (ALGO == 2 ? 2 : 1) + SG_NST * sizeof(uint64_t);
+}
+
+template <int ALGO>
+__global__ void __launch_bounds__(SG_T, 2) gather_stream_kernel(const JobDesc* __restrict__ jd,
+                                                                 const StoreDesc* __restrict__ sd,
+                                                                 int adaptive) {
+  extern __shared__ __align__(128) uint8_t smem_raw[];
+  uint32_t* ebuf = reinterpret_cast<uint32_t*>(smem_raw);
+  uint32_t* wbuf = ebuf + SG_NST * SG_E;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + (size_t)SG_NST * SG_E * 4 * (ALGO == 2 ? 2 : 1));
+
+  LoopState* ls = jd->ls;
+  if (!ls->cont) return;
+  const unsigned p = ls->iter & 1u;
+  const uint64_t T = sd->T;
+  const unsigned* __restrict__ rows_cur = jd->rows + p * T;
+  unsigned* rows_nxt = jd->rows + (p ^ 1u) * T;
+  {
+    uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < T; i += stride)
+      rows_nxt[i] = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      ls->active[p ^ 1u] = 0;
+      ls->teps[p ^ 1u] = 0;
+      ls->count_edges += adaptive ? ls->teps[p] : sd->E;
+    }
+  }
+  const uint32_t* __restrict__ edges = sd->edges;
+  const uint32_t* __restrict__ wts = sd->wts;
+  const unsigned long long* __restrict__ tile_ptr = sd->tile_ptr;
+  const uint32_t* __restrict__ chunk_tile = sd->chunk_tile;
+  const uint32_t* __restrict__ fa = jd->fa;
+  const uint32_t* __restrict__ cur = jd->cur;
+  uint32_t* next = jd->next;
+  uint32_t* ch = jd->ch;
+  const uint64_t E = sd->E, nchunks = sd->nchunks;
+  const uint32_t lT = sd->lT, lvpt = sd->lvpt;
+  const uint32_t ymask = (uint32_t)(T - 1);
+  const uint64_t nst = (E + SG_E - 1) / SG_E;
+  const uint64_t G = gridDim.x;
+
+  // rows spanned by stage s: [row of its first edge, row of the first edge after it]
+  auto stage_rows = [&](uint64_t s, uint32_t& x0, uint32_t& x1) {
+    uint64_t c0 = s * (SG_E / kChunk);
+    uint64_t c1 = c0 + SG_E / kChunk;
+    if (c1 > nchunks) c1 = nchunks;
+    x0 = chunk_tile[c0] >> lT;
+    x1 = chunk_tile[c1] >> lT;
+  };
+  auto stage_active = [&](uint64_t s) -> bool {
+    if (!adaptive) return true;
+    uint32_t x0, x1;
+    stage_rows(s, x0, x1);
+    for (uint32_t x = x0; x <= x1; ++x)
+      if (rows_cur[x]) return true;
+    return false;
+  };
+  // the block's stage sequence: groups blockIdx.x, blockIdx.x + G, ... of SG_GROUP stages
+  auto advance = [&](uint64_t s) -> uint64_t {
+    uint64_t n1 = s + 1;
+    if ((n1 % SG_GROUP) != 0 && n1 < nst) return n1;
+    return (s / SG_GROUP + G) * SG_GROUP;
+  };
+  auto next_active = [&](uint64_t s) -> uint64_t {
+    while (s < nst && !stage_active(s)) s = advance(s);
+    return s < nst ? s : nst;
+  };
+  auto issue = [&](int slot, uint64_t s) {
+    const uint64_t e0 = s * SG_E;
+    const uint64_t rem = E - e0;
+    const uint32_t cnt = rem < (uint64_t)SG_E ? (uint32_t)rem : (uint32_t)SG_E;
+    const uint32_t bytes = ((cnt + 3u) & ~3u) * 4u;
+    fence_proxy_async_smem();
+    mbar_arrive_expect_tx(&bar[slot], bytes * (ALGO == 2 ? 2u : 1u));
+    bulk_g2s(ebuf + slot * SG_E, edges + e0, bytes, &bar[slot]);
+    if (ALGO == 2) bulk_g2s(wbuf + slot * SG_E, wts + e0, bytes, &bar[slot]);
+  };
+
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < SG_NST; ++k) mbar_init(&bar[k], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  const uint64_t first = (uint64_t)blockIdx.x * SG_GROUP;
+  uint64_t st0 = next_active(first < nst ? first : nst);
+  uint64_t st1 = (st0 < nst) ? next_active(advance(st0)) : nst;
+  uint64_t st2 = (st1 < nst) ? next_active(advance(st1)) : nst;
+  if (threadIdx.x == 0) {
+    if (st0 < nst) issue(0, st0);
+    if (st1 < nst) issue(1, st1);
+    if (st2 < nst) issue(2, st2);
+  }
+  uint64_t s_next = (st2 < nst) ? next_active(advance(st2)) : nst;
+  uint32_t phases = 0;  // bit k: parity to wait for on slot k
+  int slot = 0;
+  unsigned long long scanned = 0;
+  bool failed = false;
+
+  while (st0 < nst) {
+    const bool ok = mbar_wait(&bar[slot], (phases >> slot) & 1u);
+    if (!__syncthreads_and(ok)) {
+      failed = true;
+      break;
+    }
+    phases ^= 1u << slot;
+    const uint64_t e0 = st0 * SG_E;
+    const uint64_t rem = E - e0;
+    const uint32_t cnt = rem < (uint64_t)SG_E ? (uint32_t)rem : (uint32_t)SG_E;
+    if (threadIdx.x == 0) scanned += cnt;
+    const uint32_t* eb = ebuf + slot * SG_E;
+    const uint32_t* wb = wbuf + slot * SG_E;
+    // tiles of the stage's first edge and of the first edge after it
+    uint32_t tf, ta;
+    {
+      const uint64_t c0 = st0 * (SG_E / kChunk);
+      uint64_t c1 = c0 + SG_E / kChunk;
+      if (c1 > nchunks) c1 = nchunks;
+      tf = chunk_tile[c0];
+      ta = chunk_tile[c1];
+    }
+    const bool single_row = (tf >> lT) == (ta >> lT);
+    const bool single_tile = tf == ta;
+    const uint32_t vpt = 1u << lvpt;
+    // a fully active row needs no frontier test
+    const bool full_row = single_row && (!adaptive || rows_cur[tf >> lT] == vpt);
+
+    uint32_t qv[16], ww[16], uu[16];
+    uint32_t vmask = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const uint32_t i0 = threadIdx.x * 4 + (uint32_t)k * (SG_T * 4);
+      const uint4 q = *reinterpret_cast<const uint4*>(eb + i0);
+      qv[4 * k + 0] = q.x;
+      qv[4 * k + 1] = q.y;
+      qv[4 * k + 2] = q.z;
+      qv[4 * k + 3] = q.w;
+      if (ALGO == 2) {
+        const uint4 wq = *reinterpret_cast<const uint4*>(wb + i0);
+        ww[4 * k + 0] = wq.x;
+        ww[4 * k + 1] = wq.y;
+        ww[4 * k + 2] = wq.z;
+        ww[4 * k + 3] = wq.w;
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) vmask |= ((i0 + j) < cnt) ? (1u << (4 * k + j)) : 0u;
+    }
+    if (single_row) {
+      const uint32_t xb = (tf >> lT) << lvpt;
+#pragma unroll
+      for (int idx = 0; idx < 16; ++idx) uu[idx] = xb | (qv[idx] >> 16);
+    } else {
+      // general path: per-edge tile lookup for the source row
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const uint32_t i0 = threadIdx.x * 4 + (uint32_t)k * (SG_T * 4);
+        const uint64_t eg = e0 + i0;
+        uint32_t t = 0;
+        unsigned long long tend = 0;
+        if (i0 < cnt) {
+          t = chunk_tile[eg >> 7];
+          tend = tile_ptr[t + 1];
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int idx = 4 * k + j;
+          if ((vmask >> idx) & 1u) {
+            while (tend <= eg + j) {
+              ++t;
+              tend = tile_ptr[t + 1];
+            }
+            const uint32_t x = t >> lT;
+            uu[idx] = (x << lvpt) | (qv[idx] >> 16);
+            if (adaptive && rows_cur[x] == 0) vmask &= ~(1u << idx);
+          } else {
+            uu[idx] = 0;
+          }
+        }
+      }
+    }
+    uint32_t amask = vmask;
+    if (adaptive && !full_row) {
+      uint32_t fw[16];
+#pragma unroll
+      for (int idx = 0; idx < 16; ++idx)
+        fw[idx] = ((vmask >> idx) & 1u) ? __ldg(fa + (uu[idx] >> 5)) : 0u;
+      amask = 0;
+#pragma unroll
+      for (int idx = 0; idx < 16; ++idx) amask |= ((fw[idx] >> (uu[idx] & 31)) & 1u) << idx;
+      amask &= vmask;
+    }
+    if (amask) {
+      uint32_t cand[16], vv[16];
+#pragma unroll
+      for (int idx = 0; idx < 16; ++idx) cand[idx] = ((amask >> idx) & 1u) ? __ldg(cur + uu[idx]) : kInf;
+      if (single_tile) {
+        const uint32_t yb = (tf & ymask) << lvpt;
+#pragma unroll
+        for (int idx = 0; idx < 16; ++idx) vv[idx] = yb | (qv[idx] & 0xFFFFu);
+      } else {
+        // target tiles of the edges with an active source
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const uint32_t i0 = threadIdx.x * 4 + (uint32_t)k * (SG_T * 4);
+          const uint64_t eg = e0 + i0;
+          const uint32_t kmask = (amask >> (4 * k)) & 0xFu;
+          uint32_t t = 0;
+          unsigned long long tend = 0;
+          if (kmask) {
+            t = chunk_tile[eg >> 7];
+            tend = tile_ptr[t + 1];
+          }
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int idx = 4 * k + j;
+            vv[idx] = 0;
+            if ((kmask >> j) & 1u) {
+              while (tend <= eg + j) {
+                ++t;
+                tend = tile_ptr[t + 1];
+              }
+              vv[idx] = ((t & ymask) << lvpt) | (qv[idx] & 0xFFFFu);
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int idx = 0; idx < 16; ++idx) {
+        const uint32_t c = cand[idx];
+        if (c == kInf) continue;
+        if (ALGO == 0) {
+          cand[idx] = c + 1;
+        } else if (ALGO == 2) {
+          const unsigned long long sum = (unsigned long long)c + ww[idx];
+          cand[idx] = sum >= kInf ? kInf : (uint32_t)sum;
+        }
+      }
+      uint32_t nv[16];
+#pragma unroll
+      for (int idx = 0; idx < 16; ++idx) nv[idx] = (cand[idx] != kInf) ? __ldcg(next + vv[idx]) : 0u;
+      // A candidate below the value read is below current[v] too (next <= current), so
+      // next[v] ends the round below current[v]: v changed. Both updates are
+      // fire-and-forget reductions.
+#pragma unroll
+      for (int idx = 0; idx < 16; ++idx)
+        if (cand[idx] != kInf && cand[idx] < nv[idx]) atomicMin(next + vv[idx], cand[idx]);
+#pragma unroll
+      for (int idx = 0; idx < 16; ++idx)
+        if (cand[idx] != kInf && cand[idx] < nv[idx]) atomicOr(ch + (vv[idx] >> 5), 1u << (vv[idx] & 31));
+    }
+    __syncthreads();  // every thread is done with this slot
+    // refill the slot with the next stage of this block
+    if (threadIdx.x == 0 && s_next < nst) issue(slot, s_next);
+    st0 = st1;
+    st1 = st2;
+    st2 = s_next;
+    if (s_next < nst) s_next = next_active(advance(s_next));
+    slot = (slot + 1 == SG_NST) ? 0 : slot + 1;
+  }
+  if (failed) {
+    // give up: record the error, then wait (bounded) for the copies this block still has in flight
+    if (threadIdx.x == 0) {
+      atomicExch(&ls->err, 1u);
+      for (int k = 0; k < SG_NST; ++k) {
+        const uint64_t sk = (k == 0) ? st0 : (k == 1 ? st1 : st2);
+        const int sl = (slot + k) % SG_NST;
+        if (sk < nst) mbar_wait(&bar[sl], (phases >> sl) & 1u);
+      }
+    }
+    __syncthreads();
+    return;
+  }
+  if (threadIdx.x == 0 && scanned) atomicAdd(&ls->edges_scanned, scanned);
+}
+
 // ---- job state -----------------------------------------------------------
 
 __global__ void init_minprop_kernel(const JobDesc* __restrict__ jd, const StoreDesc* __restrict__ sd,
@@ -352,32 +683,66 @@ int minprop_seed(Ctx* c, Job* j, const uint32_t* src, const uint32_t* tgt, const
   return cuda_err(c, cudaGetLastError(), "seed_minprop");
 }
 
-static void* gather_fn(int algo) {
-  switch (algo) {
-    case CYTOM_ALGO_BFS: return (void*)gather_minprop_kernel<0>;
-    case CYTOM_ALGO_CC: return (void*)gather_minprop_kernel<1>;
-    default: return (void*)gather_minprop_kernel<2>;
+// Gather variant: "stream" (bulk-copy pipeline, default) or "simple" (direct
+// 128-bit loads, one chunk per warp); CYTOM_GATHER selects it.
+static int gather_mode() {
+  static int v = -1;
+  if (v < 0) {
+    const char* s = getenv("CYTOM_GATHER");
+    v = (s && strcmp(s, "simple") == 0) ? 0 : 1;
   }
+  return v;
+}
+
+struct GatherLaunch {
+  void* fn;
+  dim3 grid, block;
+  size_t smem;
+};
+
+static GatherLaunch gather_launch(Ctx* c, int algo) {
+  GatherLaunch g{};
+  if (gather_mode() == 0) {
+    g.fn = algo == CYTOM_ALGO_BFS ? (void*)gather_minprop_kernel<0>
+           : algo == CYTOM_ALGO_CC ? (void*)gather_minprop_kernel<1>
+                                   : (void*)gather_minprop_kernel<2>;
+    g.grid = dim3(grid_persistent(c, 8));
+    g.block = dim3(GATHER_T);
+    g.smem = 0;
+    return g;
+  }
+  static bool attr_set[3] = {false, false, false};
+  int a = algo == CYTOM_ALGO_BFS ? 0 : (algo == CYTOM_ALGO_CC ? 1 : 2);
+  g.fn = a == 0 ? (void*)gather_stream_kernel<0> : a == 1 ? (void*)gather_stream_kernel<1>
+                                                          : (void*)gather_stream_kernel<2>;
+  g.smem = a == 2 ? gather_stream_smem<2>() : gather_stream_smem<0>();
+  if (!attr_set[a]) {
+    cudaFuncSetAttribute(g.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
+    attr_set[a] = true;
+  }
+  g.grid = dim3(grid_persistent(c, 2));
+  g.block = dim3(SG_T);
+  return g;
 }
 
 static int launch_gather(Ctx* c, Job* j, int adaptive) {
-  int g = grid_persistent(c, 8);
-  switch (j->algo) {
-    case CYTOM_ALGO_BFS: gather_minprop_kernel<0><<<g, GATHER_T, 0, c->stream>>>(j->d, c->dsd, adaptive); break;
-    case CYTOM_ALGO_CC: gather_minprop_kernel<1><<<g, GATHER_T, 0, c->stream>>>(j->d, c->dsd, adaptive); break;
-    default: gather_minprop_kernel<2><<<g, GATHER_T, 0, c->stream>>>(j->d, c->dsd, adaptive); break;
-  }
+  GatherLaunch g = gather_launch(c, j->algo);
+  const JobDesc* jd = j->d;
+  const StoreDesc* sd = c->dsd;
+  void* args[] = {(void*)&jd, (void*)&sd, (void*)&adaptive};
+  cudaError_t e = cudaLaunchKernel(g.fn, g.grid, g.block, args, g.smem, c->stream);
   c->launches++;
-  return cuda_err(c, cudaGetLastError(), "gather");
+  return cuda_err(c, e, "gather");
 }
 
 static cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* deps,
-                              size_t ndeps, void* fn, dim3 grid, dim3 block, void** args) {
+                              size_t ndeps, void* fn, dim3 grid, dim3 block, void** args,
+                              size_t smem = 0) {
   cudaKernelNodeParams kp{};
   kp.func = fn;
   kp.gridDim = grid;
   kp.blockDim = block;
-  kp.sharedMemBytes = 0;
+  kp.sharedMemBytes = (unsigned)smem;
   kp.kernelParams = args;
   kp.extra = nullptr;
   return cudaGraphAddKernelNode(node, g, deps, ndeps, &kp);
@@ -415,7 +780,8 @@ static int build_minprop_graph(Ctx* c, Job* j) {
   if (e == cudaSuccess) {
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     void* a_g[] = {(void*)&jd, (void*)&sd, (void*)&adaptive};
-    e = add_kernel(body, &b_gather, nullptr, 0, gather_fn(j->algo), dim3(gper), dim3(GATHER_T), a_g);
+    GatherLaunch gl = gather_launch(c, j->algo);
+    e = add_kernel(body, &b_gather, nullptr, 0, gl.fn, gl.grid, gl.block, a_g, gl.smem);
     void* a_a[] = {(void*)&jd, (void*)&sd, (void*)&zero};
     if (e == cudaSuccess)
       e = add_kernel(body, &b_apply, &b_gather, 1, (void*)apply_minprop_kernel, dim3(gper), dim3(APPLY_T), a_a);

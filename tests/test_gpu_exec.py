@@ -125,3 +125,39 @@ def test_graph_and_host_loop_agree(cg, orc, monkeypatch):
             assert sa[k] == sb[k], k
         ks = eng.kernel_stats()
         assert ks["gather"]["launches"] >= sb["iterations"]
+
+
+@pytest.mark.parametrize("mode", ["simple", "stream"])
+def test_gather_variants_agree(cg, orc, mode, tmp_path):
+    # both gather kernels run in a subprocess with CYTOM_GATHER set, on the same graph
+    import json
+    import os
+    import subprocess
+    import sys
+    code = f"""
+import sys, json, numpy as np
+sys.path.insert(0, {str(tmp_path.parents[0])!r})
+sys.path.insert(0, {str(__import__('pathlib').Path(__file__).resolve().parents[1])!r})
+import cytom_gb300 as cg
+from oracle import oracle as orc
+n = 1 << 16
+s, t = orc.rmat(16, 0, 16 << 16, 21)
+w = orc.edge_weights(s, t, 3)
+st = orc.Store(n, 4096, True); st.insert(s, t, w); st.compact()
+out = {{}}
+with cg.Engine(n, 4096, weight_type=cg.WEIGHT_U32) as eng:
+    eng.insert_edges(s, t, w); eng.do_global_compaction()
+    for name, algo in (("BFS", 0), ("CC", 1), ("SSSP", 2)):
+        p = getattr(cg, name)(eng, start_vertex=0, max_iterations=1000)
+        stt = p.execute_algorithm()
+        ref, info = st.run_minprop(algo, start=0, max_iter=1000)
+        out[name] = [bool(np.array_equal(p.result(), ref)), stt["iterations"] == info["iterations"],
+                     stt["count_edges"] == info["count_edges"]]
+print(json.dumps(out))
+"""
+    env = dict(os.environ, CYTOM_GATHER=mode)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    res = json.loads(r.stdout.strip().splitlines()[-1])
+    for name, checks in res.items():
+        assert all(checks), (mode, name, checks)

@@ -98,8 +98,11 @@ def test_compaction_corner_edge_and_keep_min(cg, orc):
     n, vpt = 1 << 17, 1 << 16
     with cg.Engine(n, vpt, weight_type=cg.WEIGHT_U32) as eng:
         st = orc.Store(n, vpt, True)
+        # tile (0,1): only the local corner edge (65535, 65535) -> dropped
+        # tile (1,0): the corner edge next to another edge -> kept
+        # tile (0,0): (7,9) three times with different weights -> one copy, least weight
         src = np.array([65535, 65535, 65536 + 65535, 65536 + 5, 7, 7, 7], np.uint32)
-        tgt = np.array([65535, 65535, 65535, 65535, 9, 9, 9], np.uint32)
+        tgt = np.array([65536 + 65535, 65536 + 65535, 65535, 65535, 9, 9, 9], np.uint32)
         w = np.array([5, 5, 3, 4, 30, 10, 20], np.uint32)
         eng.insert_edges(src, tgt, w)
         st.insert(src, tgt, w)
@@ -113,8 +116,10 @@ def test_compaction_corner_edge_and_keep_min(cg, orc):
         tp, ed, gw, cf = eng.dump_tiles(weights=True)
         otp, oed, ow, ocf = st.dump()
         assert np.array_equal(tp, otp) and np.array_equal(ed, oed) and np.array_equal(gw, ow)
-        assert tp[1] - tp[0] == 1  # tile (0,0): only (7,9); the corner edge was dropped
-        assert gw[0] == 2
+        assert tp[1] - tp[0] == 1  # tile (0,0): (7,9)
+        assert gw[0] == 2          # lowered by the later copy
+        assert tp[2] - tp[1] == 0  # tile (0,1): the lone corner edge was dropped
+        assert tp[3] - tp[2] == 2  # tile (1,0): both kept
 
 
 def test_insert_rejects_out_of_range_batch(cg):

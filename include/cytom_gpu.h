@@ -196,6 +196,30 @@ int cytom_run_many(cytom_ctx* ctx, const int* job_ids, int count, cytom_run_stat
  * PR_DELTA and PAGERANK ranks as float. `out` holds vertices elements. */
 int cytom_get_result(cytom_ctx* ctx, int job_id, void* out, int where);
 
+/* ---- Allocation-free batch compaction ---------------------------------- */
+
+/* No counterpart in the reference. For callers that cannot allocate device memory
+ * (an application that owns the device heap through its own pool or arena, or a
+ * stream that must not see an allocation): compacts ONE edge batch into the tile
+ * store's form -- sorted by (x, y, src_local, tgt_local), duplicates removed (least
+ * weight kept), exactly the tiles cytom_get_tiles returns after inserting the batch
+ * into an empty store and compacting -- without a context and without allocating.
+ * All pointers are device pointers except edge_count (host). tile_ptr holds
+ * (T*T + 1) entries for T = vertices (rounded up to a power of two) / vertices_per_tile;
+ * edges and weights hold `count` entries (weights only when w is given). count must
+ * not exceed CYTOM_NOALLOC_MAX_EDGES (CYTOM_ERR_INVAL otherwise); an id >= vertices is
+ * CYTOM_ERR_RANGE and leaves the outputs undefined. Scratch lives in one static device
+ * array of CYTOM_NOALLOC_SCRATCH_BYTES per GPU, held until exit and shared by every
+ * call: calls that overlap on the GPU race. The first call on a device looks the
+ * array up (cudaGetSymbolAddress) with that device current; make it before any
+ * stream capture. The call synchronises `stream` before it returns. */
+#define CYTOM_NOALLOC_MAX_EDGES (1u << 18)
+#define CYTOM_NOALLOC_SCRATCH_BYTES ((size_t)9 << 20)
+int cytom_tile_batch_noalloc(const uint32_t* src, const uint32_t* tgt, const uint32_t* w,
+                             uint64_t count, uint64_t vertices, uint64_t vertices_per_tile,
+                             unsigned long long* tile_ptr, uint32_t* edges, uint32_t* weights,
+                             uint64_t* edge_count, void* stream);
+
 /* ---- Instrumentation --------------------------------------------------- */
 
 /* Per-kernel-class timing, recorded with CUDA events around each launch when

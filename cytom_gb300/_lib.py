@@ -109,6 +109,7 @@ SIGNATURES = [
     ("cytom_run", C.c_int, [C.c_void_p, C.c_int, C.POINTER(RunStats)]),
     ("cytom_run_many", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.c_int, C.POINTER(RunStats)]),
     ("cytom_get_result", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
+    ("cytom_get_result_f64", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
     ("cytom_set_profiling", C.c_int, [C.c_void_p, C.c_int]),
     ("cytom_get_kernel_stats", C.c_int, [C.c_void_p, C.POINTER(KernelStats)]),
     ("cytom_reset_kernel_stats", C.c_int, [C.c_void_p]),

@@ -24,6 +24,8 @@ int pagerank_seed(Ctx* c, Job* j, const uint32_t* src, const uint32_t* tgt, cons
                   uint64_t count);
 int pagerank_run(Ctx* c, Job* j);
 int pagerank_result(Ctx* c, Job* j, void* out, int where);
+int pagerank_result64(Ctx* c, Job* j, double* out, int where);
+void pagerank_free(Job* j);
 
 int set_err(Ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg;
@@ -133,6 +135,7 @@ int job_alloc(Ctx* c, Job* j) {
 void job_free(Ctx* c, Job* j) {
   (void)c;
   if (j->loop_exec) cudaGraphExecDestroy(j->loop_exec);
+  if (j->ext) pagerank_free(j);
   void* ptrs[] = {j->h.cur, j->h.next, j->h.fa, j->h.ch, j->h.rows, j->h.rank, j->h.rank_c,
                   j->h.delta, j->h.dsum, j->h.contrib, j->h.rank64, j->h.dsum64, j->h.deg_distinct,
                   j->ls, j->d};
@@ -611,6 +614,13 @@ int cytom_get_result(cytom_ctx* ctx, int job_id, void* out, int where) {
   cudaError_t e = cudaMemcpyAsync(out, j->h.next, c->n * 4, k, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   return cuda_err(c, e, "get_result");
+}
+
+int cytom_get_result_f64(cytom_ctx* ctx, int job_id, double* out, int where) {
+  Ctx* c = (Ctx*)ctx;
+  Job* j = get_job(c, job_id);
+  if (!j || !out) return CYTOM_ERR_INVAL;
+  return pagerank_result64(c, j, out, where);
 }
 
 int cytom_set_profiling(cytom_ctx* ctx, int on) {

@@ -61,6 +61,11 @@ struct LoopState {
   double dangling[2];
   double tol;
   double resid_final;
+  double base_sum;          // PageRank-delta: rank sum at the start of the run
+  double change_sum;        // PageRank-delta: sum of all rank changes of the run
+  double best_resid;        // PageRank FP32: best residual so far (rounding-floor detection)
+  unsigned int stall;       // rounds without a residual improvement
+  unsigned int pad2;
 };
 
 struct JobDesc {
@@ -98,6 +103,7 @@ struct Job {
   cudaGraphExec_t loop_exec = nullptr;
   bool graph_failed = false;
   bool last_run_graph = false;  // the last run went through the graph (launch accounting)
+  void* ext = nullptr;          // per-algorithm state (PageRank family)
 };
 
 struct Ctx {
@@ -117,6 +123,7 @@ struct Ctx {
   uint32_t* chunk_tile = nullptr;
   uint64_t cap = 0, chunk_cap = 0;
   uint64_t E = 0;  // exact after compaction
+  uint64_t version = 0;  // bumped by every compaction that merged edges
   uint64_t *app_keys = nullptr, *app_keys_alt = nullptr;
   uint32_t *app_w = nullptr, *app_w_alt = nullptr;
   uint64_t A = 0, app_cap = 0;

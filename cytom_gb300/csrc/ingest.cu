@@ -785,6 +785,7 @@ int compact(Ctx* c) {
   std::swap(c->tile_ptr, c->tile_ptr_alt);
   c->E += Kn;
   c->A = 0;
+  c->version++;
   uint64_t nch = (c->E + kChunk - 1) / kChunk;
   chunk_tile_kernel<<<grid_for(c, nch + 1, 256), 256, 0, c->stream>>>(c->tile_ptr, c->ntiles, nch,
                                                                      c->chunk_tile);

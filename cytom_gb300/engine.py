@@ -266,6 +266,13 @@ class Program:
         self.engine._check(self.engine.lib.cytom_get_result(self.engine.ctx, self.job, p, where))
         return out
 
+    def result64(self):
+        """FP64 ranks (PageRank run in the FP64 plain form, kahan=False)."""
+        r = np.empty(self.engine.n, np.float64)
+        self.engine._check(self.engine.lib.cytom_get_result_f64(self.engine.ctx, self.job,
+                                                                r.ctypes.data, L.PTR_HOST))
+        return r
+
     def destroy(self):
         self.engine._check(self.engine.lib.cytom_job_destroy(self.engine.ctx, self.job))
 

@@ -195,6 +195,8 @@ int cytom_run_many(cytom_ctx* ctx, const int* job_ids, int count, cytom_run_stat
  * BFS levels / CC labels / SSSP distances as uint32 (UINT32_MAX = unreached),
  * PR_DELTA and PAGERANK ranks as float. `out` holds vertices elements. */
 int cytom_get_result(cytom_ctx* ctx, int job_id, void* out, int where);
+/* FP64 ranks of a PAGERANK job run with kahan = 0 (the FP64 plain form). */
+int cytom_get_result_f64(cytom_ctx* ctx, int job_id, double* out, int where);
 
 /* ---- Allocation-free batch compaction ---------------------------------- */
 

@@ -38,6 +38,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=61)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="cytom", choices=["cytom", "reference"])
+    ap.add_argument("--workload", default="streaming", choices=["streaming", "prdelta", "precision"],
+                    help="streaming: RMAT-22 BFS/CC/SSSP stream (default); prdelta: RMAT-16 PageRank-delta "
+                         "stream; precision: RMAT-26 PageRank FP32-compensated vs FP64")
     ap.add_argument("--scale", type=int, default=22)
     ap.add_argument("--batch", type=int, default=1 << 20)
     ap.add_argument("--vpt", type=int, default=65536)
@@ -46,6 +49,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-steps", type=int, default=4)
+    ap.add_argument("--precision-scale", type=int, default=26)
     ap.add_argument("--programs", default="bfs,cc,sssp",
                     help="vertex programs run after every batch (profiling cases use a subset)")
     ap.add_argument("--preload", type=int, default=0,
@@ -162,6 +166,10 @@ def run_reference(args, rank):
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.workload != "streaming":
+        from bench_workloads import run_workload
+        run_workload(args, rank, world, local)
+        return
     if args.impl == "reference":
         run_reference(args, rank)
         return
@@ -280,18 +288,32 @@ def main():
     eng.set_profiling(False)
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    gbytes = 0.0
     prog_names = args.programs.split(",")
-    for runs in prof_stats:
-        for i, s in runs:
-            wbytes = 4 if prog_names[i] == "sssp" else 0
-            # algorithmic bytes of the gather: packed edge (+ weight) per
-            # scanned edge, one value per active source, atomic read+write per changed
-            # target, the frontier bitmap once per round
-            gbytes += s["edges_scanned"] * (4 + wbytes) + s["active_vertices"] * (4 + 8) \
-                + s["iterations"] * (n / 8)
-    g = ks["gather"]
-    achieved = gbytes / (g["total_ms"] / 1e3) / 1e9 if g["total_ms"] > 0 else None
+    # Executor gather, both round kinds: the library attributes to every gather launch
+    # its algorithmic bytes (scanned edges + weights, one value per active source, a
+    # read and a reduction per changed target, the frontier bitmap or, in a sparse
+    # round, the listed frontier words and their directory entries).
+    def _variant(k):
+        v = ks[k]
+        if not v["launches"] or v["total_ms"] <= 0:
+            return None
+        gbs = v["algo_bytes"] / (v["total_ms"] / 1e3) / 1e9
+        return {"launches": v["launches"], "avg_launch_us": v["total_ms"] * 1e3 / v["launches"],
+                "bytes_per_launch": v["algo_bytes"] / v["launches"], "achieved_gbs": gbs,
+                "frac": gbs / hbm_peak}
+    variants = {"dense_stream": _variant("gather"), "sparse_directory": _variant("gather_sparse")}
+    g_ms = ks["gather"]["total_ms"] + ks["gather_sparse"]["total_ms"]
+    g_launches = ks["gather"]["launches"] + ks["gather_sparse"]["launches"]
+    g_bytes = ks["gather"]["algo_bytes"] + ks["gather_sparse"]["algo_bytes"]
+    achieved = g_bytes / (g_ms / 1e3) / 1e9 if g_ms > 0 else None
+    run_profile = {}
+    for i, name in enumerate(prog_names):
+        runs = [st for r in prof_stats for (k, st) in r if k == i]
+        rounds = sum(st["iterations"] for st in runs)
+        if runs and rounds:
+            run_profile[name] = {"rounds_per_run": rounds / len(runs),
+                                 "active_vertices_per_round": sum(st["active_vertices"] for st in runs) / rounds,
+                                 "edges_scanned_per_round": sum(st["edges_scanned"] for st in runs) / rounds}
     traffic = None
     tfile = ROOT / "profiles" / "gather_traffic.json"
     if tfile.exists():
@@ -364,10 +386,15 @@ def main():
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": (achieved / hbm_peak) if achieved else None, "traffic": traffic,
-                         "kernel": "gather_minprop", "launches": g["launches"],
-                         "avg_launch_us": (g["total_ms"] * 1e3 / g["launches"]) if g["launches"] else None,
+                         "kernel": "executor gather (gather_stream_kernel dense rounds + "
+                                   "gather_sparse_kernel/gather_sparse_chunks sparse rounds)",
+                         "launches": g_launches,
+                         "avg_launch_us": (g_ms * 1e3 / g_launches) if g_launches else None,
+                         "bytes_per_launch": (g_bytes / g_launches) if g_launches else None,
+                         "variants": variants,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
             "kernel_time_ms": {k: v["total_ms"] for k, v in ks.items() if v["launches"]},
+            "run_profile": run_profile,
             "clocks": clk,
             "e2e": e2e,
             "cpu_baseline": cpu,

@@ -41,7 +41,7 @@ int cuda_err(Ctx* c, cudaError_t e, const char* what) {
 
 // ---- profiling: CUDA events around launches --------------------------------
 static const char* kClassNames[CYTOM_KERNEL_CLASSES] = {"rmat", "insert", "sort", "merge",
-                                                        "gather", "apply", "pagerank", "other"};
+                                                        "gather", "apply", "pagerank", "gather_sparse"};
 
 int prof_begin(Ctx* c, int cls) {
   if (!c->profiling) return -1;
@@ -99,6 +99,12 @@ int upload_store_desc(Ctx* c) {
   h.lvpt = c->lvpt;
   h.lT = c->lT;
   h.wtype = c->wtype;
+  h.adaptive = c->cfg.enable_adaptive_scheduling;
+  h.dir = c->dir;
+  h.nbw = c->lvpt >= 5 ? (uint32_t)(c->vpt / 32) : 0u;
+  h.dir_ok = (c->dir && c->spq && c->dir_version == c->version && !c->dir_disabled) ? 1 : 0;
+  h.spq = c->spq;
+  h.spq_cap = c->spq_cap;
   // pageable source: the copy is staged before the call returns, so h may change later
   cudaError_t e = cudaMemcpyAsync(c->dsd, &h, sizeof(StoreDesc), cudaMemcpyHostToDevice, c->stream);
   return cuda_err(c, e, "store descriptor upload");
@@ -136,7 +142,7 @@ void job_free(Ctx* c, Job* j) {
   (void)c;
   if (j->loop_exec) cudaGraphExecDestroy(j->loop_exec);
   if (j->ext) pagerank_free(j);
-  void* ptrs[] = {j->h.cur, j->h.next, j->h.fa, j->h.ch, j->h.rows, j->h.rank, j->h.rank_c,
+  void* ptrs[] = {j->h.aw, j->h.cur, j->h.next, j->h.fa, j->h.ch, j->h.rows, j->h.rank, j->h.rank_c,
                   j->h.delta, j->h.dsum, j->h.contrib, j->h.rank64, j->h.dsum64, j->h.deg_distinct,
                   j->ls, j->d};
   for (void* p : ptrs)
@@ -156,6 +162,10 @@ int job_seed(Ctx* c, Job* j, const uint32_t* src, const uint32_t* tgt, const uin
 int job_run(Ctx* c, Job* j, cytom_run_stats* st) {
   int rc = compact(c);
   if (rc) return rc;
+  if (is_minprop(j->algo)) {
+    rc = build_directory(c);
+    if (rc) return rc;
+  }
   if (j->fresh) {
     rc = job_init_state(c, j);
     if (rc) return rc;
@@ -172,7 +182,7 @@ int job_run(Ctx* c, Job* j, cytom_run_stats* st) {
   rc = prof_flush(c);
   if (rc) return rc;
   if (ls.err) return set_err(c, CYTOM_ERR_TIMEOUT, "a bounded device wait gave up");
-  if (j->last_run_graph) c->launches += 3ULL * ls.iter;
+  if (j->last_run_graph) c->launches += 5ULL * ls.iter;
   if (st) {
     memset(st, 0, sizeof(*st));
     st->iterations = ls.iter;
@@ -323,7 +333,7 @@ int cytom_destroy(cytom_ctx* ctx) {
       job_free(c, j);
       delete j;
     }
-  void* ptrs[] = {c->edges, c->wts, c->edges_alt, c->wts_alt, c->tile_ptr, c->tile_ptr_alt,
+  void* ptrs[] = {c->spq, c->dir, c->edges, c->wts, c->edges_alt, c->wts_alt, c->tile_ptr, c->tile_ptr_alt,
                   c->chunk_tile, c->app_keys, c->app_keys_alt, c->app_w, c->app_w_alt,
                   c->out_deg, c->in_deg, c->dsd, c->scratch, c->d_flag};
   for (void* p : ptrs)

@@ -41,7 +41,14 @@ struct StoreDesc {
   unsigned long long ntiles;
   uint32_t lvpt, lT;           // log2(vertices per tile), log2(T)
   int wtype;
-  int pad;
+  int adaptive;                // adaptive scheduling (skip inactive tile rows)
+  // source directory: dir[t*(nbw+1) + b] = offset, inside tile t = x*T + y, of its
+  // first edge with src_local >= 32*b (b = nbw: the tile size)
+  const uint32_t* dir;
+  uint32_t nbw;                // 32-source blocks per tile row (vpt / 32)
+  int dir_ok;                  // directory current (sparse rounds allowed)
+  uint2* spq;                  // sparse rounds: queue of (item, chunk) of heavy items
+  unsigned long long spq_cap;
 };
 
 // Loop state of one job run, in device memory. Kernels index the double-buffered
@@ -52,6 +59,9 @@ struct LoopState {
   unsigned int cont;       // 1 while the run continues
   unsigned int err;
   unsigned int active[2];  // vertices activated for the next round (by parity)
+  unsigned int nact_words[2];  // non-zero frontier words listed for the next round
+  unsigned int mode;       // gather of the current round: 0 dense (stream), 1 sparse (directory)
+  unsigned int spq_count;  // heavy-item chunks queued in this round
   unsigned long long teps[2];  // edges of newly active tile rows (by parity)
   unsigned long long count_edges;   // reference counting rule, summed
   unsigned long long edges_scanned; // edges this engine read
@@ -74,6 +84,7 @@ struct JobDesc {
   uint32_t* fa;       // frontier (active_current) bitmap, n/32 words
   uint32_t* ch;       // changed bitmap
   uint32_t* rows;     // 2 x T tile-row activity flags (by parity)
+  uint32_t* aw;       // indices of the non-zero frontier words (sparse rounds)
   float* rank;        // PageRank family
   float* rank_c;      // Kahan compensation of rank
   float* delta;
@@ -124,6 +135,12 @@ struct Ctx {
   uint64_t cap = 0, chunk_cap = 0;
   uint64_t E = 0;  // exact after compaction
   uint64_t version = 0;  // bumped by every compaction that merged edges
+  uint32_t* dir = nullptr;  // source directory (sparse rounds)
+  uint2* spq = nullptr;     // heavy-item chunk queue of sparse rounds
+  uint64_t spq_cap = 0;
+  uint64_t dir_entries = 0;
+  uint64_t dir_version = ~0ULL;
+  bool dir_disabled = false;
   uint64_t *app_keys = nullptr, *app_keys_alt = nullptr;
   uint32_t *app_w = nullptr, *app_w_alt = nullptr;
   uint64_t A = 0, app_cap = 0;
@@ -164,6 +181,7 @@ int insert_device(Ctx* c, const uint32_t* src, const uint32_t* tgt, const uint32
                   uint64_t count);
 int compact(Ctx* c);
 int compute_compact_flags(Ctx* c, uint8_t* dflags);
+int build_directory(Ctx* c);
 int ensure_app_capacity(Ctx* c, uint64_t need);
 
 // device-wide utilities

@@ -51,6 +51,9 @@ __global__ void begin_kernel(const JobDesc* __restrict__ jd, const StoreDesc* __
     ls->cont = 1;
     ls->err = 0;
     ls->active[0] = ls->active[1] = 0;
+    ls->nact_words[0] = ls->nact_words[1] = 0;
+    ls->mode = 0;
+    ls->spq_count = 0;
     ls->teps[0] = ls->teps[1] = 0;
     ls->count_edges = 0;
     ls->edges_scanned = 0;
@@ -100,6 +103,16 @@ __global__ void __launch_bounds__(APPLY_T) apply_minprop_kernel(const JobDesc* _
     }
     const unsigned pc = __popc(w);
     cnt += pc;
+    {
+      // warp-ballot compaction of the non-zero frontier words (sparse rounds read the list)
+      const unsigned nz = __ballot_sync(0xFFFFFFFFu, w != 0);
+      if (nz) {
+        unsigned slot0 = 0;
+        if (lane == 0) slot0 = atomicAdd(&ls->nact_words[pw], (unsigned)__popc(nz));
+        slot0 = __shfl_sync(0xFFFFFFFFu, slot0, 0);
+        if (w) jd->aw[slot0 + __popc(nz & ((1u << lane) - 1u))] = (uint32_t)i;
+      }
+    }
     if (lvpt >= 10) {
       // the warp's 32 words (1024 vertices) lie in one tile row
       unsigned tot = pc;
@@ -151,8 +164,8 @@ __global__ void __launch_bounds__(APPLY_T) apply_minprop_kernel(const JobDesc* _
   }
 }
 
-__global__ void control_kernel(const JobDesc* __restrict__ jd, cudaGraphConditionalHandle h,
-                               int initial, int use_handle) {
+__global__ void control_kernel(const JobDesc* __restrict__ jd, const StoreDesc* __restrict__ sd,
+                               cudaGraphConditionalHandle h, int initial, int use_handle) {
   LoopState* ls = jd->ls;
   if (ls->cont) {
     unsigned p;
@@ -165,6 +178,11 @@ __global__ void control_kernel(const JobDesc* __restrict__ jd, cudaGraphConditio
     unsigned a = ls->active[p];
     ls->active_total += a;
     ls->cont = (a > 0 && ls->iter < ls->max_iter && ls->err == 0) ? 1u : 0u;
+    // Next round's gather: sparse (directory, only the listed frontier words) while at
+    // most 1/8 of the frontier words are non-zero, dense (stream every active row) above.
+    const uint64_t nwords = (sd->n + 31) >> 5;
+    ls->mode = (sd->dir_ok && sd->adaptive && (uint64_t)ls->nact_words[p] * 8 <= nwords) ? 1u : 0u;
+    ls->spq_count = 0;
   }
   if (use_handle) cudaGraphSetConditional(h, ls->cont);
 }
@@ -177,7 +195,7 @@ __global__ void __launch_bounds__(GATHER_T) gather_minprop_kernel(const JobDesc*
                                                                   const StoreDesc* __restrict__ sd,
                                                                   int adaptive) {
   LoopState* ls = jd->ls;
-  if (!ls->cont) return;
+  if (!ls->cont || ls->mode != 0) return;
   const unsigned p = ls->iter & 1u;
   const uint64_t T = sd->T;
   const unsigned* __restrict__ rows_cur = jd->rows + p * T;
@@ -188,6 +206,7 @@ __global__ void __launch_bounds__(GATHER_T) gather_minprop_kernel(const JobDesc*
       rows_nxt[i] = 0;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       ls->active[p ^ 1u] = 0;
+      ls->nact_words[p ^ 1u] = 0;
       ls->teps[p ^ 1u] = 0;
       ls->count_edges += adaptive ? ls->teps[p] : sd->E;
     }
@@ -310,7 +329,7 @@ __global__ void __launch_bounds__(SG_T, 2) gather_stream_kernel(const JobDesc* _
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + (size_t)SG_NST * SG_E * 4 * (ALGO == 2 ? 2 : 1));
 
   LoopState* ls = jd->ls;
-  if (!ls->cont) return;
+  if (!ls->cont || ls->mode != 0) return;
   const unsigned p = ls->iter & 1u;
   const uint64_t T = sd->T;
   const unsigned* __restrict__ rows_cur = jd->rows + p * T;
@@ -321,6 +340,7 @@ __global__ void __launch_bounds__(SG_T, 2) gather_stream_kernel(const JobDesc* _
       rows_nxt[i] = 0;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       ls->active[p ^ 1u] = 0;
+      ls->nact_words[p ^ 1u] = 0;
       ls->teps[p ^ 1u] = 0;
       ls->count_edges += adaptive ? ls->teps[p] : sd->E;
     }
@@ -574,6 +594,236 @@ __global__ void __launch_bounds__(SG_T, 2) gather_stream_kernel(const JobDesc* _
   if (threadIdx.x == 0 && scanned) atomicAdd(&ls->edges_scanned, scanned);
 }
 
+// Sparse gather: the round of gather_stream_kernel restricted to the edges of the
+// listed non-zero frontier words. Work item = (frontier word, tile column y); the
+// source directory gives the item's edge range inside tile (x, y), x being the word's
+// tile row. A warp takes 32 consecutive items (consecutive y of one word: coalesced
+// directory loads) and walks the light items' edges with all 32 lanes. Items longer
+// than SP_HEAVY edges, and, when the 32 items of a warp hold more than SP_WARP_MAX
+// edges in total, every item longer than SP_LIGHT, are cut into SP_CHUNK-edge chunks
+// queued for gather_sparse_chunks, so no warp is left with more than about
+// SP_WARP_MAX edges of light items or one chunk per queue entry (RMAT hub blocks).
+constexpr uint32_t SP_HEAVY = 256;
+constexpr uint32_t SP_CHUNK = 256;
+constexpr uint32_t SP_LIGHT = 32;
+constexpr uint32_t SP_WARP_MAX = 2048;
+
+struct SpItem {
+  uint32_t x, y, bits, lo, hi;
+  unsigned long long base;
+};
+
+__device__ __forceinline__ SpItem sp_item(const JobDesc* __restrict__ jd, const StoreDesc* __restrict__ sd,
+                                          uint64_t it) {
+  const uint32_t lT = sd->lT, lnbw = sd->lvpt - 5, nbw = sd->nbw;
+  const uint64_t T = sd->T;
+  SpItem r;
+  const uint32_t w = jd->aw[it >> lT];
+  r.y = (uint32_t)(it & (T - 1));
+  r.x = w >> lnbw;
+  const uint32_t b = w & (nbw - 1);
+  r.bits = __ldg(jd->fa + w);
+  const uint64_t dbase = (((uint64_t)r.x << lT) + r.y) * (nbw + 1) + b;
+  r.lo = sd->dir[dbase];
+  r.hi = sd->dir[dbase + 1];
+  r.base = sd->tile_ptr[((uint64_t)r.x << lT) | r.y];
+  return r;
+}
+
+// Relaxes edge `e` of item `m` when its source is in the item's frontier word.
+// Batched form: the loads of SP_ILP edges are issued before any of them is used.
+constexpr int SP_ILP = 8;
+
+template <int ALGO>
+__device__ __forceinline__ void sp_batch(const JobDesc* __restrict__ jd, const StoreDesc* __restrict__ sd,
+                                         const uint32_t (&xs)[SP_ILP], const uint32_t (&ys)[SP_ILP],
+                                         const uint32_t (&bits)[SP_ILP], const unsigned long long (&pos)[SP_ILP],
+                                         uint32_t valid) {
+  const uint32_t lvpt = sd->lvpt;
+  uint32_t pk[SP_ILP], wv[SP_ILP], cand[SP_ILP], nv[SP_ILP];
+#pragma unroll
+  for (int k = 0; k < SP_ILP; ++k) {
+    pk[k] = ((valid >> k) & 1u) ? sd->edges[pos[k]] : 0u;
+    wv[k] = (ALGO == 2 && ((valid >> k) & 1u)) ? sd->wts[pos[k]] : 0u;
+  }
+#pragma unroll
+  for (int k = 0; k < SP_ILP; ++k) {
+    const uint32_t sl = pk[k] >> 16;
+    const bool act = ((valid >> k) & 1u) && ((bits[k] >> (sl & 31)) & 1u);
+    cand[k] = act ? __ldg(jd->cur + ((xs[k] << lvpt) | sl)) : kInf;
+  }
+#pragma unroll
+  for (int k = 0; k < SP_ILP; ++k) {
+    const uint32_t c = cand[k];
+    if (c == kInf) continue;
+    if (ALGO == 0) {
+      cand[k] = c + 1;
+    } else if (ALGO == 2) {
+      const unsigned long long sum = (unsigned long long)c + wv[k];
+      cand[k] = sum >= kInf ? kInf : (uint32_t)sum;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < SP_ILP; ++k)
+    nv[k] = (cand[k] != kInf) ? __ldcg(jd->next + ((ys[k] << lvpt) | (pk[k] & 0xFFFFu))) : 0u;
+#pragma unroll
+  for (int k = 0; k < SP_ILP; ++k) {
+    if (cand[k] != kInf && cand[k] < nv[k]) {
+      const uint32_t v = (ys[k] << lvpt) | (pk[k] & 0xFFFFu);
+      atomicMin(jd->next + v, cand[k]);
+      atomicOr(jd->ch + (v >> 5), 1u << (v & 31));
+    }
+  }
+}
+
+// The warp relaxes the edges [e0, e1) of one item: SP_ILP edges per lane per step.
+template <int ALGO>
+__device__ __forceinline__ void sp_range(const JobDesc* __restrict__ jd, const StoreDesc* __restrict__ sd,
+                                         const SpItem& m, uint32_t e0, uint32_t e1, unsigned lane) {
+  uint32_t xs[SP_ILP], ys[SP_ILP], bits[SP_ILP];
+#pragma unroll
+  for (int k = 0; k < SP_ILP; ++k) {
+    xs[k] = m.x;
+    ys[k] = m.y;
+    bits[k] = m.bits;
+  }
+  for (uint32_t e = e0 + lane; e < e1; e += 32 * SP_ILP) {
+    unsigned long long pos[SP_ILP];
+    uint32_t valid = 0;
+#pragma unroll
+    for (int k = 0; k < SP_ILP; ++k) {
+      const uint32_t ek = e + 32u * k;
+      pos[k] = m.base + ek;
+      valid |= (ek < e1) ? (1u << k) : 0u;
+    }
+    sp_batch<ALGO>(jd, sd, xs, ys, bits, pos, valid);
+  }
+}
+
+template <int ALGO>
+__global__ void __launch_bounds__(256) gather_sparse_kernel(const JobDesc* __restrict__ jd,
+                                                             const StoreDesc* __restrict__ sd, int adaptive) {
+  LoopState* ls = jd->ls;
+  if (!ls->cont || ls->mode != 1) return;
+  const unsigned p = ls->iter & 1u;
+  const uint64_t T = sd->T;
+  unsigned* rows_nxt = jd->rows + (p ^ 1u) * T;
+  {
+    uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < T; i += stride) rows_nxt[i] = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      ls->active[p ^ 1u] = 0;
+      ls->nact_words[p ^ 1u] = 0;
+      ls->teps[p ^ 1u] = 0;
+      ls->count_edges += adaptive ? ls->teps[p] : sd->E;
+    }
+  }
+  const unsigned lane = threadIdx.x & 31;
+  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint64_t items = (uint64_t)ls->nact_words[p] << sd->lT;
+  const uint64_t qcap = sd->spq_cap;
+  unsigned long long scanned = 0;
+  for (uint64_t g = warp * 32; g < items; g += nwarps * 32) {
+    const uint64_t it = g + lane;
+    SpItem m{};
+    uint32_t len = 0;
+    if (it < items) {
+      m = sp_item(jd, sd, it);
+      len = m.hi > m.lo ? m.hi - m.lo : 0u;
+    }
+    uint32_t tot = len;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xFFFFFFFFu, tot, o);
+    const bool heavy = len > SP_HEAVY || (tot > SP_WARP_MAX && len > SP_LIGHT);
+    bool queued = false;
+    if (heavy) {
+      const uint32_t nch = (len + SP_CHUNK - 1) / SP_CHUNK;
+      const unsigned slot = atomicAdd(&ls->spq_count, nch);
+      if ((uint64_t)slot + nch <= qcap) {
+        for (uint32_t k = 0; k < nch; ++k) sd->spq[slot + k] = make_uint2((uint32_t)it, k);
+        queued = true;
+      }
+    }
+    // light items: the group's edges are numbered 0..total-1 (warp prefix sum over the
+    // items' lengths); lanes take SP_ILP of them per step and find their item by a
+    // binary search over the prefix sums held in the lanes
+    const uint32_t mine = (len > 0 && !queued) ? len : 0u;
+    scanned += mine;
+    uint32_t incl = mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y2 = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+      if (lane >= (unsigned)o) incl += y2;
+    }
+    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    for (uint32_t f0 = 0; f0 < total; f0 += 32 * SP_ILP) {
+      uint32_t xs[SP_ILP], ys[SP_ILP], bits[SP_ILP];
+      unsigned long long pos[SP_ILP];
+      uint32_t valid = 0;
+#pragma unroll
+      for (int k = 0; k < SP_ILP; ++k) {
+        const uint32_t f = f0 + lane + 32u * k;
+        // item j holding flattened edge f: the least j with incl[j] > f
+        uint32_t j = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+          const uint32_t probe = __shfl_sync(0xFFFFFFFFu, incl, j + step - 1);
+          if (probe <= f) j += step;
+        }
+        const uint32_t incl_j = __shfl_sync(0xFFFFFFFFu, incl, j);
+        const uint32_t mine_j = __shfl_sync(0xFFFFFFFFu, mine, j);
+        xs[k] = __shfl_sync(0xFFFFFFFFu, m.x, j);
+        ys[k] = __shfl_sync(0xFFFFFFFFu, m.y, j);
+        bits[k] = __shfl_sync(0xFFFFFFFFu, m.bits, j);
+        const uint32_t lo_j = __shfl_sync(0xFFFFFFFFu, m.lo, j);
+        const unsigned long long base_j = __shfl_sync(0xFFFFFFFFu, m.base, j);
+        pos[k] = base_j + lo_j + (f - (incl_j - mine_j));
+        valid |= (f < total) ? (1u << k) : 0u;
+      }
+      sp_batch<ALGO>(jd, sd, xs, ys, bits, pos, valid);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) scanned += __shfl_xor_sync(0xFFFFFFFFu, scanned, o);
+  if (lane == 0 && scanned) atomicAdd(&ls->edges_scanned, scanned);
+}
+
+// Chunks of heavy items queued by gather_sparse_kernel: one warp per chunk. Sources
+// are sorted inside an item, so a chunk whose first and last edges span no source of
+// the item's frontier word is skipped after two loads.
+template <int ALGO>
+__global__ void __launch_bounds__(256) gather_sparse_chunks(const JobDesc* __restrict__ jd,
+                                                             const StoreDesc* __restrict__ sd) {
+  LoopState* ls = jd->ls;
+  if (!ls->cont || ls->mode != 1) return;
+  const unsigned lane = threadIdx.x & 31;
+  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  uint64_t nq = ls->spq_count;
+  if (nq > sd->spq_cap) nq = sd->spq_cap;
+  const uint64_t items = (uint64_t)ls->nact_words[ls->iter & 1u] << sd->lT;
+  unsigned long long scanned = 0;
+  for (uint64_t q = warp; q < nq; q += nwarps) {
+    const uint2 c = sd->spq[q];
+    if (c.x >= items) continue;  // never indexes outside this round's items
+    const SpItem m = sp_item(jd, sd, c.x);
+    const uint32_t e0 = m.lo + c.y * SP_CHUNK;
+    const uint32_t e1 = min(m.hi, e0 + SP_CHUNK);
+    if (e0 >= e1) continue;
+    uint32_t bound = 0;
+    if (lane == 0) bound = sd->edges[m.base + e0];
+    if (lane == 1) bound = sd->edges[m.base + e1 - 1];
+    const uint32_t s_first = (__shfl_sync(0xFFFFFFFFu, bound, 0) >> 16) & 31u;
+    const uint32_t s_last = (__shfl_sync(0xFFFFFFFFu, bound, 1) >> 16) & 31u;
+    const uint32_t span = (s_last >= 31u ? 0xFFFFFFFFu : ((2u << s_last) - 1u)) & ~((1u << s_first) - 1u);
+    if ((m.bits & span) == 0) continue;
+    if (lane == 0) scanned += e1 - e0;
+    sp_range<ALGO>(jd, sd, m, e0, e1, lane);
+  }
+  if (lane == 0 && scanned) atomicAdd(&ls->edges_scanned, scanned);
+}
+
 // ---- job state -----------------------------------------------------------
 
 __global__ void init_minprop_kernel(const JobDesc* __restrict__ jd, const StoreDesc* __restrict__ sd,
@@ -651,6 +901,7 @@ int minprop_alloc(Ctx* c, Job* j) {
   if (e == cudaSuccess) e = cudaMalloc(&h.fa, nwords * 4);
   if (e == cudaSuccess) e = cudaMalloc(&h.ch, nwords * 4);
   if (e == cudaSuccess) e = cudaMalloc(&h.rows, 2 * c->T * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&h.aw, nwords * 4);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return set_err(c, CYTOM_ERR_OOM, "job state");
@@ -735,6 +986,18 @@ static int launch_gather(Ctx* c, Job* j, int adaptive) {
   return cuda_err(c, e, "gather");
 }
 
+static void* sparse_fn(int algo) {
+  return algo == CYTOM_ALGO_BFS ? (void*)gather_sparse_kernel<0>
+         : algo == CYTOM_ALGO_CC ? (void*)gather_sparse_kernel<1>
+                                 : (void*)gather_sparse_kernel<2>;
+}
+
+static void* chunks_fn(int algo) {
+  return algo == CYTOM_ALGO_BFS ? (void*)gather_sparse_chunks<0>
+         : algo == CYTOM_ALGO_CC ? (void*)gather_sparse_chunks<1>
+                                 : (void*)gather_sparse_chunks<2>;
+}
+
 static cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* deps,
                               size_t ndeps, void* fn, dim3 grid, dim3 block, void** args,
                               size_t smem = 0) {
@@ -761,14 +1024,14 @@ static int build_minprop_graph(Ctx* c, Job* j) {
   int adaptive = c->cfg.enable_adaptive_scheduling;
   int zero = 0, one = 1;
   int gper = grid_persistent(c, 8);
-  cudaGraphNode_t n_begin, n_apply0, n_ctl0, n_while, b_gather, b_apply, b_ctl;
+  cudaGraphNode_t n_begin, n_apply0, n_ctl0, n_while, b_gather, b_sparse, b_chunks, b_apply, b_ctl;
   void* a_begin[] = {(void*)&jd, (void*)&sd, (void*)&max_iter};
   if (e == cudaSuccess)
     e = add_kernel(g, &n_begin, nullptr, 0, (void*)begin_kernel, dim3(std::max(1, c->num_sms)), dim3(256), a_begin);
   void* a_apply0[] = {(void*)&jd, (void*)&sd, (void*)&one};
   if (e == cudaSuccess)
     e = add_kernel(g, &n_apply0, &n_begin, 1, (void*)apply_minprop_kernel, dim3(gper), dim3(APPLY_T), a_apply0);
-  void* a_ctl0[] = {(void*)&jd, (void*)&h, (void*)&one, (void*)&one};
+  void* a_ctl0[] = {(void*)&jd, (void*)&sd, (void*)&h, (void*)&one, (void*)&one};
   if (e == cudaSuccess)
     e = add_kernel(g, &n_ctl0, &n_apply0, 1, (void*)control_kernel, dim3(1), dim3(1), a_ctl0);
   cudaGraphNodeParams cp{};
@@ -782,10 +1045,16 @@ static int build_minprop_graph(Ctx* c, Job* j) {
     void* a_g[] = {(void*)&jd, (void*)&sd, (void*)&adaptive};
     GatherLaunch gl = gather_launch(c, j->algo);
     e = add_kernel(body, &b_gather, nullptr, 0, gl.fn, gl.grid, gl.block, a_g, gl.smem);
+    // the round's other gather exits at once: dense and sparse are picked on the device
+    if (e == cudaSuccess)
+      e = add_kernel(body, &b_sparse, &b_gather, 1, sparse_fn(j->algo), dim3(gper), dim3(256), a_g);
+    void* a_q[] = {(void*)&jd, (void*)&sd};
+    if (e == cudaSuccess)
+      e = add_kernel(body, &b_chunks, &b_sparse, 1, chunks_fn(j->algo), dim3(gper), dim3(256), a_q);
     void* a_a[] = {(void*)&jd, (void*)&sd, (void*)&zero};
     if (e == cudaSuccess)
-      e = add_kernel(body, &b_apply, &b_gather, 1, (void*)apply_minprop_kernel, dim3(gper), dim3(APPLY_T), a_a);
-    void* a_c[] = {(void*)&jd, (void*)&h, (void*)&zero, (void*)&one};
+      e = add_kernel(body, &b_apply, &b_chunks, 1, (void*)apply_minprop_kernel, dim3(gper), dim3(APPLY_T), a_a);
+    void* a_c[] = {(void*)&jd, (void*)&sd, (void*)&h, (void*)&zero, (void*)&one};
     if (e == cudaSuccess)
       e = add_kernel(body, &b_ctl, &b_apply, 1, (void*)control_kernel, dim3(1), dim3(1), a_c);
   }
@@ -809,6 +1078,22 @@ static bool use_graphs() {
   return v == 1;
 }
 
+// Algorithmic bytes of one gather round, from the loop state before (`a`) and after
+// (`b`) it: every scanned edge (+ its weight), one value per active source, a read and a
+// reduction per changed target (bounded by the vertices the round activates), and the
+// frontier: the whole bitmap for a dense round; for a sparse round the listed words
+// (index + word) and per (word, tile column) item its two directory entries and tile offset.
+static double round_bytes(const Ctx* c, const LoopState& a, const LoopState& b, double wbytes) {
+  const unsigned p = a.iter & 1u;
+  const double scanned = (double)(b.edges_scanned - a.edges_scanned);
+  const double act = (double)a.active[p];
+  const double changed = (double)b.active[p ^ 1u];
+  double bytes = scanned * (4.0 + wbytes) + act * 4.0 + changed * 8.0;
+  if (a.mode == 0) bytes += (double)c->n / 8.0;
+  else bytes += (double)a.nact_words[p] * (8.0 + 16.0 * (double)c->T);
+  return bytes;
+}
+
 int minprop_run(Ctx* c, Job* j) {
   int adaptive = c->cfg.enable_adaptive_scheduling;
   unsigned max_iter = (unsigned)std::min<uint64_t>(j->params.max_iterations, 0xFFFFFFFFu);
@@ -827,28 +1112,76 @@ int minprop_run(Ctx* c, Job* j) {
   int gper = grid_persistent(c, 8);
   begin_kernel<<<std::max(1, c->num_sms), 256, 0, c->stream>>>(j->d, c->dsd, max_iter);
   apply_minprop_kernel<<<gper, APPLY_T, 0, c->stream>>>(j->d, c->dsd, 1);
-  control_kernel<<<1, 1, 0, c->stream>>>(j->d, 0, 1, 0);
+  control_kernel<<<1, 1, 0, c->stream>>>(j->d, c->dsd, 0, 1, 0);
   c->launches += 3;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_err(c, e, "run prologue");
+  const JobDesc* jd = j->d;
+  const StoreDesc* sd = c->dsd;
+  void* a_g[] = {(void*)&jd, (void*)&sd, (void*)&adaptive};
+  // profiling: the gather slot of the previous round and its loop-state snapshot; the
+  // round's algorithmic bytes are known once the next snapshot is read
+  int prev_slot = -1;
+  LoopState prev{};
+  const double wbytes = j->algo == CYTOM_ALGO_SSSP ? 4.0 : 0.0;
   for (uint64_t round = 0; round < max_iter;) {
-    // launch a few rounds before checking: kernels are no-ops once the run ended
-    int batch = 4;
-    for (int k = 0; k < batch && round < max_iter; ++k, ++round) {
-      int s1 = prof_begin(c, KC_GATHER);
-      int rc = launch_gather(c, j, adaptive);
-      if (rc) return rc;
-      prof_end(c, s1, -1.0);
+    if (c->profiling) {
+      // one round at a time, only the gather the device chose, so per-launch times are clean
+      LoopState snap;
+      e = cudaMemcpyAsync(&snap, j->ls, sizeof(LoopState), cudaMemcpyDeviceToHost, c->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+      if (e != cudaSuccess) return cuda_err(c, e, "run loop");
+      if (prev_slot >= 0) c->pending[prev_slot].bytes = round_bytes(c, prev, snap, wbytes);
+      prev_slot = -1;
+      if (!snap.cont) break;
+      prev = snap;
+      if (snap.mode == 0) {
+        int s1 = prof_begin(c, KC_GATHER);
+        int rc = launch_gather(c, j, adaptive);
+        if (rc) return rc;
+        prof_end(c, s1, 0.0);
+        prev_slot = s1;
+      } else {
+        int s1 = prof_begin(c, KC_OTHER);
+        e = cudaLaunchKernel(sparse_fn(j->algo), dim3(gper), dim3(256), a_g, 0, c->stream);
+        void* a_q[] = {(void*)&jd, (void*)&sd};
+        if (e == cudaSuccess) e = cudaLaunchKernel(chunks_fn(j->algo), dim3(gper), dim3(256), a_q, 0, c->stream);
+        c->launches += 2;
+        prof_end(c, s1, 0.0);
+        prev_slot = s1;
+        if (e != cudaSuccess) return cuda_err(c, e, "sparse gather");
+      }
       int s2 = prof_begin(c, KC_APPLY);
       apply_minprop_kernel<<<gper, APPLY_T, 0, c->stream>>>(j->d, c->dsd, 0);
       prof_end(c, s2, -1.0);
-      control_kernel<<<1, 1, 0, c->stream>>>(j->d, 0, 0, 0);
+      control_kernel<<<1, 1, 0, c->stream>>>(j->d, c->dsd, 0, 0, 0);
       c->launches += 2;
+      ++round;
+      continue;
+    }
+    // launch a few rounds before checking: kernels are no-ops once the run ended
+    for (int k = 0; k < 4 && round < max_iter; ++k, ++round) {
+      int rc = launch_gather(c, j, adaptive);
+      if (rc) return rc;
+      e = cudaLaunchKernel(sparse_fn(j->algo), dim3(gper), dim3(256), a_g, 0, c->stream);
+      void* a_q[] = {(void*)&jd, (void*)&sd};
+      if (e == cudaSuccess) e = cudaLaunchKernel(chunks_fn(j->algo), dim3(gper), dim3(256), a_q, 0, c->stream);
+      if (e != cudaSuccess) return cuda_err(c, e, "sparse gather");
+      apply_minprop_kernel<<<gper, APPLY_T, 0, c->stream>>>(j->d, c->dsd, 0);
+      control_kernel<<<1, 1, 0, c->stream>>>(j->d, c->dsd, 0, 0, 0);
+      c->launches += 4;
     }
     e = cudaMemcpyAsync(c->h_pinned, &j->ls->cont, 4, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_err(c, e, "run loop");
     if (*(unsigned*)c->h_pinned == 0) break;
+  }
+  if (prev_slot >= 0) {
+    LoopState snap;
+    e = cudaMemcpyAsync(&snap, j->ls, sizeof(LoopState), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "run loop");
+    c->pending[prev_slot].bytes = round_bytes(c, prev, snap, wbytes);
   }
   return CYTOM_OK;
 }

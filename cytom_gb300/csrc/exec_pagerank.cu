@@ -369,15 +369,34 @@ __global__ void __launch_bounds__(PR_T) pr_pull_small(PrArgs a) {
       const uint32_t v = a.bins[a.bin_off + i];
       const uint32_t lo = a.csc_ptr[v], hi = a.csc_ptr[v + 1];
       double sum;
+      // four independent gathers in flight, accumulated in edge order
       if constexpr (MODE == PR_NORM64) {
         Acc64 acc;
         acc.init();
-        for (uint32_t e = lo; e < hi; ++e) acc.add(a.contrib64[a.csc_src[e]]);
+        uint32_t e = lo;
+        for (; e + 4 <= hi; e += 4) {
+          const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + 1], s2 = a.csc_src[e + 2], s3 = a.csc_src[e + 3];
+          const double c0 = a.contrib64[s0], c1 = a.contrib64[s1], c2 = a.contrib64[s2], c3 = a.contrib64[s3];
+          acc.add(c0);
+          acc.add(c1);
+          acc.add(c2);
+          acc.add(c3);
+        }
+        for (; e < hi; ++e) acc.add(a.contrib64[a.csc_src[e]]);
         sum = acc.value();
       } else {
         Acc32 acc;
         acc.init();
-        for (uint32_t e = lo; e < hi; ++e) acc.add(a.contrib[a.csc_src[e]]);
+        uint32_t e = lo;
+        for (; e + 4 <= hi; e += 4) {
+          const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + 1], s2 = a.csc_src[e + 2], s3 = a.csc_src[e + 3];
+          const float c0 = a.contrib[s0], c1 = a.contrib[s1], c2 = a.contrib[s2], c3 = a.contrib[s3];
+          acc.add(c0);
+          acc.add(c1);
+          acc.add(c2);
+          acc.add(c3);
+        }
+        for (; e < hi; ++e) acc.add(a.contrib[a.csc_src[e]]);
         sum = (double)acc.s + (double)acc.e;
       }
       resid += pr_finish<MODE>(a, v, sum, p, dang, &rsum);
@@ -403,14 +422,32 @@ __global__ void __launch_bounds__(PR_T) pr_pull_medium(PrArgs a) {
     double sum;
     if constexpr (MODE == PR_NORM64) {
       double s = 0.0;
-      for (uint32_t e = lo + lane; e < hi; e += 32) s += a.contrib64[a.csc_src[e]];
+      uint32_t e = lo + lane;
+      for (; e + 96 < hi; e += 128) {
+        const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + 32], s2 = a.csc_src[e + 64], s3 = a.csc_src[e + 96];
+        const double c0 = a.contrib64[s0], c1 = a.contrib64[s1], c2 = a.contrib64[s2], c3 = a.contrib64[s3];
+        s += c0;
+        s += c1;
+        s += c2;
+        s += c3;
+      }
+      for (; e < hi; e += 32) s += a.contrib64[a.csc_src[e]];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
       sum = s;
     } else {
       Acc32 acc;
       acc.init();
-      for (uint32_t e = lo + lane; e < hi; e += 32) acc.add(a.contrib[a.csc_src[e]]);
+      uint32_t e = lo + lane;
+      for (; e + 96 < hi; e += 128) {
+        const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + 32], s2 = a.csc_src[e + 64], s3 = a.csc_src[e + 96];
+        const float c0 = a.contrib[s0], c1 = a.contrib[s1], c2 = a.contrib[s2], c3 = a.contrib[s3];
+        acc.add(c0);
+        acc.add(c1);
+        acc.add(c2);
+        acc.add(c3);
+      }
+      for (; e < hi; e += 32) acc.add(a.contrib[a.csc_src[e]]);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         const float s2 = __shfl_xor_sync(0xFFFFFFFFu, acc.s, o);
@@ -441,7 +478,17 @@ __global__ void __launch_bounds__(PR_BLOCK_T) pr_pull_large(PrArgs a) {
     double sum = 0.0;
     if constexpr (MODE == PR_NORM64) {
       double s = 0.0;
-      for (uint32_t e = lo + threadIdx.x; e < hi; e += PR_BLOCK_T) s += a.contrib64[a.csc_src[e]];
+      uint32_t e = lo + threadIdx.x;
+      for (; e + 3 * PR_BLOCK_T < hi; e += 4 * PR_BLOCK_T) {
+        const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + PR_BLOCK_T], s2 = a.csc_src[e + 2 * PR_BLOCK_T],
+                       s3 = a.csc_src[e + 3 * PR_BLOCK_T];
+        const double c0 = a.contrib64[s0], c1 = a.contrib64[s1], c2 = a.contrib64[s2], c3 = a.contrib64[s3];
+        s += c0;
+        s += c1;
+        s += c2;
+        s += c3;
+      }
+      for (; e < hi; e += PR_BLOCK_T) s += a.contrib64[a.csc_src[e]];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
       if (lane == 0) s_d[wid] = s;
@@ -452,7 +499,17 @@ __global__ void __launch_bounds__(PR_BLOCK_T) pr_pull_large(PrArgs a) {
     } else {
       Acc32 acc;
       acc.init();
-      for (uint32_t e = lo + threadIdx.x; e < hi; e += PR_BLOCK_T) acc.add(a.contrib[a.csc_src[e]]);
+      uint32_t e = lo + threadIdx.x;
+      for (; e + 3 * PR_BLOCK_T < hi; e += 4 * PR_BLOCK_T) {
+        const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + PR_BLOCK_T], s2 = a.csc_src[e + 2 * PR_BLOCK_T],
+                       s3 = a.csc_src[e + 3 * PR_BLOCK_T];
+        const float c0 = a.contrib[s0], c1 = a.contrib[s1], c2 = a.contrib[s2], c3 = a.contrib[s3];
+        acc.add(c0);
+        acc.add(c1);
+        acc.add(c2);
+        acc.add(c3);
+      }
+      for (; e < hi; e += PR_BLOCK_T) acc.add(a.contrib[a.csc_src[e]]);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         const float s2 = __shfl_xor_sync(0xFFFFFFFFu, acc.s, o);

@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 
 #include "engine.h"
 
@@ -815,6 +816,106 @@ __global__ void count_sources_kernel(const uint32_t* __restrict__ edges,
     for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xFFFFFFFFu, cnt, o);
     if (lane == 0) flags[t] = (hi > lo) ? (uint8_t)(cnt >= vpt / 2 ? 1 : 0) : 2;  // 2 = empty
   }
+}
+
+// Source directory for sparse rounds. Per edge: the 32-source blocks from just after
+// the previous edge's block up to its own start at this edge. Per tile: the blocks after
+// the last edge's block (all blocks of an empty tile) hold the tile size.
+__global__ void dir_edges_kernel(const StoreDesc* __restrict__ sd, uint32_t* __restrict__ dir, uint32_t nbw) {
+  // one warp per 128-edge chunk: one tile lookup per chunk, four edges per lane
+  const uint64_t E = sd->E, nchunks = sd->nchunks;
+  const unsigned lane = threadIdx.x & 31;
+  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t c = warp; c < nchunks; c += nwarps) {
+    const uint64_t e0 = c * kChunk + (uint64_t)lane * 4;
+    if (e0 >= E) continue;
+    const uint4 q = *reinterpret_cast<const uint4*>(sd->edges + e0);
+    const uint32_t prev0 = e0 > 0 ? sd->edges[e0 - 1] : 0u;
+    const uint32_t ev[5] = {prev0, q.x, q.y, q.z, q.w};
+    uint32_t t = sd->chunk_tile[c];
+    unsigned long long tlo = sd->tile_ptr[t], thi = sd->tile_ptr[t + 1];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const uint64_t e = e0 + k;
+      if (e >= E) break;
+      while (thi <= e) {
+        ++t;
+        tlo = thi;
+        thi = sd->tile_ptr[t + 1];
+      }
+      const int b = (int)((ev[k + 1] >> 16) >> 5);
+      const int bprev = (e == tlo) ? -1 : (int)((ev[k] >> 16) >> 5);
+      if (b == bprev) continue;
+      uint32_t* dt = dir + (uint64_t)t * (nbw + 1);
+      for (int bb = bprev + 1; bb <= b; ++bb) dt[bb] = (uint32_t)(e - tlo);
+    }
+  }
+}
+
+__global__ void dir_tiles_kernel(const StoreDesc* __restrict__ sd, uint32_t* __restrict__ dir, uint32_t nbw) {
+  const uint64_t ntiles = sd->ntiles;
+  const unsigned lane = threadIdx.x & 31;
+  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t t = warp; t < ntiles; t += nwarps) {
+    const uint64_t lo = sd->tile_ptr[t], hi = sd->tile_ptr[t + 1];
+    const int blast = (hi > lo) ? (int)((sd->edges[hi - 1] >> 16) >> 5) : -1;
+    uint32_t* dt = dir + t * (nbw + 1);
+    for (int bb = blast + 1 + (int)lane; bb <= (int)nbw; bb += 32) dt[bb] = (uint32_t)(hi - lo);
+  }
+}
+
+int build_directory(Ctx* c) {
+  if (c->dir_version == c->version || c->dir_disabled) return CYTOM_OK;
+  const char* env = getenv("CYTOM_SPARSE");  // "0": dense rounds only
+  if (c->lvpt < 5 || !c->cfg.enable_adaptive_scheduling || (env && env[0] == '0')) {
+    c->dir_disabled = true;
+    return upload_store_desc(c);
+  }
+  const uint64_t nbw = c->vpt / 32;
+  const uint64_t entries = c->T * (nbw + 1) * c->T;
+  // the directory is worth its memory only while it is small next to the edges
+  if (entries * 4 > (4ULL << 30)) {
+    c->dir_disabled = true;
+    return upload_store_desc(c);
+  }
+  if (!c->dir) {
+    if (cudaMalloc(&c->dir, entries * 4) != cudaSuccess) {
+      cudaGetLastError();
+      c->dir_disabled = true;
+      return upload_store_desc(c);
+    }
+    c->dir_entries = entries;
+  }
+  // chunk queue of sparse rounds: queued items are longer than 32 edges (at most E / 32
+  // of them) and give one chunk per 256 edges, so E / 32 + E / 256 entries always fit
+  const uint64_t need = c->E / 32 + c->E / 256 + 1024;
+  if (need > c->spq_cap) {
+    cudaFree(c->spq);
+    c->spq = nullptr;
+    const uint64_t cap = need + need / 2;
+    if (cudaMalloc(&c->spq, cap * sizeof(uint2)) != cudaSuccess) {
+      cudaGetLastError();
+      c->spq_cap = 0;
+      c->dir_disabled = true;
+      return upload_store_desc(c);
+    }
+    c->spq_cap = cap;
+    cudaMemsetAsync(c->spq, 0, cap * sizeof(uint2), c->stream);
+  }
+  int slot = prof_begin(c, KC_MERGE);
+  if (c->E) {
+    dir_edges_kernel<<<grid_for(c, (c->E + 3) / 4, 256), 256, 0, c->stream>>>(c->dsd, c->dir, (uint32_t)nbw);
+    c->launches++;
+  }
+  dir_tiles_kernel<<<grid_for(c, c->ntiles * 32, 256), 256, 0, c->stream>>>(c->dsd, c->dir, (uint32_t)nbw);
+  c->launches++;
+  prof_end(c, slot, (double)c->E * 8.0 + (double)entries * 4.0);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_err(c, e, "directory");
+  c->dir_version = c->version;
+  return upload_store_desc(c);
 }
 
 int compute_compact_flags(Ctx* c, uint8_t* dflags) {

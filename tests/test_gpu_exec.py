@@ -124,7 +124,7 @@ def test_graph_and_host_loop_agree(cg, orc, monkeypatch):
         for k in ("iterations", "count_edges", "edges_scanned", "active_vertices"):
             assert sa[k] == sb[k], k
         ks = eng.kernel_stats()
-        assert ks["gather"]["launches"] >= sb["iterations"]
+        assert ks["gather"]["launches"] + ks["gather_sparse"]["launches"] == sb["iterations"]
 
 
 @pytest.mark.parametrize("mode", ["simple", "stream"])
@@ -161,3 +161,44 @@ print(json.dumps(out))
     res = json.loads(r.stdout.strip().splitlines()[-1])
     for name, checks in res.items():
         assert all(checks), (mode, name, checks)
+
+
+@pytest.mark.parametrize("sparse", ["0", "1"])
+def test_sparse_and_dense_rounds_agree(cg, orc, sparse, tmp_path):
+    # incremental runs on a growing graph, with sparse (directory) rounds allowed or not
+    import json
+    import os
+    import subprocess
+    import sys
+    code = f"""
+import sys, json, numpy as np
+sys.path.insert(0, {str(__import__('pathlib').Path(__file__).resolve().parents[1])!r})
+import cytom_gb300 as cg
+from oracle import oracle as orc
+scale, vpt = 17, 8192
+n = 1 << scale
+ok = []
+with cg.Engine(n, vpt, weight_type=cg.WEIGHT_U32) as eng:
+    progs = [cg.BFS(eng, start_vertex=0, max_iterations=1000), cg.CC(eng, max_iterations=1000),
+             cg.SSSP(eng, start_vertex=0, max_iterations=1000)]
+    st = orc.Store(n, vpt, True)
+    for b in range(6):
+        s, t = orc.rmat(scale, b * 200000, 200000, 3)
+        w = orc.edge_weights(s, t, 8)
+        eng.insert_edges(s, t, w); st.insert(s, t, w); st.compact()
+        for prog, algo in zip(progs, (0, 1, 2)):
+            stt = prog.execute_algorithm()
+            ref, info = st.run_minprop(algo, start=0, max_iter=1000)
+            ok.append(bool(np.array_equal(prog.result(), ref)) and stt["converged"] == 1)
+    fresh = cg.SSSP(eng, start_vertex=0, max_iterations=1000)
+    stt = fresh.execute_algorithm()
+    ref, info = st.run_minprop(2, start=0, max_iter=1000)
+    ok.append(bool(np.array_equal(fresh.result(), ref)) and stt["iterations"] == info["iterations"]
+              and stt["count_edges"] == info["count_edges"])
+print(json.dumps(ok))
+"""
+    env = dict(os.environ, CYTOM_SPARSE=sparse)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=900)
+    assert r.returncode == 0, r.stderr[-2000:]
+    ok = json.loads(r.stdout.strip().splitlines()[-1])
+    assert all(ok), (sparse, ok)

@@ -1,4 +1,4 @@
-"""Secondary benchmark workloads of bench.py (--workload prdelta | precision).
+"""Secondary benchmark workloads of bench.py (--workload prdelta | precision | batching).
 
 prdelta: RMAT scale 16 (65,536 vertices, 1,048,576 edges, graph500 a,b,c, seed 1,
     duplicates and self-loops kept) streamed in 16 batches of 65,536 edges in
@@ -144,6 +144,122 @@ def run_precision(args, rank, world, local):
                                 "e2e": None, "cpu_baseline": None})), flush=True)
 
 
+def run_batching(args, rank, world, local):
+    """64 jobs over 8 snapshots (RMAT scales 14..21, edge factor 16, seeds 10..17, uint32
+    weights uniform in [1, 255]): 16 each of BFS (sources 0, 1), CC, SSSP (sources 0, 1)
+    and PageRank (FP32 compensated, FP64 L1 tolerance 1e-8), 8 per snapshot. A job round
+    runs every job; the first round computes from scratch, then each snapshot receives
+    4 further insert batches of 5% of its edges with a job round after each. The batched
+    arm runs each job round as ONE persistent launch (cytom_run_batch); the plain arm
+    runs each job by itself (cytom_run: one CUDA-graph launch per BFS/CC/SSSP run, a
+    host-driven round loop per PageRank run). Inserts and compactions are untimed and
+    identical in both arms; a job round is timed from the first call to the readback of
+    the last job's statistics. BFS/CC/SSSP results of the two arms are compared bit for
+    bit after every round."""
+    import torch
+    import cytom_gb300 as cg
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    scales, seeds, rounds = list(range(14, 22)), list(range(10, 18)), 4
+    gen = cg.Engine(1 << 14, 4096, weight_type=cg.WEIGHT_U32, stream=stream.cuda_stream)
+    inputs = []
+    for scale, seed in zip(scales, seeds):
+        m = 16 << scale
+        b = m // 20
+        total = m + rounds * b
+        t3 = [torch.empty(total, dtype=torch.int32, device=dev) for _ in range(3)]
+        gen.generate_rmat(0, total, scale, seed=seed, weight_seed=seed + 1000, wmin=1, wmax=255, out=tuple(t3))
+        inputs.append((scale, m, b, t3))
+    gen.close()
+
+    def make_arm():
+        engs, progs = [], []
+        for scale, m, b, (s, t, w) in inputs:
+            n = 1 << scale
+            e = cg.Engine(n, min(65536, n >> 2), weight_type=cg.WEIGHT_U32, stream=stream.cuda_stream)
+            e.insert_edges_device(s.data_ptr(), t.data_ptr(), w.data_ptr(), m)
+            e.do_global_compaction()
+            engs.append(e)
+            progs += [cg.BFS(e, start_vertex=0, max_iterations=100), cg.BFS(e, start_vertex=1, max_iterations=100),
+                      cg.CC(e, max_iterations=100), cg.CC(e, max_iterations=100),
+                      cg.SSSP(e, start_vertex=0, max_iterations=100), cg.SSSP(e, start_vertex=1, max_iterations=100),
+                      cg.PageRank(e, max_iterations=100, tolerance=1e-8, kahan=True),
+                      cg.PageRank(e, max_iterations=100, tolerance=1e-8, kahan=True)]
+        return engs, progs
+
+    def insert_round(engs, r):
+        for e, (scale, m, b, (s, t, w)) in zip(engs, inputs):
+            off = 4 * (m + r * b)
+            e.insert_edges_device(s.data_ptr() + off, t.data_ptr() + off, w.data_ptr() + off, b)
+            e.do_global_compaction()
+
+    per_kind = [0.0] * 8  # plain arm: wall time by job slot of a snapshot
+
+    def run_arm(batched, check_against=None):
+        engs, progs = make_arm()
+        for k in range(8):
+            per_kind[k] = 0.0
+        torch.cuda.synchronize()
+        times, results, stats_all = [], [], []
+        for r in range(rounds + 1):
+            if r:
+                insert_round(engs, r - 1)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if batched:
+                st = cg.run_batch(progs)
+            else:
+                st = []
+                for k, p in enumerate(progs):
+                    t1 = time.perf_counter()
+                    st.append(p.execute_algorithm())
+                    per_kind[k % 8] += time.perf_counter() - t1
+            times.append(time.perf_counter() - t0)
+            stats_all.append(st)
+            results.append([p.result() for p in progs if not isinstance(p, cg.PageRank)])
+        launches = sum(e.launch_count() for e in engs)
+        for e in engs:
+            e.close()
+        return times, results, stats_all, launches
+
+    # warm-up pass of each arm (allocations, graph builds), then the timed passes
+    for _ in range(max(1, min(args.warmup, 1))):
+        run_arm(False)
+        run_arm(True)
+    tp, rp, sp, lp = run_arm(False)
+    plain_kind = list(per_kind)
+    tb, rb, sb, lb = run_arm(True)
+    exact = all(np.array_equal(x, y) for ra, rb_ in zip(rp, rb) for x, y in zip(ra, rb_))
+    njobs = len(sb[0])
+    minprop = [k for k in range(njobs) if k % 8 < 6]  # BFS, CC, SSSP jobs of each snapshot
+    counts_equal = all(sa[k]["iterations"] == sb_[k]["iterations"] and sa[k]["count_edges"] == sb_[k]["count_edges"]
+                       for sa, sb_ in zip(sp, sb) for k in minprop)
+    jobs_b = njobs * (rounds + 1) / sum(tb)
+    jobs_p = njobs * (rounds + 1) / sum(tp)
+    edges_b = sum(x["count_edges"] for st in sb for x in st)
+    if rank == 0:
+        line = _line(args, world, jobs_b, 1e3 * sum(tb) / (rounds + 1),
+                     {"workload": "batching: 64 jobs (16 each of BFS, CC, SSSP, PageRank) over 8 RMAT snapshots "
+                                  "(scales 14..21, edge factor 16, seeds 10..17), 4 rounds of +5% inserts",
+                      "jobs": njobs, "job_rounds": rounds + 1, "snapshot_scales": scales,
+                      "vertices_per_tile": "min(65536, vertices / 4)"},
+                     {"unit": "jobs/s", "dtype": "u32 (BFS/CC/SSSP), f32 (PageRank)",
+                      "batched_jobs_per_s": jobs_b, "plain_jobs_per_s": jobs_p,
+                      "batched_over_plain": jobs_b / jobs_p,
+                      "round_ms_batched": [1e3 * x for x in tb], "round_ms_plain": [1e3 * x for x in tp],
+                      "integer_results_bit_exact": bool(exact), "rounds_and_counts_equal": bool(counts_equal),
+                      "batched_gteps": edges_b / sum(tb) / 1e9,
+                      "batched_device_ms_per_round": [st[0]["elapsed_ms"] for st in sb],
+                      "pagerank_rounds_per_run": [[st[k]["iterations"] for k in range(njobs) if k % 8 == 6] for st in sb],
+                      "plain_ms_by_job_kind": dict(zip(["bfs0", "bfs1", "cc", "cc2", "sssp0", "sssp1", "pr", "pr2"],
+                                                       [1e3 * x for x in plain_kind])),
+                      "gpu_launches_batched_pass": lb, "gpu_launches_plain_pass": lp,
+                      "e2e": None, "cpu_baseline": None})
+        line["unit"] = "jobs/s"
+        print(json.dumps(line), flush=True)
+
+
 def run_workload(args, rank, world, local):
     if args.impl == "reference":
         if rank == 0:
@@ -152,5 +268,7 @@ def run_workload(args, rank, world, local):
         return
     if args.workload == "prdelta":
         run_prdelta(args, rank, world, local)
+    elif args.workload == "batching":
+        run_batching(args, rank, world, local)
     else:
         run_precision(args, rank, world, local)

@@ -108,6 +108,8 @@ SIGNATURES = [
     ("cytom_job_reset", C.c_int, [C.c_void_p, C.c_int]),
     ("cytom_run", C.c_int, [C.c_void_p, C.c_int, C.POINTER(RunStats)]),
     ("cytom_run_many", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.c_int, C.POINTER(RunStats)]),
+    ("cytom_run_batch", C.c_int, [C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.c_int, C.POINTER(RunStats)]),
+    ("cytom_batch_units", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
     ("cytom_get_result", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
     ("cytom_get_result_f64", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
     ("cytom_set_profiling", C.c_int, [C.c_void_p, C.c_int]),

@@ -102,9 +102,7 @@ int upload_store_desc(Ctx* c) {
   h.adaptive = c->cfg.enable_adaptive_scheduling;
   h.dir = c->dir;
   h.nbw = c->lvpt >= 5 ? (uint32_t)(c->vpt / 32) : 0u;
-  h.dir_ok = (c->dir && c->spq && c->dir_version == c->version && !c->dir_disabled) ? 1 : 0;
-  h.spq = c->spq;
-  h.spq_cap = c->spq_cap;
+  h.dir_ok = (c->dir && c->dir_version == c->version && !c->dir_disabled) ? 1 : 0;
   // pageable source: the copy is staged before the call returns, so h may change later
   cudaError_t e = cudaMemcpyAsync(c->dsd, &h, sizeof(StoreDesc), cudaMemcpyHostToDevice, c->stream);
   return cuda_err(c, e, "store descriptor upload");
@@ -142,11 +140,34 @@ void job_free(Ctx* c, Job* j) {
   (void)c;
   if (j->loop_exec) cudaGraphExecDestroy(j->loop_exec);
   if (j->ext) pagerank_free(j);
-  void* ptrs[] = {j->h.aw, j->h.cur, j->h.next, j->h.fa, j->h.ch, j->h.rows, j->h.rank, j->h.rank_c,
+  void* ptrs[] = {j->h.spq, j->h.aw, j->h.cur, j->h.next, j->h.fa, j->h.ch, j->h.rows, j->h.rank, j->h.rank_c,
                   j->h.delta, j->h.dsum, j->h.contrib, j->h.rank64, j->h.dsum64, j->h.deg_distinct,
                   j->ls, j->d};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+}
+
+// Chunk queue of a job's sparse rounds: queued items are longer than 32 edges (at most
+// E / 32 of them) and give one chunk per 256 edges, so E / 32 + E / 256 entries always
+// fit. Without a queue (allocation failed) heavy items are walked as light ones.
+int ensure_job_queue(Ctx* c, Job* j) {
+  const uint64_t need = c->E / 32 + c->E / 256 + 1024;
+  if (need <= j->h.spq_cap) return CYTOM_OK;
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "queue resize");
+  if (j->h.spq) cudaFree(j->h.spq);
+  j->h.spq = nullptr;
+  j->h.spq_cap = 0;
+  const uint64_t cap = need + need / 2;
+  if (cudaMalloc(&j->h.spq, cap * sizeof(uint2)) == cudaSuccess) {
+    j->h.spq_cap = cap;
+  } else {
+    cudaGetLastError();
+    j->h.spq = nullptr;
+  }
+  // pageable source: the copy is staged before the call returns
+  e = cudaMemcpyAsync(j->d, &j->h, sizeof(JobDesc), cudaMemcpyHostToDevice, c->stream);
+  return cuda_err(c, e, "job descriptor upload");
 }
 
 int job_init_state(Ctx* c, Job* j) {
@@ -164,6 +185,7 @@ int job_run(Ctx* c, Job* j, cytom_run_stats* st) {
   if (rc) return rc;
   if (is_minprop(j->algo)) {
     rc = build_directory(c);
+    if (!rc) rc = ensure_job_queue(c, j);
     if (rc) return rc;
   }
   if (j->fresh) {
@@ -333,7 +355,9 @@ int cytom_destroy(cytom_ctx* ctx) {
       job_free(c, j);
       delete j;
     }
-  void* ptrs[] = {c->spq, c->dir, c->edges, c->wts, c->edges_alt, c->wts_alt, c->tile_ptr, c->tile_ptr_alt,
+  batch_free(c);
+  pagerank_ctx_free(c);
+  void* ptrs[] = {c->dir, c->edges, c->wts, c->edges_alt, c->wts_alt, c->tile_ptr, c->tile_ptr_alt,
                   c->chunk_tile, c->app_keys, c->app_keys_alt, c->app_w, c->app_w_alt,
                   c->out_deg, c->in_deg, c->dsd, c->scratch, c->d_flag};
   for (void* p : ptrs)

@@ -47,8 +47,6 @@ struct StoreDesc {
   const uint32_t* dir;
   uint32_t nbw;                // 32-source blocks per tile row (vpt / 32)
   int dir_ok;                  // directory current (sparse rounds allowed)
-  uint2* spq;                  // sparse rounds: queue of (item, chunk) of heavy items
-  unsigned long long spq_cap;
 };
 
 // Loop state of one job run, in device memory. Kernels index the double-buffered
@@ -85,6 +83,8 @@ struct JobDesc {
   uint32_t* ch;       // changed bitmap
   uint32_t* rows;     // 2 x T tile-row activity flags (by parity)
   uint32_t* aw;       // indices of the non-zero frontier words (sparse rounds)
+  uint2* spq;         // sparse rounds: queue of (item, chunk) of heavy items
+  unsigned long long spq_cap;
   float* rank;        // PageRank family
   float* rank_c;      // Kahan compensation of rank
   float* delta;
@@ -136,8 +136,6 @@ struct Ctx {
   uint64_t E = 0;  // exact after compaction
   uint64_t version = 0;  // bumped by every compaction that merged edges
   uint32_t* dir = nullptr;  // source directory (sparse rounds)
-  uint2* spq = nullptr;     // heavy-item chunk queue of sparse rounds
-  uint64_t spq_cap = 0;
   uint64_t dir_entries = 0;
   uint64_t dir_version = ~0ULL;
   bool dir_disabled = false;
@@ -163,6 +161,11 @@ struct Ctx {
   std::vector<cudaEvent_t> ev_pool;
   cytom_kernel_stats kstats{};
   cudaEvent_t run_a = nullptr, run_b = nullptr;
+  // batched executor: device tables kept by the first context of a batch
+  void* batch = nullptr;
+  uint64_t batch_units = 0;
+  // PageRank family: the snapshot's CSC, shared by the context's PageRank jobs
+  void* pr_csc = nullptr;
 };
 
 // ---- helpers (capi.cu) ----
@@ -197,5 +200,8 @@ int job_seed(Ctx* c, Job* j, const uint32_t* src, const uint32_t* tgt, const uin
              uint64_t count);
 int job_run(Ctx* c, Job* j, cytom_run_stats* st);
 int job_result(Ctx* c, Job* j, void* out, int where);
+int ensure_job_queue(Ctx* c, Job* j);
+void batch_free(Ctx* c);
+void pagerank_ctx_free(Ctx* c);
 
 }  // namespace cytom

@@ -1,0 +1,609 @@
+// exec_batch.cu — batched persistent executor: many jobs (BFS, CC, SSSP, PageRank,
+// PageRank-delta) over one or more graph snapshots run together in ONE kernel launch.
+//
+// The reference runs every job as its own ContinuousAlgorithmExecutor on its own
+// threads (src/include/core/jobs.h:79-83, src/include/main/execute.h:534-771); a job's
+// rounds are separated by barriers (continuous-algorithm-executor.h:49-249). Here the
+// jobs share the GPU inside one persistent kernel:
+//  - every job has a work queue for its current phase: the 4096-edge stages (dense
+//    round) or 256-item groups and 256-edge chunks (sparse round) of a gather, the
+//    1024-word ranges of an apply, the 4096-vertex ranges of a PageRank contribution
+//    pass and the target bins of its pull;
+//  - a block claims a unit of any job with one 64-bit atomic on that job's claim word
+//    [phase : 8][units : 24][next unit : 32], so the phase and its size travel with the
+//    claim;
+//  - the block that completes the last unit of a phase (a per-phase completion
+//    counter) runs the job's control step — the same device code as the one-job
+//    executors (minprop_dev.cuh, pagerank_dev.cuh) — and publishes the next phase;
+//  - no block ever waits on another block: a block that finds no unit polls the claim
+//    words again (bounded: after kIdleLimit empty polls in a row it records a timeout
+//    and exits, so the launch always ends).
+// Values written during the launch are read through L2 (the PERSIST load policy).
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <vector>
+
+#include "engine.h"
+#include "minprop_dev.cuh"
+#include "pagerank_dev.cuh"
+
+namespace cytom {
+
+int minprop_batch_prep(Ctx* c, Job* j);
+int pagerank_batch_prep(Ctx* c, Job* j, PrArgs* out, uint64_t nb[3], int* first_mode);
+
+constexpr int BT = 256;  // threads of a batch block (every unit kind is written for 256)
+static_assert(BT == APPLY_T && BT == SG_T && BT == PR_BLOCK_T, "one block shape for every unit");
+
+enum BatchPhase : unsigned {
+  PH_NONE = 0,
+  PH_APPLY0 = 1,     // seeding apply of a BFS / CC / SSSP run
+  PH_DENSE = 2,      // dense gather: one 4096-edge stage per unit
+  PH_SPARSE = 3,     // sparse gather: 256 items per unit
+  PH_CHUNKS = 4,     // sparse chunk pass: 8 queued chunks per unit
+  PH_APPLY = 5,      // apply: 1024 frontier words per unit
+  PH_PR_CONTRIB = 6, // PageRank contributions: 4096 sources per unit
+  PH_PR_PULL = 7,    // PageRank pull: 1024 small, 32 medium or 1 large target per unit
+  PH_DONE = 8
+};
+constexpr uint32_t BU_APPLY_WORDS = 1024;
+constexpr uint32_t BU_SPARSE_ITEMS = 256;
+constexpr uint32_t BU_CHUNKS = BT / 32;
+constexpr uint32_t BU_PR_VERTS = 4096;
+constexpr uint32_t BU_PR_SMALL = 1024;
+constexpr uint32_t BU_PR_MEDIUM = 32;
+constexpr uint32_t kMaxUnits = (1u << 24) - 1;
+constexpr uint32_t kIdleLimit = 1u << 22;
+
+struct BJob {
+  const JobDesc* jd;
+  const StoreDesc* sd;
+  PrArgs pr;
+  unsigned long long nb0, nb1, nb2;  // PageRank target bins
+  int algo;
+  int adaptive;
+};
+
+struct __align__(128) BSched {
+  unsigned long long claim;  // [phase:8][units:24][next:32]
+  unsigned done;             // units of the current phase completed
+  int prmode;                // PageRank: mode of the current round
+};
+
+struct BCtl {
+  unsigned jobs_left;
+  unsigned err;
+  unsigned long long units;  // units processed (statistics)
+};
+
+__host__ __device__ constexpr unsigned long long pack_claim(unsigned phase, unsigned total) {
+  return ((unsigned long long)phase << 56) | ((unsigned long long)(total & 0xFFFFFFu) << 32);
+}
+
+__device__ __forceinline__ uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
+
+// Block-wide sums of two doubles onto thread 0.
+__device__ __forceinline__ void block_sum2(double& a, double& b) {
+  __shared__ double s_a[BT / 32], s_b[BT / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xFFFFFFFFu, a, o);
+    b += __shfl_xor_sync(0xFFFFFFFFu, b, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    s_a[threadIdx.x >> 5] = a;
+    s_b[threadIdx.x >> 5] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    a = 0.0;
+    b = 0.0;
+    for (int k = 0; k < BT / 32; ++k) {
+      a += s_a[k];
+      b += s_b[k];
+    }
+  }
+  __syncthreads();
+}
+
+// ---- units -----------------------------------------------------------------
+
+__device__ __forceinline__ unsigned ls_iter(const LoopState* ls) { return *(const volatile unsigned*)&ls->iter; }
+
+__device__ void unit_apply(const BJob* J, bool initial, uint32_t unit) {
+  const JobDesc* jd = J->jd;
+  const StoreDesc* sd = J->sd;
+  const unsigned pw = initial ? 0u : ((ls_iter(jd->ls) & 1u) ^ 1u);
+  const uint64_t nwords = (sd->n + 31) >> 5;
+  unsigned cnt = 0;
+  unsigned long long teps = 0;
+  const uint64_t base0 = (uint64_t)unit * BU_APPLY_WORDS;
+  for (uint32_t k = 0; k < BU_APPLY_WORDS / BT; ++k) {
+    const uint64_t base = base0 + (uint64_t)k * BT;
+    if (base < nwords) apply_step<true>(jd, sd, pw, base, cnt, teps);
+  }
+  apply_flush(jd->ls, pw, cnt, teps);
+}
+
+template <int ALGO>
+__device__ void unit_dense(const BJob* J, uint32_t st) {
+  const JobDesc* jd = J->jd;
+  const StoreDesc* sd = J->sd;
+  const unsigned p = ls_iter(jd->ls) & 1u;
+  if (!stage_active<true>(jd, sd, st, p, J->adaptive)) return;
+  const uint64_t e0 = (uint64_t)st * SG_E;
+  dense_stage<ALGO, true, true>(jd, sd, sd->edges + e0, ALGO == 2 ? sd->wts + e0 : nullptr, st, p, J->adaptive);
+  if (threadIdx.x == 0) {
+    const uint64_t rem = sd->E - e0;
+    atomicAdd(&jd->ls->edges_scanned, (unsigned long long)(rem < (uint64_t)SG_E ? rem : (uint64_t)SG_E));
+  }
+}
+
+template <int ALGO>
+__device__ void unit_sparse(const BJob* J, uint32_t unit) {
+  const JobDesc* jd = J->jd;
+  const StoreDesc* sd = J->sd;
+  const unsigned p = ls_iter(jd->ls) & 1u;
+  const uint64_t items = (uint64_t)__ldcg(&jd->ls->nact_words[p]) << sd->lT;
+  const uint64_t g = (uint64_t)unit * BU_SPARSE_ITEMS + (threadIdx.x >> 5) * 32;
+  unsigned long long scanned = 0;
+  if (g < items) scanned = sparse_group<ALGO, true>(jd, sd, g, items);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) scanned += __shfl_xor_sync(0xFFFFFFFFu, scanned, o);
+  if ((threadIdx.x & 31) == 0 && scanned) atomicAdd(&jd->ls->edges_scanned, scanned);
+}
+
+template <int ALGO>
+__device__ void unit_chunks(const BJob* J, uint32_t unit) {
+  const JobDesc* jd = J->jd;
+  const StoreDesc* sd = J->sd;
+  const unsigned p = ls_iter(jd->ls) & 1u;
+  const uint64_t items = (uint64_t)__ldcg(&jd->ls->nact_words[p]) << sd->lT;
+  uint64_t nq = __ldcg(&jd->ls->spq_count);
+  if (nq > jd->spq_cap) nq = jd->spq_cap;
+  const uint64_t q = (uint64_t)unit * BU_CHUNKS + (threadIdx.x >> 5);
+  uint32_t scanned = 0;
+  if (q < nq) scanned = sparse_chunk<ALGO, true>(jd, sd, q, items);
+  if ((threadIdx.x & 31) == 0 && scanned) atomicAdd(&jd->ls->edges_scanned, (unsigned long long)scanned);
+}
+
+template <int MODE>
+__device__ void unit_pr_contrib(const BJob* J, uint32_t unit) {
+  const PrArgs& a = J->pr;
+  const unsigned p = ls_iter(a.ls) & 1u;
+  const uint64_t lo = (uint64_t)unit * BU_PR_VERTS;
+  const uint64_t hi = std::min<uint64_t>(lo + BU_PR_VERTS, a.n);
+  const uint64_t wlo = lo >> 5, whi = std::min<uint64_t>((hi + 31) >> 5, a.nwords);
+  const double dangling = pr_contrib_range<MODE, true>(a, p, lo, hi, wlo, whi, threadIdx.x, BT);
+  pr_dangling_flush<MODE>(a.ls, p, dangling);
+}
+
+template <int MODE>
+__device__ void unit_pr_pull(const BJob* J, uint32_t unit) {
+  const PrArgs& a = J->pr;
+  LoopState* ls = a.ls;
+  const unsigned p = ls_iter(ls) & 1u;
+  const double dang = (MODE == PR_NORM32 || MODE == PR_NORM64) ? __ldcg(&ls->dangling[p]) / (double)a.n : 0.0;
+  const uint32_t ns = ceil_div(J->nb0, BU_PR_SMALL), nm = ceil_div(J->nb1, BU_PR_MEDIUM);
+  double resid = 0.0, rsum = 0.0;
+  if (unit < ns) {
+#pragma unroll 1
+    for (uint32_t k = 0; k < BU_PR_SMALL / BT; ++k) {
+      const uint64_t i = (uint64_t)unit * BU_PR_SMALL + k * BT + threadIdx.x;
+      if (i < J->nb0) {
+        const uint32_t v = a.bins[i];
+        const double sum = pr_sum_thread<MODE, true>(a, v);
+        resid += pr_finish<MODE, true>(a, v, sum, p, dang, &rsum);
+      }
+    }
+  } else if (unit < ns + nm) {
+    const unsigned lane = threadIdx.x & 31;
+#pragma unroll 1
+    for (uint32_t k = 0; k < BU_PR_MEDIUM / (BT / 32); ++k) {
+      const uint64_t i = (uint64_t)(unit - ns) * BU_PR_MEDIUM + k * (BT / 32) + (threadIdx.x >> 5);
+      if (i < J->nb1) {
+        const uint32_t v = a.bins[J->nb0 + i];
+        const double sum = pr_sum_warp<MODE, true>(a, v, lane);
+        if (lane == 0) resid += pr_finish<MODE, true>(a, v, sum, p, dang, &rsum);
+      }
+    }
+  } else {
+    const uint64_t i = (uint64_t)(unit - ns - nm);
+    const uint32_t v = a.bins[J->nb0 + J->nb1 + i];
+    const double sum = pr_sum_block<MODE, true>(a, v);
+    if (threadIdx.x == 0) resid += pr_finish<MODE, true>(a, v, sum, p, dang, &rsum);
+  }
+  block_sum2(resid, rsum);
+  if (threadIdx.x == 0) {
+    if (resid != 0.0) atomicAdd(&ls->resid[p], resid);
+    if (rsum != 0.0) atomicAdd(&ls->rank_sum[p], rsum);
+  }
+}
+
+__device__ __forceinline__ uint32_t pr_pull_units(const BJob* J) {
+  return ceil_div(J->nb0, BU_PR_SMALL) + ceil_div(J->nb1, BU_PR_MEDIUM) + (uint32_t)J->nb2;
+}
+
+// ---- phase transitions (whole block, after the last unit of `phase`) --------
+
+__device__ void advance(const BJob* J, BSched* S, BCtl* ctl, unsigned phase) {
+  __shared__ unsigned s_next, s_total, s_cont;
+  __shared__ int s_mode;
+  const JobDesc* jd = J->jd;
+  const StoreDesc* sd = J->sd;
+  const bool pr = J->algo == CYTOM_ALGO_PR_DELTA || J->algo == CYTOM_ALGO_PAGERANK;
+  if (threadIdx.x == 0) {
+    s_mode = *(volatile int*)&S->prmode;
+    s_next = PH_DONE;
+    s_total = 0;
+    s_cont = 1;
+    if (pr) {
+      if (phase == PH_PR_CONTRIB) {
+        s_next = PH_PR_PULL;
+        s_total = pr_pull_units(J);
+      } else {
+        s_cont = pr_control_step(J->pr.ls, s_mode);
+        if (s_cont) {
+          if (s_mode == PR_DELTA_RESIDUAL) s_mode = PR_DELTA_PUSH;
+          s_next = PH_PR_CONTRIB;
+          s_total = ceil_div(J->pr.n, BU_PR_VERTS);
+        }
+      }
+    } else if (phase == PH_DENSE || phase == PH_CHUNKS) {
+      s_next = PH_APPLY;
+    } else if (phase == PH_SPARSE) {
+      uint64_t nq = __ldcg(&jd->ls->spq_count);
+      if (nq > jd->spq_cap) nq = jd->spq_cap;
+      s_next = nq ? PH_CHUNKS : PH_APPLY;
+      s_total = nq ? ceil_div(nq, BU_CHUNKS) : 0;
+    } else {
+      s_cont = control_step(jd, sd, phase == PH_APPLY0 ? 1 : 0);
+    }
+  }
+  __syncthreads();
+  if (!pr && (phase == PH_APPLY0 || phase == PH_APPLY) && s_cont) {
+    // open the next round (all threads clear the row flags), then pick its gather
+    const unsigned p = ls_iter(jd->ls) & 1u;
+    round_open<true>(jd, sd, p, J->adaptive, threadIdx.x, BT);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const unsigned mode = *(volatile unsigned*)&jd->ls->mode;
+      if (mode == 0) {
+        s_next = PH_DENSE;
+        s_total = ceil_div(sd->E, SG_E);
+      } else {
+        s_next = PH_SPARSE;
+        s_total = ceil_div((uint64_t)__ldcg(&jd->ls->nact_words[p]) << sd->lT, BU_SPARSE_ITEMS);
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    unsigned next = s_next, total = s_total;
+    // an empty gather phase goes straight to the apply
+    if (!pr && (next == PH_DENSE || next == PH_SPARSE || next == PH_CHUNKS) && total == 0) next = PH_APPLY;
+    if (next == PH_APPLY) total = ceil_div((sd->n + 31) >> 5, BU_APPLY_WORDS);
+    if (total > kMaxUnits) {
+      atomicExch(&ctl->err, 2u);
+      next = PH_DONE;
+    }
+    if (!s_cont || next == PH_DONE) {
+      __threadfence();
+      atomicExch(&S->claim, pack_claim(PH_DONE, 0));
+      atomicSub(&ctl->jobs_left, 1u);
+    } else {
+      S->done = 0;
+      S->prmode = s_mode;
+      __threadfence();
+      atomicExch(&S->claim, pack_claim(next, total));
+    }
+  }
+  __syncthreads();
+}
+
+__device__ void run_unit(const BJob* J, unsigned phase, uint32_t unit, int prmode) {
+  const int algo = J->algo;
+  switch (phase) {
+    case PH_APPLY0:
+    case PH_APPLY:
+      unit_apply(J, phase == PH_APPLY0, unit);
+      break;
+    case PH_DENSE:
+      if (algo == CYTOM_ALGO_BFS) unit_dense<0>(J, unit);
+      else if (algo == CYTOM_ALGO_CC) unit_dense<1>(J, unit);
+      else unit_dense<2>(J, unit);
+      break;
+    case PH_SPARSE:
+      if (algo == CYTOM_ALGO_BFS) unit_sparse<0>(J, unit);
+      else if (algo == CYTOM_ALGO_CC) unit_sparse<1>(J, unit);
+      else unit_sparse<2>(J, unit);
+      break;
+    case PH_CHUNKS:
+      if (algo == CYTOM_ALGO_BFS) unit_chunks<0>(J, unit);
+      else if (algo == CYTOM_ALGO_CC) unit_chunks<1>(J, unit);
+      else unit_chunks<2>(J, unit);
+      break;
+    case PH_PR_CONTRIB:
+      if (prmode == PR_DELTA_RESIDUAL) unit_pr_contrib<PR_DELTA_RESIDUAL>(J, unit);
+      else if (prmode == PR_DELTA_PUSH) unit_pr_contrib<PR_DELTA_PUSH>(J, unit);
+      else if (prmode == PR_NORM32) unit_pr_contrib<PR_NORM32>(J, unit);
+      else unit_pr_contrib<PR_NORM64>(J, unit);
+      break;
+    case PH_PR_PULL:
+      if (prmode == PR_DELTA_RESIDUAL) unit_pr_pull<PR_DELTA_RESIDUAL>(J, unit);
+      else if (prmode == PR_DELTA_PUSH) unit_pr_pull<PR_DELTA_PUSH>(J, unit);
+      else if (prmode == PR_NORM32) unit_pr_pull<PR_NORM32>(J, unit);
+      else unit_pr_pull<PR_NORM64>(J, unit);
+      break;
+    default:
+      break;
+  }
+}
+
+__global__ void __launch_bounds__(BT, 2) batch_kernel(const BJob* __restrict__ jobs, BSched* sched, BCtl* ctl,
+                                                        int njobs) {
+  __shared__ int s_job, s_state, s_last, s_mode;
+  __shared__ unsigned s_unit, s_total, s_phase;
+  int cursor = (int)(blockIdx.x % (unsigned)njobs);
+  unsigned idle = 0;
+  unsigned long long done_units = 0;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      int found = -1;
+      unsigned unit = 0, total = 0, phase = 0;
+      for (int k = 0; k < njobs && found < 0; ++k) {
+        int jj = cursor + k;
+        if (jj >= njobs) jj -= njobs;
+        const unsigned long long cw = *(volatile unsigned long long*)&sched[jj].claim;
+        if ((unsigned)cw >= ((unsigned)(cw >> 32) & 0xFFFFFFu)) continue;
+        const unsigned long long old = atomicAdd(&sched[jj].claim, 1ULL);
+        const unsigned tot = (unsigned)(old >> 32) & 0xFFFFFFu;
+        if ((unsigned)old < tot) {
+          found = jj;
+          unit = (unsigned)old;
+          total = tot;
+          phase = (unsigned)(old >> 56);
+        }
+      }
+      int state = 0;
+      if (found >= 0) {
+        __threadfence();  // the phase's state was published before the claim word
+        s_mode = *(volatile int*)&sched[found].prmode;
+        idle = 0;
+      } else if (*(volatile unsigned*)&ctl->jobs_left == 0 || *(volatile unsigned*)&ctl->err != 0) {
+        state = 2;
+      } else if (++idle > kIdleLimit) {
+        atomicExch(&ctl->err, 1u);
+        state = 2;
+      } else {
+        state = 1;
+        __nanosleep(200);
+      }
+      s_job = found;
+      s_unit = unit;
+      s_total = total;
+      s_phase = phase;
+      s_state = state;
+    }
+    __syncthreads();
+    const int state = s_state;
+    if (state == 2) break;
+    if (state == 1) {
+      __syncthreads();
+      continue;
+    }
+    const int jb = s_job;
+    const BJob* J = jobs + jb;
+    run_unit(J, s_phase, s_unit, s_mode);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      const unsigned d = atomicAdd(&sched[jb].done, 1u);
+      s_last = (d + 1 == s_total) ? 1 : 0;
+      ++done_units;
+    }
+    __syncthreads();
+    if (s_last) {
+      __threadfence();
+      advance(J, sched + jb, ctl, s_phase);
+    }
+    cursor = jb;
+  }
+  if (threadIdx.x == 0 && done_units) atomicAdd(&ctl->units, done_units);
+}
+
+// ---- host ---------------------------------------------------------------------
+
+static bool is_pr(int algo) { return algo == CYTOM_ALGO_PR_DELTA || algo == CYTOM_ALGO_PAGERANK; }
+
+struct BatchBuffers {
+  int device = -1;
+  BJob* jobs = nullptr;
+  BSched* sched = nullptr;
+  BCtl* ctl = nullptr;
+  int cap = 0;
+  cudaEvent_t a = nullptr, b = nullptr;
+};
+
+static int batch_run(Ctx* const* ctxs, const int* job_ids, int count, cytom_run_stats* stats) {
+  Ctx* c0 = ctxs[0];
+  std::vector<Job*> jobs(count);
+  std::vector<Ctx*> uniq;
+  for (int k = 0; k < count; ++k) {
+    Ctx* c = ctxs[k];
+    if (!c) return CYTOM_ERR_INVAL;
+    if (c->device != c0->device) return set_err(c0, CYTOM_ERR_INVAL, "batched jobs must share one device");
+    if (job_ids[k] < 0 || job_ids[k] >= (int)c->jobs.size() || !c->jobs[job_ids[k]])
+      return set_err(c0, CYTOM_ERR_INVAL, "unknown job in batch");
+    jobs[k] = c->jobs[job_ids[k]];
+    for (int m = 0; m < k; ++m)
+      if (ctxs[m] == c && job_ids[m] == job_ids[k]) return set_err(c0, CYTOM_ERR_INVAL, "job listed twice in batch");
+    if (std::find(uniq.begin(), uniq.end(), c) == uniq.end()) uniq.push_back(c);
+  }
+  // per snapshot: merge pending edges, refresh the source directory
+  for (Ctx* c : uniq) {
+    int rc = compact(c);
+    if (!rc) rc = build_directory(c);
+    if (rc) {
+      if (c != c0) c0->err = c->err;
+      return rc;
+    }
+  }
+  std::vector<BJob> hj(count);
+  std::vector<BSched> hs(count);
+  for (int k = 0; k < count; ++k) {
+    Ctx* c = ctxs[k];
+    Job* j = jobs[k];
+    int rc = CYTOM_OK;
+    if (j->fresh) {
+      rc = job_init_state(c, j);
+      if (rc) return rc;
+      j->fresh = false;
+    }
+    BJob b{};
+    b.jd = j->d;
+    b.sd = c->dsd;
+    b.algo = j->algo;
+    b.adaptive = c->cfg.enable_adaptive_scheduling;
+    memset(&hs[k], 0, sizeof(BSched));
+    if (is_pr(j->algo)) {
+      uint64_t nb[3];
+      int mode = 0;
+      rc = pagerank_batch_prep(c, j, &b.pr, nb, &mode);
+      if (rc) return rc;
+      b.nb0 = nb[0];
+      b.nb1 = nb[1];
+      b.nb2 = nb[2];
+      hs[k].prmode = mode;
+      const uint64_t units = (c->n + BU_PR_VERTS - 1) / BU_PR_VERTS;
+      if (units > kMaxUnits) return set_err(c, CYTOM_ERR_RANGE, "graph too large for the batched executor");
+      hs[k].claim = (j->params.max_iterations > 0) ? pack_claim(PH_PR_CONTRIB, (unsigned)units)
+                                                   : pack_claim(PH_DONE, 0);
+    } else {
+      rc = minprop_batch_prep(c, j);
+      if (rc) return rc;
+      const uint64_t units = (((c->n + 31) >> 5) + BU_APPLY_WORDS - 1) / BU_APPLY_WORDS;
+      const uint64_t stages = (c->E + SG_E - 1) / SG_E;
+      if (units > kMaxUnits || stages > kMaxUnits)
+        return set_err(c, CYTOM_ERR_RANGE, "graph too large for the batched executor");
+      hs[k].claim = pack_claim(PH_APPLY0, (unsigned)units);
+    }
+    hj[k] = b;
+  }
+  unsigned left = 0;
+  for (int k = 0; k < count; ++k)
+    if ((unsigned)(hs[k].claim >> 56) != PH_DONE) ++left;
+  // prep work of every snapshot's stream is done before the launch
+  for (Ctx* c : uniq) {
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(c0, e, "batch prep");
+  }
+  // device tables, kept by the first context and grown on demand
+  BatchBuffers*& bb = reinterpret_cast<BatchBuffers*&>(c0->batch);
+  if (!bb) {
+    bb = new (std::nothrow) BatchBuffers();
+    if (!bb) return set_err(c0, CYTOM_ERR_OOM, "batch buffers");
+    cudaEventCreate(&bb->a);
+    cudaEventCreate(&bb->b);
+  }
+  if (bb->cap < count) {
+    cudaFree(bb->jobs);
+    cudaFree(bb->sched);
+    bb->jobs = nullptr;
+    bb->sched = nullptr;
+    bb->cap = 0;
+    if (cudaMalloc(&bb->jobs, sizeof(BJob) * count) != cudaSuccess ||
+        cudaMalloc(&bb->sched, sizeof(BSched) * count) != cudaSuccess) {
+      cudaGetLastError();
+      return set_err(c0, CYTOM_ERR_OOM, "batch tables");
+    }
+    bb->cap = count;
+  }
+  if (!bb->ctl && cudaMalloc(&bb->ctl, sizeof(BCtl)) != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(c0, CYTOM_ERR_OOM, "batch control");
+  }
+  BCtl hctl{};
+  hctl.jobs_left = left;
+  cudaStream_t st = c0->stream;
+  cudaError_t e = cudaMemcpyAsync(bb->jobs, hj.data(), sizeof(BJob) * count, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(bb->sched, hs.data(), sizeof(BSched) * count, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(bb->ctl, &hctl, sizeof(BCtl), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_err(c0, e, "batch upload");
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, BT, 0);
+  per_sm = std::max(1, std::min(per_sm, 2));
+  const int grid = c0->num_sms * per_sm;
+  cudaEventRecord(bb->a, st);
+  if (left) {
+    batch_kernel<<<grid, BT, 0, st>>>(bb->jobs, bb->sched, bb->ctl, count);
+    c0->launches++;
+  }
+  cudaEventRecord(bb->b, st);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&hctl, bb->ctl, sizeof(BCtl), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_err(c0, e, "batch run");
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, bb->a, bb->b);
+  c0->batch_units += hctl.units;
+  if (hctl.err == 1) return set_err(c0, CYTOM_ERR_TIMEOUT, "batched executor: a block found no work for too long");
+  if (hctl.err) return set_err(c0, CYTOM_ERR_RANGE, "batched executor: a phase exceeds the unit limit");
+  for (int k = 0; k < count; ++k) {
+    Ctx* c = ctxs[k];
+    Job* j = jobs[k];
+    j->last_run_graph = false;
+    if (!stats) continue;
+    LoopState ls;
+    e = cudaMemcpy(&ls, j->ls, sizeof(LoopState), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_err(c, e, "batch stats");
+    cytom_run_stats& s = stats[k];
+    memset(&s, 0, sizeof(s));
+    s.iterations = ls.iter;
+    s.count_edges = ls.count_edges;
+    s.edges_scanned = ls.edges_scanned;
+    s.active_vertices = ls.active_total;
+    s.converged = ls.cont == 0 ? 1 : 0;
+    s.residual = ls.resid_final;
+    s.elapsed_ms = ms;
+  }
+  return CYTOM_OK;
+}
+
+void batch_free(Ctx* c) {
+  BatchBuffers* bb = reinterpret_cast<BatchBuffers*>(c->batch);
+  if (!bb) return;
+  if (bb->jobs) cudaFree(bb->jobs);
+  if (bb->sched) cudaFree(bb->sched);
+  if (bb->ctl) cudaFree(bb->ctl);
+  if (bb->a) cudaEventDestroy(bb->a);
+  if (bb->b) cudaEventDestroy(bb->b);
+  delete bb;
+  c->batch = nullptr;
+}
+
+}  // namespace cytom
+
+using namespace cytom;
+
+extern "C" int cytom_run_batch(cytom_ctx* const* ctxs, const int* job_ids, int count, cytom_run_stats* stats) {
+  if (!ctxs || !job_ids || count <= 0 || !ctxs[0]) return CYTOM_ERR_INVAL;
+  Ctx* const* cs = reinterpret_cast<Ctx* const*>(ctxs);
+  int dev = -1;
+  cudaGetDevice(&dev);
+  if (dev != cs[0]->device) cudaSetDevice(cs[0]->device);
+  int rc = batch_run(cs, job_ids, count, stats);
+  if (dev >= 0 && dev != cs[0]->device) cudaSetDevice(dev);
+  return rc;
+}
+
+extern "C" int cytom_batch_units(const cytom_ctx* ctx, uint64_t* units) {
+  const Ctx* c = reinterpret_cast<const Ctx*>(ctx);
+  if (!c || !units) return CYTOM_ERR_INVAL;
+  *units = c->batch_units;
+  return CYTOM_OK;
+}

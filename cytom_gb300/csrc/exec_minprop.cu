@@ -26,16 +26,12 @@
 #include <cstring>
 
 #include "engine.h"
+#include "minprop_dev.cuh"
 #include "ptx.cuh"
 
 namespace cytom {
 
 constexpr int GATHER_T = 256;
-constexpr int APPLY_T = 256;
-
-__device__ __forceinline__ unsigned long long row_edges(const StoreDesc* sd, uint64_t x) {
-  return sd->tile_ptr[(x + 1) << sd->lT] - sd->tile_ptr[x << sd->lT];
-}
 
 // Clears both parities of the row flags and the loop counters before a run.
 __global__ void begin_kernel(const JobDesc* __restrict__ jd, const StoreDesc* __restrict__ sd,
@@ -61,130 +57,26 @@ __global__ void begin_kernel(const JobDesc* __restrict__ jd, const StoreDesc* __
   }
 }
 
-// Apply: `initial` = the seeding apply before round 0 (writes parity 0).
-// rows[parity][x] receives the number of vertices of tile row x that are active in
-// the next round (0 = the row is skipped; vpt = every source active, the frontier
-// test is skipped). A warp covers 32 consecutive bitmap words; when they share one
-// row (vpt >= 1024) it adds its row count with a single atomic.
+// Apply over every frontier word (apply_step), then the block's counters (apply_flush).
 __global__ void __launch_bounds__(APPLY_T) apply_minprop_kernel(const JobDesc* __restrict__ jd,
                                                                 const StoreDesc* __restrict__ sd,
                                                                 int initial) {
   LoopState* ls = jd->ls;
   if (!ls->cont) return;
   const unsigned pw = initial ? 0u : ((ls->iter & 1u) ^ 1u);
-  const uint64_t n = sd->n, T = sd->T;
-  const uint32_t lvpt = sd->lvpt;
-  const uint64_t nwords = (n + 31) >> 5;
-  unsigned* rows_w = jd->rows + pw * T;
-  uint32_t* __restrict__ ch = jd->ch;
-  uint32_t* __restrict__ fa = jd->fa;
-  uint32_t* __restrict__ cur = jd->cur;
-  const uint32_t* __restrict__ next = jd->next;
-  const unsigned lane = threadIdx.x & 31;
+  const uint64_t nwords = (sd->n + 31) >> 5;
   unsigned cnt = 0;
   unsigned long long teps = 0;
-  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < nwords; base += stride) {
-    const uint64_t i = base + threadIdx.x;
-    uint32_t w = 0;
-    if (i < nwords) {
-      w = ch[i];
-      fa[i] = w;
-      if (w) {
-        ch[i] = 0;
-        uint32_t bits = w;
-        while (bits) {
-          const int b = __ffs(bits) - 1;
-          bits &= bits - 1;
-          const uint64_t v = (i << 5) + b;
-          cur[v] = next[v];
-        }
-      }
-    }
-    const unsigned pc = __popc(w);
-    cnt += pc;
-    {
-      // warp-ballot compaction of the non-zero frontier words (sparse rounds read the list)
-      const unsigned nz = __ballot_sync(0xFFFFFFFFu, w != 0);
-      if (nz) {
-        unsigned slot0 = 0;
-        if (lane == 0) slot0 = atomicAdd(&ls->nact_words[pw], (unsigned)__popc(nz));
-        slot0 = __shfl_sync(0xFFFFFFFFu, slot0, 0);
-        if (w) jd->aw[slot0 + __popc(nz & ((1u << lane) - 1u))] = (uint32_t)i;
-      }
-    }
-    if (lvpt >= 10) {
-      // the warp's 32 words (1024 vertices) lie in one tile row
-      unsigned tot = pc;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xFFFFFFFFu, tot, o);
-      if (lane == 0 && tot) {
-        const uint64_t x = ((base + (threadIdx.x & ~31u)) << 5) >> lvpt;
-        if (atomicAdd(&rows_w[x], tot) == 0) teps += row_edges(sd, x);
-      }
-    } else if (w) {
-      uint32_t bits = w;
-      while (bits) {
-        const int b = __ffs(bits) - 1;
-        const uint64_t v = (i << 5) + b;
-        const uint64_t x = v >> lvpt;
-        // count this row's bits of the word at once
-        const uint64_t row_first = x << lvpt;
-        const uint64_t row_last = row_first + (1ULL << lvpt);  // exclusive
-        uint32_t mrow = bits;
-        if (row_last < ((i + 1) << 5)) mrow &= (1u << (uint32_t)(row_last - (i << 5))) - 1u;
-        bits &= ~mrow;
-        if (atomicAdd(&rows_w[x], (unsigned)__popc(mrow)) == 0) teps += row_edges(sd, x);
-      }
-    }
-  }
-  // block reduction
-  __shared__ unsigned s_cnt[APPLY_T / 32];
-  __shared__ unsigned long long s_teps[APPLY_T / 32];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    cnt += __shfl_xor_sync(0xFFFFFFFFu, cnt, o);
-    teps += __shfl_xor_sync(0xFFFFFFFFu, teps, o);
-  }
-  const unsigned wid = threadIdx.x >> 5;
-  if (lane == 0) {
-    s_cnt[wid] = cnt;
-    s_teps[wid] = teps;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned c = 0;
-    unsigned long long t = 0;
-    for (int k = 0; k < APPLY_T / 32; ++k) {
-      c += s_cnt[k];
-      t += s_teps[k];
-    }
-    if (c) atomicAdd(&ls->active[pw], c);
-    if (t) atomicAdd(&ls->teps[pw], t);
-  }
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < nwords; base += stride)
+    apply_step<false>(jd, sd, pw, base, cnt, teps);
+  apply_flush(ls, pw, cnt, teps);
 }
 
 __global__ void control_kernel(const JobDesc* __restrict__ jd, const StoreDesc* __restrict__ sd,
                                cudaGraphConditionalHandle h, int initial, int use_handle) {
-  LoopState* ls = jd->ls;
-  if (ls->cont) {
-    unsigned p;
-    if (initial) {
-      p = 0;
-    } else {
-      ls->iter += 1;
-      p = ls->iter & 1u;
-    }
-    unsigned a = ls->active[p];
-    ls->active_total += a;
-    ls->cont = (a > 0 && ls->iter < ls->max_iter && ls->err == 0) ? 1u : 0u;
-    // Next round's gather: sparse (directory, only the listed frontier words) while at
-    // most 1/8 of the frontier words are non-zero, dense (stream every active row) above.
-    const uint64_t nwords = (sd->n + 31) >> 5;
-    ls->mode = (sd->dir_ok && sd->adaptive && (uint64_t)ls->nact_words[p] * 8 <= nwords) ? 1u : 0u;
-    ls->spq_count = 0;
-  }
-  if (use_handle) cudaGraphSetConditional(h, ls->cont);
+  const unsigned cont = control_step(jd, sd, initial);
+  if (use_handle) cudaGraphSetConditional(h, cont);
 }
 
 // Gather for BFS (ALGO 0), CC (1), SSSP (2). A warp owns a 128-edge chunk: lane l
@@ -199,18 +91,8 @@ __global__ void __launch_bounds__(GATHER_T) gather_minprop_kernel(const JobDesc*
   const unsigned p = ls->iter & 1u;
   const uint64_t T = sd->T;
   const unsigned* __restrict__ rows_cur = jd->rows + p * T;
-  unsigned* rows_nxt = jd->rows + (p ^ 1u) * T;
-  {
-    uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < T; i += stride)
-      rows_nxt[i] = 0;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-      ls->active[p ^ 1u] = 0;
-      ls->nact_words[p ^ 1u] = 0;
-      ls->teps[p ^ 1u] = 0;
-      ls->count_edges += adaptive ? ls->teps[p] : sd->E;
-    }
-  }
+  round_open<false>(jd, sd, p, adaptive, (uint64_t)blockIdx.x * blockDim.x + threadIdx.x,
+                    (uint64_t)gridDim.x * blockDim.x);
   const uint32_t* __restrict__ edges = sd->edges;
   const uint32_t* __restrict__ wts = sd->wts;
   const unsigned long long* __restrict__ tile_ptr = sd->tile_ptr;
@@ -308,11 +190,8 @@ __global__ void __launch_bounds__(GATHER_T) gather_minprop_kernel(const JobDesc*
 //  - Single-row stages (the common case at large vertices-per-tile) take the source
 //    row from the stage: the frontier test needs no per-edge tile lookup, and only
 //    edges with an active source look up their target tile.
-constexpr int SG_T = 256;
-constexpr int SG_E = 4096;
 constexpr int SG_NST = 3;
 constexpr int SG_GROUP = 8;
-static_assert(SG_E == SG_T * 16, "16 edges per thread per stage");
 
 template <int ALGO>
 __host__ __device__ constexpr size_t gather_stream_smem() {
@@ -331,50 +210,14 @@ __global__ void __launch_bounds__(SG_T, 2) gather_stream_kernel(const JobDesc* _
   LoopState* ls = jd->ls;
   if (!ls->cont || ls->mode != 0) return;
   const unsigned p = ls->iter & 1u;
-  const uint64_t T = sd->T;
-  const unsigned* __restrict__ rows_cur = jd->rows + p * T;
-  unsigned* rows_nxt = jd->rows + (p ^ 1u) * T;
-  {
-    uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < T; i += stride)
-      rows_nxt[i] = 0;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-      ls->active[p ^ 1u] = 0;
-      ls->nact_words[p ^ 1u] = 0;
-      ls->teps[p ^ 1u] = 0;
-      ls->count_edges += adaptive ? ls->teps[p] : sd->E;
-    }
-  }
+  round_open<false>(jd, sd, p, adaptive, (uint64_t)blockIdx.x * blockDim.x + threadIdx.x,
+                    (uint64_t)gridDim.x * blockDim.x);
   const uint32_t* __restrict__ edges = sd->edges;
   const uint32_t* __restrict__ wts = sd->wts;
-  const unsigned long long* __restrict__ tile_ptr = sd->tile_ptr;
-  const uint32_t* __restrict__ chunk_tile = sd->chunk_tile;
-  const uint32_t* __restrict__ fa = jd->fa;
-  const uint32_t* __restrict__ cur = jd->cur;
-  uint32_t* next = jd->next;
-  uint32_t* ch = jd->ch;
-  const uint64_t E = sd->E, nchunks = sd->nchunks;
-  const uint32_t lT = sd->lT, lvpt = sd->lvpt;
-  const uint32_t ymask = (uint32_t)(T - 1);
+  const uint64_t E = sd->E;
   const uint64_t nst = (E + SG_E - 1) / SG_E;
   const uint64_t G = gridDim.x;
 
-  // rows spanned by stage s: [row of its first edge, row of the first edge after it]
-  auto stage_rows = [&](uint64_t s, uint32_t& x0, uint32_t& x1) {
-    uint64_t c0 = s * (SG_E / kChunk);
-    uint64_t c1 = c0 + SG_E / kChunk;
-    if (c1 > nchunks) c1 = nchunks;
-    x0 = chunk_tile[c0] >> lT;
-    x1 = chunk_tile[c1] >> lT;
-  };
-  auto stage_active = [&](uint64_t s) -> bool {
-    if (!adaptive) return true;
-    uint32_t x0, x1;
-    stage_rows(s, x0, x1);
-    for (uint32_t x = x0; x <= x1; ++x)
-      if (rows_cur[x]) return true;
-    return false;
-  };
   // the block's stage sequence: groups blockIdx.x, blockIdx.x + G, ... of SG_GROUP stages
   auto advance = [&](uint64_t s) -> uint64_t {
     uint64_t n1 = s + 1;
@@ -382,7 +225,7 @@ __global__ void __launch_bounds__(SG_T, 2) gather_stream_kernel(const JobDesc* _
     return (s / SG_GROUP + G) * SG_GROUP;
   };
   auto next_active = [&](uint64_t s) -> uint64_t {
-    while (s < nst && !stage_active(s)) s = advance(s);
+    while (s < nst && !stage_active<false>(jd, sd, s, p, adaptive)) s = advance(s);
     return s < nst ? s : nst;
   };
   auto issue = [&](int slot, uint64_t s) {
@@ -425,150 +268,11 @@ __global__ void __launch_bounds__(SG_T, 2) gather_stream_kernel(const JobDesc* _
       break;
     }
     phases ^= 1u << slot;
-    const uint64_t e0 = st0 * SG_E;
-    const uint64_t rem = E - e0;
-    const uint32_t cnt = rem < (uint64_t)SG_E ? (uint32_t)rem : (uint32_t)SG_E;
-    if (threadIdx.x == 0) scanned += cnt;
-    const uint32_t* eb = ebuf + slot * SG_E;
-    const uint32_t* wb = wbuf + slot * SG_E;
-    // tiles of the stage's first edge and of the first edge after it
-    uint32_t tf, ta;
-    {
-      const uint64_t c0 = st0 * (SG_E / kChunk);
-      uint64_t c1 = c0 + SG_E / kChunk;
-      if (c1 > nchunks) c1 = nchunks;
-      tf = chunk_tile[c0];
-      ta = chunk_tile[c1];
+    if (threadIdx.x == 0) {
+      const uint64_t rem = E - st0 * SG_E;
+      scanned += rem < (uint64_t)SG_E ? rem : (uint64_t)SG_E;
     }
-    const bool single_row = (tf >> lT) == (ta >> lT);
-    const bool single_tile = tf == ta;
-    const uint32_t vpt = 1u << lvpt;
-    // a fully active row needs no frontier test
-    const bool full_row = single_row && (!adaptive || rows_cur[tf >> lT] == vpt);
-
-    uint32_t qv[16], ww[16], uu[16];
-    uint32_t vmask = 0;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const uint32_t i0 = threadIdx.x * 4 + (uint32_t)k * (SG_T * 4);
-      const uint4 q = *reinterpret_cast<const uint4*>(eb + i0);
-      qv[4 * k + 0] = q.x;
-      qv[4 * k + 1] = q.y;
-      qv[4 * k + 2] = q.z;
-      qv[4 * k + 3] = q.w;
-      if (ALGO == 2) {
-        const uint4 wq = *reinterpret_cast<const uint4*>(wb + i0);
-        ww[4 * k + 0] = wq.x;
-        ww[4 * k + 1] = wq.y;
-        ww[4 * k + 2] = wq.z;
-        ww[4 * k + 3] = wq.w;
-      }
-#pragma unroll
-      for (int j = 0; j < 4; ++j) vmask |= ((i0 + j) < cnt) ? (1u << (4 * k + j)) : 0u;
-    }
-    if (single_row) {
-      const uint32_t xb = (tf >> lT) << lvpt;
-#pragma unroll
-      for (int idx = 0; idx < 16; ++idx) uu[idx] = xb | (qv[idx] >> 16);
-    } else {
-      // general path: per-edge tile lookup for the source row
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const uint32_t i0 = threadIdx.x * 4 + (uint32_t)k * (SG_T * 4);
-        const uint64_t eg = e0 + i0;
-        uint32_t t = 0;
-        unsigned long long tend = 0;
-        if (i0 < cnt) {
-          t = chunk_tile[eg >> 7];
-          tend = tile_ptr[t + 1];
-        }
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int idx = 4 * k + j;
-          if ((vmask >> idx) & 1u) {
-            while (tend <= eg + j) {
-              ++t;
-              tend = tile_ptr[t + 1];
-            }
-            const uint32_t x = t >> lT;
-            uu[idx] = (x << lvpt) | (qv[idx] >> 16);
-            if (adaptive && rows_cur[x] == 0) vmask &= ~(1u << idx);
-          } else {
-            uu[idx] = 0;
-          }
-        }
-      }
-    }
-    uint32_t amask = vmask;
-    if (adaptive && !full_row) {
-      uint32_t fw[16];
-#pragma unroll
-      for (int idx = 0; idx < 16; ++idx)
-        fw[idx] = ((vmask >> idx) & 1u) ? __ldg(fa + (uu[idx] >> 5)) : 0u;
-      amask = 0;
-#pragma unroll
-      for (int idx = 0; idx < 16; ++idx) amask |= ((fw[idx] >> (uu[idx] & 31)) & 1u) << idx;
-      amask &= vmask;
-    }
-    if (amask) {
-      uint32_t cand[16], vv[16];
-#pragma unroll
-      for (int idx = 0; idx < 16; ++idx) cand[idx] = ((amask >> idx) & 1u) ? __ldg(cur + uu[idx]) : kInf;
-      if (single_tile) {
-        const uint32_t yb = (tf & ymask) << lvpt;
-#pragma unroll
-        for (int idx = 0; idx < 16; ++idx) vv[idx] = yb | (qv[idx] & 0xFFFFu);
-      } else {
-        // target tiles of the edges with an active source
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const uint32_t i0 = threadIdx.x * 4 + (uint32_t)k * (SG_T * 4);
-          const uint64_t eg = e0 + i0;
-          const uint32_t kmask = (amask >> (4 * k)) & 0xFu;
-          uint32_t t = 0;
-          unsigned long long tend = 0;
-          if (kmask) {
-            t = chunk_tile[eg >> 7];
-            tend = tile_ptr[t + 1];
-          }
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const int idx = 4 * k + j;
-            vv[idx] = 0;
-            if ((kmask >> j) & 1u) {
-              while (tend <= eg + j) {
-                ++t;
-                tend = tile_ptr[t + 1];
-              }
-              vv[idx] = ((t & ymask) << lvpt) | (qv[idx] & 0xFFFFu);
-            }
-          }
-        }
-      }
-#pragma unroll
-      for (int idx = 0; idx < 16; ++idx) {
-        const uint32_t c = cand[idx];
-        if (c == kInf) continue;
-        if (ALGO == 0) {
-          cand[idx] = c + 1;
-        } else if (ALGO == 2) {
-          const unsigned long long sum = (unsigned long long)c + ww[idx];
-          cand[idx] = sum >= kInf ? kInf : (uint32_t)sum;
-        }
-      }
-      uint32_t nv[16];
-#pragma unroll
-      for (int idx = 0; idx < 16; ++idx) nv[idx] = (cand[idx] != kInf) ? __ldcg(next + vv[idx]) : 0u;
-      // A candidate below the value read is below current[v] too (next <= current), so
-      // next[v] ends the round below current[v]: v changed. Both updates are
-      // fire-and-forget reductions.
-#pragma unroll
-      for (int idx = 0; idx < 16; ++idx)
-        if (cand[idx] != kInf && cand[idx] < nv[idx]) atomicMin(next + vv[idx], cand[idx]);
-#pragma unroll
-      for (int idx = 0; idx < 16; ++idx)
-        if (cand[idx] != kInf && cand[idx] < nv[idx]) atomicOr(ch + (vv[idx] >> 5), 1u << (vv[idx] & 31));
-    }
+    dense_stage<ALGO, false, false>(jd, sd, ebuf + slot * SG_E, wbuf + slot * SG_E, st0, p, adaptive);
     __syncthreads();  // every thread is done with this slot
     // refill the slot with the next stage of this block
     if (threadIdx.x == 0 && s_next < nst) issue(slot, s_next);
@@ -594,204 +298,27 @@ __global__ void __launch_bounds__(SG_T, 2) gather_stream_kernel(const JobDesc* _
   if (threadIdx.x == 0 && scanned) atomicAdd(&ls->edges_scanned, scanned);
 }
 
-// Sparse gather: the round of gather_stream_kernel restricted to the edges of the
-// listed non-zero frontier words. Work item = (frontier word, tile column y); the
-// source directory gives the item's edge range inside tile (x, y), x being the word's
-// tile row. A warp takes 32 consecutive items (consecutive y of one word: coalesced
-// directory loads) and walks the light items' edges with all 32 lanes. Items longer
-// than SP_HEAVY edges, and, when the 32 items of a warp hold more than SP_WARP_MAX
-// edges in total, every item longer than SP_LIGHT, are cut into SP_CHUNK-edge chunks
-// queued for gather_sparse_chunks, so no warp is left with more than about
-// SP_WARP_MAX edges of light items or one chunk per queue entry (RMAT hub blocks).
-constexpr uint32_t SP_HEAVY = 256;
-constexpr uint32_t SP_CHUNK = 256;
-constexpr uint32_t SP_LIGHT = 32;
-constexpr uint32_t SP_WARP_MAX = 2048;
-
-struct SpItem {
-  uint32_t x, y, bits, lo, hi;
-  unsigned long long base;
-};
-
-__device__ __forceinline__ SpItem sp_item(const JobDesc* __restrict__ jd, const StoreDesc* __restrict__ sd,
-                                          uint64_t it) {
-  const uint32_t lT = sd->lT, lnbw = sd->lvpt - 5, nbw = sd->nbw;
-  const uint64_t T = sd->T;
-  SpItem r;
-  const uint32_t w = jd->aw[it >> lT];
-  r.y = (uint32_t)(it & (T - 1));
-  r.x = w >> lnbw;
-  const uint32_t b = w & (nbw - 1);
-  r.bits = __ldg(jd->fa + w);
-  const uint64_t dbase = (((uint64_t)r.x << lT) + r.y) * (nbw + 1) + b;
-  r.lo = sd->dir[dbase];
-  r.hi = sd->dir[dbase + 1];
-  r.base = sd->tile_ptr[((uint64_t)r.x << lT) | r.y];
-  return r;
-}
-
-// Relaxes edge `e` of item `m` when its source is in the item's frontier word.
-// Batched form: the loads of SP_ILP edges are issued before any of them is used.
-constexpr int SP_ILP = 8;
-
-template <int ALGO>
-__device__ __forceinline__ void sp_batch(const JobDesc* __restrict__ jd, const StoreDesc* __restrict__ sd,
-                                         const uint32_t (&xs)[SP_ILP], const uint32_t (&ys)[SP_ILP],
-                                         const uint32_t (&bits)[SP_ILP], const unsigned long long (&pos)[SP_ILP],
-                                         uint32_t valid) {
-  const uint32_t lvpt = sd->lvpt;
-  uint32_t pk[SP_ILP], wv[SP_ILP], cand[SP_ILP], nv[SP_ILP];
-#pragma unroll
-  for (int k = 0; k < SP_ILP; ++k) {
-    pk[k] = ((valid >> k) & 1u) ? sd->edges[pos[k]] : 0u;
-    wv[k] = (ALGO == 2 && ((valid >> k) & 1u)) ? sd->wts[pos[k]] : 0u;
-  }
-#pragma unroll
-  for (int k = 0; k < SP_ILP; ++k) {
-    const uint32_t sl = pk[k] >> 16;
-    const bool act = ((valid >> k) & 1u) && ((bits[k] >> (sl & 31)) & 1u);
-    cand[k] = act ? __ldg(jd->cur + ((xs[k] << lvpt) | sl)) : kInf;
-  }
-#pragma unroll
-  for (int k = 0; k < SP_ILP; ++k) {
-    const uint32_t c = cand[k];
-    if (c == kInf) continue;
-    if (ALGO == 0) {
-      cand[k] = c + 1;
-    } else if (ALGO == 2) {
-      const unsigned long long sum = (unsigned long long)c + wv[k];
-      cand[k] = sum >= kInf ? kInf : (uint32_t)sum;
-    }
-  }
-#pragma unroll
-  for (int k = 0; k < SP_ILP; ++k)
-    nv[k] = (cand[k] != kInf) ? __ldcg(jd->next + ((ys[k] << lvpt) | (pk[k] & 0xFFFFu))) : 0u;
-#pragma unroll
-  for (int k = 0; k < SP_ILP; ++k) {
-    if (cand[k] != kInf && cand[k] < nv[k]) {
-      const uint32_t v = (ys[k] << lvpt) | (pk[k] & 0xFFFFu);
-      atomicMin(jd->next + v, cand[k]);
-      atomicOr(jd->ch + (v >> 5), 1u << (v & 31));
-    }
-  }
-}
-
-// The warp relaxes the edges [e0, e1) of one item: SP_ILP edges per lane per step.
-template <int ALGO>
-__device__ __forceinline__ void sp_range(const JobDesc* __restrict__ jd, const StoreDesc* __restrict__ sd,
-                                         const SpItem& m, uint32_t e0, uint32_t e1, unsigned lane) {
-  uint32_t xs[SP_ILP], ys[SP_ILP], bits[SP_ILP];
-#pragma unroll
-  for (int k = 0; k < SP_ILP; ++k) {
-    xs[k] = m.x;
-    ys[k] = m.y;
-    bits[k] = m.bits;
-  }
-  for (uint32_t e = e0 + lane; e < e1; e += 32 * SP_ILP) {
-    unsigned long long pos[SP_ILP];
-    uint32_t valid = 0;
-#pragma unroll
-    for (int k = 0; k < SP_ILP; ++k) {
-      const uint32_t ek = e + 32u * k;
-      pos[k] = m.base + ek;
-      valid |= (ek < e1) ? (1u << k) : 0u;
-    }
-    sp_batch<ALGO>(jd, sd, xs, ys, bits, pos, valid);
-  }
-}
-
+// Sparse gather (sparse_group over every group of 32 items) and its chunk pass
+// (sparse_chunk over the queue the first pass filled).
 template <int ALGO>
 __global__ void __launch_bounds__(256) gather_sparse_kernel(const JobDesc* __restrict__ jd,
                                                              const StoreDesc* __restrict__ sd, int adaptive) {
   LoopState* ls = jd->ls;
   if (!ls->cont || ls->mode != 1) return;
   const unsigned p = ls->iter & 1u;
-  const uint64_t T = sd->T;
-  unsigned* rows_nxt = jd->rows + (p ^ 1u) * T;
-  {
-    uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < T; i += stride) rows_nxt[i] = 0;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-      ls->active[p ^ 1u] = 0;
-      ls->nact_words[p ^ 1u] = 0;
-      ls->teps[p ^ 1u] = 0;
-      ls->count_edges += adaptive ? ls->teps[p] : sd->E;
-    }
-  }
+  round_open<false>(jd, sd, p, adaptive, (uint64_t)blockIdx.x * blockDim.x + threadIdx.x,
+                    (uint64_t)gridDim.x * blockDim.x);
   const unsigned lane = threadIdx.x & 31;
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   const uint64_t items = (uint64_t)ls->nact_words[p] << sd->lT;
-  const uint64_t qcap = sd->spq_cap;
   unsigned long long scanned = 0;
-  for (uint64_t g = warp * 32; g < items; g += nwarps * 32) {
-    const uint64_t it = g + lane;
-    SpItem m{};
-    uint32_t len = 0;
-    if (it < items) {
-      m = sp_item(jd, sd, it);
-      len = m.hi > m.lo ? m.hi - m.lo : 0u;
-    }
-    uint32_t tot = len;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xFFFFFFFFu, tot, o);
-    const bool heavy = len > SP_HEAVY || (tot > SP_WARP_MAX && len > SP_LIGHT);
-    bool queued = false;
-    if (heavy) {
-      const uint32_t nch = (len + SP_CHUNK - 1) / SP_CHUNK;
-      const unsigned slot = atomicAdd(&ls->spq_count, nch);
-      if ((uint64_t)slot + nch <= qcap) {
-        for (uint32_t k = 0; k < nch; ++k) sd->spq[slot + k] = make_uint2((uint32_t)it, k);
-        queued = true;
-      }
-    }
-    // light items: the group's edges are numbered 0..total-1 (warp prefix sum over the
-    // items' lengths); lanes take SP_ILP of them per step and find their item by a
-    // binary search over the prefix sums held in the lanes
-    const uint32_t mine = (len > 0 && !queued) ? len : 0u;
-    scanned += mine;
-    uint32_t incl = mine;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y2 = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-      if (lane >= (unsigned)o) incl += y2;
-    }
-    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-    for (uint32_t f0 = 0; f0 < total; f0 += 32 * SP_ILP) {
-      uint32_t xs[SP_ILP], ys[SP_ILP], bits[SP_ILP];
-      unsigned long long pos[SP_ILP];
-      uint32_t valid = 0;
-#pragma unroll
-      for (int k = 0; k < SP_ILP; ++k) {
-        const uint32_t f = f0 + lane + 32u * k;
-        // item j holding flattened edge f: the least j with incl[j] > f
-        uint32_t j = 0;
-#pragma unroll
-        for (int step = 16; step > 0; step >>= 1) {
-          const uint32_t probe = __shfl_sync(0xFFFFFFFFu, incl, j + step - 1);
-          if (probe <= f) j += step;
-        }
-        const uint32_t incl_j = __shfl_sync(0xFFFFFFFFu, incl, j);
-        const uint32_t mine_j = __shfl_sync(0xFFFFFFFFu, mine, j);
-        xs[k] = __shfl_sync(0xFFFFFFFFu, m.x, j);
-        ys[k] = __shfl_sync(0xFFFFFFFFu, m.y, j);
-        bits[k] = __shfl_sync(0xFFFFFFFFu, m.bits, j);
-        const uint32_t lo_j = __shfl_sync(0xFFFFFFFFu, m.lo, j);
-        const unsigned long long base_j = __shfl_sync(0xFFFFFFFFu, m.base, j);
-        pos[k] = base_j + lo_j + (f - (incl_j - mine_j));
-        valid |= (f < total) ? (1u << k) : 0u;
-      }
-      sp_batch<ALGO>(jd, sd, xs, ys, bits, pos, valid);
-    }
-  }
+  for (uint64_t g = warp * 32; g < items; g += nwarps * 32) scanned += sparse_group<ALGO, false>(jd, sd, g, items);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) scanned += __shfl_xor_sync(0xFFFFFFFFu, scanned, o);
   if (lane == 0 && scanned) atomicAdd(&ls->edges_scanned, scanned);
 }
 
-// Chunks of heavy items queued by gather_sparse_kernel: one warp per chunk. Sources
-// are sorted inside an item, so a chunk whose first and last edges span no source of
-// the item's frontier word is skipped after two loads.
 template <int ALGO>
 __global__ void __launch_bounds__(256) gather_sparse_chunks(const JobDesc* __restrict__ jd,
                                                              const StoreDesc* __restrict__ sd) {
@@ -801,26 +328,10 @@ __global__ void __launch_bounds__(256) gather_sparse_chunks(const JobDesc* __res
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   uint64_t nq = ls->spq_count;
-  if (nq > sd->spq_cap) nq = sd->spq_cap;
+  if (nq > jd->spq_cap) nq = jd->spq_cap;
   const uint64_t items = (uint64_t)ls->nact_words[ls->iter & 1u] << sd->lT;
   unsigned long long scanned = 0;
-  for (uint64_t q = warp; q < nq; q += nwarps) {
-    const uint2 c = sd->spq[q];
-    if (c.x >= items) continue;  // never indexes outside this round's items
-    const SpItem m = sp_item(jd, sd, c.x);
-    const uint32_t e0 = m.lo + c.y * SP_CHUNK;
-    const uint32_t e1 = min(m.hi, e0 + SP_CHUNK);
-    if (e0 >= e1) continue;
-    uint32_t bound = 0;
-    if (lane == 0) bound = sd->edges[m.base + e0];
-    if (lane == 1) bound = sd->edges[m.base + e1 - 1];
-    const uint32_t s_first = (__shfl_sync(0xFFFFFFFFu, bound, 0) >> 16) & 31u;
-    const uint32_t s_last = (__shfl_sync(0xFFFFFFFFu, bound, 1) >> 16) & 31u;
-    const uint32_t span = (s_last >= 31u ? 0xFFFFFFFFu : ((2u << s_last) - 1u)) & ~((1u << s_first) - 1u);
-    if ((m.bits & span) == 0) continue;
-    if (lane == 0) scanned += e1 - e0;
-    sp_range<ALGO>(jd, sd, m, e0, e1, lane);
-  }
+  for (uint64_t q = warp; q < nq; q += nwarps) scanned += sparse_chunk<ALGO, false>(jd, sd, q, items);
   if (lane == 0 && scanned) atomicAdd(&ls->edges_scanned, scanned);
 }
 
@@ -1092,6 +603,15 @@ static double round_bytes(const Ctx* c, const LoopState& a, const LoopState& b, 
   if (a.mode == 0) bytes += (double)c->n / 8.0;
   else bytes += (double)a.nact_words[p] * (8.0 + 16.0 * (double)c->T);
   return bytes;
+}
+
+// Prepares a run of the batched executor: clears the loop state and the row flags
+// (the persistent kernel starts with the seeding apply).
+int minprop_batch_prep(Ctx* c, Job* j) {
+  unsigned max_iter = (unsigned)std::min<uint64_t>(j->params.max_iterations, 0xFFFFFFFFu);
+  begin_kernel<<<std::max(1, c->num_sms), 256, 0, c->stream>>>(j->d, c->dsd, max_iter);
+  c->launches++;
+  return cuda_err(c, cudaGetLastError(), "batch prep");
 }
 
 int minprop_run(Ctx* c, Job* j) {

@@ -29,13 +29,9 @@
 #include <cstring>
 
 #include "engine.h"
+#include "pagerank_dev.cuh"
 
 namespace cytom {
-
-constexpr uint32_t kBinSmall = 16;
-constexpr uint32_t kBinMedium = 4096;
-constexpr int PR_T = 256;
-constexpr int PR_BLOCK_T = 512;
 
 // CSC of the compacted store, per job (PageRank family).
 struct Csc {
@@ -50,7 +46,7 @@ struct Csc {
 };
 
 struct PrState {
-  Csc csc;
+  Csc* csc = nullptr;         // the context's CSC, shared by its PageRank-family jobs
   float* rank = nullptr;      // PR_DELTA: rank; PAGERANK fp32: r (double-buffered with rank_c)
   float* comp = nullptr;      // PR_DELTA: Kahan compensation of rank; PAGERANK fp32: r_next
   float* delta = nullptr;     // PR_DELTA: delta of the last round
@@ -61,37 +57,6 @@ struct PrState {
   uint32_t* fa2 = nullptr;    // PR_DELTA: frontier bitmaps by parity (2 x n/32)
   bool need_residual = true;
   uint64_t seen_version = ~0ULL;
-};
-
-// --------------------------------------------------------------------------
-// Compensated accumulation (Neumaier): true sum ~= s + e.
-// --------------------------------------------------------------------------
-struct Acc32 {
-  float s, e;
-  __device__ __forceinline__ void init() { s = 0.f, e = 0.f; }
-  __device__ __forceinline__ void add(float x) {
-    const float t = s + x;
-    if (fabsf(s) >= fabsf(x)) e += (s - t) + x;
-    else e += (x - t) + s;
-    s = t;
-  }
-  __device__ __forceinline__ void merge(float s2, float e2) {
-    const float t = s + s2;
-    float err;
-    if (fabsf(s) >= fabsf(s2)) err = (s - t) + s2;
-    else err = (s2 - t) + s;
-    s = t;
-    e += e2 + err;
-  }
-  __device__ __forceinline__ float value() const { return s + e; }
-};
-
-struct Acc64 {
-  double s;
-  __device__ __forceinline__ void init() { s = 0.0; }
-  __device__ __forceinline__ void add(double x) { s += x; }
-  __device__ __forceinline__ void merge(double s2, double) { s += s2; }
-  __device__ __forceinline__ double value() const { return s; }
 };
 
 // --------------------------------------------------------------------------
@@ -224,134 +189,16 @@ static int build_csc(Ctx* c, Csc& q) {
 // --------------------------------------------------------------------------
 // Round kernels
 // --------------------------------------------------------------------------
-enum PrMode { PR_DELTA_RESIDUAL = 0, PR_DELTA_PUSH = 1, PR_NORM32 = 2, PR_NORM64 = 3 };
-
-struct PrArgs {
-  const uint32_t* csc_src;
-  const uint32_t* csc_ptr;
-  const uint32_t* bins;
-  uint64_t bin_off, bin_count;
-  const uint32_t* deg;      // out-degree used for contributions
-  float* rank;
-  float* comp;
-  float* delta;
-  float* contrib;
-  double* r64;
-  double* r64n;
-  double* contrib64;
-  uint32_t* fa2;            // 2 x nwords (PR_DELTA)
-  LoopState* ls;
-  uint64_t n;
-  uint64_t nwords;
-  double alpha, delta_param, base;
-};
-
 // Per-vertex contribution of the round and the dangling mass (PAGERANK).
 template <int MODE>
 __global__ void pr_contrib_kernel(PrArgs a) {
   LoopState* ls = a.ls;
   if (!ls->cont) return;
   const unsigned p = ls->iter & 1u;
-  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  double dangling = 0.0;
-  if (MODE == PR_DELTA_RESIDUAL || MODE == PR_DELTA_PUSH) {
-    const uint32_t* fa = a.fa2 + p * a.nwords;
-    uint32_t* fn = a.fa2 + (p ^ 1u) * a.nwords;
-    for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < a.nwords; w += stride) fn[w] = 0;
-    for (uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; u < a.n; u += stride) {
-      const uint32_t d = a.deg[u];
-      float v = 0.f;
-      if (d) {
-        if (MODE == PR_DELTA_RESIDUAL) v = a.rank[u] / (float)d;
-        else if ((fa[u >> 5] >> (u & 31)) & 1u) v = a.delta[u] / (float)d;
-      }
-      a.contrib[u] = v;
-    }
-  } else if (MODE == PR_NORM32) {
-    const float* r = (p == 0) ? a.rank : a.comp;
-    for (uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; u < a.n; u += stride) {
-      const uint32_t d = a.deg[u];
-      const float rv = r[u];
-      a.contrib[u] = d ? rv / (float)d : 0.f;
-      if (!d) dangling += (double)rv;
-    }
-  } else {
-    const double* r = (p == 0) ? a.r64 : a.r64n;
-    for (uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; u < a.n; u += stride) {
-      const uint32_t d = a.deg[u];
-      const double rv = r[u];
-      a.contrib64[u] = d ? rv / (double)d : 0.0;
-      if (!d) dangling += rv;
-    }
-  }
-  if (MODE == PR_NORM32 || MODE == PR_NORM64) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) dangling += __shfl_xor_sync(0xFFFFFFFFu, dangling, o);
-    if ((threadIdx.x & 31) == 0 && dangling != 0.0) atomicAdd(&ls->dangling[p], dangling);
-  }
-}
-
-// Applies the finished sum of target v; returns |change| for the FP64 residual.
-template <int MODE>
-__device__ __forceinline__ double pr_finish(const PrArgs& a, uint64_t v, double sum, unsigned p, double dang,
-                                            double* rsum) {
-  if (MODE == PR_NORM32) {
-    const float* r = (p == 0) ? a.rank : a.comp;
-    float* rn = (p == 0) ? a.comp : a.rank;
-    const float nv = (float)(a.base + a.alpha * (sum + dang));
-    const double d = fabs((double)nv - (double)r[v]);
-    rn[v] = nv;
-    *rsum += (double)nv;
-    return d;
-  } else if (MODE == PR_NORM64) {
-    const double* r = (p == 0) ? a.r64 : a.r64n;
-    double* rn = (p == 0) ? a.r64n : a.r64;
-    const double nv = a.base + a.alpha * (sum + dang);
-    const double d = fabs(nv - r[v]);
-    rn[v] = nv;
-    *rsum += nv;
-    return d;
-  } else {
-    // PageRank-delta: residual round or delta round, rank += change (compensated)
-    float change;
-    if (MODE == PR_DELTA_RESIDUAL) {
-      change = (float)((1.0 - a.alpha) + a.alpha * sum - (double)a.rank[v] - (double)a.comp[v]);
-    } else {
-      change = (sum == 0.0) ? 0.f : (float)(a.alpha * sum);
-    }
-    a.delta[v] = change;
-    // Kahan: rank + comp carries the exact running sum of the changes
-    const float y = change + a.comp[v];
-    const float t = a.rank[v] + y;
-    a.comp[v] = y - (t - a.rank[v]);
-    a.rank[v] = t;
-    *rsum += (double)change;
-    if (change != 0.f && (double)fabsf(change) > a.delta_param * (double)t) {
-      uint32_t* fn = a.fa2 + (p ^ 1u) * a.nwords;
-      atomicOr(&fn[v >> 5], 1u << (v & 31));
-      atomicAdd(&a.ls->active[p ^ 1u], 1u);
-    }
-    return fabs((double)change);
-  }
-}
-
-template <int MODE>
-__device__ __forceinline__ void pr_flush(LoopState* ls, unsigned p, double resid, double rsum) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    resid += __shfl_xor_sync(0xFFFFFFFFu, resid, o);
-    rsum += __shfl_xor_sync(0xFFFFFFFFu, rsum, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    if (resid != 0.0) atomicAdd(&ls->resid[p], resid);
-    if (rsum != 0.0) atomicAdd(&ls->rank_sum[p], rsum);
-  }
-}
-
-template <int MODE>
-__device__ __forceinline__ auto pr_load(const PrArgs& a, uint32_t u) {
-  if constexpr (MODE == PR_NORM64) return a.contrib64[u];
-  else return a.contrib[u];
+  const double dangling = pr_contrib_range<MODE, false>(a, p, 0, a.n, 0, a.nwords,
+                                                        (uint64_t)blockIdx.x * blockDim.x + threadIdx.x,
+                                                        (uint64_t)gridDim.x * blockDim.x);
+  pr_dangling_flush<MODE>(ls, p, dangling);
 }
 
 // One thread per target (in-degree <= 16).
@@ -367,42 +214,11 @@ __global__ void __launch_bounds__(PR_T) pr_pull_small(PrArgs a) {
     const uint64_t i = base + threadIdx.x;
     if (i < a.bin_count) {
       const uint32_t v = a.bins[a.bin_off + i];
-      const uint32_t lo = a.csc_ptr[v], hi = a.csc_ptr[v + 1];
-      double sum;
-      // four independent gathers in flight, accumulated in edge order
-      if constexpr (MODE == PR_NORM64) {
-        Acc64 acc;
-        acc.init();
-        uint32_t e = lo;
-        for (; e + 4 <= hi; e += 4) {
-          const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + 1], s2 = a.csc_src[e + 2], s3 = a.csc_src[e + 3];
-          const double c0 = a.contrib64[s0], c1 = a.contrib64[s1], c2 = a.contrib64[s2], c3 = a.contrib64[s3];
-          acc.add(c0);
-          acc.add(c1);
-          acc.add(c2);
-          acc.add(c3);
-        }
-        for (; e < hi; ++e) acc.add(a.contrib64[a.csc_src[e]]);
-        sum = acc.value();
-      } else {
-        Acc32 acc;
-        acc.init();
-        uint32_t e = lo;
-        for (; e + 4 <= hi; e += 4) {
-          const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + 1], s2 = a.csc_src[e + 2], s3 = a.csc_src[e + 3];
-          const float c0 = a.contrib[s0], c1 = a.contrib[s1], c2 = a.contrib[s2], c3 = a.contrib[s3];
-          acc.add(c0);
-          acc.add(c1);
-          acc.add(c2);
-          acc.add(c3);
-        }
-        for (; e < hi; ++e) acc.add(a.contrib[a.csc_src[e]]);
-        sum = (double)acc.s + (double)acc.e;
-      }
-      resid += pr_finish<MODE>(a, v, sum, p, dang, &rsum);
+      const double sum = pr_sum_thread<MODE, false>(a, v);
+      resid += pr_finish<MODE, false>(a, v, sum, p, dang, &rsum);
     }
   }
-  pr_flush<MODE>(ls, p, resid, rsum);
+  pr_flush(ls, p, resid, rsum);
 }
 
 // One warp per target (16 < in-degree <= 4096).
@@ -418,47 +234,10 @@ __global__ void __launch_bounds__(PR_T) pr_pull_medium(PrArgs a) {
   double resid = 0.0, rsum = 0.0;
   for (uint64_t i = warp; i < a.bin_count; i += nwarps) {
     const uint32_t v = a.bins[a.bin_off + i];
-    const uint32_t lo = a.csc_ptr[v], hi = a.csc_ptr[v + 1];
-    double sum;
-    if constexpr (MODE == PR_NORM64) {
-      double s = 0.0;
-      uint32_t e = lo + lane;
-      for (; e + 96 < hi; e += 128) {
-        const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + 32], s2 = a.csc_src[e + 64], s3 = a.csc_src[e + 96];
-        const double c0 = a.contrib64[s0], c1 = a.contrib64[s1], c2 = a.contrib64[s2], c3 = a.contrib64[s3];
-        s += c0;
-        s += c1;
-        s += c2;
-        s += c3;
-      }
-      for (; e < hi; e += 32) s += a.contrib64[a.csc_src[e]];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
-      sum = s;
-    } else {
-      Acc32 acc;
-      acc.init();
-      uint32_t e = lo + lane;
-      for (; e + 96 < hi; e += 128) {
-        const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + 32], s2 = a.csc_src[e + 64], s3 = a.csc_src[e + 96];
-        const float c0 = a.contrib[s0], c1 = a.contrib[s1], c2 = a.contrib[s2], c3 = a.contrib[s3];
-        acc.add(c0);
-        acc.add(c1);
-        acc.add(c2);
-        acc.add(c3);
-      }
-      for (; e < hi; e += 32) acc.add(a.contrib[a.csc_src[e]]);
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const float s2 = __shfl_xor_sync(0xFFFFFFFFu, acc.s, o);
-        const float e2 = __shfl_xor_sync(0xFFFFFFFFu, acc.e, o);
-        acc.merge(s2, e2);
-      }
-      sum = (double)acc.s + (double)acc.e;
-    }
-    if (lane == 0) resid += pr_finish<MODE>(a, v, sum, p, dang, &rsum);
+    const double sum = pr_sum_warp<MODE, false>(a, v, lane);
+    if (lane == 0) resid += pr_finish<MODE, false>(a, v, sum, p, dang, &rsum);
   }
-  pr_flush<MODE>(ls, p, resid, rsum);
+  pr_flush(ls, p, resid, rsum);
 }
 
 // One block per target (in-degree > 4096: RMAT hubs).
@@ -468,111 +247,19 @@ __global__ void __launch_bounds__(PR_BLOCK_T) pr_pull_large(PrArgs a) {
   if (!ls->cont) return;
   const unsigned p = ls->iter & 1u;
   const double dang = (MODE == PR_NORM32 || MODE == PR_NORM64) ? ls->dangling[p] / (double)a.n : 0.0;
-  __shared__ float s_s[PR_BLOCK_T / 32], s_e[PR_BLOCK_T / 32];
-  __shared__ double s_d[PR_BLOCK_T / 32];
-  const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   double resid = 0.0, rsum = 0.0;
   for (uint64_t i = blockIdx.x; i < a.bin_count; i += gridDim.x) {
     const uint32_t v = a.bins[a.bin_off + i];
-    const uint32_t lo = a.csc_ptr[v], hi = a.csc_ptr[v + 1];
-    double sum = 0.0;
-    if constexpr (MODE == PR_NORM64) {
-      double s = 0.0;
-      uint32_t e = lo + threadIdx.x;
-      for (; e + 3 * PR_BLOCK_T < hi; e += 4 * PR_BLOCK_T) {
-        const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + PR_BLOCK_T], s2 = a.csc_src[e + 2 * PR_BLOCK_T],
-                       s3 = a.csc_src[e + 3 * PR_BLOCK_T];
-        const double c0 = a.contrib64[s0], c1 = a.contrib64[s1], c2 = a.contrib64[s2], c3 = a.contrib64[s3];
-        s += c0;
-        s += c1;
-        s += c2;
-        s += c3;
-      }
-      for (; e < hi; e += PR_BLOCK_T) s += a.contrib64[a.csc_src[e]];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
-      if (lane == 0) s_d[wid] = s;
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        for (int k = 0; k < PR_BLOCK_T / 32; ++k) sum += s_d[k];
-      }
-    } else {
-      Acc32 acc;
-      acc.init();
-      uint32_t e = lo + threadIdx.x;
-      for (; e + 3 * PR_BLOCK_T < hi; e += 4 * PR_BLOCK_T) {
-        const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + PR_BLOCK_T], s2 = a.csc_src[e + 2 * PR_BLOCK_T],
-                       s3 = a.csc_src[e + 3 * PR_BLOCK_T];
-        const float c0 = a.contrib[s0], c1 = a.contrib[s1], c2 = a.contrib[s2], c3 = a.contrib[s3];
-        acc.add(c0);
-        acc.add(c1);
-        acc.add(c2);
-        acc.add(c3);
-      }
-      for (; e < hi; e += PR_BLOCK_T) acc.add(a.contrib[a.csc_src[e]]);
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const float s2 = __shfl_xor_sync(0xFFFFFFFFu, acc.s, o);
-        const float e2 = __shfl_xor_sync(0xFFFFFFFFu, acc.e, o);
-        acc.merge(s2, e2);
-      }
-      if (lane == 0) {
-        s_s[wid] = acc.s;
-        s_e[wid] = acc.e;
-      }
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        Acc32 t;
-        t.init();
-        for (int k = 0; k < PR_BLOCK_T / 32; ++k) t.merge(s_s[k], s_e[k]);
-        sum = (double)t.s + (double)t.e;
-      }
-    }
-    if (threadIdx.x == 0) resid += pr_finish<MODE>(a, v, sum, p, dang, &rsum);
-    __syncthreads();
+    const double sum = pr_sum_block<MODE, false>(a, v);
+    if (threadIdx.x == 0) resid += pr_finish<MODE, false>(a, v, sum, p, dang, &rsum);
   }
-  pr_flush<MODE>(ls, p, resid, rsum);
+  pr_flush(ls, p, resid, rsum);
 }
 
 // Ends the round: records the FP64 residual, decides whether to continue.
 __global__ void pr_control_kernel(LoopState* ls, int mode, cudaGraphConditionalHandle h, int use_handle) {
-  if (ls->cont) {
-    const unsigned p = ls->iter & 1u;
-    const double resid = ls->resid[p];
-    ls->resid_final = resid;
-    if (mode == PR_DELTA_RESIDUAL || mode == PR_DELTA_PUSH) {
-      ls->change_sum += ls->rank_sum[p];
-      ls->active_total += ls->active[p ^ 1u];
-    }
-    ls->count_edges += ls->teps[0];
-    ls->edges_scanned += ls->teps[0];
-    ls->iter += 1;
-    const unsigned q = ls->iter & 1u;
-    bool more = ls->iter < ls->max_iter;
-    if (mode == PR_DELTA_RESIDUAL || mode == PR_DELTA_PUSH) {
-      const double total = ls->base_sum + ls->change_sum;
-      more = more && ls->active[q] > 0;
-      if (ls->tol > 0.0) more = more && resid > ls->tol * total;
-    } else {
-      more = more && resid > ls->tol;
-      // FP32 ranks cannot change by less than their rounding floor (about 6e-8 of the rank
-      // mass per round); once the FP64-measured change stops shrinking, the run is done
-      if (mode == PR_NORM32) {
-        if (resid < ls->best_resid * 0.999) {
-          ls->best_resid = resid;
-          ls->stall = 0;
-        } else if (++ls->stall >= 4) {
-          more = false;
-        }
-      }
-    }
-    ls->resid[q] = 0.0;
-    ls->dangling[q] = 0.0;
-    ls->active[q ^ 1u] = 0;
-    ls->rank_sum[q] = 0.0;
-    ls->cont = more ? 1u : 0u;
-  }
-  if (use_handle) cudaGraphSetConditional(h, ls->cont);
+  const unsigned cont = pr_control_step(ls, mode);
+  if (use_handle) cudaGraphSetConditional(h, cont);
 }
 
 // --------------------------------------------------------------------------
@@ -623,10 +310,29 @@ __global__ void pr_begin_kernel(LoopState* ls, unsigned max_iter, double tol, un
 
 static PrState* prs(Job* j) { return reinterpret_cast<PrState*>(j->ext); }
 
+// One CSC per context (per snapshot), rebuilt when the store changed, shared by every
+// PageRank-family job of the context.
+static Csc* ctx_csc(Ctx* c) {
+  if (!c->pr_csc) c->pr_csc = new (std::nothrow) Csc();
+  return reinterpret_cast<Csc*>(c->pr_csc);
+}
+
+void pagerank_ctx_free(Ctx* c) {
+  Csc* q = reinterpret_cast<Csc*>(c->pr_csc);
+  if (!q) return;
+  void* ptrs[] = {q->src, q->ptr, q->deg_out, q->bins};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  delete q;
+  c->pr_csc = nullptr;
+}
+
 int pagerank_alloc(Ctx* c, Job* j) {
   PrState* s = new (std::nothrow) PrState();
   if (!s) return set_err(c, CYTOM_ERR_OOM, "PageRank state");
   j->ext = s;
+  s->csc = ctx_csc(c);
+  if (!s->csc) return set_err(c, CYTOM_ERR_OOM, "PageRank CSC");
   const uint64_t n = c->n;
   const uint64_t nwords = (n + 31) / 32;
   bool ok = true;
@@ -656,7 +362,7 @@ int pagerank_alloc(Ctx* c, Job* j) {
 void pagerank_free(Job* j) {
   PrState* s = prs(j);
   if (!s) return;
-  void* ptrs[] = {s->csc.src, s->csc.ptr, s->csc.deg_out, s->csc.bins, s->rank, s->comp, s->delta,
+  void* ptrs[] = {s->rank, s->comp, s->delta,
                   s->contrib, s->r64, s->r64n, s->contrib64, s->fa2};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -700,18 +406,18 @@ static int launch_round(Ctx* c, Job* j, const PrArgs& base_args) {
   PrArgs a = base_args;
   pr_contrib_kernel<MODE><<<grid_n(c, c->n), 256, 0, c->stream>>>(a);
   a.bin_off = 0;
-  a.bin_count = s->csc.nb[0];
+  a.bin_count = s->csc->nb[0];
   if (a.bin_count) pr_pull_small<MODE><<<grid_n(c, a.bin_count, PR_T), PR_T, 0, c->stream>>>(a);
-  a.bin_off = s->csc.nb[0];
-  a.bin_count = s->csc.nb[1];
+  a.bin_off = s->csc->nb[0];
+  a.bin_count = s->csc->nb[1];
   if (a.bin_count) pr_pull_medium<MODE><<<grid_n(c, a.bin_count * 32, PR_T), PR_T, 0, c->stream>>>(a);
-  a.bin_off = s->csc.nb[0] + s->csc.nb[1];
-  a.bin_count = s->csc.nb[2];
+  a.bin_off = s->csc->nb[0] + s->csc->nb[1];
+  a.bin_count = s->csc->nb[2];
   if (a.bin_count)
     pr_pull_large<MODE><<<(unsigned)std::min<uint64_t>(a.bin_count, (uint64_t)c->num_sms * 4), PR_BLOCK_T, 0,
                           c->stream>>>(a);
   pr_control_kernel<<<1, 1, 0, c->stream>>>(a.ls, MODE, 0, 0);
-  c->launches += 2 + (s->csc.nb[0] ? 1 : 0) + (s->csc.nb[1] ? 1 : 0) + (s->csc.nb[2] ? 1 : 0);
+  c->launches += 2 + (s->csc->nb[0] ? 1 : 0) + (s->csc->nb[1] ? 1 : 0) + (s->csc->nb[2] ? 1 : 0);
   return cuda_err(c, cudaGetLastError(), "pagerank round");
 }
 
@@ -735,10 +441,10 @@ static int run_rounds(Ctx* c, Job* j, const PrArgs& a, uint64_t max_rounds) {
 int pagerank_run(Ctx* c, Job* j) {
   PrState* s = prs(j);
   const uint64_t ver = store_version(c);
-  if (s->csc.built_version != ver) {
-    int rc = build_csc(c, s->csc);
+  if (s->csc->built_version != ver) {
+    int rc = build_csc(c, *s->csc);
     if (rc) return rc;
-    s->csc.built_version = ver;
+    s->csc->built_version = ver;
   }
   if (s->seen_version != ver) {
     s->need_residual = true;
@@ -746,9 +452,9 @@ int pagerank_run(Ctx* c, Job* j) {
   }
   const uint64_t n = c->n;
   PrArgs a{};
-  a.csc_src = s->csc.src;
-  a.csc_ptr = s->csc.ptr;
-  a.bins = s->csc.bins;
+  a.csc_src = s->csc->src;
+  a.csc_ptr = s->csc->ptr;
+  a.bins = s->csc->bins;
   a.rank = s->rank;
   a.comp = s->comp;
   a.delta = s->delta;
@@ -764,7 +470,7 @@ int pagerank_run(Ctx* c, Job* j) {
   a.delta_param = j->params.delta;
   a.base = (1.0 - j->params.alpha) / (double)n;
   unsigned max_iter = (unsigned)std::min<uint64_t>(j->params.max_iterations, 0xFFFFFFFFu);
-  pr_begin_kernel<<<1, 1, 0, c->stream>>>(j->ls, max_iter, j->params.tolerance, (unsigned long long)s->csc.E);
+  pr_begin_kernel<<<1, 1, 0, c->stream>>>(j->ls, max_iter, j->params.tolerance, (unsigned long long)s->csc->E);
   c->launches++;
   j->last_run_graph = false;
   if (j->algo == CYTOM_ALGO_PR_DELTA) {
@@ -779,12 +485,63 @@ int pagerank_run(Ctx* c, Job* j) {
     s->need_residual = false;
     return run_rounds<PR_DELTA_PUSH>(c, j, a, max_iter);
   }
-  a.deg = s->csc.deg_out;
+  a.deg = s->csc->deg_out;
   if (j->params.kahan) {
     int rc = run_rounds<PR_NORM32>(c, j, a, max_iter);
     return rc;
   }
   return run_rounds<PR_NORM64>(c, j, a, max_iter);
+}
+
+// Prepares a run of the batched executor: the snapshot's CSC, the loop state (and for
+// PageRank-delta the rank sum before the run), the round arguments, the bin sizes and
+// the mode of the first round.
+int pagerank_batch_prep(Ctx* c, Job* j, PrArgs* out, uint64_t nb[3], int* first_mode) {
+  PrState* s = prs(j);
+  const uint64_t ver = store_version(c);
+  if (s->csc->built_version != ver) {
+    int rc = build_csc(c, *s->csc);
+    if (rc) return rc;
+    s->csc->built_version = ver;
+  }
+  s->seen_version = ver;
+  const uint64_t n = c->n;
+  PrArgs a{};
+  a.csc_src = s->csc->src;
+  a.csc_ptr = s->csc->ptr;
+  a.bins = s->csc->bins;
+  a.rank = s->rank;
+  a.comp = s->comp;
+  a.delta = s->delta;
+  a.contrib = s->contrib;
+  a.r64 = s->r64;
+  a.r64n = s->r64n;
+  a.contrib64 = s->contrib64;
+  a.fa2 = s->fa2;
+  a.ls = j->ls;
+  a.n = n;
+  a.nwords = (n + 31) / 32;
+  a.alpha = j->params.alpha;
+  a.delta_param = j->params.delta;
+  a.base = (1.0 - j->params.alpha) / (double)n;
+  unsigned max_iter = (unsigned)std::min<uint64_t>(j->params.max_iterations, 0xFFFFFFFFu);
+  pr_begin_kernel<<<1, 1, 0, c->stream>>>(j->ls, max_iter, j->params.tolerance, (unsigned long long)s->csc->E);
+  c->launches++;
+  if (j->algo == CYTOM_ALGO_PR_DELTA) {
+    a.deg = c->out_deg;
+    pr_rank_sum_kernel<<<grid_n(c, n), 256, 0, c->stream>>>(s->rank, n, j->ls);
+    c->launches++;
+    *first_mode = PR_DELTA_RESIDUAL;
+    s->need_residual = false;
+  } else {
+    a.deg = s->csc->deg_out;
+    *first_mode = j->params.kahan ? PR_NORM32 : PR_NORM64;
+  }
+  nb[0] = s->csc->nb[0];
+  nb[1] = s->csc->nb[1];
+  nb[2] = s->csc->nb[2];
+  *out = a;
+  return cuda_err(c, cudaGetLastError(), "batch prep");
 }
 
 int pagerank_result(Ctx* c, Job* j, void* out, int where) {

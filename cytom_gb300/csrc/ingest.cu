@@ -888,22 +888,6 @@ int build_directory(Ctx* c) {
     }
     c->dir_entries = entries;
   }
-  // chunk queue of sparse rounds: queued items are longer than 32 edges (at most E / 32
-  // of them) and give one chunk per 256 edges, so E / 32 + E / 256 entries always fit
-  const uint64_t need = c->E / 32 + c->E / 256 + 1024;
-  if (need > c->spq_cap) {
-    cudaFree(c->spq);
-    c->spq = nullptr;
-    const uint64_t cap = need + need / 2;
-    if (cudaMalloc(&c->spq, cap * sizeof(uint2)) != cudaSuccess) {
-      cudaGetLastError();
-      c->spq_cap = 0;
-      c->dir_disabled = true;
-      return upload_store_desc(c);
-    }
-    c->spq_cap = cap;
-    cudaMemsetAsync(c->spq, 0, cap * sizeof(uint2), c->stream);
-  }
   int slot = prof_begin(c, KC_MERGE);
   if (c->E) {
     dir_edges_kernel<<<grid_for(c, (c->E + 3) / 4, 256), 256, 0, c->stream>>>(c->dsd, c->dir, (uint32_t)nbw);

@@ -277,6 +277,22 @@ class Program:
         self.engine._check(self.engine.lib.cytom_job_destroy(self.engine.ctx, self.job))
 
 
+def run_batch(programs) -> list[dict]:
+    """Runs the given programs (of one or more engines on one device) together in one
+    persistent launch (cytom_run_batch); returns their run statistics in order."""
+    programs = list(programs)
+    if not programs:
+        return []
+    lib = programs[0].engine.lib
+    n = len(programs)
+    ctxs = (C.c_void_p * n)(*[p.engine.ctx for p in programs])
+    ids = (C.c_int * n)(*[p.job for p in programs])
+    stats = (L.RunStats * n)()
+    rc = lib.cytom_run_batch(ctxs, ids, n, stats)
+    programs[0].engine._check(rc)
+    return [stats[k].as_dict() for k in range(n)]
+
+
 class BFS(Program):
     """examples/bfs.cc: hop levels from start_vertex, UINT32_MAX = unreached."""
     ALGO = L.ALGO_BFS

@@ -191,6 +191,21 @@ int cytom_run(cytom_ctx* ctx, int job_id, cytom_run_stats* stats);
 /* Runs several jobs of this context back to back. */
 int cytom_run_many(cytom_ctx* ctx, const int* job_ids, int count, cytom_run_stats* stats);
 
+/* Batched persistent executor. Runs `count` jobs -- job_ids[k] of context ctxs[k]; the
+ * contexts (graph snapshots of any size) may differ but must share one device -- together
+ * in ONE persistent kernel launch on ctxs[0]'s stream, each job continuing exactly as
+ * cytom_run would continue it (same rounds, same results; integer programs bit-exact).
+ * The reference runs one executor thread pool per job (Jobs::Jobs starts a thread per
+ * job, src/include/core/jobs.h:79-83; each runs ContinuousAlgorithmExecutor::executeAlgorithm,
+ * continuous-algorithm-executor.h:49-249); here every job keeps a work queue of units
+ * for its current phase (edge stages, frontier-item groups, vertex ranges, target bins)
+ * and the blocks of the one launch take units from all jobs. Pending edges of every
+ * context are compacted first. stats[k] (may be NULL) as cytom_run; elapsed_ms is the
+ * device time of the whole batch. A job may appear once per call. */
+int cytom_run_batch(cytom_ctx* const* ctxs, const int* job_ids, int count, cytom_run_stats* stats);
+/* Work units processed by batched launches whose first context was ctx (statistics). */
+int cytom_batch_units(const cytom_ctx* ctx, uint64_t* units);
+
 /* Result of a job (ResultsWriter dumps vertices_.next, results-writer.h:54-64):
  * BFS levels / CC labels / SSSP distances as uint32 (UINT32_MAX = unreached),
  * PR_DELTA and PAGERANK ranks as float. `out` holds vertices elements. */

@@ -38,10 +38,12 @@ def parse():
     ap.add_argument("--steps", type=int, default=61)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="cytom", choices=["cytom", "reference"])
-    ap.add_argument("--workload", default="streaming", choices=["streaming", "prdelta", "precision", "batching"],
+    ap.add_argument("--workload", default="streaming",
+                    choices=["streaming", "prdelta", "precision", "batching", "adjoint"],
                     help="streaming: RMAT-22 BFS/CC/SSSP stream (default); prdelta: RMAT-16 PageRank-delta "
                          "stream; precision: RMAT-26 PageRank FP32-compensated vs FP64; batching: 64 jobs over "
-                         "8 snapshots, one persistent launch per job round vs one job per launch")
+                         "8 snapshots, one persistent launch per job round vs one job per launch; adjoint: weighted "
+                         "PageRank RMAT-20 forward + adjoint with gradient checks")
     ap.add_argument("--scale", type=int, default=22)
     ap.add_argument("--batch", type=int, default=1 << 20)
     ap.add_argument("--vpt", type=int, default=65536)

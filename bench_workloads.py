@@ -1,4 +1,4 @@
-"""Secondary benchmark workloads of bench.py (--workload prdelta | precision | batching).
+"""Secondary benchmark workloads of bench.py (--workload prdelta | precision | batching | adjoint).
 
 prdelta: RMAT scale 16 (65,536 vertices, 1,048,576 edges, graph500 a,b,c, seed 1,
     duplicates and self-loops kept) streamed in 16 batches of 65,536 edges in
@@ -260,6 +260,98 @@ def run_batching(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+def run_adjoint(args, rank, world, local):
+    """Weighted PageRank on RMAT scale 20 (1,048,576 vertices, 16,777,216 edges, seed 4),
+    FP32 edge weights uniform in [0.1, 1.0] (a hash of (src, tgt)) normalised per source,
+    damping 0.85, FP32-compensated forward to L1 residual 1e-8; L = c . r with c ~ N(0,1)
+    (seed 5); the adjoint gives dL/d(edge weights) and dL/d(teleport). One step = one
+    forward + adjoint. Checks: FP64 central differences (eps 1e-3 on raw weights, GPU FP64
+    forward solves) on 64 random edges, and the FP64 CPU adjoint (oracle) on every edge."""
+    import torch
+    import cytom_gb300 as cg
+    from oracle import oracle as orc
+    torch.cuda.set_device(local)
+    stream = torch.cuda.Stream()
+    scale, seed = 20, 4
+    n, m = 1 << scale, 16 << 20
+    eng = cg.Engine(n, 65536, weight_type=cg.WEIGHT_F32, stream=stream.cuda_stream)
+    s, t, q = eng.generate_rmat(0, m, scale, seed=seed, weight_seed=seed + 1000, wmin=0, wmax=(1 << 24) - 1)
+    w = (0.1 + 0.9 * q.astype(np.float64) / float((1 << 24) - 1)).astype(np.float32)
+    eng.insert_edges(s, t, w.view(np.uint32))
+    eng.do_global_compaction()
+    E = eng.count_edges()[0]
+    c = np.random.default_rng(5).standard_normal(n)
+    fwd = cg.WeightedPageRank(eng, max_iterations=1000, tolerance=1e-8, kahan=True)
+    times, fst, ast = [], None, None
+    for k in range(max(args.warmup, 1) + max(args.steps, 1)):
+        fwd.init_algorithm()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fst = fwd.execute_algorithm()
+        gw, gt, ast = fwd.adjoint(c)
+        if k >= max(args.warmup, 1):
+            times.append((time.perf_counter() - t0, fst["elapsed_ms"], ast["elapsed_ms"]))
+    wall = float(np.median([x[0] for x in times]))
+    fwd_ms = float(np.median([x[1] for x in times]))
+    adj_ms = float(np.median([x[2] for x in times]))
+    edges = fst["iterations"] * E + ast["iterations"] * E
+    # FP64 central differences on the GPU
+    tp, ed, wb, _ = eng.dump_tiles(weights=True)
+    T = n // 65536
+    tiles = np.repeat(np.arange(len(tp) - 1, dtype=np.uint64), np.diff(tp).astype(np.int64))
+    src = (((tiles // T) << np.uint64(16)) | (ed >> 16).astype(np.uint64)).astype(np.uint32)
+    tgt = (((tiles % T) << np.uint64(16)) | (ed & 0xFFFF).astype(np.uint64)).astype(np.uint32)
+    wst = wb.view(np.float32)
+    f64 = cg.WeightedPageRank(eng, max_iterations=5000, tolerance=1e-15, kahan=False)
+    f64.execute_algorithm()
+    eps = 1e-3
+    gmax = float(np.abs(gw).max())
+    fd_err = 0.0
+    t_fd = time.perf_counter()
+    for e in np.random.default_rng(6).choice(E, 64, replace=False):
+        vals = []
+        for d in (eps, -eps):
+            eng.set_edge_weights(src[e:e + 1], tgt[e:e + 1], np.array([wst[e] + d], np.float32))
+            f64.execute_algorithm()
+            vals.append(float(c @ f64.result64()))
+        eng.set_edge_weights(src[e:e + 1], tgt[e:e + 1], wst[e:e + 1].copy())
+        step = float(np.float32(wst[e] + eps)) - float(np.float32(wst[e] - eps))
+        fd = (vals[0] - vals[1]) / step
+        fd_err = max(fd_err, abs(fd - float(gw[e])) / max(abs(fd), 1e-2 * gmax))
+    t_fd = time.perf_counter() - t_fd
+    # FP64 CPU adjoint (oracle) on every edge: the CPU baseline as well
+    t_cpu = time.perf_counter()
+    r_ref, it_f = orc.wpagerank(n, src, tgt, wst.astype(np.float64), tol=1e-8)
+    _, gw_ref, gt_ref, it_a = orc.wpagerank_adjoint(n, src, tgt, wst.astype(np.float64), r_ref, c, tol=1e-8)
+    t_cpu = time.perf_counter() - t_cpu
+    r_ref14, _ = orc.wpagerank(n, src, tgt, wst.astype(np.float64), tol=1e-14)
+    _, gw_ref14, gt_ref14, _ = orc.wpagerank_adjoint(n, src, tgt, wst.astype(np.float64), r_ref14, c, tol=1e-14)
+    ew = float(np.abs(gw - gw_ref14).max() / np.abs(gw_ref14).max())
+    et = float(np.abs(gt - gt_ref14).max() / np.abs(gt_ref14).max())
+    r32 = fwd.result().astype(np.float64)
+    l1 = float(np.abs(r32 - r_ref14).sum() / np.abs(r_ref14).sum())
+    eng.close()
+    if rank == 0:
+        print(json.dumps(_line(args, world, edges / (wall), 1e3 * wall,
+                               {"workload": "differentiation: weighted PageRank RMAT-20 (16,777,216 edges, seed 4), "
+                                            "forward to L1 1e-8 + adjoint, c ~ N(0,1) seed 5",
+                                "vertices": n, "distinct_edges": E},
+                               {"unit": "edges/s (forward + adjoint rounds x stored edges)",
+                                "forward_ms": fwd_ms, "adjoint_ms": adj_ms, "forward_rounds": fst["iterations"],
+                                "adjoint_rounds": ast["iterations"],
+                                "forward_gteps": fst["iterations"] * E / (fwd_ms / 1e3) / 1e9,
+                                "adjoint_gteps": ast["iterations"] * E / (adj_ms / 1e3) / 1e9,
+                                "grad_w_vs_central_diff_max_rel": fd_err, "central_diff_edges": 64,
+                                "central_diff_eps": eps, "central_diff_seconds": t_fd,
+                                "grad_w_vs_fp64_cpu_adjoint_max_rel": ew, "grad_t_vs_fp64_cpu_adjoint_max_rel": et,
+                                "forward_l1_vs_fp64": l1,
+                                "cpu_baseline": {"value": (it_f + it_a) * E / t_cpu, "unit": "edges/s", "cores": 1,
+                                                 "kind": "port",
+                                                 "sample": "the FP64 CPU forward (L1 1e-8) + adjoint on the same graph"},
+                                "e2e": {"value": edges / wall, "unit": "edges/s", "h2d_bytes_per_step": n * 8,
+                                        "d2h_bytes_per_step": E * 4 + n * 4 + 2 * 56}})), flush=True)
+
+
 def run_workload(args, rank, world, local):
     if args.impl == "reference":
         if rank == 0:
@@ -270,5 +362,7 @@ def run_workload(args, rank, world, local):
         run_prdelta(args, rank, world, local)
     elif args.workload == "batching":
         run_batching(args, rank, world, local)
+    elif args.workload == "adjoint":
+        run_adjoint(args, rank, world, local)
     else:
         run_precision(args, rank, world, local)

@@ -19,7 +19,7 @@ ERRORS = {
 }
 PTR_HOST, PTR_DEVICE = 0, 1
 UNWEIGHTED, WEIGHT_U32, WEIGHT_F32 = 0, 1, 2
-ALGO_BFS, ALGO_CC, ALGO_SSSP, ALGO_PR_DELTA, ALGO_PAGERANK = 0, 1, 2, 3, 4
+ALGO_BFS, ALGO_CC, ALGO_SSSP, ALGO_PR_DELTA, ALGO_PAGERANK, ALGO_WPAGERANK = 0, 1, 2, 3, 4, 5
 KERNEL_CLASSES = 8
 
 
@@ -110,6 +110,10 @@ SIGNATURES = [
     ("cytom_run_many", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.c_int, C.POINTER(RunStats)]),
     ("cytom_run_batch", C.c_int, [C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.c_int, C.POINTER(RunStats)]),
     ("cytom_batch_units", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
+    ("cytom_job_set_teleport", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
+    ("cytom_pagerank_adjoint", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                         C.c_int, C.POINTER(RunStats)]),
+    ("cytom_set_edge_weights", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int]),
     ("cytom_get_result", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
     ("cytom_get_result_f64", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
     ("cytom_set_profiling", C.c_int, [C.c_void_p, C.c_int]),

@@ -25,6 +25,10 @@ int pagerank_seed(Ctx* c, Job* j, const uint32_t* src, const uint32_t* tgt, cons
 int pagerank_run(Ctx* c, Job* j);
 int pagerank_result(Ctx* c, Job* j, void* out, int where);
 int pagerank_result64(Ctx* c, Job* j, double* out, int where);
+int pagerank_set_teleport(Ctx* c, Job* j, const double* t, int where);
+int pagerank_adjoint(Ctx* c, Job* j, const double* cv, int cwhere, float* d_w, float* d_t, int owhere,
+                     cytom_run_stats* st);
+int set_edge_weights(Ctx* c, const uint32_t* src, const uint32_t* tgt, const uint32_t* w, uint64_t count);
 void pagerank_free(Job* j);
 
 int set_err(Ctx* c, int code, const std::string& msg) {
@@ -572,7 +576,7 @@ int cytom_get_degrees(cytom_ctx* ctx, uint32_t* out_degree, uint32_t* in_degree)
 
 int cytom_job_create(cytom_ctx* ctx, int algo, const cytom_job_params* params, int* job_id) {
   Ctx* c = (Ctx*)ctx;
-  if (!c || !job_id || algo < CYTOM_ALGO_BFS || algo > CYTOM_ALGO_PAGERANK) return CYTOM_ERR_INVAL;
+  if (!c || !job_id || algo < CYTOM_ALGO_BFS || algo > CYTOM_ALGO_WPAGERANK) return CYTOM_ERR_INVAL;
   Job* j = new (std::nothrow) Job();
   if (!j) return CYTOM_ERR_OOM;
   j->algo = algo;
@@ -585,6 +589,10 @@ int cytom_job_create(cytom_ctx* ctx, int algo, const cytom_job_params* params, i
   if (algo == CYTOM_ALGO_SSSP && c->wtype != CYTOM_WEIGHT_U32) {
     delete j;
     return set_err(c, CYTOM_ERR_INVAL, "SSSP needs a store with uint32 weights");
+  }
+  if (algo == CYTOM_ALGO_WPAGERANK && c->wtype != CYTOM_WEIGHT_F32) {
+    delete j;
+    return set_err(c, CYTOM_ERR_INVAL, "weighted PageRank needs a store with float weights");
   }
   int rc = job_alloc(c, j);
   if (rc) {
@@ -648,6 +656,37 @@ int cytom_get_result(cytom_ctx* ctx, int job_id, void* out, int where) {
   cudaError_t e = cudaMemcpyAsync(out, j->h.next, c->n * 4, k, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   return cuda_err(c, e, "get_result");
+}
+
+int cytom_job_set_teleport(cytom_ctx* ctx, int job_id, const double* teleport, int where) {
+  Ctx* c = (Ctx*)ctx;
+  Job* j = get_job(c, job_id);
+  if (!j) return CYTOM_ERR_INVAL;
+  return pagerank_set_teleport(c, j, teleport, where);
+}
+
+int cytom_pagerank_adjoint(cytom_ctx* ctx, int job_id, const double* c_weights, int c_where,
+                           float* d_weights, float* d_teleport, int out_where, cytom_run_stats* stats) {
+  Ctx* c = (Ctx*)ctx;
+  Job* j = get_job(c, job_id);
+  if (!j || !c_weights) return CYTOM_ERR_INVAL;
+  return pagerank_adjoint(c, j, c_weights, c_where, d_weights, d_teleport, out_where, stats);
+}
+
+int cytom_set_edge_weights(cytom_ctx* ctx, const uint32_t* src, const uint32_t* tgt, const uint32_t* w,
+                           uint64_t count, int where) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || (count && (!src || !tgt || !w))) return CYTOM_ERR_INVAL;
+  if (c->wtype == CYTOM_UNWEIGHTED) return set_err(c, CYTOM_ERR_INVAL, "the store has no weights");
+  if (where == CYTOM_PTR_DEVICE || count == 0) return set_edge_weights(c, src, tgt, w, count);
+  Staging st;
+  st.s = c->stream;
+  if (cudaMallocAsync(&st.p, count * 12, c->stream) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "staging");
+  uint32_t* ds = (uint32_t*)st.p;
+  cudaMemcpyAsync(ds, src, count * 4, cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(ds + count, tgt, count * 4, cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(ds + 2 * count, w, count * 4, cudaMemcpyHostToDevice, c->stream);
+  return set_edge_weights(c, ds, ds + count, ds + 2 * count, count);
 }
 
 int cytom_get_result_f64(cytom_ctx* ctx, int job_id, double* out, int where) {

@@ -166,6 +166,7 @@ struct Ctx {
   uint64_t batch_units = 0;
   // PageRank family: the snapshot's CSC, shared by the context's PageRank jobs
   void* pr_csc = nullptr;
+  void* pr_wgraph = nullptr;  // weighted PageRank: CSC + CSR with weights
 };
 
 // ---- helpers (capi.cu) ----

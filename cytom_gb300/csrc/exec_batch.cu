@@ -187,7 +187,7 @@ __device__ void unit_pr_pull(const BJob* J, uint32_t unit) {
   const PrArgs& a = J->pr;
   LoopState* ls = a.ls;
   const unsigned p = ls_iter(ls) & 1u;
-  const double dang = (MODE == PR_NORM32 || MODE == PR_NORM64) ? __ldcg(&ls->dangling[p]) / (double)a.n : 0.0;
+  const double dang = pr_dang_arg<MODE, true>(ls, p, a.n);
   const uint32_t ns = ceil_div(J->nb0, BU_PR_SMALL), nm = ceil_div(J->nb1, BU_PR_MEDIUM);
   double resid = 0.0, rsum = 0.0;
   if (unit < ns) {

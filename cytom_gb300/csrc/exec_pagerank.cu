@@ -57,13 +57,36 @@ struct PrState {
   uint32_t* fa2 = nullptr;    // PR_DELTA: frontier bitmaps by parity (2 x n/32)
   bool need_residual = true;
   uint64_t seen_version = ~0ULL;
+  // WPAGERANK
+  double* tele = nullptr;     // teleport vector (NULL = uniform 1/n)
+  // WPAGERANK adjoint (allocated by the first adjoint call)
+  float* lam = nullptr;       // FP32: lambda, double-buffered (2 x n)
+  double* lam64 = nullptr;    // FP64: lambda, double-buffered (2 x n)
+  float* pt = nullptr;        // (P^T lambda) of the last round
+  double* pt64 = nullptr;
+  double* cvec = nullptr;     // loss weights c
+  LoopState* adj_ls = nullptr;
+};
+
+// Weighted graph of a context (WPAGERANK): CSC by target and CSR by source, both with
+// the raw FP32 weights, and every vertex's out-weight sum (FP64, summed in CSR order).
+struct WGraph {
+  Csc in, out;
+  float* in_w = nullptr;
+  float* out_w = nullptr;
+  uint64_t in_wcap = 0, out_wcap = 0;
+  double* wsum = nullptr;
+  uint64_t built_version = ~0ULL;
 };
 
 // --------------------------------------------------------------------------
 // CSC construction from the tile store
 // --------------------------------------------------------------------------
+// Sort keys of every stored edge u -> v: (v, u) for the target-major CSC, (u, v) for the
+// source-major CSR (by_source); the edge's weight bits ride along (vals, weighted stores).
 __global__ void csc_keys_kernel(const StoreDesc* __restrict__ sd, uint64_t* __restrict__ keys,
-                                uint32_t* __restrict__ deg_out, uint32_t* __restrict__ in_cnt, uint32_t lg_n) {
+                                uint32_t* __restrict__ vals, uint32_t* __restrict__ deg_out,
+                                uint32_t* __restrict__ major_cnt, uint32_t lg_n, int by_source) {
   const uint64_t E = sd->E;
   const uint32_t lT = sd->lT, lvpt = sd->lvpt;
   const uint32_t ymask = (uint32_t)(sd->T - 1);
@@ -74,9 +97,10 @@ __global__ void csc_keys_kernel(const StoreDesc* __restrict__ sd, uint64_t* __re
     const uint32_t p = sd->edges[e];
     const uint32_t u = ((t >> lT) << lvpt) | (p >> 16);
     const uint32_t v = ((t & ymask) << lvpt) | (p & 0xFFFFu);
-    keys[e] = ((uint64_t)v << lg_n) | u;
-    atomicAdd(&deg_out[u], 1u);
-    atomicAdd(&in_cnt[v], 1u);
+    keys[e] = by_source ? (((uint64_t)u << lg_n) | v) : (((uint64_t)v << lg_n) | u);
+    if (vals) vals[e] = sd->wts[e];
+    if (deg_out) atomicAdd(&deg_out[u], 1u);
+    atomicAdd(&major_cnt[by_source ? u : v], 1u);
   }
 }
 
@@ -122,7 +146,12 @@ static int grid_n(Ctx* c, uint64_t work, int threads = 256, int per_sm = 8) {
 
 static uint64_t store_version(Ctx* c) { return c->version; }
 
-static int build_csc(Ctx* c, Csc& q) {
+// Builds a CSC (by_source = 0: each target's in-edges, `src` = their sources) or a CSR
+// (by_source = 1: each source's out-edges, `src` = their targets) of the compacted store
+// by one radix sort of (major, minor) keys; minor ids ascend inside each segment. With
+// w != NULL the edges' weights are sorted along into *w (grown to hold E). Vertices are
+// binned by segment length for the pull (small / medium / large).
+static int build_csx(Ctx* c, Csc& q, int by_source, float** w, uint64_t* wcap) {
   const uint64_t n = c->n, E = c->E;
   uint32_t lg_n = 0;
   while ((1ULL << lg_n) < n) ++lg_n;
@@ -132,6 +161,11 @@ static int build_csc(Ctx* c, Csc& q) {
     q.cap = std::max<uint64_t>(E + E / 4, 1024);
     if (cudaMalloc(&q.src, q.cap * 4) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "CSC");
   }
+  if (w && (E > *wcap || !*w)) {
+    cudaFree(*w);
+    *wcap = std::max<uint64_t>(E + E / 4, 1024);
+    if (cudaMalloc(w, *wcap * 4) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "CSC weights");
+  }
   if (!q.ptr) {
     if (cudaMalloc(&q.ptr, (n + 1) * 4) != cudaSuccess || cudaMalloc(&q.deg_out, n * 4) != cudaSuccess ||
         cudaMalloc(&q.bins, n * 4) != cudaSuccess)
@@ -139,13 +173,16 @@ static int build_csc(Ctx* c, Csc& q) {
   }
   char* tmp = nullptr;
   const size_t kbytes = std::max<uint64_t>(E, 1) * 8;
+  const size_t vbytes = w ? std::max<uint64_t>(E, 1) * 4 : 0;
   const size_t nbytes = n * 4;
-  if (cudaMallocAsync((void**)&tmp, 2 * kbytes + 7 * nbytes + 64, c->stream) != cudaSuccess)
+  if (cudaMallocAsync((void**)&tmp, 2 * kbytes + 2 * vbytes + 7 * nbytes + 64, c->stream) != cudaSuccess)
     return set_err(c, CYTOM_ERR_OOM, "CSC temporaries");
   uint64_t* k0 = (uint64_t*)tmp;
   uint64_t* k1 = (uint64_t*)(tmp + kbytes);
-  uint32_t* in_cnt = (uint32_t*)(tmp + 2 * kbytes);
-  uint32_t* f0 = in_cnt + n;
+  uint32_t* v0 = w ? (uint32_t*)(tmp + 2 * kbytes) : nullptr;
+  uint32_t* v1 = w ? (uint32_t*)(tmp + 2 * kbytes + vbytes) : nullptr;
+  uint32_t* cnt = (uint32_t*)(tmp + 2 * kbytes + 2 * vbytes);
+  uint32_t* f0 = cnt + n;
   uint32_t* f1 = f0 + n;
   uint32_t* f2 = f1 + n;
   uint32_t* p0 = f2 + n;
@@ -153,20 +190,22 @@ static int build_csc(Ctx* c, Csc& q) {
   uint32_t* p2 = p1 + n;
   uint32_t* tot = p2 + n;  // 3 totals + 1
   cudaMemsetAsync(q.deg_out, 0, n * 4, c->stream);
-  cudaMemsetAsync(in_cnt, 0, n * 4, c->stream);
+  cudaMemsetAsync(cnt, 0, n * 4, c->stream);
   int rc = CYTOM_OK;
   if (E) {
-    csc_keys_kernel<<<grid_n(c, E), 256, 0, c->stream>>>(c->dsd, k0, q.deg_out, in_cnt, lg_n);
+    csc_keys_kernel<<<grid_n(c, E), 256, 0, c->stream>>>(c->dsd, k0, v0, by_source ? nullptr : q.deg_out, cnt,
+                                                         lg_n, by_source);
     c->launches++;
     bool alt = false;
-    rc = radix_sort_pairs(c, k0, k1, nullptr, nullptr, E, (int)(2 * lg_n), &alt);
+    rc = radix_sort_pairs(c, k0, k1, v0, v1, E, (int)(2 * lg_n), &alt);
     if (rc) return rc;
     csc_src_kernel<<<grid_n(c, E), 256, 0, c->stream>>>(alt ? k1 : k0, E, lg_n, q.src);
     c->launches++;
+    if (w) cudaMemcpyAsync(*w, alt ? v1 : v0, E * 4, cudaMemcpyDeviceToDevice, c->stream);
   }
-  rc = exclusive_scan_u32(c, in_cnt, q.ptr, n, q.ptr + n);
+  rc = exclusive_scan_u32(c, cnt, q.ptr, n, q.ptr + n);
   if (rc) return rc;
-  csc_class_kernel<<<grid_n(c, n), 256, 0, c->stream>>>(in_cnt, n, f0, f1, f2);
+  csc_class_kernel<<<grid_n(c, n), 256, 0, c->stream>>>(cnt, n, f0, f1, f2);
   c->launches++;
   rc = exclusive_scan_u32(c, f0, p0, n, tot + 0);
   if (!rc) rc = exclusive_scan_u32(c, f1, p1, n, tot + 1);
@@ -185,6 +224,8 @@ static int build_csc(Ctx* c, Csc& q) {
   q.E = E;
   return CYTOM_OK;
 }
+
+static int build_csc(Ctx* c, Csc& q) { return build_csx(c, q, 0, nullptr, nullptr); }
 
 // --------------------------------------------------------------------------
 // Round kernels
@@ -207,7 +248,7 @@ __global__ void __launch_bounds__(PR_T) pr_pull_small(PrArgs a) {
   LoopState* ls = a.ls;
   if (!ls->cont) return;
   const unsigned p = ls->iter & 1u;
-  const double dang = (MODE == PR_NORM32 || MODE == PR_NORM64) ? ls->dangling[p] / (double)a.n : 0.0;
+  const double dang = pr_dang_arg<MODE, false>(ls, p, a.n);
   double resid = 0.0, rsum = 0.0;
   uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < a.bin_count; base += stride) {
@@ -227,7 +268,7 @@ __global__ void __launch_bounds__(PR_T) pr_pull_medium(PrArgs a) {
   LoopState* ls = a.ls;
   if (!ls->cont) return;
   const unsigned p = ls->iter & 1u;
-  const double dang = (MODE == PR_NORM32 || MODE == PR_NORM64) ? ls->dangling[p] / (double)a.n : 0.0;
+  const double dang = pr_dang_arg<MODE, false>(ls, p, a.n);
   const unsigned lane = threadIdx.x & 31;
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -246,7 +287,7 @@ __global__ void __launch_bounds__(PR_BLOCK_T) pr_pull_large(PrArgs a) {
   LoopState* ls = a.ls;
   if (!ls->cont) return;
   const unsigned p = ls->iter & 1u;
-  const double dang = (MODE == PR_NORM32 || MODE == PR_NORM64) ? ls->dangling[p] / (double)a.n : 0.0;
+  const double dang = pr_dang_arg<MODE, false>(ls, p, a.n);
   double resid = 0.0, rsum = 0.0;
   for (uint64_t i = blockIdx.x; i < a.bin_count; i += gridDim.x) {
     const uint32_t v = a.bins[a.bin_off + i];
@@ -317,14 +358,34 @@ static Csc* ctx_csc(Ctx* c) {
   return reinterpret_cast<Csc*>(c->pr_csc);
 }
 
-void pagerank_ctx_free(Ctx* c) {
-  Csc* q = reinterpret_cast<Csc*>(c->pr_csc);
-  if (!q) return;
+static void csc_free(Csc* q) {
   void* ptrs[] = {q->src, q->ptr, q->deg_out, q->bins};
   for (void* p : ptrs)
     if (p) cudaFree(p);
-  delete q;
-  c->pr_csc = nullptr;
+}
+
+static WGraph* ctx_wgraph(Ctx* c) {
+  if (!c->pr_wgraph) c->pr_wgraph = new (std::nothrow) WGraph();
+  return reinterpret_cast<WGraph*>(c->pr_wgraph);
+}
+
+void pagerank_ctx_free(Ctx* c) {
+  Csc* q = reinterpret_cast<Csc*>(c->pr_csc);
+  if (q) {
+    csc_free(q);
+    delete q;
+    c->pr_csc = nullptr;
+  }
+  WGraph* g = reinterpret_cast<WGraph*>(c->pr_wgraph);
+  if (g) {
+    csc_free(&g->in);
+    csc_free(&g->out);
+    void* ptrs[] = {g->in_w, g->out_w, g->wsum};
+    for (void* p : ptrs)
+      if (p) cudaFree(p);
+    delete g;
+    c->pr_wgraph = nullptr;
+  }
 }
 
 int pagerank_alloc(Ctx* c, Job* j) {
@@ -362,8 +423,8 @@ int pagerank_alloc(Ctx* c, Job* j) {
 void pagerank_free(Job* j) {
   PrState* s = prs(j);
   if (!s) return;
-  void* ptrs[] = {s->rank, s->comp, s->delta,
-                  s->contrib, s->r64, s->r64n, s->contrib64, s->fa2};
+  void* ptrs[] = {s->rank, s->comp, s->delta, s->contrib, s->r64, s->r64n, s->contrib64, s->fa2,
+                  s->tele, s->lam, s->lam64, s->pt, s->pt64, s->cvec, s->adj_ls};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete s;
@@ -381,6 +442,10 @@ int pagerank_init(Ctx* c, Job* j) {
     cudaMemsetAsync(s->comp, 0, n * 4, c->stream);
     cudaMemsetAsync(s->delta, 0, n * 4, c->stream);
     cudaMemsetAsync(s->fa2, 0xFF, 2 * ((n + 31) / 32) * 4, c->stream);
+    c->launches++;
+  } else if (j->algo == CYTOM_ALGO_WPAGERANK && s->tele) {
+    if (j->params.kahan) pr_to_float_kernel<<<g, 256, 0, c->stream>>>(s->tele, s->rank, n);
+    else cudaMemcpyAsync(s->r64, s->tele, n * 8, cudaMemcpyDeviceToDevice, c->stream);
     c->launches++;
   } else if (j->params.kahan) {
     pr_fill_kernel<<<g, 256, 0, c->stream>>>(s->rank, (float)(1.0 / (double)n), n);
@@ -401,36 +466,35 @@ int pagerank_seed(Ctx* c, Job* j, const uint32_t*, const uint32_t*, const uint32
 }
 
 template <int MODE>
-static int launch_round(Ctx* c, Job* j, const PrArgs& base_args) {
-  PrState* s = prs(j);
+static int launch_round(Ctx* c, const PrArgs& base_args, const uint64_t* nb) {
   PrArgs a = base_args;
   pr_contrib_kernel<MODE><<<grid_n(c, c->n), 256, 0, c->stream>>>(a);
   a.bin_off = 0;
-  a.bin_count = s->csc->nb[0];
+  a.bin_count = nb[0];
   if (a.bin_count) pr_pull_small<MODE><<<grid_n(c, a.bin_count, PR_T), PR_T, 0, c->stream>>>(a);
-  a.bin_off = s->csc->nb[0];
-  a.bin_count = s->csc->nb[1];
+  a.bin_off = nb[0];
+  a.bin_count = nb[1];
   if (a.bin_count) pr_pull_medium<MODE><<<grid_n(c, a.bin_count * 32, PR_T), PR_T, 0, c->stream>>>(a);
-  a.bin_off = s->csc->nb[0] + s->csc->nb[1];
-  a.bin_count = s->csc->nb[2];
+  a.bin_off = nb[0] + nb[1];
+  a.bin_count = nb[2];
   if (a.bin_count)
     pr_pull_large<MODE><<<(unsigned)std::min<uint64_t>(a.bin_count, (uint64_t)c->num_sms * 4), PR_BLOCK_T, 0,
                           c->stream>>>(a);
   pr_control_kernel<<<1, 1, 0, c->stream>>>(a.ls, MODE, 0, 0);
-  c->launches += 2 + (s->csc->nb[0] ? 1 : 0) + (s->csc->nb[1] ? 1 : 0) + (s->csc->nb[2] ? 1 : 0);
+  c->launches += 2 + (nb[0] ? 1 : 0) + (nb[1] ? 1 : 0) + (nb[2] ? 1 : 0);
   return cuda_err(c, cudaGetLastError(), "pagerank round");
 }
 
 template <int MODE>
-static int run_rounds(Ctx* c, Job* j, const PrArgs& a, uint64_t max_rounds) {
+static int run_rounds(Ctx* c, Job* j, const PrArgs& a, uint64_t max_rounds, const uint64_t* nb) {
   for (uint64_t r = 0; r < max_rounds;) {
     for (int k = 0; k < 8 && r < max_rounds; ++k, ++r) {
       int slot = prof_begin(c, KC_PAGERANK);
-      int rc = launch_round<MODE>(c, j, a);
+      int rc = launch_round<MODE>(c, a, nb);
       prof_end(c, slot, -1.0);
       if (rc) return rc;
     }
-    cudaError_t e = cudaMemcpyAsync(c->h_pinned, &j->ls->cont, 4, cudaMemcpyDeviceToHost, c->stream);
+    cudaError_t e = cudaMemcpyAsync(c->h_pinned, &a.ls->cont, 4, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_err(c, e, "pagerank loop");
     if (*(unsigned*)c->h_pinned == 0) break;
@@ -438,7 +502,10 @@ static int run_rounds(Ctx* c, Job* j, const PrArgs& a, uint64_t max_rounds) {
   return CYTOM_OK;
 }
 
+static int wpagerank_run(Ctx* c, Job* j);
+
 int pagerank_run(Ctx* c, Job* j) {
+  if (j->algo == CYTOM_ALGO_WPAGERANK) return wpagerank_run(c, j);
   PrState* s = prs(j);
   const uint64_t ver = store_version(c);
   if (s->csc->built_version != ver) {
@@ -480,23 +547,25 @@ int pagerank_run(Ctx* c, Job* j) {
     c->launches++;
     // Every run opens with the residual round (all sources contribute rank / outdeg):
     // exact after any change of the graph, and a no-op correction when nothing changed.
-    int rc = run_rounds<PR_DELTA_RESIDUAL>(c, j, a, 1);
+    int rc = run_rounds<PR_DELTA_RESIDUAL>(c, j, a, 1, s->csc->nb);
     if (rc) return rc;
     s->need_residual = false;
-    return run_rounds<PR_DELTA_PUSH>(c, j, a, max_iter);
+    return run_rounds<PR_DELTA_PUSH>(c, j, a, max_iter, s->csc->nb);
   }
   a.deg = s->csc->deg_out;
   if (j->params.kahan) {
-    int rc = run_rounds<PR_NORM32>(c, j, a, max_iter);
+    int rc = run_rounds<PR_NORM32>(c, j, a, max_iter, s->csc->nb);
     return rc;
   }
-  return run_rounds<PR_NORM64>(c, j, a, max_iter);
+  return run_rounds<PR_NORM64>(c, j, a, max_iter, s->csc->nb);
 }
 
 // Prepares a run of the batched executor: the snapshot's CSC, the loop state (and for
 // PageRank-delta the rank sum before the run), the round arguments, the bin sizes and
 // the mode of the first round.
 int pagerank_batch_prep(Ctx* c, Job* j, PrArgs* out, uint64_t nb[3], int* first_mode) {
+  if (j->algo == CYTOM_ALGO_WPAGERANK)
+    return set_err(c, CYTOM_ERR_UNIMPLEMENTED, "weighted PageRank runs through cytom_run only");
   PrState* s = prs(j);
   const uint64_t ver = store_version(c);
   if (s->csc->built_version != ver) {
@@ -552,7 +621,7 @@ int pagerank_result(Ctx* c, Job* j, void* out, int where) {
   cudaMemcpyAsync(&ls, j->ls, sizeof(ls), cudaMemcpyDeviceToHost, c->stream);
   cudaStreamSynchronize(c->stream);
   const unsigned p = ls.iter & 1u;  // buffer holding the newest ranks
-  if (j->algo == CYTOM_ALGO_PAGERANK) {
+  if (j->algo == CYTOM_ALGO_PAGERANK || j->algo == CYTOM_ALGO_WPAGERANK) {
     if (j->params.kahan) {
       src = (p == 0) ? s->rank : s->comp;
     } else {
@@ -570,7 +639,8 @@ int pagerank_result(Ctx* c, Job* j, void* out, int where) {
 
 int pagerank_result64(Ctx* c, Job* j, double* out, int where) {
   PrState* s = prs(j);
-  if (j->algo != CYTOM_ALGO_PAGERANK || j->params.kahan) return set_err(c, CYTOM_ERR_INVAL, "not an FP64 job");
+  if ((j->algo != CYTOM_ALGO_PAGERANK && j->algo != CYTOM_ALGO_WPAGERANK) || j->params.kahan)
+    return set_err(c, CYTOM_ERR_INVAL, "not an FP64 job");
   LoopState ls;
   cudaMemcpyAsync(&ls, j->ls, sizeof(ls), cudaMemcpyDeviceToHost, c->stream);
   cudaStreamSynchronize(c->stream);
@@ -579,6 +649,270 @@ int pagerank_result64(Ctx* c, Job* j, double* out, int where) {
   cudaError_t e = cudaMemcpyAsync(out, r, c->n * 8, k, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   return cuda_err(c, e, "pagerank result64");
+}
+
+
+// --------------------------------------------------------------------------
+// Weighted PageRank (WPAGERANK) and its adjoint
+// --------------------------------------------------------------------------
+
+// s_u = sum of u's out-weights, one warp per source in CSR order (deterministic).
+__global__ void wsum_kernel(const uint32_t* __restrict__ ptr, const float* __restrict__ w, uint64_t n,
+                            double* __restrict__ wsum) {
+  const unsigned lane = threadIdx.x & 31;
+  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t u = warp; u < n; u += nwarps) {
+    double s = 0.0;
+    for (uint32_t e = ptr[u] + lane; e < ptr[u + 1]; e += 32) s += (double)w[e];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
+    if (lane == 0) wsum[u] = s;
+  }
+}
+
+static int build_wgraph(Ctx* c, WGraph& g) {
+  if (g.built_version == c->version) return CYTOM_OK;
+  int rc = build_csx(c, g.in, 0, &g.in_w, &g.in_wcap);
+  if (!rc) rc = build_csx(c, g.out, 1, &g.out_w, &g.out_wcap);
+  if (rc) return rc;
+  if (!g.wsum && cudaMalloc(&g.wsum, c->n * 8) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "weight sums");
+  wsum_kernel<<<grid_n(c, c->n * 32), 256, 0, c->stream>>>(g.out.ptr, g.out_w, c->n, g.wsum);
+  c->launches++;
+  g.built_version = c->version;
+  return cuda_err(c, cudaGetLastError(), "weight sums");
+}
+
+static PrArgs wargs(Ctx* c, Job* j, const WGraph& g) {
+  PrState* s = prs(j);
+  PrArgs a{};
+  a.csc_src = g.in.src;
+  a.csc_ptr = g.in.ptr;
+  a.bins = g.in.bins;
+  a.csc_w = g.in_w;
+  a.wsum = g.wsum;
+  a.tele = s->tele;
+  a.rank = s->rank;
+  a.comp = s->comp;
+  a.contrib = s->contrib;
+  a.r64 = s->r64;
+  a.r64n = s->r64n;
+  a.contrib64 = s->contrib64;
+  a.ls = j->ls;
+  a.n = c->n;
+  a.nwords = (c->n + 31) / 32;
+  a.alpha = j->params.alpha;
+  return a;
+}
+
+static int wpagerank_run(Ctx* c, Job* j) {
+  WGraph* g = ctx_wgraph(c);
+  if (!g) return set_err(c, CYTOM_ERR_OOM, "weighted graph");
+  int rc = build_wgraph(c, *g);
+  if (rc) return rc;
+  PrArgs a = wargs(c, j, *g);
+  unsigned max_iter = (unsigned)std::min<uint64_t>(j->params.max_iterations, 0xFFFFFFFFu);
+  pr_begin_kernel<<<1, 1, 0, c->stream>>>(j->ls, max_iter, j->params.tolerance, (unsigned long long)g->in.E);
+  c->launches++;
+  j->last_run_graph = false;
+  return j->params.kahan ? run_rounds<PR_W32>(c, j, a, max_iter, g->in.nb)
+                         : run_rounds<PR_W64>(c, j, a, max_iter, g->in.nb);
+}
+
+int pagerank_set_teleport(Ctx* c, Job* j, const double* t, int where) {
+  PrState* s = prs(j);
+  if (j->algo != CYTOM_ALGO_WPAGERANK) return set_err(c, CYTOM_ERR_INVAL, "teleport vectors are for WPAGERANK jobs");
+  if (!t) {
+    if (s->tele) {
+      cudaStreamSynchronize(c->stream);
+      cudaFree(s->tele);
+    }
+    s->tele = nullptr;
+    return CYTOM_OK;
+  }
+  if (!s->tele && cudaMalloc(&s->tele, c->n * 8) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "teleport");
+  cudaError_t e = cudaMemcpyAsync(s->tele, t, c->n * 8,
+                                  where == CYTOM_PTR_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                  c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  return cuda_err(c, e, "teleport upload");
+}
+
+__global__ void adj_init_kernel(const double* __restrict__ cvec, uint64_t n, float* lam32, double* lam64,
+                                LoopState* ls) {
+  double l1 = 0.0;
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
+    const double cv = cvec[v];
+    if (lam32) lam32[v] = (float)cv;
+    if (lam64) lam64[v] = cv;
+    l1 += fabs(cv);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) l1 += __shfl_xor_sync(0xFFFFFFFFu, l1, o);
+  if ((threadIdx.x & 31) == 0 && l1 != 0.0) atomicAdd(&ls->base_sum, l1);
+}
+
+// The adjoint stops at an L1 change <= rel * |c|_1.
+__global__ void adj_tol_kernel(LoopState* ls, double rel) { ls->tol = rel * ls->base_sum; }
+
+// D = sum of r over vertices without out-weight.
+template <typename T>
+__global__ void dangling_sum_kernel(const T* __restrict__ r, const double* __restrict__ wsum, uint64_t n,
+                                    double* out) {
+  double d = 0.0;
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride)
+    if (!(wsum[v] > 0.0)) d += (double)r[v];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xFFFFFFFFu, d, o);
+  if ((threadIdx.x & 31) == 0 && d != 0.0) atomicAdd(out, d);
+}
+
+// dL/dw of every stored edge u -> k, in store order:
+// alpha * r_u / s_u * (lambda_k - (P^T lambda)_u), evaluated in FP64.
+template <typename T>
+__global__ void grad_w_kernel(const StoreDesc* __restrict__ sd, const T* __restrict__ r,
+                              const T* __restrict__ lam, const T* __restrict__ pt,
+                              const double* __restrict__ wsum, double alpha, float* __restrict__ gw) {
+  const uint64_t E = sd->E;
+  const uint32_t lT = sd->lT, lvpt = sd->lvpt;
+  const uint32_t ymask = (uint32_t)(sd->T - 1);
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += stride) {
+    uint32_t t = sd->chunk_tile[e >> 7];
+    while (sd->tile_ptr[t + 1] <= e) ++t;
+    const uint32_t p = sd->edges[e];
+    const uint32_t u = ((t >> lT) << lvpt) | (p >> 16);
+    const uint32_t k = ((t & ymask) << lvpt) | (p & 0xFFFFu);
+    gw[e] = (float)(alpha * (double)r[u] / wsum[u] * ((double)lam[k] - (double)pt[u]));
+  }
+}
+
+// dL/dt_v = ((1 - alpha) + alpha * D) * lambda_v.
+template <typename T>
+__global__ void grad_t_kernel(const T* __restrict__ lam, uint64_t n, const double* __restrict__ dang,
+                              double alpha, float* __restrict__ gt) {
+  const double f = (1.0 - alpha) + alpha * dang[0];
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride)
+    gt[v] = (float)(f * (double)lam[v]);
+}
+
+// Adjoint of L = c . r at the converged ranks of WPAGERANK job j: solves
+// lambda = c + alpha (P^T lambda + a (t . lambda)) over the source-major CSR (the same
+// edges in reverse orientation), then writes dL/dw (every stored edge, store order) and
+// dL/dt. Only the converged rank vector of the forward run is used (no per-round state).
+int pagerank_adjoint(Ctx* c, Job* j, const double* cv, int cwhere, float* d_w, float* d_t, int owhere,
+                     cytom_run_stats* st) {
+  PrState* s = prs(j);
+  if (j->algo != CYTOM_ALGO_WPAGERANK) return set_err(c, CYTOM_ERR_INVAL, "the adjoint needs a WPAGERANK job");
+  WGraph* g = ctx_wgraph(c);
+  if (j->fresh || !g || g->built_version != c->version || c->A)
+    return set_err(c, CYTOM_ERR_INVAL, "run the forward PageRank on the current graph first");
+  const uint64_t n = c->n, E = c->E;
+  const bool f32 = j->params.kahan != 0;
+  cudaError_t e = cudaSuccess;
+  if (!s->adj_ls) e = cudaMalloc(&s->adj_ls, sizeof(LoopState));
+  if (e == cudaSuccess && !s->cvec) e = cudaMalloc(&s->cvec, n * 8);
+  if (f32) {
+    if (e == cudaSuccess && !s->lam) e = cudaMalloc(&s->lam, 2 * n * 4);
+    if (e == cudaSuccess && !s->pt) e = cudaMalloc(&s->pt, n * 4);
+  } else {
+    if (e == cudaSuccess && !s->lam64) e = cudaMalloc(&s->lam64, 2 * n * 8);
+    if (e == cudaSuccess && !s->pt64) e = cudaMalloc(&s->pt64, n * 8);
+  }
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(c, CYTOM_ERR_OOM, "adjoint state");
+  }
+  // the forward's newest ranks
+  LoopState fls;
+  e = cudaMemcpyAsync(&fls, j->ls, sizeof(LoopState), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(s->cvec, cv, n * 8, cwhere == CYTOM_PTR_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                        c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "adjoint setup");
+  const unsigned pf = fls.iter & 1u;
+  const float* r32 = f32 ? ((pf == 0) ? s->rank : s->comp) : nullptr;
+  const double* r64 = f32 ? nullptr : ((pf == 0) ? s->r64 : s->r64n);
+
+  cudaEventRecord(c->run_a, c->stream);
+  unsigned max_iter = (unsigned)std::min<uint64_t>(j->params.max_iterations, 0xFFFFFFFFu);
+  pr_begin_kernel<<<1, 1, 0, c->stream>>>(s->adj_ls, max_iter, 0.0, (unsigned long long)g->out.E);
+  adj_init_kernel<<<grid_n(c, n), 256, 0, c->stream>>>(s->cvec, n, f32 ? s->lam : nullptr, f32 ? nullptr : s->lam64,
+                                                        s->adj_ls);
+  adj_tol_kernel<<<1, 1, 0, c->stream>>>(s->adj_ls, j->params.tolerance);
+  c->launches += 3;
+  PrArgs a{};
+  a.csc_src = g->out.src;
+  a.csc_ptr = g->out.ptr;
+  a.bins = g->out.bins;
+  a.csc_w = g->out_w;
+  a.wsum = g->wsum;
+  a.tele = s->tele;
+  a.cvec = s->cvec;
+  a.pt = s->pt;
+  a.pt64 = s->pt64;
+  a.rank = f32 ? s->lam : nullptr;
+  a.comp = f32 ? s->lam + n : nullptr;
+  a.r64 = f32 ? nullptr : s->lam64;
+  a.r64n = f32 ? nullptr : s->lam64 + n;
+  a.contrib = s->contrib;  // the forward's contribution buffer is free once it has converged
+  a.contrib64 = s->contrib64;
+  a.ls = s->adj_ls;
+  a.n = n;
+  a.nwords = (n + 31) / 32;
+  a.alpha = j->params.alpha;
+  int rc = f32 ? run_rounds<PR_ADJ32>(c, j, a, max_iter, g->out.nb) : run_rounds<PR_ADJ64>(c, j, a, max_iter, g->out.nb);
+  if (rc) return rc;
+  LoopState als;
+  e = cudaMemcpyAsync(&als, s->adj_ls, sizeof(LoopState), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "adjoint run");
+  const unsigned pa = als.iter & 1u;  // buffer holding the newest lambda
+  // gradients into device scratch, then to the caller
+  char* tmp = nullptr;
+  const size_t wbytes = std::max<uint64_t>(E, 1) * 4, tbytes = n * 4;
+  if (cudaMallocAsync((void**)&tmp, wbytes + tbytes + 16, c->stream) != cudaSuccess)
+    return set_err(c, CYTOM_ERR_OOM, "adjoint outputs");
+  float* gw = (owhere == CYTOM_PTR_DEVICE && d_w) ? d_w : (float*)tmp;
+  float* gt = (owhere == CYTOM_PTR_DEVICE && d_t) ? d_t : (float*)(tmp + wbytes);
+  double* dang = (double*)(tmp + wbytes + tbytes);
+  cudaMemsetAsync(dang, 0, 8, c->stream);
+  if (f32) {
+    const float* lam = (pa == 0) ? s->lam : s->lam + n;
+    dangling_sum_kernel<float><<<grid_n(c, n), 256, 0, c->stream>>>(r32, g->wsum, n, dang);
+    if (E) grad_w_kernel<float><<<grid_n(c, E), 256, 0, c->stream>>>(c->dsd, r32, lam, s->pt, g->wsum, a.alpha, gw);
+    grad_t_kernel<float><<<grid_n(c, n), 256, 0, c->stream>>>(lam, n, dang, a.alpha, gt);
+  } else {
+    const double* lam = (pa == 0) ? s->lam64 : s->lam64 + n;
+    dangling_sum_kernel<double><<<grid_n(c, n), 256, 0, c->stream>>>(r64, g->wsum, n, dang);
+    if (E) grad_w_kernel<double><<<grid_n(c, E), 256, 0, c->stream>>>(c->dsd, r64, lam, s->pt64, g->wsum, a.alpha, gw);
+    grad_t_kernel<double><<<grid_n(c, n), 256, 0, c->stream>>>(lam, n, dang, a.alpha, gt);
+  }
+  c->launches += 3;
+  cudaEventRecord(c->run_b, c->stream);
+  if (owhere != CYTOM_PTR_DEVICE) {
+    if (d_w && E) cudaMemcpyAsync(d_w, gw, E * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (d_t) cudaMemcpyAsync(d_t, gt, n * 4, cudaMemcpyDeviceToHost, c->stream);
+  }
+  cudaFreeAsync(tmp, c->stream);
+  e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "adjoint gradients");
+  if (st) {
+    memset(st, 0, sizeof(*st));
+    st->iterations = als.iter;
+    st->count_edges = als.count_edges;
+    st->edges_scanned = als.edges_scanned;
+    st->converged = als.cont == 0 ? 1 : 0;
+    st->residual = als.resid_final;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->run_a, c->run_b);
+    st->elapsed_ms = ms;
+  }
+  return CYTOM_OK;
 }
 
 }  // namespace cytom

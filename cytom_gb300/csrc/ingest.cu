@@ -909,4 +909,57 @@ int compute_compact_flags(Ctx* c, uint8_t* dflags) {
   return cuda_err(c, cudaGetLastError(), "count_sources");
 }
 
+
+// Weight update of stored edges: update i finds (src[i], tgt[i]) in its tile (binary
+// search over the tile's sorted packed edges) and overwrites its weight; an edge that
+// is not stored sets *missing.
+__global__ void set_weights_kernel(const StoreDesc* __restrict__ sd, const uint32_t* __restrict__ src,
+                                   const uint32_t* __restrict__ tgt, const uint32_t* __restrict__ w, uint64_t count,
+                                   uint32_t* wts, unsigned* missing) {
+  const uint32_t lvpt = sd->lvpt, lT = sd->lT;
+  const uint32_t lmask = (1u << lvpt) - 1u;
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+    const uint32_t u = src[i], v = tgt[i];
+    if ((uint64_t)u >= sd->n || (uint64_t)v >= sd->n) {
+      atomicOr(missing, 1u);
+      continue;
+    }
+    const uint64_t t = ((uint64_t)(u >> lvpt) << lT) | (v >> lvpt);
+    const uint32_t key = ((u & lmask) << 16) | (v & lmask);
+    uint64_t lo = sd->tile_ptr[t], hi = sd->tile_ptr[t + 1];
+    while (lo < hi) {
+      const uint64_t mid = (lo + hi) >> 1;
+      if (sd->edges[mid] < key) lo = mid + 1;
+      else hi = mid;
+    }
+    if (lo < sd->tile_ptr[t + 1] && sd->edges[lo] == key) wts[lo] = w[i];
+    else atomicOr(missing, 1u);
+  }
+}
+
+int set_edge_weights(Ctx* c, const uint32_t* src, const uint32_t* tgt, const uint32_t* w, uint64_t count) {
+  int rc = compact(c);
+  if (rc) return rc;
+  cudaMemsetAsync(c->d_flag, 0, 4, c->stream);
+  if (count) {
+    set_weights_kernel<<<grid_for(c, count, 256), 256, 0, c->stream>>>(c->dsd, src, tgt, w, count, c->wts,
+                                                                          c->d_flag);
+    c->launches++;
+  }
+  unsigned missing = 0;
+  cudaError_t e = cudaMemcpyAsync(&missing, c->d_flag, 4, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "weight update");
+  // every weight-dependent structure is rebuilt; SSSP jobs restart (a heavier edge can
+  // lengthen shortest paths, which min-propagation cannot undo)
+  c->version++;
+  rc = upload_store_desc(c);
+  if (rc) return rc;
+  for (Job* j : c->jobs)
+    if (j && j->algo == CYTOM_ALGO_SSSP) j->fresh = true;
+  if (missing) return set_err(c, CYTOM_ERR_RANGE, "weight update of an edge that is not stored");
+  return CYTOM_OK;
+}
+
 }  // namespace cytom

@@ -24,7 +24,29 @@ constexpr uint32_t kBinMedium = 4096;
 constexpr int PR_T = 256;
 constexpr int PR_BLOCK_T = 256;
 
-enum PrMode { PR_DELTA_RESIDUAL = 0, PR_DELTA_PUSH = 1, PR_NORM32 = 2, PR_NORM64 = 3 };
+// PR_W*: weighted PageRank r = (1-alpha) t + alpha (P r + D t), P[v,u] = w_uv / s_u
+// (pull over the CSC with its raw weights; s_u = sum of u's out-weights; t = teleport).
+// PR_ADJ*: its adjoint lambda = c + alpha (P^T lambda + a (t . lambda)) (pull over the
+// source-major CSR; a_u = 1 when s_u = 0). 32 = FP32 values with compensated sums,
+// 64 = FP64 plain.
+enum PrMode {
+  PR_DELTA_RESIDUAL = 0,
+  PR_DELTA_PUSH = 1,
+  PR_NORM32 = 2,
+  PR_NORM64 = 3,
+  PR_W32 = 4,
+  PR_W64 = 5,
+  PR_ADJ32 = 6,
+  PR_ADJ64 = 7
+};
+template <int MODE>
+__host__ __device__ constexpr bool pr_is64() {
+  return MODE == PR_NORM64 || MODE == PR_W64 || MODE == PR_ADJ64;
+}
+template <int MODE>
+__host__ __device__ constexpr bool pr_weighted() {
+  return MODE >= PR_W32;
+}
 
 // Compensated accumulation (Neumaier): true sum ~= s + e.
 struct Acc32 {
@@ -69,6 +91,12 @@ struct PrArgs {
   double* r64n;
   double* contrib64;
   uint32_t* fa2;            // 2 x nwords (PR_DELTA)
+  const float* csc_w;       // weighted modes: raw weight of each in-edge (CSC) / out-edge (CSR)
+  const double* wsum;       // weighted modes: out-weight sum s_u of each vertex
+  const double* tele;       // weighted modes: teleport vector (NULL = uniform 1/n)
+  const double* cvec;       // adjoint: the loss weights c
+  float* pt;                // adjoint FP32: (P^T lambda)_u of the last round
+  double* pt64;             // adjoint FP64
   LoopState* ls;
   uint64_t n;
   uint64_t nwords;
@@ -79,6 +107,21 @@ template <bool PERSIST, class T>
 __device__ __forceinline__ T pr_ld(const T* p) {
   if constexpr (PERSIST) return __ldcg(p);
   else return *p;
+}
+
+// Contribution of in-edge e with source s: contrib[s], times the edge's raw weight in
+// the weighted modes (an FP32 product in the FP32 modes).
+template <int MODE, bool PERSIST>
+__device__ __forceinline__ float pr_c32(const PrArgs& a, uint32_t e, uint32_t s) {
+  const float c = pr_ld<PERSIST>(a.contrib + s);
+  if constexpr (pr_weighted<MODE>()) return c * a.csc_w[e];
+  else return c;
+}
+template <int MODE, bool PERSIST>
+__device__ __forceinline__ double pr_c64(const PrArgs& a, uint32_t e, uint32_t s) {
+  const double c = pr_ld<PERSIST>(a.contrib64 + s);
+  if constexpr (pr_weighted<MODE>()) return c * (double)a.csc_w[e];
+  else return c;
 }
 
 // Contributions of the sources handled by this thread (u = lo + tid, lo + tid + nthr, ...
@@ -109,6 +152,39 @@ __device__ __forceinline__ double pr_contrib_range(const PrArgs& a, unsigned p, 
       a.contrib[u] = d ? rv / (float)d : 0.f;
       if (!d) dangling += (double)rv;
     }
+  } else if (MODE == PR_W32) {
+    const float* r = (p == 0) ? a.rank : a.comp;
+    for (uint64_t u = lo + tid; u < hi; u += nthr) {
+      const double s = a.wsum[u];
+      const float rv = pr_ld<PERSIST>(r + u);
+      a.contrib[u] = s > 0.0 ? rv / (float)s : 0.f;
+      if (!(s > 0.0)) dangling += (double)rv;
+    }
+  } else if (MODE == PR_W64) {
+    const double* r = (p == 0) ? a.r64 : a.r64n;
+    for (uint64_t u = lo + tid; u < hi; u += nthr) {
+      const double s = a.wsum[u];
+      const double rv = pr_ld<PERSIST>(r + u);
+      a.contrib64[u] = s > 0.0 ? rv / s : 0.0;
+      if (!(s > 0.0)) dangling += rv;
+    }
+  } else if (MODE == PR_ADJ32) {
+    // gather source = lambda itself; the returned sum is t . lambda
+    const float* l = (p == 0) ? a.rank : a.comp;
+    const double tu = 1.0 / (double)a.n;
+    for (uint64_t u = lo + tid; u < hi; u += nthr) {
+      const float lv = pr_ld<PERSIST>(l + u);
+      a.contrib[u] = lv;
+      dangling += (a.tele ? a.tele[u] : tu) * (double)lv;
+    }
+  } else if (MODE == PR_ADJ64) {
+    const double* l = (p == 0) ? a.r64 : a.r64n;
+    const double tu = 1.0 / (double)a.n;
+    for (uint64_t u = lo + tid; u < hi; u += nthr) {
+      const double lv = pr_ld<PERSIST>(l + u);
+      a.contrib64[u] = lv;
+      dangling += (a.tele ? a.tele[u] : tu) * lv;
+    }
   } else {
     const double* r = (p == 0) ? a.r64 : a.r64n;
     for (uint64_t u = lo + tid; u < hi; u += nthr) {
@@ -124,11 +200,20 @@ __device__ __forceinline__ double pr_contrib_range(const PrArgs& a, unsigned p, 
 // Warp-reduced dangling mass into the loop state (every lane calls it).
 template <int MODE>
 __device__ __forceinline__ void pr_dangling_flush(LoopState* ls, unsigned p, double dangling) {
-  if (MODE == PR_NORM32 || MODE == PR_NORM64) {
+  if (MODE >= PR_NORM32) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) dangling += __shfl_xor_sync(0xFFFFFFFFu, dangling, o);
     if ((threadIdx.x & 31) == 0 && dangling != 0.0) atomicAdd(&ls->dangling[p], dangling);
   }
+}
+
+// The round's dangling term as pr_finish takes it: D / n (normalised PageRank), D
+// (weighted: scaled by t_v in pr_finish), t . lambda (adjoint), none (PageRank-delta).
+template <int MODE, bool PERSIST>
+__device__ __forceinline__ double pr_dang_arg(const LoopState* ls, unsigned p, uint64_t n) {
+  if (MODE < PR_NORM32) return 0.0;
+  const double d = pr_ld<PERSIST>(&ls->dangling[p]);
+  return (MODE == PR_NORM32 || MODE == PR_NORM64) ? d / (double)n : d;
 }
 
 // Applies the finished sum of target v; returns |change| for the FP64 residual.
@@ -151,6 +236,44 @@ __device__ __forceinline__ double pr_finish(const PrArgs& a, uint64_t v, double 
     rn[v] = nv;
     *rsum += nv;
     return d;
+  } else if (MODE == PR_W32 || MODE == PR_W64) {
+    const double tv = a.tele ? a.tele[v] : 1.0 / (double)a.n;
+    const double nv = tv * ((1.0 - a.alpha) + a.alpha * dang) + a.alpha * sum;
+    if (MODE == PR_W32) {
+      const float* r = (p == 0) ? a.rank : a.comp;
+      float* rn = (p == 0) ? a.comp : a.rank;
+      const float nf = (float)nv;
+      rn[v] = nf;
+      *rsum += (double)nf;
+      return fabs((double)nf - (double)pr_ld<PERSIST>(r + v));
+    } else {
+      const double* r = (p == 0) ? a.r64 : a.r64n;
+      double* rn = (p == 0) ? a.r64n : a.r64;
+      rn[v] = nv;
+      *rsum += nv;
+      return fabs(nv - pr_ld<PERSIST>(r + v));
+    }
+  } else if (MODE == PR_ADJ32 || MODE == PR_ADJ64) {
+    // v is a source here: lambda'_v = c_v + alpha ((P^T lambda)_v + a_v (t . lambda))
+    const double s = a.wsum[v];
+    const double ptv = s > 0.0 ? sum / s : 0.0;
+    const double nl = a.cvec[v] + a.alpha * (ptv + (s > 0.0 ? 0.0 : dang));
+    if (MODE == PR_ADJ32) {
+      const float* l = (p == 0) ? a.rank : a.comp;
+      float* ln = (p == 0) ? a.comp : a.rank;
+      const float nf = (float)nl;
+      ln[v] = nf;
+      a.pt[v] = (float)ptv;
+      *rsum += (double)nf;
+      return fabs((double)nf - (double)pr_ld<PERSIST>(l + v));
+    } else {
+      const double* l = (p == 0) ? a.r64 : a.r64n;
+      double* ln = (p == 0) ? a.r64n : a.r64;
+      ln[v] = nl;
+      a.pt64[v] = ptv;
+      *rsum += nl;
+      return fabs(nl - pr_ld<PERSIST>(l + v));
+    }
   } else {
     // PageRank-delta: residual round or delta round, rank += change (compensated)
     const float rank_v = pr_ld<PERSIST>(a.rank + v);
@@ -195,20 +318,20 @@ __device__ __forceinline__ void pr_flush(LoopState* ls, unsigned p, double resid
 template <int MODE, bool PERSIST>
 __device__ __forceinline__ double pr_sum_thread(const PrArgs& a, uint32_t v) {
   const uint32_t lo = a.csc_ptr[v], hi = a.csc_ptr[v + 1];
-  if constexpr (MODE == PR_NORM64) {
+  if constexpr (pr_is64<MODE>()) {
     Acc64 acc;
     acc.init();
     uint32_t e = lo;
     for (; e + 4 <= hi; e += 4) {
       const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + 1], s2 = a.csc_src[e + 2], s3 = a.csc_src[e + 3];
-      const double c0 = pr_ld<PERSIST>(a.contrib64 + s0), c1 = pr_ld<PERSIST>(a.contrib64 + s1),
-                   c2 = pr_ld<PERSIST>(a.contrib64 + s2), c3 = pr_ld<PERSIST>(a.contrib64 + s3);
+      const double c0 = pr_c64<MODE, PERSIST>(a, e, s0), c1 = pr_c64<MODE, PERSIST>(a, e + 1, s1),
+                   c2 = pr_c64<MODE, PERSIST>(a, e + 2, s2), c3 = pr_c64<MODE, PERSIST>(a, e + 3, s3);
       acc.add(c0);
       acc.add(c1);
       acc.add(c2);
       acc.add(c3);
     }
-    for (; e < hi; ++e) acc.add(pr_ld<PERSIST>(a.contrib64 + a.csc_src[e]));
+    for (; e < hi; ++e) acc.add(pr_c64<MODE, PERSIST>(a, e, a.csc_src[e]));
     return acc.value();
   } else {
     Acc32 acc;
@@ -216,14 +339,14 @@ __device__ __forceinline__ double pr_sum_thread(const PrArgs& a, uint32_t v) {
     uint32_t e = lo;
     for (; e + 4 <= hi; e += 4) {
       const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + 1], s2 = a.csc_src[e + 2], s3 = a.csc_src[e + 3];
-      const float c0 = pr_ld<PERSIST>(a.contrib + s0), c1 = pr_ld<PERSIST>(a.contrib + s1),
-                  c2 = pr_ld<PERSIST>(a.contrib + s2), c3 = pr_ld<PERSIST>(a.contrib + s3);
+      const float c0 = pr_c32<MODE, PERSIST>(a, e, s0), c1 = pr_c32<MODE, PERSIST>(a, e + 1, s1),
+                  c2 = pr_c32<MODE, PERSIST>(a, e + 2, s2), c3 = pr_c32<MODE, PERSIST>(a, e + 3, s3);
       acc.add(c0);
       acc.add(c1);
       acc.add(c2);
       acc.add(c3);
     }
-    for (; e < hi; ++e) acc.add(pr_ld<PERSIST>(a.contrib + a.csc_src[e]));
+    for (; e < hi; ++e) acc.add(pr_c32<MODE, PERSIST>(a, e, a.csc_src[e]));
     return (double)acc.s + (double)acc.e;
   }
 }
@@ -232,19 +355,19 @@ __device__ __forceinline__ double pr_sum_thread(const PrArgs& a, uint32_t v) {
 template <int MODE, bool PERSIST>
 __device__ __forceinline__ double pr_sum_warp(const PrArgs& a, uint32_t v, unsigned lane) {
   const uint32_t lo = a.csc_ptr[v], hi = a.csc_ptr[v + 1];
-  if constexpr (MODE == PR_NORM64) {
+  if constexpr (pr_is64<MODE>()) {
     double s = 0.0;
     uint32_t e = lo + lane;
     for (; e + 96 < hi; e += 128) {
       const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + 32], s2 = a.csc_src[e + 64], s3 = a.csc_src[e + 96];
-      const double c0 = pr_ld<PERSIST>(a.contrib64 + s0), c1 = pr_ld<PERSIST>(a.contrib64 + s1),
-                   c2 = pr_ld<PERSIST>(a.contrib64 + s2), c3 = pr_ld<PERSIST>(a.contrib64 + s3);
+      const double c0 = pr_c64<MODE, PERSIST>(a, e, s0), c1 = pr_c64<MODE, PERSIST>(a, e + 32, s1),
+                   c2 = pr_c64<MODE, PERSIST>(a, e + 64, s2), c3 = pr_c64<MODE, PERSIST>(a, e + 96, s3);
       s += c0;
       s += c1;
       s += c2;
       s += c3;
     }
-    for (; e < hi; e += 32) s += pr_ld<PERSIST>(a.contrib64 + a.csc_src[e]);
+    for (; e < hi; e += 32) s += pr_c64<MODE, PERSIST>(a, e, a.csc_src[e]);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
     return s;
@@ -254,14 +377,14 @@ __device__ __forceinline__ double pr_sum_warp(const PrArgs& a, uint32_t v, unsig
     uint32_t e = lo + lane;
     for (; e + 96 < hi; e += 128) {
       const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + 32], s2 = a.csc_src[e + 64], s3 = a.csc_src[e + 96];
-      const float c0 = pr_ld<PERSIST>(a.contrib + s0), c1 = pr_ld<PERSIST>(a.contrib + s1),
-                  c2 = pr_ld<PERSIST>(a.contrib + s2), c3 = pr_ld<PERSIST>(a.contrib + s3);
+      const float c0 = pr_c32<MODE, PERSIST>(a, e, s0), c1 = pr_c32<MODE, PERSIST>(a, e + 32, s1),
+                  c2 = pr_c32<MODE, PERSIST>(a, e + 64, s2), c3 = pr_c32<MODE, PERSIST>(a, e + 96, s3);
       acc.add(c0);
       acc.add(c1);
       acc.add(c2);
       acc.add(c3);
     }
-    for (; e < hi; e += 32) acc.add(pr_ld<PERSIST>(a.contrib + a.csc_src[e]));
+    for (; e < hi; e += 32) acc.add(pr_c32<MODE, PERSIST>(a, e, a.csc_src[e]));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       const float s2 = __shfl_xor_sync(0xFFFFFFFFu, acc.s, o);
@@ -281,20 +404,21 @@ __device__ __forceinline__ double pr_sum_block(const PrArgs& a, uint32_t v) {
   const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const uint32_t lo = a.csc_ptr[v], hi = a.csc_ptr[v + 1];
   double sum = 0.0;
-  if constexpr (MODE == PR_NORM64) {
+  if constexpr (pr_is64<MODE>()) {
     double s = 0.0;
     uint32_t e = lo + threadIdx.x;
     for (; e + 3 * PR_BLOCK_T < hi; e += 4 * PR_BLOCK_T) {
       const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + PR_BLOCK_T], s2 = a.csc_src[e + 2 * PR_BLOCK_T],
                      s3 = a.csc_src[e + 3 * PR_BLOCK_T];
-      const double c0 = pr_ld<PERSIST>(a.contrib64 + s0), c1 = pr_ld<PERSIST>(a.contrib64 + s1),
-                   c2 = pr_ld<PERSIST>(a.contrib64 + s2), c3 = pr_ld<PERSIST>(a.contrib64 + s3);
+      const double c0 = pr_c64<MODE, PERSIST>(a, e, s0), c1 = pr_c64<MODE, PERSIST>(a, e + PR_BLOCK_T, s1),
+                   c2 = pr_c64<MODE, PERSIST>(a, e + 2 * PR_BLOCK_T, s2),
+                   c3 = pr_c64<MODE, PERSIST>(a, e + 3 * PR_BLOCK_T, s3);
       s += c0;
       s += c1;
       s += c2;
       s += c3;
     }
-    for (; e < hi; e += PR_BLOCK_T) s += pr_ld<PERSIST>(a.contrib64 + a.csc_src[e]);
+    for (; e < hi; e += PR_BLOCK_T) s += pr_c64<MODE, PERSIST>(a, e, a.csc_src[e]);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
     if (lane == 0) s_d[wid] = s;
@@ -309,14 +433,15 @@ __device__ __forceinline__ double pr_sum_block(const PrArgs& a, uint32_t v) {
     for (; e + 3 * PR_BLOCK_T < hi; e += 4 * PR_BLOCK_T) {
       const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + PR_BLOCK_T], s2 = a.csc_src[e + 2 * PR_BLOCK_T],
                      s3 = a.csc_src[e + 3 * PR_BLOCK_T];
-      const float c0 = pr_ld<PERSIST>(a.contrib + s0), c1 = pr_ld<PERSIST>(a.contrib + s1),
-                  c2 = pr_ld<PERSIST>(a.contrib + s2), c3 = pr_ld<PERSIST>(a.contrib + s3);
+      const float c0 = pr_c32<MODE, PERSIST>(a, e, s0), c1 = pr_c32<MODE, PERSIST>(a, e + PR_BLOCK_T, s1),
+                  c2 = pr_c32<MODE, PERSIST>(a, e + 2 * PR_BLOCK_T, s2),
+                  c3 = pr_c32<MODE, PERSIST>(a, e + 3 * PR_BLOCK_T, s3);
       acc.add(c0);
       acc.add(c1);
       acc.add(c2);
       acc.add(c3);
     }
-    for (; e < hi; e += PR_BLOCK_T) acc.add(pr_ld<PERSIST>(a.contrib + a.csc_src[e]));
+    for (; e < hi; e += PR_BLOCK_T) acc.add(pr_c32<MODE, PERSIST>(a, e, a.csc_src[e]));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       const float s2 = __shfl_xor_sync(0xFFFFFFFFu, acc.s, o);
@@ -363,7 +488,7 @@ __device__ __forceinline__ unsigned pr_control_step(LoopState* ls_, int mode) {
       more = more && resid > ls->tol;
       // FP32 ranks cannot change by less than their rounding floor (about 6e-8 of the rank
       // mass per round); once the FP64-measured change stops shrinking, the run is done
-      if (mode == PR_NORM32) {
+      if (mode == PR_NORM32 || mode == PR_W32 || mode == PR_ADJ32) {
         if (resid < ls->best_resid * 0.999) {
           ls->best_resid = resid;
           ls->stall = 0;

@@ -171,6 +171,17 @@ class Engine:
         self._check(self.lib.cytom_insert_batch(self.ctx, src_addr, tgt_addr, w_addr, count,
                                                 L.PTR_DEVICE))
 
+    def set_edge_weights(self, src, tgt, w):
+        """Overwrites the weights of stored edges (uint32 values or float32 bit patterns)."""
+        src = np.ascontiguousarray(src, np.uint32)
+        tgt = np.ascontiguousarray(tgt, np.uint32)
+        w = np.ascontiguousarray(w)
+        if w.dtype == np.float32:
+            w = w.view(np.uint32)
+        w = np.ascontiguousarray(w, np.uint32)
+        self._check(self.lib.cytom_set_edge_weights(self.ctx, src.ctypes.data, tgt.ctypes.data, w.ctypes.data,
+                                                    len(src), L.PTR_HOST))
+
     def do_global_compaction(self):
         self._check(self.lib.cytom_compact(self.ctx))
 
@@ -318,3 +329,30 @@ class PageRank(Program):
     """Normalised PageRank with dangling redistribution (FP32 + Kahan or FP64 plain)."""
     ALGO = L.ALGO_PAGERANK
     result_dtype = np.float32
+
+
+class WeightedPageRank(Program):
+    """PageRank over raw float edge weights normalised per source, teleport vector t
+    (uniform unless set), differentiable through its adjoint."""
+    ALGO = L.ALGO_WPAGERANK
+    result_dtype = np.float32
+
+    def set_teleport(self, t=None):
+        if t is None:
+            self.engine._check(self.engine.lib.cytom_job_set_teleport(self.engine.ctx, self.job, None, L.PTR_HOST))
+            return
+        t = np.ascontiguousarray(t, np.float64)
+        self.engine._check(self.engine.lib.cytom_job_set_teleport(self.engine.ctx, self.job, t.ctypes.data,
+                                                                  L.PTR_HOST))
+
+    def adjoint(self, c):
+        """dL/d(edge weights) in store order and dL/d(teleport) for L = c . r."""
+        c = np.ascontiguousarray(c, np.float64)
+        E = self.engine.count_edges()[0]
+        gw = np.empty(E, np.float32)
+        gt = np.empty(self.engine.n, np.float32)
+        st = L.RunStats()
+        self.engine._check(self.engine.lib.cytom_pagerank_adjoint(
+            self.engine.ctx, self.job, c.ctypes.data, L.PTR_HOST, gw.ctypes.data, gt.ctypes.data, L.PTR_HOST,
+            C.byref(st)))
+        return gw, gt, st.as_dict()

@@ -55,6 +55,12 @@ extern "C" {
 #define CYTOM_ALGO_SSSP 2
 #define CYTOM_ALGO_PR_DELTA 3
 #define CYTOM_ALGO_PAGERANK 4
+/* Weighted PageRank on a CYTOM_WEIGHT_F32 store (no counterpart in the reference, whose
+ * pullGatherWeighted is "not applicable", examples/pagerank.cc:98): raw edge weights
+ * normalised per source, teleport vector t (uniform unless set), dangling mass sent
+ * along t: r = (1-alpha) t + alpha (P r + D t). FP32 + compensated sums (kahan = 1)
+ * or FP64 plain; FP64 L1 residual. Differentiable: cytom_pagerank_adjoint. */
+#define CYTOM_ALGO_WPAGERANK 5
 
 /* Context configuration: the subset of ConfigContext (src/include/util/config.h:529-567)
  * and its command-line flags (src/include/core/jobs.h:176-216) that the hot path uses. */
@@ -212,6 +218,34 @@ int cytom_batch_units(const cytom_ctx* ctx, uint64_t* units);
 int cytom_get_result(cytom_ctx* ctx, int job_id, void* out, int where);
 /* FP64 ranks of a PAGERANK job run with kahan = 0 (the FP64 plain form). */
 int cytom_get_result_f64(cytom_ctx* ctx, int job_id, double* out, int where);
+
+/* ---- Weighted PageRank: teleport, adjoint, weight updates --------------- */
+
+/* Sets the teleport vector of a WPAGERANK job (`vertices` doubles, host or device;
+ * NULL restores the uniform 1/n). A fresh run starts from t. */
+int cytom_job_set_teleport(cytom_ctx* ctx, int job_id, const double* teleport, int where);
+
+/* Adjoint of L = sum_v c_v r_v at the converged ranks r of WPAGERANK job `job_id` (run it
+ * first; its converged rank vector is the only state kept from the forward). Solves the
+ * transposed fixed point lambda = c + alpha (P^T lambda + a (t . lambda)) (a_u = 1 for
+ * vertices without out-weight) over the store's edges in source-major orientation, in
+ * the job's precision, to an L1 change <= tolerance * |c|_1, then writes
+ *   d_weights[e]  = dL/dw_e for every stored edge e = u->k, in the order of
+ *                   cytom_get_tiles: alpha r_u / s_u (lambda_k - (P^T lambda)_u)
+ *                   (w_e the raw weight, s_u = sum of u's out-weights);
+ *   d_teleport[v] = dL/dt_v = ((1-alpha) + alpha D) lambda_v.
+ * c: `vertices` doubles (c_where); outputs (out_where) may be NULL to skip.
+ * stats: the adjoint's rounds, residual and device time. No counterpart in the reference. */
+int cytom_pagerank_adjoint(cytom_ctx* ctx, int job_id, const double* c_weights, int c_where,
+                           float* d_weights, float* d_teleport, int out_where, cytom_run_stats* stats);
+
+/* Overwrites the weights of stored edges (src[i], tgt[i]) with w[i] (uint32, or float
+ * bits in a CYTOM_WEIGHT_F32 store), after compacting pending edges: the weight carried
+ * by the reference's Edge (mutate_weight, src/include/edge-inserter/i-edge-provider.h:88)
+ * changed in place. Weight-dependent state is rebuilt; SSSP jobs restart from scratch on
+ * their next run. An edge that is not stored is CYTOM_ERR_RANGE (the others are updated). */
+int cytom_set_edge_weights(cytom_ctx* ctx, const uint32_t* src, const uint32_t* tgt, const uint32_t* w,
+                           uint64_t count, int where);
 
 /* ---- Allocation-free batch compaction ---------------------------------- */
 

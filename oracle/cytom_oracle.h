@@ -98,6 +98,21 @@ uint64_t orc_pagerank_unnorm_f64(const orc_store* s, double alpha, double tol,
 uint64_t orc_pagerank_norm_f64(const orc_store* s, double alpha, double tol,
                                uint64_t max_iter, double* r);
 
+/* Weighted PageRank with teleport vector t (NULL = uniform 1/n), dangling mass sent
+ * along t, FP64, over m edges given as arrays (raw weights w, normalised per source):
+ * r = (1-alpha) t + alpha (P r + D t), P[v,u] = w_uv / s_u. Stops at an L1 change
+ * <= tol. Returns iterations. The reference has no weighted PageRank. */
+uint64_t orc_wpagerank_f64(uint64_t n, uint64_t m, const uint32_t* src, const uint32_t* tgt,
+                           const double* w, const double* t, double alpha, double tol,
+                           uint64_t max_iter, double* r);
+/* Adjoint of L = c . r at the fixed point r: lambda = c + alpha (P^T lambda + a (t . lambda))
+ * (L1 change <= tol * |c|_1), then dL/dw for every edge (g_w, in the arrays' order) and
+ * dL/dt (g_t); either may be NULL. Returns iterations. */
+uint64_t orc_wpagerank_adjoint_f64(uint64_t n, uint64_t m, const uint32_t* src, const uint32_t* tgt,
+                                   const double* w, const double* t, double alpha, double tol,
+                                   uint64_t max_iter, const double* r, const double* c,
+                                   double* lambda, double* g_w, double* g_t);
+
 #ifdef __cplusplus
 }
 #endif

@@ -70,6 +70,11 @@ def lib() -> C.CDLL:
         L.orc_pagerank_unnorm_f64.argtypes = [vp, C.c_double, C.c_double, u64, vp]
         L.orc_pagerank_norm_f64.restype = u64
         L.orc_pagerank_norm_f64.argtypes = [vp, C.c_double, C.c_double, u64, vp]
+        L.orc_wpagerank_f64.restype = u64
+        L.orc_wpagerank_f64.argtypes = [u64, u64, vp, vp, vp, vp, C.c_double, C.c_double, u64, vp]
+        L.orc_wpagerank_adjoint_f64.restype = u64
+        L.orc_wpagerank_adjoint_f64.argtypes = [u64, u64, vp, vp, vp, vp, C.c_double, C.c_double, u64,
+                                                vp, vp, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -180,3 +185,54 @@ class Store:
         r = np.empty(self.n, np.float64)
         it = lib().orc_pagerank_norm_f64(self.h, alpha, tol, max_iter, r.ctypes.data)
         return r, it
+
+
+def _vp(a):
+    return None if a is None else a.ctypes.data
+
+
+def wpagerank(n, src, tgt, w, t=None, alpha=0.85, tol=1e-15, max_iter=100000):
+    """FP64 weighted PageRank over edge arrays (raw weights, normalised per source)."""
+    src = np.ascontiguousarray(src, np.uint32)
+    tgt = np.ascontiguousarray(tgt, np.uint32)
+    w = np.ascontiguousarray(w, np.float64)
+    t = None if t is None else np.ascontiguousarray(t, np.float64)
+    r = np.empty(n, np.float64)
+    it = lib().orc_wpagerank_f64(n, len(src), src.ctypes.data, tgt.ctypes.data, w.ctypes.data, _vp(t),
+                                 alpha, tol, max_iter, r.ctypes.data)
+    return r, it
+
+
+def wpagerank_adjoint(n, src, tgt, w, r, c, t=None, alpha=0.85, tol=1e-15, max_iter=100000):
+    """FP64 adjoint of L = c . r: (lambda, dL/dw per edge, dL/dt, iterations)."""
+    src = np.ascontiguousarray(src, np.uint32)
+    tgt = np.ascontiguousarray(tgt, np.uint32)
+    w = np.ascontiguousarray(w, np.float64)
+    t = None if t is None else np.ascontiguousarray(t, np.float64)
+    r = np.ascontiguousarray(r, np.float64)
+    c = np.ascontiguousarray(c, np.float64)
+    lam = np.empty(n, np.float64)
+    gw = np.empty(len(src), np.float64)
+    gt = np.empty(n, np.float64)
+    it = lib().orc_wpagerank_adjoint_f64(n, len(src), src.ctypes.data, tgt.ctypes.data, w.ctypes.data, _vp(t),
+                                         alpha, tol, max_iter, r.ctypes.data, c.ctypes.data, lam.ctypes.data,
+                                         gw.ctypes.data, gt.ctypes.data)
+    return lam, gw, gt, it
+
+
+def store_edges(store):
+    """(src, tgt, w_bits) global arrays of a compacted store, in tile (store) order."""
+    tp, ed, wt, _ = store.dump()
+    T = store.n // store.vpt
+    lv = store.vpt.bit_length() - 1
+    tiles = np.repeat(np.arange(len(tp) - 1, dtype=np.uint64), np.diff(tp).astype(np.int64))
+    x, y = tiles // T, tiles % T
+    src = ((x << np.uint64(lv)) | (ed >> 16).astype(np.uint64)).astype(np.uint32)
+    tgt = ((y << np.uint64(lv)) | (ed & 0xFFFF).astype(np.uint64)).astype(np.uint32)
+    return src, tgt, wt
+
+
+def unit_weights(src, tgt, wseed):
+    """FP32 edge weights uniform in [0.1, 1.0], a function of (src, tgt) (duplicates agree)."""
+    q = edge_weights(src, tgt, wseed, 0, (1 << 24) - 1).astype(np.float64)
+    return (0.1 + 0.9 * q / float((1 << 24) - 1)).astype(np.float32)

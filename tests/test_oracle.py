@@ -249,3 +249,53 @@ def test_prdelta_ref_converges_toward_fixed_point(orc):
     r64, _ = st.pagerank_unnorm()
     rel = np.abs(rank - r64).sum() / r64.sum()
     assert rel < 1e-5, rel
+
+
+def _wgraph(orc, scale, vpt, seed, wseed, ef=8):
+    n = 1 << scale
+    s, t = orc.rmat(scale, 0, ef * n, seed)
+    w = orc.unit_weights(s, t, wseed)
+    st = orc.Store(n, vpt, True)
+    st.insert(s, t, w.view(np.uint32))
+    st.compact()
+    src, tgt, wb = orc.store_edges(st)
+    return n, st, src, tgt, wb.view(np.float32).astype(np.float64)
+
+
+def test_wpagerank_fixed_point_and_mass(orc):
+    n, st, src, tgt, w = _wgraph(orc, 10, 256, 4, 7)
+    assert ((w >= 0.1) & (w <= 1.0)).all()
+    r, it = orc.wpagerank(n, src, tgt, w, tol=1e-15)
+    assert abs(r.sum() - 1.0) < 1e-12
+    # one more application of the map leaves r unchanged
+    s = np.bincount(src, weights=w, minlength=n)
+    acc = np.bincount(tgt, weights=w / s[src] * r[src], minlength=n)
+    dang = r[s == 0].sum()
+    r2 = 0.15 / n + 0.85 * (acc + dang / n)
+    assert np.abs(r2 - r).sum() < 1e-13
+
+
+def test_wpagerank_adjoint_matches_central_differences(orc):
+    # the FP64 adjoint against FP64 central differences (eps 1e-3 on raw weights)
+    n, st, src, tgt, w = _wgraph(orc, 10, 256, 4, 7)
+    r, _ = orc.wpagerank(n, src, tgt, w, tol=1e-16)
+    c = np.random.default_rng(5).standard_normal(n)
+    lam, gw, gt, _ = orc.wpagerank_adjoint(n, src, tgt, w, r, c, tol=1e-16)
+    rng = np.random.default_rng(9)
+    scale_w = np.abs(gw).max()
+    eps = 1e-3
+    for e in rng.choice(len(src), 12, replace=False):
+        wp, wm = w.copy(), w.copy()
+        wp[e] += eps
+        wm[e] -= eps
+        fd = (c @ orc.wpagerank(n, src, tgt, wp, tol=1e-16)[0] - c @ orc.wpagerank(n, src, tgt, wm, tol=1e-16)[0]) / (2 * eps)
+        assert abs(fd - gw[e]) <= 1e-4 * max(abs(fd), 1e-2 * scale_w), (e, fd, gw[e])
+    # teleport: perturb one entry of the (unnormalised) teleport vector
+    t0 = np.full(n, 1.0 / n)
+    et = 1e-7
+    for v in rng.choice(n, 6, replace=False):
+        tp, tm = t0.copy(), t0.copy()
+        tp[v] += et
+        tm[v] -= et
+        fd = (c @ orc.wpagerank(n, src, tgt, w, t=tp, tol=1e-16)[0] - c @ orc.wpagerank(n, src, tgt, w, t=tm, tol=1e-16)[0]) / (2 * et)
+        assert abs(fd - gt[v]) <= 1e-4 * max(abs(fd), 1e-2 * np.abs(gt).max()), (v, fd, gt[v])

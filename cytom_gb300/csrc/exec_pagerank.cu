@@ -873,13 +873,15 @@ int pagerank_adjoint(Ctx* c, Job* j, const double* cv, int cwhere, float* d_w, f
   if (e != cudaSuccess) return cuda_err(c, e, "adjoint run");
   const unsigned pa = als.iter & 1u;  // buffer holding the newest lambda
   // gradients into device scratch, then to the caller
+  // layout (256-byte aligned regions): D (one double), dL/dw (E floats), dL/dt (n floats)
   char* tmp = nullptr;
-  const size_t wbytes = std::max<uint64_t>(E, 1) * 4, tbytes = n * 4;
-  if (cudaMallocAsync((void**)&tmp, wbytes + tbytes + 16, c->stream) != cudaSuccess)
+  auto align256 = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t wbytes = align256(std::max<uint64_t>(E, 1) * 4), tbytes = align256(n * 4);
+  if (cudaMallocAsync((void**)&tmp, 256 + wbytes + tbytes, c->stream) != cudaSuccess)
     return set_err(c, CYTOM_ERR_OOM, "adjoint outputs");
-  float* gw = (owhere == CYTOM_PTR_DEVICE && d_w) ? d_w : (float*)tmp;
-  float* gt = (owhere == CYTOM_PTR_DEVICE && d_t) ? d_t : (float*)(tmp + wbytes);
-  double* dang = (double*)(tmp + wbytes + tbytes);
+  double* dang = (double*)tmp;
+  float* gw = (owhere == CYTOM_PTR_DEVICE && d_w) ? d_w : (float*)(tmp + 256);
+  float* gt = (owhere == CYTOM_PTR_DEVICE && d_t) ? d_t : (float*)(tmp + 256 + wbytes);
   cudaMemsetAsync(dang, 0, 8, c->stream);
   if (f32) {
     const float* lam = (pa == 0) ? s->lam : s->lam + n;

@@ -102,3 +102,28 @@ def test_set_edge_weights(cg, orc):
         v = next(v for v in range(n) if v not in present)
         with pytest.raises(cg.CytomError):
             eng.set_edge_weights(np.array([0], np.uint32), np.array([v], np.uint32), np.array([1.0], np.float32))
+
+
+def test_adjoint_odd_edge_count(cg, orc):
+    # an odd number of stored edges (scratch regions after E floats must stay aligned)
+    n, vpt = 64, 32
+    src = np.array([0, 1, 2, 2, 5, 40, 41], np.uint32)
+    tgt = np.array([1, 2, 0, 33, 40, 41, 5], np.uint32)
+    w = np.array([0.5, 0.25, 1.0, 0.75, 0.3, 0.9, 0.6], np.float32)
+    with cg.Engine(n, vpt, weight_type=cg.WEIGHT_F32) as eng:
+        eng.insert_edges(src, tgt, w.view(np.uint32))
+        eng.do_global_compaction()
+        assert eng.count_edges()[0] % 2 == 1
+        st = orc.Store(n, vpt, True)
+        st.insert(src, tgt, w.view(np.uint32))
+        st.compact()
+        s2, t2, wb = orc.store_edges(st)
+        w2 = wb.view(np.float32).astype(np.float64)
+        c = np.random.default_rng(1).standard_normal(n)
+        r_ref, _ = orc.wpagerank(n, s2, t2, w2, tol=1e-16)
+        _, gw_ref, gt_ref, _ = orc.wpagerank_adjoint(n, s2, t2, w2, r_ref, c, tol=1e-16)
+        p = cg.WeightedPageRank(eng, max_iterations=2000, tolerance=1e-14, kahan=False)
+        p.execute_algorithm()
+        gw, gt, _ = p.adjoint(c)
+        assert np.abs(gw - gw_ref).max() <= GRAD_TOL * np.abs(gw_ref).max()
+        assert np.abs(gt - gt_ref).max() <= GRAD_TOL * np.abs(gt_ref).max()

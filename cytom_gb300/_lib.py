@@ -84,6 +84,20 @@ class KernelStats(C.Structure):
     ]
 
 
+class TuneReport(C.Structure):
+    _fields_ = [("variants", C.c_int32), ("chosen", C.c_int32 * 2), ("edges_per_thread", C.c_int32 * 8),
+                ("pipeline_depth", C.c_int32 * 8), ("blocks_per_sm", C.c_int32 * 8), ("reserved", C.c_int32),
+                ("us", (C.c_double * 8) * 2), ("tuned_edges", C.c_uint64)]
+
+    def as_dict(self) -> dict:
+        k = self.variants
+        shapes = [{"edges_per_thread": self.edges_per_thread[v], "pipeline_depth": self.pipeline_depth[v],
+                   "blocks_per_sm": self.blocks_per_sm[v]} for v in range(k)]
+        return {"shapes": shapes, "chosen": {"bfs_cc": self.chosen[0], "sssp": self.chosen[1]},
+                "round_us": {"bfs_cc": [self.us[0][v] for v in range(k)], "sssp": [self.us[1][v] for v in range(k)]},
+                "tuned_edges": self.tuned_edges}
+
+
 # (name, restype, argtypes) of every exported entry point of include/cytom_gpu.h
 SIGNATURES = [
     ("cytom_config_default", None, [C.POINTER(Config)]),
@@ -116,6 +130,8 @@ SIGNATURES = [
     ("cytom_set_edge_weights", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int]),
     ("cytom_get_result", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
     ("cytom_get_result_f64", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
+    ("cytom_autotune", C.c_int, [C.c_void_p, C.POINTER(TuneReport)]),
+    ("cytom_get_tune_report", C.c_int, [C.c_void_p, C.POINTER(TuneReport)]),
     ("cytom_set_profiling", C.c_int, [C.c_void_p, C.c_int]),
     ("cytom_get_kernel_stats", C.c_int, [C.c_void_p, C.POINTER(KernelStats)]),
     ("cytom_reset_kernel_stats", C.c_int, [C.c_void_p]),

@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -184,12 +185,24 @@ int job_seed(Ctx* c, Job* j, const uint32_t* src, const uint32_t* tgt, const uin
                              : pagerank_seed(c, j, src, tgt, w, count);
 }
 
+// The streaming gather is tuned once per context, on the first run at >= 2^20 edges
+// (cytom_autotune re-tunes on demand; CYTOM_AUTOTUNE=0 keeps the default shapes).
+static bool autotune_due(Ctx* c) {
+  static int env = -1;
+  if (env < 0) {
+    const char* s = getenv("CYTOM_AUTOTUNE");
+    env = (s && s[0] == '0') ? 0 : 1;
+  }
+  return env && !c->profiling && c->tune_E == 0 && c->E >= (1ULL << 20);
+}
+
 int job_run(Ctx* c, Job* j, cytom_run_stats* st) {
   int rc = compact(c);
   if (rc) return rc;
   if (is_minprop(j->algo)) {
     rc = build_directory(c);
     if (!rc) rc = ensure_job_queue(c, j);
+    if (!rc && autotune_due(c)) rc = minprop_autotune(c);
     if (rc) return rc;
   }
   if (j->fresh) {
@@ -687,6 +700,35 @@ int cytom_set_edge_weights(cytom_ctx* ctx, const uint32_t* src, const uint32_t* 
   cudaMemcpyAsync(ds + count, tgt, count * 4, cudaMemcpyHostToDevice, c->stream);
   cudaMemcpyAsync(ds + 2 * count, w, count * 4, cudaMemcpyHostToDevice, c->stream);
   return set_edge_weights(c, ds, ds + count, ds + 2 * count, count);
+}
+
+static void fill_tune_report(const Ctx* c, cytom_tune_report* out) {
+  memset(out, 0, sizeof(*out));
+  int cnt = 0;
+  sg_shapes(out->edges_per_thread, out->pipeline_depth, out->blocks_per_sm, &cnt);
+  out->variants = cnt;
+  out->chosen[0] = c->sg_variant[0];
+  out->chosen[1] = c->sg_variant[1];
+  for (int k = 0; k < 2; ++k)
+    for (int v = 0; v < cnt && v < 8; ++v) out->us[k][v] = c->tune_us[k][v];
+  out->tuned_edges = c->tune_E;
+}
+
+int cytom_autotune(cytom_ctx* ctx, cytom_tune_report* out) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c) return CYTOM_ERR_INVAL;
+  int rc = compact(c);
+  if (!rc) rc = minprop_autotune(c);
+  if (rc) return rc;
+  if (out) fill_tune_report(c, out);
+  return CYTOM_OK;
+}
+
+int cytom_get_tune_report(const cytom_ctx* ctx, cytom_tune_report* out) {
+  const Ctx* c = (const Ctx*)ctx;
+  if (!c || !out) return CYTOM_ERR_INVAL;
+  fill_tune_report(c, out);
+  return CYTOM_OK;
 }
 
 int cytom_get_result_f64(cytom_ctx* ctx, int job_id, double* out, int where) {

@@ -114,6 +114,7 @@ struct Job {
   cudaGraphExec_t loop_exec = nullptr;
   bool graph_failed = false;
   bool last_run_graph = false;  // the last run went through the graph (launch accounting)
+  uint64_t graph_epoch = 0;     // tune epoch the captured graph was built with
   void* ext = nullptr;          // per-algorithm state (PageRank family)
 };
 
@@ -165,6 +166,12 @@ struct Ctx {
   void* batch = nullptr;
   uint64_t batch_units = 0;
   // PageRank family: the snapshot's CSC, shared by the context's PageRank jobs
+  // autotuner: streaming-gather variant per program class (0: BFS / CC, 1: SSSP),
+  // the edge count it was tuned at, and an epoch that invalidates captured graphs
+  int sg_variant[2] = {0, 0};
+  uint64_t tune_E = 0;
+  uint64_t tune_epoch = 0;
+  double tune_us[2][8] = {};
   void* pr_csc = nullptr;
   void* pr_wgraph = nullptr;  // weighted PageRank: CSC + CSR with weights
 };
@@ -202,6 +209,8 @@ int job_seed(Ctx* c, Job* j, const uint32_t* src, const uint32_t* tgt, const uin
 int job_run(Ctx* c, Job* j, cytom_run_stats* st);
 int job_result(Ctx* c, Job* j, void* out, int where);
 int ensure_job_queue(Ctx* c, Job* j);
+int minprop_autotune(Ctx* c);
+void sg_shapes(int* ept, int* nst, int* minb, int* count);
 void batch_free(Ctx* c);
 void pagerank_ctx_free(Ctx* c);
 

@@ -179,33 +179,34 @@ __global__ void __launch_bounds__(GATHER_T) gather_minprop_kernel(const JobDesc*
 }
 
 // Streaming gather: the same round as gather_minprop_kernel, with the edge array
-// (and weights) streamed through shared memory by bulk copies (cp.async.bulk) in a
-// SG_NST-deep mbarrier pipeline, so each SM keeps tens of KB of HBM reads in
-// flight while its threads resolve the dependent frontier / value / atomic loads of
-// 16 edges each in batches.
-//  - Stages are 4096-edge slices of the tile-major edge array. A block owns groups
-//    of SG_GROUP consecutive stages (group g, g + gridDim.x, ...), so consecutive
-//    stages of a block usually lie in one tile row and its frontier words stay in L1.
+// (and weights) streamed through shared memory by bulk copies (cp.async.bulk) in an
+// NST-deep mbarrier pipeline, so each SM keeps tens of KB of HBM reads in flight while
+// its threads resolve the dependent frontier / value / atomic loads of EPT edges each
+// in batches.
+//  - Stages are SG_T * EPT-edge slices of the tile-major edge array. A block owns
+//    groups of 128 / EPT consecutive stages (group g, g + gridDim.x, ...), so
+//    consecutive stages of a block usually lie in one tile row and its frontier words
+//    stay in L1.
 //  - A stage whose tile rows are all inactive is skipped without being copied.
 //  - Single-row stages (the common case at large vertices-per-tile) take the source
 //    row from the stage: the frontier test needs no per-edge tile lookup, and only
 //    edges with an active source look up their target tile.
-constexpr int SG_NST = 3;
-constexpr int SG_GROUP = 8;
-
-template <int ALGO>
+// The shape (EPT, NST, blocks per SM) is a variant picked by the autotuner.
+template <int ALGO, int EPT, int NST>
 __host__ __device__ constexpr size_t gather_stream_smem() {
-  return (size_t)SG_NST * SG_E * 4 * (ALGO == 2 ? 2 : 1) + SG_NST * sizeof(uint64_t);
+  return (size_t)NST * SG_T * EPT * 4 * (ALGO == 2 ? 2 : 1) + NST * sizeof(uint64_t);
 }
 
-template <int ALGO>
-__global__ void __launch_bounds__(SG_T, 2) gather_stream_kernel(const JobDesc* __restrict__ jd,
-                                                                 const StoreDesc* __restrict__ sd,
-                                                                 int adaptive) {
+template <int ALGO, int EPT, int NST, int MINB>
+__global__ void __launch_bounds__(SG_T, MINB) gather_stream_kernel(const JobDesc* __restrict__ jd,
+                                                                    const StoreDesc* __restrict__ sd,
+                                                                    int adaptive) {
+  constexpr uint32_t SE = SG_T * EPT;
+  constexpr int SG_GROUP = 128 / EPT;
   extern __shared__ __align__(128) uint8_t smem_raw[];
   uint32_t* ebuf = reinterpret_cast<uint32_t*>(smem_raw);
-  uint32_t* wbuf = ebuf + SG_NST * SG_E;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + (size_t)SG_NST * SG_E * 4 * (ALGO == 2 ? 2 : 1));
+  uint32_t* wbuf = ebuf + NST * SE;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + (size_t)NST * SE * 4 * (ALGO == 2 ? 2 : 1));
 
   LoopState* ls = jd->ls;
   if (!ls->cont || ls->mode != 0) return;
@@ -215,7 +216,7 @@ __global__ void __launch_bounds__(SG_T, 2) gather_stream_kernel(const JobDesc* _
   const uint32_t* __restrict__ edges = sd->edges;
   const uint32_t* __restrict__ wts = sd->wts;
   const uint64_t E = sd->E;
-  const uint64_t nst = (E + SG_E - 1) / SG_E;
+  const uint64_t nst = (E + SE - 1) / SE;
   const uint64_t G = gridDim.x;
 
   // the block's stage sequence: groups blockIdx.x, blockIdx.x + G, ... of SG_GROUP stages
@@ -225,43 +226,50 @@ __global__ void __launch_bounds__(SG_T, 2) gather_stream_kernel(const JobDesc* _
     return (s / SG_GROUP + G) * SG_GROUP;
   };
   auto next_active = [&](uint64_t s) -> uint64_t {
-    while (s < nst && !stage_active<false>(jd, sd, s, p, adaptive)) s = advance(s);
+    while (s < nst && !stage_active<false, EPT>(jd, sd, s, p, adaptive)) s = advance(s);
     return s < nst ? s : nst;
   };
   auto issue = [&](int slot, uint64_t s) {
-    const uint64_t e0 = s * SG_E;
+    const uint64_t e0 = s * SE;
     const uint64_t rem = E - e0;
-    const uint32_t cnt = rem < (uint64_t)SG_E ? (uint32_t)rem : (uint32_t)SG_E;
+    const uint32_t cnt = rem < (uint64_t)SE ? (uint32_t)rem : SE;
     const uint32_t bytes = ((cnt + 3u) & ~3u) * 4u;
     fence_proxy_async_smem();
     mbar_arrive_expect_tx(&bar[slot], bytes * (ALGO == 2 ? 2u : 1u));
-    bulk_g2s(ebuf + slot * SG_E, edges + e0, bytes, &bar[slot]);
-    if (ALGO == 2) bulk_g2s(wbuf + slot * SG_E, wts + e0, bytes, &bar[slot]);
+    bulk_g2s(ebuf + slot * SE, edges + e0, bytes, &bar[slot]);
+    if (ALGO == 2) bulk_g2s(wbuf + slot * SE, wts + e0, bytes, &bar[slot]);
   };
 
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int k = 0; k < SG_NST; ++k) mbar_init(&bar[k], 1);
+    for (int k = 0; k < NST; ++k) mbar_init(&bar[k], 1);
     fence_mbar_init();
   }
   __syncthreads();
 
-  const uint64_t first = (uint64_t)blockIdx.x * SG_GROUP;
-  uint64_t st0 = next_active(first < nst ? first : nst);
-  uint64_t st1 = (st0 < nst) ? next_active(advance(st0)) : nst;
-  uint64_t st2 = (st1 < nst) ? next_active(advance(st1)) : nst;
-  if (threadIdx.x == 0) {
-    if (st0 < nst) issue(0, st0);
-    if (st1 < nst) issue(1, st1);
-    if (st2 < nst) issue(2, st2);
+  // stq[k]: the stage in slot (slot + k) % NST, k = 0 the one consumed next
+  uint64_t stq[NST];
+  {
+    const uint64_t first = (uint64_t)blockIdx.x * SG_GROUP;
+    uint64_t s0 = next_active(first < nst ? first : nst);
+#pragma unroll
+    for (int k = 0; k < NST; ++k) {
+      stq[k] = s0;
+      if (s0 < nst) s0 = next_active(advance(s0));
+    }
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int k = 0; k < NST; ++k)
+        if (stq[k] < nst) issue(k, stq[k]);
+    }
   }
-  uint64_t s_next = (st2 < nst) ? next_active(advance(st2)) : nst;
+  uint64_t s_next = (stq[NST - 1] < nst) ? next_active(advance(stq[NST - 1])) : nst;
   uint32_t phases = 0;  // bit k: parity to wait for on slot k
   int slot = 0;
   unsigned long long scanned = 0;
   bool failed = false;
 
-  while (st0 < nst) {
+  while (stq[0] < nst) {
     const bool ok = mbar_wait(&bar[slot], (phases >> slot) & 1u);
     if (!__syncthreads_and(ok)) {
       failed = true;
@@ -269,27 +277,26 @@ __global__ void __launch_bounds__(SG_T, 2) gather_stream_kernel(const JobDesc* _
     }
     phases ^= 1u << slot;
     if (threadIdx.x == 0) {
-      const uint64_t rem = E - st0 * SG_E;
-      scanned += rem < (uint64_t)SG_E ? rem : (uint64_t)SG_E;
+      const uint64_t rem = E - stq[0] * SE;
+      scanned += rem < (uint64_t)SE ? rem : (uint64_t)SE;
     }
-    dense_stage<ALGO, false, false>(jd, sd, ebuf + slot * SG_E, wbuf + slot * SG_E, st0, p, adaptive);
+    dense_stage<ALGO, false, false, EPT>(jd, sd, ebuf + slot * SE, wbuf + slot * SE, stq[0], p, adaptive);
     __syncthreads();  // every thread is done with this slot
     // refill the slot with the next stage of this block
     if (threadIdx.x == 0 && s_next < nst) issue(slot, s_next);
-    st0 = st1;
-    st1 = st2;
-    st2 = s_next;
+#pragma unroll
+    for (int k = 0; k + 1 < NST; ++k) stq[k] = stq[k + 1];
+    stq[NST - 1] = s_next;
     if (s_next < nst) s_next = next_active(advance(s_next));
-    slot = (slot + 1 == SG_NST) ? 0 : slot + 1;
+    slot = (slot + 1 == NST) ? 0 : slot + 1;
   }
   if (failed) {
     // give up: record the error, then wait (bounded) for the copies this block still has in flight
     if (threadIdx.x == 0) {
       atomicExch(&ls->err, 1u);
-      for (int k = 0; k < SG_NST; ++k) {
-        const uint64_t sk = (k == 0) ? st0 : (k == 1 ? st1 : st2);
-        const int sl = (slot + k) % SG_NST;
-        if (sk < nst) mbar_wait(&bar[sl], (phases >> sl) & 1u);
+      for (int k = 0; k < NST; ++k) {
+        const int sl = (slot + k) % NST;
+        if (stq[k] < nst) mbar_wait(&bar[sl], (phases >> sl) & 1u);
       }
     }
     __syncthreads();
@@ -462,6 +469,60 @@ struct GatherLaunch {
   size_t smem;
 };
 
+// Shapes of the streaming gather the autotuner chooses from: edges per thread, pipeline
+// depth, resident blocks per SM (shared memory per SM: blocks x depth x stage bytes).
+struct SgVariant {
+  int ept, nst, minb;
+};
+static const SgVariant kSgVariants[] = {{16, 3, 2}, {8, 4, 3}, {8, 3, 4}, {4, 6, 4}};
+constexpr int kSgVariantCount = 4;
+
+template <int ALGO>
+static void* sg_fn(int v) {
+  switch (v) {
+    case 1: return (void*)gather_stream_kernel<ALGO, 8, 4, 3>;
+    case 2: return (void*)gather_stream_kernel<ALGO, 8, 3, 4>;
+    case 3: return (void*)gather_stream_kernel<ALGO, 4, 6, 4>;
+    default: return (void*)gather_stream_kernel<ALGO, 16, 3, 2>;
+  }
+}
+template <int ALGO>
+static size_t sg_smem(int v) {
+  switch (v) {
+    case 1: return gather_stream_smem<ALGO, 8, 4>();
+    case 2: return gather_stream_smem<ALGO, 8, 3>();
+    case 3: return gather_stream_smem<ALGO, 4, 6>();
+    default: return gather_stream_smem<ALGO, 16, 3>();
+  }
+}
+
+static GatherLaunch stream_launch(Ctx* c, int a, int v) {
+  static bool attr_set[3][kSgVariantCount] = {};
+  GatherLaunch g{};
+  g.fn = a == 0 ? sg_fn<0>(v) : a == 1 ? sg_fn<1>(v) : sg_fn<2>(v);
+  g.smem = a == 2 ? sg_smem<2>(v) : sg_smem<0>(v);
+  if (!attr_set[a][v]) {
+    cudaFuncSetAttribute(g.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
+    attr_set[a][v] = true;
+  }
+  g.grid = dim3(grid_persistent(c, kSgVariants[v].minb));
+  g.block = dim3(SG_T);
+  return g;
+}
+
+// The variant in use: CYTOM_SG_VARIANT overrides; else the autotuner's choice for the
+// program's class (unweighted BFS / CC, weighted SSSP).
+static int sg_variant(Ctx* c, int algo) {
+  static int env = -2;
+  if (env == -2) {
+    const char* s = getenv("CYTOM_SG_VARIANT");
+    env = s ? atoi(s) : -1;
+    if (env >= kSgVariantCount) env = -1;
+  }
+  if (env >= 0) return env;
+  return c->sg_variant[algo == CYTOM_ALGO_SSSP ? 1 : 0];
+}
+
 static GatherLaunch gather_launch(Ctx* c, int algo) {
   GatherLaunch g{};
   if (gather_mode() == 0) {
@@ -473,18 +534,8 @@ static GatherLaunch gather_launch(Ctx* c, int algo) {
     g.smem = 0;
     return g;
   }
-  static bool attr_set[3] = {false, false, false};
-  int a = algo == CYTOM_ALGO_BFS ? 0 : (algo == CYTOM_ALGO_CC ? 1 : 2);
-  g.fn = a == 0 ? (void*)gather_stream_kernel<0> : a == 1 ? (void*)gather_stream_kernel<1>
-                                                          : (void*)gather_stream_kernel<2>;
-  g.smem = a == 2 ? gather_stream_smem<2>() : gather_stream_smem<0>();
-  if (!attr_set[a]) {
-    cudaFuncSetAttribute(g.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
-    attr_set[a] = true;
-  }
-  g.grid = dim3(grid_persistent(c, 2));
-  g.block = dim3(SG_T);
-  return g;
+  const int a = algo == CYTOM_ALGO_BFS ? 0 : (algo == CYTOM_ALGO_CC ? 1 : 2);
+  return stream_launch(c, a, sg_variant(c, algo));
 }
 
 static int launch_gather(Ctx* c, Job* j, int adaptive) {
@@ -618,7 +669,14 @@ int minprop_run(Ctx* c, Job* j) {
   int adaptive = c->cfg.enable_adaptive_scheduling;
   unsigned max_iter = (unsigned)std::min<uint64_t>(j->params.max_iterations, 0xFFFFFFFFu);
   if (!c->profiling && use_graphs() && !j->graph_failed) {
-    if (!j->loop_exec) build_minprop_graph(c, j);
+    if (j->loop_exec && j->graph_epoch != c->tune_epoch) {
+      cudaGraphExecDestroy(j->loop_exec);
+      j->loop_exec = nullptr;
+    }
+    if (!j->loop_exec) {
+      build_minprop_graph(c, j);
+      j->graph_epoch = c->tune_epoch;
+    }
     if (j->loop_exec) {
       j->last_run_graph = true;
       cudaError_t e = cudaGraphLaunch(j->loop_exec, c->stream);
@@ -704,6 +762,118 @@ int minprop_run(Ctx* c, Job* j) {
     c->pending[prev_slot].bytes = round_bytes(c, prev, snap, wbytes);
   }
   return CYTOM_OK;
+}
+
+
+// ---- autotuner ---------------------------------------------------------------
+// Picks the streaming-gather shape (kSgVariants) per program class by timing every
+// variant on the context's current graph: a scratch job in a representative dense
+// state (current = next = vertex id, every other vertex active, every tile row active
+// but not full, so each edge takes the frontier test and about half take the value
+// path) runs one round per variant; next and changed are restored before every launch,
+// so each variant sees identical input. Best of three launches per variant.
+__global__ void tune_state_kernel(JobDesc* jd, const StoreDesc* __restrict__ sd, LoopState* ls, int full) {
+  const uint64_t n = sd->n, nwords = (n + 31) >> 5, T = sd->T;
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (uint64_t v = tid; v < n; v += stride) {
+    if (full) jd->cur[v] = (uint32_t)v;
+    jd->next[v] = (uint32_t)v;
+  }
+  for (uint64_t i = tid; i < nwords; i += stride) {
+    if (full) jd->fa[i] = 0x55555555u;
+    jd->ch[i] = 0;
+  }
+  for (uint64_t x = tid; x < 2 * T; x += stride) jd->rows[x] = x < T ? 1u : 0u;
+  if (tid == 0) {
+    ls->iter = 0;
+    ls->cont = 1;
+    ls->mode = 0;
+    ls->err = 0;
+    ls->teps[0] = ls->teps[1] = 0;
+  }
+}
+
+int minprop_autotune(Ctx* c) {
+  const uint64_t n = c->n, nwords = (n + 31) / 32;
+  JobDesc h{};
+  LoopState* ls = nullptr;
+  JobDesc* d = nullptr;
+  char* buf = nullptr;
+  const size_t bytes = n * 8 + nwords * 8 + 2 * c->T * 4 + nwords * 4 + sizeof(LoopState) + sizeof(JobDesc) + 4096;
+  if (cudaMallocAsync((void**)&buf, bytes, c->stream) != cudaSuccess) {
+    cudaGetLastError();
+    return CYTOM_OK;  // no memory to tune with: keep the current shapes
+  }
+  char* q = buf;
+  auto take = [&](size_t b) {
+    char* r = q;
+    q += (b + 255) & ~(size_t)255;
+    return r;
+  };
+  h.cur = (uint32_t*)take(n * 4);
+  h.next = (uint32_t*)take(n * 4);
+  h.fa = (uint32_t*)take(nwords * 4);
+  h.ch = (uint32_t*)take(nwords * 4);
+  h.rows = (uint32_t*)take(2 * c->T * 4);
+  h.aw = (uint32_t*)take(nwords * 4);
+  ls = (LoopState*)take(sizeof(LoopState));
+  d = (JobDesc*)take(sizeof(JobDesc));
+  h.ls = ls;
+  cudaMemsetAsync(ls, 0, sizeof(LoopState), c->stream);
+  cudaMemcpyAsync(d, &h, sizeof(JobDesc), cudaMemcpyHostToDevice, c->stream);
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  int adaptive = 1;
+  const StoreDesc* sd = c->dsd;
+  const JobDesc* jd = d;
+  void* args[] = {(void*)&jd, (void*)&sd, (void*)&adaptive};
+  const int classes = c->wtype == CYTOM_WEIGHT_U32 ? 2 : 1;
+  cudaError_t e = cudaSuccess;
+  for (int cls = 0; cls < classes && e == cudaSuccess; ++cls) {
+    const int algo = cls == 0 ? 1 : 2;
+    int best = 0;
+    double best_us = 1e300;
+    for (int v = 0; v < kSgVariantCount && e == cudaSuccess; ++v) {
+      GatherLaunch g = stream_launch(c, algo, v);
+      double vbest = 1e300;
+      for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
+        tune_state_kernel<<<grid_persistent(c, 4), 256, 0, c->stream>>>(d, sd, ls, rep == 0 && v == 0 ? 1 : 0);
+        cudaEventRecord(a, c->stream);
+        e = cudaLaunchKernel(g.fn, g.grid, g.block, args, g.smem, c->stream);
+        cudaEventRecord(b, c->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(b);
+        float ms = 0.f;
+        if (e == cudaSuccess) cudaEventElapsedTime(&ms, a, b);
+        vbest = std::min(vbest, (double)ms * 1e3);
+        c->launches += 2;
+      }
+      c->tune_us[cls][v] = vbest;
+      if (vbest < best_us) {
+        best_us = vbest;
+        best = v;
+      }
+    }
+    if (e == cudaSuccess) c->sg_variant[cls] = best;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFreeAsync(buf, c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "autotune");
+  c->tune_E = c->E;
+  c->tune_epoch++;
+  return cuda_err(c, cudaStreamSynchronize(c->stream), "autotune");
+}
+
+
+void sg_shapes(int* ept, int* nst, int* minb, int* count) {
+  *count = kSgVariantCount;
+  for (int v = 0; v < kSgVariantCount; ++v) {
+    ept[v] = kSgVariants[v].ept;
+    nst[v] = kSgVariants[v].nst;
+    minb[v] = kSgVariants[v].minb;
+  }
 }
 
 }  // namespace cytom

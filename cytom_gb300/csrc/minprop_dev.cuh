@@ -192,15 +192,15 @@ __device__ __forceinline__ unsigned control_step(const JobDesc* __restrict__ jd,
   return ls->cont;
 }
 
-// ---- dense gather: one 4096-edge stage --------------------------------------
-// Processes stage `st` whose edges (and weights) are at eb / wb: shared memory for the
+// ---- dense gather: one stage of SG_T * EPT edges ---------------------------
+// Processes stage `st` (EPT edges per thread, a multiple of 4) whose edges (and weights) are at eb / wb: shared memory for the
 // bulk-copy pipeline, global memory (FROM_GLOBAL, guarded loads) for the persistent
 // kernel. Single-row stages (the common case at large vertices-per-tile) take the source
 // row from the stage: the frontier test needs no per-edge tile lookup, and only edges
 // with an active source look up their target tile. Target updates are fire-and-forget
 // red.min / red.or: a candidate below the value read is below current[v] too
 // (next <= current), so next[v] ends the round below current[v] and v changed.
-template <int ALGO, bool PERSIST, bool FROM_GLOBAL>
+template <int ALGO, bool PERSIST, bool FROM_GLOBAL, int EPT = 16>
 __device__ __forceinline__ void dense_stage(const JobDesc* __restrict__ jd, const StoreDesc* __restrict__ sd,
                                             const uint32_t* eb, const uint32_t* wb, uint64_t st, unsigned p,
                                             int adaptive) {
@@ -215,14 +215,16 @@ __device__ __forceinline__ void dense_stage(const JobDesc* __restrict__ jd, cons
   const uint64_t E = sd->E, nchunks = sd->nchunks;
   const uint32_t lT = sd->lT, lvpt = sd->lvpt;
   const uint32_t ymask = (uint32_t)(T - 1);
-  const uint64_t e0 = st * SG_E;
+  constexpr uint32_t SE = SG_T * EPT;  // edges of a stage
+  static_assert(EPT % 4 == 0 && EPT <= 32 && SE % kChunk == 0, "stage shape");
+  const uint64_t e0 = st * SE;
   const uint64_t rem = E - e0;
-  const uint32_t cnt = rem < (uint64_t)SG_E ? (uint32_t)rem : (uint32_t)SG_E;
+  const uint32_t cnt = rem < (uint64_t)SE ? (uint32_t)rem : SE;
   // tiles of the stage's first edge and of the first edge after it
   uint32_t tf, ta;
   {
-    const uint64_t c0 = st * (SG_E / kChunk);
-    uint64_t c1 = c0 + SG_E / kChunk;
+    const uint64_t c0 = st * (SE / kChunk);
+    uint64_t c1 = c0 + SE / kChunk;
     if (c1 > nchunks) c1 = nchunks;
     tf = chunk_tile[c0];
     ta = chunk_tile[c1];
@@ -233,10 +235,10 @@ __device__ __forceinline__ void dense_stage(const JobDesc* __restrict__ jd, cons
   // a fully active row needs no frontier test
   const bool full_row = single_row && (!adaptive || ld_plain<PERSIST>(rows_cur + (tf >> lT)) == vpt);
 
-  uint32_t qv[16], ww[16], uu[16];
+  uint32_t qv[EPT], ww[EPT], uu[EPT];
   uint32_t vmask = 0;
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
+  for (int k = 0; k < EPT / 4; ++k) {
     const uint32_t i0 = threadIdx.x * 4 + (uint32_t)k * (SG_T * 4);
     uint4 q, wq = make_uint4(0, 0, 0, 0);
     if (!FROM_GLOBAL || i0 + 4 <= cnt) {
@@ -267,11 +269,11 @@ __device__ __forceinline__ void dense_stage(const JobDesc* __restrict__ jd, cons
   if (single_row) {
     const uint32_t xb = (tf >> lT) << lvpt;
 #pragma unroll
-    for (int idx = 0; idx < 16; ++idx) uu[idx] = xb | (qv[idx] >> 16);
+    for (int idx = 0; idx < EPT; ++idx) uu[idx] = xb | (qv[idx] >> 16);
   } else {
     // general path: per-edge tile lookup for the source row
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < EPT / 4; ++k) {
       const uint32_t i0 = threadIdx.x * 4 + (uint32_t)k * (SG_T * 4);
       const uint64_t eg = e0 + i0;
       uint32_t t = 0;
@@ -299,26 +301,26 @@ __device__ __forceinline__ void dense_stage(const JobDesc* __restrict__ jd, cons
   }
   uint32_t amask = vmask;
   if (adaptive && !full_row) {
-    uint32_t fw[16];
+    uint32_t fw[EPT];
 #pragma unroll
-    for (int idx = 0; idx < 16; ++idx) fw[idx] = ((vmask >> idx) & 1u) ? ld_state<PERSIST>(fa + (uu[idx] >> 5)) : 0u;
+    for (int idx = 0; idx < EPT; ++idx) fw[idx] = ((vmask >> idx) & 1u) ? ld_state<PERSIST>(fa + (uu[idx] >> 5)) : 0u;
     amask = 0;
 #pragma unroll
-    for (int idx = 0; idx < 16; ++idx) amask |= ((fw[idx] >> (uu[idx] & 31)) & 1u) << idx;
+    for (int idx = 0; idx < EPT; ++idx) amask |= ((fw[idx] >> (uu[idx] & 31)) & 1u) << idx;
     amask &= vmask;
   }
   if (amask) {
-    uint32_t cand[16], vv[16];
+    uint32_t cand[EPT], vv[EPT];
 #pragma unroll
-    for (int idx = 0; idx < 16; ++idx) cand[idx] = ((amask >> idx) & 1u) ? ld_state<PERSIST>(cur + uu[idx]) : kInf;
+    for (int idx = 0; idx < EPT; ++idx) cand[idx] = ((amask >> idx) & 1u) ? ld_state<PERSIST>(cur + uu[idx]) : kInf;
     if (single_tile) {
       const uint32_t yb = (tf & ymask) << lvpt;
 #pragma unroll
-      for (int idx = 0; idx < 16; ++idx) vv[idx] = yb | (qv[idx] & 0xFFFFu);
+      for (int idx = 0; idx < EPT; ++idx) vv[idx] = yb | (qv[idx] & 0xFFFFu);
     } else {
       // target tiles of the edges with an active source
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
+      for (int k = 0; k < EPT / 4; ++k) {
         const uint32_t i0 = threadIdx.x * 4 + (uint32_t)k * (SG_T * 4);
         const uint64_t eg = e0 + i0;
         const uint32_t kmask = (amask >> (4 * k)) & 0xFu;
@@ -343,7 +345,7 @@ __device__ __forceinline__ void dense_stage(const JobDesc* __restrict__ jd, cons
       }
     }
 #pragma unroll
-    for (int idx = 0; idx < 16; ++idx) {
+    for (int idx = 0; idx < EPT; ++idx) {
       const uint32_t c = cand[idx];
       if (c == kInf) continue;
       if (ALGO == 0) {
@@ -353,27 +355,28 @@ __device__ __forceinline__ void dense_stage(const JobDesc* __restrict__ jd, cons
         cand[idx] = sum >= kInf ? kInf : (uint32_t)sum;
       }
     }
-    uint32_t nv[16];
+    uint32_t nv[EPT];
 #pragma unroll
-    for (int idx = 0; idx < 16; ++idx) nv[idx] = (cand[idx] != kInf) ? __ldcg(next + vv[idx]) : 0u;
+    for (int idx = 0; idx < EPT; ++idx) nv[idx] = (cand[idx] != kInf) ? __ldcg(next + vv[idx]) : 0u;
 #pragma unroll
-    for (int idx = 0; idx < 16; ++idx)
+    for (int idx = 0; idx < EPT; ++idx)
       if (cand[idx] != kInf && cand[idx] < nv[idx]) atomicMin(next + vv[idx], cand[idx]);
 #pragma unroll
-    for (int idx = 0; idx < 16; ++idx)
+    for (int idx = 0; idx < EPT; ++idx)
       if (cand[idx] != kInf && cand[idx] < nv[idx]) atomicOr(ch + (vv[idx] >> 5), 1u << (vv[idx] & 31));
   }
 }
 
 // Whether stage st holds an edge of an active tile row (adaptive scheduling).
-template <bool PERSIST>
+template <bool PERSIST, int EPT = 16>
 __device__ __forceinline__ bool stage_active(const JobDesc* __restrict__ jd, const StoreDesc* __restrict__ sd,
                                              uint64_t st, unsigned p, int adaptive) {
   if (!adaptive) return true;
   const unsigned* rows_cur = jd->rows + p * sd->T;
   const uint64_t nchunks = sd->nchunks;
-  const uint64_t c0 = st * (SG_E / kChunk);
-  uint64_t c1 = c0 + SG_E / kChunk;
+  constexpr uint32_t SE = SG_T * EPT;
+  const uint64_t c0 = st * (SE / kChunk);
+  uint64_t c1 = c0 + SE / kChunk;
   if (c1 > nchunks) c1 = nchunks;
   const uint32_t x0 = sd->chunk_tile[c0] >> sd->lT;
   const uint32_t x1 = sd->chunk_tile[c1] >> sd->lT;

@@ -182,6 +182,17 @@ class Engine:
         self._check(self.lib.cytom_set_edge_weights(self.ctx, src.ctypes.data, tgt.ctypes.data, w.ctypes.data,
                                                     len(src), L.PTR_HOST))
 
+    def autotune(self) -> dict:
+        """Times the streaming-gather shapes on the current graph and keeps the fastest."""
+        rep = L.TuneReport()
+        self._check(self.lib.cytom_autotune(self.ctx, C.byref(rep)))
+        return rep.as_dict()
+
+    def tune_report(self) -> dict:
+        rep = L.TuneReport()
+        self._check(self.lib.cytom_get_tune_report(self.ctx, C.byref(rep)))
+        return rep.as_dict()
+
     def do_global_compaction(self):
         self._check(self.lib.cytom_compact(self.ctx))
 

@@ -271,6 +271,28 @@ int cytom_tile_batch_noalloc(const uint32_t* src, const uint32_t* tgt, const uin
                              unsigned long long* tile_ptr, uint32_t* edges, uint32_t* weights,
                              uint64_t* edge_count, void* stream);
 
+/* ---- Autotuner ---------------------------------------------------------- */
+
+/* Shapes of the streaming gather (edges per thread, bulk-copy pipeline depth, resident
+ * blocks per SM) and the round time each took on the context's graph, per program class
+ * (0 = BFS / CC, 1 = SSSP); chosen[k] is the shape in use. No counterpart in the
+ * reference (its tile batching, algorithm-tile-batching, is a fixed flag). */
+typedef struct cytom_tune_report {
+  int32_t variants;
+  int32_t chosen[2];
+  int32_t edges_per_thread[8];
+  int32_t pipeline_depth[8];
+  int32_t blocks_per_sm[8];
+  int32_t reserved;
+  double us[2][8];       /* best of three timed rounds; 0 = not measured */
+  uint64_t tuned_edges;  /* edge count the choice was made at (0 = never tuned) */
+} cytom_tune_report;
+/* Times every shape on the current graph (compacting first) and keeps the fastest.
+ * Runs by itself once per context, on a job's first run at >= 2^20 edges (environment
+ * CYTOM_AUTOTUNE=0 disables that); call it again to re-tune a grown graph. `out` may be NULL. */
+int cytom_autotune(cytom_ctx* ctx, cytom_tune_report* out);
+int cytom_get_tune_report(const cytom_ctx* ctx, cytom_tune_report* out);
+
 /* ---- Instrumentation --------------------------------------------------- */
 
 /* Per-kernel-class timing, recorded with CUDA events around each launch when

@@ -202,3 +202,62 @@ print(json.dumps(ok))
     assert r.returncode == 0, r.stderr[-2000:]
     ok = json.loads(r.stdout.strip().splitlines()[-1])
     assert all(ok), (sparse, ok)
+
+
+@pytest.mark.parametrize("variant", ["0", "1", "2", "3"])
+def test_stream_shapes_agree(cg, orc, variant):
+    # every streaming-gather shape the autotuner may pick gives the oracle's values,
+    # round counts and processed-edge counts (dense rounds only; single- and multi-row stages)
+    import json
+    import os
+    import subprocess
+    import sys
+    code = f"""
+import sys, json, numpy as np
+sys.path.insert(0, {str(__import__('pathlib').Path(__file__).resolve().parents[1])!r})
+import cytom_gb300 as cg
+from oracle import oracle as orc
+ok = []
+for scale, vpt in ((16, 4096), (15, 256)):
+    n = 1 << scale
+    s, t = orc.rmat(scale, 0, 16 * n, 5)
+    w = orc.edge_weights(s, t, 6)
+    st = orc.Store(n, vpt, True)
+    st.insert(s, t, w); st.compact()
+    with cg.Engine(n, vpt, weight_type=cg.WEIGHT_U32) as eng:
+        eng.insert_edges(s, t, w)
+        for prog, algo in ((cg.BFS, 0), (cg.CC, 1), (cg.SSSP, 2)):
+            p = prog(eng, start_vertex=0, max_iterations=1000)
+            stt = p.execute_algorithm()
+            ref, info = st.run_minprop(algo, start=0, max_iter=1000)
+            ok.append(bool(np.array_equal(p.result(), ref)) and stt["iterations"] == info["iterations"]
+                      and stt["count_edges"] == info["count_edges"])
+print(json.dumps(ok))
+"""
+    env = dict(os.environ, CYTOM_SG_VARIANT=variant, CYTOM_SPARSE="0", CYTOM_AUTOTUNE="0")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=900)
+    assert r.returncode == 0, r.stderr[-2000:]
+    ok = json.loads(r.stdout.strip().splitlines()[-1])
+    assert all(ok), (variant, ok)
+
+
+def test_autotune_report(cg, orc):
+    scale, vpt = 17, 8192
+    n = 1 << scale
+    s, t = orc.rmat(scale, 0, 16 * n, 9)
+    w = orc.edge_weights(s, t, 10)
+    with cg.Engine(n, vpt, weight_type=cg.WEIGHT_U32) as eng:
+        eng.insert_edges(s, t, w)
+        rep = eng.autotune()
+        assert rep["tuned_edges"] == eng.count_edges()[0]
+        k = len(rep["shapes"])
+        assert k >= 2 and all(x > 0 for x in rep["round_us"]["bfs_cc"]) and all(x > 0 for x in rep["round_us"]["sssp"])
+        best = rep["chosen"]["sssp"]
+        assert rep["round_us"]["sssp"][best] == min(rep["round_us"]["sssp"])
+        p = cg.SSSP(eng, start_vertex=0, max_iterations=1000)
+        p.execute_algorithm()
+        st = orc.Store(n, vpt, True)
+        st.insert(s, t, w)
+        st.compact()
+        ref, _ = st.run_minprop(2, start=0, max_iter=1000)
+        assert np.array_equal(p.result(), ref)

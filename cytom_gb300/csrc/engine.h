@@ -172,6 +172,14 @@ struct Ctx {
   uint64_t tune_E = 0;
   uint64_t tune_epoch = 0;
   double tune_us[2][8] = {};
+  // PageRank family: vertices renumbered by out-degree (hubs first) so the hot part of
+  // the gathered contribution vector packs densely into L2. perm[v] = position of vertex
+  // v, inv[position] = v; fixed once computed. deg_mult = multiplicity out-degrees in
+  // that numbering (PageRank-delta), rebuilt when the graph changes.
+  uint32_t* pr_perm = nullptr;
+  uint32_t* pr_inv = nullptr;
+  uint32_t* pr_deg_mult = nullptr;
+  uint64_t pr_deg_mult_version = ~0ULL;
   void* pr_csc = nullptr;
   void* pr_wgraph = nullptr;  // weighted PageRank: CSC + CSR with weights
 };

@@ -34,7 +34,7 @@
 namespace cytom {
 
 int minprop_batch_prep(Ctx* c, Job* j);
-int pagerank_batch_prep(Ctx* c, Job* j, PrArgs* out, uint64_t nb[3], int* first_mode);
+int pagerank_batch_prep(Ctx* c, Job* j, PrArgs* out, uint64_t* nb, int* first_mode);
 
 constexpr int BT = 256;  // threads of a batch block (every unit kind is written for 256)
 static_assert(BT == APPLY_T && BT == SG_T && BT == PR_BLOCK_T, "one block shape for every unit");
@@ -47,15 +47,18 @@ enum BatchPhase : unsigned {
   PH_CHUNKS = 4,     // sparse chunk pass: 8 queued chunks per unit
   PH_APPLY = 5,      // apply: 1024 frontier words per unit
   PH_PR_CONTRIB = 6, // PageRank contributions: 4096 sources per unit
-  PH_PR_PULL = 7,    // PageRank pull: 1024 small, 32 medium or 1 large target per unit
+  PH_PR_PULL = 7,    // PageRank pull: targets of one in-degree bin per unit (pr_bin_unit)
   PH_DONE = 8
 };
 constexpr uint32_t BU_APPLY_WORDS = 1024;
 constexpr uint32_t BU_SPARSE_ITEMS = 256;
 constexpr uint32_t BU_CHUNKS = BT / 32;
 constexpr uint32_t BU_PR_VERTS = 4096;
-constexpr uint32_t BU_PR_SMALL = 1024;
-constexpr uint32_t BU_PR_MEDIUM = 32;
+// targets per pull unit of each bin: 4 per thread (one thread per target), 4 per group of
+// VW lanes, one for the block bin
+__host__ __device__ constexpr uint32_t pr_bin_unit(int k) {
+  return pr_bin_vw(k) == 1 ? 4 * BT : (pr_bin_vw(k) == 0 ? 1 : 4 * (BT / pr_bin_vw(k)));
+}
 constexpr uint32_t kMaxUnits = (1u << 24) - 1;
 constexpr uint32_t kIdleLimit = 1u << 22;
 
@@ -63,7 +66,7 @@ struct BJob {
   const JobDesc* jd;
   const StoreDesc* sd;
   PrArgs pr;
-  unsigned long long nb0, nb1, nb2;  // PageRank target bins
+  unsigned long long nb[kPrBins];  // PageRank target bins
   int algo;
   int adaptive;
 };
@@ -182,40 +185,65 @@ __device__ void unit_pr_contrib(const BJob* J, uint32_t unit) {
   pr_dangling_flush<MODE>(a.ls, p, dangling);
 }
 
+template <int MODE, int VW>
+__device__ __forceinline__ void pull_groups(const PrArgs& a, uint64_t off, uint64_t cnt, uint64_t first, unsigned p,
+                                            double dang, double& resid, double& rsum) {
+  constexpr uint32_t GPB = BT / VW;  // groups per block
+  const unsigned gl = threadIdx.x & (VW - 1);
+  const uint32_t g = threadIdx.x / VW;
+#pragma unroll 1
+  for (uint32_t k = 0; k < 4; ++k) {
+    const uint64_t i = first + (uint64_t)k * GPB + g;
+    uint32_t v = 0, lo = 0, hi = 0;
+    if (i < cnt) {
+      v = a.bins[off + i];
+      lo = a.csc_ptr[v];
+      hi = a.csc_ptr[v + 1];
+    }
+    const double sum = pr_sum_group<MODE, true, VW>(a, lo, hi, gl);
+    if (gl == 0 && i < cnt) resid += pr_finish<MODE, true>(a, v, sum, p, dang, &rsum);
+  }
+}
+
 template <int MODE>
 __device__ void unit_pr_pull(const BJob* J, uint32_t unit) {
   const PrArgs& a = J->pr;
   LoopState* ls = a.ls;
   const unsigned p = ls_iter(ls) & 1u;
   const double dang = pr_dang_arg<MODE, true>(ls, p, a.n);
-  const uint32_t ns = ceil_div(J->nb0, BU_PR_SMALL), nm = ceil_div(J->nb1, BU_PR_MEDIUM);
+  // the bin this unit belongs to
+  int k = 0;
+  uint64_t off = 0;
+  uint32_t u = unit;
+  for (; k < kPrBins - 1; ++k) {
+    const uint32_t units_k = ceil_div(J->nb[k], pr_bin_unit(k));
+    if (u < units_k) break;
+    u -= units_k;
+    off += J->nb[k];
+  }
+  const uint64_t cnt = J->nb[k];
+  const uint64_t first = (uint64_t)u * pr_bin_unit(k);
   double resid = 0.0, rsum = 0.0;
-  if (unit < ns) {
+  switch (pr_bin_vw(k)) {
+    case 1:
 #pragma unroll 1
-    for (uint32_t k = 0; k < BU_PR_SMALL / BT; ++k) {
-      const uint64_t i = (uint64_t)unit * BU_PR_SMALL + k * BT + threadIdx.x;
-      if (i < J->nb0) {
-        const uint32_t v = a.bins[i];
-        const double sum = pr_sum_thread<MODE, true>(a, v);
-        resid += pr_finish<MODE, true>(a, v, sum, p, dang, &rsum);
+      for (uint32_t r = 0; r < 4; ++r) {
+        const uint64_t i = first + (uint64_t)r * BT + threadIdx.x;
+        if (i < cnt) {
+          const uint32_t v = a.bins[off + i];
+          const double sum = pr_sum_thread<MODE, true>(a, v);
+          resid += pr_finish<MODE, true>(a, v, sum, p, dang, &rsum);
+        }
       }
+      break;
+    case 4: pull_groups<MODE, 4>(a, off, cnt, first, p, dang, resid, rsum); break;
+    case 8: pull_groups<MODE, 8>(a, off, cnt, first, p, dang, resid, rsum); break;
+    case 32: pull_groups<MODE, 32>(a, off, cnt, first, p, dang, resid, rsum); break;
+    default: {
+      const uint32_t v = a.bins[off + first];
+      const double sum = pr_sum_block<MODE, true>(a, v);
+      if (threadIdx.x == 0) resid += pr_finish<MODE, true>(a, v, sum, p, dang, &rsum);
     }
-  } else if (unit < ns + nm) {
-    const unsigned lane = threadIdx.x & 31;
-#pragma unroll 1
-    for (uint32_t k = 0; k < BU_PR_MEDIUM / (BT / 32); ++k) {
-      const uint64_t i = (uint64_t)(unit - ns) * BU_PR_MEDIUM + k * (BT / 32) + (threadIdx.x >> 5);
-      if (i < J->nb1) {
-        const uint32_t v = a.bins[J->nb0 + i];
-        const double sum = pr_sum_warp<MODE, true>(a, v, lane);
-        if (lane == 0) resid += pr_finish<MODE, true>(a, v, sum, p, dang, &rsum);
-      }
-    }
-  } else {
-    const uint64_t i = (uint64_t)(unit - ns - nm);
-    const uint32_t v = a.bins[J->nb0 + J->nb1 + i];
-    const double sum = pr_sum_block<MODE, true>(a, v);
-    if (threadIdx.x == 0) resid += pr_finish<MODE, true>(a, v, sum, p, dang, &rsum);
   }
   block_sum2(resid, rsum);
   if (threadIdx.x == 0) {
@@ -225,7 +253,9 @@ __device__ void unit_pr_pull(const BJob* J, uint32_t unit) {
 }
 
 __device__ __forceinline__ uint32_t pr_pull_units(const BJob* J) {
-  return ceil_div(J->nb0, BU_PR_SMALL) + ceil_div(J->nb1, BU_PR_MEDIUM) + (uint32_t)J->nb2;
+  uint32_t t = 0;
+  for (int k = 0; k < kPrBins; ++k) t += ceil_div(J->nb[k], pr_bin_unit(k));
+  return t;
 }
 
 // ---- phase transitions (whole block, after the last unit of `phase`) --------
@@ -471,13 +501,11 @@ static int batch_run(Ctx* const* ctxs, const int* job_ids, int count, cytom_run_
     b.adaptive = c->cfg.enable_adaptive_scheduling;
     memset(&hs[k], 0, sizeof(BSched));
     if (is_pr(j->algo)) {
-      uint64_t nb[3];
+      uint64_t nb[kPrBins];
       int mode = 0;
       rc = pagerank_batch_prep(c, j, &b.pr, nb, &mode);
       if (rc) return rc;
-      b.nb0 = nb[0];
-      b.nb1 = nb[1];
-      b.nb2 = nb[2];
+      for (int k = 0; k < kPrBins; ++k) b.nb[k] = nb[k];
       hs[k].prmode = mode;
       const uint64_t units = (c->n + BU_PR_VERTS - 1) / BU_PR_VERTS;
       if (units > kMaxUnits) return set_err(c, CYTOM_ERR_RANGE, "graph too large for the batched executor");

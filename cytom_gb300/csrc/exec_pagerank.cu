@@ -39,7 +39,7 @@ struct Csc {
   uint32_t* ptr = nullptr;       // n+1
   uint32_t* deg_out = nullptr;   // n: distinct out-degree (stored edges)
   uint32_t* bins = nullptr;      // n: targets, small | medium | large
-  uint64_t nb[3] = {0, 0, 0};
+  uint64_t nb[kPrBins] = {};
   uint64_t E = 0;
   uint64_t cap = 0;
   uint64_t built_version = ~0ULL;
@@ -82,11 +82,13 @@ struct WGraph {
 // --------------------------------------------------------------------------
 // CSC construction from the tile store
 // --------------------------------------------------------------------------
-// Sort keys of every stored edge u -> v: (v, u) for the target-major CSC, (u, v) for the
-// source-major CSR (by_source); the edge's weight bits ride along (vals, weighted stores).
-__global__ void csc_keys_kernel(const StoreDesc* __restrict__ sd, uint64_t* __restrict__ keys,
-                                uint32_t* __restrict__ vals, uint32_t* __restrict__ deg_out,
-                                uint32_t* __restrict__ major_cnt, uint32_t lg_n, int by_source) {
+// Sort keys of every stored edge u -> v in the renumbered ids u' = perm[u], v' = perm[v]:
+// (v', u') for the target-major CSC, (u', v') for the source-major CSR (by_source); the
+// edge's weight bits ride along (vals, weighted stores).
+__global__ void csc_keys_kernel(const StoreDesc* __restrict__ sd, const uint32_t* __restrict__ perm,
+                                uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                                uint32_t* __restrict__ deg_out, uint32_t* __restrict__ major_cnt, uint32_t lg_n,
+                                int by_source) {
   const uint64_t E = sd->E;
   const uint32_t lT = sd->lT, lvpt = sd->lvpt;
   const uint32_t ymask = (uint32_t)(sd->T - 1);
@@ -95,8 +97,8 @@ __global__ void csc_keys_kernel(const StoreDesc* __restrict__ sd, uint64_t* __re
     uint32_t t = sd->chunk_tile[e >> 7];
     while (sd->tile_ptr[t + 1] <= e) ++t;
     const uint32_t p = sd->edges[e];
-    const uint32_t u = ((t >> lT) << lvpt) | (p >> 16);
-    const uint32_t v = ((t & ymask) << lvpt) | (p & 0xFFFFu);
+    const uint32_t u = perm[((t >> lT) << lvpt) | (p >> 16)];
+    const uint32_t v = perm[((t & ymask) << lvpt) | (p & 0xFFFFu)];
     keys[e] = by_source ? (((uint64_t)u << lg_n) | v) : (((uint64_t)v << lg_n) | u);
     if (vals) vals[e] = sd->wts[e];
     if (deg_out) atomicAdd(&deg_out[u], 1u);
@@ -112,29 +114,24 @@ __global__ void csc_src_kernel(const uint64_t* __restrict__ keys, uint64_t E, ui
     src[e] = (uint32_t)(keys[e] & mask);
 }
 
-// class of each target by in-degree: 0 small, 1 medium, 2 large (flags for three scans)
-__global__ void csc_class_kernel(const uint32_t* __restrict__ in_cnt, uint64_t n, uint32_t* __restrict__ f0,
-                                 uint32_t* __restrict__ f1, uint32_t* __restrict__ f2) {
+// flag[v] = 1 when v's segment length falls in bin k (pr_bin_hi)
+__global__ void csc_class_kernel(const uint32_t* __restrict__ cnt, uint64_t n, int k, uint32_t* __restrict__ flag) {
+  const uint32_t lo = k ? pr_bin_hi(k - 1) : 0u, hi = pr_bin_hi(k);
   uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
-    const uint32_t d = in_cnt[v];
-    f0[v] = d <= kBinSmall ? 1u : 0u;
-    f1[v] = (d > kBinSmall && d <= kBinMedium) ? 1u : 0u;
-    f2[v] = d > kBinMedium ? 1u : 0u;
+    const uint32_t d = cnt[v];
+    flag[v] = (k == 0 ? d <= hi : (d > lo && d <= hi)) ? 1u : 0u;
   }
 }
 
-__global__ void csc_bins_kernel(const uint32_t* __restrict__ f0, const uint32_t* __restrict__ f1,
-                                const uint32_t* __restrict__ f2, const uint32_t* __restrict__ p0,
-                                const uint32_t* __restrict__ p1, const uint32_t* __restrict__ p2,
-                                const uint32_t* __restrict__ tot, uint64_t n, uint32_t* __restrict__ bins) {
-  const uint32_t n0 = tot[0], n1 = tot[1];
+// bins[base_k + pos[v]] = v for the vertices of bin k; base_k = sizes of the bins before k
+__global__ void csc_bins_kernel(const uint32_t* __restrict__ flag, const uint32_t* __restrict__ pos,
+                                const uint32_t* __restrict__ tot, int k, uint64_t n, uint32_t* __restrict__ bins) {
+  uint64_t base = 0;
+  for (int b = 0; b < k; ++b) base += tot[b];
   uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
-    if (f0[v]) bins[p0[v]] = (uint32_t)v;
-    else if (f1[v]) bins[n0 + p1[v]] = (uint32_t)v;
-    else if (f2[v]) bins[n0 + n1 + p2[v]] = (uint32_t)v;
-  }
+  for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride)
+    if (flag[v]) bins[base + pos[v]] = (uint32_t)v;
 }
 
 static int grid_n(Ctx* c, uint64_t work, int threads = 256, int per_sm = 8) {
@@ -151,7 +148,11 @@ static uint64_t store_version(Ctx* c) { return c->version; }
 // by one radix sort of (major, minor) keys; minor ids ascend inside each segment. With
 // w != NULL the edges' weights are sorted along into *w (grown to hold E). Vertices are
 // binned by segment length for the pull (small / medium / large).
+static int pr_ensure_perm(Ctx* c);
+
 static int build_csx(Ctx* c, Csc& q, int by_source, float** w, uint64_t* wcap) {
+  int prc = pr_ensure_perm(c);
+  if (prc) return prc;
   const uint64_t n = c->n, E = c->E;
   uint32_t lg_n = 0;
   while ((1ULL << lg_n) < n) ++lg_n;
@@ -175,26 +176,22 @@ static int build_csx(Ctx* c, Csc& q, int by_source, float** w, uint64_t* wcap) {
   const size_t kbytes = std::max<uint64_t>(E, 1) * 8;
   const size_t vbytes = w ? std::max<uint64_t>(E, 1) * 4 : 0;
   const size_t nbytes = n * 4;
-  if (cudaMallocAsync((void**)&tmp, 2 * kbytes + 2 * vbytes + 7 * nbytes + 64, c->stream) != cudaSuccess)
+  if (cudaMallocAsync((void**)&tmp, 2 * kbytes + 2 * vbytes + 3 * nbytes + 64, c->stream) != cudaSuccess)
     return set_err(c, CYTOM_ERR_OOM, "CSC temporaries");
   uint64_t* k0 = (uint64_t*)tmp;
   uint64_t* k1 = (uint64_t*)(tmp + kbytes);
   uint32_t* v0 = w ? (uint32_t*)(tmp + 2 * kbytes) : nullptr;
   uint32_t* v1 = w ? (uint32_t*)(tmp + 2 * kbytes + vbytes) : nullptr;
   uint32_t* cnt = (uint32_t*)(tmp + 2 * kbytes + 2 * vbytes);
-  uint32_t* f0 = cnt + n;
-  uint32_t* f1 = f0 + n;
-  uint32_t* f2 = f1 + n;
-  uint32_t* p0 = f2 + n;
-  uint32_t* p1 = p0 + n;
-  uint32_t* p2 = p1 + n;
-  uint32_t* tot = p2 + n;  // 3 totals + 1
+  uint32_t* flag = cnt + n;
+  uint32_t* pos = flag + n;
+  uint32_t* tot = pos + n;  // kPrBins totals
   cudaMemsetAsync(q.deg_out, 0, n * 4, c->stream);
   cudaMemsetAsync(cnt, 0, n * 4, c->stream);
   int rc = CYTOM_OK;
   if (E) {
-    csc_keys_kernel<<<grid_n(c, E), 256, 0, c->stream>>>(c->dsd, k0, v0, by_source ? nullptr : q.deg_out, cnt,
-                                                         lg_n, by_source);
+    csc_keys_kernel<<<grid_n(c, E), 256, 0, c->stream>>>(c->dsd, c->pr_perm, k0, v0, by_source ? nullptr : q.deg_out,
+                                                         cnt, lg_n, by_source);
     c->launches++;
     bool alt = false;
     rc = radix_sort_pairs(c, k0, k1, v0, v1, E, (int)(2 * lg_n), &alt);
@@ -205,27 +202,94 @@ static int build_csx(Ctx* c, Csc& q, int by_source, float** w, uint64_t* wcap) {
   }
   rc = exclusive_scan_u32(c, cnt, q.ptr, n, q.ptr + n);
   if (rc) return rc;
-  csc_class_kernel<<<grid_n(c, n), 256, 0, c->stream>>>(cnt, n, f0, f1, f2);
-  c->launches++;
-  rc = exclusive_scan_u32(c, f0, p0, n, tot + 0);
-  if (!rc) rc = exclusive_scan_u32(c, f1, p1, n, tot + 1);
-  if (!rc) rc = exclusive_scan_u32(c, f2, p2, n, tot + 2);
-  if (rc) return rc;
-  csc_bins_kernel<<<grid_n(c, n), 256, 0, c->stream>>>(f0, f1, f2, p0, p1, p2, tot, n, q.bins);
-  c->launches++;
-  uint32_t ht[3];
-  cudaMemcpyAsync(ht, tot, 12, cudaMemcpyDeviceToHost, c->stream);
+  for (int k = 0; k < kPrBins; ++k) {
+    csc_class_kernel<<<grid_n(c, n), 256, 0, c->stream>>>(cnt, n, k, flag);
+    rc = exclusive_scan_u32(c, flag, pos, n, tot + k);
+    if (rc) return rc;
+    csc_bins_kernel<<<grid_n(c, n), 256, 0, c->stream>>>(flag, pos, tot, k, n, q.bins);
+    c->launches += 2;
+  }
+  uint32_t ht[kPrBins];
+  cudaMemcpyAsync(ht, tot, sizeof(ht), cudaMemcpyDeviceToHost, c->stream);
   cudaFreeAsync(tmp, c->stream);
   cudaError_t e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_err(c, e, "CSC build");
-  q.nb[0] = ht[0];
-  q.nb[1] = ht[1];
-  q.nb[2] = ht[2];
+  for (int k = 0; k < kPrBins; ++k) q.nb[k] = ht[k];
   q.E = E;
   return CYTOM_OK;
 }
 
 static int build_csc(Ctx* c, Csc& q) { return build_csx(c, q, 0, nullptr, nullptr); }
+
+// ---- renumbering by out-degree ---------------------------------------------------
+__global__ void perm_keys_kernel(const uint32_t* __restrict__ deg, uint64_t n, uint32_t lg_n,
+                                 uint64_t* __restrict__ keys) {
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride)
+    keys[v] = ((uint64_t)(0xFFFFFFFFu - deg[v]) << lg_n) | v;  // descending degree, then id
+}
+__global__ void perm_from_keys_kernel(const uint64_t* __restrict__ keys, uint64_t n, uint32_t lg_n,
+                                      uint32_t* __restrict__ perm, uint32_t* __restrict__ inv) {
+  const uint64_t mask = (lg_n >= 64) ? ~0ULL : ((1ULL << lg_n) - 1ULL);
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const uint32_t v = (uint32_t)(keys[i] & mask);
+    inv[i] = v;
+    perm[v] = (uint32_t)i;
+  }
+}
+// out[perm[v]] = in[v] (to the renumbering) or out[v] = in[perm[v]] (back), any 4- or 8-byte type
+template <typename T>
+__global__ void permute_kernel(const T* __restrict__ in, const uint32_t* __restrict__ perm, uint64_t n,
+                               int to_renumbered, T* __restrict__ out) {
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
+    if (to_renumbered) out[perm[v]] = in[v];
+    else out[v] = in[perm[v]];
+  }
+}
+
+// The renumbering, made once per context from the out-degrees of the graph at that time
+// (a later graph keeps it: any numbering gives the same results, this one only packs
+// the sources most edges read into few cache lines).
+static int pr_ensure_perm(Ctx* c) {
+  if (c->pr_perm) return CYTOM_OK;
+  const uint64_t n = c->n;
+  uint32_t lg_n = 0;
+  while ((1ULL << lg_n) < n) ++lg_n;
+  uint64_t* k = nullptr;
+  uint32_t *perm = nullptr, *inv = nullptr;
+  if (cudaMallocAsync((void**)&k, 2 * n * 8, c->stream) != cudaSuccess || cudaMalloc(&perm, n * 4) != cudaSuccess ||
+      cudaMalloc(&inv, n * 4) != cudaSuccess) {
+    cudaGetLastError();
+    if (k) cudaFreeAsync(k, c->stream);
+    if (perm) cudaFree(perm);
+    return set_err(c, CYTOM_ERR_OOM, "vertex renumbering");
+  }
+  c->pr_perm = perm;
+  c->pr_inv = inv;
+  perm_keys_kernel<<<grid_n(c, n), 256, 0, c->stream>>>(c->out_deg, n, lg_n, k);
+  bool alt = false;
+  int rc = radix_sort_pairs(c, k, k + n, nullptr, nullptr, n, (int)(32 + lg_n), &alt);
+  if (rc) return rc;
+  perm_from_keys_kernel<<<grid_n(c, n), 256, 0, c->stream>>>(alt ? k + n : k, n, lg_n, c->pr_perm, c->pr_inv);
+  c->launches += 2;
+  cudaFreeAsync(k, c->stream);
+  return cuda_err(c, cudaGetLastError(), "vertex renumbering");
+}
+
+// Multiplicity out-degrees in the renumbering (PageRank-delta), per graph version.
+static int pr_deg_mult(Ctx* c) {
+  int rc = pr_ensure_perm(c);
+  if (rc) return rc;
+  if (c->pr_deg_mult && c->pr_deg_mult_version == c->version) return CYTOM_OK;
+  if (!c->pr_deg_mult && cudaMalloc(&c->pr_deg_mult, c->n * 4) != cudaSuccess)
+    return set_err(c, CYTOM_ERR_OOM, "degrees");
+  permute_kernel<uint32_t><<<grid_n(c, c->n), 256, 0, c->stream>>>(c->out_deg, c->pr_perm, c->n, 1, c->pr_deg_mult);
+  c->launches++;
+  c->pr_deg_mult_version = c->version;
+  return cuda_err(c, cudaGetLastError(), "degrees");
+}
 
 // --------------------------------------------------------------------------
 // Round kernels
@@ -262,21 +326,30 @@ __global__ void __launch_bounds__(PR_T) pr_pull_small(PrArgs a) {
   pr_flush(ls, p, resid, rsum);
 }
 
-// One warp per target (16 < in-degree <= 4096).
-template <int MODE>
-__global__ void __launch_bounds__(PR_T) pr_pull_medium(PrArgs a) {
+// VW lanes per target (bins 1..3: in-degrees up to 32, 256, 4096).
+template <int MODE, int VW>
+__global__ void __launch_bounds__(PR_T) pr_pull_group(PrArgs a) {
   LoopState* ls = a.ls;
   if (!ls->cont) return;
   const unsigned p = ls->iter & 1u;
   const double dang = pr_dang_arg<MODE, false>(ls, p, a.n);
-  const unsigned lane = threadIdx.x & 31;
-  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  constexpr uint64_t GPW = 32 / VW;  // groups per warp
+  const unsigned gl = threadIdx.x & (VW - 1);
+  const uint64_t gid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / VW;
+  const uint64_t ngroups = ((uint64_t)gridDim.x * blockDim.x) / VW;
   double resid = 0.0, rsum = 0.0;
-  for (uint64_t i = warp; i < a.bin_count; i += nwarps) {
-    const uint32_t v = a.bins[a.bin_off + i];
-    const double sum = pr_sum_warp<MODE, false>(a, v, lane);
-    if (lane == 0) resid += pr_finish<MODE, false>(a, v, sum, p, dang, &rsum);
+  // warp-uniform trip count: every lane stays in the loop for the group shuffles
+  const uint64_t gbase = gid - (gid % GPW);
+  for (uint64_t b = gbase; b < a.bin_count; b += ngroups) {
+    const uint64_t i = b + (gid - gbase);
+    uint32_t v = 0, lo = 0, hi = 0;
+    if (i < a.bin_count) {
+      v = a.bins[a.bin_off + i];
+      lo = a.csc_ptr[v];
+      hi = a.csc_ptr[v + 1];
+    }
+    const double sum = pr_sum_group<MODE, false, VW>(a, lo, hi, gl);
+    if (gl == 0 && i < a.bin_count) resid += pr_finish<MODE, false>(a, v, sum, p, dang, &rsum);
   }
   pr_flush(ls, p, resid, rsum);
 }
@@ -370,6 +443,10 @@ static WGraph* ctx_wgraph(Ctx* c) {
 }
 
 void pagerank_ctx_free(Ctx* c) {
+  void* pp[] = {c->pr_perm, c->pr_inv, c->pr_deg_mult};
+  for (void* p : pp)
+    if (p) cudaFree(p);
+  c->pr_perm = c->pr_inv = c->pr_deg_mult = nullptr;
   Csc* q = reinterpret_cast<Csc*>(c->pr_csc);
   if (q) {
     csc_free(q);
@@ -433,6 +510,8 @@ void pagerank_free(Job* j) {
 
 int pagerank_init(Ctx* c, Job* j) {
   PrState* s = prs(j);
+  int prc = pr_ensure_perm(c);
+  if (prc) return prc;
   const uint64_t n = c->n;
   int g = grid_n(c, n);
   if (j->algo == CYTOM_ALGO_PR_DELTA) {
@@ -469,19 +548,26 @@ template <int MODE>
 static int launch_round(Ctx* c, const PrArgs& base_args, const uint64_t* nb) {
   PrArgs a = base_args;
   pr_contrib_kernel<MODE><<<grid_n(c, c->n), 256, 0, c->stream>>>(a);
-  a.bin_off = 0;
-  a.bin_count = nb[0];
-  if (a.bin_count) pr_pull_small<MODE><<<grid_n(c, a.bin_count, PR_T), PR_T, 0, c->stream>>>(a);
-  a.bin_off = nb[0];
-  a.bin_count = nb[1];
-  if (a.bin_count) pr_pull_medium<MODE><<<grid_n(c, a.bin_count * 32, PR_T), PR_T, 0, c->stream>>>(a);
-  a.bin_off = nb[0] + nb[1];
-  a.bin_count = nb[2];
-  if (a.bin_count)
-    pr_pull_large<MODE><<<(unsigned)std::min<uint64_t>(a.bin_count, (uint64_t)c->num_sms * 4), PR_BLOCK_T, 0,
-                          c->stream>>>(a);
+  int launched = 2;
+  uint64_t off = 0;
+  for (int k = 0; k < kPrBins; ++k) {
+    a.bin_off = off;
+    a.bin_count = nb[k];
+    off += nb[k];
+    if (!nb[k]) continue;
+    ++launched;
+    switch (pr_bin_vw(k)) {
+      case 1: pr_pull_small<MODE><<<grid_n(c, nb[k], PR_T), PR_T, 0, c->stream>>>(a); break;
+      case 4: pr_pull_group<MODE, 4><<<grid_n(c, nb[k] * 4, PR_T), PR_T, 0, c->stream>>>(a); break;
+      case 8: pr_pull_group<MODE, 8><<<grid_n(c, nb[k] * 8, PR_T), PR_T, 0, c->stream>>>(a); break;
+      case 32: pr_pull_group<MODE, 32><<<grid_n(c, nb[k] * 32, PR_T), PR_T, 0, c->stream>>>(a); break;
+      default:
+        pr_pull_large<MODE><<<(unsigned)std::min<uint64_t>(nb[k], (uint64_t)c->num_sms * 4), PR_BLOCK_T, 0,
+                              c->stream>>>(a);
+    }
+  }
   pr_control_kernel<<<1, 1, 0, c->stream>>>(a.ls, MODE, 0, 0);
-  c->launches += 2 + (nb[0] ? 1 : 0) + (nb[1] ? 1 : 0) + (nb[2] ? 1 : 0);
+  c->launches += launched;
   return cuda_err(c, cudaGetLastError(), "pagerank round");
 }
 
@@ -541,7 +627,9 @@ int pagerank_run(Ctx* c, Job* j) {
   c->launches++;
   j->last_run_graph = false;
   if (j->algo == CYTOM_ALGO_PR_DELTA) {
-    a.deg = c->out_deg;  // multiplicity out-degrees, as the reference's vertex store
+    int drc = pr_deg_mult(c);
+    if (drc) return drc;
+    a.deg = c->pr_deg_mult;  // multiplicity out-degrees, as the reference's vertex store
     // rank sum before the run (relative stopping rule)
     pr_rank_sum_kernel<<<grid_n(c, n), 256, 0, c->stream>>>(s->rank, n, j->ls);
     c->launches++;
@@ -563,7 +651,7 @@ int pagerank_run(Ctx* c, Job* j) {
 // Prepares a run of the batched executor: the snapshot's CSC, the loop state (and for
 // PageRank-delta the rank sum before the run), the round arguments, the bin sizes and
 // the mode of the first round.
-int pagerank_batch_prep(Ctx* c, Job* j, PrArgs* out, uint64_t nb[3], int* first_mode) {
+int pagerank_batch_prep(Ctx* c, Job* j, PrArgs* out, uint64_t* nb, int* first_mode) {
   if (j->algo == CYTOM_ALGO_WPAGERANK)
     return set_err(c, CYTOM_ERR_UNIMPLEMENTED, "weighted PageRank runs through cytom_run only");
   PrState* s = prs(j);
@@ -597,7 +685,9 @@ int pagerank_batch_prep(Ctx* c, Job* j, PrArgs* out, uint64_t nb[3], int* first_
   pr_begin_kernel<<<1, 1, 0, c->stream>>>(j->ls, max_iter, j->params.tolerance, (unsigned long long)s->csc->E);
   c->launches++;
   if (j->algo == CYTOM_ALGO_PR_DELTA) {
-    a.deg = c->out_deg;
+    int drc = pr_deg_mult(c);
+    if (drc) return drc;
+    a.deg = c->pr_deg_mult;
     pr_rank_sum_kernel<<<grid_n(c, n), 256, 0, c->stream>>>(s->rank, n, j->ls);
     c->launches++;
     *first_mode = PR_DELTA_RESIDUAL;
@@ -606,11 +696,30 @@ int pagerank_batch_prep(Ctx* c, Job* j, PrArgs* out, uint64_t nb[3], int* first_
     a.deg = s->csc->deg_out;
     *first_mode = j->params.kahan ? PR_NORM32 : PR_NORM64;
   }
-  nb[0] = s->csc->nb[0];
-  nb[1] = s->csc->nb[1];
-  nb[2] = s->csc->nb[2];
+  for (int k = 0; k < kPrBins; ++k) nb[k] = s->csc->nb[k];
   *out = a;
   return cuda_err(c, cudaGetLastError(), "batch prep");
+}
+
+// Copies a renumbered vertex vector out in vertex order (host or device destination).
+template <typename T>
+static int unpermute_out(Ctx* c, const T* src, void* out, int where, const char* what) {
+  const uint64_t n = c->n;
+  T* dst = (T*)out;
+  T* tmp = nullptr;
+  if (where != CYTOM_PTR_DEVICE) {
+    if (cudaMallocAsync((void**)&tmp, n * sizeof(T), c->stream) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, what);
+    dst = tmp;
+  }
+  permute_kernel<T><<<grid_n(c, n), 256, 0, c->stream>>>(src, c->pr_perm, n, 0, dst);
+  c->launches++;
+  cudaError_t e = cudaSuccess;
+  if (tmp) {
+    e = cudaMemcpyAsync(out, tmp, n * sizeof(T), cudaMemcpyDeviceToHost, c->stream);
+    cudaFreeAsync(tmp, c->stream);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  return cuda_err(c, e, what);
 }
 
 int pagerank_result(Ctx* c, Job* j, void* out, int where) {
@@ -631,10 +740,7 @@ int pagerank_result(Ctx* c, Job* j, void* out, int where) {
       src = s->rank;
     }
   }
-  cudaMemcpyKind k = where == CYTOM_PTR_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-  cudaError_t e = cudaMemcpyAsync(out, src, n * 4, k, c->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-  return cuda_err(c, e, "pagerank result");
+  return unpermute_out<float>(c, src, out, where, "pagerank result");
 }
 
 int pagerank_result64(Ctx* c, Job* j, double* out, int where) {
@@ -645,10 +751,7 @@ int pagerank_result64(Ctx* c, Job* j, double* out, int where) {
   cudaMemcpyAsync(&ls, j->ls, sizeof(ls), cudaMemcpyDeviceToHost, c->stream);
   cudaStreamSynchronize(c->stream);
   const double* r = ((ls.iter & 1u) == 0) ? s->r64 : s->r64n;
-  cudaMemcpyKind k = where == CYTOM_PTR_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-  cudaError_t e = cudaMemcpyAsync(out, r, c->n * 8, k, c->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-  return cuda_err(c, e, "pagerank result64");
+  return unpermute_out<double>(c, r, out, where, "pagerank result64");
 }
 
 
@@ -730,10 +833,18 @@ int pagerank_set_teleport(Ctx* c, Job* j, const double* t, int where) {
     s->tele = nullptr;
     return CYTOM_OK;
   }
+  int prc = pr_ensure_perm(c);
+  if (prc) return prc;
   if (!s->tele && cudaMalloc(&s->tele, c->n * 8) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "teleport");
-  cudaError_t e = cudaMemcpyAsync(s->tele, t, c->n * 8,
+  // kept in the renumbering
+  double* tmp = nullptr;
+  if (cudaMallocAsync((void**)&tmp, c->n * 8, c->stream) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "teleport");
+  cudaError_t e = cudaMemcpyAsync(tmp, t, c->n * 8,
                                   where == CYTOM_PTR_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                                   c->stream);
+  permute_kernel<double><<<grid_n(c, c->n), 256, 0, c->stream>>>(tmp, c->pr_perm, c->n, 1, s->tele);
+  c->launches++;
+  cudaFreeAsync(tmp, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   return cuda_err(c, e, "teleport upload");
 }
@@ -772,8 +883,8 @@ __global__ void dangling_sum_kernel(const T* __restrict__ r, const double* __res
 // dL/dw of every stored edge u -> k, in store order:
 // alpha * r_u / s_u * (lambda_k - (P^T lambda)_u), evaluated in FP64.
 template <typename T>
-__global__ void grad_w_kernel(const StoreDesc* __restrict__ sd, const T* __restrict__ r,
-                              const T* __restrict__ lam, const T* __restrict__ pt,
+__global__ void grad_w_kernel(const StoreDesc* __restrict__ sd, const uint32_t* __restrict__ perm,
+                              const T* __restrict__ r, const T* __restrict__ lam, const T* __restrict__ pt,
                               const double* __restrict__ wsum, double alpha, float* __restrict__ gw) {
   const uint64_t E = sd->E;
   const uint32_t lT = sd->lT, lvpt = sd->lvpt;
@@ -783,20 +894,20 @@ __global__ void grad_w_kernel(const StoreDesc* __restrict__ sd, const T* __restr
     uint32_t t = sd->chunk_tile[e >> 7];
     while (sd->tile_ptr[t + 1] <= e) ++t;
     const uint32_t p = sd->edges[e];
-    const uint32_t u = ((t >> lT) << lvpt) | (p >> 16);
-    const uint32_t k = ((t & ymask) << lvpt) | (p & 0xFFFFu);
+    const uint32_t u = perm[((t >> lT) << lvpt) | (p >> 16)];
+    const uint32_t k = perm[((t & ymask) << lvpt) | (p & 0xFFFFu)];
     gw[e] = (float)(alpha * (double)r[u] / wsum[u] * ((double)lam[k] - (double)pt[u]));
   }
 }
 
 // dL/dt_v = ((1 - alpha) + alpha * D) * lambda_v.
 template <typename T>
-__global__ void grad_t_kernel(const T* __restrict__ lam, uint64_t n, const double* __restrict__ dang,
-                              double alpha, float* __restrict__ gt) {
+__global__ void grad_t_kernel(const T* __restrict__ lam, const uint32_t* __restrict__ perm, uint64_t n,
+                              const double* __restrict__ dang, double alpha, float* __restrict__ gt) {
   const double f = (1.0 - alpha) + alpha * dang[0];
   uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride)
-    gt[v] = (float)(f * (double)lam[v]);
+    gt[v] = (float)(f * (double)lam[perm[v]]);
 }
 
 // Adjoint of L = c . r at the converged ranks of WPAGERANK job j: solves
@@ -829,9 +940,17 @@ int pagerank_adjoint(Ctx* c, Job* j, const double* cv, int cwhere, float* d_w, f
   // the forward's newest ranks
   LoopState fls;
   e = cudaMemcpyAsync(&fls, j->ls, sizeof(LoopState), cudaMemcpyDeviceToHost, c->stream);
+  double* ctmp = nullptr;
+  if (e == cudaSuccess && cudaMallocAsync((void**)&ctmp, n * 8, c->stream) != cudaSuccess)
+    return set_err(c, CYTOM_ERR_OOM, "adjoint setup");
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(s->cvec, cv, n * 8, cwhere == CYTOM_PTR_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+    e = cudaMemcpyAsync(ctmp, cv, n * 8, cwhere == CYTOM_PTR_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                         c->stream);
+  if (e == cudaSuccess) {
+    permute_kernel<double><<<grid_n(c, n), 256, 0, c->stream>>>(ctmp, c->pr_perm, n, 1, s->cvec);
+    c->launches++;
+  }
+  if (ctmp) cudaFreeAsync(ctmp, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_err(c, e, "adjoint setup");
   const unsigned pf = fls.iter & 1u;
@@ -886,13 +1005,15 @@ int pagerank_adjoint(Ctx* c, Job* j, const double* cv, int cwhere, float* d_w, f
   if (f32) {
     const float* lam = (pa == 0) ? s->lam : s->lam + n;
     dangling_sum_kernel<float><<<grid_n(c, n), 256, 0, c->stream>>>(r32, g->wsum, n, dang);
-    if (E) grad_w_kernel<float><<<grid_n(c, E), 256, 0, c->stream>>>(c->dsd, r32, lam, s->pt, g->wsum, a.alpha, gw);
-    grad_t_kernel<float><<<grid_n(c, n), 256, 0, c->stream>>>(lam, n, dang, a.alpha, gt);
+    if (E)
+      grad_w_kernel<float><<<grid_n(c, E), 256, 0, c->stream>>>(c->dsd, c->pr_perm, r32, lam, s->pt, g->wsum, a.alpha, gw);
+    grad_t_kernel<float><<<grid_n(c, n), 256, 0, c->stream>>>(lam, c->pr_perm, n, dang, a.alpha, gt);
   } else {
     const double* lam = (pa == 0) ? s->lam64 : s->lam64 + n;
     dangling_sum_kernel<double><<<grid_n(c, n), 256, 0, c->stream>>>(r64, g->wsum, n, dang);
-    if (E) grad_w_kernel<double><<<grid_n(c, E), 256, 0, c->stream>>>(c->dsd, r64, lam, s->pt64, g->wsum, a.alpha, gw);
-    grad_t_kernel<double><<<grid_n(c, n), 256, 0, c->stream>>>(lam, n, dang, a.alpha, gt);
+    if (E)
+      grad_w_kernel<double><<<grid_n(c, E), 256, 0, c->stream>>>(c->dsd, c->pr_perm, r64, lam, s->pt64, g->wsum, a.alpha, gw);
+    grad_t_kernel<double><<<grid_n(c, n), 256, 0, c->stream>>>(lam, c->pr_perm, n, dang, a.alpha, gt);
   }
   c->launches += 3;
   cudaEventRecord(c->run_b, c->stream);

@@ -19,8 +19,13 @@
 
 namespace cytom {
 
-constexpr uint32_t kBinSmall = 16;
-constexpr uint32_t kBinMedium = 4096;
+// Targets are binned by in-degree: bin k holds in-degrees in (pr_bin_hi(k-1), pr_bin_hi(k)];
+// its pull uses pr_bin_vw(k) lanes per target (1 = one thread, 0 = one whole block).
+constexpr int kPrBins = 5;
+__host__ __device__ constexpr uint32_t pr_bin_hi(int k) {
+  return k == 0 ? 4u : k == 1 ? 32u : k == 2 ? 256u : k == 3 ? 4096u : 0xFFFFFFFFu;
+}
+__host__ __device__ constexpr int pr_bin_vw(int k) { return k == 0 ? 1 : k == 1 ? 4 : k == 2 ? 8 : k == 3 ? 32 : 0; }
 constexpr int PR_T = 256;
 constexpr int PR_BLOCK_T = 256;
 
@@ -80,7 +85,7 @@ struct Acc64 {
 struct PrArgs {
   const uint32_t* csc_src;
   const uint32_t* csc_ptr;
-  const uint32_t* bins;
+  const uint32_t* bins;     // targets grouped by in-degree bin (pr_bin_hi), bin after bin
   uint64_t bin_off, bin_count;
   const uint32_t* deg;      // out-degree used for contributions
   float* rank;
@@ -351,44 +356,46 @@ __device__ __forceinline__ double pr_sum_thread(const PrArgs& a, uint32_t v) {
   }
 }
 
-// The same by one warp (16 < in-degree <= 4096); every lane returns the sum.
-template <int MODE, bool PERSIST>
-__device__ __forceinline__ double pr_sum_warp(const PrArgs& a, uint32_t v, unsigned lane) {
-  const uint32_t lo = a.csc_ptr[v], hi = a.csc_ptr[v + 1];
+// The same by a group of VW lanes (lanes of one group are VW consecutive lanes of a
+// warp; every lane of the warp calls it, an idle group with lo = hi): lane gl of the
+// group sums edges lo+gl, lo+gl+VW, ... in order, then the group merges its lanes by an
+// xor tree. Every lane of the group returns the sum.
+template <int MODE, bool PERSIST, int VW>
+__device__ __forceinline__ double pr_sum_group(const PrArgs& a, uint32_t lo, uint32_t hi, unsigned gl) {
   if constexpr (pr_is64<MODE>()) {
     double s = 0.0;
-    uint32_t e = lo + lane;
-    for (; e + 96 < hi; e += 128) {
-      const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + 32], s2 = a.csc_src[e + 64], s3 = a.csc_src[e + 96];
-      const double c0 = pr_c64<MODE, PERSIST>(a, e, s0), c1 = pr_c64<MODE, PERSIST>(a, e + 32, s1),
-                   c2 = pr_c64<MODE, PERSIST>(a, e + 64, s2), c3 = pr_c64<MODE, PERSIST>(a, e + 96, s3);
+    uint32_t e = lo + gl;
+    for (; e + 3 * VW < hi; e += 4 * VW) {
+      const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + VW], s2 = a.csc_src[e + 2 * VW], s3 = a.csc_src[e + 3 * VW];
+      const double c0 = pr_c64<MODE, PERSIST>(a, e, s0), c1 = pr_c64<MODE, PERSIST>(a, e + VW, s1),
+                   c2 = pr_c64<MODE, PERSIST>(a, e + 2 * VW, s2), c3 = pr_c64<MODE, PERSIST>(a, e + 3 * VW, s3);
       s += c0;
       s += c1;
       s += c2;
       s += c3;
     }
-    for (; e < hi; e += 32) s += pr_c64<MODE, PERSIST>(a, e, a.csc_src[e]);
+    for (; e < hi; e += VW) s += pr_c64<MODE, PERSIST>(a, e, a.csc_src[e]);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
+    for (int o = VW / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o, VW);
     return s;
   } else {
     Acc32 acc;
     acc.init();
-    uint32_t e = lo + lane;
-    for (; e + 96 < hi; e += 128) {
-      const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + 32], s2 = a.csc_src[e + 64], s3 = a.csc_src[e + 96];
-      const float c0 = pr_c32<MODE, PERSIST>(a, e, s0), c1 = pr_c32<MODE, PERSIST>(a, e + 32, s1),
-                  c2 = pr_c32<MODE, PERSIST>(a, e + 64, s2), c3 = pr_c32<MODE, PERSIST>(a, e + 96, s3);
+    uint32_t e = lo + gl;
+    for (; e + 3 * VW < hi; e += 4 * VW) {
+      const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + VW], s2 = a.csc_src[e + 2 * VW], s3 = a.csc_src[e + 3 * VW];
+      const float c0 = pr_c32<MODE, PERSIST>(a, e, s0), c1 = pr_c32<MODE, PERSIST>(a, e + VW, s1),
+                  c2 = pr_c32<MODE, PERSIST>(a, e + 2 * VW, s2), c3 = pr_c32<MODE, PERSIST>(a, e + 3 * VW, s3);
       acc.add(c0);
       acc.add(c1);
       acc.add(c2);
       acc.add(c3);
     }
-    for (; e < hi; e += 32) acc.add(pr_c32<MODE, PERSIST>(a, e, a.csc_src[e]));
+    for (; e < hi; e += VW) acc.add(pr_c32<MODE, PERSIST>(a, e, a.csc_src[e]));
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const float s2 = __shfl_xor_sync(0xFFFFFFFFu, acc.s, o);
-      const float e2 = __shfl_xor_sync(0xFFFFFFFFu, acc.e, o);
+    for (int o = VW / 2; o > 0; o >>= 1) {
+      const float s2 = __shfl_xor_sync(0xFFFFFFFFu, acc.s, o, VW);
+      const float e2 = __shfl_xor_sync(0xFFFFFFFFu, acc.e, o, VW);
       acc.merge(s2, e2);
     }
     return (double)acc.s + (double)acc.e;

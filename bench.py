@@ -53,6 +53,10 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-steps", type=int, default=4)
     ap.add_argument("--precision-scale", type=int, default=26)
+    ap.add_argument("--profile-only", action="store_true",
+                    help="run preload, warm-up and --profile-steps batches with every launch timed and "
+                         "its algorithmic bytes recorded (host-driven rounds), print the per-class totals "
+                         "and exit: pairs with an ncu capture of the same command")
     ap.add_argument("--programs", default="bfs,cc,sssp",
                     help="vertex programs run after every batch (profiling cases use a subset)")
     ap.add_argument("--preload", type=int, default=0,
@@ -221,11 +225,23 @@ def main():
 
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
            torch.cuda.Event(enable_timing=True)) for _ in range(nsteps)]
+    if args.profile_only:
+        eng.set_profiling(True)
     if args.preload:
         eng.insert_edges_device(d_src.data_ptr(), d_tgt.data_ptr(), d_w.data_ptr(), args.preload * B)
         eng.do_global_compaction()
     for k in range(args.preload, args.preload + args.warmup):
         step(eng, progs, k, (d_src, d_tgt, d_w))
+    if args.profile_only:
+        for k in range(args.preload + args.warmup, nsteps):
+            step(eng, progs, k, (d_src, d_tgt, d_w))
+        if rank == 0:
+            print(json.dumps({"profile_only": True, "config": {"scale": args.scale, "batch": B,
+                                                               "steps": nsteps, "programs": args.programs},
+                              "kernel_stats": {k: v for k, v in eng.kernel_stats().items() if v["launches"]}}),
+                  flush=True)
+        eng.close()
+        return
     # streaming-gather shapes tuned once on the warmed-up graph (outside the timed steps)
     tune = eng.autotune() if os.environ.get("CYTOM_AUTOTUNE", "1") != "0" else eng.tune_report()
     if world > 1:

@@ -54,6 +54,7 @@ struct PrState {
   double* r64 = nullptr;      // PAGERANK fp64: r
   double* r64n = nullptr;     // PAGERANK fp64: r_next
   double* contrib64 = nullptr;
+  float* lo = nullptr;        // PAGERANK / WPAGERANK fp32: low words of the ranks (2 x n)
   uint32_t* fa2 = nullptr;    // PR_DELTA: frontier bitmaps by parity (2 x n/32)
   bool need_residual = true;
   uint64_t seen_version = ~0ULL;
@@ -483,6 +484,7 @@ int pagerank_alloc(Ctx* c, Job* j) {
   } else if (j->params.kahan) {
     ok = ok && cudaMalloc(&s->rank, n * 4) == cudaSuccess;
     ok = ok && cudaMalloc(&s->comp, n * 4) == cudaSuccess;
+    ok = ok && cudaMalloc(&s->lo, 2 * n * 4) == cudaSuccess;
     ok = ok && cudaMalloc(&s->contrib, n * 4) == cudaSuccess;
   } else {
     ok = ok && cudaMalloc(&s->r64, n * 8) == cudaSuccess;
@@ -500,7 +502,7 @@ int pagerank_alloc(Ctx* c, Job* j) {
 void pagerank_free(Job* j) {
   PrState* s = prs(j);
   if (!s) return;
-  void* ptrs[] = {s->rank, s->comp, s->delta, s->contrib, s->r64, s->r64n, s->contrib64, s->fa2,
+  void* ptrs[] = {s->rank, s->comp, s->delta, s->contrib, s->r64, s->r64n, s->contrib64, s->lo, s->fa2,
                   s->tele, s->lam, s->lam64, s->pt, s->pt64, s->cvec, s->adj_ls};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -533,6 +535,7 @@ int pagerank_init(Ctx* c, Job* j) {
     pr_fill64_kernel<<<g, 256, 0, c->stream>>>(s->r64, 1.0 / (double)n, n);
     c->launches++;
   }
+  if (s->lo) cudaMemsetAsync(s->lo, 0, 2 * n * 4, c->stream);
   s->need_residual = true;
   return cuda_err(c, cudaGetLastError(), "pagerank init");
 }
@@ -610,6 +613,8 @@ int pagerank_run(Ctx* c, Job* j) {
   a.bins = s->csc->bins;
   a.rank = s->rank;
   a.comp = s->comp;
+  a.lo0 = s->lo;
+  a.lo1 = s->lo ? s->lo + c->n : nullptr;
   a.delta = s->delta;
   a.contrib = s->contrib;
   a.r64 = s->r64;
@@ -669,6 +674,8 @@ int pagerank_batch_prep(Ctx* c, Job* j, PrArgs* out, uint64_t* nb, int* first_mo
   a.bins = s->csc->bins;
   a.rank = s->rank;
   a.comp = s->comp;
+  a.lo0 = s->lo;
+  a.lo1 = s->lo ? s->lo + c->n : nullptr;
   a.delta = s->delta;
   a.contrib = s->contrib;
   a.r64 = s->r64;
@@ -797,6 +804,8 @@ static PrArgs wargs(Ctx* c, Job* j, const WGraph& g) {
   a.tele = s->tele;
   a.rank = s->rank;
   a.comp = s->comp;
+  a.lo0 = s->lo;
+  a.lo1 = s->lo ? s->lo + c->n : nullptr;
   a.contrib = s->contrib;
   a.r64 = s->r64;
   a.r64n = s->r64n;

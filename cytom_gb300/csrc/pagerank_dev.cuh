@@ -96,6 +96,8 @@ struct PrArgs {
   double* r64n;
   double* contrib64;
   uint32_t* fa2;            // 2 x nwords (PR_DELTA)
+  float* lo0;               // FP32 PAGERANK / WPAGERANK: low words of the ranks (rank + lo0,
+  float* lo1;               //   comp + lo1): each rank is carried as an unevaluated float pair
   const float* csc_w;       // weighted modes: raw weight of each in-edge (CSC) / out-edge (CSR)
   const double* wsum;       // weighted modes: out-weight sum s_u of each vertex
   const double* tele;       // weighted modes: teleport vector (NULL = uniform 1/n)
@@ -151,19 +153,23 @@ __device__ __forceinline__ double pr_contrib_range(const PrArgs& a, unsigned p, 
     }
   } else if (MODE == PR_NORM32) {
     const float* r = (p == 0) ? a.rank : a.comp;
+    const float* rl = (p == 0) ? a.lo0 : a.lo1;
+    // the contribution is an FP32 quotient of the high word (the low word is below its
+    // rounding); the low word enters the FP64 dangling sum and the residual
     for (uint64_t u = lo + tid; u < hi; u += nthr) {
       const uint32_t d = a.deg[u];
-      const float rv = pr_ld<PERSIST>(r + u);
-      a.contrib[u] = d ? rv / (float)d : 0.f;
-      if (!d) dangling += (double)rv;
+      const float rh = pr_ld<PERSIST>(r + u);
+      a.contrib[u] = d ? rh / (float)d : 0.f;
+      if (!d) dangling += (double)rh + (double)pr_ld<PERSIST>(rl + u);
     }
   } else if (MODE == PR_W32) {
     const float* r = (p == 0) ? a.rank : a.comp;
+    const float* rl = (p == 0) ? a.lo0 : a.lo1;
     for (uint64_t u = lo + tid; u < hi; u += nthr) {
       const double s = a.wsum[u];
-      const float rv = pr_ld<PERSIST>(r + u);
-      a.contrib[u] = s > 0.0 ? rv / (float)s : 0.f;
-      if (!(s > 0.0)) dangling += (double)rv;
+      const float rh = pr_ld<PERSIST>(r + u);
+      a.contrib[u] = s > 0.0 ? rh / (float)s : 0.f;
+      if (!(s > 0.0)) dangling += (double)rh + (double)pr_ld<PERSIST>(rl + u);
     }
   } else if (MODE == PR_W64) {
     const double* r = (p == 0) ? a.r64 : a.r64n;
@@ -227,11 +233,15 @@ __device__ __forceinline__ double pr_finish(const PrArgs& a, uint64_t v, double 
                                             double* rsum) {
   if (MODE == PR_NORM32) {
     const float* r = (p == 0) ? a.rank : a.comp;
+    const float* rl = (p == 0) ? a.lo0 : a.lo1;
     float* rn = (p == 0) ? a.comp : a.rank;
-    const float nv = (float)(a.base + a.alpha * (sum + dang));
-    const double d = fabs((double)nv - (double)pr_ld<PERSIST>(r + v));
-    rn[v] = nv;
-    *rsum += (double)nv;
+    float* rnl = (p == 0) ? a.lo1 : a.lo0;
+    const double nv = a.base + a.alpha * (sum + dang);
+    const float hi = (float)nv;
+    const double d = fabs(nv - ((double)pr_ld<PERSIST>(r + v) + (double)pr_ld<PERSIST>(rl + v)));
+    rn[v] = hi;
+    rnl[v] = (float)(nv - (double)hi);
+    *rsum += nv;
     return d;
   } else if (MODE == PR_NORM64) {
     const double* r = (p == 0) ? a.r64 : a.r64n;
@@ -246,11 +256,14 @@ __device__ __forceinline__ double pr_finish(const PrArgs& a, uint64_t v, double 
     const double nv = tv * ((1.0 - a.alpha) + a.alpha * dang) + a.alpha * sum;
     if (MODE == PR_W32) {
       const float* r = (p == 0) ? a.rank : a.comp;
+      const float* rl = (p == 0) ? a.lo0 : a.lo1;
       float* rn = (p == 0) ? a.comp : a.rank;
-      const float nf = (float)nv;
-      rn[v] = nf;
-      *rsum += (double)nf;
-      return fabs((double)nf - (double)pr_ld<PERSIST>(r + v));
+      float* rnl = (p == 0) ? a.lo1 : a.lo0;
+      const float hi = (float)nv;
+      rn[v] = hi;
+      rnl[v] = (float)(nv - (double)hi);
+      *rsum += nv;
+      return fabs(nv - ((double)pr_ld<PERSIST>(r + v) + (double)pr_ld<PERSIST>(rl + v)));
     } else {
       const double* r = (p == 0) ? a.r64 : a.r64n;
       double* rn = (p == 0) ? a.r64n : a.r64;

@@ -335,11 +335,15 @@ def main():
             run_profile[name] = {"rounds_per_run": rounds / len(runs),
                                  "active_vertices_per_round": sum(st["active_vertices"] for st in runs) / rounds,
                                  "edges_scanned_per_round": sum(st["edges_scanned"] for st in runs) / rounds}
+    # DRAM traffic per launch: the ncu-measured DRAM bytes per algorithmic byte of each
+    # round kind (profiles/gather_traffic_rmat22.md) times this run's algorithmic bytes
     traffic = None
     tfile = ROOT / "profiles" / "gather_traffic.json"
-    if tfile.exists():
+    if tfile.exists() and g_launches:
         try:
-            traffic = json.loads(tfile.read_text()).get("bytes_per_launch")
+            ratio = json.loads(tfile.read_text())["dram_per_algorithmic_byte"]
+            traffic = (ratio["dense_stream"] * ks["gather"]["algo_bytes"]
+                       + ratio["sparse_directory"] * ks["gather_sparse"]["algo_bytes"]) / g_launches
         except Exception:
             traffic = None
 

@@ -221,7 +221,7 @@ int job_run(Ctx* c, Job* j, cytom_run_stats* st) {
   rc = prof_flush(c);
   if (rc) return rc;
   if (ls.err) return set_err(c, CYTOM_ERR_TIMEOUT, "a bounded device wait gave up");
-  if (j->last_run_graph) c->launches += 5ULL * ls.iter;
+  if (j->last_run_graph) c->launches += 4ULL * ls.iter;  // per round: two gathers, chunk pass, apply
   if (st) {
     memset(st, 0, sizeof(*st));
     st->iterations = ls.iter;

@@ -73,6 +73,8 @@ struct LoopState {
   double change_sum;        // PageRank-delta: sum of all rank changes of the run
   double best_resid;        // PageRank FP32: best residual so far (rounding-floor detection)
   unsigned int stall;       // rounds without a residual improvement
+  unsigned int apply_done;  // blocks of the running apply that finished (last one runs control)
+  unsigned int sel_rounds;  // rounds started by the captured loop (bounds it independently)
   unsigned int pad2;
 };
 

@@ -54,14 +54,30 @@ __global__ void begin_kernel(const JobDesc* __restrict__ jd, const StoreDesc* __
     ls->count_edges = 0;
     ls->edges_scanned = 0;
     ls->active_total = 0;
+    ls->apply_done = 0;
+    ls->sel_rounds = 0;
   }
 }
 
-// Apply over every frontier word (apply_step), then the block's counters (apply_flush).
+// Apply over every frontier word (apply_step), then the block's counters (apply_flush);
+// the last block to finish runs the round's control step and, inside a captured loop,
+// sets the loop's while-condition. Independently of that, block 0 counts the rounds a
+// captured loop started and ends the loop with an error status past max_iterations + 1,
+// so the loop is bounded whatever the control step does.
 __global__ void __launch_bounds__(APPLY_T) apply_minprop_kernel(const JobDesc* __restrict__ jd,
-                                                                const StoreDesc* __restrict__ sd,
-                                                                int initial) {
+                                                                const StoreDesc* __restrict__ sd, int initial,
+                                                                cudaGraphConditionalHandle h, int use_handle) {
   LoopState* ls = jd->ls;
+  if (use_handle && blockIdx.x == 0 && threadIdx.x == 0) {
+    volatile LoopState* vls = ls;
+    const unsigned started = vls->sel_rounds + 1;
+    vls->sel_rounds = started;
+    if ((uint64_t)started > (uint64_t)vls->max_iter + 2) {
+      vls->err = 2;
+      vls->cont = 0;
+      cudaGraphSetConditional(h, 0u);
+    }
+  }
   if (!ls->cont) return;
   const unsigned pw = initial ? 0u : ((ls->iter & 1u) ^ 1u);
   const uint64_t nwords = (sd->n + 31) >> 5;
@@ -71,12 +87,15 @@ __global__ void __launch_bounds__(APPLY_T) apply_minprop_kernel(const JobDesc* _
   for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < nwords; base += stride)
     apply_step<false>(jd, sd, pw, base, cnt, teps);
   apply_flush(ls, pw, cnt, teps);
-}
-
-__global__ void control_kernel(const JobDesc* __restrict__ jd, const StoreDesc* __restrict__ sd,
-                               cudaGraphConditionalHandle h, int initial, int use_handle) {
-  const unsigned cont = control_step(jd, sd, initial);
-  if (use_handle) cudaGraphSetConditional(h, cont);
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&ls->apply_done, 1u) == gridDim.x - 1) {
+      __threadfence();
+      atomicExch(&ls->apply_done, 0u);
+      const unsigned cont = control_step(jd, sd, initial);
+      if (use_handle) cudaGraphSetConditional(h, cont);
+    }
+  }
 }
 
 // Gather for BFS (ALGO 0), CC (1), SSSP (2). A warp owns a 128-edge chunk: lane l
@@ -573,7 +592,10 @@ static cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGr
   return cudaGraphAddKernelNode(node, g, deps, ndeps, &kp);
 }
 
-// Graph: begin -> seeding apply -> control(initial) -> while(cond) { gather -> apply -> control }.
+// Graph: begin -> seeding apply + control -> while(cont) { dense gather -> sparse gather ->
+// chunk pass -> apply + control }. Dense and sparse are picked on the device per round;
+// the kernels not needed exit at once (measured cheaper than conditional IF nodes around
+// them: 182-189 vs 166 GTEPS on the RMAT-22 stream).
 static int build_minprop_graph(Ctx* c, Job* j) {
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaGraphCreate(&g, 0);
@@ -586,39 +608,30 @@ static int build_minprop_graph(Ctx* c, Job* j) {
   int adaptive = c->cfg.enable_adaptive_scheduling;
   int zero = 0, one = 1;
   int gper = grid_persistent(c, 8);
-  cudaGraphNode_t n_begin, n_apply0, n_ctl0, n_while, b_gather, b_sparse, b_chunks, b_apply, b_ctl;
+  cudaGraphNode_t n_begin, n_apply0, n_while, b_apply, d_gather, s_sparse, c_chunks;
   void* a_begin[] = {(void*)&jd, (void*)&sd, (void*)&max_iter};
   if (e == cudaSuccess)
     e = add_kernel(g, &n_begin, nullptr, 0, (void*)begin_kernel, dim3(std::max(1, c->num_sms)), dim3(256), a_begin);
-  void* a_apply0[] = {(void*)&jd, (void*)&sd, (void*)&one};
+  void* a_apply0[] = {(void*)&jd, (void*)&sd, (void*)&one, (void*)&h, (void*)&one};
   if (e == cudaSuccess)
     e = add_kernel(g, &n_apply0, &n_begin, 1, (void*)apply_minprop_kernel, dim3(gper), dim3(APPLY_T), a_apply0);
-  void* a_ctl0[] = {(void*)&jd, (void*)&sd, (void*)&h, (void*)&one, (void*)&one};
-  if (e == cudaSuccess)
-    e = add_kernel(g, &n_ctl0, &n_apply0, 1, (void*)control_kernel, dim3(1), dim3(1), a_ctl0);
   cudaGraphNodeParams cp{};
   cp.type = cudaGraphNodeTypeConditional;
   cp.conditional.handle = h;
   cp.conditional.type = cudaGraphCondTypeWhile;
   cp.conditional.size = 1;
-  if (e == cudaSuccess) e = cudaGraphAddNode(&n_while, g, &n_ctl0, nullptr, 1, &cp);
+  if (e == cudaSuccess) e = cudaGraphAddNode(&n_while, g, &n_apply0, nullptr, 1, &cp);
   if (e == cudaSuccess) {
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     void* a_g[] = {(void*)&jd, (void*)&sd, (void*)&adaptive};
     GatherLaunch gl = gather_launch(c, j->algo);
-    e = add_kernel(body, &b_gather, nullptr, 0, gl.fn, gl.grid, gl.block, a_g, gl.smem);
-    // the round's other gather exits at once: dense and sparse are picked on the device
-    if (e == cudaSuccess)
-      e = add_kernel(body, &b_sparse, &b_gather, 1, sparse_fn(j->algo), dim3(gper), dim3(256), a_g);
+    e = add_kernel(body, &d_gather, nullptr, 0, gl.fn, gl.grid, gl.block, a_g, gl.smem);
+    if (e == cudaSuccess) e = add_kernel(body, &s_sparse, &d_gather, 1, sparse_fn(j->algo), dim3(gper), dim3(256), a_g);
     void* a_q[] = {(void*)&jd, (void*)&sd};
+    if (e == cudaSuccess) e = add_kernel(body, &c_chunks, &s_sparse, 1, chunks_fn(j->algo), dim3(gper), dim3(256), a_q);
+    void* a_a[] = {(void*)&jd, (void*)&sd, (void*)&zero, (void*)&h, (void*)&one};
     if (e == cudaSuccess)
-      e = add_kernel(body, &b_chunks, &b_sparse, 1, chunks_fn(j->algo), dim3(gper), dim3(256), a_q);
-    void* a_a[] = {(void*)&jd, (void*)&sd, (void*)&zero};
-    if (e == cudaSuccess)
-      e = add_kernel(body, &b_apply, &b_chunks, 1, (void*)apply_minprop_kernel, dim3(gper), dim3(APPLY_T), a_a);
-    void* a_c[] = {(void*)&jd, (void*)&sd, (void*)&h, (void*)&zero, (void*)&one};
-    if (e == cudaSuccess)
-      e = add_kernel(body, &b_ctl, &b_apply, 1, (void*)control_kernel, dim3(1), dim3(1), a_c);
+      e = add_kernel(body, &b_apply, &c_chunks, 1, (void*)apply_minprop_kernel, dim3(gper), dim3(APPLY_T), a_a);
   }
   if (e == cudaSuccess) e = cudaGraphInstantiate(&j->loop_exec, g, 0);
   cudaGraphDestroy(g);
@@ -680,7 +693,7 @@ int minprop_run(Ctx* c, Job* j) {
     if (j->loop_exec) {
       j->last_run_graph = true;
       cudaError_t e = cudaGraphLaunch(j->loop_exec, c->stream);
-      c->launches += 3;  // per-round launches are counted from the loop state afterwards
+      c->launches += 2;  // per-round launches are counted from the loop state afterwards
       if (e != cudaSuccess) return cuda_err(c, e, "graph launch");
       return CYTOM_OK;
     }
@@ -689,9 +702,8 @@ int minprop_run(Ctx* c, Job* j) {
   j->last_run_graph = false;
   int gper = grid_persistent(c, 8);
   begin_kernel<<<std::max(1, c->num_sms), 256, 0, c->stream>>>(j->d, c->dsd, max_iter);
-  apply_minprop_kernel<<<gper, APPLY_T, 0, c->stream>>>(j->d, c->dsd, 1);
-  control_kernel<<<1, 1, 0, c->stream>>>(j->d, c->dsd, 0, 1, 0);
-  c->launches += 3;
+  apply_minprop_kernel<<<gper, APPLY_T, 0, c->stream>>>(j->d, c->dsd, 1, 0, 0);
+  c->launches += 2;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_err(c, e, "run prologue");
   const JobDesc* jd = j->d;
@@ -730,10 +742,9 @@ int minprop_run(Ctx* c, Job* j) {
         if (e != cudaSuccess) return cuda_err(c, e, "sparse gather");
       }
       int s2 = prof_begin(c, KC_APPLY);
-      apply_minprop_kernel<<<gper, APPLY_T, 0, c->stream>>>(j->d, c->dsd, 0);
+      apply_minprop_kernel<<<gper, APPLY_T, 0, c->stream>>>(j->d, c->dsd, 0, 0, 0);
       prof_end(c, s2, -1.0);
-      control_kernel<<<1, 1, 0, c->stream>>>(j->d, c->dsd, 0, 0, 0);
-      c->launches += 2;
+      c->launches += 1;
       ++round;
       continue;
     }
@@ -745,9 +756,8 @@ int minprop_run(Ctx* c, Job* j) {
       void* a_q[] = {(void*)&jd, (void*)&sd};
       if (e == cudaSuccess) e = cudaLaunchKernel(chunks_fn(j->algo), dim3(gper), dim3(256), a_q, 0, c->stream);
       if (e != cudaSuccess) return cuda_err(c, e, "sparse gather");
-      apply_minprop_kernel<<<gper, APPLY_T, 0, c->stream>>>(j->d, c->dsd, 0);
-      control_kernel<<<1, 1, 0, c->stream>>>(j->d, c->dsd, 0, 0, 0);
-      c->launches += 4;
+      apply_minprop_kernel<<<gper, APPLY_T, 0, c->stream>>>(j->d, c->dsd, 0, 0, 0);
+      c->launches += 3;
     }
     e = cudaMemcpyAsync(c->h_pinned, &j->ls->cont, 4, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);

@@ -327,7 +327,7 @@ __global__ void __launch_bounds__(SG_T, MINB) gather_stream_kernel(const JobDesc
 // Sparse gather (sparse_group over every group of 32 items) and its chunk pass
 // (sparse_chunk over the queue the first pass filled).
 template <int ALGO>
-__global__ void __launch_bounds__(256) gather_sparse_kernel(const JobDesc* __restrict__ jd,
+__global__ void __launch_bounds__(256, 4) gather_sparse_kernel(const JobDesc* __restrict__ jd,
                                                              const StoreDesc* __restrict__ sd, int adaptive) {
   LoopState* ls = jd->ls;
   if (!ls->cont || ls->mode != 1) return;
@@ -346,7 +346,7 @@ __global__ void __launch_bounds__(256) gather_sparse_kernel(const JobDesc* __res
 }
 
 template <int ALGO>
-__global__ void __launch_bounds__(256) gather_sparse_chunks(const JobDesc* __restrict__ jd,
+__global__ void __launch_bounds__(256, 4) gather_sparse_chunks(const JobDesc* __restrict__ jd,
                                                              const StoreDesc* __restrict__ sd) {
   LoopState* ls = jd->ls;
   if (!ls->cont || ls->mode != 1) return;
@@ -567,6 +567,18 @@ static int launch_gather(Ctx* c, Job* j, int adaptive) {
   return cuda_err(c, e, "gather");
 }
 
+// One wave of resident blocks: grid = SMs x blocks of `fn` that fit on an SM at once
+// (a larger grid runs in several waves, which costs a sparse round of a few microseconds
+// of work one wave per extra set of blocks).
+static int resident_grid(Ctx* c, void* fn, int threads) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  return c->num_sms * per_sm;
+}
+
 static void* sparse_fn(int algo) {
   return algo == CYTOM_ALGO_BFS ? (void*)gather_sparse_kernel<0>
          : algo == CYTOM_ALGO_CC ? (void*)gather_sparse_kernel<1>
@@ -607,14 +619,16 @@ static int build_minprop_graph(Ctx* c, Job* j) {
   unsigned max_iter = (unsigned)std::min<uint64_t>(j->params.max_iterations, 0xFFFFFFFFu);
   int adaptive = c->cfg.enable_adaptive_scheduling;
   int zero = 0, one = 1;
-  int gper = grid_persistent(c, 8);
+  const int g_apply = resident_grid(c, (void*)apply_minprop_kernel, APPLY_T);
+  const int g_sparse = resident_grid(c, sparse_fn(j->algo), 256);
+  const int g_chunks = resident_grid(c, chunks_fn(j->algo), 256);
   cudaGraphNode_t n_begin, n_apply0, n_while, b_apply, d_gather, s_sparse, c_chunks;
   void* a_begin[] = {(void*)&jd, (void*)&sd, (void*)&max_iter};
   if (e == cudaSuccess)
     e = add_kernel(g, &n_begin, nullptr, 0, (void*)begin_kernel, dim3(std::max(1, c->num_sms)), dim3(256), a_begin);
   void* a_apply0[] = {(void*)&jd, (void*)&sd, (void*)&one, (void*)&h, (void*)&one};
   if (e == cudaSuccess)
-    e = add_kernel(g, &n_apply0, &n_begin, 1, (void*)apply_minprop_kernel, dim3(gper), dim3(APPLY_T), a_apply0);
+    e = add_kernel(g, &n_apply0, &n_begin, 1, (void*)apply_minprop_kernel, dim3(g_apply), dim3(APPLY_T), a_apply0);
   cudaGraphNodeParams cp{};
   cp.type = cudaGraphNodeTypeConditional;
   cp.conditional.handle = h;
@@ -626,12 +640,14 @@ static int build_minprop_graph(Ctx* c, Job* j) {
     void* a_g[] = {(void*)&jd, (void*)&sd, (void*)&adaptive};
     GatherLaunch gl = gather_launch(c, j->algo);
     e = add_kernel(body, &d_gather, nullptr, 0, gl.fn, gl.grid, gl.block, a_g, gl.smem);
-    if (e == cudaSuccess) e = add_kernel(body, &s_sparse, &d_gather, 1, sparse_fn(j->algo), dim3(gper), dim3(256), a_g);
+    if (e == cudaSuccess)
+      e = add_kernel(body, &s_sparse, &d_gather, 1, sparse_fn(j->algo), dim3(g_sparse), dim3(256), a_g);
     void* a_q[] = {(void*)&jd, (void*)&sd};
-    if (e == cudaSuccess) e = add_kernel(body, &c_chunks, &s_sparse, 1, chunks_fn(j->algo), dim3(gper), dim3(256), a_q);
+    if (e == cudaSuccess)
+      e = add_kernel(body, &c_chunks, &s_sparse, 1, chunks_fn(j->algo), dim3(g_chunks), dim3(256), a_q);
     void* a_a[] = {(void*)&jd, (void*)&sd, (void*)&zero, (void*)&h, (void*)&one};
     if (e == cudaSuccess)
-      e = add_kernel(body, &b_apply, &c_chunks, 1, (void*)apply_minprop_kernel, dim3(gper), dim3(APPLY_T), a_a);
+      e = add_kernel(body, &b_apply, &c_chunks, 1, (void*)apply_minprop_kernel, dim3(g_apply), dim3(APPLY_T), a_a);
   }
   if (e == cudaSuccess) e = cudaGraphInstantiate(&j->loop_exec, g, 0);
   cudaGraphDestroy(g);
@@ -700,9 +716,11 @@ int minprop_run(Ctx* c, Job* j) {
   }
   // host-driven loop (profiling mode or no graph support)
   j->last_run_graph = false;
-  int gper = grid_persistent(c, 8);
+  const int g_apply = resident_grid(c, (void*)apply_minprop_kernel, APPLY_T);
+  const int g_sparse = resident_grid(c, sparse_fn(j->algo), 256);
+  const int g_chunks = resident_grid(c, chunks_fn(j->algo), 256);
   begin_kernel<<<std::max(1, c->num_sms), 256, 0, c->stream>>>(j->d, c->dsd, max_iter);
-  apply_minprop_kernel<<<gper, APPLY_T, 0, c->stream>>>(j->d, c->dsd, 1, 0, 0);
+  apply_minprop_kernel<<<g_apply, APPLY_T, 0, c->stream>>>(j->d, c->dsd, 1, 0, 0);
   c->launches += 2;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_err(c, e, "run prologue");
@@ -733,16 +751,16 @@ int minprop_run(Ctx* c, Job* j) {
         prev_slot = s1;
       } else {
         int s1 = prof_begin(c, KC_OTHER);
-        e = cudaLaunchKernel(sparse_fn(j->algo), dim3(gper), dim3(256), a_g, 0, c->stream);
+        e = cudaLaunchKernel(sparse_fn(j->algo), dim3(g_sparse), dim3(256), a_g, 0, c->stream);
         void* a_q[] = {(void*)&jd, (void*)&sd};
-        if (e == cudaSuccess) e = cudaLaunchKernel(chunks_fn(j->algo), dim3(gper), dim3(256), a_q, 0, c->stream);
+        if (e == cudaSuccess) e = cudaLaunchKernel(chunks_fn(j->algo), dim3(g_chunks), dim3(256), a_q, 0, c->stream);
         c->launches += 2;
         prof_end(c, s1, 0.0);
         prev_slot = s1;
         if (e != cudaSuccess) return cuda_err(c, e, "sparse gather");
       }
       int s2 = prof_begin(c, KC_APPLY);
-      apply_minprop_kernel<<<gper, APPLY_T, 0, c->stream>>>(j->d, c->dsd, 0, 0, 0);
+      apply_minprop_kernel<<<g_apply, APPLY_T, 0, c->stream>>>(j->d, c->dsd, 0, 0, 0);
       prof_end(c, s2, -1.0);
       c->launches += 1;
       ++round;
@@ -752,11 +770,11 @@ int minprop_run(Ctx* c, Job* j) {
     for (int k = 0; k < 4 && round < max_iter; ++k, ++round) {
       int rc = launch_gather(c, j, adaptive);
       if (rc) return rc;
-      e = cudaLaunchKernel(sparse_fn(j->algo), dim3(gper), dim3(256), a_g, 0, c->stream);
+      e = cudaLaunchKernel(sparse_fn(j->algo), dim3(g_sparse), dim3(256), a_g, 0, c->stream);
       void* a_q[] = {(void*)&jd, (void*)&sd};
-      if (e == cudaSuccess) e = cudaLaunchKernel(chunks_fn(j->algo), dim3(gper), dim3(256), a_q, 0, c->stream);
+      if (e == cudaSuccess) e = cudaLaunchKernel(chunks_fn(j->algo), dim3(g_chunks), dim3(256), a_q, 0, c->stream);
       if (e != cudaSuccess) return cuda_err(c, e, "sparse gather");
-      apply_minprop_kernel<<<gper, APPLY_T, 0, c->stream>>>(j->d, c->dsd, 0, 0, 0);
+      apply_minprop_kernel<<<g_apply, APPLY_T, 0, c->stream>>>(j->d, c->dsd, 0, 0, 0);
       c->launches += 3;
     }
     e = cudaMemcpyAsync(c->h_pinned, &j->ls->cont, 4, cudaMemcpyDeviceToHost, c->stream);

@@ -108,6 +108,14 @@ int upload_store_desc(Ctx* c) {
   h.dir = c->dir;
   h.nbw = c->lvpt >= 5 ? (uint32_t)(c->vpt / 32) : 0u;
   h.dir_ok = (c->dir && c->dir_version == c->version && !c->dir_disabled) ? 1 : 0;
+  {
+    static int div = -1;
+    if (div < 0) {
+      const char* ev = getenv("CYTOM_SPARSE_DIV");
+      div = (ev && atoi(ev) > 0) ? atoi(ev) : 8;
+    }
+    h.sparse_div = (uint32_t)div;
+  }
   // pageable source: the copy is staged before the call returns, so h may change later
   cudaError_t e = cudaMemcpyAsync(c->dsd, &h, sizeof(StoreDesc), cudaMemcpyHostToDevice, c->stream);
   return cuda_err(c, e, "store descriptor upload");

@@ -47,6 +47,8 @@ struct StoreDesc {
   const uint32_t* dir;
   uint32_t nbw;                // 32-source blocks per tile row (vpt / 32)
   int dir_ok;                  // directory current (sparse rounds allowed)
+  uint32_t sparse_div;         // sparse round while non-zero frontier words * sparse_div <= all words
+  uint32_t pad_sd;
 };
 
 // Loop state of one job run, in device memory. Kernels index the double-buffered

@@ -169,8 +169,8 @@ __device__ __forceinline__ void apply_flush(LoopState* ls, unsigned pw, unsigned
 // ---- control -------------------------------------------------------------
 // Ends a round (or, `initial`, the seeding apply): advances the round counter, ends the
 // run when nothing changed or max_iterations rounds ran, and picks the next round's
-// gather: sparse (directory, only the listed frontier words) while at most 1/8 of the
-// frontier words are non-zero, dense (stream every active row) above.
+// gather: sparse (directory, only the listed frontier words) while at most 1/sparse_div
+// of the frontier words are non-zero, dense (stream every active row) above.
 __device__ __forceinline__ unsigned control_step(const JobDesc* __restrict__ jd, const StoreDesc* __restrict__ sd,
                                                  int initial) {
   volatile LoopState* ls = jd->ls;
@@ -186,7 +186,7 @@ __device__ __forceinline__ unsigned control_step(const JobDesc* __restrict__ jd,
     ls->active_total = ls->active_total + a;
     ls->cont = (a > 0 && iter < ls->max_iter && ls->err == 0) ? 1u : 0u;
     const uint64_t nwords = (sd->n + 31) >> 5;
-    ls->mode = (sd->dir_ok && sd->adaptive && (uint64_t)ls->nact_words[p] * 8 <= nwords) ? 1u : 0u;
+    ls->mode = (sd->dir_ok && sd->adaptive && (uint64_t)ls->nact_words[p] * sd->sparse_div <= nwords) ? 1u : 0u;
     ls->spq_count = 0;
   }
   return ls->cont;

@@ -32,6 +32,11 @@ int pagerank_adjoint(Ctx* c, Job* j, const double* cv, int cwhere, float* d_w, f
 int set_edge_weights(Ctx* c, const uint32_t* src, const uint32_t* tgt, const uint32_t* w, uint64_t count);
 void pagerank_free(Job* j);
 
+__global__ void complement_kernel(const uint32_t* __restrict__ in, uint64_t n, uint32_t* __restrict__ out) {
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) out[i] = ~in[i];
+}
+
 int set_err(Ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg;
   return code;
@@ -128,7 +133,9 @@ static uint32_t ilog2(uint64_t v) {
 }
 
 // ---- jobs -----------------------------------------------------------------
-static bool is_minprop(int a) { return a == CYTOM_ALGO_BFS || a == CYTOM_ALGO_CC || a == CYTOM_ALGO_SSSP; }
+static bool is_minprop(int a) {
+  return a == CYTOM_ALGO_BFS || a == CYTOM_ALGO_CC || a == CYTOM_ALGO_SSSP || a == CYTOM_ALGO_SSWP;
+}
 
 int job_alloc(Ctx* c, Job* j) {
   cudaError_t e = cudaMalloc(&j->ls, sizeof(LoopState));
@@ -597,19 +604,20 @@ int cytom_get_degrees(cytom_ctx* ctx, uint32_t* out_degree, uint32_t* in_degree)
 
 int cytom_job_create(cytom_ctx* ctx, int algo, const cytom_job_params* params, int* job_id) {
   Ctx* c = (Ctx*)ctx;
-  if (!c || !job_id || algo < CYTOM_ALGO_BFS || algo > CYTOM_ALGO_WPAGERANK) return CYTOM_ERR_INVAL;
+  if (!c || !job_id || algo < CYTOM_ALGO_BFS || algo > CYTOM_ALGO_SSWP) return CYTOM_ERR_INVAL;
   Job* j = new (std::nothrow) Job();
   if (!j) return CYTOM_ERR_OOM;
   j->algo = algo;
   if (params) j->params = *params;
   else cytom_job_params_default(&j->params);
-  if ((algo == CYTOM_ALGO_BFS || algo == CYTOM_ALGO_SSSP) && j->params.start_vertex >= c->n) {
+  if ((algo == CYTOM_ALGO_BFS || algo == CYTOM_ALGO_SSSP || algo == CYTOM_ALGO_SSWP) &&
+      j->params.start_vertex >= c->n) {
     delete j;
     return set_err(c, CYTOM_ERR_RANGE, "start vertex >= vertex count");
   }
-  if (algo == CYTOM_ALGO_SSSP && c->wtype != CYTOM_WEIGHT_U32) {
+  if ((algo == CYTOM_ALGO_SSSP || algo == CYTOM_ALGO_SSWP) && c->wtype != CYTOM_WEIGHT_U32) {
     delete j;
-    return set_err(c, CYTOM_ERR_INVAL, "SSSP needs a store with uint32 weights");
+    return set_err(c, CYTOM_ERR_INVAL, "SSSP and SSWP need a store with uint32 weights");
   }
   if (algo == CYTOM_ALGO_WPAGERANK && c->wtype != CYTOM_WEIGHT_F32) {
     delete j;
@@ -674,7 +682,19 @@ int cytom_get_result(cytom_ctx* ctx, int job_id, void* out, int where) {
   if (!j || !out) return CYTOM_ERR_INVAL;
   if (!is_minprop(j->algo)) return pagerank_result(c, j, out, where);
   cudaMemcpyKind k = where == CYTOM_PTR_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-  cudaError_t e = cudaMemcpyAsync(out, j->h.next, c->n * 4, k, c->stream);
+  const uint32_t* src = j->h.next;
+  uint32_t* tmp = nullptr;
+  cudaError_t e = cudaSuccess;
+  if (j->algo == CYTOM_ALGO_SSWP) {
+    // SSWP runs on complemented values: widths = ~values
+    if (cudaMallocAsync((void**)&tmp, c->n * 4, c->stream) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "result");
+    complement_kernel<<<(unsigned)std::min<uint64_t>((c->n + 255) / 256, (uint64_t)c->num_sms * 8), 256, 0,
+                        c->stream>>>(src, c->n, tmp);
+    c->launches++;
+    src = tmp;
+  }
+  e = cudaMemcpyAsync(out, src, c->n * 4, k, c->stream);
+  if (tmp) cudaFreeAsync(tmp, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   return cuda_err(c, e, "get_result");
 }

@@ -139,7 +139,8 @@ __device__ void unit_dense(const BJob* J, uint32_t st) {
   const unsigned p = ls_iter(jd->ls) & 1u;
   if (!stage_active<true>(jd, sd, st, p, J->adaptive)) return;
   const uint64_t e0 = (uint64_t)st * SG_E;
-  dense_stage<ALGO, true, true>(jd, sd, sd->edges + e0, ALGO == 2 ? sd->wts + e0 : nullptr, st, p, J->adaptive);
+  dense_stage<ALGO, true, true>(jd, sd, sd->edges + e0, mp_weighted<ALGO>() ? sd->wts + e0 : nullptr, st, p,
+                                J->adaptive);
   if (threadIdx.x == 0) {
     const uint64_t rem = sd->E - e0;
     atomicAdd(&jd->ls->edges_scanned, (unsigned long long)(rem < (uint64_t)SG_E ? rem : (uint64_t)SG_E));
@@ -345,16 +346,19 @@ __device__ void run_unit(const BJob* J, unsigned phase, uint32_t unit, int prmod
     case PH_DENSE:
       if (algo == CYTOM_ALGO_BFS) unit_dense<0>(J, unit);
       else if (algo == CYTOM_ALGO_CC) unit_dense<1>(J, unit);
+      else if (algo == CYTOM_ALGO_SSWP) unit_dense<3>(J, unit);
       else unit_dense<2>(J, unit);
       break;
     case PH_SPARSE:
       if (algo == CYTOM_ALGO_BFS) unit_sparse<0>(J, unit);
       else if (algo == CYTOM_ALGO_CC) unit_sparse<1>(J, unit);
+      else if (algo == CYTOM_ALGO_SSWP) unit_sparse<3>(J, unit);
       else unit_sparse<2>(J, unit);
       break;
     case PH_CHUNKS:
       if (algo == CYTOM_ALGO_BFS) unit_chunks<0>(J, unit);
       else if (algo == CYTOM_ALGO_CC) unit_chunks<1>(J, unit);
+      else if (algo == CYTOM_ALGO_SSWP) unit_chunks<3>(J, unit);
       else unit_chunks<2>(J, unit);
       break;
     case PH_PR_CONTRIB:

@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(GATHER_T) gather_minprop_kernel(const JobDesc*
     if (e0 >= E) continue;
     const uint4 ev = *reinterpret_cast<const uint4*>(edges + e0);
     uint4 wv = make_uint4(0, 0, 0, 0);
-    if (ALGO == 2) wv = *reinterpret_cast<const uint4*>(wts + e0);
+    if (mp_weighted<ALGO>()) wv = *reinterpret_cast<const uint4*>(wts + e0);
     // locate the tile of e0: last t in [t0, t1] with tile_ptr[t] <= e0
     uint32_t t = t0;
     if (tile_ptr[t + 1] <= e0) {
@@ -169,16 +169,8 @@ __global__ void __launch_bounds__(GATHER_T) gather_minprop_kernel(const JobDesc*
       if (adaptive && !((fa[u >> 5] >> (u & 31)) & 1u)) continue;
       const uint32_t uv = cur[u];
       if (uv == kInf) continue;
-      uint32_t cand;
-      if (ALGO == 0) {
-        cand = uv + 1;
-      } else if (ALGO == 1) {
-        cand = uv;
-      } else {
-        unsigned long long s = (unsigned long long)uv + wvk[k];
-        if (s >= kInf) continue;
-        cand = (uint32_t)s;
-      }
+      const uint32_t cand = mp_cand<ALGO>(uv, wvk[k]);
+      if (cand == kInf) continue;
       const uint32_t v = (y << lvpt) | (evk[k] & 0xFFFFu);
       if (cand < __ldcg(next + v)) {
         uint32_t old = atomicMin(next + v, cand);
@@ -213,7 +205,7 @@ __global__ void __launch_bounds__(GATHER_T) gather_minprop_kernel(const JobDesc*
 // The shape (EPT, NST, blocks per SM) is a variant picked by the autotuner.
 template <int ALGO, int EPT, int NST>
 __host__ __device__ constexpr size_t gather_stream_smem() {
-  return (size_t)NST * SG_T * EPT * 4 * (ALGO == 2 ? 2 : 1) + NST * sizeof(uint64_t);
+  return (size_t)NST * SG_T * EPT * 4 * (mp_weighted<ALGO>() ? 2 : 1) + NST * sizeof(uint64_t);
 }
 
 template <int ALGO, int EPT, int NST, int MINB>
@@ -225,7 +217,7 @@ __global__ void __launch_bounds__(SG_T, MINB) gather_stream_kernel(const JobDesc
   extern __shared__ __align__(128) uint8_t smem_raw[];
   uint32_t* ebuf = reinterpret_cast<uint32_t*>(smem_raw);
   uint32_t* wbuf = ebuf + NST * SE;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + (size_t)NST * SE * 4 * (ALGO == 2 ? 2 : 1));
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + (size_t)NST * SE * 4 * (mp_weighted<ALGO>() ? 2 : 1));
 
   LoopState* ls = jd->ls;
   if (!ls->cont || ls->mode != 0) return;
@@ -254,9 +246,9 @@ __global__ void __launch_bounds__(SG_T, MINB) gather_stream_kernel(const JobDesc
     const uint32_t cnt = rem < (uint64_t)SE ? (uint32_t)rem : SE;
     const uint32_t bytes = ((cnt + 3u) & ~3u) * 4u;
     fence_proxy_async_smem();
-    mbar_arrive_expect_tx(&bar[slot], bytes * (ALGO == 2 ? 2u : 1u));
+    mbar_arrive_expect_tx(&bar[slot], bytes * (mp_weighted<ALGO>() ? 2u : 1u));
     bulk_g2s(ebuf + slot * SE, edges + e0, bytes, &bar[slot]);
-    if (ALGO == 2) bulk_g2s(wbuf + slot * SE, wts + e0, bytes, &bar[slot]);
+    if (mp_weighted<ALGO>()) bulk_g2s(wbuf + slot * SE, wts + e0, bytes, &bar[slot]);
   };
 
   if (threadIdx.x == 0) {
@@ -408,14 +400,8 @@ __global__ void seed_minprop_kernel(const JobDesc* __restrict__ jd, const uint32
     uint32_t u = src[i], v = tgt[i];
     uint32_t uv = cur[u];
     if (uv == kInf) continue;
-    uint32_t cand;
-    if (ALGO == 0) cand = uv + 1;
-    else if (ALGO == 1) cand = uv;
-    else {
-      unsigned long long s = (unsigned long long)uv + (w ? w[i] : 1u);
-      if (s >= kInf) continue;
-      cand = (uint32_t)s;
-    }
+    const uint32_t cand = mp_cand<ALGO>(uv, w ? w[i] : 1u);
+    if (cand == kInf) continue;
     if (cand < __ldcg(next + v)) {
       uint32_t old = atomicMin(next + v, cand);
       if (cand < old) atomicOr(ch + (v >> 5), 1u << (v & 31));
@@ -426,7 +412,7 @@ __global__ void seed_minprop_kernel(const JobDesc* __restrict__ jd, const uint32
 static int grid_persistent(Ctx* c, int per_sm) { return c->num_sms * per_sm; }
 
 static bool is_minprop(int algo) {
-  return algo == CYTOM_ALGO_BFS || algo == CYTOM_ALGO_CC || algo == CYTOM_ALGO_SSSP;
+  return algo == CYTOM_ALGO_BFS || algo == CYTOM_ALGO_CC || algo == CYTOM_ALGO_SSSP || algo == CYTOM_ALGO_SSWP;
 }
 
 int minprop_alloc(Ctx* c, Job* j) {
@@ -464,6 +450,7 @@ int minprop_seed(Ctx* c, Job* j, const uint32_t* src, const uint32_t* tgt, const
   switch (j->algo) {
     case CYTOM_ALGO_BFS: seed_minprop_kernel<0><<<g, 256, 0, c->stream>>>(j->d, src, tgt, w, count); break;
     case CYTOM_ALGO_CC: seed_minprop_kernel<1><<<g, 256, 0, c->stream>>>(j->d, src, tgt, w, count); break;
+    case CYTOM_ALGO_SSWP: seed_minprop_kernel<3><<<g, 256, 0, c->stream>>>(j->d, src, tgt, w, count); break;
     default: seed_minprop_kernel<2><<<g, 256, 0, c->stream>>>(j->d, src, tgt, w, count); break;
   }
   c->launches++;
@@ -516,10 +503,10 @@ static size_t sg_smem(int v) {
 }
 
 static GatherLaunch stream_launch(Ctx* c, int a, int v) {
-  static bool attr_set[3][kSgVariantCount] = {};
+  static bool attr_set[4][kSgVariantCount] = {};
   GatherLaunch g{};
-  g.fn = a == 0 ? sg_fn<0>(v) : a == 1 ? sg_fn<1>(v) : sg_fn<2>(v);
-  g.smem = a == 2 ? sg_smem<2>(v) : sg_smem<0>(v);
+  g.fn = a == 0 ? sg_fn<0>(v) : a == 1 ? sg_fn<1>(v) : a == 3 ? sg_fn<3>(v) : sg_fn<2>(v);
+  g.smem = a >= 2 ? sg_smem<2>(v) : sg_smem<0>(v);
   if (!attr_set[a][v]) {
     cudaFuncSetAttribute(g.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
     attr_set[a][v] = true;
@@ -539,21 +526,22 @@ static int sg_variant(Ctx* c, int algo) {
     if (env >= kSgVariantCount) env = -1;
   }
   if (env >= 0) return env;
-  return c->sg_variant[algo == CYTOM_ALGO_SSSP ? 1 : 0];
+  return c->sg_variant[(algo == CYTOM_ALGO_SSSP || algo == CYTOM_ALGO_SSWP) ? 1 : 0];
 }
 
 static GatherLaunch gather_launch(Ctx* c, int algo) {
   GatherLaunch g{};
   if (gather_mode() == 0) {
-    g.fn = algo == CYTOM_ALGO_BFS ? (void*)gather_minprop_kernel<0>
-           : algo == CYTOM_ALGO_CC ? (void*)gather_minprop_kernel<1>
-                                   : (void*)gather_minprop_kernel<2>;
+    g.fn = algo == CYTOM_ALGO_BFS    ? (void*)gather_minprop_kernel<0>
+           : algo == CYTOM_ALGO_CC   ? (void*)gather_minprop_kernel<1>
+           : algo == CYTOM_ALGO_SSWP ? (void*)gather_minprop_kernel<3>
+                                     : (void*)gather_minprop_kernel<2>;
     g.grid = dim3(grid_persistent(c, 8));
     g.block = dim3(GATHER_T);
     g.smem = 0;
     return g;
   }
-  const int a = algo == CYTOM_ALGO_BFS ? 0 : (algo == CYTOM_ALGO_CC ? 1 : 2);
+  const int a = algo == CYTOM_ALGO_BFS ? 0 : algo == CYTOM_ALGO_CC ? 1 : algo == CYTOM_ALGO_SSWP ? 3 : 2;
   return stream_launch(c, a, sg_variant(c, algo));
 }
 
@@ -580,15 +568,17 @@ static int resident_grid(Ctx* c, void* fn, int threads) {
 }
 
 static void* sparse_fn(int algo) {
-  return algo == CYTOM_ALGO_BFS ? (void*)gather_sparse_kernel<0>
-         : algo == CYTOM_ALGO_CC ? (void*)gather_sparse_kernel<1>
-                                 : (void*)gather_sparse_kernel<2>;
+  return algo == CYTOM_ALGO_BFS    ? (void*)gather_sparse_kernel<0>
+         : algo == CYTOM_ALGO_CC   ? (void*)gather_sparse_kernel<1>
+         : algo == CYTOM_ALGO_SSWP ? (void*)gather_sparse_kernel<3>
+                                   : (void*)gather_sparse_kernel<2>;
 }
 
 static void* chunks_fn(int algo) {
-  return algo == CYTOM_ALGO_BFS ? (void*)gather_sparse_chunks<0>
-         : algo == CYTOM_ALGO_CC ? (void*)gather_sparse_chunks<1>
-                                 : (void*)gather_sparse_chunks<2>;
+  return algo == CYTOM_ALGO_BFS    ? (void*)gather_sparse_chunks<0>
+         : algo == CYTOM_ALGO_CC   ? (void*)gather_sparse_chunks<1>
+         : algo == CYTOM_ALGO_SSWP ? (void*)gather_sparse_chunks<3>
+                                   : (void*)gather_sparse_chunks<2>;
 }
 
 static cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* deps,
@@ -731,7 +721,7 @@ int minprop_run(Ctx* c, Job* j) {
   // round's algorithmic bytes are known once the next snapshot is read
   int prev_slot = -1;
   LoopState prev{};
-  const double wbytes = j->algo == CYTOM_ALGO_SSSP ? 4.0 : 0.0;
+  const double wbytes = (j->algo == CYTOM_ALGO_SSSP || j->algo == CYTOM_ALGO_SSWP) ? 4.0 : 0.0;
   for (uint64_t round = 0; round < max_iter;) {
     if (c->profiling) {
       // one round at a time, only the gather the device chose, so per-launch times are clean

@@ -951,13 +951,13 @@ int set_edge_weights(Ctx* c, const uint32_t* src, const uint32_t* tgt, const uin
   cudaError_t e = cudaMemcpyAsync(&missing, c->d_flag, 4, cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_err(c, e, "weight update");
-  // every weight-dependent structure is rebuilt; SSSP jobs restart (a heavier edge can
-  // lengthen shortest paths, which min-propagation cannot undo)
+  // every weight-dependent structure is rebuilt; SSSP and SSWP jobs restart (a changed
+  // weight can worsen a path, which min- or max-propagation cannot undo)
   c->version++;
   rc = upload_store_desc(c);
   if (rc) return rc;
   for (Job* j : c->jobs)
-    if (j && j->algo == CYTOM_ALGO_SSSP) j->fresh = true;
+    if (j && (j->algo == CYTOM_ALGO_SSSP || j->algo == CYTOM_ALGO_SSWP)) j->fresh = true;
   if (missing) return set_err(c, CYTOM_ERR_RANGE, "weight update of an edge that is not stored");
   return CYTOM_OK;
 }

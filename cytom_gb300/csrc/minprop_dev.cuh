@@ -44,6 +44,25 @@ __device__ __forceinline__ T ld_plain(const T* p) {
   else return *p;
 }
 
+// Programs: ALGO 0 BFS, 1 CC, 2 SSSP, 3 SSWP. SSWP runs on complemented values (v' = ~v),
+// which turns its max(v, min(u, w)) into the same min-propagation as the others:
+// v' = min(v', max(u', ~w)); unreached (0) is kInf, the start (UINT32_MAX) is 0.
+template <int ALGO>
+__host__ __device__ constexpr bool mp_weighted() {
+  return ALGO >= 2;
+}
+// The value an edge offers its target from source value c (c != kInf) and weight w.
+template <int ALGO>
+__device__ __forceinline__ uint32_t mp_cand(uint32_t c, uint32_t w) {
+  if (ALGO == 0) return c + 1;
+  if (ALGO == 1) return c;
+  if (ALGO == 2) {
+    const unsigned long long sum = (unsigned long long)c + w;
+    return sum >= kInf ? kInf : (uint32_t)sum;
+  }
+  return max(c, ~w);
+}
+
 __device__ __forceinline__ unsigned long long row_edges(const StoreDesc* sd, uint64_t x) {
   return sd->tile_ptr[(x + 1) << sd->lT] - sd->tile_ptr[x << sd->lT];
 }
@@ -243,13 +262,13 @@ __device__ __forceinline__ void dense_stage(const JobDesc* __restrict__ jd, cons
     uint4 q, wq = make_uint4(0, 0, 0, 0);
     if (!FROM_GLOBAL || i0 + 4 <= cnt) {
       q = *reinterpret_cast<const uint4*>(eb + i0);
-      if (ALGO == 2) wq = *reinterpret_cast<const uint4*>(wb + i0);
+      if (mp_weighted<ALGO>()) wq = *reinterpret_cast<const uint4*>(wb + i0);
     } else {
       q.x = i0 < cnt ? eb[i0] : 0u;
       q.y = i0 + 1 < cnt ? eb[i0 + 1] : 0u;
       q.z = i0 + 2 < cnt ? eb[i0 + 2] : 0u;
       q.w = 0u;
-      if (ALGO == 2) {
+      if (mp_weighted<ALGO>()) {
         wq.x = i0 < cnt ? wb[i0] : 0u;
         wq.y = i0 + 1 < cnt ? wb[i0 + 1] : 0u;
         wq.z = i0 + 2 < cnt ? wb[i0 + 2] : 0u;
@@ -345,16 +364,8 @@ __device__ __forceinline__ void dense_stage(const JobDesc* __restrict__ jd, cons
       }
     }
 #pragma unroll
-    for (int idx = 0; idx < EPT; ++idx) {
-      const uint32_t c = cand[idx];
-      if (c == kInf) continue;
-      if (ALGO == 0) {
-        cand[idx] = c + 1;
-      } else if (ALGO == 2) {
-        const unsigned long long sum = (unsigned long long)c + ww[idx];
-        cand[idx] = sum >= kInf ? kInf : (uint32_t)sum;
-      }
-    }
+    for (int idx = 0; idx < EPT; ++idx)
+      if (cand[idx] != kInf) cand[idx] = mp_cand<ALGO>(cand[idx], ww[idx]);
     uint32_t nv[EPT];
 #pragma unroll
     for (int idx = 0; idx < EPT; ++idx) nv[idx] = (cand[idx] != kInf) ? __ldcg(next + vv[idx]) : 0u;
@@ -435,7 +446,7 @@ __device__ __forceinline__ void sp_batch(const JobDesc* __restrict__ jd, const S
 #pragma unroll
   for (int k = 0; k < SP_ILP; ++k) {
     pk[k] = ((valid >> k) & 1u) ? sd->edges[pos[k]] : 0u;
-    wv[k] = (ALGO == 2 && ((valid >> k) & 1u)) ? sd->wts[pos[k]] : 0u;
+    wv[k] = (mp_weighted<ALGO>() && ((valid >> k) & 1u)) ? sd->wts[pos[k]] : 0u;
   }
 #pragma unroll
   for (int k = 0; k < SP_ILP; ++k) {
@@ -444,16 +455,8 @@ __device__ __forceinline__ void sp_batch(const JobDesc* __restrict__ jd, const S
     cand[k] = act ? ld_state<PERSIST>(jd->cur + ((xs[k] << lvpt) | sl)) : kInf;
   }
 #pragma unroll
-  for (int k = 0; k < SP_ILP; ++k) {
-    const uint32_t c = cand[k];
-    if (c == kInf) continue;
-    if (ALGO == 0) {
-      cand[k] = c + 1;
-    } else if (ALGO == 2) {
-      const unsigned long long sum = (unsigned long long)c + wv[k];
-      cand[k] = sum >= kInf ? kInf : (uint32_t)sum;
-    }
-  }
+  for (int k = 0; k < SP_ILP; ++k)
+    if (cand[k] != kInf) cand[k] = mp_cand<ALGO>(cand[k], wv[k]);
 #pragma unroll
   for (int k = 0; k < SP_ILP; ++k)
     nv[k] = (cand[k] != kInf) ? __ldcg(jd->next + ((ys[k] << lvpt) | (pk[k] & 0xFFFFu))) : 0u;

@@ -330,6 +330,12 @@ class SSSP(Program):
     ALGO = L.ALGO_SSSP
 
 
+class SSWP(Program):
+    """examples/sswp.cc over uint32 weights: widest-path (bottleneck) value from
+    start_vertex; 0 = unreached, UINT32_MAX at the start."""
+    ALGO = L.ALGO_SSWP
+
+
 class PageRankDelta(Program):
     """examples/pagerank-delta.cc: unnormalised delta PageRank, float ranks."""
     ALGO = L.ALGO_PR_DELTA

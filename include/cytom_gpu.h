@@ -61,6 +61,11 @@ extern "C" {
  * along t: r = (1-alpha) t + alpha (P r + D t). FP32 + compensated sums (kahan = 1)
  * or FP64 plain; FP64 L1 residual. Differentiable: cytom_pagerank_adjoint. */
 #define CYTOM_ALGO_WPAGERANK 5
+/* Single-source widest path (examples/sswp.cc): value = the largest bottleneck weight of
+ * a path from start_vertex (v = max(v, min(u, w)); 0 = unreached, UINT32_MAX at the start),
+ * uint32 weights (a CYTOM_WEIGHT_U32 store; the reference's float values are exact for
+ * them). */
+#define CYTOM_ALGO_SSWP 6
 
 /* Context configuration: the subset of ConfigContext (src/include/util/config.h:529-567)
  * and its command-line flags (src/include/core/jobs.h:176-216) that the hot path uses. */

@@ -339,11 +339,16 @@ uint64_t orc_run_minprop(const orc_store* s, int algo, uint64_t start, uint64_t 
   uint8_t* fa = (uint8_t*)calloc(n, 1);
   uint8_t* fn = (uint8_t*)calloc(n, 1);
   uint8_t* ch = (uint8_t*)calloc(n, 1);
-  for (uint64_t v = 0; v < n; ++v) cur[v] = next[v] = (algo == ORC_CC) ? (uint32_t)v : UINT32_MAX;
+  /* SSWP (examples/sswp.cc): values start at 0 (unreached), the start vertex at FLT_MAX
+   * (here UINT32_MAX); an edge offers max(v, min(u, w)) when u != 0 (pullGatherWeighted,
+   * sswp.cc:45-53); reduce = max. */
+  const int sswp = (algo == ORC_SSWP);
+  for (uint64_t v = 0; v < n; ++v)
+    cur[v] = next[v] = sswp ? 0u : ((algo == ORC_CC) ? (uint32_t)v : UINT32_MAX);
   if (algo == ORC_CC) {
     memset(fa, 1, n);
   } else {
-    cur[start] = next[start] = 0;
+    cur[start] = next[start] = sswp ? UINT32_MAX : 0u;
     fa[start] = 1;
   }
   uint64_t edges = 0, it = 0;
@@ -364,6 +369,15 @@ uint64_t orc_run_minprop(const orc_store* s, int algo, uint64_t start, uint64_t 
           uint64_t v = y * s->vpt + (e[i] & 0xFFFF);
           if (adaptive && !fa[u]) continue;
           uint32_t uv = cur[u];
+          if (sswp) {
+            if (uv == 0) continue;
+            uint32_t cand = uv < w[i] ? uv : w[i];
+            if (cand > next[v]) {
+              next[v] = cand;
+              ch[v] = 1;
+            }
+            continue;
+          }
           if (uv == UINT32_MAX) continue;
           uint64_t cand;
           if (algo == ORC_BFS) cand = (uint64_t)uv + 1;
@@ -378,7 +392,7 @@ uint64_t orc_run_minprop(const orc_store* s, int algo, uint64_t start, uint64_t 
     }
     conv = 1;
     for (uint64_t v = 0; v < n; ++v) {
-      if (algo != ORC_SSSP && !ch[v]) continue;
+      if (algo != ORC_SSSP && !sswp && !ch[v]) continue;
       if (next[v] != cur[v]) {
         cur[v] = next[v];
         fn[v] = 1;

@@ -64,8 +64,8 @@ void orc_store_dump(const orc_store* s, uint64_t* tile_ptr, uint32_t* edges,
 void orc_store_degrees(const orc_store* s, uint32_t* out_deg, uint32_t* in_deg);
 
 /* ---- Executors (inc/core/continuous-algorithm-executor.h:49-249) ------- */
-enum { ORC_BFS = 0, ORC_CC = 1, ORC_SSSP = 2 };
-/* From-scratch run of BFS / CC / SSSP with the reference's Jacobi iteration
+enum { ORC_BFS = 0, ORC_CC = 1, ORC_SSSP = 2, ORC_SSWP = 3 };
+/* From-scratch run of BFS / CC / SSSP / SSWP with the reference's Jacobi iteration
  * (pull over tiles with an active source, reduce into next, apply changed,
  * swap active bitmaps). values[n] receives the result (UINT32_MAX = not
  * reached). Returns iterations executed; *converged and the reference's

@@ -14,7 +14,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liborc.so"
 
-BFS, CC, SSSP = 0, 1, 2
+BFS, CC, SSSP, SSWP = 0, 1, 2, 3
 RMAT_A, RMAT_B, RMAT_C = float(np.float32(0.57)), float(np.float32(0.19)), float(np.float32(0.19))
 
 _lib = None

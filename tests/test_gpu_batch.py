@@ -1,8 +1,8 @@
 """GPU tests of the batched persistent executor (cytom_run_batch).
 
-Mixed programs (BFS from two sources, CC, SSSP, PageRank FP32-compensated and FP64,
+Mixed programs (BFS from two sources, CC, SSSP, SSWP, PageRank FP32-compensated and FP64,
 PageRank-delta) over graph snapshots of uneven size run in ONE launch. Every job must
-end exactly where the one-job executor (cytom_run) ends: BFS / CC / SSSP values, round
+end exactly where the one-job executor (cytom_run) ends: BFS / CC / SSSP / SSWP values, round
 counts and processed-edge counts bit-exact (and equal to the CPU oracle's fixed point);
 PageRank within the FP64-oracle tolerance (relative L1 <= 1e-6, max relative <= 1e-5)
 -- on a fresh run and after further insert batches (incremental runs)."""
@@ -36,6 +36,7 @@ class Snap:
                          ("bfs1", lambda e: cg.BFS(e, start_vertex=1, max_iterations=1000)),
                          ("cc", lambda e: cg.CC(e, max_iterations=1000)),
                          ("sssp", lambda e: cg.SSSP(e, start_vertex=0, max_iterations=1000)),
+                         ("sswp", lambda e: cg.SSWP(e, start_vertex=0, max_iterations=1000)),
                          ("pr32", lambda e: cg.PageRank(e, max_iterations=500, tolerance=1e-10, kahan=True)),
                          ("pr64", lambda e: cg.PageRank(e, max_iterations=500, tolerance=1e-12, kahan=False)),
                          ("prd", lambda e: cg.PageRankDelta(e, delta=0.0, max_iterations=500, tolerance=1e-9))):
@@ -64,8 +65,8 @@ def check_round(cg, orc, snaps):
             sa = bstats[k]
             k += 1
             sb = pb.execute_algorithm()
-            if name.startswith(("bfs", "cc", "sssp")):
-                algo = {"bfs": 0, "cc": 1, "sss": 2}[name[:3]]
+            if name.startswith(("bfs", "cc", "sssp", "sswp")):
+                algo = {"bfs": 0, "cc": 1, "sss": 2, "ssw": 3}[name[:3]]
                 start = 1 if name == "bfs1" else 0
                 ref, info = s.st.run_minprop(algo, start=start, max_iter=1000)
                 ra, rb = pa.result(), pb.result()

@@ -1,4 +1,4 @@
-"""GPU parity of the BFS / CC / SSSP executors against the CPU oracle.
+"""GPU parity of the BFS / CC / SSSP / SSWP executors against the CPU oracle.
 
 Fresh runs: values, round count and the reference's processed-edge count equal the
 oracle's Jacobi run round for round. Streaming runs: after every batch the
@@ -8,7 +8,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-ALGOS = [("BFS", 0), ("CC", 1), ("SSSP", 2)]
+ALGOS = [("BFS", 0), ("CC", 1), ("SSSP", 2), ("SSWP", 3)]
 
 
 def build(cg, orc, scale, vpt, m, seed, adaptive=True):
@@ -72,7 +72,7 @@ def test_streaming_incremental_equals_from_scratch(cg, orc, scale, vpt, nb, batc
     n = 1 << scale
     with cg.Engine(n, vpt, weight_type=cg.WEIGHT_U32) as eng:
         progs = [cg.BFS(eng, start_vertex=0, max_iterations=1000), cg.CC(eng, max_iterations=1000),
-                 cg.SSSP(eng, start_vertex=0, max_iterations=1000)]
+                 cg.SSSP(eng, start_vertex=0, max_iterations=1000), cg.SSWP(eng, start_vertex=0, max_iterations=1000)]
         st = orc.Store(n, vpt, weighted=True)
         for b in range(nb):
             s, t = orc.rmat(scale, b * batch, batch, seed=scale)
@@ -101,6 +101,10 @@ def test_isolated_start_vertex(cg):
         q.execute_algorithm()
         d = q.result()
         assert d[1] == 0 and d[2] == 4 and d[3] == 9
+        r = cg.SSWP(eng, start_vertex=1)
+        r.execute_algorithm()
+        wv = r.result()
+        assert wv[1] == 0xFFFFFFFF and wv[2] == 4 and wv[3] == 4 and wv[0] == 0
 
 
 def test_start_vertex_out_of_range(cg):
@@ -180,13 +184,13 @@ n = 1 << scale
 ok = []
 with cg.Engine(n, vpt, weight_type=cg.WEIGHT_U32) as eng:
     progs = [cg.BFS(eng, start_vertex=0, max_iterations=1000), cg.CC(eng, max_iterations=1000),
-             cg.SSSP(eng, start_vertex=0, max_iterations=1000)]
+             cg.SSSP(eng, start_vertex=0, max_iterations=1000), cg.SSWP(eng, start_vertex=0, max_iterations=1000)]
     st = orc.Store(n, vpt, True)
     for b in range(6):
         s, t = orc.rmat(scale, b * 200000, 200000, 3)
         w = orc.edge_weights(s, t, 8)
         eng.insert_edges(s, t, w); st.insert(s, t, w); st.compact()
-        for prog, algo in zip(progs, (0, 1, 2)):
+        for prog, algo in zip(progs, (0, 1, 2, 3)):
             stt = prog.execute_algorithm()
             ref, info = st.run_minprop(algo, start=0, max_iter=1000)
             ok.append(bool(np.array_equal(prog.result(), ref)) and stt["converged"] == 1)
@@ -226,7 +230,7 @@ for scale, vpt in ((16, 4096), (15, 256)):
     st.insert(s, t, w); st.compact()
     with cg.Engine(n, vpt, weight_type=cg.WEIGHT_U32) as eng:
         eng.insert_edges(s, t, w)
-        for prog, algo in ((cg.BFS, 0), (cg.CC, 1), (cg.SSSP, 2)):
+        for prog, algo in ((cg.BFS, 0), (cg.CC, 1), (cg.SSSP, 2), (cg.SSWP, 3)):
             p = prog(eng, start_vertex=0, max_iterations=1000)
             stt = p.execute_algorithm()
             ref, info = st.run_minprop(algo, start=0, max_iter=1000)

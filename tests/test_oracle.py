@@ -299,3 +299,31 @@ def test_wpagerank_adjoint_matches_central_differences(orc):
         tm[v] -= et
         fd = (c @ orc.wpagerank(n, src, tgt, w, t=tp, tol=1e-16)[0] - c @ orc.wpagerank(n, src, tgt, w, t=tm, tol=1e-16)[0]) / (2 * et)
         assert abs(fd - gt[v]) <= 1e-4 * max(abs(fd), 1e-2 * np.abs(gt).max()), (v, fd, gt[v])
+
+
+def _widest_path(n, src, tgt, w, start):
+    # independent restatement: max-min relaxation to the fixed point (unique widest widths)
+    val = np.zeros(n, np.uint64)
+    val[start] = 0xFFFFFFFF
+    while True:
+        live = val[src] > 0
+        cand = np.minimum(val[src[live]], w[live].astype(np.uint64))
+        new = val.copy()
+        np.maximum.at(new, tgt[live], cand)
+        if np.array_equal(new, val):
+            return val.astype(np.uint32)
+        val = new
+
+
+@pytest.mark.parametrize("scale,vpt", [(10, 256), (12, 1024)])
+def test_sswp_oracle_matches_widest_path(orc, scale, vpt):
+    n = 1 << scale
+    s, t = orc.rmat(scale, 0, 8 * n, 3)
+    w = orc.edge_weights(s, t, 4)
+    st = orc.Store(n, vpt, True)
+    st.insert(s, t, w)
+    st.compact()
+    for start in (0, 5):
+        vals, info = st.run_minprop(orc.SSWP, start=start, max_iter=10000)
+        assert info["converged"] == 1
+        assert np.array_equal(vals, _widest_path(n, s, t, w, start))

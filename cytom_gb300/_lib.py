@@ -137,6 +137,9 @@ SIGNATURES = [
     ("cytom_reset_kernel_stats", C.c_int, [C.c_void_p]),
     ("cytom_launch_count", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
     ("cytom_sync", C.c_int, [C.c_void_p]),
+    ("cytom_persist_edges", C.c_int, [C.c_void_p, C.c_char_p]),
+    ("cytom_read_edges", C.c_int, [C.c_void_p, C.c_char_p, C.c_uint64, C.POINTER(C.c_uint64)]),
+    ("cytom_write_results", C.c_int, [C.c_void_p, C.c_int, C.c_char_p]),
     ("cytom_tile_batch_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint64,
                                            C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p,
                                            C.POINTER(C.c_uint64), C.c_void_p]),

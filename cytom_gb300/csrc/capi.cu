@@ -389,6 +389,7 @@ int cytom_destroy(cytom_ctx* ctx) {
     }
   batch_free(c);
   pagerank_ctx_free(c);
+  edge_log_close(c);
   void* ptrs[] = {c->dir, c->edges, c->wts, c->edges_alt, c->wts_alt, c->tile_ptr, c->tile_ptr_alt,
                   c->chunk_tile, c->app_keys, c->app_keys_alt, c->app_w, c->app_w_alt,
                   c->out_deg, c->in_deg, c->dsd, c->scratch, c->d_flag};
@@ -494,7 +495,9 @@ int cytom_insert_batch(cytom_ctx* ctx, const uint32_t* src, const uint32_t* tgt,
   if (where == CYTOM_PTR_DEVICE) {
     int rc = insert_device(c, src, tgt, w, count);
     if (rc) return rc;
-    return cuda_err(c, cudaStreamSynchronize(c->stream), "insert");
+    rc = cuda_err(c, cudaStreamSynchronize(c->stream), "insert");
+    if (rc) return rc;
+    return edge_log_append(c, src, tgt, w, count, CYTOM_PTR_DEVICE);
   }
   Staging st;
   st.s = c->stream;
@@ -509,7 +512,9 @@ int cytom_insert_batch(cytom_ctx* ctx, const uint32_t* src, const uint32_t* tgt,
   if (dw) cudaMemcpyAsync(dw, w, count * 4, cudaMemcpyHostToDevice, c->stream);
   int rc = insert_device(c, ds, dt, dw, count);
   if (rc) return rc;
-  return cuda_err(c, cudaStreamSynchronize(c->stream), "insert");
+  rc = cuda_err(c, cudaStreamSynchronize(c->stream), "insert");
+  if (rc) return rc;
+  return edge_log_append(c, src, tgt, w, count, CYTOM_PTR_HOST);
 }
 
 int cytom_load_gridgraph(cytom_ctx* ctx, const char* path, uint64_t batch, uint64_t* count) {

@@ -186,6 +186,7 @@ struct Ctx {
   uint64_t pr_deg_mult_version = ~0ULL;
   void* pr_csc = nullptr;
   void* pr_wgraph = nullptr;  // weighted PageRank: CSC + CSR with weights
+  void* edge_log = nullptr;   // open edge log (cytom_persist_edges)
 };
 
 // ---- helpers (capi.cu) ----
@@ -225,5 +226,7 @@ int minprop_autotune(Ctx* c);
 void sg_shapes(int* ept, int* nst, int* minb, int* count);
 void batch_free(Ctx* c);
 void pagerank_ctx_free(Ctx* c);
+void edge_log_close(Ctx* c);
+int edge_log_append(Ctx* c, const uint32_t* src, const uint32_t* tgt, const uint32_t* w, uint64_t count, int where);
 
 }  // namespace cytom

@@ -750,6 +750,23 @@ int pagerank_result(Ctx* c, Job* j, void* out, int where) {
   return unpermute_out<float>(c, src, out, where, "pagerank result");
 }
 
+// PageRank-delta rank and last delta in vertex order (host buffers), for the results dump.
+int pagerank_delta_out(Ctx* c, Job* j, float* rank, float* delta) {
+  PrState* s = prs(j);
+  if (j->algo != CYTOM_ALGO_PR_DELTA) return set_err(c, CYTOM_ERR_INVAL, "not a PageRank-delta job");
+  if (!c->pr_perm) {
+    // never run: the initial state (rank 1, delta 0)
+    for (uint64_t v = 0; v < c->n; ++v) {
+      rank[v] = 1.f;
+      delta[v] = 0.f;
+    }
+    return CYTOM_OK;
+  }
+  int rc = unpermute_out<float>(c, s->rank, rank, CYTOM_PTR_HOST, "pagerank-delta rank");
+  if (!rc) rc = unpermute_out<float>(c, s->delta, delta, CYTOM_PTR_HOST, "pagerank-delta delta");
+  return rc;
+}
+
 int pagerank_result64(Ctx* c, Job* j, double* out, int where) {
   PrState* s = prs(j);
   if ((j->algo != CYTOM_ALGO_PAGERANK && j->algo != CYTOM_ALGO_WPAGERANK) || j->params.kahan)

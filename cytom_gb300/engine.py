@@ -182,6 +182,16 @@ class Engine:
         self._check(self.lib.cytom_set_edge_weights(self.ctx, src.ctypes.data, tgt.ctypes.data, w.ctypes.data,
                                                     len(src), L.PTR_HOST))
 
+    def persist_edges(self, path):
+        """Start (or, with None, stop) logging inserted batches to `path` (EdgesWriter format)."""
+        self._check(self.lib.cytom_persist_edges(self.ctx, None if path is None else str(path).encode()))
+
+    def read_edges(self, path, batch: int = 1 << 20) -> int:
+        """Insert the records of an edge log (EdgesWriter format); returns the record count."""
+        cnt = C.c_uint64()
+        self._check(self.lib.cytom_read_edges(self.ctx, str(path).encode(), batch, C.byref(cnt)))
+        return cnt.value
+
     def autotune(self) -> dict:
         """Times the streaming-gather shapes on the current graph and keeps the fastest."""
         rep = L.TuneReport()
@@ -294,6 +304,10 @@ class Program:
         self.engine._check(self.engine.lib.cytom_get_result_f64(self.engine.ctx, self.job,
                                                                 r.ctypes.data, L.PTR_HOST))
         return r
+
+    def write_results(self, path):
+        """ResultsWriter dump of this job's values (the reference's raw VertexType array)."""
+        self.engine._check(self.engine.lib.cytom_write_results(self.engine.ctx, self.job, str(path).encode()))
 
     def destroy(self):
         self.engine._check(self.engine.lib.cytom_job_destroy(self.engine.ctx, self.job))

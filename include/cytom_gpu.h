@@ -252,6 +252,25 @@ int cytom_pagerank_adjoint(cytom_ctx* ctx, int job_id, const double* c_weights, 
 int cytom_set_edge_weights(cytom_ctx* ctx, const uint32_t* src, const uint32_t* tgt, const uint32_t* w,
                            uint64_t count, int where);
 
+/* ---- On-disk formats --------------------------------------------------- */
+
+/* Edge log (EdgesWriter, src/include/tile-manager/edges-writer.h:114-185): from this call
+ * on, every inserted batch is appended to `path` in arrival order, duplicates included,
+ * as packed edge_compact_t {u32 src; u32 tgt} records, or edge_compact_weighted_t
+ * {u32 src; u32 tgt; float weight} for a weighted store (datatypes.h:55-64). The file is
+ * created (truncated); NULL closes the log. */
+int cytom_persist_edges(cytom_ctx* ctx, const char* path);
+/* Reads an edge log written that way (EdgesWriter::readEdges, edges-writer.h:30-90) and
+ * inserts its records in batches of `batch` (0 = 2^20); weighted records for a weighted
+ * store. *count receives the records read. */
+int cytom_read_edges(cytom_ctx* ctx, const char* path, uint64_t batch, uint64_t* count);
+/* Results dump (ResultsWriter::run, src/include/core/results-writer.h:46-81): the job's
+ * values as the reference's raw VertexType array, vertex by vertex -- uint32 (BFS, CC),
+ * float (SSSP, SSWP; FLT_MAX = not reached / the widest-path start), the 12-byte
+ * {float delta_sum; float rank; float delta} (PageRank-delta, examples/pagerank-delta.cc:30-33;
+ * delta_sum = delta / alpha, the sum that produced the last delta), float (PageRank). */
+int cytom_write_results(cytom_ctx* ctx, int job_id, const char* path);
+
 /* ---- Allocation-free batch compaction ---------------------------------- */
 
 /* No counterpart in the reference. For callers that cannot allocate device memory

@@ -128,6 +128,10 @@ SIGNATURES = [
     ("cytom_pagerank_adjoint", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                                          C.c_int, C.POINTER(RunStats)]),
     ("cytom_set_edge_weights", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int]),
+    ("cytom_delete_batch", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int,
+                                     C.POINTER(C.c_uint64)]),
+    ("cytom_delete_random", C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.c_void_p, C.c_void_p, C.c_int,
+                                      C.POINTER(C.c_uint64)]),
     ("cytom_get_result", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
     ("cytom_get_result_f64", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
     ("cytom_autotune", C.c_int, [C.c_void_p, C.POINTER(TuneReport)]),

@@ -30,6 +30,8 @@ int pagerank_set_teleport(Ctx* c, Job* j, const double* t, int where);
 int pagerank_adjoint(Ctx* c, Job* j, const double* cv, int cwhere, float* d_w, float* d_t, int owhere,
                      cytom_run_stats* st);
 int set_edge_weights(Ctx* c, const uint32_t* src, const uint32_t* tgt, const uint32_t* w, uint64_t count);
+int delete_edges(Ctx* c, const uint32_t* src, const uint32_t* tgt, uint64_t count, uint64_t* removed);
+int delete_random(Ctx* c, uint64_t count, uint64_t seed, uint32_t* src, uint32_t* tgt, uint64_t* removed);
 void pagerank_free(Job* j);
 
 __global__ void complement_kernel(const uint32_t* __restrict__ in, uint64_t n, uint32_t* __restrict__ out) {
@@ -733,6 +735,40 @@ int cytom_set_edge_weights(cytom_ctx* ctx, const uint32_t* src, const uint32_t* 
   cudaMemcpyAsync(ds + count, tgt, count * 4, cudaMemcpyHostToDevice, c->stream);
   cudaMemcpyAsync(ds + 2 * count, w, count * 4, cudaMemcpyHostToDevice, c->stream);
   return set_edge_weights(c, ds, ds + count, ds + 2 * count, count);
+}
+
+int cytom_delete_batch(cytom_ctx* ctx, const uint32_t* src, const uint32_t* tgt, uint64_t count, int where,
+                       uint64_t* deleted) {
+  Ctx* c = (Ctx*)ctx;
+  if (deleted) *deleted = 0;
+  if (!c || (count && (!src || !tgt))) return CYTOM_ERR_INVAL;
+  if (where == CYTOM_PTR_DEVICE || count == 0) return delete_edges(c, src, tgt, count, deleted);
+  Staging st;
+  st.s = c->stream;
+  if (cudaMallocAsync(&st.p, count * 8, c->stream) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "staging");
+  uint32_t* ds = (uint32_t*)st.p;
+  cudaMemcpyAsync(ds, src, count * 4, cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(ds + count, tgt, count * 4, cudaMemcpyHostToDevice, c->stream);
+  return delete_edges(c, ds, ds + count, count, deleted);
+}
+
+int cytom_delete_random(cytom_ctx* ctx, uint64_t count, uint64_t seed, uint32_t* src, uint32_t* tgt, int where,
+                        uint64_t* deleted) {
+  Ctx* c = (Ctx*)ctx;
+  if (deleted) *deleted = 0;
+  if (!c || (src && !tgt) || (!src && tgt)) return CYTOM_ERR_INVAL;
+  if (count == 0) return delete_edges(c, nullptr, nullptr, 0, nullptr);
+  if (src && where == CYTOM_PTR_DEVICE) return delete_random(c, count, seed, src, tgt, deleted);
+  Staging st;
+  st.s = c->stream;
+  if (cudaMallocAsync(&st.p, count * 8, c->stream) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "staging");
+  uint32_t* ds = (uint32_t*)st.p;
+  int rc = delete_random(c, count, seed, ds, ds + count, deleted);
+  if (rc || !src) return rc;
+  cudaError_t e = cudaMemcpyAsync(src, ds, count * 4, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(tgt, ds + count, count * 4, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  return cuda_err(c, e, "random deletion picks");
 }
 
 static void fill_tune_report(const Ctx* c, cytom_tune_report* out) {

@@ -409,7 +409,44 @@ __global__ void seed_minprop_kernel(const JobDesc* __restrict__ jd, const uint32
   }
 }
 
+// edgeChanged(DELETE) (examples/sssp.cc:135-139: the reference re-runs a job when a
+// deleted edge was its target's critical neighbour). A deleted edge (u, v, w) matters when
+// it is tight: cand(cur[u], w) equals the value v holds (cur, or next when a pending insert
+// seeded v through it). Without a tight deleted edge every value is still carried by a
+// path of tight edges that all remain stored, and deleting edges cannot lower any value,
+// so the values stay the fixed point of the new graph. A run that stopped before
+// converging (cont still set) counts as tight. *tight becomes 1 if the job must restart.
+template <int ALGO>
+__global__ void delete_tight_kernel(const JobDesc* __restrict__ jd, const uint32_t* __restrict__ dsrc,
+                                    const uint32_t* __restrict__ dtgt, const uint32_t* __restrict__ dw,
+                                    uint64_t count, unsigned* tight) {
+  if (blockIdx.x == 0 && threadIdx.x == 0 && *(volatile unsigned*)&jd->ls->cont != 0) *tight = 1u;
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint32_t* cur = jd->cur;
+  const uint32_t* next = jd->next;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+    const uint32_t uv = cur[dsrc[i]];
+    if (uv == kInf) continue;
+    const uint32_t cand = mp_cand<ALGO>(uv, dw ? dw[i] : 1u);
+    const uint32_t v = dtgt[i];
+    if (cand == cur[v] || cand == next[v]) *tight = 1u;
+  }
+}
+
 static int grid_persistent(Ctx* c, int per_sm) { return c->num_sms * per_sm; }
+
+int minprop_delete_check(Ctx* c, Job* j, const uint32_t* dsrc, const uint32_t* dtgt, const uint32_t* dw,
+                         uint64_t count, unsigned* tight) {
+  int g = std::max(1, std::min<int>(grid_persistent(c, 8), (int)((count + 255) / 256)));
+  switch (j->algo) {
+    case CYTOM_ALGO_BFS: delete_tight_kernel<0><<<g, 256, 0, c->stream>>>(j->d, dsrc, dtgt, dw, count, tight); break;
+    case CYTOM_ALGO_CC: delete_tight_kernel<1><<<g, 256, 0, c->stream>>>(j->d, dsrc, dtgt, dw, count, tight); break;
+    case CYTOM_ALGO_SSWP: delete_tight_kernel<3><<<g, 256, 0, c->stream>>>(j->d, dsrc, dtgt, dw, count, tight); break;
+    default: delete_tight_kernel<2><<<g, 256, 0, c->stream>>>(j->d, dsrc, dtgt, dw, count, tight); break;
+  }
+  c->launches++;
+  return cuda_err(c, cudaGetLastError(), "delete_tight");
+}
 
 static bool is_minprop(int algo) {
   return algo == CYTOM_ALGO_BFS || algo == CYTOM_ALGO_CC || algo == CYTOM_ALGO_SSSP || algo == CYTOM_ALGO_SSWP;

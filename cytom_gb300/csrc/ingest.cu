@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <vector>
 
 #include "engine.h"
 
@@ -909,6 +910,213 @@ int compute_compact_flags(Ctx* c, uint8_t* dflags) {
   return cuda_err(c, cudaGetLastError(), "count_sources");
 }
 
+
+// Deletion of stored edges: the store side of TileManager::deleteEdge and of the
+// deleted-edge filter of compactStorage / fillCSR (tile-manager.h:165-173, 249-253,
+// 532-535), applied at once instead of kept as a deleted set. Request i finds
+// (src[i], tgt[i]) in its tile (binary search over the sorted packed edges); the request
+// that sets the edge's kill bit first drops out_deg[src] and in_deg[tgt] by one and
+// appends (src, tgt, weight) to the deleted list. A pair that is not stored is skipped.
+__global__ void delete_mark_kernel(const StoreDesc* __restrict__ sd, const uint32_t* __restrict__ src,
+                                   const uint32_t* __restrict__ tgt, uint64_t count, uint32_t* kill,
+                                   uint32_t* out_deg, uint32_t* in_deg, uint32_t* dsrc, uint32_t* dtgt,
+                                   uint32_t* dw, unsigned long long* ndel) {
+  const uint32_t lvpt = sd->lvpt, lT = sd->lT;
+  const uint32_t lmask = (1u << lvpt) - 1u;
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+    const uint32_t u = src[i], v = tgt[i];
+    if ((uint64_t)u >= sd->n || (uint64_t)v >= sd->n) continue;
+    const uint64_t t = ((uint64_t)(u >> lvpt) << lT) | (v >> lvpt);
+    const uint32_t key = ((u & lmask) << 16) | (v & lmask);
+    const uint64_t end = sd->tile_ptr[t + 1];
+    uint64_t lo = sd->tile_ptr[t], hi = end;
+    while (lo < hi) {
+      const uint64_t mid = (lo + hi) >> 1;
+      if (sd->edges[mid] < key) lo = mid + 1;
+      else hi = mid;
+    }
+    if (lo >= end || sd->edges[lo] != key) continue;
+    const uint32_t bit = 1u << (lo & 31);
+    if (atomicOr(kill + (lo >> 5), bit) & bit) continue;  // another request took it
+    atomicSub(out_deg + u, 1u);
+    atomicSub(in_deg + v, 1u);
+    const unsigned long long k = atomicAdd(ndel, 1ULL);
+    dsrc[k] = u;
+    dtgt[k] = v;
+    if (dw) dw[k] = sd->wts[lo];
+  }
+}
+
+// Kept edges per 32-edge word of the kill bitmap; word nw (one past the last) counts 0,
+// so the exclusive scan's entry nw is the new edge count.
+__global__ void keep_count_kernel(const uint32_t* __restrict__ kill, uint64_t E, uint64_t nw,
+                                  uint32_t* __restrict__ cnt) {
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w <= nw; w += stride) {
+    if (w == nw) {
+      cnt[w] = 0;
+      continue;
+    }
+    const unsigned r = (unsigned)(E - w * 32);
+    const uint32_t valid = r >= 32 ? 0xFFFFFFFFu : ((1u << r) - 1u);
+    cnt[w] = __popc(~kill[w] & valid);
+  }
+}
+
+// New position of old position p: kept edges before p.
+__device__ __forceinline__ uint64_t kept_before(const uint32_t* kill, const uint32_t* P, uint64_t p) {
+  const uint64_t w = p >> 5;
+  const unsigned b = (unsigned)(p & 31);
+  return (uint64_t)P[w] + (b ? (uint64_t)__popc(~kill[w] & ((1u << b) - 1u)) : 0ULL);
+}
+
+// Order-preserving gather of the kept edges (each tile stays sorted).
+__global__ void delete_gather_kernel(const uint32_t* __restrict__ edges, const uint32_t* __restrict__ wts,
+                                     uint64_t E, const uint32_t* __restrict__ kill, const uint32_t* __restrict__ P,
+                                     uint32_t* __restrict__ oe, uint32_t* __restrict__ ow) {
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < E; i += stride) {
+    const uint32_t k = kill[i >> 5];
+    const unsigned b = (unsigned)(i & 31);
+    if ((k >> b) & 1u) continue;
+    const uint64_t o = (uint64_t)P[i >> 5] + __popc(~k & ((1u << b) - 1u));
+    oe[o] = edges[i];
+    if (ow) ow[o] = wts[i];
+  }
+}
+
+__global__ void delete_tile_ptr_kernel(const unsigned long long* __restrict__ tile_ptr, uint64_t ntiles,
+                                       const uint32_t* __restrict__ kill, const uint32_t* __restrict__ P,
+                                       unsigned long long* __restrict__ out) {
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t <= ntiles; t += stride)
+    out[t] = kept_before(kill, P, tile_ptr[t]);
+}
+
+int minprop_delete_check(Ctx* c, Job* j, const uint32_t* dsrc, const uint32_t* dtgt, const uint32_t* dw,
+                         uint64_t count, unsigned* tight);
+
+// Removes the stored (src, tgt) pairs listed (device pointers) after compacting pending
+// inserts. The store is rewritten without them in one order-preserving pass; BFS / CC /
+// SSSP / SSWP jobs restart only if a deleted edge was tight for them, the PageRank
+// family re-converges on the new snapshot (its first round is a residual round).
+int delete_edges(Ctx* c, const uint32_t* src, const uint32_t* tgt, uint64_t count, uint64_t* removed) {
+  if (removed) *removed = 0;
+  int rc = compact(c);
+  if (rc) return rc;
+  const uint64_t E = c->E;
+  if (E == 0 || count == 0) return CYTOM_OK;
+  const bool wt = c->wtype != CYTOM_UNWEIGHTED;
+  const uint64_t nw = (E + 31) / 32;
+  std::vector<Job*> mp;
+  for (Job* j : c->jobs)
+    if (j && !j->fresh && (j->algo == CYTOM_ALGO_BFS || j->algo == CYTOM_ALGO_CC || j->algo == CYTOM_ALGO_SSSP ||
+                           j->algo == CYTOM_ALGO_SSWP))
+      mp.push_back(j);
+  // temporaries: kill[nw+1], cnt[nw+1], P[nw+1], total, deleted list 3 x count, ndel, tight flags
+  const uint64_t words = 3 * (nw + 1) + 1 + 3 * count;
+  const size_t bytes = ((words * 4 + 15) / 16) * 16 + 8 + (mp.size() + 1) * 4;
+  char* tmp = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&tmp, bytes, c->stream);
+  if (e != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "deletion temporaries");
+  uint32_t* kill = (uint32_t*)tmp;
+  uint32_t* cnt = kill + (nw + 1);
+  uint32_t* P = cnt + (nw + 1);
+  uint32_t* total = P + (nw + 1);
+  uint32_t* dsrc = total + 1;
+  uint32_t* dtgt = dsrc + count;
+  uint32_t* dw = dtgt + count;
+  unsigned long long* ndel = (unsigned long long*)(tmp + ((words * 4 + 15) / 16) * 16);
+  unsigned* tight = (unsigned*)(ndel + 1);
+  cudaMemsetAsync(kill, 0, (nw + 1) * 4, c->stream);
+  cudaMemsetAsync(ndel, 0, 8 + (mp.size() + 1) * 4, c->stream);
+  int slot = prof_begin(c, KC_MERGE);
+  delete_mark_kernel<<<grid_for(c, count, 256), 256, 0, c->stream>>>(c->dsd, src, tgt, count, kill, c->out_deg,
+                                                                       c->in_deg, dsrc, dtgt, wt ? dw : nullptr, ndel);
+  c->launches++;
+  e = cudaMemcpyAsync(c->h_pinned, ndel, 8, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    cudaFreeAsync(tmp, c->stream);
+    return cuda_err(c, e, "deletion");
+  }
+  const uint64_t nd = *(unsigned long long*)c->h_pinned;
+  if (nd == 0) {
+    cudaFreeAsync(tmp, c->stream);
+    prof_end(c, slot, (double)count * 8.0);
+    return CYTOM_OK;
+  }
+  keep_count_kernel<<<grid_for(c, nw + 1, 256), 256, 0, c->stream>>>(kill, E, nw, cnt);
+  c->launches++;
+  rc = exclusive_scan_u32(c, cnt, P, nw + 1, total);
+  if (rc) return rc;
+  delete_gather_kernel<<<grid_for(c, E, 256, 16), 256, 0, c->stream>>>(c->edges, c->wts, E, kill, P, c->edges_alt,
+                                                                       wt ? c->wts_alt : nullptr);
+  c->launches++;
+  delete_tile_ptr_kernel<<<grid_for(c, c->ntiles + 1, 256), 256, 0, c->stream>>>(c->tile_ptr, c->ntiles, kill, P,
+                                                                                  c->tile_ptr_alt);
+  c->launches++;
+  for (size_t k = 0; k < mp.size(); ++k) {
+    rc = minprop_delete_check(c, mp[k], dsrc, dtgt, wt ? dw : nullptr, nd, tight + k);
+    if (rc) return rc;
+  }
+  std::vector<unsigned> tflags(mp.size() + 1, 0);
+  e = cudaMemcpyAsync(tflags.data(), tight, (mp.size() + 1) * 4, cudaMemcpyDeviceToHost, c->stream);
+  cudaFreeAsync(tmp, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "deletion");
+  prof_end(c, slot, (double)count * 8.0 + (double)E * (wt ? 16.0 : 8.0));
+  std::swap(c->edges, c->edges_alt);
+  std::swap(c->wts, c->wts_alt);
+  std::swap(c->tile_ptr, c->tile_ptr_alt);
+  c->E = E - nd;
+  c->version++;
+  for (size_t k = 0; k < mp.size(); ++k)
+    if (tflags[k]) mp[k]->fresh = true;
+  if (removed) *removed = nd;
+  const uint64_t nch = (c->E + kChunk - 1) / kChunk;
+  chunk_tile_kernel<<<grid_for(c, nch + 1, 256), 256, 0, c->stream>>>(c->tile_ptr, c->ntiles, nch, c->chunk_tile);
+  c->launches++;
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_err(c, e, "chunk_tile");
+  return upload_store_desc(c);
+}
+
+// Random deletion picks (the reference's deletion_percentage mode,
+// meta-tile-manager.h:201-231, with TileManager::deleteRandomEdge, tile-manager.h:175-190):
+// pick i chooses a tile uniformly by hash64(hash64(seed) + 2i) and one of its edges
+// uniformly by hash64(hash64(seed) + 2i + 1); an empty tile yields no edge (UINT32_MAX
+// twice, which the deletion skips).
+__global__ void pick_random_kernel(const StoreDesc* __restrict__ sd, uint64_t ntiles, uint64_t count,
+                                   uint64_t hs, uint32_t* __restrict__ src, uint32_t* __restrict__ tgt) {
+  const uint32_t lvpt = sd->lvpt, lT = sd->lT;
+  const uint64_t tmask = (1ULL << lT) - 1ULL;
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+    const uint64_t t = hash64(hs + 2 * i) % ntiles;
+    const uint64_t lo = sd->tile_ptr[t], len = sd->tile_ptr[t + 1] - lo;
+    if (len == 0) {
+      src[i] = tgt[i] = 0xFFFFFFFFu;
+      continue;
+    }
+    const uint32_t e = sd->edges[lo + hash64(hs + 2 * i + 1) % len];
+    src[i] = (uint32_t)((t >> lT) << lvpt) | (e >> 16);
+    tgt[i] = (uint32_t)((t & tmask) << lvpt) | (e & 0xFFFFu);
+  }
+}
+
+int delete_random(Ctx* c, uint64_t count, uint64_t seed, uint32_t* src, uint32_t* tgt, uint64_t* removed) {
+  if (removed) *removed = 0;
+  int rc = compact(c);
+  if (rc || count == 0) return rc;
+  pick_random_kernel<<<grid_for(c, count, 256), 256, 0, c->stream>>>(c->dsd, c->ntiles, count, hash64(seed), src,
+                                                                     tgt);
+  c->launches++;
+  rc = cuda_err(c, cudaGetLastError(), "random picks");
+  if (rc) return rc;
+  return delete_edges(c, src, tgt, count, removed);
+}
 
 // Weight update of stored edges: update i finds (src[i], tgt[i]) in its tile (binary
 // search over the tile's sorted packed edges) and overwrites its weight; an edge that

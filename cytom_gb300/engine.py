@@ -171,6 +171,35 @@ class Engine:
         self._check(self.lib.cytom_insert_batch(self.ctx, src_addr, tgt_addr, w_addr, count,
                                                 L.PTR_DEVICE))
 
+    def delete_edges(self, src, tgt) -> int:
+        """Deletes stored edges (MetaTileManager::deleteEdge); returns how many were stored.
+
+        Arrays may be numpy (host) or CUDA tensors (device)."""
+        if isinstance(src, np.ndarray):
+            src = np.ascontiguousarray(src, np.uint32)
+        if isinstance(tgt, np.ndarray):
+            tgt = np.ascontiguousarray(tgt, np.uint32)
+        sp, where = _ptr(src)
+        tp, where2 = _ptr(tgt)
+        if where != where2:
+            raise ValueError("src and tgt must live on the same side")
+        if isinstance(src, int):
+            raise ValueError("pass arrays or tensors, not raw addresses")
+        cnt = C.c_uint64()
+        self._check(self.lib.cytom_delete_batch(self.ctx, sp, tp, len(src), where, C.byref(cnt)))
+        return cnt.value
+
+    def delete_random(self, count: int, seed: int = 0):
+        """Deletes `count` random stored edges (uniform tile, then uniform edge: the
+        reference's deletion_percentage mode). Returns (deleted, src picks, tgt picks),
+        UINT32_MAX where a pick hit an empty tile."""
+        src = np.empty(count, np.uint32)
+        tgt = np.empty(count, np.uint32)
+        cnt = C.c_uint64()
+        self._check(self.lib.cytom_delete_random(self.ctx, count, seed, src.ctypes.data, tgt.ctypes.data,
+                                                 L.PTR_HOST, C.byref(cnt)))
+        return cnt.value, src, tgt
+
     def set_edge_weights(self, src, tgt, w):
         """Overwrites the weights of stored edges (uint32 values or float32 bit patterns)."""
         src = np.ascontiguousarray(src, np.uint32)

@@ -244,6 +244,30 @@ int cytom_job_set_teleport(cytom_ctx* ctx, int job_id, const double* teleport, i
 int cytom_pagerank_adjoint(cytom_ctx* ctx, int job_id, const double* c_weights, int c_where,
                            float* d_weights, float* d_teleport, int out_where, cytom_run_stats* stats);
 
+/* Deletes the stored edges (src[i], tgt[i]) after compacting pending edges; replaces
+ * TileManager::deleteEdge / deleteRandomEdge with the compactStorage filter
+ * (src/include/tile-manager/tile-manager.h:165-186, 249-253, 532-535) and
+ * MetaTileManager::deleteEdge (src/include/tile-manager/meta-tile-manager.h:127-131).
+ * A pair listed twice is deleted once; a pair that is not stored is skipped. Each deleted
+ * edge lowers out_degree[src] and in_degree[tgt] by one. BFS / CC / SSSP / SSWP jobs for
+ * which a deleted edge was tight (it carried its target's value: the reference's
+ * critical-neighbour test, meta-tile-manager.h:213-226) restart from scratch on their
+ * next run; the others keep their values, which stay exact. PageRank jobs re-converge.
+ * *deleted (may be NULL) = edges deleted. */
+int cytom_delete_batch(cytom_ctx* ctx, const uint32_t* src, const uint32_t* tgt, uint64_t count, int where,
+                       uint64_t* deleted);
+
+/* Deletes `count` randomly picked stored edges: the reference's deletion_percentage mode
+ * (src/include/tile-manager/meta-tile-manager.h:201-231 with TileManager::deleteRandomEdge,
+ * tile-manager.h:175-190). After compacting pending edges, pick i takes a tile uniformly
+ * (hash64(hash64(seed) + 2i) mod tiles, the hash of src/include/util/util.h:188-196) and
+ * one of its edges uniformly (hash64(hash64(seed) + 2i + 1) mod its edge count); an empty
+ * tile gives no edge. The picks are then deleted as by cytom_delete_batch (a pair picked
+ * twice once). src / tgt (both NULL, or `count` words each on the `where` side) receive
+ * the picks, UINT32_MAX for none. *deleted (may be NULL) = edges deleted. */
+int cytom_delete_random(cytom_ctx* ctx, uint64_t count, uint64_t seed, uint32_t* src, uint32_t* tgt, int where,
+                        uint64_t* deleted);
+
 /* Overwrites the weights of stored edges (src[i], tgt[i]) with w[i] (uint32, or float
  * bits in a CYTOM_WEIGHT_F32 store), after compacting pending edges: the weight carried
  * by the reference's Edge (mutate_weight, src/include/edge-inserter/i-edge-provider.h:88)

@@ -273,6 +273,70 @@ void orc_store_compact(orc_store* s) {
   }
 }
 
+/* Deletion (the working part of TileManager::deleteEdge / compactStorage's deleted-edge
+ * filter, tile-manager.h:165-173, 251, 534): pending edges are compacted first, then each
+ * listed (src, tgt) is removed from its tile if stored; every removed edge decrements
+ * out_deg[src] and in_deg[tgt] once; the compact flag follows the remaining sources.
+ * Returns the edges removed (a pair listed twice is removed once). */
+uint64_t orc_store_delete(orc_store* s, const uint32_t* src, const uint32_t* tgt, uint64_t count) {
+  orc_store_compact(s);
+  const uint64_t mask = s->vpt - 1;
+  uint64_t removed = 0;
+  uint8_t* touched = (uint8_t*)calloc(s->ntiles, 1);
+  for (uint64_t i = 0; i < count; ++i) {
+    if (src[i] >= s->n || tgt[i] >= s->n) continue;
+    const uint64_t ti = (src[i] / s->vpt) * s->T + tgt[i] / s->vpt;
+    orc_tile* t = &s->tiles[ti];
+    const uint32_t key = ((uint32_t)(src[i] & mask) << 16) | (uint32_t)(tgt[i] & mask);
+    uint64_t lo = 0, hi = t->csr_len;
+    while (lo < hi) {
+      const uint64_t mid = (lo + hi) / 2;
+      if (t->csr[mid] < key) lo = mid + 1;
+      else hi = mid;
+    }
+    if (lo >= t->csr_len || t->csr[lo] != key) continue;
+    memmove(t->csr + lo, t->csr + lo + 1, (t->csr_len - lo - 1) * 4);
+    if (s->weighted) memmove(t->csr_w + lo, t->csr_w + lo + 1, (t->csr_len - lo - 1) * 4);
+    t->csr_len--;
+    s->out_deg[src[i]]--;
+    s->in_deg[tgt[i]]--;
+    touched[ti] = 1;
+    ++removed;
+  }
+  for (uint64_t ti = 0; ti < s->ntiles; ++ti) {
+    if (!touched[ti]) continue;
+    orc_tile* t = &s->tiles[ti];
+    uint64_t sources = 0;
+    for (uint64_t i = 0; i < t->csr_len; ++i)
+      if (i == 0 || (t->csr[i] >> 16) != (t->csr[i - 1] >> 16)) ++sources;
+    t->compact = (sources >= s->vpt / 2) ? 1 : 0;
+  }
+  free(touched);
+  return removed;
+}
+
+/* Random deletion picks (the reference's deletion_percentage mode,
+ * meta-tile-manager.h:201-231 with TileManager::deleteRandomEdge, tile-manager.h:175-190):
+ * pick i chooses a tile uniformly (hash64(hash64(seed) + 2i) mod tiles) and, if the tile
+ * holds edges, one of them uniformly (hash64(hash64(seed) + 2i + 1) mod its edge count);
+ * an empty tile yields no edge (0xFFFFFFFF, 0xFFFFFFFF). Picks are taken from the store
+ * after compaction, all from the same snapshot. */
+void orc_store_pick_random(orc_store* s, uint64_t count, uint64_t seed, uint32_t* src, uint32_t* tgt) {
+  orc_store_compact(s);
+  const uint64_t hs = orc_hash64(seed);
+  for (uint64_t i = 0; i < count; ++i) {
+    const uint64_t ti = orc_hash64(hs + 2 * i) % s->ntiles;
+    const orc_tile* t = &s->tiles[ti];
+    if (t->csr_len == 0) {
+      src[i] = tgt[i] = 0xFFFFFFFFu;
+      continue;
+    }
+    const uint32_t e = t->csr[orc_hash64(hs + 2 * i + 1) % t->csr_len];
+    src[i] = (uint32_t)((ti / s->T) * s->vpt) | (e >> 16);
+    tgt[i] = (uint32_t)((ti % s->T) * s->vpt) | (e & 0xFFFFu);
+  }
+}
+
 uint64_t orc_store_count_edges(const orc_store* s) {
   uint64_t c = 0;
   for (uint64_t t = 0; t < s->ntiles; ++t) c += s->tiles[t].csr_len + s->tiles[t].ovf_len;

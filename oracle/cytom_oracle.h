@@ -55,6 +55,12 @@ int orc_store_insert(orc_store* s, const uint32_t* src, const uint32_t* tgt,
 /* TileStore::doGlobalCompaction -> TileManager::compactStorage per tile. */
 void orc_store_compact(orc_store* s);
 uint64_t orc_store_count_edges(const orc_store* s); /* CSR + overflow */
+/* Removes stored (src, tgt) pairs after compacting; degrees drop by one per removed
+ * edge. Returns the edges removed. */
+uint64_t orc_store_delete(orc_store* s, const uint32_t* src, const uint32_t* tgt, uint64_t count);
+/* Random deletion picks: uniform tile, then a uniform edge in it (none for an empty tile:
+ * 0xFFFFFFFF twice), hash-seeded, from the compacted store. */
+void orc_store_pick_random(orc_store* s, uint64_t count, uint64_t seed, uint32_t* src, uint32_t* tgt);
 uint64_t orc_store_count_tiles(const orc_store* s);
 /* Dump of the compacted CSR part in tile-id order (id = x*T + y):
  * tile_ptr[ntiles+1], packed edges (src_l<<16 | tgt_l), weights (nullable),

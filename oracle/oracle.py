@@ -50,6 +50,10 @@ def lib() -> C.CDLL:
         L.orc_store_destroy.argtypes = [vp]
         L.orc_store_insert.restype = C.c_int
         L.orc_store_insert.argtypes = [vp, vp, vp, vp, u64]
+        L.orc_store_delete.restype = u64
+        L.orc_store_delete.argtypes = [vp, vp, vp, u64]
+        L.orc_store_pick_random.restype = None
+        L.orc_store_pick_random.argtypes = [vp, u64, u64, vp, vp]
         L.orc_store_compact.restype = None
         L.orc_store_compact.argtypes = [vp]
         L.orc_store_count_edges.restype = u64
@@ -137,6 +141,17 @@ class Store:
 
     def compact(self):
         lib().orc_store_compact(self.h)
+
+    def delete(self, src, tgt) -> int:
+        src = np.ascontiguousarray(src, np.uint32)
+        tgt = np.ascontiguousarray(tgt, np.uint32)
+        return lib().orc_store_delete(self.h, src.ctypes.data, tgt.ctypes.data, len(src))
+
+    def pick_random(self, count: int, seed: int):
+        src = np.empty(count, np.uint32)
+        tgt = np.empty(count, np.uint32)
+        lib().orc_store_pick_random(self.h, count, seed, src.ctypes.data, tgt.ctypes.data)
+        return src, tgt
 
     def count_edges(self) -> int:
         return lib().orc_store_count_edges(self.h)

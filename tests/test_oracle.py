@@ -146,6 +146,74 @@ def test_compaction_matches_numpy(orc, n, vpt, weighted):
     assert np.array_equal(cf, rcf)
 
 
+@pytest.mark.parametrize("weighted", [False, True])
+def test_store_delete_matches_numpy(orc, weighted):
+    # deletion after compaction of pending edges: the stored set minus the listed pairs
+    # (duplicates deleted once, absent and out-of-range pairs skipped), degrees lowered by
+    # the deleted edges, storage flags from the remaining distinct sources
+    n, vpt = 512, 64
+    rng = np.random.default_rng(7 + weighted)
+    st = orc.Store(n, vpt, weighted)
+    ref = orc.Store(n, vpt, weighted)
+    for b in range(2):  # the second batch stays pending until the deletion compacts it
+        src = rng.integers(0, n, 6000, dtype=np.uint32)
+        tgt = rng.integers(0, n // 2, 6000, dtype=np.uint32)
+        w = rng.integers(1, 255, 6000, dtype=np.uint32)
+        for x in (st, ref):
+            x.insert(src, tgt, w if weighted else None)
+        if b == 0:
+            st.compact()
+    ref.compact()
+    s1, t1, w1 = orc.store_edges(ref)
+    o1, i1 = ref.degrees()
+    k = rng.choice(len(s1), 900, replace=False)
+    ds = np.concatenate([s1[k], s1[k[:60]], rng.integers(0, n, 300, dtype=np.uint32),
+                         np.array([n + 3, 5], np.uint32)])
+    dt = np.concatenate([t1[k], t1[k[:60]], rng.integers(0, n, 300, dtype=np.uint32),
+                         np.array([1, n + 9], np.uint32)])
+    removed = st.delete(ds, dt)
+    gone = np.isin(s1.astype(np.uint64) << np.uint64(32) | t1, ds.astype(np.uint64) << np.uint64(32) | dt)
+    assert removed == int(gone.sum()) and removed >= 900
+    s2, t2, w2 = orc.store_edges(st)
+    assert np.array_equal(s2, s1[~gone]) and np.array_equal(t2, t1[~gone])
+    if weighted:
+        assert np.array_equal(w2, w1[~gone])
+    o2, i2 = st.degrees()
+    assert np.array_equal(o2, o1 - np.bincount(s1[gone], minlength=n).astype(np.uint32))
+    assert np.array_equal(i2, i1 - np.bincount(t1[gone], minlength=n).astype(np.uint32))
+    tp, ed, _, cf = st.dump()
+    T = n // vpt
+    for ti in range(T * T):
+        srcs = np.unique(ed[int(tp[ti]):int(tp[ti + 1])] >> 16)
+        assert cf[ti] == (1 if len(srcs) >= vpt // 2 else 0), ti
+    # a deleted pair inserted again is stored again
+    st.insert(ds[:10], dt[:10], np.full(10, 7, np.uint32) if weighted else None)
+    st.compact()
+    assert st.count_edges() == len(s2) + len(np.unique(ds[:10].astype(np.uint64) << np.uint64(32) | dt[:10]))
+
+
+def test_store_pick_random(orc):
+    # picks are stored edges of the hashed tile (none for an empty tile), deterministic in
+    # the seed, and roughly uniform over tiles
+    n, vpt = 256, 64
+    st = orc.Store(n, vpt)
+    rng = np.random.default_rng(2)
+    src = rng.integers(0, n // 2, 3000, dtype=np.uint32)  # tiles of source block >= 2 stay empty
+    tgt = rng.integers(0, n, 3000, dtype=np.uint32)
+    st.insert(src, tgt)
+    s, t = st.pick_random(4000, 9)
+    s2, t2 = st.pick_random(4000, 9)
+    assert np.array_equal(s, s2) and np.array_equal(t, t2)
+    none = s == 0xFFFFFFFF
+    assert np.array_equal(none, t == 0xFFFFFFFF)
+    stored = set(zip(src.tolist(), tgt.tolist()))
+    assert all((a, b) in stored for a, b in zip(s[~none].tolist(), t[~none].tolist()))
+    assert 0.4 < none.mean() < 0.6  # half of the 16 tiles are empty
+    T = n // vpt
+    counts = np.bincount((s[~none] // vpt) * T + t[~none] // vpt, minlength=T * T)[: T * T // 2]
+    assert counts.min() > 0.6 * counts.mean()
+
+
 def test_fillcsr_corner_edge_dropped(orc):
     # tile-manager.h:519-541: with vpt = 65536 an otherwise empty tile whose only edge is
     # local (65535, 65535) comes out empty; next to another edge it survives.

@@ -373,7 +373,7 @@ int exclusive_scan_u32(Ctx* c, const uint32_t* in, uint32_t* out, uint64_t n, ui
 // Upsweep: per-block digit histogram (digit-major). Scan. Downsweep: warps rank
 // items with __match_any_sync in input order and scatter.
 // --------------------------------------------------------------------------
-constexpr int RS_T = 256, RS_IPT = 16, RS_TILE = RS_T * RS_IPT, RS_WARPS = RS_T / 32;
+constexpr int RS_T = 256, RS_IPT = 16, RS_TILE = RS_T * RS_IPT, RS_WARPS = RS_T / 32;  // tile size shared with noalloc.cu
 
 __global__ void radix_upsweep_kernel(const uint64_t* __restrict__ keys, uint64_t n, int shift,
                                      uint32_t* __restrict__ hist, uint32_t nb) {
@@ -381,40 +381,60 @@ __global__ void radix_upsweep_kernel(const uint64_t* __restrict__ keys, uint64_t
   cnt[threadIdx.x] = 0;
   __syncthreads();
   uint64_t base = (uint64_t)blockIdx.x * RS_TILE;
-#pragma unroll 4
+  uint32_t d_reg[RS_IPT];
+#pragma unroll
   for (int k = 0; k < RS_IPT; ++k) {
     uint64_t i = base + (uint64_t)k * RS_T + threadIdx.x;
-    if (i < n) atomicAdd(&cnt[(keys[i] >> shift) & 0xFF], 1u);
+    d_reg[k] = (i < n) ? (uint32_t)((keys[i] >> shift) & 0xFF) : 256u;
+  }
+  // warp-aggregated counts (skewed digits would serialise per-key shared atomics)
+  const unsigned lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < RS_IPT; ++k) {
+    const unsigned peers = __match_any_sync(0xFFFFFFFFu, d_reg[k]);
+    if (d_reg[k] < 256u && (__ffs(peers) - 1) == (int)lane) atomicAdd(&cnt[d_reg[k]], (uint32_t)__popc(peers));
   }
   __syncthreads();
   hist[(uint64_t)threadIdx.x * nb + blockIdx.x] = cnt[threadIdx.x];
 }
 
-__global__ void radix_downsweep_kernel(const uint64_t* __restrict__ keys,
-                                       const uint32_t* __restrict__ vals, uint64_t n, int shift,
-                                       const uint32_t* __restrict__ offs, uint32_t nb,
-                                       uint64_t* __restrict__ keys_out,
-                                       uint32_t* __restrict__ vals_out) {
+__global__ void __launch_bounds__(RS_T) radix_downsweep_kernel(const uint64_t* __restrict__ keys,
+                                                                const uint32_t* __restrict__ vals, uint64_t n,
+                                                                int shift, const uint32_t* __restrict__ offs,
+                                                                uint32_t nb, uint64_t* __restrict__ keys_out,
+                                                                uint32_t* __restrict__ vals_out) {
   __shared__ uint32_t wcnt[RS_WARPS][256];
   __shared__ uint32_t base_d[256];
   const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
   for (int d = threadIdx.x; d < RS_WARPS * 256; d += RS_T) (&wcnt[0][0])[d] = 0;
   base_d[threadIdx.x] = offs[(uint64_t)threadIdx.x * nb + blockIdx.x];
   __syncthreads();
   const uint64_t wbase = (uint64_t)blockIdx.x * RS_TILE + (uint64_t)wid * (32 * RS_IPT);
+  // every key and value is loaded before any is used
   uint64_t k_reg[RS_IPT];
+  uint32_t v_reg[RS_IPT];
   uint32_t d_reg[RS_IPT];
 #pragma unroll
   for (int k = 0; k < RS_IPT; ++k) {
     uint64_t i = wbase + (uint64_t)k * 32 + lane;
     k_reg[k] = (i < n) ? keys[i] : 0ULL;
+    v_reg[k] = (vals && i < n) ? vals[i] : 0u;
     d_reg[k] = (i < n) ? (uint32_t)((k_reg[k] >> shift) & 0xFF) : 256u;
   }
-  // phase 1: per-warp digit counts
+  // phase 1: each key's rank among the warp's keys of its digit, in input order
+  uint32_t r_reg[RS_IPT];
 #pragma unroll
   for (int k = 0; k < RS_IPT; ++k) {
-    unsigned peers = __match_any_sync(0xFFFFFFFFu, d_reg[k]);
-    if (d_reg[k] < 256u && (__ffs(peers) - 1) == (int)lane) wcnt[wid][d_reg[k]] += __popc(peers);
+    const uint32_t d = d_reg[k];
+    const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
+    const int leader = __ffs(peers) - 1;
+    uint32_t old = 0;
+    if ((int)lane == leader && d < 256u) {
+      old = wcnt[wid][d];
+      wcnt[wid][d] = old + __popc(peers);
+    }
+    r_reg[k] = __shfl_sync(0xFFFFFFFFu, old, leader) + __popc(peers & lt);
     __syncwarp();
   }
   __syncthreads();
@@ -430,21 +450,15 @@ __global__ void radix_downsweep_kernel(const uint64_t* __restrict__ keys,
     }
   }
   __syncthreads();
-  // phase 3: rank and scatter in input order
-  const unsigned lt = (1u << lane) - 1u;
+  // phase 3: scatter (stable: block offset + warp offset + rank)
 #pragma unroll
   for (int k = 0; k < RS_IPT; ++k) {
-    uint32_t d = d_reg[k];
-    unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
-    uint32_t before = (d < 256u) ? wcnt[wid][d] : 0u;
-    __syncwarp();
+    const uint32_t d = d_reg[k];
     if (d < 256u) {
-      uint32_t pos = base_d[d] + before + __popc(peers & lt);
+      const uint32_t pos = base_d[d] + wcnt[wid][d] + r_reg[k];
       keys_out[pos] = k_reg[k];
-      if (vals) vals_out[pos] = vals[wbase + (uint64_t)k * 32 + lane];
-      if ((__ffs(peers) - 1) == (int)lane) wcnt[wid][d] = before + __popc(peers);
+      if (vals) vals_out[pos] = v_reg[k];
     }
-    __syncwarp();
   }
 }
 
@@ -584,56 +598,210 @@ __global__ void new_tile_ptr_kernel(const unsigned long long* __restrict__ tile_
 
 // Output position o of the merged store holds kept batch element b when q[b] == o,
 // otherwise old store element o - (number of q below o). One warp produces 32
-// consecutive outputs per step: lane j loads candidate q[b + j], the warp ORs the
-// window bits of the candidates that land in the window, and every lane derives its
-// source from the mask. Stores are coalesced 128-byte warp writes.
-constexpr int MERGE_STEPS = 32;  // 1024 outputs per warp
+// consecutive outputs per step, 1024 per span. merge_spans_kernel gives every span its
+// first new element (sb) and the tile of its first output (ts) by binary searches that
+// all run at once. When a span holds at most 64 new elements (the usual case: new edges
+// are sparse in the store) they sit in two registers per lane and each step finds its
+// candidates by shuffles, so the sources of MG steps are known without memory round
+// trips and their loads issue together; a span with more new elements loads its
+// candidates step by step. Stores are coalesced 128-byte warp writes.
+//
+// The same pass writes the chunk table of the new store and, when the context keeps a
+// source directory, its per-edge entries (the work of dir_edges_kernel): each output
+// knows its tile (walked from the span's first tile) and the edge before it.
+constexpr int MERGE_STEPS = 32;  // 1024 outputs per warp span
+constexpr uint64_t MERGE_SPAN = 32ULL * MERGE_STEPS;
+constexpr int MG = 8;            // steps whose loads are issued together
+
+__global__ void merge_spans_kernel(const unsigned long long* __restrict__ q, const uint32_t* __restrict__ Kdev,
+                                   uint64_t E, const unsigned long long* __restrict__ tp, uint64_t ntiles,
+                                   uint64_t nsp, uint32_t* __restrict__ sb, uint32_t* __restrict__ ts,
+                                   uint32_t* __restrict__ chunk_tile) {
+  const uint64_t K = *Kdev;
+  const uint64_t total = E + K;
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid == 0) chunk_tile[(total + kChunk - 1) / kChunk] = (uint32_t)(ntiles - 1);
+  for (uint64_t sp = gid; sp <= nsp; sp += stride) {
+    const uint64_t target = sp * MERGE_SPAN;
+    uint64_t lo = 0, hi = K;
+    while (lo < hi) {
+      uint64_t mid = lo + ((hi - lo) >> 1);
+      if (q[mid] < target) lo = mid + 1;
+      else hi = mid;
+    }
+    sb[sp] = (uint32_t)lo;
+    // the last tile t with tp[t] <= target
+    lo = 0;
+    hi = ntiles - 1;
+    while (lo < hi) {
+      const uint64_t mid = (lo + hi + 1) >> 1;
+      if (tp[mid] <= target) lo = mid;
+      else hi = mid - 1;
+    }
+    ts[sp] = (uint32_t)lo;
+  }
+}
+
+// Per output (offsets relative to the span start): its tile, walked forward from the
+// warp's tile state (tile t; toff turns a span offset into an offset within the tile;
+// tend = the span offset where the tile ends), the chunk-table entry at every 128th
+// output, and the directory entries of the 32-source blocks that start at this edge.
+// The tile state of lane 31 carries over to the next step.
+__device__ __forceinline__ void merge_index_step(uint32_t o, uint32_t nout, uint32_t ev, uint32_t pv, uint32_t& t,
+                                                 uint32_t& toff, uint32_t& tend, uint64_t wbase,
+                                                 const unsigned long long* __restrict__ tp,
+                                                 uint32_t* __restrict__ ctb, uint32_t* __restrict__ dir,
+                                                 uint32_t nbw) {
+  uint32_t lt = t, loff = toff, lend = tend;
+  if (o < nout) {
+    while (o >= lend) {
+      ++lt;
+      loff = 0u - lend;
+      const unsigned long long nx = tp[lt + 1] - wbase;
+      lend = nx > 0xFFFFFFFFULL ? 0xFFFFFFFFu : (uint32_t)nx;
+    }
+    if ((o & (kChunk - 1)) == 0) ctb[o / kChunk] = lt;
+    if (dir) {
+      const uint32_t off = o + loff;
+      const int bk = (int)(ev >> 21);
+      const int bprev = off == 0 ? -1 : (int)(pv >> 21);
+      if (bk != bprev) {
+        uint32_t* dt = dir + (uint64_t)lt * (nbw + 1);
+        for (int bb = bprev + 1; bb <= bk; ++bb) dt[bb] = off;
+      }
+    }
+  }
+  t = __shfl_sync(0xFFFFFFFFu, lt, 31);
+  toff = __shfl_sync(0xFFFFFFFFu, loff, 31);
+  tend = __shfl_sync(0xFFFFFFFFu, lend, 31);
+}
+
 __global__ void merge_gather_kernel(const uint32_t* __restrict__ edges, const uint32_t* __restrict__ wts,
                                     uint64_t E, const unsigned long long* __restrict__ q,
                                     const uint32_t* __restrict__ nloc, const uint32_t* __restrict__ nw,
-                                    const uint32_t* __restrict__ Kdev, uint32_t* __restrict__ oe,
+                                    const uint32_t* __restrict__ Kdev, const uint32_t* __restrict__ sb,
+                                    const uint32_t* __restrict__ ts, uint64_t nsp,
+                                    const unsigned long long* __restrict__ tp, uint32_t* __restrict__ chunk_tile,
+                                    uint32_t* __restrict__ dir, uint32_t nbw, uint32_t* __restrict__ oe,
                                     uint32_t* __restrict__ ow) {
   const uint64_t K = *Kdev;
   const uint64_t total = E + K;
   const unsigned lane = threadIdx.x & 31;
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  const uint64_t span = 32ULL * MERGE_STEPS;
   const unsigned lt = (1u << lane) - 1u;
-  for (uint64_t wbase = warp * span; wbase < total; wbase += nwarps * span) {
-    uint64_t b = 0;
-    if (lane == 0) {
-      uint64_t lo = 0, hi = K;
-      while (lo < hi) {
-        uint64_t mid = lo + ((hi - lo) >> 1);
-        if (q[mid] < wbase) lo = mid + 1;
-        else hi = mid;
-      }
-      b = lo;
+  for (uint64_t sp = warp; sp < nsp; sp += nwarps) {
+    const uint64_t wbase = sp * MERGE_SPAN;
+    if (wbase >= total) break;
+    const uint32_t nout = (uint32_t)(total - wbase < MERGE_SPAN ? total - wbase : MERGE_SPAN);
+    const uint64_t b0 = sb[sp];
+    const uint32_t cnt = sb[sp + 1] - (uint32_t)b0;
+    // span-relative views: output x preceded by y new elements of the span comes from
+    // eb[x - y] (old) or nb[y] (new)
+    const uint32_t* eb = edges + (wbase - b0);
+    const uint32_t* wb = wts ? wts + (wbase - b0) : nullptr;
+    const uint32_t* nb = nloc + b0;
+    const uint32_t* nwb = nw ? nw + b0 : nullptr;
+    uint32_t* oeb = oe + wbase;
+    uint32_t* owb = ow ? ow + wbase : nullptr;
+    uint32_t* ctb = chunk_tile + wbase / kChunk;
+    uint32_t t = ts[sp];
+    uint32_t toff = (uint32_t)(wbase - tp[t]);
+    uint32_t tend;
+    {
+      const unsigned long long nx = tp[t + 1] - wbase;
+      tend = nx > 0xFFFFFFFFULL ? 0xFFFFFFFFu : (uint32_t)nx;
     }
-    b = __shfl_sync(0xFFFFFFFFu, b, 0);
-    for (int st = 0; st < MERGE_STEPS; ++st) {
-      const uint64_t o_start = wbase + (uint64_t)st * 32;
-      if (o_start >= total) break;
-      uint64_t cand = (b + lane < K) ? q[b + lane] : ~0ULL;
-      unsigned bitv = (cand >= o_start && cand < o_start + 32) ? (1u << (unsigned)(cand - o_start)) : 0u;
-      unsigned mask = __reduce_or_sync(0xFFFFFFFFu, bitv);
-      const uint64_t o = o_start + lane;
-      if (o < total) {
-        unsigned before = __popc(mask & lt);
-        uint32_t ev, wv = 0;
-        if ((mask >> lane) & 1u) {
-          ev = nloc[b + before];
-          if (ow) wv = nw[b + before];
-        } else {
-          uint64_t s = o - (b + before);
-          ev = edges[s];
-          if (ow) wv = wts[s];
+    // the edge before the span (the first output's predecessor)
+    uint32_t plast = 0;
+    if (lane == 0 && wbase > 0) {
+      if (b0 > 0 && q[b0 - 1] == wbase - 1) plast = nloc[b0 - 1];
+      else plast = edges[wbase - 1 - b0];
+    }
+    plast = __shfl_sync(0xFFFFFFFFu, plast, 0);
+    if (cnt <= 64) {
+      const uint32_t qa = (lane < cnt) ? (uint32_t)(q[b0 + lane] - wbase) : 0xFFFFFFFFu;
+      const uint32_t qb = (32 + lane < cnt) ? (uint32_t)(q[b0 + 32 + lane] - wbase) : 0xFFFFFFFFu;
+      uint32_t r = 0;  // new elements consumed so far in this span
+      for (int g = 0; g < MERGE_STEPS; g += MG) {
+        if ((uint32_t)g * 32 >= nout) break;
+        uint32_t src[MG];
+        unsigned isnew = 0;
+#pragma unroll
+        for (int k = 0; k < MG; ++k) {
+          const uint32_t o_start = (uint32_t)(g + k) * 32;
+          const uint32_t idx = r + lane;
+          const uint32_t ca = __shfl_sync(0xFFFFFFFFu, qa, idx & 31);
+          const uint32_t cb = __shfl_sync(0xFFFFFFFFu, qb, idx & 31);
+          const uint32_t rel = (idx < 32 ? ca : (idx < 64 ? cb : 0xFFFFFFFFu)) - o_start;
+          const unsigned mask = __reduce_or_sync(0xFFFFFFFFu, rel < 32u ? (1u << rel) : 0u);
+          const uint32_t y = r + __popc(mask & lt);
+          if ((mask >> lane) & 1u) {
+            isnew |= 1u << k;
+            src[k] = y;
+          } else {
+            src[k] = o_start + lane - y;
+          }
+          r += __popc(mask);
         }
-        oe[o] = ev;
-        if (ow) ow[o] = wv;
+        uint32_t ev[MG], wv[MG];
+#pragma unroll
+        for (int k = 0; k < MG; ++k) {
+          const uint32_t o = (uint32_t)(g + k) * 32 + lane;
+          ev[k] = 0;
+          wv[k] = 0;
+          if (o < nout) {
+            if ((isnew >> k) & 1u) {
+              ev[k] = nb[src[k]];
+              if (owb) wv[k] = nwb[src[k]];
+            } else {
+              ev[k] = eb[src[k]];
+              if (owb) wv[k] = wb[src[k]];
+            }
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < MG; ++k) {
+          const uint32_t o = (uint32_t)(g + k) * 32 + lane;
+          if (o < nout) {
+            oeb[o] = ev[k];
+            if (owb) owb[o] = wv[k];
+          }
+          uint32_t pv = __shfl_up_sync(0xFFFFFFFFu, ev[k], 1);
+          if (lane == 0) pv = plast;
+          merge_index_step(o, nout, ev[k], pv, t, toff, tend, wbase, tp, ctb, dir, nbw);
+          plast = __shfl_sync(0xFFFFFFFFu, ev[k], 31);
+        }
       }
-      b += __popc(mask);
+      continue;
+    }
+    uint32_t r = 0;
+    for (int st = 0; st < MERGE_STEPS; ++st) {
+      const uint32_t o_start = (uint32_t)st * 32;
+      if (o_start >= nout) break;
+      const uint32_t cand = (r + lane < cnt) ? (uint32_t)(q[b0 + r + lane] - wbase) : 0xFFFFFFFFu;
+      const uint32_t rel = cand - o_start;
+      const unsigned mask = __reduce_or_sync(0xFFFFFFFFu, rel < 32u ? (1u << rel) : 0u);
+      const uint32_t o = o_start + lane;
+      uint32_t ev = 0, wv = 0;
+      if (o < nout) {
+        const uint32_t y = r + __popc(mask & lt);
+        if ((mask >> lane) & 1u) {
+          ev = nb[y];
+          if (owb) wv = nwb[y];
+        } else {
+          ev = eb[o - y];
+          if (owb) wv = wb[o - y];
+        }
+        oeb[o] = ev;
+        if (owb) owb[o] = wv;
+      }
+      uint32_t pv = __shfl_up_sync(0xFFFFFFFFu, ev, 1);
+      if (lane == 0) pv = plast;
+      merge_index_step(o, nout, ev, pv, t, toff, tend, wbase, tp, ctb, dir, nbw);
+      plast = __shfl_sync(0xFFFFFFFFu, ev, 31);
+      r += __popc(mask);
     }
   }
 }
@@ -735,6 +903,8 @@ int ensure_app_capacity(Ctx* c, uint64_t need) {
   return CYTOM_OK;
 }
 
+__global__ void dir_tiles_kernel(const StoreDesc* __restrict__ sd, uint32_t* __restrict__ dir, uint32_t nbw);
+
 int compact(Ctx* c) {
   if (c->A == 0) return CYTOM_OK;
   const uint64_t A = c->A;
@@ -748,7 +918,8 @@ int compact(Ctx* c) {
   rc = grow_store(c, c->E + A);
   if (rc) return rc;
   // temporaries
-  size_t bytes = A * (4 + 4 + 8 + 4 + 8 + 4 + 4 + 4) + 64;
+  const uint64_t nsp = (c->E + A + MERGE_SPAN - 1) / MERGE_SPAN;  // merge spans (upper bound)
+  size_t bytes = A * (4 + 4 + 8 + 4 + 8 + 4 + 4 + 4) + 64 + 2 * (nsp + 1) * 4;
   char* tmp = nullptr;
   cudaError_t e = cudaMallocAsync((void**)&tmp, bytes, c->stream);
   if (e != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "compaction temporaries");
@@ -761,6 +932,8 @@ int compact(Ctx* c) {
   uint32_t* nw = nloc + A;
   uint32_t* ntile = nw + A;
   uint32_t* Kdev = ntile + A;
+  uint32_t* sb = Kdev + 16;
+  uint32_t* ts = sb + (nsp + 1);
   int slot = prof_begin(c, KC_MERGE);
   dedupe_lookup_kernel<<<grid_for(c, A, 256), 256, 0, c->stream>>>(
       K, W, A, c->edges, c->wts, c->tile_ptr, c->lvpt, keep, lb, wsel);
@@ -773,9 +946,15 @@ int compact(Ctx* c) {
   new_tile_ptr_kernel<<<grid_for(c, c->ntiles + 1, 256), 256, 0, c->stream>>>(
       c->tile_ptr, c->ntiles, ntile, Kdev, c->tile_ptr_alt);
   c->launches++;
-  merge_gather_kernel<<<grid_for(c, (c->E + A + 31) / 32, 256, 16), 256, 0, c->stream>>>(
-      c->edges, c->wts, c->E, q, nloc, nw, Kdev, c->edges_alt, wt ? c->wts_alt : nullptr);
-  c->launches++;
+  // the directory is kept up to date by the merge once a context has one
+  uint32_t* mdir = (c->dir && !c->dir_disabled) ? c->dir : nullptr;
+  merge_spans_kernel<<<grid_for(c, nsp + 1, 256), 256, 0, c->stream>>>(q, Kdev, c->E, c->tile_ptr_alt, c->ntiles,
+                                                                       nsp, sb, ts, c->chunk_tile);
+  merge_gather_kernel<<<(unsigned)std::max<uint64_t>(1, std::min<uint64_t>((nsp + 7) / 8, (uint64_t)c->num_sms * 8)),
+                        256, 0, c->stream>>>(c->edges, c->wts, c->E, q, nloc, nw, Kdev, sb, ts, nsp, c->tile_ptr_alt,
+                                             c->chunk_tile, mdir, (uint32_t)(c->vpt / 32), c->edges_alt,
+                                             wt ? c->wts_alt : nullptr);
+  c->launches += 2;
   e = cudaMemcpyAsync(c->h_pinned, Kdev, 4, cudaMemcpyDeviceToHost, c->stream);
   cudaFreeAsync(tmp, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
@@ -788,13 +967,15 @@ int compact(Ctx* c) {
   c->E += Kn;
   c->A = 0;
   c->version++;
-  uint64_t nch = (c->E + kChunk - 1) / kChunk;
-  chunk_tile_kernel<<<grid_for(c, nch + 1, 256), 256, 0, c->stream>>>(c->tile_ptr, c->ntiles, nch,
-                                                                     c->chunk_tile);
-  c->launches++;
   e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_err(c, e, "chunk_tile");
-  return upload_store_desc(c);
+  if (e != cudaSuccess) return cuda_err(c, e, "merge");
+  if (mdir) c->dir_version = c->version;  // completed below, before any later launch reads it
+  int urc = upload_store_desc(c);
+  if (urc || !mdir) return urc;
+  // the merge wrote every directory entry up to each tile's last source block
+  dir_tiles_kernel<<<grid_for(c, c->ntiles * 32, 256), 256, 0, c->stream>>>(c->dsd, c->dir, (uint32_t)(c->vpt / 32));
+  c->launches++;
+  return cuda_err(c, cudaGetLastError(), "directory");
 }
 
 // Compact-vs-sparse flag per tile: distinct sources >= vpt / 2 (tile-manager.h:261-263).
@@ -823,19 +1004,34 @@ __global__ void count_sources_kernel(const uint32_t* __restrict__ edges,
 // the previous edge's block up to its own start at this edge. Per tile: the blocks after
 // the last edge's block (all blocks of an empty tile) hold the tile size.
 __global__ void dir_edges_kernel(const StoreDesc* __restrict__ sd, uint32_t* __restrict__ dir, uint32_t nbw) {
-  // one warp per 128-edge chunk: one tile lookup per chunk, four edges per lane
+  // one warp per 128-edge chunk, four edges per lane; a chunk inside one tile (nearly
+  // all of them) takes a 32-bit fast path
   const uint64_t E = sd->E, nchunks = sd->nchunks;
   const unsigned lane = threadIdx.x & 31;
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   for (uint64_t c = warp; c < nchunks; c += nwarps) {
-    const uint64_t e0 = c * kChunk + (uint64_t)lane * 4;
-    if (e0 >= E) continue;
-    const uint4 q = *reinterpret_cast<const uint4*>(sd->edges + e0);
-    const uint32_t prev0 = e0 > 0 ? sd->edges[e0 - 1] : 0u;
+    const uint64_t cbase = c * kChunk;
+    const uint64_t e0 = cbase + (uint64_t)lane * 4;
+    const uint4 q = *reinterpret_cast<const uint4*>(sd->edges + e0);  // the store has kChunk slack
+    uint32_t prev0 = __shfl_up_sync(0xFFFFFFFFu, q.w, 1);
+    if (lane == 0) prev0 = cbase > 0 ? sd->edges[cbase - 1] : 0u;
     const uint32_t ev[5] = {prev0, q.x, q.y, q.z, q.w};
     uint32_t t = sd->chunk_tile[c];
     unsigned long long tlo = sd->tile_ptr[t], thi = sd->tile_ptr[t + 1];
+    const uint64_t cend = cbase + kChunk < E ? cbase + kChunk : E;
+    if (tlo <= cbase && cend <= thi) {
+      uint32_t* dt = dir + (uint64_t)t * (nbw + 1);
+      const uint32_t r0 = (uint32_t)(e0 - tlo);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (e0 + k >= E) break;
+        const int b = (int)(ev[k + 1] >> 21);
+        const int bprev = (r0 + k == 0) ? -1 : (int)(ev[k] >> 21);
+        for (int bb = bprev + 1; bb <= b; ++bb) dt[bb] = r0 + k;
+      }
+      continue;
+    }
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       const uint64_t e = e0 + k;

@@ -20,6 +20,7 @@ ERRORS = {
 PTR_HOST, PTR_DEVICE = 0, 1
 UNWEIGHTED, WEIGHT_U32, WEIGHT_F32 = 0, 1, 2
 ALGO_BFS, ALGO_CC, ALGO_SSSP, ALGO_PR_DELTA, ALGO_PAGERANK, ALGO_WPAGERANK, ALGO_SSWP = 0, 1, 2, 3, 4, 5, 6
+ALGO_BFS_ASYNC, ALGO_CC_ASYNC = 7, 8
 KERNEL_CLASSES = 8
 
 

@@ -37,7 +37,7 @@ def sources() -> list[Path]:
 def _stale(obj: Path, src: Path) -> bool:
     if not obj.exists():
         return True
-    deps = [src, *CSRC.glob("*.h"), *(PKG.parent / "include").glob("*.h")]
+    deps = [src, *CSRC.glob("*.h"), *CSRC.glob("*.cuh"), *(PKG.parent / "include").glob("*.h")]
     return any(d.stat().st_mtime > obj.stat().st_mtime for d in deps)
 
 

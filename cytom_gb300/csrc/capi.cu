@@ -146,6 +146,7 @@ int job_alloc(Ctx* c, Job* j) {
   j->h.ls = j->ls;
   j->h.algo = j->algo;
   j->h.kahan = j->params.kahan;
+  j->h.async = j->async ? 1 : 0;
   j->h.alpha = j->params.alpha;
   j->h.delta_param = j->params.delta;
   j->h.start = j->params.start_vertex;
@@ -611,9 +612,14 @@ int cytom_get_degrees(cytom_ctx* ctx, uint32_t* out_degree, uint32_t* in_degree)
 
 int cytom_job_create(cytom_ctx* ctx, int algo, const cytom_job_params* params, int* job_id) {
   Ctx* c = (Ctx*)ctx;
-  if (!c || !job_id || algo < CYTOM_ALGO_BFS || algo > CYTOM_ALGO_SSWP) return CYTOM_ERR_INVAL;
+  if (!c || !job_id || algo < CYTOM_ALGO_BFS || algo > CYTOM_ALGO_CC_ASYNC) return CYTOM_ERR_INVAL;
   Job* j = new (std::nothrow) Job();
   if (!j) return CYTOM_ERR_OOM;
+  if (algo == CYTOM_ALGO_BFS_ASYNC || algo == CYTOM_ALGO_CC_ASYNC) {
+    // the same program as BFS / CC with the asynchronous pull
+    j->async = true;
+    algo = algo == CYTOM_ALGO_BFS_ASYNC ? CYTOM_ALGO_BFS : CYTOM_ALGO_CC;
+  }
   j->algo = algo;
   if (params) j->params = *params;
   else cytom_job_params_default(&j->params);

@@ -100,6 +100,7 @@ struct JobDesc {
   LoopState* ls;
   int algo;
   int kahan;
+  int async;          // BFS / CC asynchronous programs: sources read from next
   double alpha, delta_param;
   unsigned long long start;
 };
@@ -111,6 +112,7 @@ struct Job {
   int algo = 0;
   cytom_job_params params{};
   bool fresh = true;          // next run starts from scratch
+  bool async = false;         // asynchronous program (CYTOM_ALGO_BFS_ASYNC / CC_ASYNC)
   JobDesc h{};                // host copy of the descriptor
   JobDesc* d = nullptr;       // device copy
   LoopState* ls = nullptr;    // device

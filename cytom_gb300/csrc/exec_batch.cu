@@ -509,7 +509,7 @@ static int batch_run(Ctx* const* ctxs, const int* job_ids, int count, cytom_run_
       int mode = 0;
       rc = pagerank_batch_prep(c, j, &b.pr, nb, &mode);
       if (rc) return rc;
-      for (int k = 0; k < kPrBins; ++k) b.nb[k] = nb[k];
+      for (int bi = 0; bi < kPrBins; ++bi) b.nb[bi] = nb[bi];
       hs[k].prmode = mode;
       const uint64_t units = (c->n + BU_PR_VERTS - 1) / BU_PR_VERTS;
       if (units > kMaxUnits) return set_err(c, CYTOM_ERR_RANGE, "graph too large for the batched executor");

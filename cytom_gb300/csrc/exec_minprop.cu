@@ -118,6 +118,7 @@ __global__ void __launch_bounds__(GATHER_T) gather_minprop_kernel(const JobDesc*
   const uint32_t* __restrict__ chunk_tile = sd->chunk_tile;
   const uint32_t* __restrict__ fa = jd->fa;
   const uint32_t* __restrict__ cur = jd->cur;
+  const bool async = jd->async != 0;
   uint32_t* next = jd->next;
   uint32_t* ch = jd->ch;
   const uint64_t E = sd->E, nchunks = sd->nchunks;
@@ -167,7 +168,7 @@ __global__ void __launch_bounds__(GATHER_T) gather_minprop_kernel(const JobDesc*
       if (adaptive && rows_cur[x] == 0) continue;
       const uint32_t u = (x << lvpt) | (evk[k] >> 16);
       if (adaptive && !((fa[u >> 5] >> (u & 31)) & 1u)) continue;
-      const uint32_t uv = cur[u];
+      const uint32_t uv = async ? __ldcg(next + u) : cur[u];
       if (uv == kInf) continue;
       const uint32_t cand = mp_cand<ALGO>(uv, wvk[k]);
       if (cand == kInf) continue;
@@ -446,10 +447,6 @@ int minprop_delete_check(Ctx* c, Job* j, const uint32_t* dsrc, const uint32_t* d
   }
   c->launches++;
   return cuda_err(c, cudaGetLastError(), "delete_tight");
-}
-
-static bool is_minprop(int algo) {
-  return algo == CYTOM_ALGO_BFS || algo == CYTOM_ALGO_CC || algo == CYTOM_ALGO_SSSP || algo == CYTOM_ALGO_SSWP;
 }
 
 int minprop_alloc(Ctx* c, Job* j) {

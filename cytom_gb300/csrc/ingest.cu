@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "radix.cuh"
 
 namespace cytom {
 
@@ -373,100 +374,14 @@ int exclusive_scan_u32(Ctx* c, const uint32_t* in, uint32_t* out, uint64_t n, ui
 // Upsweep: per-block digit histogram (digit-major). Scan. Downsweep: warps rank
 // items with __match_any_sync in input order and scatter.
 // --------------------------------------------------------------------------
-constexpr int RS_T = 256, RS_IPT = 16, RS_TILE = RS_T * RS_IPT, RS_WARPS = RS_T / 32;  // tile size shared with noalloc.cu
-
-__global__ void radix_upsweep_kernel(const uint64_t* __restrict__ keys, uint64_t n, int shift,
-                                     uint32_t* __restrict__ hist, uint32_t nb) {
-  __shared__ uint32_t cnt[256];
-  cnt[threadIdx.x] = 0;
-  __syncthreads();
-  uint64_t base = (uint64_t)blockIdx.x * RS_TILE;
-  uint32_t d_reg[RS_IPT];
-#pragma unroll
-  for (int k = 0; k < RS_IPT; ++k) {
-    uint64_t i = base + (uint64_t)k * RS_T + threadIdx.x;
-    d_reg[k] = (i < n) ? (uint32_t)((keys[i] >> shift) & 0xFF) : 256u;
-  }
-  // warp-aggregated counts (skewed digits would serialise per-key shared atomics)
-  const unsigned lane = threadIdx.x & 31;
-#pragma unroll
-  for (int k = 0; k < RS_IPT; ++k) {
-    const unsigned peers = __match_any_sync(0xFFFFFFFFu, d_reg[k]);
-    if (d_reg[k] < 256u && (__ffs(peers) - 1) == (int)lane) atomicAdd(&cnt[d_reg[k]], (uint32_t)__popc(peers));
-  }
-  __syncthreads();
-  hist[(uint64_t)threadIdx.x * nb + blockIdx.x] = cnt[threadIdx.x];
-}
-
-__global__ void __launch_bounds__(RS_T) radix_downsweep_kernel(const uint64_t* __restrict__ keys,
-                                                                const uint32_t* __restrict__ vals, uint64_t n,
-                                                                int shift, const uint32_t* __restrict__ offs,
-                                                                uint32_t nb, uint64_t* __restrict__ keys_out,
-                                                                uint32_t* __restrict__ vals_out) {
-  __shared__ uint32_t wcnt[RS_WARPS][256];
-  __shared__ uint32_t base_d[256];
-  const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const unsigned lt = (1u << lane) - 1u;
-  for (int d = threadIdx.x; d < RS_WARPS * 256; d += RS_T) (&wcnt[0][0])[d] = 0;
-  base_d[threadIdx.x] = offs[(uint64_t)threadIdx.x * nb + blockIdx.x];
-  __syncthreads();
-  const uint64_t wbase = (uint64_t)blockIdx.x * RS_TILE + (uint64_t)wid * (32 * RS_IPT);
-  // every key and value is loaded before any is used
-  uint64_t k_reg[RS_IPT];
-  uint32_t v_reg[RS_IPT];
-  uint32_t d_reg[RS_IPT];
-#pragma unroll
-  for (int k = 0; k < RS_IPT; ++k) {
-    uint64_t i = wbase + (uint64_t)k * 32 + lane;
-    k_reg[k] = (i < n) ? keys[i] : 0ULL;
-    v_reg[k] = (vals && i < n) ? vals[i] : 0u;
-    d_reg[k] = (i < n) ? (uint32_t)((k_reg[k] >> shift) & 0xFF) : 256u;
-  }
-  // phase 1: each key's rank among the warp's keys of its digit, in input order
-  uint32_t r_reg[RS_IPT];
-#pragma unroll
-  for (int k = 0; k < RS_IPT; ++k) {
-    const uint32_t d = d_reg[k];
-    const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
-    const int leader = __ffs(peers) - 1;
-    uint32_t old = 0;
-    if ((int)lane == leader && d < 256u) {
-      old = wcnt[wid][d];
-      wcnt[wid][d] = old + __popc(peers);
-    }
-    r_reg[k] = __shfl_sync(0xFFFFFFFFu, old, leader) + __popc(peers & lt);
-    __syncwarp();
-  }
-  __syncthreads();
-  // phase 2: exclusive prefix across warps per digit
-  {
-    uint32_t run = 0;
-    const int d = threadIdx.x;
-#pragma unroll
-    for (int w = 0; w < RS_WARPS; ++w) {
-      uint32_t t = wcnt[w][d];
-      wcnt[w][d] = run;
-      run += t;
-    }
-  }
-  __syncthreads();
-  // phase 3: scatter (stable: block offset + warp offset + rank)
-#pragma unroll
-  for (int k = 0; k < RS_IPT; ++k) {
-    const uint32_t d = d_reg[k];
-    if (d < 256u) {
-      const uint32_t pos = base_d[d] + wcnt[wid][d] + r_reg[k];
-      keys_out[pos] = k_reg[k];
-      if (vals) vals_out[pos] = v_reg[k];
-    }
-  }
-}
 
 int radix_sort_pairs(Ctx* c, uint64_t* keys, uint64_t* keys_alt, uint32_t* vals, uint32_t* vals_alt,
                      uint64_t n, int bits, bool* result_in_alt) {
   *result_in_alt = false;
   if (n <= 1 || bits <= 0) return CYTOM_OK;
-  uint64_t nb = (n + RS_TILE - 1) / RS_TILE;
+  const bool small = n < (1ULL << 24);
+  const uint64_t tile = (uint64_t)RS_T * (small ? RS_IPT_SMALL : RS_IPT_LARGE);
+  uint64_t nb = (n + tile - 1) / tile;
   uint32_t* hist = nullptr;
   cudaError_t e = cudaMallocAsync((void**)&hist, nb * 256 * 4 * 2, c->stream);
   if (e != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "radix histogram");
@@ -476,12 +391,17 @@ int radix_sort_pairs(Ctx* c, uint64_t* keys, uint64_t* keys_alt, uint32_t* vals,
   bool alt = false;
   for (int shift = 0; shift < bits; shift += 8) {
     int slot = prof_begin(c, KC_SORT);
-    radix_upsweep_kernel<<<(unsigned)nb, RS_T, 0, c->stream>>>(kin, n, shift, hist, (uint32_t)nb);
+    if (small) radix_upsweep_kernel<RS_IPT_SMALL><<<(unsigned)nb, RS_T, 0, c->stream>>>(kin, n, shift, hist, (uint32_t)nb);
+    else radix_upsweep_kernel<RS_IPT_LARGE><<<(unsigned)nb, RS_T, 0, c->stream>>>(kin, n, shift, hist, (uint32_t)nb);
     c->launches++;
     int rc = exclusive_scan_u32(c, hist, offs, nb * 256, nullptr);
     if (rc) return rc;
-    radix_downsweep_kernel<<<(unsigned)nb, RS_T, 0, c->stream>>>(kin, vin, n, shift, offs,
-                                                                 (uint32_t)nb, kout, vout);
+    if (small)
+      radix_downsweep_kernel<RS_IPT_SMALL><<<(unsigned)nb, RS_T, 0, c->stream>>>(kin, vin, n, shift, offs, (uint32_t)nb,
+                                                                               kout, vout);
+    else
+      radix_downsweep_kernel<RS_IPT_LARGE><<<(unsigned)nb, RS_T, 0, c->stream>>>(kin, vin, n, shift, offs, (uint32_t)nb,
+                                                                               kout, vout);
     c->launches++;
     prof_end(c, slot, (double)n * (vals ? 12.0 : 8.0) * 3.0);
     e = cudaGetLastError();

@@ -63,6 +63,16 @@ __device__ __forceinline__ uint32_t mp_cand(uint32_t c, uint32_t w) {
   return max(c, ~w);
 }
 
+// Source value of a gather. The asynchronous programs (examples/bfs-async.cc,
+// cc-async.cc: ASYNC = true) pull from next[src], which other blocks lower during the
+// round (algorithm-executor.h:303-312); read through L2, a value is either the one at
+// the round's start or a lower one, and both are valid bounds.
+template <bool PERSIST>
+__device__ __forceinline__ uint32_t ld_src(const JobDesc* __restrict__ jd, bool async, uint64_t u) {
+  if (async) return __ldcg(jd->next + u);
+  return ld_state<PERSIST>(jd->cur + u);
+}
+
 __device__ __forceinline__ unsigned long long row_edges(const StoreDesc* sd, uint64_t x) {
   return sd->tile_ptr[(x + 1) << sd->lT] - sd->tile_ptr[x << sd->lT];
 }
@@ -228,7 +238,7 @@ __device__ __forceinline__ void dense_stage(const JobDesc* __restrict__ jd, cons
   const uint32_t* __restrict__ chunk_tile = sd->chunk_tile;
   const unsigned long long* __restrict__ tile_ptr = sd->tile_ptr;
   const uint32_t* fa = jd->fa;
-  const uint32_t* cur = jd->cur;
+  const bool async = jd->async != 0;
   uint32_t* next = jd->next;
   uint32_t* ch = jd->ch;
   const uint64_t E = sd->E, nchunks = sd->nchunks;
@@ -331,7 +341,7 @@ __device__ __forceinline__ void dense_stage(const JobDesc* __restrict__ jd, cons
   if (amask) {
     uint32_t cand[EPT], vv[EPT];
 #pragma unroll
-    for (int idx = 0; idx < EPT; ++idx) cand[idx] = ((amask >> idx) & 1u) ? ld_state<PERSIST>(cur + uu[idx]) : kInf;
+    for (int idx = 0; idx < EPT; ++idx) cand[idx] = ((amask >> idx) & 1u) ? ld_src<PERSIST>(jd, async, uu[idx]) : kInf;
     if (single_tile) {
       const uint32_t yb = (tf & ymask) << lvpt;
 #pragma unroll
@@ -442,6 +452,7 @@ __device__ __forceinline__ void sp_batch(const JobDesc* __restrict__ jd, const S
                                          const uint32_t (&bits)[SP_ILP], const unsigned long long (&pos)[SP_ILP],
                                          uint32_t valid) {
   const uint32_t lvpt = sd->lvpt;
+  const bool async = jd->async != 0;
   uint32_t pk[SP_ILP], wv[SP_ILP], cand[SP_ILP], nv[SP_ILP];
 #pragma unroll
   for (int k = 0; k < SP_ILP; ++k) {
@@ -452,7 +463,7 @@ __device__ __forceinline__ void sp_batch(const JobDesc* __restrict__ jd, const S
   for (int k = 0; k < SP_ILP; ++k) {
     const uint32_t sl = pk[k] >> 16;
     const bool act = ((valid >> k) & 1u) && ((bits[k] >> (sl & 31)) & 1u);
-    cand[k] = act ? ld_state<PERSIST>(jd->cur + ((xs[k] << lvpt) | sl)) : kInf;
+    cand[k] = act ? ld_src<PERSIST>(jd, async, (xs[k] << lvpt) | sl) : kInf;
   }
 #pragma unroll
   for (int k = 0; k < SP_ILP; ++k)

@@ -22,6 +22,7 @@
 #include <mutex>
 
 #include "../../include/cytom_gpu.h"
+#include "radix.cuh"
 
 namespace cytom {
 
@@ -29,17 +30,13 @@ namespace cytom {
 __global__ void scan_reduce_kernel(const uint32_t* __restrict__ in, uint64_t n, uint32_t* __restrict__ sums);
 __global__ void scan_down_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, uint64_t n,
                                  const uint32_t* __restrict__ offs, uint32_t* total_out);
-__global__ void radix_upsweep_kernel(const uint64_t* __restrict__ keys, uint64_t n, int shift,
-                                     uint32_t* __restrict__ hist, uint32_t nb);
-__global__ void radix_downsweep_kernel(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals,
-                                       uint64_t n, int shift, const uint32_t* __restrict__ offs, uint32_t nb,
-                                       uint64_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out);
 
 namespace noalloc {
 
 constexpr uint64_t kMax = CYTOM_NOALLOC_MAX_EDGES;
-constexpr uint64_t kTile = 4096;                 // items per sort / scan block
-constexpr uint64_t kBlocks = kMax / kTile;       // 64
+constexpr uint64_t kTile = 4096;                 // items per scan block
+constexpr uint64_t kSortTile = (uint64_t)RS_T * RS_IPT_SMALL;
+constexpr uint64_t kBlocks = kMax / kSortTile;   // sort tiles
 // scratch layout (byte offsets, 256-aligned)
 constexpr size_t kKeys0 = 0;
 constexpr size_t kKeys1 = kKeys0 + kMax * 8;
@@ -203,13 +200,13 @@ extern "C" int cytom_tile_batch_noalloc(const uint32_t* src, const uint32_t* tgt
     noalloc::keys_kernel<<<grid, 256, 0, s>>>(src, tgt, w, count, n, lvpt, lT, k0, w0, &flags[0]);
     // LSD radix sort of the composite keys (stable), weights ride along
     const int bits = (int)(2 * (lvpt + lT));
-    const uint64_t nb = (count + kTile - 1) / kTile;
+    const uint64_t nb = (count + kSortTile - 1) / kSortTile;
     uint64_t *kin = k0, *kout = k1;
     uint32_t *vin = w0, *vout = w1;
     for (int shift = 0; shift < bits; shift += 8) {
-      radix_upsweep_kernel<<<(unsigned)nb, 256, 0, s>>>(kin, count, shift, hist, (uint32_t)nb);
+      radix_upsweep_kernel<RS_IPT_SMALL><<<(unsigned)nb, RS_T, 0, s>>>(kin, count, shift, hist, (uint32_t)nb);
       noalloc::scan(hist, offs, nb * 256, sums, nullptr, s);
-      radix_downsweep_kernel<<<(unsigned)nb, 256, 0, s>>>(kin, vin, count, shift, offs, (uint32_t)nb, kout, vout);
+      radix_downsweep_kernel<RS_IPT_SMALL><<<(unsigned)nb, RS_T, 0, s>>>(kin, vin, count, shift, offs, (uint32_t)nb, kout, vout);
       std::swap(kin, kout);
       std::swap(vin, vout);
     }

@@ -368,6 +368,17 @@ class CC(Program):
     ALGO = L.ALGO_CC
 
 
+class BFSAsync(Program):
+    """examples/bfs-async.cc: BFS whose pull reads the freshest source values (next);
+    the same levels as BFS, usually in fewer rounds."""
+    ALGO = L.ALGO_BFS_ASYNC
+
+
+class CCAsync(Program):
+    """examples/cc-async.cc: CC whose pull reads the freshest source values (next)."""
+    ALGO = L.ALGO_CC_ASYNC
+
+
 class SSSP(Program):
     """examples/sssp.cc over uint32 weights: distances from start_vertex."""
     ALGO = L.ALGO_SSSP

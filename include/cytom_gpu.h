@@ -66,6 +66,13 @@ extern "C" {
  * uint32 weights (a CYTOM_WEIGHT_U32 store; the reference's float values are exact for
  * them). */
 #define CYTOM_ALGO_SSWP 6
+/* Asynchronous BFS and CC (examples/bfs-async.cc, cc-async.cc: ASYNC = true): the pull
+ * reads the freshest value of every source, next[src], instead of current[src]
+ * (src/include/core/algorithm-executor.h:303-312, 332-340), so a value lowered early in a
+ * round can travel further in the same round. Same fixed points as BFS and CC; round and
+ * processed-edge counts depend on scheduling, as in the reference. */
+#define CYTOM_ALGO_BFS_ASYNC 7
+#define CYTOM_ALGO_CC_ASYNC 8
 
 /* Context configuration: the subset of ConfigContext (src/include/util/config.h:529-567)
  * and its command-line flags (src/include/core/jobs.h:176-216) that the hot path uses. */

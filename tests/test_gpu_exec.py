@@ -265,3 +265,38 @@ def test_autotune_report(cg, orc):
         st.compact()
         ref, _ = st.run_minprop(2, start=0, max_iter=1000)
         assert np.array_equal(p.result(), ref)
+
+
+@pytest.mark.parametrize("name,algo", [("BFSAsync", 0), ("CCAsync", 1)])
+@pytest.mark.parametrize("scale,vpt", [(12, 256), (16, 4096), (18, 65536)])
+def test_async_programs_reach_the_fixed_point(cg, orc, name, algo, scale, vpt):
+    # examples/bfs-async.cc / cc-async.cc: the pull reads next[src]; the values equal the
+    # synchronous fixed point, in no more rounds than the synchronous program, fresh, after
+    # further batches, and in the batched executor
+    n = 1 << scale
+    s, t = orc.rmat(scale, 0, 8 << scale, scale + 3)
+    w = orc.edge_weights(s, t, 1)
+    st = orc.Store(n, vpt, weighted=True)
+    with cg.Engine(n, vpt, weight_type=cg.WEIGHT_U32) as eng:
+        eng.insert_edges(s, t, w)
+        st.insert(s, t, w)
+        st.compact()
+        pa = getattr(cg, name)(eng, start_vertex=0, max_iterations=1000)
+        pb = getattr(cg, name)(eng, start_vertex=0, max_iterations=1000)
+        sa = pa.execute_algorithm()
+        ref, rinfo = st.run_minprop(algo, start=0, max_iter=1000)
+        assert np.array_equal(pa.result(), ref)
+        assert sa["converged"] == 1 and 1 <= sa["iterations"] <= rinfo["iterations"]
+        cg.run_batch([pb])
+        assert np.array_equal(pb.result(), ref)
+        for b in range(2):
+            s2, t2 = orc.rmat(scale, (8 << scale) + b * n, n, scale + 3)
+            w2 = orc.edge_weights(s2, t2, 1)
+            eng.insert_edges(s2, t2, w2)
+            st.insert(s2, t2, w2)
+            st.compact()
+            pa.execute_algorithm()
+            cg.run_batch([pb])
+            ref, _ = st.run_minprop(algo, start=0, max_iter=1000)
+            assert np.array_equal(pa.result(), ref), b
+            assert np.array_equal(pb.result(), ref), b

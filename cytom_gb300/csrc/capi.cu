@@ -214,7 +214,9 @@ static bool autotune_due(Ctx* c) {
   return env && !c->profiling && c->tune_E == 0 && c->E >= (1ULL << 20);
 }
 
-int job_run(Ctx* c, Job* j, cytom_run_stats* st) {
+// Everything a run needs before its loop: pending edges merged, the source directory,
+// the job's sparse queue, the one-time shape tuning, and the initial state of a fresh job.
+static int job_prepare(Ctx* c, Job* j) {
   int rc = compact(c);
   if (rc) return rc;
   if (is_minprop(j->algo)) {
@@ -228,16 +230,12 @@ int job_run(Ctx* c, Job* j, cytom_run_stats* st) {
     if (rc) return rc;
     j->fresh = false;
   }
-  cudaEventRecord(c->run_a, c->stream);
-  rc = is_minprop(j->algo) ? minprop_run(c, j) : pagerank_run(c, j);
-  if (rc) return rc;
-  cudaEventRecord(c->run_b, c->stream);
-  LoopState ls;
-  cudaError_t e = cudaMemcpyAsync(&ls, j->ls, sizeof(LoopState), cudaMemcpyDeviceToHost, c->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-  if (e != cudaSuccess) return cuda_err(c, e, "run");
-  rc = prof_flush(c);
-  if (rc) return rc;
+  return CYTOM_OK;
+}
+
+// Statistics of a finished run from its loop state; ev_a / ev_b bracket its launches.
+static int job_finish(Ctx* c, Job* j, const LoopState& ls, cudaEvent_t ev_a, cudaEvent_t ev_b,
+                      cytom_run_stats* st) {
   if (ls.err) return set_err(c, CYTOM_ERR_TIMEOUT, "a bounded device wait gave up");
   if (j->last_run_graph) c->launches += 4ULL * ls.iter;  // per round: two gathers, chunk pass, apply
   if (st) {
@@ -249,8 +247,85 @@ int job_run(Ctx* c, Job* j, cytom_run_stats* st) {
     st->converged = (ls.cont == 0 && ls.iter < ls.max_iter) ? 1 : (ls.cont == 0 ? 1 : 0);
     st->residual = ls.resid_final;
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, c->run_a, c->run_b);
+    cudaEventElapsedTime(&ms, ev_a, ev_b);
     st->elapsed_ms = ms;
+  }
+  return CYTOM_OK;
+}
+
+int job_run(Ctx* c, Job* j, cytom_run_stats* st) {
+  int rc = job_prepare(c, j);
+  if (rc) return rc;
+  cudaEventRecord(c->run_a, c->stream);
+  rc = is_minprop(j->algo) ? minprop_run(c, j) : pagerank_run(c, j);
+  if (rc) return rc;
+  cudaEventRecord(c->run_b, c->stream);
+  LoopState ls;
+  cudaError_t e = cudaMemcpyAsync(&ls, j->ls, sizeof(LoopState), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "run");
+  rc = prof_flush(c);
+  if (rc) return rc;
+  return job_finish(c, j, ls, c->run_a, c->run_b, st);
+}
+
+// Several jobs of one context: BFS / CC / SSSP / SSWP jobs are independent once the
+// snapshot is prepared, as the reference's jobs are (one thread per job), so after a
+// shared preparation each job's captured loop is launched on its own stream and they
+// overlap (the small, latency-bound rounds of one job fill the GPU around another's).
+// The caller's stream waits for all of them. Other jobs, and profiling runs, run in turn.
+int job_run_many(Ctx* c, Job** jobs, int count, cytom_run_stats* stats) {
+  bool conc = count > 1 && !c->profiling;
+  for (int k = 0; k < count && conc; ++k) conc = is_minprop(jobs[k]->algo);
+  if (!conc) {
+    for (int k = 0; k < count; ++k) {
+      int rc = job_run(c, jobs[k], stats ? stats + k : nullptr);
+      if (rc) return rc;
+    }
+    return CYTOM_OK;
+  }
+  for (int k = 0; k < count; ++k) {
+    int rc = job_prepare(c, jobs[k]);
+    if (rc) return rc;
+  }
+  while ((int)c->conc.size() < count) {
+    ConcSlot slot{};
+    cudaError_t e = cudaStreamCreateWithFlags(&slot.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&slot.a);
+    if (e == cudaSuccess) e = cudaEventCreate(&slot.b);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&slot.done, cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_err(c, e, "job streams");
+    c->conc.push_back(slot);
+  }
+  if (!c->fork_ev && cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess)
+    return set_err(c, CYTOM_ERR_CUDA, "fork event");
+  cudaEventRecord(c->fork_ev, c->stream);
+  cudaStream_t home = c->stream;
+  int rc = CYTOM_OK;
+  for (int k = 0; k < count && !rc; ++k) {
+    ConcSlot& sl = c->conc[k];
+    cudaStreamWaitEvent(sl.stream, c->fork_ev, 0);
+    cudaEventRecord(sl.a, sl.stream);
+    c->stream = sl.stream;  // the job's launches go to its own stream
+    rc = minprop_run(c, jobs[k]);
+    c->stream = home;
+    cudaEventRecord(sl.b, sl.stream);
+    cudaEventRecord(sl.done, sl.stream);
+    cudaStreamWaitEvent(home, sl.done, 0);
+  }
+  if (rc) {
+    cudaStreamSynchronize(home);
+    return rc;
+  }
+  std::vector<LoopState> ls(count);
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < count && e == cudaSuccess; ++k)
+    e = cudaMemcpyAsync(&ls[k], jobs[k]->ls, sizeof(LoopState), cudaMemcpyDeviceToHost, home);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(home);
+  if (e != cudaSuccess) return cuda_err(c, e, "run");
+  for (int k = 0; k < count; ++k) {
+    rc = job_finish(c, jobs[k], ls[k], c->conc[k].a, c->conc[k].b, stats ? stats + k : nullptr);
+    if (rc) return rc;
   }
   return CYTOM_OK;
 }
@@ -406,6 +481,14 @@ int cytom_destroy(cytom_ctx* ctx) {
   for (auto ev : c->ev_pool) cudaEventDestroy(ev);
   if (c->run_a) cudaEventDestroy(c->run_a);
   if (c->run_b) cudaEventDestroy(c->run_b);
+  for (auto& sl : c->conc) {
+    cudaStreamSynchronize(sl.stream);
+    cudaEventDestroy(sl.a);
+    cudaEventDestroy(sl.b);
+    cudaEventDestroy(sl.done);
+    cudaStreamDestroy(sl.stream);
+  }
+  if (c->fork_ev) cudaEventDestroy(c->fork_ev);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return CYTOM_OK;
@@ -681,12 +764,15 @@ int cytom_run(cytom_ctx* ctx, int job_id, cytom_run_stats* stats) {
 
 int cytom_run_many(cytom_ctx* ctx, const int* job_ids, int count, cytom_run_stats* stats) {
   Ctx* c = (Ctx*)ctx;
-  if (!c || (count > 0 && !job_ids)) return CYTOM_ERR_INVAL;
+  if (!c || count < 0 || (count > 0 && !job_ids)) return CYTOM_ERR_INVAL;
+  std::vector<Job*> jobs(count);
   for (int k = 0; k < count; ++k) {
-    int rc = cytom_run(ctx, job_ids[k], stats ? stats + k : nullptr);
-    if (rc) return rc;
+    jobs[k] = get_job(c, job_ids[k]);
+    if (!jobs[k]) return CYTOM_ERR_INVAL;
+    for (int i = 0; i < k; ++i)
+      if (jobs[i] == jobs[k]) return set_err(c, CYTOM_ERR_INVAL, "a job listed twice");
   }
-  return CYTOM_OK;
+  return job_run_many(c, jobs.data(), count, stats);
 }
 
 int cytom_get_result(cytom_ctx* ctx, int job_id, void* out, int where) {

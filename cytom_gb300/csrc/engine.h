@@ -124,6 +124,12 @@ struct Job {
   void* ext = nullptr;          // per-algorithm state (PageRank family)
 };
 
+// A stream of its own for one job of a concurrent run, and the events around its launches.
+struct ConcSlot {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t a = nullptr, b = nullptr, done = nullptr;
+};
+
 struct Ctx {
   cytom_config cfg{};
   std::string err;
@@ -142,6 +148,8 @@ struct Ctx {
   uint64_t cap = 0, chunk_cap = 0;
   uint64_t E = 0;  // exact after compaction
   uint64_t version = 0;  // bumped by every compaction that merged edges
+  std::vector<ConcSlot> conc;      // concurrent runs: one stream per job
+  cudaEvent_t fork_ev = nullptr;
   uint32_t* dir = nullptr;  // source directory (sparse rounds)
   uint64_t dir_entries = 0;
   uint64_t dir_version = ~0ULL;

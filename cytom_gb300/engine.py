@@ -221,6 +221,18 @@ class Engine:
         self._check(self.lib.cytom_read_edges(self.ctx, str(path).encode(), batch, C.byref(cnt)))
         return cnt.value
 
+    def run_many(self, programs) -> list[dict]:
+        """Runs programs of this engine together (cytom_run_many): BFS / CC / SSSP / SSWP
+        jobs run concurrently, each on a stream of its own; returns their statistics."""
+        programs = list(programs)
+        if not programs:
+            return []
+        n = len(programs)
+        ids = (C.c_int * n)(*[p.job for p in programs])
+        stats = (L.RunStats * n)()
+        self._check(self.lib.cytom_run_many(self.ctx, ids, n, stats))
+        return [stats[k].as_dict() for k in range(n)]
+
     def autotune(self) -> dict:
         """Times the streaming-gather shapes on the current graph and keeps the fastest."""
         rep = L.TuneReport()

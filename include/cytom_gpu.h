@@ -206,7 +206,12 @@ typedef struct cytom_run_stats {
  * for one job: compacts pending edges, then iterates pull -> apply -> swap until no
  * vertex changes or max_iterations. */
 int cytom_run(cytom_ctx* ctx, int job_id, cytom_run_stats* stats);
-/* Runs several jobs of this context back to back. */
+/* Runs several jobs of this context (each listed once), as the reference runs its jobs
+ * side by side (one thread per job, src/include/core/jobs.h:79-83). After one shared
+ * preparation (compaction, directory), BFS / CC / SSSP / SSWP jobs run concurrently, each
+ * on a stream of its own that waits for the context's stream; the context's stream then
+ * waits for all of them. Lists with other jobs run one after another. stats: `count`
+ * entries or NULL. */
 int cytom_run_many(cytom_ctx* ctx, const int* job_ids, int count, cytom_run_stats* stats);
 
 /* Batched persistent executor. Runs `count` jobs -- job_ids[k] of context ctxs[k]; the

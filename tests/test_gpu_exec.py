@@ -300,3 +300,40 @@ def test_async_programs_reach_the_fixed_point(cg, orc, name, algo, scale, vpt):
             ref, _ = st.run_minprop(algo, start=0, max_iter=1000)
             assert np.array_equal(pa.result(), ref), b
             assert np.array_equal(pb.result(), ref), b
+
+
+def test_run_many_concurrent_jobs(cg, orc):
+    # cytom_run_many: BFS / CC / SSSP / SSWP (and the asynchronous programs) of one context
+    # run side by side on their own streams; every batch ends at the oracle's fixed points,
+    # with the same round and processed-edge counts as one-at-a-time runs
+    scale, vpt = 14, 2048
+    n = 1 << scale
+    st = orc.Store(n, vpt, weighted=True)
+    with cg.Engine(n, vpt, weight_type=cg.WEIGHT_U32) as ea, cg.Engine(n, vpt, weight_type=cg.WEIGHT_U32) as eb:
+        mk = lambda e: [cg.BFS(e, start_vertex=0, max_iterations=1000), cg.CC(e, max_iterations=1000),
+                        cg.SSSP(e, start_vertex=0, max_iterations=1000), cg.SSWP(e, start_vertex=0, max_iterations=1000),
+                        cg.BFSAsync(e, start_vertex=0, max_iterations=1000)]
+        pa, pb = mk(ea), mk(eb)
+        algos = [0, 1, 2, 3, 0]
+        for b in range(4):
+            s, t = orc.rmat(scale, b * 4 * n, 4 * n, 17)
+            w = orc.edge_weights(s, t, 18)
+            for e in (ea, eb):
+                e.insert_edges(s.copy(), t.copy(), w.copy())
+            st.insert(s, t, w)
+            st.compact()
+            sa = ea.run_many(pa)
+            sb = [p.execute_algorithm() for p in pb]
+            for k, algo in enumerate(algos):
+                ref, _ = st.run_minprop(algo, start=0, max_iter=1000)
+                assert np.array_equal(pa[k].result(), ref), (b, k)
+                assert np.array_equal(pb[k].result(), ref), (b, k)
+                if k < 4:  # the synchronous programs: identical rounds and counts
+                    assert sa[k]["iterations"] == sb[k]["iterations"], (b, k)
+                    assert sa[k]["count_edges"] == sb[k]["count_edges"], (b, k)
+        # a list with a PageRank job runs one after another; a job listed twice is an error
+        pr = cg.PageRank(ea, max_iterations=100, tolerance=1e-9)
+        out = ea.run_many([pa[0], pr])
+        assert len(out) == 2 and out[1]["iterations"] > 0
+        with pytest.raises(cg.CytomError):
+            ea.run_many([pa[0], pa[0]])

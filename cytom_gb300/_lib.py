@@ -123,6 +123,8 @@ SIGNATURES = [
     ("cytom_job_reset", C.c_int, [C.c_void_p, C.c_int]),
     ("cytom_run", C.c_int, [C.c_void_p, C.c_int, C.POINTER(RunStats)]),
     ("cytom_run_many", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.c_int, C.POINTER(RunStats)]),
+    ("cytom_run_many_async", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.c_int]),
+    ("cytom_run_many_wait", C.c_int, [C.c_void_p, C.POINTER(RunStats)]),
     ("cytom_run_batch", C.c_int, [C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.c_int, C.POINTER(RunStats)]),
     ("cytom_batch_units", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
     ("cytom_job_set_teleport", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),

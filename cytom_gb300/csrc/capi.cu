@@ -16,6 +16,7 @@ namespace cytom {
 
 int minprop_alloc(Ctx* c, Job* j);
 int minprop_init(Ctx* c, Job* j);
+int minprop_seed_keys(Ctx* c, Job* j, const uint64_t* K, const uint32_t* W, uint64_t count);
 int minprop_seed(Ctx* c, Job* j, const uint32_t* src, const uint32_t* tgt, const uint32_t* w,
                  uint64_t count);
 int minprop_run(Ctx* c, Job* j);
@@ -203,6 +204,12 @@ int job_seed(Ctx* c, Job* j, const uint32_t* src, const uint32_t* tgt, const uin
                              : pagerank_seed(c, j, src, tgt, w, count);
 }
 
+// edgeChanged(INSERT) for the edges merged by a compaction (sorted keys and weights).
+int job_seed_keys(Ctx* c, Job* j, const uint64_t* K, const uint32_t* W, uint64_t count) {
+  return is_minprop(j->algo) ? minprop_seed_keys(c, j, K, W, count)
+                             : pagerank_seed(c, j, nullptr, nullptr, nullptr, count);
+}
+
 // The streaming gather is tuned once per context, on the first run at >= 2^20 edges
 // (cytom_autotune re-tunes on demand; CYTOM_AUTOTUNE=0 keeps the default shapes).
 static bool autotune_due(Ctx* c) {
@@ -269,21 +276,28 @@ int job_run(Ctx* c, Job* j, cytom_run_stats* st) {
   return job_finish(c, j, ls, c->run_a, c->run_b, st);
 }
 
+void join_runs(Ctx* c) {
+  if (!c->runs_unjoined) return;
+  for (size_t k = 0; k < c->async_jobs.size(); ++k) cudaStreamWaitEvent(c->stream, c->conc[k].done, 0);
+  c->runs_unjoined = false;
+}
+
 // Several jobs of one context: BFS / CC / SSSP / SSWP jobs are independent once the
 // snapshot is prepared, as the reference's jobs are (one thread per job), so after a
 // shared preparation each job's captured loop is launched on its own stream and they
 // overlap (the small, latency-bound rounds of one job fill the GPU around another's).
 // The caller's stream waits for all of them. Other jobs, and profiling runs, run in turn.
-int job_run_many(Ctx* c, Job** jobs, int count, cytom_run_stats* stats) {
-  bool conc = count > 1 && !c->profiling;
-  for (int k = 0; k < count && conc; ++k) conc = is_minprop(jobs[k]->algo);
-  if (!conc) {
-    for (int k = 0; k < count; ++k) {
-      int rc = job_run(c, jobs[k], stats ? stats + k : nullptr);
-      if (rc) return rc;
-    }
-    return CYTOM_OK;
-  }
+static int collect_runs(Ctx* c, cytom_run_stats* stats);
+
+void settle_runs(Ctx* c) {
+  if (!c->async_jobs.empty()) collect_runs(c, nullptr);
+  c->sync_jobs.clear();
+  c->sync_stats.clear();
+}
+
+// Launches the jobs' loops on their streams after the shared preparation; the context's
+// stream is not made to wait for them (join_runs does that).
+static int launch_many(Ctx* c, Job** jobs, int count) {
   for (int k = 0; k < count; ++k) {
     int rc = job_prepare(c, jobs[k]);
     if (rc) return rc;
@@ -302,6 +316,7 @@ int job_run_many(Ctx* c, Job** jobs, int count, cytom_run_stats* stats) {
   cudaEventRecord(c->fork_ev, c->stream);
   cudaStream_t home = c->stream;
   int rc = CYTOM_OK;
+  c->async_jobs.clear();
   for (int k = 0; k < count && !rc; ++k) {
     ConcSlot& sl = c->conc[k];
     cudaStreamWaitEvent(sl.stream, c->fork_ev, 0);
@@ -311,23 +326,52 @@ int job_run_many(Ctx* c, Job** jobs, int count, cytom_run_stats* stats) {
     c->stream = home;
     cudaEventRecord(sl.b, sl.stream);
     cudaEventRecord(sl.done, sl.stream);
-    cudaStreamWaitEvent(home, sl.done, 0);
+    c->async_jobs.push_back(jobs[k]);
   }
+  c->runs_unjoined = true;
   if (rc) {
+    join_runs(c);
     cudaStreamSynchronize(home);
-    return rc;
+    c->async_jobs.clear();
   }
+  return rc;
+}
+
+// Joins the last asynchronous launch and returns its statistics (stats: one entry per
+// job of that launch, or NULL).
+static int collect_runs(Ctx* c, cytom_run_stats* stats) {
+  join_runs(c);
+  const int count = (int)c->async_jobs.size();
   std::vector<LoopState> ls(count);
   cudaError_t e = cudaSuccess;
   for (int k = 0; k < count && e == cudaSuccess; ++k)
-    e = cudaMemcpyAsync(&ls[k], jobs[k]->ls, sizeof(LoopState), cudaMemcpyDeviceToHost, home);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(home);
+    e = cudaMemcpyAsync(&ls[k], c->async_jobs[k]->ls, sizeof(LoopState), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_err(c, e, "run");
-  for (int k = 0; k < count; ++k) {
-    rc = job_finish(c, jobs[k], ls[k], c->conc[k].a, c->conc[k].b, stats ? stats + k : nullptr);
-    if (rc) return rc;
+  int rc = CYTOM_OK;
+  for (int k = 0; k < count && !rc; ++k)
+    rc = job_finish(c, c->async_jobs[k], ls[k], c->conc[k].a, c->conc[k].b, stats ? stats + k : nullptr);
+  c->async_jobs.clear();
+  return rc;
+}
+
+static bool runs_concurrently(const Ctx* c, Job** jobs, int count) {
+  bool conc = count > 1 && !c->profiling;
+  for (int k = 0; k < count && conc; ++k) conc = is_minprop(jobs[k]->algo);
+  return conc;
+}
+
+int job_run_many(Ctx* c, Job** jobs, int count, cytom_run_stats* stats) {
+  if (!runs_concurrently(c, jobs, count)) {
+    for (int k = 0; k < count; ++k) {
+      int rc = job_run(c, jobs[k], stats ? stats + k : nullptr);
+      if (rc) return rc;
+    }
+    return CYTOM_OK;
   }
-  return CYTOM_OK;
+  int rc = launch_many(c, jobs, count);
+  if (rc) return rc;
+  return collect_runs(c, stats);
 }
 
 }  // namespace cytom
@@ -458,6 +502,7 @@ int cytom_create(const cytom_config* cfg, cytom_ctx** out) {
 
 int cytom_destroy(cytom_ctx* ctx) {
   Ctx* c = (Ctx*)ctx;
+  if (c) join_runs(c);
   if (!c) return CYTOM_ERR_INVAL;
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (Job* j : c->jobs)
@@ -468,8 +513,8 @@ int cytom_destroy(cytom_ctx* ctx) {
   batch_free(c);
   pagerank_ctx_free(c);
   edge_log_close(c);
-  void* ptrs[] = {c->dir, c->edges, c->wts, c->edges_alt, c->wts_alt, c->tile_ptr, c->tile_ptr_alt,
-                  c->chunk_tile, c->app_keys, c->app_keys_alt, c->app_w, c->app_w_alt,
+  void* ptrs[] = {c->dir, c->dir_alt, c->edges, c->wts, c->edges_alt, c->wts_alt, c->tile_ptr, c->tile_ptr_alt,
+                  c->chunk_tile, c->chunk_tile_alt, c->app_keys, c->app_keys_alt, c->app_w, c->app_w_alt,
                   c->out_deg, c->in_deg, c->dsd, c->scratch, c->d_flag};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -662,6 +707,7 @@ int cytom_count_edges(const cytom_ctx* ctx, uint64_t* compacted, uint64_t* pendi
 int cytom_get_tiles(cytom_ctx* ctx, uint64_t* tile_ptr, uint32_t* edges, uint32_t* weights,
                     uint8_t* compact_flags) {
   Ctx* c = (Ctx*)ctx;
+  if (c) join_runs(c);
   if (!c) return CYTOM_ERR_INVAL;
   cudaError_t e = cudaSuccess;
   if (tile_ptr)
@@ -687,6 +733,7 @@ int cytom_get_tiles(cytom_ctx* ctx, uint64_t* tile_ptr, uint32_t* edges, uint32_
 
 int cytom_get_degrees(cytom_ctx* ctx, uint32_t* out_degree, uint32_t* in_degree) {
   Ctx* c = (Ctx*)ctx;
+  if (c) join_runs(c);
   if (!c) return CYTOM_ERR_INVAL;
   if (out_degree) cudaMemcpyAsync(out_degree, c->out_deg, c->n * 4, cudaMemcpyDeviceToHost, c->stream);
   if (in_degree) cudaMemcpyAsync(in_degree, c->in_deg, c->n * 4, cudaMemcpyDeviceToHost, c->stream);
@@ -738,6 +785,7 @@ static Job* get_job(Ctx* c, int id) {
 
 int cytom_job_destroy(cytom_ctx* ctx, int job_id) {
   Ctx* c = (Ctx*)ctx;
+  if (c) settle_runs(c);
   Job* j = get_job(c, job_id);
   if (!j) return CYTOM_ERR_INVAL;
   cudaStreamSynchronize(c->stream);
@@ -749,6 +797,7 @@ int cytom_job_destroy(cytom_ctx* ctx, int job_id) {
 
 int cytom_job_reset(cytom_ctx* ctx, int job_id) {
   Ctx* c = (Ctx*)ctx;
+  if (c) settle_runs(c);
   Job* j = get_job(c, job_id);
   if (!j) return CYTOM_ERR_INVAL;
   j->fresh = true;
@@ -757,26 +806,72 @@ int cytom_job_reset(cytom_ctx* ctx, int job_id) {
 
 int cytom_run(cytom_ctx* ctx, int job_id, cytom_run_stats* stats) {
   Ctx* c = (Ctx*)ctx;
+  if (c) settle_runs(c);
   Job* j = get_job(c, job_id);
   if (!j) return CYTOM_ERR_INVAL;
   return job_run(c, j, stats);
 }
 
+static int job_list(Ctx* c, const int* job_ids, int count, std::vector<Job*>* jobs) {
+  if (count < 0 || (count > 0 && !job_ids)) return CYTOM_ERR_INVAL;
+  jobs->resize(count);
+  for (int k = 0; k < count; ++k) {
+    (*jobs)[k] = get_job(c, job_ids[k]);
+    if (!(*jobs)[k]) return CYTOM_ERR_INVAL;
+    for (int i = 0; i < k; ++i)
+      if ((*jobs)[i] == (*jobs)[k]) return set_err(c, CYTOM_ERR_INVAL, "a job listed twice");
+  }
+  return CYTOM_OK;
+}
+
 int cytom_run_many(cytom_ctx* ctx, const int* job_ids, int count, cytom_run_stats* stats) {
   Ctx* c = (Ctx*)ctx;
-  if (!c || count < 0 || (count > 0 && !job_ids)) return CYTOM_ERR_INVAL;
-  std::vector<Job*> jobs(count);
-  for (int k = 0; k < count; ++k) {
-    jobs[k] = get_job(c, job_ids[k]);
-    if (!jobs[k]) return CYTOM_ERR_INVAL;
-    for (int i = 0; i < k; ++i)
-      if (jobs[i] == jobs[k]) return set_err(c, CYTOM_ERR_INVAL, "a job listed twice");
+  if (!c) return CYTOM_ERR_INVAL;
+  std::vector<Job*> jobs;
+  int rc = job_list(c, job_ids, count, &jobs);
+  if (rc) return rc;
+  if (!c->async_jobs.empty()) {
+    rc = collect_runs(c, nullptr);
+    if (rc) return rc;
   }
   return job_run_many(c, jobs.data(), count, stats);
 }
 
+int cytom_run_many_async(cytom_ctx* ctx, const int* job_ids, int count) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c) return CYTOM_ERR_INVAL;
+  std::vector<Job*> jobs;
+  int rc = job_list(c, job_ids, count, &jobs);
+  if (rc) return rc;
+  if (!c->async_jobs.empty()) return set_err(c, CYTOM_ERR_INVAL, "the previous asynchronous runs are not collected");
+  if (!runs_concurrently(c, jobs.data(), count)) {
+    // nothing to overlap: run now, collect later
+    std::vector<cytom_run_stats> st(count);
+    rc = job_run_many(c, jobs.data(), count, st.data());
+    if (rc) return rc;
+    c->sync_stats = st;
+    c->sync_jobs = jobs;
+    return CYTOM_OK;
+  }
+  return launch_many(c, jobs.data(), count);
+}
+
+int cytom_run_many_wait(cytom_ctx* ctx, cytom_run_stats* stats) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c) return CYTOM_ERR_INVAL;
+  if (!c->sync_jobs.empty()) {
+    if (stats) memcpy(stats, c->sync_stats.data(), c->sync_stats.size() * sizeof(cytom_run_stats));
+    c->sync_jobs.clear();
+    c->sync_stats.clear();
+    return CYTOM_OK;
+  }
+  if (c->async_jobs.empty()) return set_err(c, CYTOM_ERR_INVAL, "no asynchronous runs to collect");
+  return collect_runs(c, stats);
+}
+
 int cytom_get_result(cytom_ctx* ctx, int job_id, void* out, int where) {
   Ctx* c = (Ctx*)ctx;
+  if (c) join_runs(c);
   Job* j = get_job(c, job_id);
   if (!j || !out) return CYTOM_ERR_INVAL;
   if (!is_minprop(j->algo)) return pagerank_result(c, j, out, where);
@@ -800,6 +895,7 @@ int cytom_get_result(cytom_ctx* ctx, int job_id, void* out, int where) {
 
 int cytom_job_set_teleport(cytom_ctx* ctx, int job_id, const double* teleport, int where) {
   Ctx* c = (Ctx*)ctx;
+  if (c) join_runs(c);
   Job* j = get_job(c, job_id);
   if (!j) return CYTOM_ERR_INVAL;
   return pagerank_set_teleport(c, j, teleport, where);
@@ -808,6 +904,7 @@ int cytom_job_set_teleport(cytom_ctx* ctx, int job_id, const double* teleport, i
 int cytom_pagerank_adjoint(cytom_ctx* ctx, int job_id, const double* c_weights, int c_where,
                            float* d_weights, float* d_teleport, int out_where, cytom_run_stats* stats) {
   Ctx* c = (Ctx*)ctx;
+  if (c) join_runs(c);
   Job* j = get_job(c, job_id);
   if (!j || !c_weights) return CYTOM_ERR_INVAL;
   return pagerank_adjoint(c, j, c_weights, c_where, d_weights, d_teleport, out_where, stats);
@@ -816,6 +913,7 @@ int cytom_pagerank_adjoint(cytom_ctx* ctx, int job_id, const double* c_weights, 
 int cytom_set_edge_weights(cytom_ctx* ctx, const uint32_t* src, const uint32_t* tgt, const uint32_t* w,
                            uint64_t count, int where) {
   Ctx* c = (Ctx*)ctx;
+  if (c) join_runs(c);
   if (!c || (count && (!src || !tgt || !w))) return CYTOM_ERR_INVAL;
   if (c->wtype == CYTOM_UNWEIGHTED) return set_err(c, CYTOM_ERR_INVAL, "the store has no weights");
   if (where == CYTOM_PTR_DEVICE || count == 0) return set_edge_weights(c, src, tgt, w, count);
@@ -832,6 +930,7 @@ int cytom_set_edge_weights(cytom_ctx* ctx, const uint32_t* src, const uint32_t* 
 int cytom_delete_batch(cytom_ctx* ctx, const uint32_t* src, const uint32_t* tgt, uint64_t count, int where,
                        uint64_t* deleted) {
   Ctx* c = (Ctx*)ctx;
+  if (c) join_runs(c);
   if (deleted) *deleted = 0;
   if (!c || (count && (!src || !tgt))) return CYTOM_ERR_INVAL;
   if (where == CYTOM_PTR_DEVICE || count == 0) return delete_edges(c, src, tgt, count, deleted);
@@ -847,6 +946,7 @@ int cytom_delete_batch(cytom_ctx* ctx, const uint32_t* src, const uint32_t* tgt,
 int cytom_delete_random(cytom_ctx* ctx, uint64_t count, uint64_t seed, uint32_t* src, uint32_t* tgt, int where,
                         uint64_t* deleted) {
   Ctx* c = (Ctx*)ctx;
+  if (c) join_runs(c);
   if (deleted) *deleted = 0;
   if (!c || (src && !tgt) || (!src && tgt)) return CYTOM_ERR_INVAL;
   if (count == 0) return delete_edges(c, nullptr, nullptr, 0, nullptr);
@@ -877,6 +977,7 @@ static void fill_tune_report(const Ctx* c, cytom_tune_report* out) {
 
 int cytom_autotune(cytom_ctx* ctx, cytom_tune_report* out) {
   Ctx* c = (Ctx*)ctx;
+  if (c) join_runs(c);
   if (!c) return CYTOM_ERR_INVAL;
   int rc = compact(c);
   if (!rc) rc = minprop_autotune(c);
@@ -894,6 +995,7 @@ int cytom_get_tune_report(const cytom_ctx* ctx, cytom_tune_report* out) {
 
 int cytom_get_result_f64(cytom_ctx* ctx, int job_id, double* out, int where) {
   Ctx* c = (Ctx*)ctx;
+  if (c) join_runs(c);
   Job* j = get_job(c, job_id);
   if (!j || !out) return CYTOM_ERR_INVAL;
   return pagerank_result64(c, j, out, where);
@@ -936,6 +1038,7 @@ int cytom_launch_count(const cytom_ctx* ctx, uint64_t* launches) {
 
 int cytom_sync(cytom_ctx* ctx) {
   Ctx* c = (Ctx*)ctx;
+  if (c) join_runs(c);
   if (!c) return CYTOM_ERR_INVAL;
   return cuda_err(c, cudaStreamSynchronize(c->stream), "sync");
 }

@@ -145,12 +145,20 @@ struct Ctx {
   uint32_t *edges = nullptr, *wts = nullptr, *edges_alt = nullptr, *wts_alt = nullptr;
   unsigned long long *tile_ptr = nullptr, *tile_ptr_alt = nullptr;
   uint32_t* chunk_tile = nullptr;
+  uint32_t* chunk_tile_alt = nullptr;  // written by the merge, swapped in with the store
   uint64_t cap = 0, chunk_cap = 0;
   uint64_t E = 0;  // exact after compaction
   uint64_t version = 0;  // bumped by every compaction that merged edges
   std::vector<ConcSlot> conc;      // concurrent runs: one stream per job
   cudaEvent_t fork_ev = nullptr;
+  // runs launched by cytom_run_many_async that the context's stream has not waited for
+  // yet; they read the installed snapshot and write only their jobs' state
+  std::vector<Job*> async_jobs;    // jobs of the last asynchronous launch (slot k = job k)
+  bool runs_unjoined = false;
+  std::vector<Job*> sync_jobs;     // an asynchronous request that ran synchronously
+  std::vector<cytom_run_stats> sync_stats;
   uint32_t* dir = nullptr;  // source directory (sparse rounds)
+  uint32_t* dir_alt = nullptr;  // written by the merge, swapped in with the store
   uint64_t dir_entries = 0;
   uint64_t dir_version = ~0ULL;
   bool dir_disabled = false;
@@ -229,6 +237,13 @@ void job_free(Ctx* c, Job* j);
 int job_init_state(Ctx* c, Job* j);
 int job_seed(Ctx* c, Job* j, const uint32_t* src, const uint32_t* tgt, const uint32_t* w,
              uint64_t count);
+int job_seed_keys(Ctx* c, Job* j, const uint64_t* K, const uint32_t* W, uint64_t count);
+// The context's stream waits for runs launched asynchronously (no host wait); every
+// operation that touches the installed snapshot or job state comes after it.
+void join_runs(Ctx* c);
+// Joins and drops the statistics of uncollected asynchronous runs (before jobs run again
+// or are reset or destroyed).
+void settle_runs(Ctx* c);
 int job_run(Ctx* c, Job* j, cytom_run_stats* st);
 int job_result(Ctx* c, Job* j, void* out, int where);
 int ensure_job_queue(Ctx* c, Job* j);

@@ -625,6 +625,8 @@ using namespace cytom;
 extern "C" int cytom_run_batch(cytom_ctx* const* ctxs, const int* job_ids, int count, cytom_run_stats* stats) {
   if (!ctxs || !job_ids || count <= 0 || !ctxs[0]) return CYTOM_ERR_INVAL;
   Ctx* const* cs = reinterpret_cast<Ctx* const*>(ctxs);
+  for (int k = 0; k < count; ++k)
+    if (cs[k]) settle_runs(cs[k]);
   int dev = -1;
   cudaGetDevice(&dev);
   if (dev != cs[0]->device) cudaSetDevice(cs[0]->device);

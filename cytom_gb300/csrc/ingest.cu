@@ -263,11 +263,7 @@ int insert_device(Ctx* c, const uint32_t* src, const uint32_t* tgt, const uint32
   prof_end(c, slot, (double)count * (wuse ? 28.0 : 24.0));
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_err(c, e, "append_kernel");
-  for (Job* j : c->jobs) {
-    if (!j || j->fresh) continue;
-    rc = job_seed(c, j, src, tgt, wuse, count);
-    if (rc) return rc;
-  }
+  // the jobs are seeded by these edges when the compaction installs them
   c->A += count;
   return CYTOM_OK;
 }
@@ -432,9 +428,11 @@ __device__ __forceinline__ uint64_t lower_bound_u32(const uint32_t* a, uint64_t 
 // keep[i] = 1 for a new distinct edge; lb[i] = its insertion index in the old store;
 // wsel[i] = the least weight of its run. A weight that undercuts the stored copy of
 // an existing edge lowers that copy in place.
+constexpr unsigned long long kNoFix = ~0ULL, kFixFlag = 1ULL << 62;
+
 __global__ void dedupe_lookup_kernel(const uint64_t* __restrict__ K, const uint32_t* __restrict__ W,
                                      uint64_t A, const uint32_t* __restrict__ edges,
-                                     uint32_t* __restrict__ wts,
+                                     const uint32_t* __restrict__ wts,
                                      const unsigned long long* __restrict__ tile_ptr,
                                      uint32_t lvpt, uint32_t* __restrict__ keep,
                                      unsigned long long* __restrict__ lb,
@@ -445,6 +443,7 @@ __global__ void dedupe_lookup_kernel(const uint64_t* __restrict__ K, const uint3
     uint64_t key = K[i];
     if (i > 0 && K[i - 1] == key) {
       keep[i] = 0;
+      lb[i] = kNoFix;
       continue;
     }
     uint32_t wmin = 0;
@@ -460,13 +459,17 @@ __global__ void dedupe_lookup_kernel(const uint64_t* __restrict__ K, const uint3
     // list -- an otherwise empty tile -- the reference drops it.
     if (local == 0xFFFFFFFFu && lo == hi && (i == 0 || (K[i - 1] >> (2 * lvpt)) != tile)) {
       keep[i] = 0;
+      lb[i] = kNoFix;
       continue;
     }
     uint64_t pos = lower_bound_u32(edges, lo, hi, local);
     bool found = pos < hi && edges[pos] == local;
     if (found) {
-      if (W) atomicMin(&wts[pos], wmin);
+      // a lower weight for a stored edge is applied to the merged copy (fixup_weights_kernel):
+      // the store itself may still be read by runs of the previous batch
       keep[i] = 0;
+      lb[i] = (W && wmin < wts[pos]) ? (kFixFlag | pos) : kNoFix;
+      wsel[i] = wmin;
     } else {
       keep[i] = 1;
       lb[i] = pos;
@@ -491,6 +494,27 @@ __global__ void pack_kept_kernel(const uint64_t* __restrict__ K, uint64_t A,
     nloc[p] = (uint32_t)((((key >> lvpt) & m) << 16) | (key & m));
     if (nw) nw[p] = wsel[i];
     ntile[p] = (uint32_t)(key >> (2 * lvpt));
+  }
+}
+
+// Weight of a stored edge lowered by the batch, on the merged copy: the old edge at pos
+// moved by the kept new edges inserted at or before pos (q[p] - p <= pos).
+__global__ void fixup_weights_kernel(const unsigned long long* __restrict__ lb, const uint32_t* __restrict__ wsel,
+                                     uint64_t A, const unsigned long long* __restrict__ q,
+                                     const uint32_t* __restrict__ Kdev, uint32_t* __restrict__ ow) {
+  const uint64_t K = *Kdev;
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A; i += stride) {
+    const unsigned long long v = lb[i];
+    if (v == kNoFix || !(v & kFixFlag)) continue;
+    const uint64_t pos = v & ~kFixFlag;
+    uint64_t lo = 0, hi = K;
+    while (lo < hi) {
+      const uint64_t mid = (lo + hi) >> 1;
+      if (q[mid] - mid <= pos) lo = mid + 1;
+      else hi = mid;
+    }
+    atomicMin(ow + pos + lo, wsel[i]);
   }
 }
 
@@ -749,6 +773,7 @@ __global__ void chunk_tile_kernel(const unsigned long long* __restrict__ tile_pt
 
 static int grow_store(Ctx* c, uint64_t need) {
   if (need <= c->cap) return CYTOM_OK;
+  join_runs(c);  // the old buffers are freed below
   uint64_t ncap = std::max<uint64_t>(need + need / 2, 1 << 16);
   ncap = (ncap + kChunk - 1) / kChunk * kChunk + kChunk;
   uint32_t *ne = nullptr, *nea = nullptr, *nw = nullptr, *nwa = nullptr;
@@ -780,10 +805,18 @@ static int grow_store(Ctx* c, uint64_t need) {
   c->cap = ncap;
   uint64_t nch = ncap / kChunk + 2;
   if (nch > c->chunk_cap) {
-    uint32_t* ct = nullptr;
-    if (cudaMalloc(&ct, nch * 4) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "chunk table");
+    uint32_t *ct = nullptr, *cta = nullptr;
+    if (cudaMalloc(&ct, nch * 4) != cudaSuccess || cudaMalloc(&cta, nch * 4) != cudaSuccess) {
+      cudaGetLastError();
+      cudaFree(ct);
+      return set_err(c, CYTOM_ERR_OOM, "chunk table");
+    }
+    cudaMemcpyAsync(ct, c->chunk_tile, c->chunk_cap * 4, cudaMemcpyDeviceToDevice, c->stream);
+    cudaStreamSynchronize(c->stream);
     cudaFree(c->chunk_tile);
+    cudaFree(c->chunk_tile_alt);
     c->chunk_tile = ct;
+    c->chunk_tile_alt = cta;
     c->chunk_cap = nch;
   }
   return CYTOM_OK;
@@ -866,24 +899,54 @@ int compact(Ctx* c) {
   new_tile_ptr_kernel<<<grid_for(c, c->ntiles + 1, 256), 256, 0, c->stream>>>(
       c->tile_ptr, c->ntiles, ntile, Kdev, c->tile_ptr_alt);
   c->launches++;
-  // the directory is kept up to date by the merge once a context has one
-  uint32_t* mdir = (c->dir && !c->dir_disabled) ? c->dir : nullptr;
+  // The merge writes only the alternate buffers (store, tile offsets, chunk table and,
+  // once the context keeps one, the source directory), so it may overlap runs that still
+  // read the installed snapshot.
+  uint32_t* mdir = nullptr;
+  if (c->dir && !c->dir_disabled) {
+    if (!c->dir_alt && cudaMalloc(&c->dir_alt, c->dir_entries * 4) != cudaSuccess) {
+      cudaGetLastError();
+      c->dir_alt = nullptr;
+    }
+    mdir = c->dir_alt;
+  }
   merge_spans_kernel<<<grid_for(c, nsp + 1, 256), 256, 0, c->stream>>>(q, Kdev, c->E, c->tile_ptr_alt, c->ntiles,
-                                                                       nsp, sb, ts, c->chunk_tile);
+                                                                       nsp, sb, ts, c->chunk_tile_alt);
   merge_gather_kernel<<<(unsigned)std::max<uint64_t>(1, std::min<uint64_t>((nsp + 7) / 8, (uint64_t)c->num_sms * 8)),
                         256, 0, c->stream>>>(c->edges, c->wts, c->E, q, nloc, nw, Kdev, sb, ts, nsp, c->tile_ptr_alt,
-                                             c->chunk_tile, mdir, (uint32_t)(c->vpt / 32), c->edges_alt,
+                                             c->chunk_tile_alt, mdir, (uint32_t)(c->vpt / 32), c->edges_alt,
                                              wt ? c->wts_alt : nullptr);
   c->launches += 2;
   e = cudaMemcpyAsync(c->h_pinned, Kdev, 4, cudaMemcpyDeviceToHost, c->stream);
-  cudaFreeAsync(tmp, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-  if (e != cudaSuccess) return cuda_err(c, e, "compaction");
+  if (e != cudaSuccess) {
+    cudaFreeAsync(tmp, c->stream);
+    return cuda_err(c, e, "compaction");
+  }
   uint64_t Kn = *(uint32_t*)c->h_pinned;
   prof_end(c, slot, (double)A * (wt ? 44.0 : 36.0) + (double)(c->E + Kn) * (wt ? 16.0 : 8.0));
+  // Installing the merged snapshot: runs on the previous one must have finished. The jobs
+  // are then seeded by the merged edges (edgeChanged(INSERT)) and lowered weights of
+  // stored edges are applied to the merged copy.
+  join_runs(c);
+  for (Job* j : c->jobs) {
+    if (!j || j->fresh) continue;
+    rc = job_seed_keys(c, j, K, W, A);
+    if (rc) {
+      cudaFreeAsync(tmp, c->stream);
+      return rc;
+    }
+  }
+  if (wt) {
+    fixup_weights_kernel<<<grid_for(c, A, 256), 256, 0, c->stream>>>(lb, wsel, A, q, Kdev, c->wts_alt);
+    c->launches++;
+  }
+  cudaFreeAsync(tmp, c->stream);
   std::swap(c->edges, c->edges_alt);
   std::swap(c->wts, c->wts_alt);
   std::swap(c->tile_ptr, c->tile_ptr_alt);
+  std::swap(c->chunk_tile, c->chunk_tile_alt);
+  if (mdir) std::swap(c->dir, c->dir_alt);
   c->E += Kn;
   c->A = 0;
   c->version++;

@@ -93,6 +93,7 @@ extern "C" {
 
 int cytom_persist_edges(cytom_ctx* ctx, const char* path) {
   Ctx* c = (Ctx*)ctx;
+  if (c) join_runs(c);
   if (!c) return CYTOM_ERR_INVAL;
   edge_log_close(c);
   if (!path) return CYTOM_OK;
@@ -146,6 +147,7 @@ int cytom_read_edges(cytom_ctx* ctx, const char* path, uint64_t batch, uint64_t*
 
 int cytom_write_results(cytom_ctx* ctx, int job_id, const char* path) {
   Ctx* c = (Ctx*)ctx;
+  if (c) join_runs(c);
   if (!c || !path || job_id < 0 || job_id >= (int)c->jobs.size() || !c->jobs[job_id]) return CYTOM_ERR_INVAL;
   Job* j = c->jobs[job_id];
   const uint64_t n = c->n;

@@ -233,6 +233,22 @@ class Engine:
         self._check(self.lib.cytom_run_many(self.ctx, ids, n, stats))
         return [stats[k].as_dict() for k in range(n)]
 
+    def run_many_async(self, programs):
+        """Queues programs of this engine side by side (cytom_run_many_async) and returns at
+        once; the next batch may be inserted and compacted while they run. Collect the
+        statistics with run_many_wait() before the next asynchronous launch."""
+        programs = list(programs)
+        ids = (C.c_int * len(programs))(*[p.job for p in programs])
+        self._check(self.lib.cytom_run_many_async(self.ctx, ids, len(programs)))
+        self._async_count = len(programs)
+
+    def run_many_wait(self) -> list[dict]:
+        n = getattr(self, "_async_count", 0)
+        stats = (L.RunStats * max(n, 1))()
+        self._check(self.lib.cytom_run_many_wait(self.ctx, stats))
+        self._async_count = 0
+        return [stats[k].as_dict() for k in range(n)]
+
     def autotune(self) -> dict:
         """Times the streaming-gather shapes on the current graph and keeps the fastest."""
         rep = L.TuneReport()

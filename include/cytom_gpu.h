@@ -213,6 +213,15 @@ int cytom_run(cytom_ctx* ctx, int job_id, cytom_run_stats* stats);
  * waits for all of them. Lists with other jobs run one after another. stats: `count`
  * entries or NULL. */
 int cytom_run_many(cytom_ctx* ctx, const int* job_ids, int count, cytom_run_stats* stats);
+/* The same launch without waiting: returns once the jobs' loops are queued. The next
+ * batch may then be inserted and compacted while they run: insertion, sorting and the
+ * merge into the alternate buffers overlap the runs, and the context's stream waits for
+ * them only where the merged snapshot is installed (and before any call that reads or
+ * changes job state). cytom_run_many_wait returns the statistics (`count` entries of the
+ * last cytom_run_many_async, or NULL) and must come before the next asynchronous launch.
+ * Lists that cannot run side by side run at once and are returned by the wait. */
+int cytom_run_many_async(cytom_ctx* ctx, const int* job_ids, int count);
+int cytom_run_many_wait(cytom_ctx* ctx, cytom_run_stats* stats);
 
 /* Batched persistent executor. Runs `count` jobs -- job_ids[k] of context ctxs[k]; the
  * contexts (graph snapshots of any size) may differ but must share one device -- together

@@ -63,6 +63,17 @@ __device__ __forceinline__ uint32_t mp_cand(uint32_t c, uint32_t w) {
   return max(c, ~w);
 }
 
+// Pre-check of a target's next value before the reduction. Any value read is valid: next
+// only decreases during a round and never exceeds current, so a candidate below a value
+// read (even one an L1 line kept from earlier in this launch) is below current[v] and v
+// changes. The one-job kernels therefore read through L1 (an earlier launch's lines are
+// not kept); the persistent kernel, whose earlier rounds ran in the same launch, through L2.
+template <bool PERSIST>
+__device__ __forceinline__ uint32_t ld_next(const uint32_t* p) {
+  if constexpr (PERSIST) return __ldcg(p);
+  else return *p;
+}
+
 // Source value of a gather. The asynchronous programs (examples/bfs-async.cc,
 // cc-async.cc: ASYNC = true) pull from next[src], which other blocks lower during the
 // round (algorithm-executor.h:303-312); read through L2, a value is either the one at
@@ -378,7 +389,7 @@ __device__ __forceinline__ void dense_stage(const JobDesc* __restrict__ jd, cons
       if (cand[idx] != kInf) cand[idx] = mp_cand<ALGO>(cand[idx], ww[idx]);
     uint32_t nv[EPT];
 #pragma unroll
-    for (int idx = 0; idx < EPT; ++idx) nv[idx] = (cand[idx] != kInf) ? __ldcg(next + vv[idx]) : 0u;
+    for (int idx = 0; idx < EPT; ++idx) nv[idx] = (cand[idx] != kInf) ? ld_next<PERSIST>(next + vv[idx]) : 0u;
 #pragma unroll
     for (int idx = 0; idx < EPT; ++idx)
       if (cand[idx] != kInf && cand[idx] < nv[idx]) atomicMin(next + vv[idx], cand[idx]);
@@ -470,7 +481,7 @@ __device__ __forceinline__ void sp_batch(const JobDesc* __restrict__ jd, const S
     if (cand[k] != kInf) cand[k] = mp_cand<ALGO>(cand[k], wv[k]);
 #pragma unroll
   for (int k = 0; k < SP_ILP; ++k)
-    nv[k] = (cand[k] != kInf) ? __ldcg(jd->next + ((ys[k] << lvpt) | (pk[k] & 0xFFFFu))) : 0u;
+    nv[k] = (cand[k] != kInf) ? ld_next<PERSIST>(jd->next + ((ys[k] << lvpt) | (pk[k] & 0xFFFFu))) : 0u;
 #pragma unroll
   for (int k = 0; k < SP_ILP; ++k) {
     if (cand[k] != kInf && cand[k] < nv[k]) {

@@ -16,7 +16,6 @@ namespace cytom {
 
 int minprop_alloc(Ctx* c, Job* j);
 int minprop_init(Ctx* c, Job* j);
-int minprop_seed_keys(Ctx* c, Job* j, const uint64_t* K, const uint32_t* W, uint64_t count);
 int minprop_seed(Ctx* c, Job* j, const uint32_t* src, const uint32_t* tgt, const uint32_t* w,
                  uint64_t count);
 int minprop_run(Ctx* c, Job* j);
@@ -204,10 +203,12 @@ int job_seed(Ctx* c, Job* j, const uint32_t* src, const uint32_t* tgt, const uin
                              : pagerank_seed(c, j, src, tgt, w, count);
 }
 
-// edgeChanged(INSERT) for the edges merged by a compaction (sorted keys and weights).
+// edgeChanged(INSERT) for the edges merged by a compaction, PageRank family (the
+// min-propagation jobs are seeded together by minprop_seed_keys_many).
 int job_seed_keys(Ctx* c, Job* j, const uint64_t* K, const uint32_t* W, uint64_t count) {
-  return is_minprop(j->algo) ? minprop_seed_keys(c, j, K, W, count)
-                             : pagerank_seed(c, j, nullptr, nullptr, nullptr, count);
+  (void)K;
+  (void)W;
+  return pagerank_seed(c, j, nullptr, nullptr, nullptr, count);
 }
 
 // The streaming gather is tuned once per context, on the first run at >= 2^20 edges

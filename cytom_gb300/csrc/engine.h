@@ -241,6 +241,9 @@ int job_seed_keys(Ctx* c, Job* j, const uint64_t* K, const uint32_t* W, uint64_t
 // The context's stream waits for runs launched asynchronously (no host wait); every
 // operation that touches the installed snapshot or job state comes after it.
 void join_runs(Ctx* c);
+constexpr int kMaxSeedJobs = 16;  // jobs seeded by one pass over a compaction's keys
+int minprop_seed_keys_many(Ctx* c, Job* const* jobs, int njobs, const uint64_t* K, const uint32_t* W,
+                           uint64_t count);
 // Joins and drops the statistics of uncollected asynchronous runs (before jobs run again
 // or are reset or destroyed).
 void settle_runs(Ctx* c);

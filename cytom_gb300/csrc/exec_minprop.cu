@@ -436,47 +436,68 @@ __global__ void delete_tight_kernel(const JobDesc* __restrict__ jd, const uint32
 
 // The same seeding from the compaction's sorted keys [x][y][src_local][tgt_local] of the
 // edges appended since the last compaction: the jobs are seeded when the merged snapshot is
-// installed, after the runs on the previous snapshot have finished.
+// installed, after the runs on the previous snapshot have finished; all min-propagation
+// jobs of the context in one pass over the keys (each key decoded, its weight read once).
+struct SeedJobs {
+  const JobDesc* jd[kMaxSeedJobs];
+  int algo[kMaxSeedJobs];
+  int count;
+};
+
 template <int ALGO>
-__global__ void seed_keys_kernel(const JobDesc* __restrict__ jd, const uint64_t* __restrict__ K,
-                                 const uint32_t* __restrict__ W, uint64_t count, uint32_t lvpt, uint32_t lT) {
+__device__ __forceinline__ void seed_one(const JobDesc* __restrict__ jd, uint32_t u, uint32_t v, uint32_t w) {
+  const uint32_t uv = jd->cur[u];
+  if (uv == kInf) return;
+  const uint32_t cand = mp_cand<ALGO>(uv, w);
+  if (cand == kInf) return;
+  if (cand < __ldcg(jd->next + v)) {
+    uint32_t old = atomicMin(jd->next + v, cand);
+    if (cand < old) atomicOr(jd->ch + (v >> 5), 1u << (v & 31));
+  }
+}
+
+__global__ void seed_keys_multi_kernel(SeedJobs sj, const uint64_t* __restrict__ K, const uint32_t* __restrict__ W,
+                                       uint64_t count, uint32_t lvpt, uint32_t lT) {
   uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const uint64_t m = (1ULL << lvpt) - 1ULL;
   const uint64_t tmask = (1ULL << lT) - 1ULL;
-  const uint32_t* cur = jd->cur;
-  uint32_t* next = jd->next;
-  uint32_t* ch = jd->ch;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
     const uint64_t key = K[i];
     const uint64_t tile = key >> (2 * lvpt);
     const uint32_t u = (uint32_t)(((tile >> lT) << lvpt) | ((key >> lvpt) & m));
     const uint32_t v = (uint32_t)(((tile & tmask) << lvpt) | (key & m));
-    const uint32_t uv = cur[u];
-    if (uv == kInf) continue;
-    const uint32_t cand = mp_cand<ALGO>(uv, W ? W[i] : 1u);
-    if (cand == kInf) continue;
-    if (cand < __ldcg(next + v)) {
-      uint32_t old = atomicMin(next + v, cand);
-      if (cand < old) atomicOr(ch + (v >> 5), 1u << (v & 31));
+    const uint32_t w = W ? W[i] : 1u;
+    for (int k = 0; k < sj.count; ++k) {
+      switch (sj.algo[k]) {
+        case CYTOM_ALGO_BFS: seed_one<0>(sj.jd[k], u, v, w); break;
+        case CYTOM_ALGO_CC: seed_one<1>(sj.jd[k], u, v, w); break;
+        case CYTOM_ALGO_SSWP: seed_one<3>(sj.jd[k], u, v, w); break;
+        default: seed_one<2>(sj.jd[k], u, v, w); break;
+      }
     }
   }
 }
 
 static int grid_persistent(Ctx* c, int per_sm) { return c->num_sms * per_sm; }
 
-int minprop_seed_keys(Ctx* c, Job* j, const uint64_t* K, const uint32_t* W, uint64_t count) {
+int minprop_seed_keys_many(Ctx* c, Job* const* jobs, int njobs, const uint64_t* K, const uint32_t* W,
+                           uint64_t count) {
   int g = std::max(1, std::min<int>(grid_persistent(c, 8), (int)((count + 255) / 256)));
-  int slot = prof_begin(c, KC_INSERT);
-  switch (j->algo) {
-    case CYTOM_ALGO_BFS: seed_keys_kernel<0><<<g, 256, 0, c->stream>>>(j->d, K, W, count, c->lvpt, c->lT); break;
-    case CYTOM_ALGO_CC: seed_keys_kernel<1><<<g, 256, 0, c->stream>>>(j->d, K, W, count, c->lvpt, c->lT); break;
-    case CYTOM_ALGO_SSWP: seed_keys_kernel<3><<<g, 256, 0, c->stream>>>(j->d, K, W, count, c->lvpt, c->lT); break;
-    default: seed_keys_kernel<2><<<g, 256, 0, c->stream>>>(j->d, K, W, count, c->lvpt, c->lT); break;
+  for (int base = 0; base < njobs; base += kMaxSeedJobs) {
+    SeedJobs sj{};
+    sj.count = std::min(kMaxSeedJobs, njobs - base);
+    for (int k = 0; k < sj.count; ++k) {
+      sj.jd[k] = jobs[base + k]->d;
+      sj.algo[k] = jobs[base + k]->algo;
+    }
+    int slot = prof_begin(c, KC_INSERT);
+    seed_keys_multi_kernel<<<g, 256, 0, c->stream>>>(sj, K, W, count, c->lvpt, c->lT);
+    c->launches++;
+    prof_end(c, slot, (double)count * (12.0 + 8.0 * sj.count));
   }
-  c->launches++;
-  prof_end(c, slot, (double)count * 20.0);
   return cuda_err(c, cudaGetLastError(), "seed_keys");
 }
+
 
 int minprop_delete_check(Ctx* c, Job* j, const uint32_t* dsrc, const uint32_t* dtgt, const uint32_t* dw,
                          uint64_t count, unsigned* tight) {

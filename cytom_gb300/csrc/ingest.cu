@@ -929,9 +929,18 @@ int compact(Ctx* c) {
   // are then seeded by the merged edges (edgeChanged(INSERT)) and lowered weights of
   // stored edges are applied to the merged copy.
   join_runs(c);
-  for (Job* j : c->jobs) {
-    if (!j || j->fresh) continue;
-    rc = job_seed_keys(c, j, K, W, A);
+  {
+    std::vector<Job*> mp;
+    for (Job* j : c->jobs) {
+      if (!j || j->fresh) continue;
+      if (j->algo == CYTOM_ALGO_BFS || j->algo == CYTOM_ALGO_CC || j->algo == CYTOM_ALGO_SSSP ||
+          j->algo == CYTOM_ALGO_SSWP)
+        mp.push_back(j);
+      else
+        rc = job_seed_keys(c, j, K, W, A);  // the PageRank family: a residual round next time
+      if (rc) break;
+    }
+    if (!rc && !mp.empty()) rc = minprop_seed_keys_many(c, mp.data(), (int)mp.size(), K, W, A);
     if (rc) {
       cudaFreeAsync(tmp, c->stream);
       return rc;

@@ -67,6 +67,10 @@ struct PrState {
   double* pt64 = nullptr;
   double* cvec = nullptr;     // loss weights c
   LoopState* adj_ls = nullptr;
+  // captured round loops (one per round kind), rebuilt when their launch arguments change
+  cudaGraphExec_t loop_exec[8] = {};
+  PrArgs loop_args[8] = {};
+  uint64_t loop_nb[8][kPrBins] = {};
 };
 
 // Weighted graph of a context (WPAGERANK): CSC by target and CSR by source, both with
@@ -372,9 +376,20 @@ __global__ void __launch_bounds__(PR_BLOCK_T) pr_pull_large(PrArgs a) {
 }
 
 // Ends the round: records the FP64 residual, decides whether to continue.
+// In a captured loop it also sets the loop condition, and bounds the loop by its own
+// count of rounds (max_iter + 2; beyond it the run stops with err = 2).
 __global__ void pr_control_kernel(LoopState* ls, int mode, cudaGraphConditionalHandle h, int use_handle) {
-  const unsigned cont = pr_control_step(ls, mode);
-  if (use_handle) cudaGraphSetConditional(h, cont);
+  unsigned cont = pr_control_step(ls, mode);
+  if (use_handle) {
+    const unsigned started = ls->sel_rounds + 1;
+    ls->sel_rounds = started;
+    if ((unsigned long long)started > (unsigned long long)ls->max_iter + 2ULL) {
+      ls->err = 2u;
+      ls->cont = 0u;
+      cont = 0u;
+    }
+    cudaGraphSetConditional(h, cont);
+  }
 }
 
 // --------------------------------------------------------------------------
@@ -403,6 +418,7 @@ __global__ void pr_rank_sum_kernel(const float* r, uint64_t n, LoopState* ls) {
 }
 __global__ void pr_begin_kernel(LoopState* ls, unsigned max_iter, double tol, unsigned long long edges) {
   ls->iter = 0;
+  ls->sel_rounds = 0;
   ls->max_iter = max_iter;
   ls->cont = max_iter > 0 ? 1u : 0u;
   ls->err = 0;
@@ -502,6 +518,8 @@ int pagerank_alloc(Ctx* c, Job* j) {
 void pagerank_free(Job* j) {
   PrState* s = prs(j);
   if (!s) return;
+  for (auto& g : s->loop_exec)
+    if (g) cudaGraphExecDestroy(g);
   void* ptrs[] = {s->rank, s->comp, s->delta, s->contrib, s->r64, s->r64n, s->contrib64, s->lo, s->fa2,
                   s->tele, s->lam, s->lam64, s->pt, s->pt64, s->cvec, s->adj_ls};
   for (void* p : ptrs)
@@ -574,8 +592,109 @@ static int launch_round(Ctx* c, const PrArgs& base_args, const uint64_t* nb) {
   return cuda_err(c, cudaGetLastError(), "pagerank round");
 }
 
+static cudaError_t pr_add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* deps, size_t ndeps,
+                                 void* fn, dim3 grid, dim3 block, void** args) {
+  cudaKernelNodeParams kp{};
+  kp.func = fn;
+  kp.gridDim = grid;
+  kp.blockDim = block;
+  kp.kernelParams = args;
+  return cudaGraphAddKernelNode(node, g, deps, ndeps, &kp);
+}
+
+// The round loop as one CUDA graph: while(cont) { contributions -> pulls of the in-degree
+// bins (side by side) -> control, which sets the condition }. A run is one graph launch.
+template <int MODE>
+static int build_round_graph(Ctx* c, const PrArgs& base, const uint64_t* nb, cudaGraphExec_t* out) {
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaGraphCreate(&g, 0);
+  if (e != cudaSuccess) return cuda_err(c, e, "graph create");
+  cudaGraphConditionalHandle h;
+  e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+  cudaGraphNodeParams cp{};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t wnode;
+  if (e == cudaSuccess) e = cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &cp);
+  if (e == cudaSuccess) {
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    PrArgs a = base;
+    void* a_c[] = {(void*)&a};
+    cudaGraphNode_t n_c, n_bins[kPrBins];
+    int nbins = 0;
+    e = pr_add_kernel(body, &n_c, nullptr, 0, (void*)pr_contrib_kernel<MODE>, dim3(grid_n(c, c->n)), dim3(256), a_c);
+    uint64_t off = 0;
+    for (int k = 0; k < kPrBins && e == cudaSuccess; ++k) {
+      PrArgs ak = base;
+      ak.bin_off = off;
+      ak.bin_count = nb[k];
+      off += nb[k];
+      if (!nb[k]) continue;
+      void* a_k[] = {(void*)&ak};
+      void* fn;
+      dim3 grid, block(PR_T);
+      switch (pr_bin_vw(k)) {
+        case 1: fn = (void*)pr_pull_small<MODE>; grid = dim3(grid_n(c, nb[k], PR_T)); break;
+        case 4: fn = (void*)pr_pull_group<MODE, 4>; grid = dim3(grid_n(c, nb[k] * 4, PR_T)); break;
+        case 8: fn = (void*)pr_pull_group<MODE, 8>; grid = dim3(grid_n(c, nb[k] * 8, PR_T)); break;
+        case 32: fn = (void*)pr_pull_group<MODE, 32>; grid = dim3(grid_n(c, nb[k] * 32, PR_T)); break;
+        default:
+          fn = (void*)pr_pull_large<MODE>;
+          grid = dim3((unsigned)std::min<uint64_t>(nb[k], (uint64_t)c->num_sms * 4));
+          block = dim3(PR_BLOCK_T);
+      }
+      e = pr_add_kernel(body, &n_bins[nbins], &n_c, 1, fn, grid, block, a_k);
+      if (e == cudaSuccess) ++nbins;
+    }
+    LoopState* ls = base.ls;
+    int mode = MODE, one = 1;
+    void* a_ctl[] = {(void*)&ls, (void*)&mode, (void*)&h, (void*)&one};
+    cudaGraphNode_t n_ctl;
+    if (e == cudaSuccess)
+      e = pr_add_kernel(body, &n_ctl, nbins ? n_bins : &n_c, nbins ? nbins : 1, (void*)pr_control_kernel, dim3(1),
+                        dim3(1), a_ctl);
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *out = nullptr;
+    return CYTOM_ERR_CUDA;
+  }
+  return CYTOM_OK;
+}
+
+static bool pr_use_graphs() {
+  static int v = -1;
+  if (v < 0) {
+    const char* s = getenv("CYTOM_NO_GRAPH");
+    v = (s && s[0] == '1') ? 0 : 1;
+  }
+  return v == 1;
+}
+
 template <int MODE>
 static int run_rounds(Ctx* c, Job* j, const PrArgs& a, uint64_t max_rounds, const uint64_t* nb) {
+  if (max_rounds > 1 && !c->profiling && pr_use_graphs()) {
+    PrState* s = prs(j);
+    cudaGraphExec_t& gx = s->loop_exec[MODE];
+    if (gx && (memcmp(&s->loop_args[MODE], &a, sizeof(PrArgs)) != 0 ||
+               memcmp(s->loop_nb[MODE], nb, sizeof(uint64_t) * kPrBins) != 0)) {
+      cudaGraphExecDestroy(gx);
+      gx = nullptr;
+    }
+    if (!gx && build_round_graph<MODE>(c, a, nb, &gx) == CYTOM_OK) {
+      memcpy(&s->loop_args[MODE], &a, sizeof(PrArgs));
+      memcpy(s->loop_nb[MODE], nb, sizeof(uint64_t) * kPrBins);
+    }
+    if (gx) {
+      cudaError_t e = cudaGraphLaunch(gx, c->stream);
+      c->launches += 1;
+      return cuda_err(c, e, "pagerank graph launch");
+    }
+  }
   for (uint64_t r = 0; r < max_rounds;) {
     for (int k = 0; k < 8 && r < max_rounds; ++k, ++r) {
       int slot = prof_begin(c, KC_PAGERANK);

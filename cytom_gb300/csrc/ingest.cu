@@ -550,6 +550,8 @@ __global__ void new_tile_ptr_kernel(const unsigned long long* __restrict__ tile_
 // trips and their loads issue together; a span with more new elements loads its
 // candidates step by step. Stores are coalesced 128-byte warp writes.
 //
+// The store is streamed with evict-first loads and stores, leaving L2 to the jobs that
+// run on the installed snapshot meanwhile (the pipelined stream).
 // The same pass writes the chunk table of the new store and, when the context keeps a
 // source directory, its per-edge entries (the work of dir_edges_kernel): each output
 // knows its tile (walked from the span's first tile) and the edge before it.
@@ -700,8 +702,8 @@ __global__ void merge_gather_kernel(const uint32_t* __restrict__ edges, const ui
               ev[k] = nb[src[k]];
               if (owb) wv[k] = nwb[src[k]];
             } else {
-              ev[k] = eb[src[k]];
-              if (owb) wv[k] = wb[src[k]];
+              ev[k] = __ldcs(eb + src[k]);
+              if (owb) wv[k] = __ldcs(wb + src[k]);
             }
           }
         }
@@ -709,8 +711,8 @@ __global__ void merge_gather_kernel(const uint32_t* __restrict__ edges, const ui
         for (int k = 0; k < MG; ++k) {
           const uint32_t o = (uint32_t)(g + k) * 32 + lane;
           if (o < nout) {
-            oeb[o] = ev[k];
-            if (owb) owb[o] = wv[k];
+            __stcs(oeb + o, ev[k]);
+            if (owb) __stcs(owb + o, wv[k]);
           }
           uint32_t pv = __shfl_up_sync(0xFFFFFFFFu, ev[k], 1);
           if (lane == 0) pv = plast;
@@ -735,11 +737,11 @@ __global__ void merge_gather_kernel(const uint32_t* __restrict__ edges, const ui
           ev = nb[y];
           if (owb) wv = nwb[y];
         } else {
-          ev = eb[o - y];
-          if (owb) wv = wb[o - y];
+          ev = __ldcs(eb + (o - y));
+          if (owb) wv = __ldcs(wb + (o - y));
         }
-        oeb[o] = ev;
-        if (owb) owb[o] = wv;
+        __stcs(oeb + o, ev);
+        if (owb) __stcs(owb + o, wv);
       }
       uint32_t pv = __shfl_up_sync(0xFFFFFFFFu, ev, 1);
       if (lane == 0) pv = plast;

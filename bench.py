@@ -71,6 +71,19 @@ def dist_env():
     return rank, world, local
 
 
+def reduce_over_ranks(ms: float, edges: float, dev, world: int):
+    """Replicas: the slowest rank's time and the edges of all ranks (one all-reduce each;
+    NCCL on GPUs, gloo for the CPU tests)."""
+    if world <= 1:
+        return float(ms), float(edges)
+    import torch
+    t = torch.tensor([ms], device=dev, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    e = torch.tensor([edges], device=dev, dtype=torch.float64)
+    torch.distributed.all_reduce(e)
+    return float(t.item()), float(e.item())
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
@@ -299,14 +312,8 @@ def main():
         a, b, c = ev[k]
         ingest_ms += a.elapsed_time(b)
     if world > 1:
-        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-        te = torch.tensor([teps_edges], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(te)
-        teps_all = float(te.item())
-    else:
-        teps_all = float(teps_edges)
+        torch.distributed.barrier()
+    total_ms, teps_all = reduce_over_ranks(total_ms, teps_edges, dev, world)
     value = teps_all / (total_ms / 1e3) / 1e9
     ingest_meps = world * args.steps * B / (ingest_ms / 1e3) / 1e6  # pipelined: replaced below
     final_edges = eng.count_edges()[0]

@@ -332,7 +332,13 @@ __global__ void __launch_bounds__(256, 4) gather_sparse_kernel(const JobDesc* __
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   const uint64_t items = (uint64_t)ls->nact_words[p] << sd->lT;
   unsigned long long scanned = 0;
-  for (uint64_t g = warp * 32; g < items; g += nwarps * 32) scanned += sparse_group<ALGO, false>(jd, sd, g, items);
+  // few groups: up to 8 warps share each group's light edges
+  const uint64_t groups = (items + 31) / 32;
+  uint32_t nslice = 1;
+  while (nslice < 8 && groups * nslice * 2 <= nwarps) nslice *= 2;
+  const uint32_t slice = (uint32_t)(warp % nslice);
+  for (uint64_t g = (warp / nslice) * 32; g < items; g += (nwarps / nslice) * 32)
+    scanned += sparse_group<ALGO, false>(jd, sd, g, items, slice, nslice);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) scanned += __shfl_xor_sync(0xFFFFFFFFu, scanned, o);
   if (lane == 0 && scanned) atomicAdd(&ls->edges_scanned, scanned);

@@ -493,9 +493,14 @@ __device__ __forceinline__ void sp_batch(const JobDesc* __restrict__ jd, const S
 }
 
 // One group of 32 items [g, g + 32) for the calling warp; returns the light edges walked.
+// With nslice > 1 several warps share the group: each reads the group's items, slice 0
+// alone queues the heavy ones, and the light edges are dealt out in steps of 32 * SP_ILP
+// (slice k takes steps k, k + nslice, ...); if the queue overflowed, slice 0 walks every
+// light edge itself (the others' share is then walked twice, which changes nothing).
 template <int ALGO, bool PERSIST>
 __device__ __forceinline__ uint32_t sparse_group(const JobDesc* __restrict__ jd, const StoreDesc* __restrict__ sd,
-                                                 uint64_t g, uint64_t items) {
+                                                 uint64_t g, uint64_t items, uint32_t slice = 0,
+                                                 uint32_t nslice = 1) {
   LoopState* ls = jd->ls;
   const unsigned lane = threadIdx.x & 31;
   const uint64_t qcap = jd->spq_cap;
@@ -510,15 +515,19 @@ __device__ __forceinline__ uint32_t sparse_group(const JobDesc* __restrict__ jd,
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xFFFFFFFFu, tot, o);
   const bool heavy = len > SP_HEAVY || (tot > SP_WARP_MAX && len > SP_LIGHT);
-  bool queued = false;
-  if (heavy) {
+  bool queued = heavy && slice != 0;  // slice 0 queues; the others leave those items to it
+  bool overflow = false;
+  if (heavy && slice == 0) {
     const uint32_t nch = (len + SP_CHUNK - 1) / SP_CHUNK;
     const unsigned slot = atomicAdd(&ls->spq_count, nch);
     if ((uint64_t)slot + nch <= qcap) {
       for (uint32_t k = 0; k < nch; ++k) jd->spq[slot + k] = make_uint2((uint32_t)it, k);
       queued = true;
+    } else {
+      overflow = true;
     }
   }
+  const bool walk_all = nslice > 1 && slice == 0 && __any_sync(0xFFFFFFFFu, overflow);
   // light items: the group's edges are numbered 0..total-1 (warp prefix sum over the
   // items' lengths); lanes take SP_ILP of them per step and find their item by a
   // binary search over the prefix sums held in the lanes
@@ -530,7 +539,8 @@ __device__ __forceinline__ uint32_t sparse_group(const JobDesc* __restrict__ jd,
     if (lane >= (unsigned)o) incl += y2;
   }
   const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-  for (uint32_t f0 = 0; f0 < total; f0 += 32 * SP_ILP) {
+  const uint32_t step0 = walk_all ? 0u : slice, nstep = walk_all ? 1u : nslice;
+  for (uint32_t f0 = step0 * 32 * SP_ILP; f0 < total; f0 += nstep * 32 * SP_ILP) {
     uint32_t xs[SP_ILP], ys[SP_ILP], bits[SP_ILP];
     unsigned long long pos[SP_ILP];
     uint32_t valid = 0;
@@ -556,7 +566,7 @@ __device__ __forceinline__ uint32_t sparse_group(const JobDesc* __restrict__ jd,
     }
     sp_batch<ALGO, PERSIST>(jd, sd, xs, ys, bits, pos, valid);
   }
-  return mine;
+  return slice == 0 ? mine : 0u;
 }
 
 // Queue entry q (a chunk of a heavy item) for the calling warp; returns the edges walked

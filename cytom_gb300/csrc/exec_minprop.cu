@@ -282,18 +282,22 @@ __global__ void __launch_bounds__(SG_T, MINB) gather_stream_kernel(const JobDesc
   bool failed = false;
 
   while (stq[0] < nst) {
+    // one block barrier per stage: a thread whose bounded wait gave up skips the stage
+    // and the barrier after it ends the block
     const bool ok = mbar_wait(&bar[slot], (phases >> slot) & 1u);
-    if (!__syncthreads_and(ok)) {
+    phases ^= 1u << slot;
+    if (ok) {
+      if (threadIdx.x == 0) {
+        const uint64_t rem = E - stq[0] * SE;
+        scanned += rem < (uint64_t)SE ? rem : (uint64_t)SE;
+      }
+      dense_stage<ALGO, false, false, EPT>(jd, sd, ebuf + slot * SE, wbuf + slot * SE, stq[0], p, adaptive);
+    }
+    if (__syncthreads_or(!ok)) {  // every thread is done with this slot
       failed = true;
+      phases ^= 1u << slot;  // the slot's copy is still owed: the cleanup waits on it
       break;
     }
-    phases ^= 1u << slot;
-    if (threadIdx.x == 0) {
-      const uint64_t rem = E - stq[0] * SE;
-      scanned += rem < (uint64_t)SE ? rem : (uint64_t)SE;
-    }
-    dense_stage<ALGO, false, false, EPT>(jd, sd, ebuf + slot * SE, wbuf + slot * SE, stq[0], p, adaptive);
-    __syncthreads();  // every thread is done with this slot
     // refill the slot with the next stage of this block
     if (threadIdx.x == 0 && s_next < nst) issue(slot, s_next);
 #pragma unroll

@@ -311,16 +311,19 @@ __global__ void pr_contrib_kernel(PrArgs a) {
   pr_dangling_flush<MODE>(ls, p, dangling);
 }
 
-// One thread per target (in-degree <= 16).
+// The pulls of one round, every in-degree bin in one launch: bin k owns blocks
+// [first[k], first[k+1]) and walks its targets with pr_bin_vw(k) lanes per target (1: one
+// thread, 0: one whole block).
+struct PrBinLaunch {
+  uint64_t off[kPrBins], count[kPrBins];
+  uint32_t first[kPrBins + 1];
+};
+
 template <int MODE>
-__global__ void __launch_bounds__(PR_T) pr_pull_small(PrArgs a) {
-  LoopState* ls = a.ls;
-  if (!ls->cont) return;
-  const unsigned p = ls->iter & 1u;
-  const double dang = pr_dang_arg<MODE, false>(ls, p, a.n);
-  double resid = 0.0, rsum = 0.0;
-  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < a.bin_count; base += stride) {
+__device__ __forceinline__ void pull_small_body(const PrArgs& a, unsigned p, double dang, uint64_t bid, uint64_t nblk,
+                                                double& resid, double& rsum) {
+  const uint64_t stride = nblk * blockDim.x;
+  for (uint64_t base = bid * blockDim.x; base < a.bin_count; base += stride) {
     const uint64_t i = base + threadIdx.x;
     if (i < a.bin_count) {
       const uint32_t v = a.bins[a.bin_off + i];
@@ -328,21 +331,15 @@ __global__ void __launch_bounds__(PR_T) pr_pull_small(PrArgs a) {
       resid += pr_finish<MODE, false>(a, v, sum, p, dang, &rsum);
     }
   }
-  pr_flush(ls, p, resid, rsum);
 }
 
-// VW lanes per target (bins 1..3: in-degrees up to 32, 256, 4096).
 template <int MODE, int VW>
-__global__ void __launch_bounds__(PR_T) pr_pull_group(PrArgs a) {
-  LoopState* ls = a.ls;
-  if (!ls->cont) return;
-  const unsigned p = ls->iter & 1u;
-  const double dang = pr_dang_arg<MODE, false>(ls, p, a.n);
+__device__ __forceinline__ void pull_group_body(const PrArgs& a, unsigned p, double dang, uint64_t bid, uint64_t nblk,
+                                                double& resid, double& rsum) {
   constexpr uint64_t GPW = 32 / VW;  // groups per warp
   const unsigned gl = threadIdx.x & (VW - 1);
-  const uint64_t gid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / VW;
-  const uint64_t ngroups = ((uint64_t)gridDim.x * blockDim.x) / VW;
-  double resid = 0.0, rsum = 0.0;
+  const uint64_t gid = (bid * blockDim.x + threadIdx.x) / VW;
+  const uint64_t ngroups = (nblk * blockDim.x) / VW;
   // warp-uniform trip count: every lane stays in the loop for the group shuffles
   const uint64_t gbase = gid - (gid % GPW);
   for (uint64_t b = gbase; b < a.bin_count; b += ngroups) {
@@ -356,21 +353,36 @@ __global__ void __launch_bounds__(PR_T) pr_pull_group(PrArgs a) {
     const double sum = pr_sum_group<MODE, false, VW>(a, lo, hi, gl);
     if (gl == 0 && i < a.bin_count) resid += pr_finish<MODE, false>(a, v, sum, p, dang, &rsum);
   }
-  pr_flush(ls, p, resid, rsum);
 }
 
-// One block per target (in-degree > 4096: RMAT hubs).
 template <int MODE>
-__global__ void __launch_bounds__(PR_BLOCK_T) pr_pull_large(PrArgs a) {
-  LoopState* ls = a.ls;
-  if (!ls->cont) return;
-  const unsigned p = ls->iter & 1u;
-  const double dang = pr_dang_arg<MODE, false>(ls, p, a.n);
-  double resid = 0.0, rsum = 0.0;
-  for (uint64_t i = blockIdx.x; i < a.bin_count; i += gridDim.x) {
+__device__ __forceinline__ void pull_large_body(const PrArgs& a, unsigned p, double dang, uint64_t bid, uint64_t nblk,
+                                                double& resid, double& rsum) {
+  for (uint64_t i = bid; i < a.bin_count; i += nblk) {
     const uint32_t v = a.bins[a.bin_off + i];
     const double sum = pr_sum_block<MODE, false>(a, v);
     if (threadIdx.x == 0) resid += pr_finish<MODE, false>(a, v, sum, p, dang, &rsum);
+  }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(PR_T) pr_pull_kernel(PrArgs a, PrBinLaunch bl) {
+  LoopState* ls = a.ls;
+  if (!ls->cont) return;
+  const unsigned p = ls->iter & 1u;
+  int k = 0;
+  while (k + 1 < kPrBins && blockIdx.x >= bl.first[k + 1]) ++k;
+  const uint64_t bid = blockIdx.x - bl.first[k], nblk = bl.first[k + 1] - bl.first[k];
+  a.bin_off = bl.off[k];
+  a.bin_count = bl.count[k];
+  const double dang = pr_dang_arg<MODE, false>(ls, p, a.n);
+  double resid = 0.0, rsum = 0.0;
+  switch (pr_bin_vw(k)) {
+    case 1: pull_small_body<MODE>(a, p, dang, bid, nblk, resid, rsum); break;
+    case 4: pull_group_body<MODE, 4>(a, p, dang, bid, nblk, resid, rsum); break;
+    case 8: pull_group_body<MODE, 8>(a, p, dang, bid, nblk, resid, rsum); break;
+    case 32: pull_group_body<MODE, 32>(a, p, dang, bid, nblk, resid, rsum); break;
+    default: pull_large_body<MODE>(a, p, dang, bid, nblk, resid, rsum);
   }
   pr_flush(ls, p, resid, rsum);
 }
@@ -565,27 +577,37 @@ int pagerank_seed(Ctx* c, Job* j, const uint32_t*, const uint32_t*, const uint32
   return CYTOM_OK;
 }
 
+// Blocks per bin of the fused pull, as the bins' own launches would use.
+static PrBinLaunch bin_launch(Ctx* c, const uint64_t* nb) {
+  PrBinLaunch bl{};
+  uint64_t off = 0, blocks = 0;
+  for (int k = 0; k < kPrBins; ++k) {
+    bl.off[k] = off;
+    bl.count[k] = nb[k];
+    bl.first[k] = (uint32_t)blocks;
+    off += nb[k];
+    if (!nb[k]) continue;
+    switch (pr_bin_vw(k)) {
+      case 1: blocks += grid_n(c, nb[k], PR_T); break;
+      case 4: blocks += grid_n(c, nb[k] * 4, PR_T); break;
+      case 8: blocks += grid_n(c, nb[k] * 8, PR_T); break;
+      case 32: blocks += grid_n(c, nb[k] * 32, PR_T); break;
+      default: blocks += std::min<uint64_t>(nb[k], (uint64_t)c->num_sms * 4);
+    }
+  }
+  bl.first[kPrBins] = (uint32_t)blocks;
+  return bl;
+}
+
 template <int MODE>
 static int launch_round(Ctx* c, const PrArgs& base_args, const uint64_t* nb) {
   PrArgs a = base_args;
   pr_contrib_kernel<MODE><<<grid_n(c, c->n), 256, 0, c->stream>>>(a);
+  const PrBinLaunch bl = bin_launch(c, nb);
   int launched = 2;
-  uint64_t off = 0;
-  for (int k = 0; k < kPrBins; ++k) {
-    a.bin_off = off;
-    a.bin_count = nb[k];
-    off += nb[k];
-    if (!nb[k]) continue;
+  if (bl.first[kPrBins]) {
+    pr_pull_kernel<MODE><<<bl.first[kPrBins], PR_T, 0, c->stream>>>(a, bl);
     ++launched;
-    switch (pr_bin_vw(k)) {
-      case 1: pr_pull_small<MODE><<<grid_n(c, nb[k], PR_T), PR_T, 0, c->stream>>>(a); break;
-      case 4: pr_pull_group<MODE, 4><<<grid_n(c, nb[k] * 4, PR_T), PR_T, 0, c->stream>>>(a); break;
-      case 8: pr_pull_group<MODE, 8><<<grid_n(c, nb[k] * 8, PR_T), PR_T, 0, c->stream>>>(a); break;
-      case 32: pr_pull_group<MODE, 32><<<grid_n(c, nb[k] * 32, PR_T), PR_T, 0, c->stream>>>(a); break;
-      default:
-        pr_pull_large<MODE><<<(unsigned)std::min<uint64_t>(nb[k], (uint64_t)c->num_sms * 4), PR_BLOCK_T, 0,
-                              c->stream>>>(a);
-    }
   }
   pr_control_kernel<<<1, 1, 0, c->stream>>>(a.ls, MODE, 0, 0);
   c->launches += launched;
@@ -622,31 +644,15 @@ static int build_round_graph(Ctx* c, const PrArgs& base, const uint64_t* nb, cud
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     PrArgs a = base;
     void* a_c[] = {(void*)&a};
-    cudaGraphNode_t n_c, n_bins[kPrBins];
+    cudaGraphNode_t n_c, n_bins[1];
     int nbins = 0;
     e = pr_add_kernel(body, &n_c, nullptr, 0, (void*)pr_contrib_kernel<MODE>, dim3(grid_n(c, c->n)), dim3(256), a_c);
-    uint64_t off = 0;
-    for (int k = 0; k < kPrBins && e == cudaSuccess; ++k) {
-      PrArgs ak = base;
-      ak.bin_off = off;
-      ak.bin_count = nb[k];
-      off += nb[k];
-      if (!nb[k]) continue;
-      void* a_k[] = {(void*)&ak};
-      void* fn;
-      dim3 grid, block(PR_T);
-      switch (pr_bin_vw(k)) {
-        case 1: fn = (void*)pr_pull_small<MODE>; grid = dim3(grid_n(c, nb[k], PR_T)); break;
-        case 4: fn = (void*)pr_pull_group<MODE, 4>; grid = dim3(grid_n(c, nb[k] * 4, PR_T)); break;
-        case 8: fn = (void*)pr_pull_group<MODE, 8>; grid = dim3(grid_n(c, nb[k] * 8, PR_T)); break;
-        case 32: fn = (void*)pr_pull_group<MODE, 32>; grid = dim3(grid_n(c, nb[k] * 32, PR_T)); break;
-        default:
-          fn = (void*)pr_pull_large<MODE>;
-          grid = dim3((unsigned)std::min<uint64_t>(nb[k], (uint64_t)c->num_sms * 4));
-          block = dim3(PR_BLOCK_T);
-      }
-      e = pr_add_kernel(body, &n_bins[nbins], &n_c, 1, fn, grid, block, a_k);
-      if (e == cudaSuccess) ++nbins;
+    PrBinLaunch bl = bin_launch(c, nb);
+    void* a_p[] = {(void*)&a, (void*)&bl};
+    if (e == cudaSuccess && bl.first[kPrBins]) {
+      e = pr_add_kernel(body, &n_bins[0], &n_c, 1, (void*)pr_pull_kernel<MODE>, dim3(bl.first[kPrBins]), dim3(PR_T),
+                        a_p);
+      if (e == cudaSuccess) nbins = 1;
     }
     LoopState* ls = base.ls;
     int mode = MODE, one = 1;

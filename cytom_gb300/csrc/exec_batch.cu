@@ -89,30 +89,6 @@ __host__ __device__ constexpr unsigned long long pack_claim(unsigned phase, unsi
 
 __device__ __forceinline__ uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
 
-// Block-wide sums of two doubles onto thread 0.
-__device__ __forceinline__ void block_sum2(double& a, double& b) {
-  __shared__ double s_a[BT / 32], s_b[BT / 32];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    a += __shfl_xor_sync(0xFFFFFFFFu, a, o);
-    b += __shfl_xor_sync(0xFFFFFFFFu, b, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    s_a[threadIdx.x >> 5] = a;
-    s_b[threadIdx.x >> 5] = b;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    a = 0.0;
-    b = 0.0;
-    for (int k = 0; k < BT / 32; ++k) {
-      a += s_a[k];
-      b += s_b[k];
-    }
-  }
-  __syncthreads();
-}
-
 // ---- units -----------------------------------------------------------------
 
 __device__ __forceinline__ unsigned ls_iter(const LoopState* ls) { return *(const volatile unsigned*)&ls->iter; }
@@ -181,14 +157,13 @@ __device__ void unit_pr_contrib(const BJob* J, uint32_t unit) {
   const unsigned p = ls_iter(a.ls) & 1u;
   const uint64_t lo = (uint64_t)unit * BU_PR_VERTS;
   const uint64_t hi = std::min<uint64_t>(lo + BU_PR_VERTS, a.n);
-  const uint64_t wlo = lo >> 5, whi = std::min<uint64_t>((hi + 31) >> 5, a.nwords);
-  const double dangling = pr_contrib_range<MODE, true>(a, p, lo, hi, wlo, whi, threadIdx.x, BT);
+  const double dangling = pr_contrib_range<MODE, true>(a, p, lo, hi, threadIdx.x, BT);
   pr_dangling_flush<MODE>(a.ls, p, dangling);
 }
 
 template <int MODE, int VW>
-__device__ __forceinline__ void pull_groups(const PrArgs& a, uint64_t off, uint64_t cnt, uint64_t first, unsigned p,
-                                            double dang, double& resid, double& rsum) {
+__device__ __forceinline__ void pull_groups(const PrArgs& a, const pr_val_t<MODE>* cr, uint64_t off, uint64_t cnt,
+                                            uint64_t first, unsigned p, double dang, PrTally& t) {
   constexpr uint32_t GPB = BT / VW;  // groups per block
   const unsigned gl = threadIdx.x & (VW - 1);
   const uint32_t g = threadIdx.x / VW;
@@ -201,8 +176,8 @@ __device__ __forceinline__ void pull_groups(const PrArgs& a, uint64_t off, uint6
       lo = a.csc_ptr[v];
       hi = a.csc_ptr[v + 1];
     }
-    const double sum = pr_sum_group<MODE, true, VW>(a, lo, hi, gl);
-    if (gl == 0 && i < cnt) resid += pr_finish<MODE, true>(a, v, sum, p, dang, &rsum);
+    const double sum = pr_sum_group<MODE, true, VW>(a, cr, lo, hi, gl);
+    if (gl == 0 && i < cnt) pr_finish<MODE, true>(a, v, sum, p, dang, t);
   }
 }
 
@@ -224,7 +199,9 @@ __device__ void unit_pr_pull(const BJob* J, uint32_t unit) {
   }
   const uint64_t cnt = J->nb[k];
   const uint64_t first = (uint64_t)u * pr_bin_unit(k);
-  double resid = 0.0, rsum = 0.0;
+  const pr_val_t<MODE>* cr = pr_cread<MODE>(a, p);
+  PrTally t;
+  t.init();
   switch (pr_bin_vw(k)) {
     case 1:
 #pragma unroll 1
@@ -232,25 +209,21 @@ __device__ void unit_pr_pull(const BJob* J, uint32_t unit) {
         const uint64_t i = first + (uint64_t)r * BT + threadIdx.x;
         if (i < cnt) {
           const uint32_t v = a.bins[off + i];
-          const double sum = pr_sum_thread<MODE, true>(a, v);
-          resid += pr_finish<MODE, true>(a, v, sum, p, dang, &rsum);
+          const double sum = pr_sum_thread<MODE, true>(a, cr, v);
+          pr_finish<MODE, true>(a, v, sum, p, dang, t);
         }
       }
       break;
-    case 4: pull_groups<MODE, 4>(a, off, cnt, first, p, dang, resid, rsum); break;
-    case 8: pull_groups<MODE, 8>(a, off, cnt, first, p, dang, resid, rsum); break;
-    case 32: pull_groups<MODE, 32>(a, off, cnt, first, p, dang, resid, rsum); break;
+    case 4: pull_groups<MODE, 4>(a, cr, off, cnt, first, p, dang, t); break;
+    case 8: pull_groups<MODE, 8>(a, cr, off, cnt, first, p, dang, t); break;
+    case 32: pull_groups<MODE, 32>(a, cr, off, cnt, first, p, dang, t); break;
     default: {
       const uint32_t v = a.bins[off + first];
-      const double sum = pr_sum_block<MODE, true>(a, v);
-      if (threadIdx.x == 0) resid += pr_finish<MODE, true>(a, v, sum, p, dang, &rsum);
+      const double sum = pr_sum_block<MODE, true>(a, cr, v);
+      if (threadIdx.x == 0) pr_finish<MODE, true>(a, v, sum, p, dang, t);
     }
   }
-  block_sum2(resid, rsum);
-  if (threadIdx.x == 0) {
-    if (resid != 0.0) atomicAdd(&ls->resid[p], resid);
-    if (rsum != 0.0) atomicAdd(&ls->rank_sum[p], rsum);
-  }
+  pr_tally_flush<MODE>(ls, p, t);
 }
 
 __device__ __forceinline__ uint32_t pr_pull_units(const BJob* J) {
@@ -279,9 +252,15 @@ __device__ void advance(const BJob* J, BSched* S, BCtl* ctl, unsigned phase) {
       } else {
         s_cont = pr_control_step(J->pr.ls, s_mode);
         if (s_cont) {
-          if (s_mode == PR_DELTA_RESIDUAL) s_mode = PR_DELTA_PUSH;
-          s_next = PH_PR_CONTRIB;
-          s_total = ceil_div(J->pr.n, BU_PR_VERTS);
+          if (s_mode == PR_DELTA_RESIDUAL || s_mode == PR_DELTA_PUSH) {
+            // PageRank-delta: the pull wrote the next round's contributions
+            s_mode = PR_DELTA_PUSH;
+            s_next = PH_PR_PULL;
+            s_total = pr_pull_units(J);
+          } else {
+            s_next = PH_PR_CONTRIB;
+            s_total = ceil_div(J->pr.n, BU_PR_VERTS);
+          }
         }
       }
     } else if (phase == PH_DENSE || phase == PH_CHUNKS) {
@@ -362,8 +341,9 @@ __device__ void run_unit(const BJob* J, unsigned phase, uint32_t unit, int prmod
       else unit_chunks<2>(J, unit);
       break;
     case PH_PR_CONTRIB:
+      // PageRank-delta: its residual round only (the delta rounds take the previous
+      // pull's contributions)
       if (prmode == PR_DELTA_RESIDUAL) unit_pr_contrib<PR_DELTA_RESIDUAL>(J, unit);
-      else if (prmode == PR_DELTA_PUSH) unit_pr_contrib<PR_DELTA_PUSH>(J, unit);
       else if (prmode == PR_NORM32) unit_pr_contrib<PR_NORM32>(J, unit);
       else unit_pr_contrib<PR_NORM64>(J, unit);
       break;

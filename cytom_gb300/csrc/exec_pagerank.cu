@@ -18,9 +18,16 @@
 // Both pull over a target-sorted CSC built from the tile store once per snapshot
 // (radix sort of (tgt, src) keys): each target's in-edges are contiguous, so its sum is
 // accumulated in a fixed order with Neumaier compensation -- deterministic and
-// compensated, no float atomics. Targets are binned by in-degree: one thread (<= 16
-// in-edges), one warp (<= 4096) or one block (more) per target. Residuals, dangling
-// mass and rank sums are FP64 reductions.
+// compensated, no float atomics. Targets are binned by in-degree: one thread (<= 4
+// in-edges), 4 lanes (<= 32), 8 lanes (<= 256), a warp (<= 4096) or a block (more) per
+// target, all bins in one launch. Residuals, dangling mass and rank sums are FP64
+// reductions.
+//
+// A round of PageRank-delta is that one launch: each finished target also writes its
+// contribution to the next round (contributions by round parity), and the last block to
+// finish runs the control step and, in a captured loop, sets the loop condition. Only the
+// run's residual round has a contribution pass before the pull. The other forms run
+// contributions -> pull -> control.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -50,12 +57,11 @@ struct PrState {
   float* rank = nullptr;      // PR_DELTA: rank; PAGERANK fp32: r (double-buffered with rank_c)
   float* comp = nullptr;      // PR_DELTA: Kahan compensation of rank; PAGERANK fp32: r_next
   float* delta = nullptr;     // PR_DELTA: delta of the last round
-  float* contrib = nullptr;   // per-source contribution of the round
+  float* contrib = nullptr;   // per-source contributions (PR_DELTA: 2 x n by round parity)
   double* r64 = nullptr;      // PAGERANK fp64: r
   double* r64n = nullptr;     // PAGERANK fp64: r_next
   double* contrib64 = nullptr;
   float* lo = nullptr;        // PAGERANK / WPAGERANK fp32: low words of the ranks (2 x n)
-  uint32_t* fa2 = nullptr;    // PR_DELTA: frontier bitmaps by parity (2 x n/32)
   bool need_residual = true;
   uint64_t seen_version = ~0ULL;
   // WPAGERANK
@@ -161,7 +167,7 @@ static int build_csx(Ctx* c, Csc& q, int by_source, float** w, uint64_t* wcap) {
   const uint64_t n = c->n, E = c->E;
   uint32_t lg_n = 0;
   while ((1ULL << lg_n) < n) ++lg_n;
-  if (E > 0xFFFFFFFFULL) return set_err(c, CYTOM_ERR_RANGE, "PageRank CSC holds at most 2^32 edges");
+  if (E > 0xFFFFFFFFULL - (1ULL << 20)) return set_err(c, CYTOM_ERR_RANGE, "PageRank CSC holds fewer than 2^32 - 2^20 edges");
   if (E > q.cap || !q.src) {
     cudaFree(q.src);
     q.cap = std::max<uint64_t>(E + E / 4, 1024);
@@ -305,37 +311,38 @@ __global__ void pr_contrib_kernel(PrArgs a) {
   LoopState* ls = a.ls;
   if (!ls->cont) return;
   const unsigned p = ls->iter & 1u;
-  const double dangling = pr_contrib_range<MODE, false>(a, p, 0, a.n, 0, a.nwords,
-                                                        (uint64_t)blockIdx.x * blockDim.x + threadIdx.x,
+  const double dangling = pr_contrib_range<MODE, false>(a, p, 0, a.n, (uint64_t)blockIdx.x * blockDim.x + threadIdx.x,
                                                         (uint64_t)gridDim.x * blockDim.x);
   pr_dangling_flush<MODE>(ls, p, dangling);
 }
 
 // The pulls of one round, every in-degree bin in one launch: bin k owns blocks
-// [first[k], first[k+1]) and walks its targets with pr_bin_vw(k) lanes per target (1: one
-// thread, 0: one whole block).
+// [first[k], first[k] + nblk[k]) and walks its targets with pr_bin_vw(k) lanes per target
+// (1: one thread, 0: one whole block). The heaviest bins take the lowest block ids, so
+// their long-running blocks start first.
 struct PrBinLaunch {
   uint64_t off[kPrBins], count[kPrBins];
-  uint32_t first[kPrBins + 1];
+  uint32_t first[kPrBins], nblk[kPrBins];
+  uint32_t blocks;  // the launch's grid (at least 1)
 };
 
 template <int MODE>
-__device__ __forceinline__ void pull_small_body(const PrArgs& a, unsigned p, double dang, uint64_t bid, uint64_t nblk,
-                                                double& resid, double& rsum) {
+__device__ __forceinline__ void pull_small_body(const PrArgs& a, const pr_val_t<MODE>* cr, unsigned p, double dang,
+                                                uint64_t bid, uint64_t nblk, PrTally& t) {
   const uint64_t stride = nblk * blockDim.x;
   for (uint64_t base = bid * blockDim.x; base < a.bin_count; base += stride) {
     const uint64_t i = base + threadIdx.x;
     if (i < a.bin_count) {
       const uint32_t v = a.bins[a.bin_off + i];
-      const double sum = pr_sum_thread<MODE, false>(a, v);
-      resid += pr_finish<MODE, false>(a, v, sum, p, dang, &rsum);
+      const double sum = pr_sum_thread<MODE, false>(a, cr, v);
+      pr_finish<MODE, false>(a, v, sum, p, dang, t);
     }
   }
 }
 
 template <int MODE, int VW>
-__device__ __forceinline__ void pull_group_body(const PrArgs& a, unsigned p, double dang, uint64_t bid, uint64_t nblk,
-                                                double& resid, double& rsum) {
+__device__ __forceinline__ void pull_group_body(const PrArgs& a, const pr_val_t<MODE>* cr, unsigned p, double dang,
+                                                uint64_t bid, uint64_t nblk, PrTally& t) {
   constexpr uint64_t GPW = 32 / VW;  // groups per warp
   const unsigned gl = threadIdx.x & (VW - 1);
   const uint64_t gid = (bid * blockDim.x + threadIdx.x) / VW;
@@ -350,47 +357,26 @@ __device__ __forceinline__ void pull_group_body(const PrArgs& a, unsigned p, dou
       lo = a.csc_ptr[v];
       hi = a.csc_ptr[v + 1];
     }
-    const double sum = pr_sum_group<MODE, false, VW>(a, lo, hi, gl);
-    if (gl == 0 && i < a.bin_count) resid += pr_finish<MODE, false>(a, v, sum, p, dang, &rsum);
+    const double sum = pr_sum_group<MODE, false, VW>(a, cr, lo, hi, gl);
+    if (gl == 0 && i < a.bin_count) pr_finish<MODE, false>(a, v, sum, p, dang, t);
   }
 }
 
 template <int MODE>
-__device__ __forceinline__ void pull_large_body(const PrArgs& a, unsigned p, double dang, uint64_t bid, uint64_t nblk,
-                                                double& resid, double& rsum) {
+__device__ __forceinline__ void pull_large_body(const PrArgs& a, const pr_val_t<MODE>* cr, unsigned p, double dang,
+                                                uint64_t bid, uint64_t nblk, PrTally& t) {
   for (uint64_t i = bid; i < a.bin_count; i += nblk) {
     const uint32_t v = a.bins[a.bin_off + i];
-    const double sum = pr_sum_block<MODE, false>(a, v);
-    if (threadIdx.x == 0) resid += pr_finish<MODE, false>(a, v, sum, p, dang, &rsum);
+    const double sum = pr_sum_block<MODE, false>(a, cr, v);
+    if (threadIdx.x == 0) pr_finish<MODE, false>(a, v, sum, p, dang, t);
   }
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(PR_T) pr_pull_kernel(PrArgs a, PrBinLaunch bl) {
-  LoopState* ls = a.ls;
-  if (!ls->cont) return;
-  const unsigned p = ls->iter & 1u;
-  int k = 0;
-  while (k + 1 < kPrBins && blockIdx.x >= bl.first[k + 1]) ++k;
-  const uint64_t bid = blockIdx.x - bl.first[k], nblk = bl.first[k + 1] - bl.first[k];
-  a.bin_off = bl.off[k];
-  a.bin_count = bl.count[k];
-  const double dang = pr_dang_arg<MODE, false>(ls, p, a.n);
-  double resid = 0.0, rsum = 0.0;
-  switch (pr_bin_vw(k)) {
-    case 1: pull_small_body<MODE>(a, p, dang, bid, nblk, resid, rsum); break;
-    case 4: pull_group_body<MODE, 4>(a, p, dang, bid, nblk, resid, rsum); break;
-    case 8: pull_group_body<MODE, 8>(a, p, dang, bid, nblk, resid, rsum); break;
-    case 32: pull_group_body<MODE, 32>(a, p, dang, bid, nblk, resid, rsum); break;
-    default: pull_large_body<MODE>(a, p, dang, bid, nblk, resid, rsum);
-  }
-  pr_flush(ls, p, resid, rsum);
-}
-
-// Ends the round: records the FP64 residual, decides whether to continue.
-// In a captured loop it also sets the loop condition, and bounds the loop by its own
-// count of rounds (max_iter + 2; beyond it the run stops with err = 2).
-__global__ void pr_control_kernel(LoopState* ls, int mode, cudaGraphConditionalHandle h, int use_handle) {
+// Ends the round: records the FP64 residual, decides whether to continue. In a captured
+// loop it also sets the loop condition, and bounds the loop by its own count of rounds
+// (max_iter + 2; beyond it the run stops with err = 2).
+__device__ __forceinline__ void pr_loop_control(LoopState* ls, int mode, cudaGraphConditionalHandle h,
+                                                int use_handle) {
   unsigned cont = pr_control_step(ls, mode);
   if (use_handle) {
     const unsigned started = ls->sel_rounds + 1;
@@ -402,6 +388,57 @@ __global__ void pr_control_kernel(LoopState* ls, int mode, cudaGraphConditionalH
     }
     cudaGraphSetConditional(h, cont);
   }
+}
+
+// Fused forms: the control step and loop condition of the round, run by the last block
+// of the pull to finish (every block counts itself in after its results are visible;
+// the wrapping increment leaves the counter at 0 for the next round).
+__device__ __forceinline__ void pr_round_end(LoopState* ls, int mode, cudaGraphConditionalHandle h, int use_handle) {
+  __shared__ unsigned s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicInc(&ls->apply_done, gridDim.x - 1u) == gridDim.x - 1u ? 1u : 0u;
+  __syncthreads();
+  if (s_last && threadIdx.x == 0) {
+    __threadfence();
+    pr_loop_control(ls, mode, h, use_handle);
+  }
+}
+
+// Every block takes part in the round end of the fused forms, whether or not the run
+// still continues (a captured loop's condition is only set here).
+template <int MODE>
+__global__ void __launch_bounds__(PR_T) pr_pull_kernel(PrArgs a, PrBinLaunch bl, cudaGraphConditionalHandle h,
+                                                       int use_handle) {
+  LoopState* ls = a.ls;
+  const bool live = ls->cont != 0;
+  if (!live && !pr_fused<MODE>()) return;
+  const unsigned p = ls->iter & 1u;
+  PrTally t;
+  t.init();
+  int k = 0;
+  while (k < kPrBins && !(blockIdx.x >= bl.first[k] && blockIdx.x - bl.first[k] < bl.nblk[k])) ++k;
+  if (live && k < kPrBins) {
+    const uint64_t bid = blockIdx.x - bl.first[k], nblk = bl.nblk[k];
+    a.bin_off = bl.off[k];
+    a.bin_count = bl.count[k];
+    const double dang = pr_dang_arg<MODE, false>(ls, p, a.n);
+    const pr_val_t<MODE>* cr = pr_cread<MODE>(a, p);
+    switch (pr_bin_vw(k)) {
+      case 1: pull_small_body<MODE>(a, cr, p, dang, bid, nblk, t); break;
+      case 4: pull_group_body<MODE, 4>(a, cr, p, dang, bid, nblk, t); break;
+      case 8: pull_group_body<MODE, 8>(a, cr, p, dang, bid, nblk, t); break;
+      case 32: pull_group_body<MODE, 32>(a, cr, p, dang, bid, nblk, t); break;
+      default: pull_large_body<MODE>(a, cr, p, dang, bid, nblk, t);
+    }
+  }
+  if (live) pr_tally_flush<MODE>(ls, p, t);
+  if constexpr (pr_fused<MODE>()) pr_round_end(ls, MODE, h, use_handle);
+}
+
+// The control step as its own launch (the forms without a fused round end).
+__global__ void pr_control_kernel(LoopState* ls, int mode, cudaGraphConditionalHandle h, int use_handle) {
+  pr_loop_control(ls, mode, h, use_handle);
 }
 
 // --------------------------------------------------------------------------
@@ -431,6 +468,7 @@ __global__ void pr_rank_sum_kernel(const float* r, uint64_t n, LoopState* ls) {
 __global__ void pr_begin_kernel(LoopState* ls, unsigned max_iter, double tol, unsigned long long edges) {
   ls->iter = 0;
   ls->sel_rounds = 0;
+  ls->apply_done = 0;
   ls->max_iter = max_iter;
   ls->cont = max_iter > 0 ? 1u : 0u;
   ls->err = 0;
@@ -501,14 +539,12 @@ int pagerank_alloc(Ctx* c, Job* j) {
   s->csc = ctx_csc(c);
   if (!s->csc) return set_err(c, CYTOM_ERR_OOM, "PageRank CSC");
   const uint64_t n = c->n;
-  const uint64_t nwords = (n + 31) / 32;
   bool ok = true;
   if (j->algo == CYTOM_ALGO_PR_DELTA) {
     ok = ok && cudaMalloc(&s->rank, n * 4) == cudaSuccess;
     ok = ok && cudaMalloc(&s->comp, n * 4) == cudaSuccess;
     ok = ok && cudaMalloc(&s->delta, n * 4) == cudaSuccess;
-    ok = ok && cudaMalloc(&s->contrib, n * 4) == cudaSuccess;
-    ok = ok && cudaMalloc(&s->fa2, 2 * nwords * 4) == cudaSuccess;
+    ok = ok && cudaMalloc(&s->contrib, 2 * n * 4) == cudaSuccess;
   } else if (j->params.kahan) {
     ok = ok && cudaMalloc(&s->rank, n * 4) == cudaSuccess;
     ok = ok && cudaMalloc(&s->comp, n * 4) == cudaSuccess;
@@ -532,8 +568,8 @@ void pagerank_free(Job* j) {
   if (!s) return;
   for (auto& g : s->loop_exec)
     if (g) cudaGraphExecDestroy(g);
-  void* ptrs[] = {s->rank, s->comp, s->delta, s->contrib, s->r64, s->r64n, s->contrib64, s->lo, s->fa2,
-                  s->tele, s->lam, s->lam64, s->pt, s->pt64, s->cvec, s->adj_ls};
+  void* ptrs[] = {s->rank, s->comp, s->delta, s->contrib, s->r64,  s->r64n, s->contrib64, s->lo,
+                  s->tele, s->lam,  s->lam64, s->pt,      s->pt64, s->cvec, s->adj_ls};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete s;
@@ -552,7 +588,6 @@ int pagerank_init(Ctx* c, Job* j) {
     pr_fill_kernel<<<g, 256, 0, c->stream>>>(s->rank, 1.0f, n);
     cudaMemsetAsync(s->comp, 0, n * 4, c->stream);
     cudaMemsetAsync(s->delta, 0, n * 4, c->stream);
-    cudaMemsetAsync(s->fa2, 0xFF, 2 * ((n + 31) / 32) * 4, c->stream);
     c->launches++;
   } else if (j->algo == CYTOM_ALGO_WPAGERANK && s->tele) {
     if (j->params.kahan) pr_to_float_kernel<<<g, 256, 0, c->stream>>>(s->tele, s->rank, n);
@@ -577,39 +612,65 @@ int pagerank_seed(Ctx* c, Job* j, const uint32_t*, const uint32_t*, const uint32
   return CYTOM_OK;
 }
 
-// Blocks per bin of the fused pull, as the bins' own launches would use.
+// Blocks per bin of the one-launch pull, heaviest bin first (as the bins' own launches
+// would use).
 static PrBinLaunch bin_launch(Ctx* c, const uint64_t* nb) {
   PrBinLaunch bl{};
-  uint64_t off = 0, blocks = 0;
+  uint64_t off = 0;
   for (int k = 0; k < kPrBins; ++k) {
     bl.off[k] = off;
     bl.count[k] = nb[k];
-    bl.first[k] = (uint32_t)blocks;
     off += nb[k];
-    if (!nb[k]) continue;
-    switch (pr_bin_vw(k)) {
-      case 1: blocks += grid_n(c, nb[k], PR_T); break;
-      case 4: blocks += grid_n(c, nb[k] * 4, PR_T); break;
-      case 8: blocks += grid_n(c, nb[k] * 8, PR_T); break;
-      case 32: blocks += grid_n(c, nb[k] * 32, PR_T); break;
-      default: blocks += std::min<uint64_t>(nb[k], (uint64_t)c->num_sms * 4);
-    }
   }
-  bl.first[kPrBins] = (uint32_t)blocks;
+  uint64_t blocks = 0;
+  for (int k = kPrBins - 1; k >= 0; --k) {
+    uint64_t b = 0;
+    if (nb[k]) {
+      switch (pr_bin_vw(k)) {
+        case 1: b = grid_n(c, nb[k], PR_T); break;
+        case 4: b = grid_n(c, nb[k] * 4, PR_T); break;
+        case 8: b = grid_n(c, nb[k] * 8, PR_T); break;
+        case 32: b = grid_n(c, nb[k] * 32, PR_T); break;
+        default: b = std::min<uint64_t>(nb[k], (uint64_t)c->num_sms * 4);
+      }
+    }
+    bl.first[k] = (uint32_t)blocks;
+    bl.nblk[k] = (uint32_t)b;
+    blocks += b;
+  }
+  bl.blocks = (uint32_t)std::max<uint64_t>(blocks, 1);
   return bl;
 }
 
+// Whether a round of this form opens with a contribution pass: every round of the
+// unfused forms, PageRank-delta's residual round (its delta rounds take the previous
+// pull's contributions).
 template <int MODE>
-static int launch_round(Ctx* c, const PrArgs& base_args, const uint64_t* nb) {
+static constexpr bool pr_opens_with_contrib() {
+  return !pr_fused<MODE>() || MODE == PR_DELTA_RESIDUAL;
+}
+
+// One round (first: the run's first round). Fused form: the pull alone (its last block
+// runs the control step), after the residual round's contribution pass; the others:
+// contributions -> pull -> control.
+template <int MODE>
+static int launch_round(Ctx* c, const PrArgs& base_args, const uint64_t* nb, bool first) {
   PrArgs a = base_args;
-  pr_contrib_kernel<MODE><<<grid_n(c, c->n), 256, 0, c->stream>>>(a);
-  const PrBinLaunch bl = bin_launch(c, nb);
-  int launched = 2;
-  if (bl.first[kPrBins]) {
-    pr_pull_kernel<MODE><<<bl.first[kPrBins], PR_T, 0, c->stream>>>(a, bl);
+  int launched = 0;
+  if (!pr_fused<MODE>() || (first && pr_opens_with_contrib<MODE>())) {
+    pr_contrib_kernel<MODE><<<grid_n(c, c->n), 256, 0, c->stream>>>(a);
     ++launched;
   }
-  pr_control_kernel<<<1, 1, 0, c->stream>>>(a.ls, MODE, 0, 0);
+  const PrBinLaunch bl = bin_launch(c, nb);
+  cudaGraphConditionalHandle h{};
+  if (pr_fused<MODE>() || bl.blocks) {
+    pr_pull_kernel<MODE><<<bl.blocks, PR_T, 0, c->stream>>>(a, bl, h, 0);
+    ++launched;
+  }
+  if (!pr_fused<MODE>()) {
+    pr_control_kernel<<<1, 1, 0, c->stream>>>(a.ls, MODE, h, 0);
+    ++launched;
+  }
   c->launches += launched;
   return cuda_err(c, cudaGetLastError(), "pagerank round");
 }
@@ -624,43 +685,50 @@ static cudaError_t pr_add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cud
   return cudaGraphAddKernelNode(node, g, deps, ndeps, &kp);
 }
 
-// The round loop as one CUDA graph: while(cont) { contributions -> pulls of the in-degree
-// bins (side by side) -> control, which sets the condition }. A run is one graph launch.
+// The round loop as one CUDA graph; a run is one graph launch. Fused form: while(cont)
+// { pull, whose last block sets the condition }; the others: while(cont) { contributions
+// -> pull -> control, which sets the condition }.
 template <int MODE>
 static int build_round_graph(Ctx* c, const PrArgs& base, const uint64_t* nb, cudaGraphExec_t* out) {
+  constexpr bool F = pr_fused<MODE>();
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaGraphCreate(&g, 0);
   if (e != cudaSuccess) return cuda_err(c, e, "graph create");
+  PrArgs a = base;
+  void* a_c[] = {(void*)&a};
+  cudaGraphNode_t n_pre;
+  const bool pre = F && pr_opens_with_contrib<MODE>();
+  if (pre)
+    e = pr_add_kernel(g, &n_pre, nullptr, 0, (void*)pr_contrib_kernel<MODE>, dim3(grid_n(c, c->n)), dim3(256), a_c);
   cudaGraphConditionalHandle h;
-  e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+  if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
   cudaGraphNodeParams cp{};
   cp.type = cudaGraphNodeTypeConditional;
   cp.conditional.handle = h;
   cp.conditional.type = cudaGraphCondTypeWhile;
   cp.conditional.size = 1;
   cudaGraphNode_t wnode;
-  if (e == cudaSuccess) e = cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &cp);
+  if (e == cudaSuccess) e = cudaGraphAddNode(&wnode, g, pre ? &n_pre : nullptr, nullptr, pre ? 1 : 0, &cp);
   if (e == cudaSuccess) {
     cudaGraph_t body = cp.conditional.phGraph_out[0];
-    PrArgs a = base;
-    void* a_c[] = {(void*)&a};
-    cudaGraphNode_t n_c, n_bins[1];
-    int nbins = 0;
-    e = pr_add_kernel(body, &n_c, nullptr, 0, (void*)pr_contrib_kernel<MODE>, dim3(grid_n(c, c->n)), dim3(256), a_c);
     PrBinLaunch bl = bin_launch(c, nb);
-    void* a_p[] = {(void*)&a, (void*)&bl};
-    if (e == cudaSuccess && bl.first[kPrBins]) {
-      e = pr_add_kernel(body, &n_bins[0], &n_c, 1, (void*)pr_pull_kernel<MODE>, dim3(bl.first[kPrBins]), dim3(PR_T),
-                        a_p);
-      if (e == cudaSuccess) nbins = 1;
-    }
     LoopState* ls = base.ls;
     int mode = MODE, one = 1;
-    void* a_ctl[] = {(void*)&ls, (void*)&mode, (void*)&h, (void*)&one};
-    cudaGraphNode_t n_ctl;
-    if (e == cudaSuccess)
-      e = pr_add_kernel(body, &n_ctl, nbins ? n_bins : &n_c, nbins ? nbins : 1, (void*)pr_control_kernel, dim3(1),
-                        dim3(1), a_ctl);
+    void* a_p[] = {(void*)&a, (void*)&bl, (void*)&h, (void*)&one};
+    if (F) {
+      cudaGraphNode_t n_p;
+      e = pr_add_kernel(body, &n_p, nullptr, 0, (void*)pr_pull_kernel<MODE>, dim3(bl.blocks), dim3(PR_T), a_p);
+    } else {
+      cudaGraphNode_t n_c, n_p, n_ctl;
+      int zero = 0;
+      void* a_p0[] = {(void*)&a, (void*)&bl, (void*)&h, (void*)&zero};
+      e = pr_add_kernel(body, &n_c, nullptr, 0, (void*)pr_contrib_kernel<MODE>, dim3(grid_n(c, c->n)), dim3(256), a_c);
+      if (e == cudaSuccess)
+        e = pr_add_kernel(body, &n_p, &n_c, 1, (void*)pr_pull_kernel<MODE>, dim3(bl.blocks), dim3(PR_T), a_p0);
+      void* a_ctl[] = {(void*)&ls, (void*)&mode, (void*)&h, (void*)&one};
+      if (e == cudaSuccess)
+        e = pr_add_kernel(body, &n_ctl, &n_p, 1, (void*)pr_control_kernel, dim3(1), dim3(1), a_ctl);
+    }
   }
   if (e == cudaSuccess) e = cudaGraphInstantiate(out, g, 0);
   cudaGraphDestroy(g);
@@ -704,7 +772,7 @@ static int run_rounds(Ctx* c, Job* j, const PrArgs& a, uint64_t max_rounds, cons
   for (uint64_t r = 0; r < max_rounds;) {
     for (int k = 0; k < 8 && r < max_rounds; ++k, ++r) {
       int slot = prof_begin(c, KC_PAGERANK);
-      int rc = launch_round<MODE>(c, a, nb);
+      int rc = launch_round<MODE>(c, a, nb, r == 0);
       prof_end(c, slot, -1.0);
       if (rc) return rc;
     }
@@ -745,7 +813,6 @@ int pagerank_run(Ctx* c, Job* j) {
   a.r64 = s->r64;
   a.r64n = s->r64n;
   a.contrib64 = s->contrib64;
-  a.fa2 = s->fa2;
   a.ls = j->ls;
   a.n = n;
   a.nwords = (n + 31) / 32;
@@ -806,7 +873,6 @@ int pagerank_batch_prep(Ctx* c, Job* j, PrArgs* out, uint64_t* nb, int* first_mo
   a.r64 = s->r64;
   a.r64n = s->r64n;
   a.contrib64 = s->contrib64;
-  a.fa2 = s->fa2;
   a.ls = j->ls;
   a.n = n;
   a.nwords = (n + 31) / 32;

@@ -3,10 +3,16 @@
 //
 // A round: per-source contributions (and the dangling mass), then a pull over the
 // target-sorted CSC — each target's in-edges summed in a fixed order with Neumaier
-// compensation, one thread (in-degree <= 16), one warp (<= 4096) or one block (more)
-// per target — then the control step (FP64 residual, convergence). PageRank-delta is
+// compensation, 1 / 4 / 8 / 32 lanes or a whole block per target by in-degree bin —
+// then the control step (FP64 residual, convergence). PageRank-delta is
 // examples/pagerank-delta.cc (pullGather :127-132, apply :142-174); PAGERANK is the
 // normalised PageRank with dangling-mass redistribution.
+//
+// Fused form (PageRank-delta; pr_fused): a target's new delta fixes its contribution to
+// the next round, so the pull writes it as it finishes each target. Contributions are
+// kept by round parity: round p reads half p and writes half p^1. Only a run's first
+// (residual) round needs a contribution pass. The PAGERANK forms keep the pass: at RMAT
+// scale 26 their pull's scattered per-target writes cost more than the pass's streamed ones.
 //
 // Load policy as in minprop_dev.cuh: PERSIST = the persistent kernel, which reads every
 // value written in the same launch (ranks, contributions) through L2.
@@ -14,6 +20,8 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <type_traits>
 
 #include "engine.h"
 
@@ -52,6 +60,13 @@ template <int MODE>
 __host__ __device__ constexpr bool pr_weighted() {
   return MODE >= PR_W32;
 }
+template <int MODE>
+__host__ __device__ constexpr bool pr_fused() {
+  return MODE == PR_DELTA_RESIDUAL || MODE == PR_DELTA_PUSH;
+}
+// Value type of the contributions (and of a lane's partial sums before the merge).
+template <int MODE>
+using pr_val_t = typename std::conditional<pr_is64<MODE>(), double, float>::type;
 
 // Compensated accumulation (Neumaier): true sum ~= s + e.
 struct Acc32 {
@@ -91,11 +106,10 @@ struct PrArgs {
   float* rank;
   float* comp;
   float* delta;
-  float* contrib;
+  float* contrib;           // FP32 contributions (PageRank-delta: 2 x n, by parity)
   double* r64;
   double* r64n;
-  double* contrib64;
-  uint32_t* fa2;            // 2 x nwords (PR_DELTA)
+  double* contrib64;        // FP64 contributions
   float* lo0;               // FP32 PAGERANK / WPAGERANK: low words of the ranks (rank + lo0,
   float* lo1;               //   comp + lo1): each rank is carried as an unevaluated float pair
   const float* csc_w;       // weighted modes: raw weight of each in-edge (CSC) / out-edge (CSR)
@@ -116,50 +130,48 @@ __device__ __forceinline__ T pr_ld(const T* p) {
   else return *p;
 }
 
-// Contribution of in-edge e with source s: contrib[s], times the edge's raw weight in
-// the weighted modes (an FP32 product in the FP32 modes).
-template <int MODE, bool PERSIST>
-__device__ __forceinline__ float pr_c32(const PrArgs& a, uint32_t e, uint32_t s) {
-  const float c = pr_ld<PERSIST>(a.contrib + s);
-  if constexpr (pr_weighted<MODE>()) return c * a.csc_w[e];
-  else return c;
+// The contributions round p reads (fused form: half p; the others: the one vector).
+template <int MODE>
+__device__ __forceinline__ const pr_val_t<MODE>* pr_cread(const PrArgs& a, unsigned p) {
+  const uint64_t off = pr_fused<MODE>() ? (uint64_t)p * a.n : 0;
+  if constexpr (pr_is64<MODE>()) return a.contrib64 + off;
+  else return a.contrib + off;
 }
+
+// Contribution of in-edge e with source s: cr[s], times the edge's raw weight in the
+// weighted modes (an FP32 product in the FP32 modes).
 template <int MODE, bool PERSIST>
-__device__ __forceinline__ double pr_c64(const PrArgs& a, uint32_t e, uint32_t s) {
-  const double c = pr_ld<PERSIST>(a.contrib64 + s);
-  if constexpr (pr_weighted<MODE>()) return c * (double)a.csc_w[e];
+__device__ __forceinline__ pr_val_t<MODE> pr_cval(const PrArgs& a, const pr_val_t<MODE>* cr, uint32_t e, uint32_t s) {
+  const pr_val_t<MODE> c = pr_ld<PERSIST>(cr + s);
+  if constexpr (pr_weighted<MODE>()) return c * (pr_val_t<MODE>)a.csc_w[e];
   else return c;
 }
 
 // Contributions of the sources handled by this thread (u = lo + tid, lo + tid + nthr, ...
-// below hi); for PageRank-delta also clears the next frontier's words [wlo, whi).
+// below hi): PageRank-delta's residual round (every source contributes rank / outdeg;
+// its later rounds take the previous pull's contributions) and every round of the
+// other forms.
 // Returns the thread's share of the dangling mass (PAGERANK).
 template <int MODE, bool PERSIST>
 __device__ __forceinline__ double pr_contrib_range(const PrArgs& a, unsigned p, uint64_t lo, uint64_t hi,
-                                                   uint64_t wlo, uint64_t whi, uint64_t tid, uint64_t nthr) {
+                                                   uint64_t tid, uint64_t nthr) {
   double dangling = 0.0;
   if (MODE == PR_DELTA_RESIDUAL || MODE == PR_DELTA_PUSH) {
-    const uint32_t* fa = a.fa2 + p * a.nwords;
-    uint32_t* fn = a.fa2 + (p ^ 1u) * a.nwords;
-    for (uint64_t w = wlo + tid; w < whi; w += nthr) fn[w] = 0;
+    float* cw = a.contrib + (uint64_t)p * a.n;
     for (uint64_t u = lo + tid; u < hi; u += nthr) {
       const uint32_t d = a.deg[u];
-      float v = 0.f;
-      if (d) {
-        if (MODE == PR_DELTA_RESIDUAL) v = pr_ld<PERSIST>(a.rank + u) / (float)d;
-        else if ((pr_ld<PERSIST>(fa + (u >> 5)) >> (u & 31)) & 1u) v = pr_ld<PERSIST>(a.delta + u) / (float)d;
-      }
-      a.contrib[u] = v;
+      cw[u] = d ? pr_ld<PERSIST>(a.rank + u) / (float)d : 0.f;
     }
   } else if (MODE == PR_NORM32) {
     const float* r = (p == 0) ? a.rank : a.comp;
     const float* rl = (p == 0) ? a.lo0 : a.lo1;
+    float* cw = a.contrib;
     // the contribution is an FP32 quotient of the high word (the low word is below its
     // rounding); the low word enters the FP64 dangling sum and the residual
     for (uint64_t u = lo + tid; u < hi; u += nthr) {
       const uint32_t d = a.deg[u];
       const float rh = pr_ld<PERSIST>(r + u);
-      a.contrib[u] = d ? rh / (float)d : 0.f;
+      cw[u] = d ? rh / (float)d : 0.f;
       if (!d) dangling += (double)rh + (double)pr_ld<PERSIST>(rl + u);
     }
   } else if (MODE == PR_W32) {
@@ -198,10 +210,11 @@ __device__ __forceinline__ double pr_contrib_range(const PrArgs& a, unsigned p, 
     }
   } else {
     const double* r = (p == 0) ? a.r64 : a.r64n;
+    double* cw = a.contrib64;
     for (uint64_t u = lo + tid; u < hi; u += nthr) {
       const uint32_t d = a.deg[u];
       const double rv = pr_ld<PERSIST>(r + u);
-      a.contrib64[u] = d ? rv / (double)d : 0.0;
+      cw[u] = d ? rv / (double)d : 0.0;
       if (!d) dangling += rv;
     }
   }
@@ -227,10 +240,10 @@ __device__ __forceinline__ double pr_dang_arg(const LoopState* ls, unsigned p, u
   return (MODE == PR_NORM32 || MODE == PR_NORM64) ? d / (double)n : d;
 }
 
-// Applies the finished sum of target v; returns |change| for the FP64 residual.
+// The update of target v (pr_finish); returns |change| for the FP64 residual.
 template <int MODE, bool PERSIST>
-__device__ __forceinline__ double pr_finish(const PrArgs& a, uint64_t v, double sum, unsigned p, double dang,
-                                            double* rsum) {
+__device__ __forceinline__ double pr_apply(const PrArgs& a, uint64_t v, double sum, unsigned p, double dang,
+                                           double* rsum, unsigned* nact) {
   if (MODE == PR_NORM32) {
     const float* r = (p == 0) ? a.rank : a.comp;
     const float* rl = (p == 0) ? a.lo0 : a.lo1;
@@ -309,62 +322,116 @@ __device__ __forceinline__ double pr_finish(const PrArgs& a, uint64_t v, double 
     a.comp[v] = y - (t - rank_v);
     a.rank[v] = t;
     *rsum += (double)change;
-    if (change != 0.f && (double)fabsf(change) > a.delta_param * (double)t) {
-      uint32_t* fn = a.fa2 + (p ^ 1u) * a.nwords;
-      atomicOr(&fn[v >> 5], 1u << (v & 31));
-      atomicAdd(&a.ls->active[p ^ 1u], 1u);
-    }
+    // v stays active (contributes delta / outdeg next round) while |delta| > delta_param * rank
+    const bool act = change != 0.f && (double)fabsf(change) > a.delta_param * (double)t;
+    *nact += act ? 1u : 0u;
+    const uint32_t dg = a.deg[v];
+    a.contrib[(uint64_t)(p ^ 1u) * a.n + v] = (act && dg) ? change / (float)dg : 0.f;
     return fabs((double)change);
   }
 }
 
-// Warp-reduced residual and rank sum into the loop state (every lane calls it).
-__device__ __forceinline__ void pr_flush(LoopState* ls, unsigned p, double resid, double rsum) {
+// A thread's share of a round's totals: FP64 residual (sum of |change|), rank sum and
+// the vertices activated for the next round (PageRank-delta). Flushed once per block
+// (pr_tally_flush).
+struct PrTally {
+  double resid, rsum;
+  unsigned nact;
+  __device__ __forceinline__ void init() { resid = rsum = 0.0, nact = 0u; }
+};
+
+// Applies the finished sum of target v and adds its share to the tally. The fused form
+// also writes v's contribution to the next round (half p^1), exactly as the
+// contribution pass would compute it from the new delta.
+template <int MODE, bool PERSIST>
+__device__ __forceinline__ void pr_finish(const PrArgs& a, uint64_t v, double sum, unsigned p, double dang,
+                                          PrTally& t) {
+  t.resid += pr_apply<MODE, PERSIST>(a, v, sum, p, dang, &t.rsum, &t.nact);
+}
+
+// The block's tally into the loop state: one atomic per quantity and block (every
+// thread of the block calls it). Residual and rank sum of round p; the next round's
+// activations by parity p^1.
+template <int MODE>
+__device__ __forceinline__ void pr_tally_flush(LoopState* ls, unsigned p, PrTally t) {
+  __shared__ double s_r[32], s_s[32];
+  __shared__ unsigned s_n[32];
+  constexpr bool kN = pr_fused<MODE>();  // activations (PageRank-delta)
+  if (!kN) t.nact = 0u;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    resid += __shfl_xor_sync(0xFFFFFFFFu, resid, o);
-    rsum += __shfl_xor_sync(0xFFFFFFFFu, rsum, o);
+    t.resid += __shfl_xor_sync(0xFFFFFFFFu, t.resid, o);
+    t.rsum += __shfl_xor_sync(0xFFFFFFFFu, t.rsum, o);
+    if (kN) t.nact += __shfl_xor_sync(0xFFFFFFFFu, t.nact, o);
   }
+  const unsigned w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
   if ((threadIdx.x & 31) == 0) {
-    if (resid != 0.0) atomicAdd(&ls->resid[p], resid);
-    if (rsum != 0.0) atomicAdd(&ls->rank_sum[p], rsum);
+    s_r[w] = t.resid;
+    s_s[w] = t.rsum;
+    s_n[w] = t.nact;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0, sm = 0.0;
+    unsigned na = 0;
+    for (unsigned k = 0; k < nw; ++k) {
+      r += s_r[k];
+      sm += s_s[k];
+      na += s_n[k];
+    }
+    if (r != 0.0) atomicAdd(&ls->resid[p], r);
+    if (sm != 0.0) atomicAdd(&ls->rank_sum[p], sm);
+    if (kN && na) atomicAdd(&ls->active[p ^ 1u], na);
+  }
+  __syncthreads();
+}
+
+// One lane's ordered sum of the in-edges e0, e0 + stride, ... below hi into acc: the
+// source ids of B edges, then their B contributions in flight, the next B ids loaded
+// while those contributions arrive (one dependent L2 round trip per B edges).
+template <int MODE, bool PERSIST, int B, class Acc>
+__device__ __forceinline__ void pr_lane_sum(const PrArgs& a, const pr_val_t<MODE>* cr, uint32_t e0, uint32_t hi,
+                                            uint32_t stride, Acc& acc) {
+  // 32-bit edge indices: the CSC holds fewer than 2^32 - 2^20 edges (build_csx), so
+  // e + B * stride cannot wrap
+  uint32_t id[B];
+#pragma unroll
+  for (int k = 0; k < B; ++k) {
+    const uint32_t e = e0 + (uint32_t)k * stride;
+    id[k] = e < hi ? a.csc_src[e] : 0u;
+  }
+  for (uint32_t e = e0; e < hi; e += (uint32_t)B * stride) {
+    pr_val_t<MODE> c[B];
+#pragma unroll
+    for (int k = 0; k < B; ++k) {
+      const uint32_t ek = e + (uint32_t)k * stride;
+      c[k] = ek < hi ? pr_cval<MODE, PERSIST>(a, cr, ek, id[k]) : (pr_val_t<MODE>)0;
+    }
+    const uint32_t en = e + (uint32_t)B * stride;
+#pragma unroll
+    for (int k = 0; k < B; ++k) {
+      const uint32_t ek = en + (uint32_t)k * stride;
+      id[k] = ek < hi ? a.csc_src[ek] : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < B; ++k)
+      if (e + (uint32_t)k * stride < hi) acc.add(c[k]);
   }
 }
 
-// Sum of target v's in-edge contributions by one thread (in-degree <= 16): four
-// independent gathers in flight, accumulated in edge order.
+// Sum of target v's in-edge contributions by one thread (in-degree <= 4), in edge order.
 template <int MODE, bool PERSIST>
-__device__ __forceinline__ double pr_sum_thread(const PrArgs& a, uint32_t v) {
+__device__ __forceinline__ double pr_sum_thread(const PrArgs& a, const pr_val_t<MODE>* cr, uint32_t v) {
   const uint32_t lo = a.csc_ptr[v], hi = a.csc_ptr[v + 1];
   if constexpr (pr_is64<MODE>()) {
     Acc64 acc;
     acc.init();
-    uint32_t e = lo;
-    for (; e + 4 <= hi; e += 4) {
-      const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + 1], s2 = a.csc_src[e + 2], s3 = a.csc_src[e + 3];
-      const double c0 = pr_c64<MODE, PERSIST>(a, e, s0), c1 = pr_c64<MODE, PERSIST>(a, e + 1, s1),
-                   c2 = pr_c64<MODE, PERSIST>(a, e + 2, s2), c3 = pr_c64<MODE, PERSIST>(a, e + 3, s3);
-      acc.add(c0);
-      acc.add(c1);
-      acc.add(c2);
-      acc.add(c3);
-    }
-    for (; e < hi; ++e) acc.add(pr_c64<MODE, PERSIST>(a, e, a.csc_src[e]));
+    pr_lane_sum<MODE, PERSIST, 4>(a, cr, lo, hi, 1u, acc);
     return acc.value();
   } else {
     Acc32 acc;
     acc.init();
-    uint32_t e = lo;
-    for (; e + 4 <= hi; e += 4) {
-      const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + 1], s2 = a.csc_src[e + 2], s3 = a.csc_src[e + 3];
-      const float c0 = pr_c32<MODE, PERSIST>(a, e, s0), c1 = pr_c32<MODE, PERSIST>(a, e + 1, s1),
-                  c2 = pr_c32<MODE, PERSIST>(a, e + 2, s2), c3 = pr_c32<MODE, PERSIST>(a, e + 3, s3);
-      acc.add(c0);
-      acc.add(c1);
-      acc.add(c2);
-      acc.add(c3);
-    }
-    for (; e < hi; ++e) acc.add(pr_c32<MODE, PERSIST>(a, e, a.csc_src[e]));
+    pr_lane_sum<MODE, PERSIST, 4>(a, cr, lo, hi, 1u, acc);
     return (double)acc.s + (double)acc.e;
   }
 }
@@ -374,37 +441,21 @@ __device__ __forceinline__ double pr_sum_thread(const PrArgs& a, uint32_t v) {
 // group sums edges lo+gl, lo+gl+VW, ... in order, then the group merges its lanes by an
 // xor tree. Every lane of the group returns the sum.
 template <int MODE, bool PERSIST, int VW>
-__device__ __forceinline__ double pr_sum_group(const PrArgs& a, uint32_t lo, uint32_t hi, unsigned gl) {
+__device__ __forceinline__ double pr_sum_group(const PrArgs& a, const pr_val_t<MODE>* cr, uint32_t lo, uint32_t hi,
+                                               unsigned gl) {
+  constexpr int B = pr_is64<MODE>() ? 4 : 8;
   if constexpr (pr_is64<MODE>()) {
-    double s = 0.0;
-    uint32_t e = lo + gl;
-    for (; e + 3 * VW < hi; e += 4 * VW) {
-      const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + VW], s2 = a.csc_src[e + 2 * VW], s3 = a.csc_src[e + 3 * VW];
-      const double c0 = pr_c64<MODE, PERSIST>(a, e, s0), c1 = pr_c64<MODE, PERSIST>(a, e + VW, s1),
-                   c2 = pr_c64<MODE, PERSIST>(a, e + 2 * VW, s2), c3 = pr_c64<MODE, PERSIST>(a, e + 3 * VW, s3);
-      s += c0;
-      s += c1;
-      s += c2;
-      s += c3;
-    }
-    for (; e < hi; e += VW) s += pr_c64<MODE, PERSIST>(a, e, a.csc_src[e]);
+    Acc64 acc;
+    acc.init();
+    pr_lane_sum<MODE, PERSIST, B>(a, cr, lo + gl, hi, VW, acc);
+    double s = acc.s;
 #pragma unroll
     for (int o = VW / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o, VW);
     return s;
   } else {
     Acc32 acc;
     acc.init();
-    uint32_t e = lo + gl;
-    for (; e + 3 * VW < hi; e += 4 * VW) {
-      const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + VW], s2 = a.csc_src[e + 2 * VW], s3 = a.csc_src[e + 3 * VW];
-      const float c0 = pr_c32<MODE, PERSIST>(a, e, s0), c1 = pr_c32<MODE, PERSIST>(a, e + VW, s1),
-                  c2 = pr_c32<MODE, PERSIST>(a, e + 2 * VW, s2), c3 = pr_c32<MODE, PERSIST>(a, e + 3 * VW, s3);
-      acc.add(c0);
-      acc.add(c1);
-      acc.add(c2);
-      acc.add(c3);
-    }
-    for (; e < hi; e += VW) acc.add(pr_c32<MODE, PERSIST>(a, e, a.csc_src[e]));
+    pr_lane_sum<MODE, PERSIST, B>(a, cr, lo + gl, hi, VW, acc);
 #pragma unroll
     for (int o = VW / 2; o > 0; o >>= 1) {
       const float s2 = __shfl_xor_sync(0xFFFFFFFFu, acc.s, o, VW);
@@ -418,27 +469,17 @@ __device__ __forceinline__ double pr_sum_group(const PrArgs& a, uint32_t lo, uin
 // The same by a block of PR_BLOCK_T threads (in-degree > 4096: RMAT hubs); thread 0
 // returns the sum. Every thread of the block calls it.
 template <int MODE, bool PERSIST>
-__device__ __forceinline__ double pr_sum_block(const PrArgs& a, uint32_t v) {
+__device__ __forceinline__ double pr_sum_block(const PrArgs& a, const pr_val_t<MODE>* cr, uint32_t v) {
   __shared__ float s_s[PR_BLOCK_T / 32], s_e[PR_BLOCK_T / 32];
   __shared__ double s_d[PR_BLOCK_T / 32];
   const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const uint32_t lo = a.csc_ptr[v], hi = a.csc_ptr[v + 1];
   double sum = 0.0;
   if constexpr (pr_is64<MODE>()) {
-    double s = 0.0;
-    uint32_t e = lo + threadIdx.x;
-    for (; e + 3 * PR_BLOCK_T < hi; e += 4 * PR_BLOCK_T) {
-      const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + PR_BLOCK_T], s2 = a.csc_src[e + 2 * PR_BLOCK_T],
-                     s3 = a.csc_src[e + 3 * PR_BLOCK_T];
-      const double c0 = pr_c64<MODE, PERSIST>(a, e, s0), c1 = pr_c64<MODE, PERSIST>(a, e + PR_BLOCK_T, s1),
-                   c2 = pr_c64<MODE, PERSIST>(a, e + 2 * PR_BLOCK_T, s2),
-                   c3 = pr_c64<MODE, PERSIST>(a, e + 3 * PR_BLOCK_T, s3);
-      s += c0;
-      s += c1;
-      s += c2;
-      s += c3;
-    }
-    for (; e < hi; e += PR_BLOCK_T) s += pr_c64<MODE, PERSIST>(a, e, a.csc_src[e]);
+    Acc64 acc;
+    acc.init();
+    pr_lane_sum<MODE, PERSIST, 4>(a, cr, lo + threadIdx.x, hi, PR_BLOCK_T, acc);
+    double s = acc.s;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
     if (lane == 0) s_d[wid] = s;
@@ -449,19 +490,7 @@ __device__ __forceinline__ double pr_sum_block(const PrArgs& a, uint32_t v) {
   } else {
     Acc32 acc;
     acc.init();
-    uint32_t e = lo + threadIdx.x;
-    for (; e + 3 * PR_BLOCK_T < hi; e += 4 * PR_BLOCK_T) {
-      const uint32_t s0 = a.csc_src[e], s1 = a.csc_src[e + PR_BLOCK_T], s2 = a.csc_src[e + 2 * PR_BLOCK_T],
-                     s3 = a.csc_src[e + 3 * PR_BLOCK_T];
-      const float c0 = pr_c32<MODE, PERSIST>(a, e, s0), c1 = pr_c32<MODE, PERSIST>(a, e + PR_BLOCK_T, s1),
-                  c2 = pr_c32<MODE, PERSIST>(a, e + 2 * PR_BLOCK_T, s2),
-                  c3 = pr_c32<MODE, PERSIST>(a, e + 3 * PR_BLOCK_T, s3);
-      acc.add(c0);
-      acc.add(c1);
-      acc.add(c2);
-      acc.add(c3);
-    }
-    for (; e < hi; e += PR_BLOCK_T) acc.add(pr_c32<MODE, PERSIST>(a, e, a.csc_src[e]));
+    pr_lane_sum<MODE, PERSIST, 8>(a, cr, lo + threadIdx.x, hi, PR_BLOCK_T, acc);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       const float s2 = __shfl_xor_sync(0xFFFFFFFFu, acc.s, o);
@@ -485,46 +514,58 @@ __device__ __forceinline__ double pr_sum_block(const PrArgs& a, uint32_t v) {
 }
 
 // Ends a round: records the FP64 residual, decides whether to continue (one thread).
-__device__ __forceinline__ unsigned pr_control_step(LoopState* ls_, int mode) {
-  volatile LoopState* ls = ls_;
-  if (ls->cont) {
-    const unsigned p = ls->iter & 1u;
-    const double resid = ls->resid[p];
-    ls->resid_final = resid;
-    if (mode == PR_DELTA_RESIDUAL || mode == PR_DELTA_PUSH) {
-      ls->change_sum = ls->change_sum + ls->rank_sum[p];
-      ls->active_total = ls->active_total + ls->active[p ^ 1u];
-    }
-    ls->count_edges = ls->count_edges + ls->teps[0];
-    ls->edges_scanned = ls->edges_scanned + ls->teps[0];
-    ls->iter = ls->iter + 1;
-    const unsigned q = ls->iter & 1u;
-    bool more = ls->iter < ls->max_iter;
-    if (mode == PR_DELTA_RESIDUAL || mode == PR_DELTA_PUSH) {
-      const double total = ls->base_sum + ls->change_sum;
-      more = more && ls->active[q] > 0;
-      if (ls->tol > 0.0) more = more && resid > ls->tol * total;
-    } else {
-      more = more && resid > ls->tol;
-      // FP32 ranks cannot change by less than their rounding floor (about 6e-8 of the rank
-      // mass per round); once the FP64-measured change stops shrinking, the run is done
-      if (mode == PR_NORM32 || mode == PR_W32 || mode == PR_ADJ32) {
-        if (resid < ls->best_resid * 0.999) {
-          ls->best_resid = resid;
-          ls->stall = 0;
-        } else {
-          ls->stall = ls->stall + 1;
-          if (ls->stall >= 4) more = false;
-        }
+// Every value the step reads is loaded from L2 up front (one round trip; the other
+// blocks' totals are complete and visible when it runs), then the new state is stored.
+__device__ __forceinline__ unsigned pr_control_step(LoopState* ls, int mode) {
+  if (__ldcg(&ls->cont) == 0u) return 0u;
+  const unsigned iter = __ldcg(&ls->iter), max_iter = __ldcg(&ls->max_iter);
+  const double resid_p[2] = {__ldcg(&ls->resid[0]), __ldcg(&ls->resid[1])};
+  const double rsum_p[2] = {__ldcg(&ls->rank_sum[0]), __ldcg(&ls->rank_sum[1])};
+  const unsigned act_p[2] = {__ldcg(&ls->active[0]), __ldcg(&ls->active[1])};
+  const double change_sum = __ldcg(&ls->change_sum), base_sum = __ldcg(&ls->base_sum);
+  const double tol = __ldcg(&ls->tol), best = __ldcg(&ls->best_resid);
+  const unsigned long long active_total = __ldcg(&ls->active_total), count_edges = __ldcg(&ls->count_edges);
+  const unsigned long long edges_scanned = __ldcg(&ls->edges_scanned), teps0 = __ldcg(&ls->teps[0]);
+  const unsigned stall = __ldcg(&ls->stall);
+  const bool delta_mode = mode == PR_DELTA_RESIDUAL || mode == PR_DELTA_PUSH;
+
+  const unsigned p = iter & 1u, q = p ^ 1u;
+  const double resid = resid_p[p];
+  ls->resid_final = resid;
+  double cs = change_sum;
+  if (delta_mode) {
+    cs = change_sum + rsum_p[p];
+    ls->change_sum = cs;
+    ls->active_total = active_total + act_p[q];
+  }
+  ls->count_edges = count_edges + teps0;
+  ls->edges_scanned = edges_scanned + teps0;
+  ls->iter = iter + 1u;
+  bool more = iter + 1u < max_iter;
+  if (delta_mode) {
+    const double total = base_sum + cs;
+    more = more && act_p[q] > 0;
+    if (tol > 0.0) more = more && resid > tol * total;
+  } else {
+    more = more && resid > tol;
+    // FP32 ranks cannot change by less than their rounding floor (about 6e-8 of the rank
+    // mass per round); once the FP64-measured change stops shrinking, the run is done
+    if (mode == PR_NORM32 || mode == PR_W32 || mode == PR_ADJ32) {
+      if (resid < best * 0.999) {
+        ls->best_resid = resid;
+        ls->stall = 0;
+      } else {
+        ls->stall = stall + 1u;
+        if (stall + 1u >= 4) more = false;
       }
     }
-    ls->resid[q] = 0.0;
-    ls->dangling[q] = 0.0;
-    ls->active[q ^ 1u] = 0;
-    ls->rank_sum[q] = 0.0;
-    ls->cont = more ? 1u : 0u;
   }
-  return ls->cont;
+  ls->resid[q] = 0.0;
+  ls->dangling[q] = 0.0;
+  ls->active[p] = 0;
+  ls->rank_sum[q] = 0.0;
+  ls->cont = more ? 1u : 0u;
+  return more ? 1u : 0u;
 }
 
 }  // namespace cytom

@@ -34,7 +34,7 @@ extern "C" {
 #define CYTOM_ERR_RANGE (-3)         /* vertex id >= vertex count, negative id */
 #define CYTOM_ERR_TIMEOUT (-4)       /* a bounded device wait gave up */
 #define CYTOM_ERR_CUDA (-5)          /* CUDA runtime error */
-#define CYTOM_ERR_UNIMPLEMENTED (-6) /* not available in this build */
+#define CYTOM_ERR_UNIMPLEMENTED (-6) /* not implemented by the library */
 #define CYTOM_ERR_IO (-7)            /* file could not be read */
 
 /* Pointer location flags for buffers passed in or out. */

@@ -40,6 +40,18 @@
 
 namespace cytom {
 
+// The pulls of one round, every in-degree bin in one launch: bin k owns the virtual
+// blocks [first[k], first[k] + nblk[k]) and walks its targets with pr_bin_vw(k) lanes per
+// target (1: one thread, 0: one whole block). The heaviest bins take the lowest ids, so
+// their long-running blocks start first. The layout lives in device memory (one per CSC,
+// rewritten by each build) and the launch has a fixed grid that strides over the
+// virtual blocks, so a captured round loop stays valid when the bins change.
+struct PrBinLaunch {
+  uint64_t off[kPrBins], count[kPrBins];
+  uint32_t first[kPrBins], nblk[kPrBins];
+  uint32_t blocks;  // virtual blocks
+};
+
 // CSC of the compacted store, per job (PageRank family).
 struct Csc {
   uint32_t* src = nullptr;       // E: global source of each in-edge, grouped by target
@@ -47,6 +59,7 @@ struct Csc {
   uint32_t* deg_out = nullptr;   // n: distinct out-degree (stored edges)
   uint32_t* bins = nullptr;      // n: targets, small | medium | large
   uint64_t nb[kPrBins] = {};
+  PrBinLaunch* dbl = nullptr;    // the pull's bin layout (device)
   uint64_t E = 0;
   uint64_t cap = 0;
   uint64_t built_version = ~0ULL;
@@ -76,7 +89,8 @@ struct PrState {
   // captured round loops (one per round kind), rebuilt when their launch arguments change
   cudaGraphExec_t loop_exec[8] = {};
   PrArgs loop_args[8] = {};
-  uint64_t loop_nb[8][kPrBins] = {};
+  const PrBinLaunch* loop_bl[8] = {};
+  unsigned loop_grid[8] = {};
 };
 
 // Weighted graph of a context (WPAGERANK): CSC by target and CSR by source, both with
@@ -95,11 +109,12 @@ struct WGraph {
 // --------------------------------------------------------------------------
 // Sort keys of every stored edge u -> v in the renumbered ids u' = perm[u], v' = perm[v]:
 // (v', u') for the target-major CSC, (u', v') for the source-major CSR (by_source); the
-// edge's weight bits ride along (vals, weighted stores).
+// edge's weight bits ride along (vals, weighted stores). deg_out (target-major CSC): the
+// distinct out-degree of each source, one atomic per source and warp (store order keeps
+// a tile's edges grouped by source).
 __global__ void csc_keys_kernel(const StoreDesc* __restrict__ sd, const uint32_t* __restrict__ perm,
                                 uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
-                                uint32_t* __restrict__ deg_out, uint32_t* __restrict__ major_cnt, uint32_t lg_n,
-                                int by_source) {
+                                uint32_t* __restrict__ deg_out, uint32_t lg_n, int by_source) {
   const uint64_t E = sd->E;
   const uint32_t lT = sd->lT, lvpt = sd->lvpt;
   const uint32_t ymask = (uint32_t)(sd->T - 1);
@@ -112,37 +127,52 @@ __global__ void csc_keys_kernel(const StoreDesc* __restrict__ sd, const uint32_t
     const uint32_t v = perm[((t & ymask) << lvpt) | (p & 0xFFFFu)];
     keys[e] = by_source ? (((uint64_t)u << lg_n) | v) : (((uint64_t)v << lg_n) | u);
     if (vals) vals[e] = sd->wts[e];
-    if (deg_out) atomicAdd(&deg_out[u], 1u);
-    atomicAdd(&major_cnt[by_source ? u : v], 1u);
+    if (deg_out) {
+      const unsigned m = __match_any_sync(__activemask(), u);
+      if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) atomicAdd(&deg_out[u], (unsigned)__popc(m));
+    }
   }
 }
 
+// src[e] = the minor id of sorted key e; seg_lo / seg_hi[major] = the major's key range
+// [lo, hi), written by the range's first and last key (both stay 0 for a major without
+// keys) -- segment lengths without per-edge counters.
 __global__ void csc_src_kernel(const uint64_t* __restrict__ keys, uint64_t E, uint32_t lg_n,
-                               uint32_t* __restrict__ src) {
+                               uint32_t* __restrict__ src, uint32_t* __restrict__ seg_lo,
+                               uint32_t* __restrict__ seg_hi) {
   const uint64_t mask = (1ULL << lg_n) - 1ULL;
   uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += stride)
-    src[e] = (uint32_t)(keys[e] & mask);
-}
-
-// flag[v] = 1 when v's segment length falls in bin k (pr_bin_hi)
-__global__ void csc_class_kernel(const uint32_t* __restrict__ cnt, uint64_t n, int k, uint32_t* __restrict__ flag) {
-  const uint32_t lo = k ? pr_bin_hi(k - 1) : 0u, hi = pr_bin_hi(k);
-  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
-    const uint32_t d = cnt[v];
-    flag[v] = (k == 0 ? d <= hi : (d > lo && d <= hi)) ? 1u : 0u;
+  for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += stride) {
+    const uint64_t k = keys[e];
+    const uint64_t mj = k >> lg_n;
+    src[e] = (uint32_t)(k & mask);
+    if (e == 0 || (keys[e - 1] >> lg_n) != mj) seg_lo[mj] = (uint32_t)e;
+    if (e + 1 == E || (keys[e + 1] >> lg_n) != mj) seg_hi[mj] = (uint32_t)(e + 1);
   }
 }
 
-// bins[base_k + pos[v]] = v for the vertices of bin k; base_k = sizes of the bins before k
-__global__ void csc_bins_kernel(const uint32_t* __restrict__ flag, const uint32_t* __restrict__ pos,
-                                const uint32_t* __restrict__ tot, int k, uint64_t n, uint32_t* __restrict__ bins) {
-  uint64_t base = 0;
-  for (int b = 0; b < k; ++b) base += tot[b];
+// Per vertex v: cnt[v] = its segment length, binkey[v] = its in-degree bin (pr_bin_hi) and
+// vid[v] = v (vid may be seg_lo: each element is read before its own thread overwrites
+// it); tot[k] += the bin sizes (one atomic per bin and block).
+__global__ void csc_cnt_bins_kernel(const uint32_t* seg_lo, const uint32_t* __restrict__ seg_hi, uint64_t n,
+                                    uint32_t* __restrict__ cnt, uint64_t* __restrict__ binkey, uint32_t* vid,
+                                    uint32_t* __restrict__ tot) {
+  __shared__ unsigned s_tot[kPrBins];
+  if (threadIdx.x < kPrBins) s_tot[threadIdx.x] = 0;
+  __syncthreads();
   uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride)
-    if (flag[v]) bins[base + pos[v]] = (uint32_t)v;
+  for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
+    const uint32_t d = seg_hi[v] - seg_lo[v];
+    int k = 0;
+    while (k + 1 < kPrBins && d > pr_bin_hi(k)) ++k;
+    cnt[v] = d;
+    binkey[v] = (uint64_t)k;
+    vid[v] = (uint32_t)v;
+    const unsigned m = __match_any_sync(__activemask(), k);
+    if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) atomicAdd(&s_tot[k], (unsigned)__popc(m));
+  }
+  __syncthreads();
+  if (threadIdx.x < kPrBins && s_tot[threadIdx.x]) atomicAdd(&tot[threadIdx.x], s_tot[threadIdx.x]);
 }
 
 static int grid_n(Ctx* c, uint64_t work, int threads = 256, int per_sm = 8) {
@@ -160,6 +190,7 @@ static uint64_t store_version(Ctx* c) { return c->version; }
 // w != NULL the edges' weights are sorted along into *w (grown to hold E). Vertices are
 // binned by segment length for the pull (small / medium / large).
 static int pr_ensure_perm(Ctx* c);
+static PrBinLaunch bin_launch(Ctx* c, const uint64_t* nb);
 
 static int build_csx(Ctx* c, Csc& q, int by_source, float** w, uint64_t* wcap) {
   int prc = pr_ensure_perm(c);
@@ -184,7 +215,7 @@ static int build_csx(Ctx* c, Csc& q, int by_source, float** w, uint64_t* wcap) {
       return set_err(c, CYTOM_ERR_OOM, "CSC index");
   }
   char* tmp = nullptr;
-  const size_t kbytes = std::max<uint64_t>(E, 1) * 8;
+  const size_t kbytes = std::max<uint64_t>(std::max<uint64_t>(E, n), 1) * 8;
   const size_t vbytes = w ? std::max<uint64_t>(E, 1) * 4 : 0;
   const size_t nbytes = n * 4;
   if (cudaMallocAsync((void**)&tmp, 2 * kbytes + 2 * vbytes + 3 * nbytes + 64, c->stream) != cudaSuccess)
@@ -194,32 +225,33 @@ static int build_csx(Ctx* c, Csc& q, int by_source, float** w, uint64_t* wcap) {
   uint32_t* v0 = w ? (uint32_t*)(tmp + 2 * kbytes) : nullptr;
   uint32_t* v1 = w ? (uint32_t*)(tmp + 2 * kbytes + vbytes) : nullptr;
   uint32_t* cnt = (uint32_t*)(tmp + 2 * kbytes + 2 * vbytes);
-  uint32_t* flag = cnt + n;
-  uint32_t* pos = flag + n;
-  uint32_t* tot = pos + n;  // kPrBins totals
+  uint32_t* seg_lo = cnt + n;  // then the vertex ids the bin sort moves
+  uint32_t* seg_hi = seg_lo + n;
+  uint32_t* tot = seg_hi + n;  // kPrBins totals
   cudaMemsetAsync(q.deg_out, 0, n * 4, c->stream);
-  cudaMemsetAsync(cnt, 0, n * 4, c->stream);
+  cudaMemsetAsync(seg_lo, 0, 2 * nbytes + 64, c->stream);
   int rc = CYTOM_OK;
   if (E) {
     csc_keys_kernel<<<grid_n(c, E), 256, 0, c->stream>>>(c->dsd, c->pr_perm, k0, v0, by_source ? nullptr : q.deg_out,
-                                                         cnt, lg_n, by_source);
+                                                         lg_n, by_source);
     c->launches++;
     bool alt = false;
     rc = radix_sort_pairs(c, k0, k1, v0, v1, E, (int)(2 * lg_n), &alt);
     if (rc) return rc;
-    csc_src_kernel<<<grid_n(c, E), 256, 0, c->stream>>>(alt ? k1 : k0, E, lg_n, q.src);
+    csc_src_kernel<<<grid_n(c, E), 256, 0, c->stream>>>(alt ? k1 : k0, E, lg_n, q.src, seg_lo, seg_hi);
     c->launches++;
     if (w) cudaMemcpyAsync(*w, alt ? v1 : v0, E * 4, cudaMemcpyDeviceToDevice, c->stream);
   }
+  // segment lengths and bin keys, then the offsets and one stable 3-bit sort of the
+  // vertices by bin (vertex order kept inside each bin)
+  csc_cnt_bins_kernel<<<grid_n(c, n), 256, 0, c->stream>>>(seg_lo, seg_hi, n, cnt, k0, seg_lo, tot);
+  c->launches++;
   rc = exclusive_scan_u32(c, cnt, q.ptr, n, q.ptr + n);
   if (rc) return rc;
-  for (int k = 0; k < kPrBins; ++k) {
-    csc_class_kernel<<<grid_n(c, n), 256, 0, c->stream>>>(cnt, n, k, flag);
-    rc = exclusive_scan_u32(c, flag, pos, n, tot + k);
-    if (rc) return rc;
-    csc_bins_kernel<<<grid_n(c, n), 256, 0, c->stream>>>(flag, pos, tot, k, n, q.bins);
-    c->launches += 2;
-  }
+  bool balt = false;
+  rc = radix_sort_pairs(c, k0, k1, seg_lo, q.bins, n, 3, &balt);
+  if (rc) return rc;
+  if (!balt) cudaMemcpyAsync(q.bins, seg_lo, nbytes, cudaMemcpyDeviceToDevice, c->stream);
   uint32_t ht[kPrBins];
   cudaMemcpyAsync(ht, tot, sizeof(ht), cudaMemcpyDeviceToHost, c->stream);
   cudaFreeAsync(tmp, c->stream);
@@ -227,7 +259,11 @@ static int build_csx(Ctx* c, Csc& q, int by_source, float** w, uint64_t* wcap) {
   if (e != cudaSuccess) return cuda_err(c, e, "CSC build");
   for (int k = 0; k < kPrBins; ++k) q.nb[k] = ht[k];
   q.E = E;
-  return CYTOM_OK;
+  if (!q.dbl && cudaMalloc(&q.dbl, sizeof(PrBinLaunch)) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "CSC bins");
+  const PrBinLaunch hb = bin_launch(c, q.nb);
+  // pageable source: the call returns once the bytes are staged
+  e = cudaMemcpyAsync(q.dbl, &hb, sizeof(hb), cudaMemcpyHostToDevice, c->stream);
+  return e == cudaSuccess ? CYTOM_OK : cuda_err(c, e, "CSC bins");
 }
 
 static int build_csc(Ctx* c, Csc& q) { return build_csx(c, q, 0, nullptr, nullptr); }
@@ -316,16 +352,6 @@ __global__ void pr_contrib_kernel(PrArgs a) {
   pr_dangling_flush<MODE>(ls, p, dangling);
 }
 
-// The pulls of one round, every in-degree bin in one launch: bin k owns blocks
-// [first[k], first[k] + nblk[k]) and walks its targets with pr_bin_vw(k) lanes per target
-// (1: one thread, 0: one whole block). The heaviest bins take the lowest block ids, so
-// their long-running blocks start first.
-struct PrBinLaunch {
-  uint64_t off[kPrBins], count[kPrBins];
-  uint32_t first[kPrBins], nblk[kPrBins];
-  uint32_t blocks;  // the launch's grid (at least 1)
-};
-
 template <int MODE>
 __device__ __forceinline__ void pull_small_body(const PrArgs& a, const pr_val_t<MODE>* cr, unsigned p, double dang,
                                                 uint64_t bid, uint64_t nblk, PrTally& t) {
@@ -408,22 +434,24 @@ __device__ __forceinline__ void pr_round_end(LoopState* ls, int mode, cudaGraphC
 // Every block takes part in the round end of the fused forms, whether or not the run
 // still continues (a captured loop's condition is only set here).
 template <int MODE>
-__global__ void __launch_bounds__(PR_T) pr_pull_kernel(PrArgs a, PrBinLaunch bl, cudaGraphConditionalHandle h,
-                                                       int use_handle) {
+__global__ void __launch_bounds__(PR_T) pr_pull_kernel(PrArgs a, const PrBinLaunch* __restrict__ blp,
+                                                       cudaGraphConditionalHandle h, int use_handle) {
   LoopState* ls = a.ls;
   const bool live = ls->cont != 0;
   if (!live && !pr_fused<MODE>()) return;
   const unsigned p = ls->iter & 1u;
   PrTally t;
   t.init();
-  int k = 0;
-  while (k < kPrBins && !(blockIdx.x >= bl.first[k] && blockIdx.x - bl.first[k] < bl.nblk[k])) ++k;
-  if (live && k < kPrBins) {
-    const uint64_t bid = blockIdx.x - bl.first[k], nblk = bl.nblk[k];
-    a.bin_off = bl.off[k];
-    a.bin_count = bl.count[k];
-    const double dang = pr_dang_arg<MODE, false>(ls, p, a.n);
-    const pr_val_t<MODE>* cr = pr_cread<MODE>(a, p);
+  const uint32_t total = live ? blp->blocks : 0u;
+  const double dang = pr_dang_arg<MODE, false>(ls, p, a.n);
+  const pr_val_t<MODE>* cr = pr_cread<MODE>(a, p);
+  for (uint32_t vb = blockIdx.x; vb < total; vb += gridDim.x) {
+    int k = 0;
+    while (k < kPrBins && !(vb >= blp->first[k] && vb - blp->first[k] < blp->nblk[k])) ++k;
+    if (k == kPrBins) continue;
+    const uint64_t bid = vb - blp->first[k], nblk = blp->nblk[k];
+    a.bin_off = blp->off[k];
+    a.bin_count = blp->count[k];
     switch (pr_bin_vw(k)) {
       case 1: pull_small_body<MODE>(a, cr, p, dang, bid, nblk, t); break;
       case 4: pull_group_body<MODE, 4>(a, cr, p, dang, bid, nblk, t); break;
@@ -499,7 +527,7 @@ static Csc* ctx_csc(Ctx* c) {
 }
 
 static void csc_free(Csc* q) {
-  void* ptrs[] = {q->src, q->ptr, q->deg_out, q->bins};
+  void* ptrs[] = {q->src, q->ptr, q->deg_out, q->bins, q->dbl};
   for (void* p : ptrs)
     if (p) cudaFree(p);
 }
@@ -638,8 +666,27 @@ static PrBinLaunch bin_launch(Ctx* c, const uint64_t* nb) {
     bl.nblk[k] = (uint32_t)b;
     blocks += b;
   }
-  bl.blocks = (uint32_t)std::max<uint64_t>(blocks, 1);
+  bl.blocks = (uint32_t)blocks;
   return bl;
+}
+
+// The pull's grid. Fused form: as many blocks as fit on the device at once, striding
+// over the virtual blocks (a captured loop outlives changes of the bins; at least one
+// block, so the round end always runs). The others: one block per virtual block, which
+// the hardware balances (a persistent grid lost 5-10 % on RMAT-26 PageRank).
+template <int MODE>
+static unsigned pull_grid(Ctx* c, const Csc& q) {
+  if (!pr_fused<MODE>()) return std::max<uint32_t>(bin_launch(c, q.nb).blocks, 1u);
+  static int per_sm = -1;
+  if (per_sm < 0) {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pr_pull_kernel<MODE>, PR_T, 0) != cudaSuccess) {
+      cudaGetLastError();
+      b = 4;
+    }
+    per_sm = std::max(b, 1);
+  }
+  return (unsigned)(c->num_sms * per_sm);
 }
 
 // Whether a round of this form opens with a contribution pass: every round of the
@@ -654,19 +701,16 @@ static constexpr bool pr_opens_with_contrib() {
 // runs the control step), after the residual round's contribution pass; the others:
 // contributions -> pull -> control.
 template <int MODE>
-static int launch_round(Ctx* c, const PrArgs& base_args, const uint64_t* nb, bool first) {
+static int launch_round(Ctx* c, const PrArgs& base_args, const Csc& q, bool first) {
   PrArgs a = base_args;
   int launched = 0;
   if (!pr_fused<MODE>() || (first && pr_opens_with_contrib<MODE>())) {
     pr_contrib_kernel<MODE><<<grid_n(c, c->n), 256, 0, c->stream>>>(a);
     ++launched;
   }
-  const PrBinLaunch bl = bin_launch(c, nb);
   cudaGraphConditionalHandle h{};
-  if (pr_fused<MODE>() || bl.blocks) {
-    pr_pull_kernel<MODE><<<bl.blocks, PR_T, 0, c->stream>>>(a, bl, h, 0);
-    ++launched;
-  }
+  pr_pull_kernel<MODE><<<pull_grid<MODE>(c, q), PR_T, 0, c->stream>>>(a, q.dbl, h, 0);
+  ++launched;
   if (!pr_fused<MODE>()) {
     pr_control_kernel<<<1, 1, 0, c->stream>>>(a.ls, MODE, h, 0);
     ++launched;
@@ -689,7 +733,7 @@ static cudaError_t pr_add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cud
 // { pull, whose last block sets the condition }; the others: while(cont) { contributions
 // -> pull -> control, which sets the condition }.
 template <int MODE>
-static int build_round_graph(Ctx* c, const PrArgs& base, const uint64_t* nb, cudaGraphExec_t* out) {
+static int build_round_graph(Ctx* c, const PrArgs& base, const Csc& q, cudaGraphExec_t* out) {
   constexpr bool F = pr_fused<MODE>();
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaGraphCreate(&g, 0);
@@ -711,20 +755,21 @@ static int build_round_graph(Ctx* c, const PrArgs& base, const uint64_t* nb, cud
   if (e == cudaSuccess) e = cudaGraphAddNode(&wnode, g, pre ? &n_pre : nullptr, nullptr, pre ? 1 : 0, &cp);
   if (e == cudaSuccess) {
     cudaGraph_t body = cp.conditional.phGraph_out[0];
-    PrBinLaunch bl = bin_launch(c, nb);
+    const PrBinLaunch* blp = q.dbl;
+    const dim3 pg(pull_grid<MODE>(c, q));
     LoopState* ls = base.ls;
     int mode = MODE, one = 1;
-    void* a_p[] = {(void*)&a, (void*)&bl, (void*)&h, (void*)&one};
+    void* a_p[] = {(void*)&a, (void*)&blp, (void*)&h, (void*)&one};
     if (F) {
       cudaGraphNode_t n_p;
-      e = pr_add_kernel(body, &n_p, nullptr, 0, (void*)pr_pull_kernel<MODE>, dim3(bl.blocks), dim3(PR_T), a_p);
+      e = pr_add_kernel(body, &n_p, nullptr, 0, (void*)pr_pull_kernel<MODE>, pg, dim3(PR_T), a_p);
     } else {
       cudaGraphNode_t n_c, n_p, n_ctl;
       int zero = 0;
-      void* a_p0[] = {(void*)&a, (void*)&bl, (void*)&h, (void*)&zero};
+      void* a_p0[] = {(void*)&a, (void*)&blp, (void*)&h, (void*)&zero};
       e = pr_add_kernel(body, &n_c, nullptr, 0, (void*)pr_contrib_kernel<MODE>, dim3(grid_n(c, c->n)), dim3(256), a_c);
       if (e == cudaSuccess)
-        e = pr_add_kernel(body, &n_p, &n_c, 1, (void*)pr_pull_kernel<MODE>, dim3(bl.blocks), dim3(PR_T), a_p0);
+        e = pr_add_kernel(body, &n_p, &n_c, 1, (void*)pr_pull_kernel<MODE>, pg, dim3(PR_T), a_p0);
       void* a_ctl[] = {(void*)&ls, (void*)&mode, (void*)&h, (void*)&one};
       if (e == cudaSuccess)
         e = pr_add_kernel(body, &n_ctl, &n_p, 1, (void*)pr_control_kernel, dim3(1), dim3(1), a_ctl);
@@ -750,18 +795,20 @@ static bool pr_use_graphs() {
 }
 
 template <int MODE>
-static int run_rounds(Ctx* c, Job* j, const PrArgs& a, uint64_t max_rounds, const uint64_t* nb) {
+static int run_rounds(Ctx* c, Job* j, const PrArgs& a, uint64_t max_rounds, const Csc& q) {
   if (max_rounds > 1 && !c->profiling && pr_use_graphs()) {
     PrState* s = prs(j);
     cudaGraphExec_t& gx = s->loop_exec[MODE];
-    if (gx && (memcmp(&s->loop_args[MODE], &a, sizeof(PrArgs)) != 0 ||
-               memcmp(s->loop_nb[MODE], nb, sizeof(uint64_t) * kPrBins) != 0)) {
+    const unsigned grid = pull_grid<MODE>(c, q);
+    if (gx && (memcmp(&s->loop_args[MODE], &a, sizeof(PrArgs)) != 0 || s->loop_bl[MODE] != q.dbl ||
+               s->loop_grid[MODE] != grid)) {
       cudaGraphExecDestroy(gx);
       gx = nullptr;
     }
-    if (!gx && build_round_graph<MODE>(c, a, nb, &gx) == CYTOM_OK) {
+    if (!gx && build_round_graph<MODE>(c, a, q, &gx) == CYTOM_OK) {
       memcpy(&s->loop_args[MODE], &a, sizeof(PrArgs));
-      memcpy(s->loop_nb[MODE], nb, sizeof(uint64_t) * kPrBins);
+      s->loop_bl[MODE] = q.dbl;
+      s->loop_grid[MODE] = grid;
     }
     if (gx) {
       cudaError_t e = cudaGraphLaunch(gx, c->stream);
@@ -772,10 +819,11 @@ static int run_rounds(Ctx* c, Job* j, const PrArgs& a, uint64_t max_rounds, cons
   for (uint64_t r = 0; r < max_rounds;) {
     for (int k = 0; k < 8 && r < max_rounds; ++k, ++r) {
       int slot = prof_begin(c, KC_PAGERANK);
-      int rc = launch_round<MODE>(c, a, nb, r == 0);
+      int rc = launch_round<MODE>(c, a, q, r == 0);
       prof_end(c, slot, -1.0);
       if (rc) return rc;
     }
+    if (r >= max_rounds) break;  // the last round: nothing to check
     cudaError_t e = cudaMemcpyAsync(c->h_pinned, &a.ls->cont, 4, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_err(c, e, "pagerank loop");
@@ -832,17 +880,17 @@ int pagerank_run(Ctx* c, Job* j) {
     c->launches++;
     // Every run opens with the residual round (all sources contribute rank / outdeg):
     // exact after any change of the graph, and a no-op correction when nothing changed.
-    int rc = run_rounds<PR_DELTA_RESIDUAL>(c, j, a, 1, s->csc->nb);
+    int rc = run_rounds<PR_DELTA_RESIDUAL>(c, j, a, 1, *s->csc);
     if (rc) return rc;
     s->need_residual = false;
-    return run_rounds<PR_DELTA_PUSH>(c, j, a, max_iter, s->csc->nb);
+    return run_rounds<PR_DELTA_PUSH>(c, j, a, max_iter, *s->csc);
   }
   a.deg = s->csc->deg_out;
   if (j->params.kahan) {
-    int rc = run_rounds<PR_NORM32>(c, j, a, max_iter, s->csc->nb);
+    int rc = run_rounds<PR_NORM32>(c, j, a, max_iter, *s->csc);
     return rc;
   }
-  return run_rounds<PR_NORM64>(c, j, a, max_iter, s->csc->nb);
+  return run_rounds<PR_NORM64>(c, j, a, max_iter, *s->csc);
 }
 
 // Prepares a run of the batched executor: the snapshot's CSC, the loop state (and for
@@ -1035,8 +1083,8 @@ static int wpagerank_run(Ctx* c, Job* j) {
   pr_begin_kernel<<<1, 1, 0, c->stream>>>(j->ls, max_iter, j->params.tolerance, (unsigned long long)g->in.E);
   c->launches++;
   j->last_run_graph = false;
-  return j->params.kahan ? run_rounds<PR_W32>(c, j, a, max_iter, g->in.nb)
-                         : run_rounds<PR_W64>(c, j, a, max_iter, g->in.nb);
+  return j->params.kahan ? run_rounds<PR_W32>(c, j, a, max_iter, g->in)
+                         : run_rounds<PR_W64>(c, j, a, max_iter, g->in);
 }
 
 int pagerank_set_teleport(Ctx* c, Job* j, const double* t, int where) {
@@ -1201,7 +1249,7 @@ int pagerank_adjoint(Ctx* c, Job* j, const double* cv, int cwhere, float* d_w, f
   a.n = n;
   a.nwords = (n + 31) / 32;
   a.alpha = j->params.alpha;
-  int rc = f32 ? run_rounds<PR_ADJ32>(c, j, a, max_iter, g->out.nb) : run_rounds<PR_ADJ64>(c, j, a, max_iter, g->out.nb);
+  int rc = f32 ? run_rounds<PR_ADJ32>(c, j, a, max_iter, g->out) : run_rounds<PR_ADJ64>(c, j, a, max_iter, g->out);
   if (rc) return rc;
   LoopState als;
   e = cudaMemcpyAsync(&als, s->adj_ls, sizeof(LoopState), cudaMemcpyDeviceToHost, c->stream);

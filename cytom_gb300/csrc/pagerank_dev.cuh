@@ -443,7 +443,7 @@ __device__ __forceinline__ double pr_sum_thread(const PrArgs& a, const pr_val_t<
 template <int MODE, bool PERSIST, int VW>
 __device__ __forceinline__ double pr_sum_group(const PrArgs& a, const pr_val_t<MODE>* cr, uint32_t lo, uint32_t hi,
                                                unsigned gl) {
-  constexpr int B = pr_is64<MODE>() ? 4 : 8;
+  constexpr int B = 4;
   if constexpr (pr_is64<MODE>()) {
     Acc64 acc;
     acc.init();
@@ -490,7 +490,7 @@ __device__ __forceinline__ double pr_sum_block(const PrArgs& a, const pr_val_t<M
   } else {
     Acc32 acc;
     acc.init();
-    pr_lane_sum<MODE, PERSIST, 8>(a, cr, lo + threadIdx.x, hi, PR_BLOCK_T, acc);
+    pr_lane_sum<MODE, PERSIST, 4>(a, cr, lo + threadIdx.x, hi, PR_BLOCK_T, acc);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       const float s2 = __shfl_xor_sync(0xFFFFFFFFu, acc.s, o);

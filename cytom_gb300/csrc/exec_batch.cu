@@ -8,7 +8,8 @@
 //  - every job has a work queue for its current phase: the 4096-edge stages (dense
 //    round) or 256-item groups and 256-edge chunks (sparse round) of a gather, the
 //    1024-word ranges of an apply, the 4096-vertex ranges of a PageRank contribution
-//    pass and the target bins of its pull;
+//    pass (every PAGERANK round; PageRank-delta's residual round only, its delta rounds
+//    take the contributions the previous pull wrote) and the target bins of its pull;
 //  - a block claims a unit of any job with one 64-bit atomic on that job's claim word
 //    [phase : 8][units : 24][next unit : 32], so the phase and its size travel with the
 //    claim;

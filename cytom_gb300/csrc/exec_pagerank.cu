@@ -863,7 +863,6 @@ int pagerank_run(Ctx* c, Job* j) {
   a.contrib64 = s->contrib64;
   a.ls = j->ls;
   a.n = n;
-  a.nwords = (n + 31) / 32;
   a.alpha = j->params.alpha;
   a.delta_param = j->params.delta;
   a.base = (1.0 - j->params.alpha) / (double)n;
@@ -923,7 +922,6 @@ int pagerank_batch_prep(Ctx* c, Job* j, PrArgs* out, uint64_t* nb, int* first_mo
   a.contrib64 = s->contrib64;
   a.ls = j->ls;
   a.n = n;
-  a.nwords = (n + 31) / 32;
   a.alpha = j->params.alpha;
   a.delta_param = j->params.delta;
   a.base = (1.0 - j->params.alpha) / (double)n;
@@ -1068,7 +1066,6 @@ static PrArgs wargs(Ctx* c, Job* j, const WGraph& g) {
   a.contrib64 = s->contrib64;
   a.ls = j->ls;
   a.n = c->n;
-  a.nwords = (c->n + 31) / 32;
   a.alpha = j->params.alpha;
   return a;
 }
@@ -1247,7 +1244,6 @@ int pagerank_adjoint(Ctx* c, Job* j, const double* cv, int cwhere, float* d_w, f
   a.contrib64 = s->contrib64;
   a.ls = s->adj_ls;
   a.n = n;
-  a.nwords = (n + 31) / 32;
   a.alpha = j->params.alpha;
   int rc = f32 ? run_rounds<PR_ADJ32>(c, j, a, max_iter, g->out) : run_rounds<PR_ADJ64>(c, j, a, max_iter, g->out);
   if (rc) return rc;

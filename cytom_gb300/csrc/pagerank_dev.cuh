@@ -120,7 +120,6 @@ struct PrArgs {
   double* pt64;             // adjoint FP64
   LoopState* ls;
   uint64_t n;
-  uint64_t nwords;
   double alpha, delta_param, base;
 };
 

@@ -116,8 +116,15 @@ __device__ void unit_dense(const BJob* J, uint32_t st) {
   const unsigned p = ls_iter(jd->ls) & 1u;
   if (!stage_active<true>(jd, sd, st, p, J->adaptive)) return;
   const uint64_t e0 = (uint64_t)st * SG_E;
-  dense_stage<ALGO, true, true>(jd, sd, sd->edges + e0, mp_weighted<ALGO>() ? sd->wts + e0 : nullptr, st, p,
-                                J->adaptive);
+  // two half-stages of 8 edges per thread: the persistent kernel's register budget is
+  // set by its largest unit, and a 16-edge stage would cap it at two blocks per SM
+#pragma unroll 1
+  for (uint32_t h = 0; h < 2; ++h) {
+    const uint64_t st8 = 2ull * st + h, h0 = st8 * (SG_E / 2);
+    if (h0 >= sd->E) break;
+    dense_stage<ALGO, true, true, 8>(jd, sd, sd->edges + h0, mp_weighted<ALGO>() ? sd->wts + h0 : nullptr, st8, p,
+                                     J->adaptive);
+  }
   if (threadIdx.x == 0) {
     const uint64_t rem = sd->E - e0;
     atomicAdd(&jd->ls->edges_scanned, (unsigned long long)(rem < (uint64_t)SG_E ? rem : (uint64_t)SG_E));
@@ -359,7 +366,11 @@ __device__ void run_unit(const BJob* J, unsigned phase, uint32_t unit, int prmod
   }
 }
 
-__global__ void __launch_bounds__(BT, 2) batch_kernel(const BJob* __restrict__ jobs, BSched* sched, BCtl* ctl,
+// Four blocks per SM (64 registers, a few hundred bytes spilled): the job rounds are
+// latency-bound gathers, and warps in flight matter more than the spills (64 jobs over
+// RMAT-14..21 snapshots: 29 ms device time per job round at two blocks per SM, 22.7
+// at three, 19.6 at four; five spill 1.4 KB per thread).
+__global__ void __launch_bounds__(BT, 4) batch_kernel(const BJob* __restrict__ jobs, BSched* sched, BCtl* ctl,
                                                         int njobs) {
   __shared__ int s_job, s_state, s_last, s_mode;
   __shared__ unsigned s_unit, s_total, s_phase;
@@ -549,7 +560,7 @@ static int batch_run(Ctx* const* ctxs, const int* job_ids, int count, cytom_run_
   if (e != cudaSuccess) return cuda_err(c0, e, "batch upload");
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, BT, 0);
-  per_sm = std::max(1, std::min(per_sm, 2));
+  per_sm = std::max(1, std::min(per_sm, 4));
   const int grid = c0->num_sms * per_sm;
   cudaEventRecord(bb->a, st);
   if (left) {

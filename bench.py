@@ -1,19 +1,24 @@
 """Benchmark: streaming RMAT scale 22 on the tile store, BFS / CC / SSSP re-run
-incrementally after every batch.
+incrementally after every batch -- plus the other configured workloads as keys of the
+same JSON line.
 
-Workload (the GPU-sized streaming configuration): 4,194,304 vertices, RMAT graph500
-parameters, seed 2, uint32 weights uniform in [1, 255] (a pure function of
-(src, tgt)), batches of 1,048,576 edges inserted in generation order; after each
-batch the tile store is compacted and BFS (source 0), CC (min label) and SSSP
-(source 0) continue from their previous state to the new fixed point. One step =
-one batch: insert + compact + the three runs. 64 batches make the full 67,108,864-
-edge stream; the default run uses W = 3 warm-up batches and K = 61 timed batches.
+Headline workload: 4,194,304 vertices, RMAT graph500 parameters, seed 2, uint32 weights
+uniform in [1, 255] (a pure function of (src, tgt)), 64 batches of 1,048,576 edges
+inserted in generation order; after each batch the tile store is compacted and BFS
+(source 0), CC (min label) and SSSP (source 0) continue from their previous state to the
+new fixed point. One step = the whole 64-batch stream (67,108,864 edges) on a cleared
+context: every batch inserted, compacted and run. Inputs are generated on the device
+before the timed steps.
 
-Metric: GTEPS by the reference's counting rule (edges of tiles with an active
-source, summed over rounds and algorithms, algorithm-executor.h:424-426) per second
-of device time, plus ingest M edges/s. `value` times device-resident inputs;
-`e2e` feeds every batch from pinned host memory through the public C ABI and reads
-the per-run statistics back.
+Metric: GTEPS by the reference's counting rule (edges of tiles with an active source,
+summed over rounds and algorithms, algorithm-executor.h:424-426) per second of device
+time, ingest included, plus ingest M edges/s. `value` times device-resident inputs;
+`e2e` feeds every batch from pinned host memory through the public C ABI and reads the
+per-run statistics back.
+
+The other configured workloads run after the headline in the same process and appear
+under "workloads" (bench_workloads.py): the RMAT-16 PageRank-delta stream, the RMAT-26
+FP32-vs-FP64 PageRank, the 64-job batched executor and the RMAT-20 PageRank adjoint.
 """
 from __future__ import annotations
 
@@ -23,6 +28,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -32,36 +38,40 @@ sys.path.insert(0, str(ROOT))
 METRIC = "GTEPS & HBM GB/s per executor, M edges/s ingest; batched/FP32 vs plain at tol"
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=61)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="cytom", choices=["cytom", "reference"])
     ap.add_argument("--workload", default="streaming",
                     choices=["streaming", "prdelta", "precision", "batching", "adjoint"],
-                    help="streaming: RMAT-22 BFS/CC/SSSP stream (default); prdelta: RMAT-16 PageRank-delta "
-                         "stream; precision: RMAT-26 PageRank FP32-compensated vs FP64; batching: 64 jobs over "
-                         "8 snapshots, one persistent launch per job round vs one job per launch; adjoint: weighted "
-                         "PageRank RMAT-20 forward + adjoint with gradient checks")
+                    help="streaming: RMAT-22 BFS/CC/SSSP stream with every other workload as keys (default); "
+                         "the others print one workload alone: prdelta: RMAT-16 PageRank-delta stream; precision: "
+                         "RMAT-26 PageRank FP32-compensated vs FP64; batching: 64 jobs over 8 snapshots, one "
+                         "persistent launch per job round vs one job per launch; adjoint: weighted PageRank RMAT-20 "
+                         "forward + adjoint with gradient checks")
     ap.add_argument("--scale", type=int, default=22)
     ap.add_argument("--batch", type=int, default=1 << 20)
+    ap.add_argument("--batches", type=int, default=64, help="batches of one stream (one step)")
     ap.add_argument("--vpt", type=int, default=65536)
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--max-iter", type=int, default=100)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--profile-steps", type=int, default=4)
+    ap.add_argument("--no-workloads", action="store_true", help="headline stream only")
+    ap.add_argument("--profile-steps", type=int, default=4,
+                    help="batches at the end of the stream timed launch by launch for the roofline")
     ap.add_argument("--precision-scale", type=int, default=26)
     ap.add_argument("--profile-only", action="store_true",
-                    help="run preload, warm-up and --profile-steps batches with every launch timed and "
-                         "its algorithmic bytes recorded (host-driven rounds), print the per-class totals "
-                         "and exit: pairs with an ncu capture of the same command")
+                    help="run --batches batches once with every launch timed and its algorithmic bytes recorded "
+                         "(host-driven rounds), print the per-class totals and exit: pairs with an ncu capture "
+                         "of the same command")
     ap.add_argument("--programs", default="bfs,cc,sssp",
                     help="vertex programs run after every batch (profiling cases use a subset)")
     ap.add_argument("--preload", type=int, default=0,
-                    help="insert this many batches as one batch before the warm-up (profiling cases)")
-    return ap.parse_args()
+                    help="with --profile-only: insert this many batches as one batch first")
+    return ap.parse_args(argv)
 
 
 def dist_env():
@@ -85,10 +95,11 @@ def reduce_over_ranks(ms: float, edges: float, dev, world: int):
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling during the timed region (samples kept in a temporary file)."""
 
-    def __init__(self, path: Path, index: int):
-        self.path, self.index, self.proc = path, index, None
+    def __init__(self, index: int):
+        self.index, self.proc = index, None
+        self.path = Path(tempfile.mkstemp(prefix="cytom_clocks_", suffix=".csv")[1])
 
     def start(self):
         try:
@@ -123,17 +134,34 @@ class Clocks:
             for k, name in enumerate(names):
                 if f[5 + k].lower() == "active":
                     reasons.add(name)
+        try:
+            self.path.unlink()
+        except OSError:
+            pass
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(args, batches: int = 8) -> dict:
+def stream_config(args, pipelined: bool = True) -> dict:
+    """The headline workload, named identically by both arms."""
+    return {"workload": f"streaming RMAT-{args.scale}: {args.batches} batches of {args.batch} edges, compaction "
+                        f"+ incremental BFS/CC/SSSP after each batch; one step = the whole stream",
+            "vertices": 1 << args.scale, "vertices_per_tile": args.vpt, "batch_edges": args.batch,
+            "batches_per_step": args.batches, "max_iterations": args.max_iter,
+            "parallelism": "replicas" if dist_env()[1] > 1 else "1 GPU",
+            "l2": "inputs (805 MB per stream) and store larger than L2; flushed (256 MiB write) before every step"}
+
+
+def cpu_stream_baseline(args, batches: int, warm: int) -> dict:
     """The reference's own hot-path code (oracle/_ref, built from its sources; all host
-    threads as executors and appliers) on a bounded sample of the same workload: the
-    first `batches` batches of the stream, each inserted and compacted, then BFS / CC /
-    SSSP run on the snapshot (from scratch: the reference's incremental re-runs stop
-    after one round, so they are not used), counted by the reference's own rule.
-    Falls back to the single-thread oracle port when the reference cannot be built."""
+    threads as executors and appliers) on a bounded sample of the same stream: the first
+    `batches` batches, each inserted and compacted, then BFS / CC / SSSP continue
+    incrementally -- the reference's edgeChanged(INSERT) seeding and executeAlgorithm
+    (with its active-bitmap swap left out, which otherwise stops every incremental run
+    after one round). The first `warm` batches are untimed; value = processed edges of
+    the others (the reference's counting rule) over their insert + compaction + run time.
+    Falls back to the single-thread oracle port (from-scratch runs) when the reference
+    cannot be built."""
     from oracle import oracle as orc
     from oracle import ref_pin
     n = 1 << args.scale
@@ -141,50 +169,58 @@ def cpu_baseline(args, batches: int = 8) -> dict:
     s, t = orc.rmat(args.scale, 0, batches * args.batch, args.seed)
     w = orc.edge_weights(s, t, args.seed + 1000)
     if ref_pin.available():
-        r = ref_pin.run("stream", n, args.vpt, s, t, w, batch=args.batch, executors=min(cores, 255),
-                        max_iter=args.max_iter, start=0)
-        return {"value": r["count_edges"] / r["run_seconds"] / 1e9, "unit": "GTEPS", "cores": min(cores, 255),
-                "kind": "reference",
-                "sample": f"first {r['batches']} batches of the stream; after each, BFS/CC/SSSP run on the "
-                          f"snapshot by the reference executor ({min(cores, 255)} executors + appliers)",
-                "ingest_medges_per_s": batches * args.batch / r["insert_seconds"] / 1e6}
+        ex = min(cores, 255)
+        r = ref_pin.run("istream", n, args.vpt, s, t, w, batch=args.batch, executors=ex, max_iter=args.max_iter,
+                        start=0)
+        ce, ins, run = r["count_edges"][warm:], r["insert_seconds"][warm:], r["run_seconds"][warm:]
+        secs = float(ins.sum() + run.sum())
+        return {"value": float(ce.sum()) / secs / 1e9, "unit": "GTEPS", "cores": ex, "kind": "reference",
+                "sample": f"batches {warm + 1}-{batches} of the stream (after {warm} untimed), BFS/CC/SSSP "
+                          f"incremental after each, insert + compaction + runs timed, {ex} executors + appliers",
+                "run_only_gteps": float(ce.sum()) / float(run.sum()) / 1e9,
+                "ingest_medges_per_s": (batches - warm) * args.batch / float(ins.sum()) / 1e6 * 3,
+                "seconds": secs}
     st = orc.Store(n, args.vpt, weighted=True)
     total_edges, total_t = 0, 0.0
     for b in range(batches):
         sl = slice(b * args.batch, (b + 1) * args.batch)
+        t0 = time.perf_counter()
         st.insert(s[sl], t[sl], w[sl])
         st.compact()
-        t0 = time.perf_counter()
         for algo in (orc.BFS, orc.CC, orc.SSSP):
             _, info = st.run_minprop(algo, start=0, max_iter=args.max_iter)
-            total_edges += info["count_edges"]
-        total_t += time.perf_counter() - t0
+            if b >= warm:
+                total_edges += info["count_edges"]
+        if b >= warm:
+            total_t += time.perf_counter() - t0
     return {"value": total_edges / total_t / 1e9, "unit": "GTEPS", "cores": 1, "kind": "port",
-            "sample": f"first {batches} batches of the stream; BFS/CC/SSSP from scratch after each "
-                      f"(single-thread oracle port)"}
+            "sample": f"batches {warm + 1}-{batches} of the stream; BFS/CC/SSSP from scratch after each "
+                      f"(single-thread oracle port)", "seconds": total_t}
 
 
 def run_reference(args, rank):
+    """The reference arm: the reference's CPU path on the host cores, same config."""
     if rank != 0:
         return
     t0 = time.time()
-    cb = cpu_baseline(args, batches=max(2, min(16, (args.steps + args.warmup) // 8)))
+    batches = max(2, min(args.batches, args.warmup + args.steps))
+    warm = min(args.warmup, batches - 1)
+    cb = cpu_stream_baseline(args, batches, warm)
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "GTEPS",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * cb["seconds"] / max(1, batches - warm) * args.batches,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
-            "data": "synthetic RMAT (graph500 a,b,c), generated",
-            "config": {"workload": f"streaming RMAT-{args.scale}, {args.batch}-edge batches, "
-                                   "compaction + BFS/CC/SSSP after each batch",
-                       "vertices_per_tile": args.vpt},
+            "data": "synthetic RMAT (graph500 a,b,c), generated", "config": stream_config(args),
             "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
-            "ingest_medges_per_s": cb.get("ingest_medges_per_s"),
+            "run_only_gteps": cb.get("run_only_gteps"), "ingest_medges_per_s": cb.get("ingest_medges_per_s"),
             "e2e": {"value": cb["value"], "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "ms_per_step extrapolates the sampled batches' mean time to a whole stream",
             "wall_s": time.time() - t0}
     print(json.dumps(line), flush=True)
 
 
-def main():
-    args = parse()
+def main(argv=None):
+    args = parse(argv)
     rank, world, local = dist_env()
     if args.workload != "streaming":
         from bench_workloads import run_workload
@@ -204,145 +240,135 @@ def main():
     import cytom_gb300 as cg
 
     n = 1 << args.scale
-    B = args.batch
-    nsteps = args.preload + args.warmup + args.steps
+    B, NB = args.batch, args.batches
     stream = torch.cuda.Stream(device=dev)
-    out_dir = ROOT / "gpurun_out"
-    out_dir.mkdir(exist_ok=True)
+    prog_names = args.programs.split(",")
 
     def make_engine():
         eng = cg.Engine(n, args.vpt, weight_type=cg.WEIGHT_U32, stream=stream.cuda_stream)
         make = {"bfs": lambda: cg.BFS(eng, start_vertex=0, max_iterations=args.max_iter),
                 "cc": lambda: cg.CC(eng, max_iterations=args.max_iter),
                 "sssp": lambda: cg.SSSP(eng, start_vertex=0, max_iterations=args.max_iter)}
-        progs = [make[name]() for name in args.programs.split(",")]
-        return eng, progs
+        return eng, [make[name]() for name in prog_names]
 
-    # device-resident inputs for every step (generated by the library's RMAT kernel)
+    # device-resident inputs of one stream (generated by the library's RMAT kernel)
     eng, progs = make_engine()
-    d_src = torch.empty(nsteps * B, dtype=torch.int32, device=dev)
+    total_edges_in = (args.preload + NB) * B
+    d_src = torch.empty(total_edges_in + args.profile_steps * B, dtype=torch.int32, device=dev)
     d_tgt = torch.empty_like(d_src)
     d_w = torch.empty_like(d_src)
     with torch.cuda.stream(stream):
-        eng.generate_rmat(0, nsteps * B, args.scale, seed=args.seed, weight_seed=args.seed + 1000,
+        eng.generate_rmat(0, len(d_src), args.scale, seed=args.seed, weight_seed=args.seed + 1000,
                           wmin=1, wmax=255, out=(d_src, d_tgt, d_w))
     stream.synchronize()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > L2 (126 MB)
     with torch.cuda.stream(stream):
         flush.zero_()  # first launch outside the timed steps (the fill kernel may be JIT-compiled)
 
-    def step(e, ps, k, srcs):
-        s, t, w = srcs
-        e.insert_edges_device(s.data_ptr() + 4 * k * B, t.data_ptr() + 4 * k * B,
-                              w.data_ptr() + 4 * k * B, B)
-        e.do_global_compaction()
-        return e.run_many(ps)
+    def ins(e, k):
+        e.insert_edges_device(d_src.data_ptr() + 4 * k * B, d_tgt.data_ptr() + 4 * k * B,
+                              d_w.data_ptr() + 4 * k * B, B)
 
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
-           torch.cuda.Event(enable_timing=True)) for _ in range(nsteps)]
     if args.profile_only:
         eng.set_profiling(True)
-    if args.preload:
-        eng.insert_edges_device(d_src.data_ptr(), d_tgt.data_ptr(), d_w.data_ptr(), args.preload * B)
-        eng.do_global_compaction()
-    for k in range(args.preload, args.preload + args.warmup):
-        step(eng, progs, k, (d_src, d_tgt, d_w))
-    if args.profile_only:
-        for k in range(args.preload + args.warmup, nsteps):
-            step(eng, progs, k, (d_src, d_tgt, d_w))
+        if args.preload:
+            eng.insert_edges_device(d_src.data_ptr(), d_tgt.data_ptr(), d_w.data_ptr(), args.preload * B)
+            eng.do_global_compaction()
+        for k in range(args.preload, args.preload + NB):
+            ins(eng, k)
+            eng.do_global_compaction()
+            eng.run_many(progs)
         if rank == 0:
             print(json.dumps({"profile_only": True, "config": {"scale": args.scale, "batch": B,
-                                                               "steps": nsteps, "programs": args.programs},
+                                                               "batches": NB, "preload": args.preload,
+                                                               "programs": args.programs},
                               "kernel_stats": {k: v for k, v in eng.kernel_stats().items() if v["launches"]}}),
                   flush=True)
         eng.close()
         return
-    # streaming-gather shapes tuned once on the warmed-up graph (outside the timed steps)
-    tune = eng.autotune() if os.environ.get("CYTOM_AUTOTUNE", "1") != "0" else eng.tune_report()
+
+    def run_stream(e, ps, from_host=None):
+        """One step: the whole stream on a cleared context, pipelined -- batch k's jobs run
+        (cytom_run_many_async) while batch k+1 is inserted, sorted and merged into the
+        alternate buffers; the compaction waits for them only where it installs the merged
+        snapshot. Returns the run statistics of every batch."""
+        e.clear()
+        out = []
+        for k in range(NB):
+            if from_host is None:
+                ins(e, k)
+            else:
+                hs, ht, hw = from_host
+                sl = slice(k * B, (k + 1) * B)
+                e.insert_edges(hs[sl], ht[sl], hw[sl])  # H2D from pinned host buffers
+            e.do_global_compaction()
+            if k:
+                out.append(e.run_many_wait())  # the previous batch's statistics (D2H)
+            e.run_many_async(ps)
+        out.append(e.run_many_wait())
+        return out
+
+    # warm-up: the first step grows every buffer; the kernel shapes are tuned once on the
+    # full graph it leaves (outside the timed steps) and kept by the context
+    tune = None
+    for w_ in range(max(1, args.warmup)):
+        run_stream(eng, progs)
+        if w_ == 0:
+            tune = eng.autotune() if os.environ.get("CYTOM_AUTOTUNE", "1") != "0" else eng.tune_report()
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    clocks = Clocks(out_dir / f"clocks_rank{rank}.csv", local)
+    clocks = Clocks(local)
     clocks.start()
     launches0 = eng.launch_count()
-    teps_edges, scanned, ingest_ms, total_ms = 0, 0, 0.0, 0.0
+    teps_edges, scanned = 0, 0
     per_algo = [0] * len(progs)
     per_algo_ms = [0.0] * len(progs)
-
-    def account(stats):
-        nonlocal teps_edges, scanned
-        for i, s in enumerate(stats):
-            teps_edges += s["count_edges"]
-            scanned += s["edges_scanned"]
-            per_algo[i] += s["count_edges"]
-            per_algo_ms[i] += s["elapsed_ms"]
-
-    # Pipelined: batch k's jobs run (cytom_run_many_async) while batch k+1 is inserted,
-    # sorted and merged into the alternate buffers; the compaction waits for them only
-    # where it installs the merged snapshot. The timed region runs from the first insert
-    # to the last batch's job statistics, L2 flushes included.
-    pipelined = os.environ.get("CYTOM_PIPELINE", "1") != "0"
-    first = args.preload + args.warmup
     t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t_start.record(stream)
-    for k in range(first, nsteps):
+    for _ in range(args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()
-        a, b, c = ev[k]
-        a.record(stream)
-        eng.insert_edges_device(d_src.data_ptr() + 4 * k * B, d_tgt.data_ptr() + 4 * k * B,
-                                d_w.data_ptr() + 4 * k * B, B)
-        eng.do_global_compaction()
-        b.record(stream)
-        if pipelined:
-            if k > first:
-                account(eng.run_many_wait())  # the previous batch's jobs
-            eng.run_many_async(progs)  # the programs side by side, as the reference's jobs
-        else:
-            account(eng.run_many(progs))
-        c.record(stream)
-    if pipelined:
-        account(eng.run_many_wait())
+        for stats in run_stream(eng, progs):
+            for i, s in enumerate(stats):
+                teps_edges += s["count_edges"]
+                scanned += s["edges_scanned"]
+                per_algo[i] += s["count_edges"]
+                per_algo_ms[i] += s["elapsed_ms"]
     t_end.record(stream)
     torch.cuda.synchronize()
     launches = eng.launch_count() - launches0
     clk = clocks.stop()
     total_ms = t_start.elapsed_time(t_end)
-    for k in range(args.preload + args.warmup, nsteps):
-        a, b, c = ev[k]
-        ingest_ms += a.elapsed_time(b)
     if world > 1:
         torch.distributed.barrier()
     total_ms, teps_all = reduce_over_ranks(total_ms, teps_edges, dev, world)
     value = teps_all / (total_ms / 1e3) / 1e9
-    ingest_meps = world * args.steps * B / (ingest_ms / 1e3) / 1e6  # pipelined: replaced below
     final_edges = eng.count_edges()[0]
 
-    # ---- roofline pass: the gather kernel timed per launch with CUDA events on the
-    # engine's stream (profiling mode drives the loop from the host), on the next
-    # batches of the same stream
+    # ---- roofline pass: the last batches of the stream, every launch timed with CUDA
+    # events on the engine's stream (profiling mode drives the loop from the host)
+    prof_k = max(0, min(args.profile_steps, NB - 1))
+    eng.clear()
+    for k in range(NB - prof_k):
+        ins(eng, k)
+        eng.do_global_compaction()
+        eng.run_many(progs)
     eng.reset_kernel_stats()
     eng.set_profiling(True)
     prof_stats = []
-    extra = min(args.profile_steps, 64)
-    src_h, tgt_h, w_h = eng.generate_rmat(nsteps * B, extra * B, args.scale, seed=args.seed,
-                                          weight_seed=args.seed + 1000, wmin=1, wmax=255)
-    for k in range(extra):
+    for k in range(NB - prof_k, NB):
         with torch.cuda.stream(stream):
             flush.zero_()
-        sl = slice(k * B, (k + 1) * B)
-        eng.insert_edges(src_h[sl].copy(), tgt_h[sl].copy(), w_h[sl].copy())
+        ins(eng, k)
         eng.do_global_compaction()
         prof_stats.append([(i, p.execute_algorithm()) for i, p in enumerate(progs)])
     ks = eng.kernel_stats()
     eng.set_profiling(False)
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    prog_names = args.programs.split(",")
-    # Executor gather, both round kinds: the library attributes to every gather launch
-    # its algorithmic bytes (scanned edges + weights, one value per active source, a
-    # read and a reduction per changed target, the frontier bitmap or, in a sparse
-    # round, the listed frontier words and their directory entries).
+    peak_src = "MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks else "fallback 6800 GB/s"
+
     def _variant(k):
         v = ks[k]
         if not v["launches"] or v["total_ms"] <= 0:
@@ -351,13 +377,10 @@ def main():
         return {"launches": v["launches"], "avg_launch_us": v["total_ms"] * 1e3 / v["launches"],
                 "bytes_per_launch": v["algo_bytes"] / v["launches"], "achieved_gbs": gbs,
                 "frac": gbs / hbm_peak}
-    variants = {"dense_stream": _variant("gather"), "sparse_directory": _variant("gather_sparse")}
-    if pipelined:
-        # insert + sort + merge device time per batch in the profiling pass: with the jobs
-        # overlapped, the timed steps' insert-to-compaction time includes waiting for them
-        ing = sum(ks[k]["total_ms"] for k in ("insert", "sort", "merge") if k in ks)
-        if ing > 0 and extra:
-            ingest_meps = world * B / (ing / extra / 1e3) / 1e6
+
+    variants = {"dense": _variant("gather"), "sparse": _variant("gather_sparse")}
+    ing = sum(ks[k]["total_ms"] for k in ("insert", "sort", "merge") if k in ks)
+    ingest_meps = world * B / (ing / prof_k / 1e3) / 1e6 if (ing > 0 and prof_k) else None
     g_ms = ks["gather"]["total_ms"] + ks["gather_sparse"]["total_ms"]
     g_launches = ks["gather"]["launches"] + ks["gather_sparse"]["launches"]
     g_bytes = ks["gather"]["algo_bytes"] + ks["gather_sparse"]["algo_bytes"]
@@ -371,98 +394,81 @@ def main():
                                  "active_vertices_per_round": sum(st["active_vertices"] for st in runs) / rounds,
                                  "edges_scanned_per_round": sum(st["edges_scanned"] for st in runs) / rounds}
     # DRAM traffic per launch: the ncu-measured DRAM bytes per algorithmic byte of each
-    # round kind (profiles/gather_traffic_rmat22.md) times this run's algorithmic bytes
+    # round kind (a capture of this workload, committed beside the kernel summaries)
+    # times this run's algorithmic bytes
     traffic = None
     tfile = ROOT / "profiles" / "gather_traffic.json"
     if tfile.exists() and g_launches:
         try:
             ratio = json.loads(tfile.read_text())["dram_per_algorithmic_byte"]
-            traffic = (ratio["dense_stream"] * ks["gather"]["algo_bytes"]
-                       + ratio["sparse_directory"] * ks["gather_sparse"]["algo_bytes"]) / g_launches
+            traffic = (ratio["dense"] * ks["gather"]["algo_bytes"]
+                       + ratio["sparse"] * ks["gather_sparse"]["algo_bytes"]) / g_launches
         except Exception:
             traffic = None
 
-    # ---- end to end: a fresh engine fed from pinned host memory through the C ABI
+    # ---- end to end: a second context fed from pinned host memory through the C ABI
     e2e = None
     if not args.no_e2e:
         eng2, progs2 = make_engine()
-        hs = torch.empty(nsteps * B, dtype=torch.int32, pin_memory=True)
+        hs = torch.empty(NB * B, dtype=torch.int32, pin_memory=True)
         ht = torch.empty_like(hs)
         hw = torch.empty_like(hs)
-        hs.copy_(d_src.cpu())
-        ht.copy_(d_tgt.cpu())
-        hw.copy_(d_w.cpu())
-        hsn, htn, hwn = hs.numpy().view(np.uint32), ht.numpy().view(np.uint32), hw.numpy().view(np.uint32)
-        if args.preload:
-            sl = slice(0, args.preload * B)
-            eng2.insert_edges(hsn[sl], htn[sl], hwn[sl])
-            eng2.do_global_compaction()
-        for k in range(args.preload, args.preload + args.warmup):
-            sl = slice(k * B, (k + 1) * B)
-            eng2.insert_edges(hsn[sl], htn[sl], hwn[sl])
-            eng2.do_global_compaction()
-            eng2.run_many(progs2)
-        if os.environ.get("CYTOM_AUTOTUNE", "1") != "0":
-            eng2.autotune()
+        hs.copy_(d_src[:NB * B].cpu())
+        ht.copy_(d_tgt[:NB * B].cpu())
+        hw.copy_(d_w[:NB * B].cpu())
+        host = (hs.numpy().view(np.uint32), ht.numpy().view(np.uint32), hw.numpy().view(np.uint32))
+        for w_ in range(max(1, args.warmup)):
+            run_stream(eng2, progs2, host)
+            if w_ == 0 and os.environ.get("CYTOM_AUTOTUNE", "1") != "0":
+                eng2.autotune()
         torch.cuda.synchronize()
-        e_edges, e_ms = 0, 0.0
+        e_edges = 0
         e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e_start.record(stream)
-        for k in range(args.preload + args.warmup, nsteps):
+        for _ in range(args.steps):
             with torch.cuda.stream(stream):
                 flush.zero_()
-            sl = slice(k * B, (k + 1) * B)
-            eng2.insert_edges(hsn[sl], htn[sl], hwn[sl])  # H2D from pinned host buffers
-            eng2.do_global_compaction()
-            if pipelined:
-                if k > args.preload + args.warmup:
-                    e_edges += sum(s["count_edges"] for s in eng2.run_many_wait())  # statistics read back (D2H)
-                eng2.run_many_async(progs2)
-            else:
-                e_edges += sum(s["count_edges"] for s in eng2.run_many(progs2))
-        if pipelined:
-            e_edges += sum(s["count_edges"] for s in eng2.run_many_wait())
+            e_edges += sum(s["count_edges"] for stats in run_stream(eng2, progs2, host) for s in stats)
         e_end.record(stream)
         torch.cuda.synchronize()
         e_ms = e_start.elapsed_time(e_end)
-        e2e = {"value": world * e_edges / (e_ms / 1e3) / 1e9, "unit": "GTEPS",
-               "h2d_bytes_per_step": B * 12, "d2h_bytes_per_step": 3 * 160 + 16}
+        e_ms, e_all = reduce_over_ranks(e_ms, e_edges, dev, world)
+        e2e = {"value": e_all / (e_ms / 1e3) / 1e9, "unit": "GTEPS",
+               "h2d_bytes_per_step": NB * B * 12, "d2h_bytes_per_step": NB * len(progs) * 56}
         eng2.close()
+    eng.close()
+    del d_src, d_tgt, d_w, flush
+    torch.cuda.empty_cache()
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_baseline(args)
+        cpu = cpu_stream_baseline(args, batches=8, warm=2)
 
+    line = None
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": total_ms / max(1, args.steps), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32",
             "data": "synthetic RMAT (graph500 a,b,c), generated on the device",
-            "config": {"workload": f"streaming RMAT-{args.scale}: {args.batch}-edge batches, compaction "
-                                   f"+ incremental BFS/CC/SSSP after each batch",
-                       "vertices": n, "vertices_per_tile": args.vpt, "batch_edges": B,
-                       "max_iterations": args.max_iter, "parallelism": "replicas" if world > 1 else "1 GPU",
-                       "l2": "flushed (256 MiB write) before every timed step",
-                       "jobs": "BFS, CC and SSSP run side by side after each batch (cytom_run_many_async); "
-                               "the next batch's insert and merge overlap them" if pipelined else
-                               "BFS, CC and SSSP run side by side after each batch (cytom_run_many)"},
+            "config": stream_config(args),
             "ingest_medges_per_s": ingest_meps,
             # each job's edges over its own device time, measured while the jobs share the GPU
             "gteps_per_algorithm": {nm: per_algo[i] / (per_algo_ms[i] / 1e3) / 1e9 if per_algo_ms[i] else None
-                                    for i, nm in enumerate(args.programs.split(","))},
+                                    for i, nm in enumerate(prog_names)},
             "edges_scanned_per_s": scanned / (total_ms / 1e3),
+            "counting_note": "value counts whole tile rows with an active source (the reference's rule); "
+                             "edges_scanned_per_s counts the edges the kernels read",
             "final_edges": final_edges,
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": (achieved / hbm_peak) if achieved else None, "traffic": traffic,
-                         "kernel": "executor gather (gather_stream_kernel dense rounds + "
-                                   "gather_sparse_kernel/gather_sparse_chunks sparse rounds)",
+                         "kernel": "executor gather, dense + sparse rounds (gather_tiles_kernel / gather_sparse_*)",
                          "launches": g_launches,
                          "avg_launch_us": (g_ms * 1e3 / g_launches) if g_launches else None,
                          "bytes_per_launch": (g_bytes / g_launches) if g_launches else None,
-                         "variants": variants,
-                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
+                         "variants": variants, "peak_source": peak_src,
+                         "measured_on": f"batches {NB - prof_k + 1}-{NB} of the stream, launches timed one by one"},
             "kernel_time_ms": {k: v["total_ms"] for k, v in ks.items() if v["launches"]},
             "run_profile": run_profile,
             "autotune": tune,
@@ -470,8 +476,13 @@ def main():
             "e2e": e2e,
             "cpu_baseline": cpu,
         }
+    if world == 1 and not args.no_workloads:
+        from bench_workloads import all_workloads
+        wl = all_workloads(args, rank, world, local)
+        if line is not None:
+            line["workloads"] = wl
+    if rank == 0:
         print(json.dumps(line), flush=True)
-    eng.close()
     if world > 1:
         torch.distributed.destroy_process_group()
 

@@ -1,98 +1,149 @@
-"""Secondary benchmark workloads of bench.py (--workload prdelta | precision | batching | adjoint).
+"""The configured workloads beside the streaming headline of bench.py.
+
+Each function returns one dict (value, unit, ms_per_step, roofline, cpu_baseline and the
+workload's own checks); bench.py puts them under "workloads" of its JSON line, and
+`bench.py --workload NAME` prints one of them alone.
 
 prdelta: RMAT scale 16 (65,536 vertices, 1,048,576 edges, graph500 a,b,c, seed 1,
-    duplicates and self-loops kept) streamed in 16 batches of 65,536 edges in
-    generation order; after each batch the store is compacted and PageRank-delta
-    (alpha 0.85, FP32 ranks, delta 0) runs until the FP64 L1 residual <= 1e-7 of the
-    rank sum. One step = one batch. Errors are measured against the FP64 fixed point
-    of the final snapshot (CPU oracle).
+    duplicates and self-loops kept) streamed in 16 batches of 65,536 edges in generation
+    order into a store with 4,096 vertices per tile; after each batch PageRank-delta
+    (alpha 0.85, FP32 ranks, delta 0) runs until the FP64 L1 residual <= 1e-7 of the rank
+    sum. One step = the 16-batch stream. Errors against the FP64 fixed point of every
+    snapshot (CPU oracle).
 precision: RMAT scale 26 (67,108,864 vertices, 1,073,741,824 edges, seed 3); normalised
-    PageRank (alpha 0.85) in FP32 with compensated sums and in FP64 plain, both run to
-    an FP64-measured L1 residual of 1e-9. Errors of the FP32 form
-    are against the FP64 form (validated against the CPU FP64 oracle at smaller scales
-    by tests/test_gpu_pagerank.py). One step = one full PageRank solve.
+    PageRank (alpha 0.85) in FP32 with compensated sums and in FP64 plain, both run to an
+    FP64-measured L1 residual of 1e-9. One step = one full solve. Errors of the FP32 form
+    against the FP64 form.
+batching: 64 jobs over 8 snapshots (RMAT scales 14..21, edge factor 16, seeds 10..17,
+    uint32 weights in [1, 255]), 4 rounds of +5 % inserts; one persistent launch per job
+    round (cytom_run_batch) against one job per call (cytom_run).
+adjoint: weighted PageRank RMAT-20 forward to L1 1e-8 and its adjoint, checked against
+    FP64 central differences and the FP64 CPU adjoint.
 """
 from __future__ import annotations
 
 import json
 import os
 import time
+import traceback
+from pathlib import Path
 
 import numpy as np
 
 METRIC = "GTEPS & HBM GB/s per executor, M edges/s ingest; batched/FP32 vs plain at tol"
+ROOT = Path(__file__).resolve().parent
 
 
-def _line(args, world, value, ms_per_step, config, extra):
-    d = {"metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": world, "steps": args.steps,
-         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-         "vs_baseline": None, "dtype": "f32", "data": "synthetic RMAT (graph500 a,b,c), generated",
-         "config": config}
-    d.update(extra)
-    return d
+def _peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return float(json.loads(p.read_text()).get("hbm_gbs", 6800.0)), "MEASURED_PEAKS.json hbm_gbs (measured)"
+    return 6800.0, "fallback 6800 GB/s"
 
 
-def run_prdelta(args, rank, world, local):
+def _roofline(kernel: str, bytes_total: float, ms: float, launches: int, note: str) -> dict:
+    peak, src = _peak()
+    gbs = bytes_total / (ms / 1e3) / 1e9 if ms > 0 else None
+    return {"bound": "hbm", "kernel": kernel, "achieved": gbs, "peak": peak, "unit": "GB/s",
+            "frac": gbs / peak if gbs else None, "traffic": None, "launches": launches,
+            "bytes_per_launch": bytes_total / max(1, launches), "peak_source": src, "bytes_rule": note}
+
+
+# Algorithmic bytes of one PageRank round over a CSC of E edges and n vertices: per edge a
+# source id and a gathered contribution (4 B FP32, 8 B FP64); per vertex its CSC offset and
+# its state (FP32 pair ranks: read + write 16 B, contribution write 4 B, degree 4 B; FP64:
+# rank read + write 16 B, contribution 8 B, degree 4 B).
+def pr_round_bytes(E: int, n: int, fp64: bool) -> float:
+    return E * (4.0 + (8.0 if fp64 else 4.0)) + n * (4.0 + (28.0 if fp64 else 24.0))
+
+
+def prdelta(args, steps: int = 3, warmup: int = 1) -> dict:
     import torch
     import cytom_gb300 as cg
     from oracle import oracle as orc
     from oracle import ref_pin
     scale, vpt, B, nb = 16, 4096, 65536, 16
     n = 1 << scale
-    torch.cuda.set_device(local)
     stream = torch.cuda.Stream()
-    src, tgt = orc.rmat(scale, 0, B * nb, 1)
-    hs = torch.from_numpy(src.view(np.int32)).pin_memory()
-    ht = torch.from_numpy(tgt.view(np.int32)).pin_memory()
     eng = cg.Engine(n, vpt, stream=stream.cuda_stream)
-    p = cg.PageRankDelta(eng, delta=0.0, max_iterations=1000, tolerance=1e-7)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nb)]
-    edges = rounds = 0
-    ms = 0.0
-    for b in range(nb):
-        a, c = ev[b]
-        a.record(stream)
-        eng.insert_edges(hs[b * B:(b + 1) * B].numpy().view(np.uint32), ht[b * B:(b + 1) * B].numpy().view(np.uint32))
-        st = p.execute_algorithm()
-        c.record(stream)
-        torch.cuda.synchronize()
-        if b >= min(args.warmup, nb - 1):
+    s, t, _ = eng.generate_rmat(0, B * nb, scale, seed=1)
+    hs = torch.from_numpy(s.view(np.int32)).pin_memory()
+    ht = torch.from_numpy(t.view(np.int32)).pin_memory()
+    hsn, htn = hs.numpy().view(np.uint32), ht.numpy().view(np.uint32)
+    times, edges, rounds = [], 0, 0
+    errs = []
+    for step in range(warmup + steps):
+        eng.clear()
+        p = cg.PageRankDelta(eng, delta=0.0, max_iterations=1000, tolerance=1e-7)
+        last = step == warmup + steps - 1
+        st_or = orc.Store(n, vpt) if last else None
+        ms = 0.0
+        for b in range(nb):
+            a, c = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            eng.insert_edges(hsn[b * B:(b + 1) * B], htn[b * B:(b + 1) * B])  # H2D from pinned memory
+            st = p.execute_algorithm()  # compacts, then runs; statistics read back
+            c.record(stream)
+            torch.cuda.synchronize()
             ms += a.elapsed_time(c)
-            edges += st["count_edges"]
-            rounds += st["iterations"]
-    timed = nb - min(args.warmup, nb - 1)
-    got = p.result().astype(np.float64)
-    store = orc.Store(n, vpt)
-    store.insert(src, tgt)
-    store.compact()
-    ref, _ = store.pagerank_unnorm(tol=1e-14)
-    l1 = float(np.abs(got - ref).sum() / np.abs(ref).sum())
-    mr = float((np.abs(got - ref) / ref).max())
-    cpu = None
-    if rank == 0 and not args.no_cpu and ref_pin.available():
-        r = ref_pin.run("prdelta", n, vpt, src, tgt, None, batch=B, executors=1, max_iter=100, delta=0.0)
-        cpu = {"value": r["count_edges"] / r["seconds"] / 1e9, "unit": "GTEPS", "cores": 1, "kind": "reference",
-               "sample": "the reference PageRankDelta (1 executor, delta 0, 100 iterations) on the final snapshot"}
+            if step >= warmup:
+                edges += st["count_edges"]
+                rounds += st["iterations"]
+            if last:
+                st_or.insert(s[b * B:(b + 1) * B], t[b * B:(b + 1) * B])
+                st_or.compact()
+                ref, _ = st_or.pagerank_unnorm(tol=1e-14)
+                got = p.result().astype(np.float64)
+                errs.append((float(np.abs(got - ref).sum() / np.abs(ref).sum()), float((np.abs(got - ref) / ref).max())))
+        if step >= warmup:
+            times.append(ms)
+        p.destroy()
+    E = eng.count_edges()[0]
+    # roofline of the PageRank-delta rounds: one timed pass with every launch timed
+    eng.clear()
+    p = cg.PageRankDelta(eng, delta=0.0, max_iterations=1000, tolerance=1e-7)
+    eng.set_profiling(True)
+    eng.reset_kernel_stats()
+    prof_rounds, prof_bytes = 0, 0.0
+    for b in range(nb):
+        eng.insert_edges(hsn[b * B:(b + 1) * B], htn[b * B:(b + 1) * B])
+        eng.do_global_compaction()
+        e_now = eng.count_edges()[0]
+        st = p.execute_algorithm()
+        prof_rounds += st["iterations"]
+        # per round: every in-edge (4 B index + 4 B contribution) and per vertex 24 B of state
+        prof_bytes += st["iterations"] * (e_now * 8.0 + n * 24.0)
+    ks = eng.kernel_stats()
+    eng.set_profiling(False)
+    pr_ms = ks["pagerank"]["total_ms"]
     eng.close()
-    if rank == 0:
-        print(json.dumps(_line(args, world, edges / (ms / 1e3) / 1e9, ms / timed,
-                               {"workload": "PageRank-delta stream: RMAT-16, 16 batches of 65,536 edges, "
-                                            "update after each to FP64 L1 residual 1e-7",
-                                "vertices": n, "vertices_per_tile": vpt},
-                               {"l1_vs_fp64": l1, "max_rel_vs_fp64": mr, "rounds_per_update": rounds / timed,
-                                "cpu_baseline": cpu,
-                                "e2e": {"value": edges / (ms / 1e3) / 1e9, "unit": "GTEPS",
-                                        "h2d_bytes_per_step": B * 8, "d2h_bytes_per_step": 160}})), flush=True)
+    cpu = None
+    if ref_pin.available():
+        r = ref_pin.run("prdelta", n, vpt, s, t, None, batch=B, executors=1, max_iter=100, delta=0.0)
+        cpu = {"value": r["count_edges"] / r["seconds"] / 1e9, "unit": "GTEPS", "cores": 1, "kind": "reference",
+               "sample": "the reference PageRankDelta (1 executor: its multi-executor reduce races) on the final "
+                         "snapshot, delta 0, 100 iterations"}
+    ms_step = float(np.median(times))
+    timed = steps * nb
+    return {"value": edges / (sum(times) / 1e3) / 1e9, "unit": "GTEPS", "ms_per_step": ms_step, "steps": steps,
+            "step": "the 16-batch stream (insert from pinned host memory + compaction + update to tolerance)",
+            "config": {"workload": "PageRank-delta stream: RMAT-16 (seed 1), 16 batches of 65,536 edges, update "
+                                   "after each to FP64 L1 residual 1e-7 of the rank sum",
+                       "vertices": n, "vertices_per_tile": vpt, "delta": 0.0, "alpha": 0.85},
+            "dtype": "f32 ranks, FP64 residual", "ms_per_update": ms_step / nb, "rounds_per_update": rounds / timed,
+            "l1_vs_fp64_max_over_batches": max(e[0] for e in errs),
+            "max_rel_vs_fp64_max_over_batches": max(e[1] for e in errs),
+            "roofline": _roofline("PageRank-delta round (pr_pull_kernel, one launch per round)", prof_bytes, pr_ms,
+                                  ks["pagerank"]["launches"], "per round: in-edges x 8 B + vertices x 24 B"),
+            "final_edges": E, "cpu_baseline": cpu}
 
 
-def run_precision(args, rank, world, local):
+def precision(args, steps: int = 3, warmup: int = 1) -> dict:
     import torch
     import cytom_gb300 as cg
     scale = args.precision_scale
     vpt = 65536
-    n = 1 << scale
-    m = 16 << scale
-    torch.cuda.set_device(local)
+    n, m = 1 << scale, 16 << scale
     stream = torch.cuda.Stream()
     eng = cg.Engine(n, vpt, stream=stream.cuda_stream)
     chunk = 1 << 28
@@ -105,61 +156,65 @@ def run_precision(args, rank, world, local):
         eng.insert_edges(s[:cnt], t[:cnt])
         eng.do_global_compaction()
     del s, t
+    torch.cuda.empty_cache()
     build_s = time.time() - t0
+    E = eng.count_edges()[0]
     res = {}
     for kahan in (False, True):
-        tol = 1e-9  # both forms stop at the same FP64-measured L1 residual
-        prog = cg.PageRank(eng, max_iterations=1000, tolerance=tol, kahan=kahan)
-        prog.execute_algorithm()  # warm-up solve (builds the CSC)
+        prog = cg.PageRank(eng, max_iterations=1000, tolerance=1e-9, kahan=kahan)
         times, stats = [], None
-        for _ in range(max(args.steps, 1)):
+        for k in range(warmup + steps):
             prog.init_algorithm()
             a, c = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
             stats = prog.execute_algorithm()
             c.record(stream)
             torch.cuda.synchronize()
-            times.append(a.elapsed_time(c))
+            if k >= warmup:
+                times.append(a.elapsed_time(c))
         res[kahan] = {"ms": float(np.median(times)), "stats": stats,
                       "result": prog.result64() if not kahan else prog.result().astype(np.float64)}
         prog.destroy()
-    ref = res[False]["result"]
-    got = res[True]["result"]
+    eng.close()
+    ref, got = res[False]["result"], res[True]["result"]
     l1 = float(np.abs(got - ref).sum() / np.abs(ref).sum())
     mr = float((np.abs(got - ref) / ref).max())
-    E = eng.count_edges()[0]
-    fp32 = res[True]
-    fp64 = res[False]
-    value = E * fp32["stats"]["iterations"] / (fp32["ms"] / 1e3) / 1e9
-    eng.close()
-    if rank == 0:
-        print(json.dumps(_line(args, world, value, fp32["ms"],
-                               {"workload": f"PageRank precision: RMAT-{scale}, FP32-compensated vs FP64 plain",
-                                "vertices": n, "distinct_edges": E},
-                               {"fp32_ms": fp32["ms"], "fp64_ms": fp64["ms"], "fp32_over_fp64_speedup": fp64["ms"] / fp32["ms"],
-                                "fp32_iterations": fp32["stats"]["iterations"], "fp64_iterations": fp64["stats"]["iterations"],
-                                "fp64_final_l1_residual": fp64["stats"]["residual"],
-                                "fp32_final_l1_residual": fp32["stats"]["residual"],
-                                "fp32_l1_vs_fp64": l1, "fp32_max_rel_vs_fp64": mr, "graph_build_s": build_s,
-                                "e2e": None, "cpu_baseline": None})), flush=True)
+    fp32, fp64 = res[True], res[False]
+    it32, it64 = fp32["stats"]["iterations"], fp64["stats"]["iterations"]
+    return {"value": E * it32 / (fp32["ms"] / 1e3) / 1e9, "unit": "GTEPS (FP32-compensated solve)",
+            "ms_per_step": fp32["ms"], "steps": steps, "step": "one full solve to L1 residual 1e-9",
+            "config": {"workload": f"PageRank precision: RMAT-{scale} (seed 3), FP32-compensated vs FP64 plain, "
+                                   f"L1 residual 1e-9", "vertices": n, "distinct_edges": E},
+            "dtype": "f32 + compensation (FP64 residual and dangling sum) vs f64",
+            "fp32_ms": fp32["ms"], "fp64_ms": fp64["ms"], "fp32_over_fp64_speedup": fp64["ms"] / fp32["ms"],
+            "fp32_iterations": it32, "fp64_iterations": it64,
+            "fp64_final_l1_residual": fp64["stats"]["residual"], "fp32_final_l1_residual": fp32["stats"]["residual"],
+            "fp32_l1_vs_fp64": l1, "fp32_max_rel_vs_fp64": mr, "graph_build_s": build_s,
+            "roofline": {"fp32": _roofline("PageRank round, whole solve (contributions + pull + control)",
+                                           it32 * pr_round_bytes(E, n, False), fp32["ms"], it32,
+                                           "per round: in-edges x 8 B + vertices x 28 B"),
+                         "fp64": _roofline("PageRank round, whole solve (contributions + pull + control)",
+                                           it64 * pr_round_bytes(E, n, True), fp64["ms"], it64,
+                                           "per round: in-edges x 12 B + vertices x 32 B")},
+            "cpu_baseline": None,
+            "cpu_baseline_note": "the reference has no normalised FP32/FP64 PageRank path to time"}
 
 
-def run_batching(args, rank, world, local):
+def batching(args) -> dict:
     """64 jobs over 8 snapshots (RMAT scales 14..21, edge factor 16, seeds 10..17, uint32
     weights uniform in [1, 255]): 16 each of BFS (sources 0, 1), CC, SSSP (sources 0, 1)
     and PageRank (FP32 compensated, FP64 L1 tolerance 1e-8), 8 per snapshot. A job round
     runs every job; the first round computes from scratch, then each snapshot receives
     4 further insert batches of 5% of its edges with a job round after each. The batched
     arm runs each job round as ONE persistent launch (cytom_run_batch); the plain arm
-    runs each job by itself (cytom_run: one CUDA-graph launch per BFS/CC/SSSP run, a
-    host-driven round loop per PageRank run). Inserts and compactions are untimed and
-    identical in both arms; a job round is timed from the first call to the readback of
-    the last job's statistics. BFS/CC/SSSP results of the two arms are compared bit for
-    bit after every round."""
+    runs each job by itself (cytom_run: one CUDA-graph launch per BFS/CC/SSSP run and per
+    PageRank run). Inserts and compactions are untimed and identical in both arms; a job
+    round is timed from the first call to the readback of the last job's statistics.
+    BFS/CC/SSSP results of the two arms are compared bit for bit after every round."""
     import torch
     import cytom_gb300 as cg
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
+    from oracle import ref_pin
+    dev = torch.device("cuda")
     stream = torch.cuda.Stream(device=dev)
     scales, seeds, rounds = list(range(14, 22)), list(range(10, 18)), 4
     gen = cg.Engine(1 << 14, 4096, weight_type=cg.WEIGHT_U32, stream=stream.cuda_stream)
@@ -194,12 +249,8 @@ def run_batching(args, rank, world, local):
             e.insert_edges_device(s.data_ptr() + off, t.data_ptr() + off, w.data_ptr() + off, b)
             e.do_global_compaction()
 
-    per_kind = [0.0] * 8  # plain arm: wall time by job slot of a snapshot
-
-    def run_arm(batched, check_against=None):
+    def run_arm(batched):
         engs, progs = make_arm()
-        for k in range(8):
-            per_kind[k] = 0.0
         torch.cuda.synchronize()
         times, results, stats_all = [], [], []
         for r in range(rounds + 1):
@@ -210,57 +261,79 @@ def run_batching(args, rank, world, local):
             if batched:
                 st = cg.run_batch(progs)
             else:
-                st = []
-                for k, p in enumerate(progs):
-                    t1 = time.perf_counter()
-                    st.append(p.execute_algorithm())
-                    per_kind[k % 8] += time.perf_counter() - t1
+                st = [p.execute_algorithm() for p in progs]
             times.append(time.perf_counter() - t0)
             stats_all.append(st)
             results.append([p.result() for p in progs if not isinstance(p, cg.PageRank)])
         launches = sum(e.launch_count() for e in engs)
+        E = [e.count_edges()[0] for e in engs]
         for e in engs:
             e.close()
-        return times, results, stats_all, launches
+        return times, results, stats_all, launches, E
 
-    # warm-up pass of each arm (allocations, graph builds), then the timed passes
-    for _ in range(max(1, min(args.warmup, 1))):
-        run_arm(False)
-        run_arm(True)
-    tp, rp, sp, lp = run_arm(False)
-    plain_kind = list(per_kind)
-    tb, rb, sb, lb = run_arm(True)
+    run_arm(False)  # warm-up passes (allocations, graph builds)
+    run_arm(True)
+    tp, rp, sp, lp, _ = run_arm(False)
+    tb, rb, sb, lb, Es = run_arm(True)
     exact = all(np.array_equal(x, y) for ra, rb_ in zip(rp, rb) for x, y in zip(ra, rb_))
     njobs = len(sb[0])
-    minprop = [k for k in range(njobs) if k % 8 < 6]  # BFS, CC, SSSP jobs of each snapshot
+    minprop = [k for k in range(njobs) if k % 8 < 6]
     counts_equal = all(sa[k]["iterations"] == sb_[k]["iterations"] and sa[k]["count_edges"] == sb_[k]["count_edges"]
                        for sa, sb_ in zip(sp, sb) for k in minprop)
     jobs_b = njobs * (rounds + 1) / sum(tb)
     jobs_p = njobs * (rounds + 1) / sum(tp)
-    edges_b = sum(x["count_edges"] for st in sb for x in st)
-    if rank == 0:
-        line = _line(args, world, jobs_b, 1e3 * sum(tb) / (rounds + 1),
-                     {"workload": "batching: 64 jobs (16 each of BFS, CC, SSSP, PageRank) over 8 RMAT snapshots "
-                                  "(scales 14..21, edge factor 16, seeds 10..17), 4 rounds of +5% inserts",
-                      "jobs": njobs, "job_rounds": rounds + 1, "snapshot_scales": scales,
-                      "vertices_per_tile": "min(65536, vertices / 4)"},
-                     {"unit": "jobs/s", "dtype": "u32 (BFS/CC/SSSP), f32 (PageRank)",
-                      "batched_jobs_per_s": jobs_b, "plain_jobs_per_s": jobs_p,
-                      "batched_over_plain": jobs_b / jobs_p,
-                      "round_ms_batched": [1e3 * x for x in tb], "round_ms_plain": [1e3 * x for x in tp],
-                      "integer_results_bit_exact": bool(exact), "rounds_and_counts_equal": bool(counts_equal),
-                      "batched_gteps": edges_b / sum(tb) / 1e9,
-                      "batched_device_ms_per_round": [st[0]["elapsed_ms"] for st in sb],
-                      "pagerank_rounds_per_run": [[st[k]["iterations"] for k in range(njobs) if k % 8 == 6] for st in sb],
-                      "plain_ms_by_job_kind": dict(zip(["bfs0", "bfs1", "cc", "cc2", "sssp0", "sssp1", "pr", "pr2"],
-                                                       [1e3 * x for x in plain_kind])),
-                      "gpu_launches_batched_pass": lb, "gpu_launches_plain_pass": lp,
-                      "e2e": None, "cpu_baseline": None})
-        line["unit"] = "jobs/s"
-        print(json.dumps(line), flush=True)
+    # algorithmic bytes of the batched launches: per BFS/CC/SSSP job round the scanned
+    # edges (4 B, +4 B weight for SSSP), 12 B per activated vertex and the frontier bitmap;
+    # per PageRank round the FP32 CSC pull (pr_round_bytes)
+    byts = 0.0
+    for st in sb:
+        for k, x in enumerate(st):
+            snap = k // 8
+            n = 1 << scales[snap]
+            if k % 8 < 6:
+                wb = 4.0 if k % 8 >= 4 else 0.0
+                byts += x["edges_scanned"] * (4.0 + wb) + x["active_vertices"] * 12.0 + x["iterations"] * n / 8.0
+            else:
+                byts += x["iterations"] * pr_round_bytes(Es[snap], n, False)
+    dev_ms = sum(st[0]["elapsed_ms"] for st in sb)
+    cpu = None
+    if ref_pin.available():
+        # one reference job at a time (its own executor threads per job, jobs.h:79-83) on
+        # the four smallest snapshots' first round: BFS 0, CC, SSSP 0 and PageRank-delta
+        # (the reference's PageRank program) per snapshot
+        from oracle import oracle as orc
+        cores = min(os.cpu_count() or 1, 255)
+        secs, jobs = 0.0, 0
+        for scale, m, b, (s, t, w) in inputs[:4]:
+            n = 1 << scale
+            hs, ht, hw = (x[:m].cpu().numpy().view(np.uint32) for x in (s, t, w))
+            vpt = min(65536, n >> 2)
+            for mode, ex in (("bfs", cores), ("cc", cores), ("sssp", cores), ("prdelta", 1)):
+                r = ref_pin.run(mode, n, vpt, hs, ht, hw if mode == "sssp" else None, batch=m, executors=ex,
+                                max_iter=100, delta=0.01, start=0)
+                secs += r["seconds"]
+                jobs += 1
+        cpu = {"value": jobs / secs, "unit": "jobs/s", "cores": cores, "kind": "reference",
+               "sample": "one reference job at a time (BFS 0, CC, SSSP 0, PageRankDelta) on the first round of the "
+                         "four smallest snapshots (scales 14-17); run time only"}
+    return {"value": jobs_b, "unit": "jobs/s", "ms_per_step": 1e3 * sum(tb) / (rounds + 1), "steps": rounds + 1,
+            "step": "one job round: all 64 jobs", "dtype": "u32 (BFS/CC/SSSP), f32 (PageRank)",
+            "config": {"workload": "batching: 64 jobs (16 each of BFS, CC, SSSP, PageRank) over 8 RMAT snapshots "
+                                   "(scales 14..21, edge factor 16, seeds 10..17), 4 rounds of +5% inserts",
+                       "jobs": njobs, "job_rounds": rounds + 1, "snapshot_scales": scales,
+                       "vertices_per_tile": "min(65536, vertices / 4)"},
+            "batched_jobs_per_s": jobs_b, "plain_jobs_per_s": jobs_p, "batched_over_plain": jobs_b / jobs_p,
+            "round_ms_batched": [1e3 * x for x in tb], "round_ms_plain": [1e3 * x for x in tp],
+            "integer_results_bit_exact": bool(exact), "rounds_and_counts_equal": bool(counts_equal),
+            "batched_device_ms_per_round": [st[0]["elapsed_ms"] for st in sb],
+            "gpu_launches_batched_pass": lb, "gpu_launches_plain_pass": lp,
+            "roofline": _roofline("batch_kernel (persistent, all job phases)", byts, dev_ms, rounds + 1,
+                                  "BFS/CC/SSSP: scanned edges x (4 B + 4 B weight) + 12 B per activated vertex + "
+                                  "n/8 per round; PageRank: pr_round_bytes per round"),
+            "cpu_baseline": cpu}
 
 
-def run_adjoint(args, rank, world, local):
+def adjoint(args, steps: int = 3, warmup: int = 1) -> dict:
     """Weighted PageRank on RMAT scale 20 (1,048,576 vertices, 16,777,216 edges, seed 4),
     FP32 edge weights uniform in [0.1, 1.0] (a hash of (src, tgt)) normalised per source,
     damping 0.85, FP32-compensated forward to L1 residual 1e-8; L = c . r with c ~ N(0,1)
@@ -270,7 +343,6 @@ def run_adjoint(args, rank, world, local):
     import torch
     import cytom_gb300 as cg
     from oracle import oracle as orc
-    torch.cuda.set_device(local)
     stream = torch.cuda.Stream()
     scale, seed = 20, 4
     n, m = 1 << scale, 16 << 20
@@ -283,19 +355,18 @@ def run_adjoint(args, rank, world, local):
     c = np.random.default_rng(5).standard_normal(n)
     fwd = cg.WeightedPageRank(eng, max_iterations=1000, tolerance=1e-8, kahan=True)
     times, fst, ast = [], None, None
-    for k in range(max(args.warmup, 1) + max(args.steps, 1)):
+    for k in range(warmup + steps):
         fwd.init_algorithm()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         fst = fwd.execute_algorithm()
-        gw, gt, ast = fwd.adjoint(c)
-        if k >= max(args.warmup, 1):
+        gw, gt, ast = fwd.adjoint(c)  # c from host, gradients to host
+        if k >= warmup:
             times.append((time.perf_counter() - t0, fst["elapsed_ms"], ast["elapsed_ms"]))
     wall = float(np.median([x[0] for x in times]))
     fwd_ms = float(np.median([x[1] for x in times]))
     adj_ms = float(np.median([x[2] for x in times]))
     edges = fst["iterations"] * E + ast["iterations"] * E
-    # FP64 central differences on the GPU
     tp, ed, wb, _ = eng.dump_tiles(weights=True)
     T = n // 65536
     tiles = np.repeat(np.arange(len(tp) - 1, dtype=np.uint64), np.diff(tp).astype(np.int64))
@@ -319,7 +390,6 @@ def run_adjoint(args, rank, world, local):
         fd = (vals[0] - vals[1]) / step
         fd_err = max(fd_err, abs(fd - float(gw[e])) / max(abs(fd), 1e-2 * gmax))
     t_fd = time.perf_counter() - t_fd
-    # FP64 CPU adjoint (oracle) on every edge: the CPU baseline as well
     t_cpu = time.perf_counter()
     r_ref, it_f = orc.wpagerank(n, src, tgt, wst.astype(np.float64), tol=1e-8)
     _, gw_ref, gt_ref, it_a = orc.wpagerank_adjoint(n, src, tgt, wst.astype(np.float64), r_ref, c, tol=1e-8)
@@ -331,25 +401,48 @@ def run_adjoint(args, rank, world, local):
     r32 = fwd.result().astype(np.float64)
     l1 = float(np.abs(r32 - r_ref14).sum() / np.abs(r_ref14).sum())
     eng.close()
-    if rank == 0:
-        print(json.dumps(_line(args, world, edges / wall / 1e9, 1e3 * wall,
-                               {"workload": "differentiation: weighted PageRank RMAT-20 (16,777,216 edges, seed 4), "
-                                            "forward to L1 1e-8 + adjoint, c ~ N(0,1) seed 5",
-                                "vertices": n, "distinct_edges": E},
-                               {"unit": "GTEPS (forward + adjoint rounds x stored edges per second)",
-                                "forward_ms": fwd_ms, "adjoint_ms": adj_ms, "forward_rounds": fst["iterations"],
-                                "adjoint_rounds": ast["iterations"],
-                                "forward_gteps": fst["iterations"] * E / (fwd_ms / 1e3) / 1e9,
-                                "adjoint_gteps": ast["iterations"] * E / (adj_ms / 1e3) / 1e9,
-                                "grad_w_vs_central_diff_max_rel": fd_err, "central_diff_edges": 64,
-                                "central_diff_eps": eps, "central_diff_seconds": t_fd,
-                                "grad_w_vs_fp64_cpu_adjoint_max_rel": ew, "grad_t_vs_fp64_cpu_adjoint_max_rel": et,
-                                "forward_l1_vs_fp64": l1,
-                                "cpu_baseline": {"value": (it_f + it_a) * E / t_cpu / 1e9, "unit": "GTEPS", "cores": 1,
-                                                 "kind": "port",
-                                                 "sample": "the FP64 CPU forward (L1 1e-8) + adjoint on the same graph"},
-                                "e2e": {"value": edges / wall / 1e9, "unit": "GTEPS", "h2d_bytes_per_step": n * 8,
-                                        "d2h_bytes_per_step": E * 4 + n * 4 + 2 * 56}})), flush=True)
+    # per round of either solve: every edge's source id, weight and gathered value (12 B)
+    # and per vertex 32 B of state
+    byts = (fst["iterations"] + ast["iterations"]) * (E * 12.0 + n * 32.0)
+    return {"value": edges / wall / 1e9, "unit": "GTEPS (forward + adjoint rounds x stored edges per second)",
+            "ms_per_step": 1e3 * wall, "steps": steps, "step": "forward solve + adjoint solve + gradients to host",
+            "config": {"workload": "differentiation: weighted PageRank RMAT-20 (16,777,216 edges, seed 4), forward to "
+                                   "L1 1e-8 + adjoint, c ~ N(0,1) seed 5", "vertices": n, "distinct_edges": E},
+            "dtype": "f32 + compensation", "forward_ms": fwd_ms, "adjoint_ms": adj_ms,
+            "forward_rounds": fst["iterations"], "adjoint_rounds": ast["iterations"],
+            "grad_w_vs_central_diff_max_rel": fd_err, "central_diff_edges": 64, "central_diff_eps": eps,
+            "central_diff_seconds": t_fd, "grad_w_vs_fp64_cpu_adjoint_max_rel": ew,
+            "grad_t_vs_fp64_cpu_adjoint_max_rel": et, "forward_l1_vs_fp64": l1,
+            "roofline": _roofline("weighted PageRank rounds, forward + adjoint solves", byts, fwd_ms + adj_ms,
+                                  fst["iterations"] + ast["iterations"], "per round: edges x 12 B + vertices x 32 B"),
+            "cpu_baseline": {"value": (it_f + it_a) * E / t_cpu / 1e9, "unit": "GTEPS", "cores": 1, "kind": "port",
+                             "sample": "the FP64 CPU forward (L1 1e-8) + adjoint on the same graph (the reference "
+                                       "has no adjoint)"},
+            "e2e": {"value": edges / wall / 1e9, "unit": "GTEPS", "h2d_bytes_per_step": n * 8,
+                    "d2h_bytes_per_step": E * 4 + n * 4 + 2 * 56}}
+
+
+WORKLOADS = {"prdelta": prdelta, "precision": precision, "batching": batching, "adjoint": adjoint}
+KEYS = {"prdelta": "prdelta_rmat16", "precision": "precision_rmat26", "batching": "batching_64jobs",
+        "adjoint": "adjoint_rmat20"}
+
+
+def all_workloads(args, rank, world, local) -> dict:
+    """Every secondary workload in turn; a workload that fails reports its error and the
+    others still run."""
+    import torch
+    torch.cuda.set_device(local)
+    out = {}
+    for name, fn in WORKLOADS.items():
+        t0 = time.time()
+        try:
+            r = fn(args)
+        except Exception as e:  # reported in the line, not hidden
+            r = {"error": f"{type(e).__name__}: {e}", "trace": traceback.format_exc()[-1500:]}
+        r["wall_s"] = time.time() - t0
+        out[KEYS[name]] = r
+        torch.cuda.empty_cache()
+    return out
 
 
 def run_workload(args, rank, world, local):
@@ -358,11 +451,13 @@ def run_workload(args, rank, world, local):
             print(json.dumps({"impl": "reference", "unavailable": "secondary workloads are measured by the cytom arm; "
                               "the reference arm runs the default streaming workload"}))
         return
-    if args.workload == "prdelta":
-        run_prdelta(args, rank, world, local)
-    elif args.workload == "batching":
-        run_batching(args, rank, world, local)
-    elif args.workload == "adjoint":
-        run_adjoint(args, rank, world, local)
-    else:
-        run_precision(args, rank, world, local)
+    import torch
+    torch.cuda.set_device(local)
+    r = WORKLOADS[args.workload](args)
+    if rank == 0:
+        line = {"metric": METRIC, "value": r["value"], "unit": r["unit"], "n_gpus": world, "steps": r.get("steps"),
+                "warmup": 1, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": r.get("dtype"), "data": "synthetic RMAT (graph500 a,b,c), generated",
+                "config": r.get("config"), "roofline": r.get("roofline"), "cpu_baseline": r.get("cpu_baseline")}
+        line.update({k: v for k, v in r.items() if k not in line})
+        print(json.dumps(line), flush=True)

@@ -99,6 +99,10 @@ class TuneReport(C.Structure):
                 "tuned_edges": self.tuned_edges}
 
 
+class FaultInjection(C.Structure):
+    _fields_ = [("fail_alloc_after", C.c_uint64), ("idle_poll_limit", C.c_uint32), ("phantom_jobs", C.c_uint32)]
+
+
 # (name, restype, argtypes) of every exported entry point of include/cytom_gpu.h
 SIGNATURES = [
     ("cytom_config_default", None, [C.POINTER(Config)]),
@@ -114,6 +118,7 @@ SIGNATURES = [
     ("cytom_load_gridgraph", C.c_int, [C.c_void_p, C.c_char_p, C.c_uint64, C.POINTER(C.c_uint64)]),
     ("cytom_insert_batch", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int]),
     ("cytom_compact", C.c_int, [C.c_void_p]),
+    ("cytom_clear", C.c_int, [C.c_void_p]),
     ("cytom_count_edges", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     ("cytom_get_tiles", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("cytom_get_degrees", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -144,6 +149,7 @@ SIGNATURES = [
     ("cytom_reset_kernel_stats", C.c_int, [C.c_void_p]),
     ("cytom_launch_count", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
     ("cytom_sync", C.c_int, [C.c_void_p]),
+    ("cytom_set_fault_injection", C.c_int, [C.c_void_p, C.POINTER(FaultInjection)]),
     ("cytom_persist_edges", C.c_int, [C.c_void_p, C.c_char_p]),
     ("cytom_read_edges", C.c_int, [C.c_void_p, C.c_char_p, C.c_uint64, C.POINTER(C.c_uint64)]),
     ("cytom_write_results", C.c_int, [C.c_void_p, C.c_int, C.c_char_p]),

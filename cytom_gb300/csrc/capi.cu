@@ -6,6 +6,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <new>
 #include <string>
 #include <vector>
@@ -37,6 +38,17 @@ void pagerank_free(Job* j);
 __global__ void complement_kernel(const uint32_t* __restrict__ in, uint64_t n, uint32_t* __restrict__ out) {
   uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) out[i] = ~in[i];
+}
+
+// Fault injection: the allocation that turns the countdown from 1 to 0 fails.
+static std::atomic<uint64_t> g_alloc_countdown{0};
+
+bool alloc_fault_fires() {
+  uint64_t v = g_alloc_countdown.load(std::memory_order_relaxed);
+  while (v != 0) {
+    if (g_alloc_countdown.compare_exchange_weak(v, v - 1, std::memory_order_relaxed)) return v == 1;
+  }
+  return false;
 }
 
 int set_err(Ctx* c, int code, const std::string& msg) {
@@ -140,7 +152,7 @@ static bool is_minprop(int a) {
 }
 
 int job_alloc(Ctx* c, Job* j) {
-  cudaError_t e = cudaMalloc(&j->ls, sizeof(LoopState));
+  cudaError_t e = cy_malloc(&j->ls, sizeof(LoopState));
   if (e != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "loop state");
   cudaMemsetAsync(j->ls, 0, sizeof(LoopState), c->stream);
   j->h.ls = j->ls;
@@ -152,7 +164,7 @@ int job_alloc(Ctx* c, Job* j) {
   j->h.start = j->params.start_vertex;
   int rc = is_minprop(j->algo) ? minprop_alloc(c, j) : pagerank_alloc(c, j);
   if (rc) return rc;
-  e = cudaMalloc(&j->d, sizeof(JobDesc));
+  e = cy_malloc(&j->d, sizeof(JobDesc));
   if (e != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "job descriptor");
   e = cudaMemcpyAsync(j->d, &j->h, sizeof(JobDesc), cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
@@ -182,7 +194,7 @@ int ensure_job_queue(Ctx* c, Job* j) {
   j->h.spq = nullptr;
   j->h.spq_cap = 0;
   const uint64_t cap = need + need / 2;
-  if (cudaMalloc(&j->h.spq, cap * sizeof(uint2)) == cudaSuccess) {
+  if (cy_malloc(&j->h.spq, cap * sizeof(uint2)) == cudaSuccess) {
     j->h.spq_cap = cap;
   } else {
     cudaGetLastError();
@@ -458,13 +470,13 @@ int cytom_create(const cytom_config* cfg, cytom_ctx** out) {
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
   }
   bool ok = e == cudaSuccess;
-  ok = ok && cudaMalloc(&c->out_deg, n * 4) == cudaSuccess;
-  ok = ok && cudaMalloc(&c->in_deg, n * 4) == cudaSuccess;
-  ok = ok && cudaMalloc(&c->tile_ptr, (c->ntiles + 1) * 8) == cudaSuccess;
-  ok = ok && cudaMalloc(&c->tile_ptr_alt, (c->ntiles + 1) * 8) == cudaSuccess;
-  ok = ok && cudaMalloc(&c->dsd, sizeof(StoreDesc)) == cudaSuccess;
-  ok = ok && cudaMalloc(&c->d_flag, 64) == cudaSuccess;
-  ok = ok && cudaMallocHost(&c->h_pinned, 64) == cudaSuccess;
+  ok = ok && cy_malloc(&c->out_deg, n * 4) == cudaSuccess;
+  ok = ok && cy_malloc(&c->in_deg, n * 4) == cudaSuccess;
+  ok = ok && cy_malloc(&c->tile_ptr, (c->ntiles + 1) * 8) == cudaSuccess;
+  ok = ok && cy_malloc(&c->tile_ptr_alt, (c->ntiles + 1) * 8) == cudaSuccess;
+  ok = ok && cy_malloc(&c->dsd, sizeof(StoreDesc)) == cudaSuccess;
+  ok = ok && cy_malloc(&c->d_flag, 64) == cudaSuccess;
+  ok = ok && cy_malloc_host(&c->h_pinned, 64) == cudaSuccess;
   ok = ok && cudaEventCreate(&c->run_a) == cudaSuccess;
   ok = ok && cudaEventCreate(&c->run_b) == cudaSuccess;
   if (!ok) {
@@ -486,7 +498,7 @@ int cytom_create(const cytom_config* cfg, cytom_ctx** out) {
   c->chunk_cap = 0;
   {
     uint32_t* ct = nullptr;
-    if (cudaMalloc(&ct, 2 * 4) != cudaSuccess) rc = CYTOM_ERR_OOM;
+    if (cy_malloc(&ct, 2 * 4) != cudaSuccess) rc = CYTOM_ERR_OOM;
     c->chunk_tile = ct;
     c->chunk_cap = 2;
     if (ct) cudaMemsetAsync(ct, 0, 8, c->stream);
@@ -578,7 +590,7 @@ int cytom_rmat_generate(cytom_ctx* ctx, const cytom_rmat_params* p, uint64_t fir
   Staging st;
   st.s = c->stream;
   size_t per = (p->wmax > 0) ? 12 : 8;
-  if (cudaMallocAsync(&st.p, count * per, c->stream) != cudaSuccess)
+  if (cy_malloc_async(&st.p, count * per, c->stream) != cudaSuccess)
     return set_err(c, CYTOM_ERR_OOM, "rmat staging");
   uint32_t* ds = (uint32_t*)st.p;
   uint32_t* dt = ds + count;
@@ -601,7 +613,7 @@ int cytom_gridgraph_decode(cytom_ctx* ctx, const void* bytes, uint64_t size, uin
   Staging st;
   st.s = c->stream;
   size_t need = m * 8 + (where == CYTOM_PTR_HOST ? m * 8 : 0);
-  if (cudaMallocAsync(&st.p, need, c->stream) != cudaSuccess)
+  if (cy_malloc_async(&st.p, need, c->stream) != cudaSuccess)
     return set_err(c, CYTOM_ERR_OOM, "gridgraph staging");
   void* drec = st.p;
   cudaMemcpyAsync(drec, bytes, m * 8, cudaMemcpyHostToDevice, c->stream);
@@ -634,7 +646,7 @@ int cytom_insert_batch(cytom_ctx* ctx, const uint32_t* src, const uint32_t* tgt,
   Staging st;
   st.s = c->stream;
   bool wt = c->wtype != CYTOM_UNWEIGHTED && w;
-  if (cudaMallocAsync(&st.p, count * (wt ? 12 : 8), c->stream) != cudaSuccess)
+  if (cy_malloc_async(&st.p, count * (wt ? 12 : 8), c->stream) != cudaSuccess)
     return set_err(c, CYTOM_ERR_OOM, "insert staging");
   uint32_t* ds = (uint32_t*)st.p;
   uint32_t* dt = ds + count;
@@ -661,7 +673,7 @@ int cytom_load_gridgraph(cytom_ctx* ctx, const char* path, uint64_t batch, uint6
   uint64_t total = 0;
   int rc = CYTOM_OK;
   void* dev = nullptr;
-  if (cudaMalloc(&dev, batch * 16) != cudaSuccess) {
+  if (cy_malloc(&dev, batch * 16) != cudaSuccess) {
     fclose(f);
     return set_err(c, CYTOM_ERR_OOM, "gridgraph staging");
   }
@@ -697,6 +709,26 @@ int cytom_compact(cytom_ctx* ctx) {
   return prof_flush(c);
 }
 
+int cytom_clear(cytom_ctx* ctx) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c) return CYTOM_ERR_INVAL;
+  settle_runs(c);
+  cudaError_t e = cudaMemsetAsync(c->out_deg, 0, c->n * 4, c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->in_deg, 0, c->n * 4, c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->tile_ptr, 0, (c->ntiles + 1) * 8, c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->tile_ptr_alt, 0, (c->ntiles + 1) * 8, c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->chunk_tile, 0, 2 * 4, c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "clear");
+  c->E = 0;
+  c->A = 0;
+  c->version++;  // directory, PageRank structures and degree copies are rebuilt on use
+  for (Job* j : c->jobs)
+    if (j) j->fresh = true;
+  int rc = upload_store_desc(c);
+  if (rc) return rc;
+  return cuda_err(c, cudaStreamSynchronize(c->stream), "clear");
+}
+
 int cytom_count_edges(const cytom_ctx* ctx, uint64_t* compacted, uint64_t* pending) {
   const Ctx* c = (const Ctx*)ctx;
   if (!c) return CYTOM_ERR_INVAL;
@@ -720,7 +752,7 @@ int cytom_get_tiles(cytom_ctx* ctx, uint64_t* tile_ptr, uint32_t* edges, uint32_
   if (e != cudaSuccess) return cuda_err(c, e, "get_tiles");
   if (compact_flags) {
     uint8_t* d = nullptr;
-    if (cudaMalloc(&d, c->ntiles) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "flags");
+    if (cy_malloc(&d, c->ntiles) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "flags");
     int rc = compute_compact_flags(c, d);
     if (!rc) e = cudaMemcpyAsync(compact_flags, d, c->ntiles, cudaMemcpyDeviceToHost, c->stream);
     cudaStreamSynchronize(c->stream);
@@ -882,7 +914,7 @@ int cytom_get_result(cytom_ctx* ctx, int job_id, void* out, int where) {
   cudaError_t e = cudaSuccess;
   if (j->algo == CYTOM_ALGO_SSWP) {
     // SSWP runs on complemented values: widths = ~values
-    if (cudaMallocAsync((void**)&tmp, c->n * 4, c->stream) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "result");
+    if (cy_malloc_async((void**)&tmp, c->n * 4, c->stream) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "result");
     complement_kernel<<<(unsigned)std::min<uint64_t>((c->n + 255) / 256, (uint64_t)c->num_sms * 8), 256, 0,
                         c->stream>>>(src, c->n, tmp);
     c->launches++;
@@ -920,7 +952,7 @@ int cytom_set_edge_weights(cytom_ctx* ctx, const uint32_t* src, const uint32_t* 
   if (where == CYTOM_PTR_DEVICE || count == 0) return set_edge_weights(c, src, tgt, w, count);
   Staging st;
   st.s = c->stream;
-  if (cudaMallocAsync(&st.p, count * 12, c->stream) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "staging");
+  if (cy_malloc_async(&st.p, count * 12, c->stream) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "staging");
   uint32_t* ds = (uint32_t*)st.p;
   cudaMemcpyAsync(ds, src, count * 4, cudaMemcpyHostToDevice, c->stream);
   cudaMemcpyAsync(ds + count, tgt, count * 4, cudaMemcpyHostToDevice, c->stream);
@@ -937,7 +969,7 @@ int cytom_delete_batch(cytom_ctx* ctx, const uint32_t* src, const uint32_t* tgt,
   if (where == CYTOM_PTR_DEVICE || count == 0) return delete_edges(c, src, tgt, count, deleted);
   Staging st;
   st.s = c->stream;
-  if (cudaMallocAsync(&st.p, count * 8, c->stream) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "staging");
+  if (cy_malloc_async(&st.p, count * 8, c->stream) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "staging");
   uint32_t* ds = (uint32_t*)st.p;
   cudaMemcpyAsync(ds, src, count * 4, cudaMemcpyHostToDevice, c->stream);
   cudaMemcpyAsync(ds + count, tgt, count * 4, cudaMemcpyHostToDevice, c->stream);
@@ -954,7 +986,7 @@ int cytom_delete_random(cytom_ctx* ctx, uint64_t count, uint64_t seed, uint32_t*
   if (src && where == CYTOM_PTR_DEVICE) return delete_random(c, count, seed, src, tgt, deleted);
   Staging st;
   st.s = c->stream;
-  if (cudaMallocAsync(&st.p, count * 8, c->stream) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "staging");
+  if (cy_malloc_async(&st.p, count * 8, c->stream) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "staging");
   uint32_t* ds = (uint32_t*)st.p;
   int rc = delete_random(c, count, seed, ds, ds + count, deleted);
   if (rc || !src) return rc;
@@ -1034,6 +1066,15 @@ int cytom_launch_count(const cytom_ctx* ctx, uint64_t* launches) {
   const Ctx* c = (const Ctx*)ctx;
   if (!c || !launches) return CYTOM_ERR_INVAL;
   *launches = c->launches;
+  return CYTOM_OK;
+}
+
+int cytom_set_fault_injection(cytom_ctx* ctx, const cytom_fault_injection* f) {
+  Ctx* c = (Ctx*)ctx;
+  if (!c || !f) return CYTOM_ERR_INVAL;
+  g_alloc_countdown.store(f->fail_alloc_after, std::memory_order_relaxed);
+  c->inj_idle_limit = f->idle_poll_limit;
+  c->inj_phantom_jobs = f->phantom_jobs;
   return CYTOM_OK;
 }
 

@@ -205,7 +205,40 @@ struct Ctx {
   void* pr_csc = nullptr;
   void* pr_wgraph = nullptr;  // weighted PageRank: CSC + CSR with weights
   void* edge_log = nullptr;   // open edge log (cytom_persist_edges)
+  // fault injection (tests): batched executor's idle-wait limit (0 = default) and
+  // phantom unfinished jobs
+  uint32_t inj_idle_limit = 0;
+  uint32_t inj_phantom_jobs = 0;
 };
+
+// ---- allocation ----
+// Every device and pinned-host allocation of the library goes through these, so a test
+// can make the n-th one fail (cytom_set_fault_injection) without a real shortage.
+bool alloc_fault_fires();
+template <class T>
+inline cudaError_t cy_malloc(T** p, size_t bytes) {
+  if (alloc_fault_fires()) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMalloc(reinterpret_cast<void**>(p), bytes);
+}
+template <class T>
+inline cudaError_t cy_malloc_async(T** p, size_t bytes, cudaStream_t s) {
+  if (alloc_fault_fires()) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMallocAsync(reinterpret_cast<void**>(p), bytes, s);
+}
+template <class T>
+inline cudaError_t cy_malloc_host(T** p, size_t bytes) {
+  if (alloc_fault_fires()) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMallocHost(reinterpret_cast<void**>(p), bytes);
+}
 
 // ---- helpers (capi.cu) ----
 int set_err(Ctx* c, int code, const std::string& msg);

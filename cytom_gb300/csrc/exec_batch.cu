@@ -17,8 +17,9 @@
 //    counter) runs the job's control step — the same device code as the one-job
 //    executors (minprop_dev.cuh, pagerank_dev.cuh) — and publishes the next phase;
 //  - no block ever waits on another block: a block that finds no unit polls the claim
-//    words again (bounded: after kIdleLimit empty polls in a row it records a timeout
-//    and exits, so the launch always ends).
+//    words again (bounded: after kIdleLimit empty polls in a row -- or the limit a test
+//    sets through cytom_set_fault_injection -- it records a timeout and exits, so the
+//    launch always ends).
 // Values written during the launch are read through L2 (the PERSIST load policy).
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -82,6 +83,7 @@ struct BCtl {
   unsigned jobs_left;
   unsigned err;
   unsigned long long units;  // units processed (statistics)
+  unsigned idle_limit;       // empty polls before a block gives up
 };
 
 __host__ __device__ constexpr unsigned long long pack_claim(unsigned phase, unsigned total) {
@@ -402,7 +404,7 @@ __global__ void __launch_bounds__(BT, 4) batch_kernel(const BJob* __restrict__ j
         idle = 0;
       } else if (*(volatile unsigned*)&ctl->jobs_left == 0 || *(volatile unsigned*)&ctl->err != 0) {
         state = 2;
-      } else if (++idle > kIdleLimit) {
+      } else if (++idle > ctl->idle_limit) {
         atomicExch(&ctl->err, 1u);
         state = 2;
       } else {
@@ -540,19 +542,22 @@ static int batch_run(Ctx* const* ctxs, const int* job_ids, int count, cytom_run_
     bb->jobs = nullptr;
     bb->sched = nullptr;
     bb->cap = 0;
-    if (cudaMalloc(&bb->jobs, sizeof(BJob) * count) != cudaSuccess ||
-        cudaMalloc(&bb->sched, sizeof(BSched) * count) != cudaSuccess) {
+    if (cy_malloc(&bb->jobs, sizeof(BJob) * count) != cudaSuccess ||
+        cy_malloc(&bb->sched, sizeof(BSched) * count) != cudaSuccess) {
       cudaGetLastError();
       return set_err(c0, CYTOM_ERR_OOM, "batch tables");
     }
     bb->cap = count;
   }
-  if (!bb->ctl && cudaMalloc(&bb->ctl, sizeof(BCtl)) != cudaSuccess) {
+  if (!bb->ctl && cy_malloc(&bb->ctl, sizeof(BCtl)) != cudaSuccess) {
     cudaGetLastError();
     return set_err(c0, CYTOM_ERR_OOM, "batch control");
   }
   BCtl hctl{};
-  hctl.jobs_left = left;
+  // phantom jobs (fault injection) are counted as unfinished but never get work
+  const unsigned launch_left = left ? left + c0->inj_phantom_jobs : 0;
+  hctl.jobs_left = launch_left;
+  hctl.idle_limit = c0->inj_idle_limit ? c0->inj_idle_limit : kIdleLimit;
   cudaStream_t st = c0->stream;
   cudaError_t e = cudaMemcpyAsync(bb->jobs, hj.data(), sizeof(BJob) * count, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(bb->sched, hs.data(), sizeof(BSched) * count, cudaMemcpyHostToDevice, st);
@@ -563,7 +568,7 @@ static int batch_run(Ctx* const* ctxs, const int* job_ids, int count, cytom_run_
   per_sm = std::max(1, std::min(per_sm, 4));
   const int grid = c0->num_sms * per_sm;
   cudaEventRecord(bb->a, st);
-  if (left) {
+  if (launch_left) {
     batch_kernel<<<grid, BT, 0, st>>>(bb->jobs, bb->sched, bb->ctl, count);
     c0->launches++;
   }
@@ -575,8 +580,12 @@ static int batch_run(Ctx* const* ctxs, const int* job_ids, int count, cytom_run_
   float ms = 0.f;
   cudaEventElapsedTime(&ms, bb->a, bb->b);
   c0->batch_units += hctl.units;
-  if (hctl.err == 1) return set_err(c0, CYTOM_ERR_TIMEOUT, "batched executor: a block found no work for too long");
-  if (hctl.err) return set_err(c0, CYTOM_ERR_RANGE, "batched executor: a phase exceeds the unit limit");
+  if (hctl.err) {
+    // the launch ended with jobs in mid-round: they restart from scratch on their next run
+    for (int k = 0; k < count; ++k) jobs[k]->fresh = true;
+    if (hctl.err == 1) return set_err(c0, CYTOM_ERR_TIMEOUT, "batched executor: a block found no work for too long");
+    return set_err(c0, CYTOM_ERR_RANGE, "batched executor: a phase exceeds the unit limit");
+  }
   for (int k = 0; k < count; ++k) {
     Ctx* c = ctxs[k];
     Job* j = jobs[k];

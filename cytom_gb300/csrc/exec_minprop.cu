@@ -526,12 +526,12 @@ int minprop_alloc(Ctx* c, Job* j) {
   const uint64_t n = c->n;
   const uint64_t nwords = (n + 31) / 32;
   JobDesc& h = j->h;
-  cudaError_t e = cudaMalloc(&h.cur, n * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&h.next, n * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&h.fa, nwords * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&h.ch, nwords * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&h.rows, 2 * c->T * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&h.aw, nwords * 4);
+  cudaError_t e = cy_malloc(&h.cur, n * 4);
+  if (e == cudaSuccess) e = cy_malloc(&h.next, n * 4);
+  if (e == cudaSuccess) e = cy_malloc(&h.fa, nwords * 4);
+  if (e == cudaSuccess) e = cy_malloc(&h.ch, nwords * 4);
+  if (e == cudaSuccess) e = cy_malloc(&h.rows, 2 * c->T * 4);
+  if (e == cudaSuccess) e = cy_malloc(&h.aw, nwords * 4);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return set_err(c, CYTOM_ERR_OOM, "job state");
@@ -926,7 +926,7 @@ int minprop_autotune(Ctx* c) {
   JobDesc* d = nullptr;
   char* buf = nullptr;
   const size_t bytes = n * 8 + nwords * 8 + 2 * c->T * 4 + nwords * 4 + sizeof(LoopState) + sizeof(JobDesc) + 4096;
-  if (cudaMallocAsync((void**)&buf, bytes, c->stream) != cudaSuccess) {
+  if (cy_malloc_async((void**)&buf, bytes, c->stream) != cudaSuccess) {
     cudaGetLastError();
     return CYTOM_OK;  // no memory to tune with: keep the current shapes
   }

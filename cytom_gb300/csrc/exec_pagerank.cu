@@ -202,23 +202,23 @@ static int build_csx(Ctx* c, Csc& q, int by_source, float** w, uint64_t* wcap) {
   if (E > q.cap || !q.src) {
     cudaFree(q.src);
     q.cap = std::max<uint64_t>(E + E / 4, 1024);
-    if (cudaMalloc(&q.src, q.cap * 4) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "CSC");
+    if (cy_malloc(&q.src, q.cap * 4) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "CSC");
   }
   if (w && (E > *wcap || !*w)) {
     cudaFree(*w);
     *wcap = std::max<uint64_t>(E + E / 4, 1024);
-    if (cudaMalloc(w, *wcap * 4) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "CSC weights");
+    if (cy_malloc(w, *wcap * 4) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "CSC weights");
   }
   if (!q.ptr) {
-    if (cudaMalloc(&q.ptr, (n + 1) * 4) != cudaSuccess || cudaMalloc(&q.deg_out, n * 4) != cudaSuccess ||
-        cudaMalloc(&q.bins, n * 4) != cudaSuccess)
+    if (cy_malloc(&q.ptr, (n + 1) * 4) != cudaSuccess || cy_malloc(&q.deg_out, n * 4) != cudaSuccess ||
+        cy_malloc(&q.bins, n * 4) != cudaSuccess)
       return set_err(c, CYTOM_ERR_OOM, "CSC index");
   }
   char* tmp = nullptr;
   const size_t kbytes = std::max<uint64_t>(std::max<uint64_t>(E, n), 1) * 8;
   const size_t vbytes = w ? std::max<uint64_t>(E, 1) * 4 : 0;
   const size_t nbytes = n * 4;
-  if (cudaMallocAsync((void**)&tmp, 2 * kbytes + 2 * vbytes + 3 * nbytes + 64, c->stream) != cudaSuccess)
+  if (cy_malloc_async((void**)&tmp, 2 * kbytes + 2 * vbytes + 3 * nbytes + 64, c->stream) != cudaSuccess)
     return set_err(c, CYTOM_ERR_OOM, "CSC temporaries");
   uint64_t* k0 = (uint64_t*)tmp;
   uint64_t* k1 = (uint64_t*)(tmp + kbytes);
@@ -259,7 +259,7 @@ static int build_csx(Ctx* c, Csc& q, int by_source, float** w, uint64_t* wcap) {
   if (e != cudaSuccess) return cuda_err(c, e, "CSC build");
   for (int k = 0; k < kPrBins; ++k) q.nb[k] = ht[k];
   q.E = E;
-  if (!q.dbl && cudaMalloc(&q.dbl, sizeof(PrBinLaunch)) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "CSC bins");
+  if (!q.dbl && cy_malloc(&q.dbl, sizeof(PrBinLaunch)) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "CSC bins");
   const PrBinLaunch hb = bin_launch(c, q.nb);
   // pageable source: the call returns once the bytes are staged
   e = cudaMemcpyAsync(q.dbl, &hb, sizeof(hb), cudaMemcpyHostToDevice, c->stream);
@@ -306,8 +306,8 @@ static int pr_ensure_perm(Ctx* c) {
   while ((1ULL << lg_n) < n) ++lg_n;
   uint64_t* k = nullptr;
   uint32_t *perm = nullptr, *inv = nullptr;
-  if (cudaMallocAsync((void**)&k, 2 * n * 8, c->stream) != cudaSuccess || cudaMalloc(&perm, n * 4) != cudaSuccess ||
-      cudaMalloc(&inv, n * 4) != cudaSuccess) {
+  if (cy_malloc_async((void**)&k, 2 * n * 8, c->stream) != cudaSuccess || cy_malloc(&perm, n * 4) != cudaSuccess ||
+      cy_malloc(&inv, n * 4) != cudaSuccess) {
     cudaGetLastError();
     if (k) cudaFreeAsync(k, c->stream);
     if (perm) cudaFree(perm);
@@ -330,7 +330,7 @@ static int pr_deg_mult(Ctx* c) {
   int rc = pr_ensure_perm(c);
   if (rc) return rc;
   if (c->pr_deg_mult && c->pr_deg_mult_version == c->version) return CYTOM_OK;
-  if (!c->pr_deg_mult && cudaMalloc(&c->pr_deg_mult, c->n * 4) != cudaSuccess)
+  if (!c->pr_deg_mult && cy_malloc(&c->pr_deg_mult, c->n * 4) != cudaSuccess)
     return set_err(c, CYTOM_ERR_OOM, "degrees");
   permute_kernel<uint32_t><<<grid_n(c, c->n), 256, 0, c->stream>>>(c->out_deg, c->pr_perm, c->n, 1, c->pr_deg_mult);
   c->launches++;
@@ -569,20 +569,20 @@ int pagerank_alloc(Ctx* c, Job* j) {
   const uint64_t n = c->n;
   bool ok = true;
   if (j->algo == CYTOM_ALGO_PR_DELTA) {
-    ok = ok && cudaMalloc(&s->rank, n * 4) == cudaSuccess;
-    ok = ok && cudaMalloc(&s->comp, n * 4) == cudaSuccess;
-    ok = ok && cudaMalloc(&s->delta, n * 4) == cudaSuccess;
-    ok = ok && cudaMalloc(&s->contrib, 2 * n * 4) == cudaSuccess;
+    ok = ok && cy_malloc(&s->rank, n * 4) == cudaSuccess;
+    ok = ok && cy_malloc(&s->comp, n * 4) == cudaSuccess;
+    ok = ok && cy_malloc(&s->delta, n * 4) == cudaSuccess;
+    ok = ok && cy_malloc(&s->contrib, 2 * n * 4) == cudaSuccess;
   } else if (j->params.kahan) {
-    ok = ok && cudaMalloc(&s->rank, n * 4) == cudaSuccess;
-    ok = ok && cudaMalloc(&s->comp, n * 4) == cudaSuccess;
-    ok = ok && cudaMalloc(&s->lo, 2 * n * 4) == cudaSuccess;
-    ok = ok && cudaMalloc(&s->contrib, n * 4) == cudaSuccess;
+    ok = ok && cy_malloc(&s->rank, n * 4) == cudaSuccess;
+    ok = ok && cy_malloc(&s->comp, n * 4) == cudaSuccess;
+    ok = ok && cy_malloc(&s->lo, 2 * n * 4) == cudaSuccess;
+    ok = ok && cy_malloc(&s->contrib, n * 4) == cudaSuccess;
   } else {
-    ok = ok && cudaMalloc(&s->r64, n * 8) == cudaSuccess;
-    ok = ok && cudaMalloc(&s->r64n, n * 8) == cudaSuccess;
-    ok = ok && cudaMalloc(&s->contrib64, n * 8) == cudaSuccess;
-    ok = ok && cudaMalloc(&s->rank, n * 4) == cudaSuccess;  // float copy for results
+    ok = ok && cy_malloc(&s->r64, n * 8) == cudaSuccess;
+    ok = ok && cy_malloc(&s->r64n, n * 8) == cudaSuccess;
+    ok = ok && cy_malloc(&s->contrib64, n * 8) == cudaSuccess;
+    ok = ok && cy_malloc(&s->rank, n * 4) == cudaSuccess;  // float copy for results
   }
   if (!ok) {
     cudaGetLastError();
@@ -952,7 +952,7 @@ static int unpermute_out(Ctx* c, const T* src, void* out, int where, const char*
   T* dst = (T*)out;
   T* tmp = nullptr;
   if (where != CYTOM_PTR_DEVICE) {
-    if (cudaMallocAsync((void**)&tmp, n * sizeof(T), c->stream) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, what);
+    if (cy_malloc_async((void**)&tmp, n * sizeof(T), c->stream) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, what);
     dst = tmp;
   }
   permute_kernel<T><<<grid_n(c, n), 256, 0, c->stream>>>(src, c->pr_perm, n, 0, dst);
@@ -1040,7 +1040,7 @@ static int build_wgraph(Ctx* c, WGraph& g) {
   int rc = build_csx(c, g.in, 0, &g.in_w, &g.in_wcap);
   if (!rc) rc = build_csx(c, g.out, 1, &g.out_w, &g.out_wcap);
   if (rc) return rc;
-  if (!g.wsum && cudaMalloc(&g.wsum, c->n * 8) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "weight sums");
+  if (!g.wsum && cy_malloc(&g.wsum, c->n * 8) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "weight sums");
   wsum_kernel<<<grid_n(c, c->n * 32), 256, 0, c->stream>>>(g.out.ptr, g.out_w, c->n, g.wsum);
   c->launches++;
   g.built_version = c->version;
@@ -1097,10 +1097,10 @@ int pagerank_set_teleport(Ctx* c, Job* j, const double* t, int where) {
   }
   int prc = pr_ensure_perm(c);
   if (prc) return prc;
-  if (!s->tele && cudaMalloc(&s->tele, c->n * 8) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "teleport");
+  if (!s->tele && cy_malloc(&s->tele, c->n * 8) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "teleport");
   // kept in the renumbering
   double* tmp = nullptr;
-  if (cudaMallocAsync((void**)&tmp, c->n * 8, c->stream) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "teleport");
+  if (cy_malloc_async((void**)&tmp, c->n * 8, c->stream) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "teleport");
   cudaError_t e = cudaMemcpyAsync(tmp, t, c->n * 8,
                                   where == CYTOM_PTR_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                                   c->stream);
@@ -1186,14 +1186,14 @@ int pagerank_adjoint(Ctx* c, Job* j, const double* cv, int cwhere, float* d_w, f
   const uint64_t n = c->n, E = c->E;
   const bool f32 = j->params.kahan != 0;
   cudaError_t e = cudaSuccess;
-  if (!s->adj_ls) e = cudaMalloc(&s->adj_ls, sizeof(LoopState));
-  if (e == cudaSuccess && !s->cvec) e = cudaMalloc(&s->cvec, n * 8);
+  if (!s->adj_ls) e = cy_malloc(&s->adj_ls, sizeof(LoopState));
+  if (e == cudaSuccess && !s->cvec) e = cy_malloc(&s->cvec, n * 8);
   if (f32) {
-    if (e == cudaSuccess && !s->lam) e = cudaMalloc(&s->lam, 2 * n * 4);
-    if (e == cudaSuccess && !s->pt) e = cudaMalloc(&s->pt, n * 4);
+    if (e == cudaSuccess && !s->lam) e = cy_malloc(&s->lam, 2 * n * 4);
+    if (e == cudaSuccess && !s->pt) e = cy_malloc(&s->pt, n * 4);
   } else {
-    if (e == cudaSuccess && !s->lam64) e = cudaMalloc(&s->lam64, 2 * n * 8);
-    if (e == cudaSuccess && !s->pt64) e = cudaMalloc(&s->pt64, n * 8);
+    if (e == cudaSuccess && !s->lam64) e = cy_malloc(&s->lam64, 2 * n * 8);
+    if (e == cudaSuccess && !s->pt64) e = cy_malloc(&s->pt64, n * 8);
   }
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -1203,7 +1203,7 @@ int pagerank_adjoint(Ctx* c, Job* j, const double* cv, int cwhere, float* d_w, f
   LoopState fls;
   e = cudaMemcpyAsync(&fls, j->ls, sizeof(LoopState), cudaMemcpyDeviceToHost, c->stream);
   double* ctmp = nullptr;
-  if (e == cudaSuccess && cudaMallocAsync((void**)&ctmp, n * 8, c->stream) != cudaSuccess)
+  if (e == cudaSuccess && cy_malloc_async((void**)&ctmp, n * 8, c->stream) != cudaSuccess)
     return set_err(c, CYTOM_ERR_OOM, "adjoint setup");
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(ctmp, cv, n * 8, cwhere == CYTOM_PTR_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
@@ -1257,7 +1257,7 @@ int pagerank_adjoint(Ctx* c, Job* j, const double* cv, int cwhere, float* d_w, f
   char* tmp = nullptr;
   auto align256 = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const size_t wbytes = align256(std::max<uint64_t>(E, 1) * 4), tbytes = align256(n * 4);
-  if (cudaMallocAsync((void**)&tmp, 256 + wbytes + tbytes, c->stream) != cudaSuccess)
+  if (cy_malloc_async((void**)&tmp, 256 + wbytes + tbytes, c->stream) != cudaSuccess)
     return set_err(c, CYTOM_ERR_OOM, "adjoint outputs");
   double* dang = (double*)tmp;
   float* gw = (owhere == CYTOM_PTR_DEVICE && d_w) ? d_w : (float*)(tmp + 256);

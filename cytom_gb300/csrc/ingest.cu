@@ -352,7 +352,7 @@ int exclusive_scan_u32(Ctx* c, const uint32_t* in, uint32_t* out, uint64_t n, ui
     return cuda_err(c, cudaGetLastError(), "scan_down");
   }
   uint32_t *sums = nullptr, *soffs = nullptr;
-  e = cudaMallocAsync((void**)&sums, nb * 4 * 2, c->stream);
+  e = cy_malloc_async((void**)&sums, nb * 4 * 2, c->stream);
   if (e != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "scan temp");
   soffs = sums + nb;
   scan_reduce_kernel<<<(unsigned)nb, SCAN_T, 0, c->stream>>>(in, n, sums);
@@ -379,7 +379,7 @@ int radix_sort_pairs(Ctx* c, uint64_t* keys, uint64_t* keys_alt, uint32_t* vals,
   const uint64_t tile = (uint64_t)RS_T * (small ? RS_IPT_SMALL : RS_IPT_LARGE);
   uint64_t nb = (n + tile - 1) / tile;
   uint32_t* hist = nullptr;
-  cudaError_t e = cudaMallocAsync((void**)&hist, nb * 256 * 4 * 2, c->stream);
+  cudaError_t e = cy_malloc_async((void**)&hist, nb * 256 * 4 * 2, c->stream);
   if (e != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "radix histogram");
   uint32_t* offs = hist + nb * 256;
   uint64_t *kin = keys, *kout = keys_alt;
@@ -779,10 +779,10 @@ static int grow_store(Ctx* c, uint64_t need) {
   uint64_t ncap = std::max<uint64_t>(need + need / 2, 1 << 16);
   ncap = (ncap + kChunk - 1) / kChunk * kChunk + kChunk;
   uint32_t *ne = nullptr, *nea = nullptr, *nw = nullptr, *nwa = nullptr;
-  cudaError_t e = cudaMalloc(&ne, ncap * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&nea, ncap * 4);
-  if (e == cudaSuccess && c->wtype) e = cudaMalloc(&nw, ncap * 4);
-  if (e == cudaSuccess && c->wtype) e = cudaMalloc(&nwa, ncap * 4);
+  cudaError_t e = cy_malloc(&ne, ncap * 4);
+  if (e == cudaSuccess) e = cy_malloc(&nea, ncap * 4);
+  if (e == cudaSuccess && c->wtype) e = cy_malloc(&nw, ncap * 4);
+  if (e == cudaSuccess && c->wtype) e = cy_malloc(&nwa, ncap * 4);
   if (e != cudaSuccess) {
     cudaGetLastError();
     cudaFree(ne);
@@ -808,7 +808,7 @@ static int grow_store(Ctx* c, uint64_t need) {
   uint64_t nch = ncap / kChunk + 2;
   if (nch > c->chunk_cap) {
     uint32_t *ct = nullptr, *cta = nullptr;
-    if (cudaMalloc(&ct, nch * 4) != cudaSuccess || cudaMalloc(&cta, nch * 4) != cudaSuccess) {
+    if (cy_malloc(&ct, nch * 4) != cudaSuccess || cy_malloc(&cta, nch * 4) != cudaSuccess) {
       cudaGetLastError();
       cudaFree(ct);
       return set_err(c, CYTOM_ERR_OOM, "chunk table");
@@ -829,10 +829,10 @@ int ensure_app_capacity(Ctx* c, uint64_t need) {
   uint64_t ncap = std::max<uint64_t>(need + need / 2, 1 << 16);
   uint64_t *k = nullptr, *ka = nullptr;
   uint32_t *w = nullptr, *wa = nullptr;
-  cudaError_t e = cudaMalloc(&k, ncap * 8);
-  if (e == cudaSuccess) e = cudaMalloc(&ka, ncap * 8);
-  if (e == cudaSuccess && c->wtype) e = cudaMalloc(&w, ncap * 4);
-  if (e == cudaSuccess && c->wtype) e = cudaMalloc(&wa, ncap * 4);
+  cudaError_t e = cy_malloc(&k, ncap * 8);
+  if (e == cudaSuccess) e = cy_malloc(&ka, ncap * 8);
+  if (e == cudaSuccess && c->wtype) e = cy_malloc(&w, ncap * 4);
+  if (e == cudaSuccess && c->wtype) e = cy_malloc(&wa, ncap * 4);
   if (e != cudaSuccess) {
     cudaGetLastError();
     cudaFree(k);
@@ -876,7 +876,7 @@ int compact(Ctx* c) {
   const uint64_t nsp = (c->E + A + MERGE_SPAN - 1) / MERGE_SPAN;  // merge spans (upper bound)
   size_t bytes = A * (4 + 4 + 8 + 4 + 8 + 4 + 4 + 4) + 64 + 2 * (nsp + 1) * 4;
   char* tmp = nullptr;
-  cudaError_t e = cudaMallocAsync((void**)&tmp, bytes, c->stream);
+  cudaError_t e = cy_malloc_async((void**)&tmp, bytes, c->stream);
   if (e != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "compaction temporaries");
   unsigned long long* lb = (unsigned long long*)tmp;
   unsigned long long* q = lb + A;
@@ -906,7 +906,7 @@ int compact(Ctx* c) {
   // read the installed snapshot.
   uint32_t* mdir = nullptr;
   if (c->dir && !c->dir_disabled) {
-    if (!c->dir_alt && cudaMalloc(&c->dir_alt, c->dir_entries * 4) != cudaSuccess) {
+    if (!c->dir_alt && cy_malloc(&c->dir_alt, c->dir_entries * 4) != cudaSuccess) {
       cudaGetLastError();
       c->dir_alt = nullptr;
     }
@@ -1072,7 +1072,7 @@ int build_directory(Ctx* c) {
     return upload_store_desc(c);
   }
   if (!c->dir) {
-    if (cudaMalloc(&c->dir, entries * 4) != cudaSuccess) {
+    if (cy_malloc(&c->dir, entries * 4) != cudaSuccess) {
       cudaGetLastError();
       c->dir_disabled = true;
       return upload_store_desc(c);
@@ -1208,7 +1208,7 @@ int delete_edges(Ctx* c, const uint32_t* src, const uint32_t* tgt, uint64_t coun
   const uint64_t words = 3 * (nw + 1) + 1 + 3 * count;
   const size_t bytes = ((words * 4 + 15) / 16) * 16 + 8 + (mp.size() + 1) * 4;
   char* tmp = nullptr;
-  cudaError_t e = cudaMallocAsync((void**)&tmp, bytes, c->stream);
+  cudaError_t e = cy_malloc_async((void**)&tmp, bytes, c->stream);
   if (e != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "deletion temporaries");
   uint32_t* kill = (uint32_t*)tmp;
   uint32_t* cnt = kill + (nw + 1);

@@ -76,7 +76,10 @@ __global__ void keys_kernel(const uint32_t* __restrict__ src, const uint32_t* __
 
 // First copy of each distinct key survives with the least weight of its copies;
 // fillCSR's filter (tile-manager.h:519-541) drops local (65535, 65535) when it is the
-// only edge of its tile.
+// only edge of its tile. The first thread of a run of equal keys walks the whole run:
+// linear in the run's length, so the worst case (one edge repeated
+// CYTOM_NOALLOC_MAX_EDGES times) is one thread making 262,144 dependent loads -- slow,
+// still correct.
 __global__ void keep_kernel(const uint64_t* __restrict__ K, const uint32_t* __restrict__ W, uint64_t count,
                             uint32_t lvpt, uint32_t* __restrict__ keep, uint32_t* __restrict__ wsel) {
   uint64_t stride = (uint64_t)gridDim.x * blockDim.x;

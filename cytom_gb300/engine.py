@@ -263,6 +263,11 @@ class Engine:
     def do_global_compaction(self):
         self._check(self.lib.cytom_compact(self.ctx))
 
+    def clear(self):
+        """Drops every edge and zeroes the degrees (cytom_clear); buffers, tuned shapes and
+        jobs stay, and every job restarts from scratch on its next run."""
+        self._check(self.lib.cytom_clear(self.ctx))
+
     def count_edges(self) -> tuple[int, int]:
         a, b = C.c_uint64(), C.c_uint64()
         self._check(self.lib.cytom_count_edges(self.ctx, C.byref(a), C.byref(b)))
@@ -317,6 +322,13 @@ class Engine:
 
     def sync(self):
         self._check(self.lib.cytom_sync(self.ctx))
+
+    def set_fault_injection(self, fail_alloc_after: int = 0, idle_poll_limit: int = 0, phantom_jobs: int = 0):
+        """Test hook (cytom_set_fault_injection): the fail_alloc_after-th allocation from now
+        on fails once; the batched executor's idle wait gives up after idle_poll_limit
+        empty polls; phantom_jobs unfinished jobs without work keep its blocks waiting."""
+        f = L.FaultInjection(fail_alloc_after, idle_poll_limit, phantom_jobs)
+        self._check(self.lib.cytom_set_fault_injection(self.ctx, C.byref(f)))
 
 
 class Program:

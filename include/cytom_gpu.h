@@ -151,6 +151,13 @@ int cytom_insert_batch(cytom_ctx* ctx, const uint32_t* src, const uint32_t* tgt,
  * weight is kept). Runs implicitly before an algorithm runs. */
 int cytom_compact(cytom_ctx* ctx);
 
+/* Drops every stored and pending edge and zeroes the degrees, keeping the context's
+ * buffers (their capacity), its tuned kernel shapes and its jobs; every job restarts
+ * from scratch on its next run. The reference builds new stores instead
+ * (TileStore::init, src/include/core/tile-store.h:27-74; VertexStore::init,
+ * vertex-store.h:25-53). */
+int cytom_clear(cytom_ctx* ctx);
+
 /* Edge counts: compacted (distinct) edges and edges still in the append region
  * (TileStore::countEdges, tile-store.h:174-185). */
 int cytom_count_edges(const cytom_ctx* ctx, uint64_t* compacted, uint64_t* pending);
@@ -327,8 +334,9 @@ int cytom_write_results(cytom_ctx* ctx, int job_id, const char* path);
  * All pointers are device pointers except edge_count (host). tile_ptr holds
  * (T*T + 1) entries for T = vertices (rounded up to a power of two) / vertices_per_tile;
  * edges and weights hold `count` entries (weights only when w is given). count must
- * not exceed CYTOM_NOALLOC_MAX_EDGES (CYTOM_ERR_INVAL otherwise); an id >= vertices is
- * CYTOM_ERR_RANGE and leaves the outputs undefined. Scratch lives in one static device
+ * not exceed CYTOM_NOALLOC_MAX_EDGES (CYTOM_ERR_INVAL otherwise); an id >= vertices
+ * rounded up to a power of two (the store's own vertex count, as cytom_create rounds it)
+ * is CYTOM_ERR_RANGE and leaves the outputs undefined. Scratch lives in one static device
  * array of CYTOM_NOALLOC_SCRATCH_BYTES per GPU, held until exit and shared by every
  * call: calls that overlap on the GPU race. The first call on a device looks the
  * array up (cudaGetSymbolAddress) with that device current; make it before any
@@ -361,6 +369,27 @@ typedef struct cytom_tune_report {
  * CYTOM_AUTOTUNE=0 disables that); call it again to re-tune a grown graph. `out` may be NULL. */
 int cytom_autotune(cytom_ctx* ctx, cytom_tune_report* out);
 int cytom_get_tune_report(const cytom_ctx* ctx, cytom_tune_report* out);
+
+/* ---- Fault injection (tests of the failure paths) ----------------------- */
+
+/* No counterpart in the reference, which aborts on any failure (util::die,
+ * src/lib/util/util.cc:21-32). Makes the library's own failure paths run without a GPU
+ * fault, so tests can check that they return their status and leave the context usable:
+ *  - fail_alloc_after: n > 0 makes the n-th device or pinned-host allocation the library
+ *    makes from this call on (any context of the process) fail, once, as
+ *    CYTOM_ERR_OOM; 0 turns it off.
+ *  - idle_poll_limit: empty polls of the batched executor's bounded idle wait before a
+ *    block gives up (CYTOM_ERR_TIMEOUT), for batches whose first context is ctx;
+ *    0 = the default, 2^22.
+ *  - phantom_jobs: the batched executor counts this many further unfinished jobs that
+ *    have no work, so its blocks find none until the idle wait gives up.
+ * After a batched run that gave up, its jobs restart from scratch on their next run. */
+typedef struct cytom_fault_injection {
+  uint64_t fail_alloc_after;
+  uint32_t idle_poll_limit;
+  uint32_t phantom_jobs;
+} cytom_fault_injection;
+int cytom_set_fault_injection(cytom_ctx* ctx, const cytom_fault_injection* f);
 
 /* ---- Instrumentation --------------------------------------------------- */
 

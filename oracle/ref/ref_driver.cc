@@ -9,7 +9,7 @@
 //
 // usage: ref_driver <mode> <n> <vpt> <edges.bin> <out.bin> <batch> <executors>
 //                   <max_iter> <delta> <start> <adaptive>
-//   mode: compact | bfs | cc | sssp | prdelta | stream
+//   mode: compact | bfs | cc | sssp | prdelta | stream | istream
 //   edges.bin: u64 count, u32 weighted, u32[count] src, u32[count] tgt, [u32[count] w]
 #include <float.h>
 #include <pthread.h>
@@ -189,6 +189,50 @@ void Job<float, algorithm::SSSP, true>::fix_start(const Args& a) {
   vs->vertices_.next[a.start] = 0.0f;
 }
 
+// One reference job run incrementally, as the reference's EdgeInserter drives it with
+// enable_edge_apis (src/include/edge-inserter/edge-inserter.h:129-184): every inserted
+// edge goes through MetaTileManager::insertEdge (tile insert + degrees,
+// meta-tile-manager.h:112-125) and then Algorithm::edgeChanged(INSERT)
+// (meta-tile-manager.h:192-198); after the batch's compaction one executeAlgorithm call
+// continues from the vertex state. One executor object lives across batches. Left out:
+// the swap of the active bitmaps right before the run (edge-inserter.h:150-151), which
+// moves the frontier edgeChanged seeded out of the first round so that the run stops
+// after one round (fix F5).
+template <typename V, class A, bool W>
+struct IncJob {
+  Job<V, A, W> base;
+  std::shared_ptr<A> algo;
+  std::shared_ptr<perf_event::PerfEventManager> pem;
+  Ringbuffer rb;
+  ContinuousAlgorithmExecutor<V, A, W>* cae = nullptr;
+  IncJob(const Args& a, uint64_t execs) : base(a, execs) {
+    algo = std::make_shared<A>(base.config, base.vs);
+    pem = std::make_shared<perf_event::PerfEventManager>();
+    cae = new ContinuousAlgorithmExecutor<V, A, W>(rb, &base.traversal, "ref", base.config, pem, algo, base.vs);
+    cae->initAlgorithm();
+    base.fix_start(a);
+    cae->init(base.vs, base.ts, std::shared_ptr<MetaTileStore<V, A, W>>(), pem);
+  }
+  ~IncJob() {
+    cae->destroy();
+    delete cae;
+  }
+  void insert(const Args& a, uint64_t lo, uint64_t hi) {
+    for (uint64_t i = lo; i < hi; ++i) {
+      Edge e(a.src[i], a.tgt[i], W ? (float)a.w[i] : 0.0f);
+      base.ts->getTileManager(e)->insertEdge(e);
+      base.vs->incrementOutDegree(a.src[i]);
+      base.vs->incrementInDegree(a.tgt[i]);
+      algo->edgeChanged(e, EdgeChangeEvent::INSERT);
+    }
+  }
+  uint64_t run(bool* converged) {
+    uint64_t count = 0;
+    cae->executeAlgorithm(base.ts->countEdges(), converged, &count);
+    return count;
+  }
+};
+
 template <class J>
 static void insert_all(J& job, const Args& a) {
   uint64_t m = a.src.size();
@@ -347,6 +391,50 @@ int main(int argc, char** argv) {
     }
     double res[4] = {(double)edges, run_s, ins_s, (double)nb};
     write_or_die(out, res, sizeof(res));
+  } else if (a.mode == "istream") {
+    // CPU baseline of the streaming workload: BFS / CC / SSSP as incremental reference
+    // jobs (IncJob); per batch: the insert + compaction time of the three stores, the run
+    // time of the three runs and their processed-edge counts (algorithm-executor.h:424-426).
+    IncJob<uint32_t, algorithm::BFS, false> bfs(a, a.execs);
+    IncJob<uint32_t, algorithm::CC, false> cc(a, a.execs);
+    IncJob<float, algorithm::SSSP, true> sssp(a, a.execs);
+    const uint64_t m2 = a.src.size();
+    std::vector<double> rec;
+    for (uint64_t lo = 0; lo < m2; lo += a.batch) {
+      const uint64_t hi = lo + a.batch < m2 ? lo + a.batch : m2;
+      double t0 = now_s();
+      bfs.insert(a, lo, hi);
+      bfs.base.ts->doGlobalCompaction();
+      cc.insert(a, lo, hi);
+      cc.base.ts->doGlobalCompaction();
+      sssp.insert(a, lo, hi);
+      sssp.base.ts->doGlobalCompaction();
+      double t1 = now_s();
+      bool conv = false, all = true;
+      uint64_t edges = bfs.run(&conv);
+      all = all && conv;
+      edges += cc.run(&conv);
+      all = all && conv;
+      edges += sssp.run(&conv);
+      all = all && conv;
+      double t2 = now_s();
+      rec.push_back((double)edges);
+      rec.push_back(t1 - t0);
+      rec.push_back(t2 - t1);
+      rec.push_back(all ? 1.0 : 0.0);
+    }
+    uint64_t nb = rec.size() / 4;
+    write_or_die(out, &nb, 8);
+    write_or_die(out, rec.data(), rec.size() * 8);
+    // final values, for parity checks of the incremental path
+    std::vector<uint32_t> vals(3 * a.n);
+    for (uint64_t v = 0; v < a.n; ++v) {
+      vals[v] = bfs.base.vs->vertices_.next[v];
+      vals[a.n + v] = cc.base.vs->vertices_.next[v];
+      float d = sssp.base.vs->vertices_.next[v];
+      vals[2 * a.n + v] = (d >= FLT_MAX) ? 0xFFFFFFFFu : (uint32_t)d;
+    }
+    write_or_die(out, vals.data(), vals.size() * 4);
   } else {
     fprintf(stderr, "unknown mode %s\n", a.mode.c_str());
     return 1;

@@ -18,7 +18,10 @@ DRIVER = HERE / "_ref" / "ref_driver"
 
 
 def build() -> bool:
-    r = subprocess.run(["make", "-C", str(HERE / "ref"), "-s"], capture_output=True, text=True)
+    cmd = ["make", "-C", str(HERE / "ref"), "-s"]
+    if os.environ.get("CYTOM_REFERENCE"):
+        cmd.append(f"REF={os.environ['CYTOM_REFERENCE']}")
+    r = subprocess.run(cmd, capture_output=True, text=True)
     return r.returncode == 0 and DRIVER.exists()
 
 
@@ -59,6 +62,12 @@ def run(mode, n, vpt, src, tgt, w=None, batch=0, executors=1, max_iter=100, delt
         off += 4 * e
         secs = struct.unpack_from("<d", data, off)[0]
         return {"tile_ptr": tp, "compact": cf, "edges": ed, "weights": wt, "seconds": secs}
+    if mode == "istream":
+        nb = struct.unpack_from("<Q", data, 0)[0]
+        rec = np.frombuffer(data, np.float64, 4 * nb, 8).reshape(nb, 4)
+        vals = np.frombuffer(data, np.uint32, 3 * n, 8 + 32 * nb).reshape(3, n)
+        return {"count_edges": rec[:, 0].astype(np.int64), "insert_seconds": rec[:, 1], "run_seconds": rec[:, 2],
+                "converged": rec[:, 3] != 0, "bfs": vals[0].copy(), "cc": vals[1].copy(), "sssp": vals[2].copy()}
     if mode == "stream":
         edges, run_s, ins_s, nb = struct.unpack_from("<dddd", data, 0)
         return {"count_edges": int(edges), "run_seconds": run_s, "insert_seconds": ins_s, "batches": int(nb)}

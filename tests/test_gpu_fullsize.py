@@ -4,10 +4,12 @@
   the pipelined path of the benchmark): the store holds exactly the distinct inserted
   pairs, in tile order, each with its weight; degrees count every inserted edge; BFS
   levels and SSSP distances satisfy their fixed-point equations over the stored edges
-  (unique solutions, positive increments); the incremental BFS / CC / SSSP results equal
-  fresh runs on the final snapshot.
-- PageRank on RMAT-26 (67,108,864 vertices, 1,073,741,824 edges): FP32-compensated within
-  relative L1 1e-6 and max relative 1e-5 of the FP64 form, whose ranks sum to 1.
+  (unique solutions, positive increments); CC labels equal an independent min-label
+  fixed point; the incremental BFS / CC / SSSP results equal fresh runs on the final
+  snapshot.
+- PageRank on RMAT-26 (67,108,864 vertices, 1,073,741,824 edges): the FP64 form within
+  relative L1 1e-8 of an independent FP64 power iteration (torch), and FP32-compensated
+  within relative L1 1e-6 and max relative 1e-5 of both.
 - Weighted PageRank on RMAT-20 and its adjoint: gradients within 1e-4 of the FP64 CPU
   adjoint and of FP64 central differences.
 The checks are computed with torch on the device (an independent implementation)."""
@@ -91,9 +93,36 @@ def test_streaming_rmat22_full_size(cg):
     # SSSP: D[v] = min(init, min_in D[u] + w), weights >= 1
     reach = dist[S] != INF
     assert torch.equal(relax_min(torch, n, S[reach], Tg[reach], dist[S[reach]] + W[reach], init), dist)
-    # CC labels: never above the vertex, never above a predecessor's
-    assert bool((lab <= torch.arange(n, device=dev)).all())
-    assert bool((lab[Tg] <= lab[S]).all())
+    # CC (directed min-label propagation, examples/cc.cc:81-91): label[v] = the least id
+    # of any vertex that reaches v. Independent fixed point: start from the ids and
+    # lower every target to its sources' labels until nothing changes.
+    ref = torch.arange(n, device=dev, dtype=torch.int64)
+    for _ in range(100000):
+        nxt = ref.scatter_reduce(0, Tg, ref[S], reduce="amin", include_self=True)
+        if torch.equal(nxt, ref):
+            break
+        ref = nxt
+    else:
+        raise AssertionError("the CC check did not reach its fixed point")
+    assert torch.equal(lab, ref)
+
+
+def torch_pagerank_f64(torch, n, S, Tg, alpha=0.85, tol=1e-13, max_iter=1000):
+    """Normalised PageRank with dangling mass spread uniformly, FP64, over the stored
+    (distinct) edges with distinct out-degrees: the model of CYTOM_ALGO_PAGERANK, written
+    independently with torch (gather + index_add) on the device."""
+    deg = torch.bincount(S, minlength=n).to(torch.float64)
+    dangling = deg == 0
+    inv = torch.where(dangling, torch.zeros_like(deg), 1.0 / torch.clamp(deg, min=1.0))
+    r = torch.full((n,), 1.0 / n, dtype=torch.float64, device=S.device)
+    for it in range(max_iter):
+        acc = torch.zeros_like(r).index_add_(0, Tg, (r * inv)[S])
+        rn = (1 - alpha) / n + alpha * (acc + r[dangling].sum() / n)
+        diff = float((rn - r).abs().sum())
+        r = rn
+        if diff <= tol:
+            return r, it + 1
+    raise AssertionError("torch PageRank did not converge")
 
 
 def test_pagerank_rmat26_full_size(cg):
@@ -114,7 +143,19 @@ def test_pagerank_rmat26_full_size(cg):
         assert st32["converged"] == 1 and st64["converged"] == 1
         r32 = p32.result().astype(np.float64)
         r64 = p64.result64()
+        S, Tg, _ = stored_edges(torch, e, n // 65536, 16, False)
+    torch.cuda.empty_cache()
+    ref, _ = torch_pagerank_f64(torch, n, S, Tg)
+    del S, Tg
+    ref = ref.cpu().numpy()
     assert abs(r64.sum() - 1.0) < 1e-9
+    # the FP64 plain form against the independent FP64 solve (both at residual <= 1e-9:
+    # at most about alpha / (1 - alpha) * 1e-9 apart)
+    l1_64 = np.abs(r64 - ref).sum() / np.abs(ref).sum()
+    assert l1_64 <= 1e-8, l1_64
+    l1 = np.abs(r32 - ref).sum() / np.abs(ref).sum()
+    mr = (np.abs(r32 - ref) / ref).max()
+    assert l1 <= 1e-6 and mr <= 1e-5, (l1, mr)
     l1 = np.abs(r32 - r64).sum() / np.abs(r64).sum()
     mr = (np.abs(r32 - r64) / r64).max()
     assert l1 <= 1e-6 and mr <= 1e-5, (l1, mr)

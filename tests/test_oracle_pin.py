@@ -120,3 +120,22 @@ def test_live_corner_edge_quirk(orc, ref):
     tp, ed, wt, cf = st.dump()
     assert np.array_equal(tp, r["tile_ptr"]) and np.array_equal(ed, r["edges"])
     assert r["tile_ptr"][2] - r["tile_ptr"][1] == 0
+
+
+def test_reference_incremental_stream_reaches_the_fixed_point(orc, ref):
+    # The reference's own incremental path (edgeChanged(INSERT) per inserted edge, then
+    # executeAlgorithm continuing from the vertex state; bitmap swap left out, fix F5),
+    # which times the streaming CPU baseline, ends every stream at the oracle's
+    # from-scratch fixed point.
+    scale, vpt = 13, 2048
+    n = 1 << scale
+    s, t = orc.rmat(scale, 0, 12 * n, 31)
+    w = orc.edge_weights(s, t, 37)
+    r = ref.run("istream", n, vpt, s, t, w, batch=2 * n, executors=4, max_iter=100, start=0)
+    assert len(r["count_edges"]) == 6 and r["converged"].all()
+    st = orc.Store(n, vpt, True)
+    st.insert(s, t, w)
+    st.compact()
+    for name, algo in (("bfs", orc.BFS), ("cc", orc.CC), ("sssp", orc.SSSP)):
+        vals, _ = st.run_minprop(algo, start=0, max_iter=100)
+        assert np.array_equal(r[name], vals), name

@@ -127,6 +127,10 @@ int upload_store_desc(Ctx* c) {
   h.dir = c->dir;
   h.nbw = c->lvpt >= 5 ? (uint32_t)(c->vpt / 32) : 0u;
   h.dir_ok = (c->dir && c->dir_version == c->version && !c->dir_disabled) ? 1 : 0;
+  h.xst = c->xs_stage;
+  h.xcum = c->xs_cum;
+  h.xcolcum = c->xs_colcum;
+  h.xnst = c->xs_tmp ? c->xs_tmp + 2 * (c->ntiles + 1) : nullptr;
   {
     static int div = -1;
     if (div < 0) {
@@ -241,6 +245,7 @@ static int job_prepare(Ctx* c, Job* j) {
   if (rc) return rc;
   if (is_minprop(j->algo)) {
     rc = build_directory(c);
+    if (!rc) rc = build_tile_stages(c);
     if (!rc) rc = ensure_job_queue(c, j);
     if (!rc && autotune_due(c)) rc = minprop_autotune(c);
     if (rc) return rc;
@@ -528,7 +533,8 @@ int cytom_destroy(cytom_ctx* ctx) {
   edge_log_close(c);
   void* ptrs[] = {c->dir, c->dir_alt, c->edges, c->wts, c->edges_alt, c->wts_alt, c->tile_ptr, c->tile_ptr_alt,
                   c->chunk_tile, c->chunk_tile_alt, c->app_keys, c->app_keys_alt, c->app_w, c->app_w_alt,
-                  c->out_deg, c->in_deg, c->dsd, c->scratch, c->d_flag};
+                  c->out_deg, c->in_deg, c->dsd, c->scratch, c->d_flag, c->xs_stage, c->xs_cum,
+                  c->xs_colcum, c->xs_tmp};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->h_pinned) cudaFreeHost(c->h_pinned);

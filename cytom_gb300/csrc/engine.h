@@ -27,6 +27,14 @@ namespace cytom {
 constexpr int kChunk = 128;  // edges per warp chunk (32 lanes x uint4)
 constexpr uint32_t kInf = 0xFFFFFFFFu;
 
+// One stage of the column-ordered dense round: `count` (<= 4096) consecutive edges of one
+// tile, starting at edge e0 of the store.
+struct TileStage {
+  uint32_t tile;
+  uint32_t count;
+  unsigned long long e0;
+};
+
 struct StoreDesc {
   const uint32_t* edges;
   const uint32_t* wts;
@@ -49,6 +57,13 @@ struct StoreDesc {
   int dir_ok;                  // directory current (sparse rounds allowed)
   uint32_t sparse_div;         // sparse round while non-zero frontier words * sparse_div <= all words
   uint32_t pad_sd;
+  // column-ordered stages of the dense round (gather_tiles_kernel): stages of every tile in
+  // column-major tile order (column y, then row x); xcum[i] = edges before stage i in that
+  // order (xcum[*xnst] = E); xcolcum[y] = edges before column y (T + 1 entries)
+  const TileStage* xst;
+  const unsigned long long* xcum;
+  const unsigned long long* xcolcum;
+  const uint32_t* xnst;
 };
 
 // Loop state of one job run, in device memory. Kernels index the double-buffered
@@ -205,6 +220,13 @@ struct Ctx {
   void* pr_csc = nullptr;
   void* pr_wgraph = nullptr;  // weighted PageRank: CSC + CSR with weights
   void* edge_log = nullptr;   // open edge log (cytom_persist_edges)
+  // column-ordered stage list of the dense round, rebuilt when the store version changes
+  TileStage* xs_stage = nullptr;
+  unsigned long long* xs_cum = nullptr;
+  unsigned long long* xs_colcum = nullptr;
+  uint32_t* xs_tmp = nullptr;       // counts, offsets and totals of the build
+  uint64_t xs_cap = 0;              // stage entries allocated
+  uint64_t xs_version = ~0ULL;
   // fault injection (tests): batched executor's idle-wait limit (0 = default) and
   // phantom unfinished jobs
   uint32_t inj_idle_limit = 0;
@@ -257,6 +279,7 @@ int insert_device(Ctx* c, const uint32_t* src, const uint32_t* tgt, const uint32
 int compact(Ctx* c);
 int compute_compact_flags(Ctx* c, uint8_t* dflags);
 int build_directory(Ctx* c);
+int build_tile_stages(Ctx* c);
 int ensure_app_capacity(Ctx* c, uint64_t need);
 
 // device-wide utilities

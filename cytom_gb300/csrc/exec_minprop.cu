@@ -33,6 +33,8 @@ namespace cytom {
 
 constexpr int GATHER_T = 256;
 
+static int grid_persistent(Ctx* c, int per_sm) { return c->num_sms * per_sm; }
+
 // Clears both parities of the row flags and the loop counters before a run.
 __global__ void begin_kernel(const JobDesc* __restrict__ jd, const StoreDesc* __restrict__ sd,
                              unsigned max_iter) {
@@ -321,6 +323,375 @@ __global__ void __launch_bounds__(SG_T, MINB) gather_stream_kernel(const JobDesc
   if (threadIdx.x == 0 && scanned) atomicAdd(&ls->edges_scanned, scanned);
 }
 
+// ---- dense round over column-ordered tile stages -----------------------------------
+// gather_tiles_kernel: the dense round with the targets of one tile column reduced in
+// shared memory, as the reference reduces a tile into its tile-local target buffer before
+// writing it back (getLocalNextArray / executeAlgoOnTile / applyTiles,
+// src/include/core/algorithm-executor.h:160-200, 214-290, 431-505).
+//  - Work: stages of at most TS_P edges that never cross a tile, listed in column-major
+//    tile order (column y, then row x, then the tile's pieces). The list is split evenly
+//    by edges over the CTAs (one per SM), so a CTA walks few columns.
+//  - Each stage's edges (and weights) arrive by bulk copy (cp.async.bulk) in an NST-deep
+//    mbarrier pipeline, as in gather_stream_kernel; a stage of an inactive tile row is
+//    skipped without a copy.
+//  - While its column holds enough of the CTA's edges, a CTA keeps next values for the
+//    column's first S target ids (the ids RMAT graphs hit most: low ids take most edges)
+//    in shared memory, neutral kInf, lowered with shared-memory atomics; when the column
+//    changes (and at the end) it writes them back in one coalesced pass: a value below
+//    next[v] lowers next[v] (red.min) and sets v's changed bit (one red.or per warp and
+//    word). That replaces, per relaxed edge, a random pre-check load of next[v] and two
+//    global atomics. Targets at or beyond S, and columns with few of the CTA's edges,
+//    take that global path directly.
+// Values are the same as every other gather's: each target ends the round at the minimum
+// over its relaxed edges, exactly.
+constexpr int TS_T = 512;                 // threads of a tiles block (8 edges per thread)
+constexpr uint32_t TS_BUF = TS_T * 8;     // words per stage buffer (16 KB)
+constexpr uint32_t TS_P = TS_BUF - 4;     // edges per stage: a copy starts up to 3 words early
+constexpr uint32_t TS_SLICE_MAX = 32768;  // targets held in shared memory (128 KB)
+constexpr int TS_NST = 3;
+
+template <int ALGO>
+__host__ __device__ constexpr size_t tiles_smem_fixed() {
+  return (size_t)TS_NST * TS_BUF * 4 * (mp_weighted<ALGO>() ? 2 : 1) + TS_NST * sizeof(uint64_t);
+}
+static inline uint32_t tiles_slice(uint32_t lvpt) {
+  return std::min<uint32_t>(TS_SLICE_MAX, 1u << lvpt);
+}
+
+__device__ __forceinline__ uint32_t tiles_lower_bound(const unsigned long long* __restrict__ a, uint32_t n,
+                                                      unsigned long long key) {
+  uint32_t lo = 0, hi = n;
+  while (lo < hi) {
+    const uint32_t mid = lo + ((hi - lo) >> 1);
+    if (a[mid] < key) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Writes the shared-memory slice of column y back to next / changed and resets it to
+// kInf. Every thread calls it; it ends with a block barrier.
+__device__ __forceinline__ void tiles_flush(const JobDesc* __restrict__ jd, uint32_t* slice, uint32_t S,
+                                            uint32_t yb) {
+  uint32_t* next = jd->next;
+  uint32_t* ch = jd->ch;
+  const unsigned lane = threadIdx.x & 31;
+  for (uint32_t base = (threadIdx.x & ~31u); base < S; base += TS_T) {
+    const uint32_t i = base + lane;
+    const uint32_t c = slice[i];
+    bool imp = false;
+    if (c != kInf) {
+      slice[i] = kInf;
+      const uint32_t v = yb + i;
+      if (c < __ldcg(next + v)) {
+        atomicMin(next + v, c);
+        imp = true;
+      }
+    }
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, imp);
+    if (lane == 0 && m) atomicOr(ch + ((yb + base) >> 5), m);
+  }
+  __syncthreads();
+}
+
+template <int ALGO>
+__global__ void __launch_bounds__(TS_T, 1) gather_tiles_kernel(const JobDesc* __restrict__ jd,
+                                                               const StoreDesc* __restrict__ sd, int adaptive) {
+  extern __shared__ __align__(128) uint8_t smem_raw[];
+  __shared__ uint32_t s_range[2];
+  LoopState* ls = jd->ls;
+  if (!ls->cont || ls->mode != 0) return;
+  const unsigned p = ls->iter & 1u;
+  round_open<false>(jd, sd, p, adaptive, (uint64_t)blockIdx.x * blockDim.x + threadIdx.x,
+                    (uint64_t)gridDim.x * blockDim.x);
+  constexpr bool WT = mp_weighted<ALGO>();
+  const uint32_t lvpt = sd->lvpt, lT = sd->lT;
+  const uint32_t vpt = 1u << lvpt;
+  const uint32_t ymask = (uint32_t)(sd->T - 1);
+  const uint32_t S = min(TS_SLICE_MAX, vpt);
+  uint32_t* slice = reinterpret_cast<uint32_t*>(smem_raw);
+  uint32_t* ebuf = slice + S;
+  uint32_t* wbuf = ebuf + TS_NST * TS_BUF;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(ebuf + TS_NST * TS_BUF * (WT ? 2 : 1));
+  if (sd->xnst == nullptr) {  // no stage list (never launched so): fail loudly
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(&ls->err, 3u);
+    return;
+  }
+  const TileStage* __restrict__ stages = sd->xst;
+  const unsigned long long* __restrict__ cum = sd->xcum;
+  const unsigned* rows_cur = jd->rows + p * sd->T;
+  const uint32_t* __restrict__ edges = sd->edges;
+  const uint32_t* __restrict__ wts = sd->wts;
+  const uint32_t* fa = jd->fa;
+  const bool async = jd->async != 0;
+  uint32_t* next = jd->next;
+  uint32_t* ch = jd->ch;
+
+  if (threadIdx.x == 0) {
+    const uint32_t nst = *sd->xnst;
+    const unsigned long long total = cum[nst];
+    const unsigned long long lo = total * blockIdx.x / gridDim.x, hi = total * (blockIdx.x + 1) / gridDim.x;
+    s_range[0] = tiles_lower_bound(cum, nst, lo);
+    s_range[1] = tiles_lower_bound(cum, nst, hi);
+#pragma unroll
+    for (int k = 0; k < TS_NST; ++k) mbar_init(&bar[k], 1);
+    fence_mbar_init();
+  }
+  for (uint32_t i = threadIdx.x; i < S; i += TS_T) slice[i] = kInf;
+  __syncthreads();
+  const uint32_t sb = s_range[0], se = s_range[1];
+  const unsigned long long cta_lo = cum[sb], cta_hi = cum[se];
+
+  auto next_active = [&](uint32_t s) -> uint32_t {
+    if (adaptive)
+      while (s < se && ld_plain<false>(rows_cur + (stages[s].tile >> lT)) == 0) ++s;
+    return s;
+  };
+  auto issue = [&](int slot, uint32_t s) {
+    const TileStage st = stages[s];
+    const unsigned long long a0 = st.e0 & ~3ULL;
+    const uint32_t words = ((uint32_t)(st.e0 & 3ULL) + st.count + 3u) & ~3u;
+    fence_proxy_async_smem();
+    mbar_arrive_expect_tx(&bar[slot], words * 4u * (WT ? 2u : 1u));
+    bulk_g2s(ebuf + slot * TS_BUF, edges + a0, words * 4u, &bar[slot]);
+    if (WT) bulk_g2s(wbuf + slot * TS_BUF, wts + a0, words * 4u, &bar[slot]);
+  };
+
+  uint32_t stq[TS_NST];
+  {
+    uint32_t s0 = next_active(sb);
+#pragma unroll
+    for (int k = 0; k < TS_NST; ++k) {
+      stq[k] = s0;
+      if (s0 < se) s0 = next_active(s0 + 1);
+    }
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int k = 0; k < TS_NST; ++k)
+        if (stq[k] < se) issue(k, stq[k]);
+    }
+  }
+  uint32_t s_next = (stq[TS_NST - 1] < se) ? next_active(stq[TS_NST - 1] + 1) : se;
+  uint32_t phases = 0;
+  int slot = 0;
+  unsigned long long scanned = 0;
+  bool failed = false;
+  uint32_t cur_col = 0xFFFFFFFFu;
+  bool slice_mode = false;
+
+  while (stq[0] < se) {
+    const TileStage st = stages[stq[0]];
+    const uint32_t y = st.tile & ymask;
+    if (y != cur_col) {  // uniform: every thread walks the same stages
+      if (slice_mode) tiles_flush(jd, slice, S, cur_col << lvpt);
+      cur_col = y;
+      const unsigned long long c0 = sd->xcolcum[y], c1 = sd->xcolcum[y + 1];
+      const unsigned long long seg = min(cta_hi, c1) - max(cta_lo, c0);
+      slice_mode = seg >= (unsigned long long)(S / 4);
+    }
+    const bool ok = mbar_wait(&bar[slot], (phases >> slot) & 1u);
+    phases ^= 1u << slot;
+    if (ok) {
+      if (threadIdx.x == 0) scanned += st.count;
+      const uint32_t x = st.tile >> lT;
+      const uint32_t xb = x << lvpt, yb = y << lvpt;
+      const uint32_t off = (uint32_t)(st.e0 & 3ULL), endp = off + st.count;
+      const bool full_row = !adaptive || ld_plain<false>(rows_cur + x) == vpt;
+      const uint32_t* eb = ebuf + slot * TS_BUF;
+      const uint32_t* wb = wbuf + slot * TS_BUF;
+      uint32_t qv[8], ww[8], uu[8];
+      uint32_t vmask = 0;
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const uint32_t i0 = threadIdx.x * 4 + (uint32_t)k * (TS_T * 4);
+        const uint4 q = *reinterpret_cast<const uint4*>(eb + i0);
+        uint4 wq = make_uint4(0, 0, 0, 0);
+        if (WT) wq = *reinterpret_cast<const uint4*>(wb + i0);
+        qv[4 * k + 0] = q.x;
+        qv[4 * k + 1] = q.y;
+        qv[4 * k + 2] = q.z;
+        qv[4 * k + 3] = q.w;
+        ww[4 * k + 0] = wq.x;
+        ww[4 * k + 1] = wq.y;
+        ww[4 * k + 2] = wq.z;
+        ww[4 * k + 3] = wq.w;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) vmask |= ((i0 + j) >= off && (i0 + j) < endp) ? (1u << (4 * k + j)) : 0u;
+      }
+#pragma unroll
+      for (int idx = 0; idx < 8; ++idx) uu[idx] = xb | (qv[idx] >> 16);
+      uint32_t amask = vmask;
+      if (!full_row && vmask) {
+        uint32_t fw[8];
+#pragma unroll
+        for (int idx = 0; idx < 8; ++idx) fw[idx] = ((vmask >> idx) & 1u) ? ld_state<false>(fa + (uu[idx] >> 5)) : 0u;
+        amask = 0;
+#pragma unroll
+        for (int idx = 0; idx < 8; ++idx) amask |= ((fw[idx] >> (uu[idx] & 31)) & 1u) << idx;
+        amask &= vmask;
+      }
+      if (amask) {
+        uint32_t cand[8];
+#pragma unroll
+        for (int idx = 0; idx < 8; ++idx) cand[idx] = ((amask >> idx) & 1u) ? ld_src<false>(jd, async, uu[idx]) : kInf;
+#pragma unroll
+        for (int idx = 0; idx < 8; ++idx)
+          if (cand[idx] != kInf) cand[idx] = mp_cand<ALGO>(cand[idx], ww[idx]);
+        uint32_t gmask = 0;  // edges taking the global path
+#pragma unroll
+        for (int idx = 0; idx < 8; ++idx) {
+          if (cand[idx] == kInf) continue;
+          const uint32_t tl = qv[idx] & 0xFFFFu;
+          if (slice_mode && tl < S) atomicMin(slice + tl, cand[idx]);
+          else gmask |= 1u << idx;
+        }
+        if (gmask) {
+          uint32_t nv[8];
+#pragma unroll
+          for (int idx = 0; idx < 8; ++idx)
+            nv[idx] = ((gmask >> idx) & 1u) ? __ldcg(next + (yb | (qv[idx] & 0xFFFFu))) : 0u;
+#pragma unroll
+          for (int idx = 0; idx < 8; ++idx) {
+            if (((gmask >> idx) & 1u) && cand[idx] < nv[idx]) {
+              const uint32_t v = yb | (qv[idx] & 0xFFFFu);
+              atomicMin(next + v, cand[idx]);
+              atomicOr(ch + (v >> 5), 1u << (v & 31));
+            }
+          }
+        }
+      }
+    }
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      phases ^= 1u << slot;  // the slot's copy is still owed: the cleanup waits on it
+      break;
+    }
+    if (threadIdx.x == 0 && s_next < se) issue(slot, s_next);
+#pragma unroll
+    for (int k = 0; k + 1 < TS_NST; ++k) stq[k] = stq[k + 1];
+    stq[TS_NST - 1] = s_next;
+    if (s_next < se) s_next = next_active(s_next + 1);
+    slot = (slot + 1 == TS_NST) ? 0 : slot + 1;
+  }
+  if (failed) {
+    if (threadIdx.x == 0) {
+      atomicExch(&ls->err, 1u);
+      for (int k = 0; k < TS_NST; ++k) {
+        const int sl = (slot + k) % TS_NST;
+        if (stq[k] < se) mbar_wait(&bar[sl], (phases >> sl) & 1u);
+      }
+    }
+    __syncthreads();
+    return;
+  }
+  if (slice_mode) tiles_flush(jd, slice, S, cur_col << lvpt);
+  if (threadIdx.x == 0 && scanned) atomicAdd(&ls->edges_scanned, scanned);
+}
+
+// Stage list of gather_tiles_kernel, per store version. Column-major rank r = y * T + x
+// names tile t = x * T + y.
+__global__ void xs_count_kernel(const unsigned long long* __restrict__ tile_ptr, uint32_t lT, uint64_t ntiles,
+                                uint32_t* __restrict__ cnt, uint32_t* __restrict__ size) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t tm = (1ULL << lT) - 1ULL;
+  for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < ntiles; r += stride) {
+    const uint64_t t = ((r & tm) << lT) | (r >> lT);
+    const uint64_t sz = tile_ptr[t + 1] - tile_ptr[t];
+    size[r] = (uint32_t)sz;
+    cnt[r] = (uint32_t)((sz + TS_P - 1) / TS_P);
+  }
+}
+
+__global__ void xs_write_kernel(const unsigned long long* __restrict__ tile_ptr, uint32_t lT, uint64_t ntiles,
+                                const uint32_t* __restrict__ cnt, const uint32_t* __restrict__ off,
+                                const uint32_t* __restrict__ size, const uint32_t* __restrict__ ecm,
+                                const uint32_t* __restrict__ nst, TileStage* __restrict__ st,
+                                unsigned long long* __restrict__ cum, unsigned long long* __restrict__ colcum,
+                                unsigned long long E) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t tm = (1ULL << lT) - 1ULL;
+  for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < ntiles; r += stride) {
+    const uint64_t t = ((r & tm) << lT) | (r >> lT);
+    if ((r & tm) == 0) colcum[r >> lT] = ecm[r];
+    const uint32_t n = cnt[r], o = off[r], sz = size[r];
+    const unsigned long long e0 = tile_ptr[t];
+    for (uint32_t k = 0; k < n; ++k) {
+      TileStage s;
+      s.tile = (uint32_t)t;
+      s.count = min(TS_P, sz - k * TS_P);
+      s.e0 = e0 + (unsigned long long)k * TS_P;
+      st[o + k] = s;
+      cum[o + k] = (unsigned long long)ecm[r] + (unsigned long long)k * TS_P;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    cum[*nst] = E;
+    colcum[1ULL << lT] = E;
+  }
+}
+
+// The column-ordered dense round needs tiles of >= 1024 vertices (a warp-aligned shared
+// slice of >= 1024 targets) and 32-bit column offsets.
+static bool tiles_geometry(const Ctx* c) { return c->lvpt >= 10; }
+static bool tiles_usable(const Ctx* c) { return tiles_geometry(c) && c->E < 0xFFFFFFF0ull; }
+constexpr int kTilesVariant = 4;
+
+int build_tile_stages(Ctx* c) {
+  if (c->xs_version == c->version) return CYTOM_OK;
+  if (!tiles_usable(c)) {
+    // a store past 2^32 edges: programs tuned to the tiles kernel go back to the stream
+    for (int k = 0; k < 2; ++k)
+      if (c->sg_variant[k] == kTilesVariant) {
+        c->sg_variant[k] = 0;
+        c->tune_epoch++;
+      }
+    c->xs_version = c->version;
+    return CYTOM_OK;
+  }
+  const uint64_t nt = c->ntiles;
+  const uint64_t need = c->E / TS_P + nt + 1;
+  if (need > c->xs_cap || !c->xs_tmp) {
+    join_runs(c);  // runs in flight may still read the old list
+    cudaError_t se = cudaStreamSynchronize(c->stream);
+    if (se != cudaSuccess) return cuda_err(c, se, "tile stage list");
+    cudaFree(c->xs_stage);
+    cudaFree(c->xs_cum);
+    c->xs_stage = nullptr;
+    c->xs_cum = nullptr;
+    c->xs_cap = 0;
+    const uint64_t cap = need + need / 2;
+    if (cy_malloc(&c->xs_stage, cap * sizeof(TileStage)) != cudaSuccess ||
+        cy_malloc(&c->xs_cum, (cap + 1) * 8) != cudaSuccess ||
+        (!c->xs_colcum && cy_malloc(&c->xs_colcum, (c->T + 1) * 8) != cudaSuccess) ||
+        (!c->xs_tmp && cy_malloc(&c->xs_tmp, (4 * nt + 8) * 4) != cudaSuccess)) {
+      cudaGetLastError();
+      return set_err(c, CYTOM_ERR_OOM, "tile stage list");
+    }
+    c->xs_cap = cap;
+  }
+  uint32_t* cnt = c->xs_tmp;
+  uint32_t* off = c->xs_tmp + (nt + 1);
+  uint32_t* nst = c->xs_tmp + 2 * (nt + 1);
+  uint32_t* tot = nst + 1;
+  uint32_t* size = nst + 2;
+  uint32_t* ecm = size + nt;
+  int slot = prof_begin(c, KC_MERGE);
+  xs_count_kernel<<<std::max(1, std::min<int>(grid_persistent(c, 8), (int)((nt + 255) / 256))), 256, 0, c->stream>>>(
+      c->tile_ptr, c->lT, nt, cnt, size);
+  c->launches++;
+  int rc = exclusive_scan_u32(c, cnt, off, nt, nst);
+  if (!rc) rc = exclusive_scan_u32(c, size, ecm, nt, tot);
+  if (rc) return rc;
+  xs_write_kernel<<<std::max(1, std::min<int>(grid_persistent(c, 8), (int)((nt + 255) / 256))), 256, 0, c->stream>>>(
+      c->tile_ptr, c->lT, nt, cnt, off, size, ecm, nst, c->xs_stage, c->xs_cum, c->xs_colcum, c->E);
+  c->launches++;
+  prof_end(c, slot, (double)nt * 28.0 + (double)need * 24.0);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_err(c, e, "tile stage list");
+  c->xs_version = c->version;
+  return upload_store_desc(c);
+}
+
 // Sparse gather (sparse_group over every group of 32 items) and its chunk pass
 // (sparse_chunk over the queue the first pass filled).
 template <int ALGO>
@@ -488,8 +859,6 @@ __global__ void seed_keys_multi_kernel(SeedJobs sj, const uint64_t* __restrict__
   }
 }
 
-static int grid_persistent(Ctx* c, int per_sm) { return c->num_sms * per_sm; }
-
 int minprop_seed_keys_many(Ctx* c, Job* const* jobs, int njobs, const uint64_t* K, const uint32_t* W,
                            uint64_t count) {
   int g = std::max(1, std::min<int>(grid_persistent(c, 8), (int)((count + 255) / 256)));
@@ -609,7 +978,29 @@ static size_t sg_smem(int v) {
   }
 }
 
+template <int ALGO>
+static GatherLaunch tiles_launch_t(Ctx* c) {
+  static int attr_set = 0;
+  GatherLaunch g{};
+  g.fn = (void*)gather_tiles_kernel<ALGO>;
+  g.smem = (size_t)tiles_slice(c->lvpt) * 4 + tiles_smem_fixed<ALGO>();
+  const size_t full = (size_t)TS_SLICE_MAX * 4 + tiles_smem_fixed<ALGO>();
+  if (!attr_set) {
+    cudaFuncSetAttribute(g.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)full);
+    attr_set = 1;
+  }
+  g.grid = dim3(grid_persistent(c, 1));
+  g.block = dim3(TS_T);
+  return g;
+}
+
+static GatherLaunch tiles_launch(Ctx* c, int a) {
+  return a == 0 ? tiles_launch_t<0>(c) : a == 1 ? tiles_launch_t<1>(c) : a == 3 ? tiles_launch_t<3>(c)
+                                                                         : tiles_launch_t<2>(c);
+}
+
 static GatherLaunch stream_launch(Ctx* c, int a, int v) {
+  if (v == kTilesVariant) return tiles_launch(c, a);
   static bool attr_set[4][kSgVariantCount] = {};
   GatherLaunch g{};
   g.fn = a == 0 ? sg_fn<0>(v) : a == 1 ? sg_fn<1>(v) : a == 3 ? sg_fn<3>(v) : sg_fn<2>(v);
@@ -630,10 +1021,11 @@ static int sg_variant(Ctx* c, int algo) {
   if (env == -2) {
     const char* s = getenv("CYTOM_SG_VARIANT");
     env = s ? atoi(s) : -1;
-    if (env >= kSgVariantCount) env = -1;
+    if (env > kTilesVariant) env = -1;
   }
-  if (env >= 0) return env;
-  return c->sg_variant[(algo == CYTOM_ALGO_SSSP || algo == CYTOM_ALGO_SSWP) ? 1 : 0];
+  int v = (env >= 0) ? env : c->sg_variant[(algo == CYTOM_ALGO_SSSP || algo == CYTOM_ALGO_SSWP) ? 1 : 0];
+  if (v == kTilesVariant && !tiles_usable(c)) v = 0;
+  return v;
 }
 
 static GatherLaunch gather_launch(Ctx* c, int algo) {
@@ -920,6 +1312,8 @@ __global__ void tune_state_kernel(JobDesc* jd, const StoreDesc* __restrict__ sd,
 }
 
 int minprop_autotune(Ctx* c) {
+  int brc = build_tile_stages(c);
+  if (brc) return brc;
   const uint64_t n = c->n, nwords = (n + 31) / 32;
   JobDesc h{};
   LoopState* ls = nullptr;
@@ -960,7 +1354,8 @@ int minprop_autotune(Ctx* c) {
     const int algo = cls == 0 ? 1 : 2;
     int best = 0;
     double best_us = 1e300;
-    for (int v = 0; v < kSgVariantCount && e == cudaSuccess; ++v) {
+    const int nvar = kSgVariantCount + (tiles_usable(c) ? 1 : 0);
+    for (int v = 0; v < nvar && e == cudaSuccess; ++v) {
       GatherLaunch g = stream_launch(c, algo, v);
       double vbest = 1e300;
       for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
@@ -993,12 +1388,16 @@ int minprop_autotune(Ctx* c) {
 
 
 void sg_shapes(int* ept, int* nst, int* minb, int* count) {
-  *count = kSgVariantCount;
+  *count = kSgVariantCount + 1;
   for (int v = 0; v < kSgVariantCount; ++v) {
     ept[v] = kSgVariants[v].ept;
     nst[v] = kSgVariants[v].nst;
     minb[v] = kSgVariants[v].minb;
   }
+  // the column-ordered tiles kernel: 8 edges per thread of 512, 3-deep pipeline, 1 block per SM
+  ept[kTilesVariant] = 8;
+  nst[kTilesVariant] = TS_NST;
+  minb[kTilesVariant] = 1;
 }
 
 }  // namespace cytom

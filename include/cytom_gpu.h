@@ -350,10 +350,13 @@ int cytom_tile_batch_noalloc(const uint32_t* src, const uint32_t* tgt, const uin
 
 /* ---- Autotuner ---------------------------------------------------------- */
 
-/* Shapes of the streaming gather (edges per thread, bulk-copy pipeline depth, resident
- * blocks per SM) and the round time each took on the context's graph, per program class
- * (0 = BFS / CC, 1 = SSSP); chosen[k] is the shape in use. No counterpart in the
- * reference (its tile batching, algorithm-tile-batching, is a fixed flag). */
+/* Kernels of the dense round and their shapes (edges per thread, bulk-copy pipeline
+ * depth, resident blocks per SM): variants 0-3 stream the tile-major edge array;
+ * variant 4 (where vertices_per_tile >= 1024) walks the tiles column by column and
+ * reduces each column's targets in shared memory. With the round time each took on the
+ * context's graph, per program class (0 = BFS / CC, 1 = SSSP); chosen[k] is the variant
+ * in use. No counterpart in the reference (its tile batching, algorithm-tile-batching,
+ * is a fixed flag). */
 typedef struct cytom_tune_report {
   int32_t variants;
   int32_t chosen[2];

@@ -208,10 +208,13 @@ print(json.dumps(ok))
     assert all(ok), (sparse, ok)
 
 
-@pytest.mark.parametrize("variant", ["0", "1", "2", "3"])
+@pytest.mark.parametrize("variant", ["0", "1", "2", "3", "4"])
 def test_stream_shapes_agree(cg, orc, variant):
-    # every streaming-gather shape the autotuner may pick gives the oracle's values,
-    # round counts and processed-edge counts (dense rounds only; single- and multi-row stages)
+    # every dense-round kernel and shape the autotuner may pick gives the oracle's values,
+    # round counts and processed-edge counts (dense rounds only; single- and multi-row
+    # stages; variant 4, the column-ordered tiles kernel, with its shared-memory slice
+    # covering all targets (4096), half of them (65536) and with small columns (1024);
+    # below 1024 vertices per tile it falls back to the stream)
     import json
     import os
     import subprocess
@@ -222,20 +225,33 @@ sys.path.insert(0, {str(__import__('pathlib').Path(__file__).resolve().parents[1
 import cytom_gb300 as cg
 from oracle import oracle as orc
 ok = []
-for scale, vpt in ((16, 4096), (15, 256)):
+for scale, vpt, adaptive in ((16, 4096, True), (15, 256, True), (17, 65536, True), (18, 1024, True),
+                             (16, 4096, False)):
     n = 1 << scale
     s, t = orc.rmat(scale, 0, 16 * n, 5)
     w = orc.edge_weights(s, t, 6)
     st = orc.Store(n, vpt, True)
     st.insert(s, t, w); st.compact()
-    with cg.Engine(n, vpt, weight_type=cg.WEIGHT_U32) as eng:
+    with cg.Engine(n, vpt, weight_type=cg.WEIGHT_U32, adaptive_scheduling=adaptive) as eng:
         eng.insert_edges(s, t, w)
         for prog, algo in ((cg.BFS, 0), (cg.CC, 1), (cg.SSSP, 2), (cg.SSWP, 3)):
             p = prog(eng, start_vertex=0, max_iterations=1000)
             stt = p.execute_algorithm()
-            ref, info = st.run_minprop(algo, start=0, max_iter=1000)
+            ref, info = st.run_minprop(algo, start=0, max_iter=1000, adaptive=adaptive)
             ok.append(bool(np.array_equal(p.result(), ref)) and stt["iterations"] == info["iterations"]
                       and stt["count_edges"] == info["count_edges"])
+        # a further batch: incremental runs on a grown store (the stage list is rebuilt)
+        s2, t2 = orc.rmat(scale, 16 * n, 2 * n, 5)
+        w2 = orc.edge_weights(s2, t2, 6)
+        progs = [cg.BFS(eng, start_vertex=0, max_iterations=1000), cg.CC(eng, max_iterations=1000)]
+        for p in progs:
+            p.execute_algorithm()
+        eng.insert_edges(s2, t2, w2)
+        st.insert(s2, t2, w2); st.compact()
+        for p, algo in zip(progs, (0, 1)):
+            p.execute_algorithm()
+            ref, _ = st.run_minprop(algo, start=0, max_iter=1000, adaptive=adaptive)
+            ok.append(bool(np.array_equal(p.result(), ref)))
 print(json.dumps(ok))
 """
     env = dict(os.environ, CYTOM_SG_VARIANT=variant, CYTOM_SPARSE="0", CYTOM_AUTOTUNE="0")

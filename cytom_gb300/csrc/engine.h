@@ -58,8 +58,9 @@ struct StoreDesc {
   uint32_t sparse_div;         // sparse round while non-zero frontier words * sparse_div <= all words
   uint32_t pad_sd;
   // column-ordered stages of the dense round (gather_tiles_kernel): stages of every tile in
-  // column-major tile order (column y, then row x); xcum[i] = edges before stage i in that
-  // order (xcum[*xnst] = E); xcolcum[y] = edges before column y (T + 1 entries)
+  // column-major tile order (column y, then row x); xcum[i] = partition weight before
+  // stage i in that order (edges + a fixed cost per stage; xcum[*xnst] = the total);
+  // xcolcum[y] = the weight before column y (T + 1 entries)
   const TileStage* xst;
   const unsigned long long* xcum;
   const unsigned long long* xcolcum;

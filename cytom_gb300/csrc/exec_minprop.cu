@@ -329,8 +329,9 @@ __global__ void __launch_bounds__(SG_T, MINB) gather_stream_kernel(const JobDesc
 // writing it back (getLocalNextArray / executeAlgoOnTile / applyTiles,
 // src/include/core/algorithm-executor.h:160-200, 214-290, 431-505).
 //  - Work: stages of at most TS_P edges that never cross a tile, listed in column-major
-//    tile order (column y, then row x, then the tile's pieces). The list is split evenly
-//    by edges over the CTAs (one per SM), so a CTA walks few columns.
+//    tile order (column y, then row x, then the tile's pieces). The list is split over the
+//    CTAs (one per SM) in contiguous ranges of equal weight (edges + TS_STAGE_COST per
+//    stage), so a CTA walks few columns.
 //  - Each stage's edges (and weights) arrive by bulk copy (cp.async.bulk) in an NST-deep
 //    mbarrier pipeline, as in gather_stream_kernel; a stage of an inactive tile row is
 //    skipped without a copy.
@@ -349,6 +350,10 @@ constexpr uint32_t TS_BUF = TS_T * 8;     // words per stage buffer (16 KB)
 constexpr uint32_t TS_P = TS_BUF - 4;     // edges per stage: a copy starts up to 3 words early
 constexpr uint32_t TS_SLICE_MAX = 32768;  // targets held in shared memory (128 KB)
 constexpr int TS_NST = 3;
+constexpr uint32_t TS_SLICE_MIN = 2;      // slice mode from 2 edges per slice target up
+// Partition weight of a stage: its edges plus a fixed cost for its copy, wait and barrier,
+// so CTAs whose ranges hold many small tiles get fewer of them.
+constexpr uint32_t TS_STAGE_COST = 2048;
 
 template <int ALGO>
 __host__ __device__ constexpr size_t tiles_smem_fixed() {
@@ -371,25 +376,40 @@ __device__ __forceinline__ uint32_t tiles_lower_bound(const unsigned long long* 
 
 // Writes the shared-memory slice of column y back to next / changed and resets it to
 // kInf. Every thread calls it; it ends with a block barrier.
+// Slice position of target tl: the low 5 bits are permuted within their group of 32 by
+// higher bits, so targets with equal low bits (RMAT ids are skewed in every bit) spread
+// over the shared-memory banks. A group of 32 targets stays one group of 32 positions.
+__device__ __forceinline__ uint32_t tiles_pos(uint32_t tl) {
+  return tl ^ (((tl >> 5) ^ (tl >> 10) ^ (tl >> 15)) & 31u);
+}
+
+// A warp covers 32 consecutive targets (one changed word) per step and keeps FL steps'
+// loads of next in flight.
+constexpr int TS_FL = 8;
 __device__ __forceinline__ void tiles_flush(const JobDesc* __restrict__ jd, uint32_t* slice, uint32_t S,
                                             uint32_t yb) {
   uint32_t* next = jd->next;
   uint32_t* ch = jd->ch;
   const unsigned lane = threadIdx.x & 31;
-  for (uint32_t base = (threadIdx.x & ~31u); base < S; base += TS_T) {
-    const uint32_t i = base + lane;
-    const uint32_t c = slice[i];
-    bool imp = false;
-    if (c != kInf) {
-      slice[i] = kInf;
-      const uint32_t v = yb + i;
-      if (c < __ldcg(next + v)) {
-        atomicMin(next + v, c);
-        imp = true;
-      }
+  for (uint32_t base0 = (threadIdx.x & ~31u); base0 < S; base0 += TS_T * TS_FL) {
+    uint32_t c[TS_FL], nv[TS_FL];
+#pragma unroll
+    for (int k = 0; k < TS_FL; ++k) {
+      const uint32_t i = tiles_pos(base0 + (uint32_t)k * TS_T + lane);  // target base0 + k*TS_T + lane
+      c[k] = (base0 + (uint32_t)k * TS_T < S) ? slice[i] : kInf;
+      if (c[k] != kInf) slice[i] = kInf;
     }
-    const unsigned m = __ballot_sync(0xFFFFFFFFu, imp);
-    if (lane == 0 && m) atomicOr(ch + ((yb + base) >> 5), m);
+#pragma unroll
+    for (int k = 0; k < TS_FL; ++k)
+      nv[k] = (c[k] != kInf) ? __ldcg(next + yb + base0 + (uint32_t)k * TS_T + lane) : 0u;
+#pragma unroll
+    for (int k = 0; k < TS_FL; ++k) {
+      const uint32_t v = yb + base0 + (uint32_t)k * TS_T + lane;
+      const bool imp = c[k] != kInf && c[k] < nv[k];
+      if (imp) atomicMin(next + v, c[k]);
+      const unsigned m = __ballot_sync(0xFFFFFFFFu, imp);
+      if (lane == 0 && m) atomicOr(ch + (v >> 5), m);
+    }
   }
   __syncthreads();
 }
@@ -487,7 +507,7 @@ __global__ void __launch_bounds__(TS_T, 1) gather_tiles_kernel(const JobDesc* __
       cur_col = y;
       const unsigned long long c0 = sd->xcolcum[y], c1 = sd->xcolcum[y + 1];
       const unsigned long long seg = min(cta_hi, c1) - max(cta_lo, c0);
-      slice_mode = seg >= (unsigned long long)(S / 4);
+      slice_mode = seg >= (unsigned long long)S * TS_SLICE_MIN;
     }
     const bool ok = mbar_wait(&bar[slot], (phases >> slot) & 1u);
     phases ^= 1u << slot;
@@ -542,8 +562,12 @@ __global__ void __launch_bounds__(TS_T, 1) gather_tiles_kernel(const JobDesc* __
         for (int idx = 0; idx < 8; ++idx) {
           if (cand[idx] == kInf) continue;
           const uint32_t tl = qv[idx] & 0xFFFFu;
-          if (slice_mode && tl < S) atomicMin(slice + tl, cand[idx]);
-          else gmask |= 1u << idx;
+          if (slice_mode && tl < S) {
+            uint32_t* sp = slice + tiles_pos(tl);
+            if (cand[idx] < *sp) atomicMin(sp, cand[idx]);
+          } else {
+            gmask |= 1u << idx;
+          }
         }
         if (gmask) {
           uint32_t nv[8];
@@ -612,8 +636,9 @@ __global__ void xs_write_kernel(const unsigned long long* __restrict__ tile_ptr,
   const uint64_t tm = (1ULL << lT) - 1ULL;
   for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < ntiles; r += stride) {
     const uint64_t t = ((r & tm) << lT) | (r >> lT);
-    if ((r & tm) == 0) colcum[r >> lT] = ecm[r];
     const uint32_t n = cnt[r], o = off[r], sz = size[r];
+    const unsigned long long wbase = (unsigned long long)ecm[r] + (unsigned long long)o * TS_STAGE_COST;
+    if ((r & tm) == 0) colcum[r >> lT] = wbase;
     const unsigned long long e0 = tile_ptr[t];
     for (uint32_t k = 0; k < n; ++k) {
       TileStage s;
@@ -621,12 +646,13 @@ __global__ void xs_write_kernel(const unsigned long long* __restrict__ tile_ptr,
       s.count = min(TS_P, sz - k * TS_P);
       s.e0 = e0 + (unsigned long long)k * TS_P;
       st[o + k] = s;
-      cum[o + k] = (unsigned long long)ecm[r] + (unsigned long long)k * TS_P;
+      cum[o + k] = wbase + (unsigned long long)k * (TS_P + TS_STAGE_COST);
     }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    cum[*nst] = E;
-    colcum[1ULL << lT] = E;
+    const unsigned long long total = E + (unsigned long long)(*nst) * TS_STAGE_COST;
+    cum[*nst] = total;
+    colcum[1ULL << lT] = total;
   }
 }
 

@@ -71,6 +71,8 @@ def parse(argv=None):
                     help="vertex programs run after every batch (profiling cases use a subset)")
     ap.add_argument("--preload", type=int, default=0,
                     help="with --profile-only: insert this many batches as one batch first")
+    ap.add_argument("--traversal", default="row", choices=["row", "column", "hilbert"],
+                    help="tile visiting order of the column-ordered dense round (the reference's --traversal)")
     return ap.parse_args(argv)
 
 
@@ -245,7 +247,9 @@ def main(argv=None):
     prog_names = args.programs.split(",")
 
     def make_engine():
-        eng = cg.Engine(n, args.vpt, weight_type=cg.WEIGHT_U32, stream=stream.cuda_stream)
+        order = {"row": cg.TRAVERSAL_ROW_FIRST, "column": cg.TRAVERSAL_COLUMN_FIRST,
+                 "hilbert": cg.TRAVERSAL_HILBERT}[args.traversal]
+        eng = cg.Engine(n, args.vpt, weight_type=cg.WEIGHT_U32, stream=stream.cuda_stream, traversal=order)
         make = {"bfs": lambda: cg.BFS(eng, start_vertex=0, max_iterations=args.max_iter),
                 "cc": lambda: cg.CC(eng, max_iterations=args.max_iter),
                 "sssp": lambda: cg.SSSP(eng, start_vertex=0, max_iterations=args.max_iter)}

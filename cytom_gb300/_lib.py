@@ -21,6 +21,7 @@ PTR_HOST, PTR_DEVICE = 0, 1
 UNWEIGHTED, WEIGHT_U32, WEIGHT_F32 = 0, 1, 2
 ALGO_BFS, ALGO_CC, ALGO_SSSP, ALGO_PR_DELTA, ALGO_PAGERANK, ALGO_WPAGERANK, ALGO_SSWP = 0, 1, 2, 3, 4, 5, 6
 ALGO_BFS_ASYNC, ALGO_CC_ASYNC = 7, 8
+TRAVERSAL_ROW_FIRST, TRAVERSAL_COLUMN_FIRST, TRAVERSAL_HILBERT = 0, 1, 2
 KERNEL_CLASSES = 8
 
 
@@ -32,6 +33,8 @@ class Config(C.Structure):
         ("enable_adaptive_scheduling", C.c_int32),
         ("edge_capacity_hint", C.c_uint64),
         ("stream", C.c_void_p),
+        ("traversal", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 
@@ -88,15 +91,23 @@ class KernelStats(C.Structure):
 class TuneReport(C.Structure):
     _fields_ = [("variants", C.c_int32), ("chosen", C.c_int32 * 2), ("edges_per_thread", C.c_int32 * 8),
                 ("pipeline_depth", C.c_int32 * 8), ("blocks_per_sm", C.c_int32 * 8), ("reserved", C.c_int32),
-                ("us", (C.c_double * 8) * 2), ("tuned_edges", C.c_uint64)]
+                ("us", (C.c_double * 8) * 2), ("tuned_edges", C.c_uint64), ("sparse_div", C.c_int32 * 2),
+                ("div_candidates", C.c_int32 * 6), ("dense_round_us", (C.c_double * 6) * 2),
+                ("sparse_round_us", (C.c_double * 6) * 2)]
 
     def as_dict(self) -> dict:
         k = self.variants
         shapes = [{"edges_per_thread": self.edges_per_thread[v], "pipeline_depth": self.pipeline_depth[v],
-                   "blocks_per_sm": self.blocks_per_sm[v]} for v in range(k)]
+                   "blocks_per_sm": self.blocks_per_sm[v], "kernel": "tiles" if v == 4 else "stream"}
+                  for v in range(k)]
         return {"shapes": shapes, "chosen": {"bfs_cc": self.chosen[0], "sssp": self.chosen[1]},
                 "round_us": {"bfs_cc": [self.us[0][v] for v in range(k)], "sssp": [self.us[1][v] for v in range(k)]},
-                "tuned_edges": self.tuned_edges}
+                "tuned_edges": self.tuned_edges,
+                "sparse_div": {"bfs_cc": self.sparse_div[0], "sssp": self.sparse_div[1]},
+                "sparse_threshold_table": {
+                    "div_candidates": list(self.div_candidates),
+                    "bfs_cc": {"dense_us": list(self.dense_round_us[0]), "sparse_us": list(self.sparse_round_us[0])},
+                    "sssp": {"dense_us": list(self.dense_round_us[1]), "sparse_us": list(self.sparse_round_us[1])}}}
 
 
 class FaultInjection(C.Structure):

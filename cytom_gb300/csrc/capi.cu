@@ -127,6 +127,7 @@ int upload_store_desc(Ctx* c) {
   h.dir = c->dir;
   h.nbw = c->lvpt >= 5 ? (uint32_t)(c->vpt / 32) : 0u;
   h.dir_ok = (c->dir && c->dir_version == c->version && !c->dir_disabled) ? 1 : 0;
+  h.traversal = (uint32_t)c->cfg.traversal;
   h.xst = c->xs_stage;
   h.xcum = c->xs_cum;
   h.xcolcum = c->xs_colcum;
@@ -249,6 +250,13 @@ static int job_prepare(Ctx* c, Job* j) {
     if (!rc) rc = ensure_job_queue(c, j);
     if (!rc && autotune_due(c)) rc = minprop_autotune(c);
     if (rc) return rc;
+    // the tuned sparse-round threshold of the job's class, read by its control step
+    const uint32_t div = c->tune_div[(j->algo == CYTOM_ALGO_SSSP || j->algo == CYTOM_ALGO_SSWP) ? 1 : 0];
+    if (div != j->h.sparse_div) {
+      j->h.sparse_div = div;
+      cudaError_t e = cudaMemcpyAsync(j->d, &j->h, sizeof(JobDesc), cudaMemcpyHostToDevice, c->stream);
+      if (e != cudaSuccess) return cuda_err(c, e, "job descriptor upload");
+    }
   }
   if (j->fresh) {
     rc = job_init_state(c, j);
@@ -407,6 +415,7 @@ void cytom_config_default(cytom_config* cfg) {
   cfg->enable_adaptive_scheduling = 1;
   cfg->edge_capacity_hint = 0;
   cfg->stream = nullptr;
+  cfg->traversal = CYTOM_TRAVERSAL_ROW_FIRST;  // TRAVERSAL, src/scripts/config.py:62
 }
 
 void cytom_rmat_default(cytom_rmat_params* p) {
@@ -443,7 +452,8 @@ int cytom_create(const cytom_config* cfg, cytom_ctx** out) {
   while (n < cfg->max_vertices) n <<= 1;  // Config::normalizeConfig rounds up to 2^k
   uint64_t vpt = cfg->vertices_per_tile;
   if (cfg->max_vertices == 0 || vpt == 0 || (vpt & (vpt - 1)) || vpt > 65536 || vpt > n ||
-      n > (1ULL << 32) || (cfg->weight_type < 0 || cfg->weight_type > 2)) {
+      n > (1ULL << 32) || (cfg->weight_type < 0 || cfg->weight_type > 2) || cfg->traversal < 0 ||
+      cfg->traversal > CYTOM_TRAVERSAL_HILBERT) {
     delete c;
     return CYTOM_ERR_INVAL;  // the reference gets 0 tiles when vpt > vertices (config.cc:18-19)
   }
@@ -1012,6 +1022,15 @@ static void fill_tune_report(const Ctx* c, cytom_tune_report* out) {
   for (int k = 0; k < 2; ++k)
     for (int v = 0; v < cnt && v < 8; ++v) out->us[k][v] = c->tune_us[k][v];
   out->tuned_edges = c->tune_E;
+  for (int k = 0; k < 2; ++k) {
+    out->sparse_div[k] = (int32_t)c->tune_div[k];
+    for (int i = 0; i < 6; ++i) {
+      out->dense_round_us[k][i] = c->tune_dense_us[k][i];
+      out->sparse_round_us[k][i] = c->tune_sparse_us[k][i];
+    }
+  }
+  const int32_t divs[6] = {128, 64, 32, 16, 8, 4};
+  for (int i = 0; i < 6; ++i) out->div_candidates[i] = divs[i];
 }
 
 int cytom_autotune(cytom_ctx* ctx, cytom_tune_report* out) {

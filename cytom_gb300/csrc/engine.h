@@ -61,6 +61,8 @@ struct StoreDesc {
   // column-major tile order (column y, then row x); xcum[i] = partition weight before
   // stage i in that order (edges + a fixed cost per stage; xcum[*xnst] = the total);
   // xcolcum[y] = the weight before column y (T + 1 entries)
+  uint32_t traversal;          // tile order of the column-ordered stages (CYTOM_TRAVERSAL_*)
+  uint32_t pad_tr;
   const TileStage* xst;
   const unsigned long long* xcum;
   const unsigned long long* xcolcum;
@@ -117,6 +119,8 @@ struct JobDesc {
   int algo;
   int kahan;
   int async;          // BFS / CC asynchronous programs: sources read from next
+  uint32_t sparse_div;  // tuned sparse-round threshold of the job's class (0: the store's)
+  uint32_t pad_jd;
   double alpha, delta_param;
   unsigned long long start;
 };
@@ -210,6 +214,9 @@ struct Ctx {
   uint64_t tune_E = 0;
   uint64_t tune_epoch = 0;
   double tune_us[2][8] = {};
+  uint32_t tune_div[2] = {0, 0};   // tuned sparse-round threshold per class (0 = untuned)
+  double tune_dense_us[2][6] = {};
+  double tune_sparse_us[2][6] = {};
   // PageRank family: vertices renumbered by out-degree (hubs first) so the hot part of
   // the gathered contribution vector packs densely into L2. perm[v] = position of vertex
   // v, inv[position] = v; fixed once computed. deg_mult = multiplicity out-degrees in

@@ -505,9 +505,12 @@ __global__ void __launch_bounds__(TS_T, 1) gather_tiles_kernel(const JobDesc* __
     if (y != cur_col) {  // uniform: every thread walks the same stages
       if (slice_mode) tiles_flush(jd, slice, S, cur_col << lvpt);
       cur_col = y;
-      const unsigned long long c0 = sd->xcolcum[y], c1 = sd->xcolcum[y + 1];
-      const unsigned long long seg = min(cta_hi, c1) - max(cta_lo, c0);
-      slice_mode = seg >= (unsigned long long)S * TS_SLICE_MIN;
+      slice_mode = false;
+      if (sd->traversal == CYTOM_TRAVERSAL_ROW_FIRST) {  // a column's tiles are consecutive
+        const unsigned long long c0 = sd->xcolcum[y], c1 = sd->xcolcum[y + 1];
+        const unsigned long long seg = min(cta_hi, c1) - max(cta_lo, c0);
+        slice_mode = seg >= (unsigned long long)S * TS_SLICE_MIN;
+      }
     }
     const bool ok = mbar_wait(&bar[slot], (phases >> slot) & 1u);
     phases ^= 1u << slot;
@@ -612,14 +615,50 @@ __global__ void __launch_bounds__(TS_T, 1) gather_tiles_kernel(const JobDesc* __
   if (threadIdx.x == 0 && scanned) atomicAdd(&ls->edges_scanned, scanned);
 }
 
-// Stage list of gather_tiles_kernel, per store version. Column-major rank r = y * T + x
-// names tile t = x * T + y.
-__global__ void xs_count_kernel(const unsigned long long* __restrict__ tile_ptr, uint32_t lT, uint64_t ntiles,
-                                uint32_t* __restrict__ cnt, uint32_t* __restrict__ size) {
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+// Tile at position d of a traversal order (x = source tile, y = target tile, T = 2^lT):
+// row-first d = y * T + x, column-first d = x * T + y (src/lib/traversal/row_first.cc,
+// column_first.cc), or the Hilbert curve's d -> (x, y) (the published curve-walk
+// algorithm that src/lib/traversal/hilbert.cc:35-47 also follows).
+__device__ __forceinline__ uint64_t traversal_tile(uint32_t order, uint64_t d, uint32_t lT) {
   const uint64_t tm = (1ULL << lT) - 1ULL;
+  uint64_t x, y;
+  if (order == CYTOM_TRAVERSAL_COLUMN_FIRST) {
+    x = d >> lT;
+    y = d & tm;
+  } else if (order == CYTOM_TRAVERSAL_HILBERT) {
+    x = 0;
+    y = 0;
+    uint64_t t = d;
+    for (uint64_t s = 1; s < (1ULL << lT); s <<= 1) {
+      const uint64_t rx = 1 & (t >> 1);
+      const uint64_t ry = 1 & (t ^ rx);
+      if (ry == 0) {  // rotate the quadrant
+        if (rx == 1) {
+          x = s - 1 - x;
+          y = s - 1 - y;
+        }
+        const uint64_t tmp = x;
+        x = y;
+        y = tmp;
+      }
+      x += s * rx;
+      y += s * ry;
+      t >>= 2;
+    }
+  } else {
+    y = d >> lT;
+    x = d & tm;
+  }
+  return (x << lT) | y;
+}
+
+// Stage list of gather_tiles_kernel, per store version: the tiles in the traversal order
+// (rank r names tile traversal_tile(r)), each cut into stages of at most TS_P edges.
+__global__ void xs_count_kernel(const unsigned long long* __restrict__ tile_ptr, uint32_t lT, uint64_t ntiles,
+                                uint32_t order, uint32_t* __restrict__ cnt, uint32_t* __restrict__ size) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < ntiles; r += stride) {
-    const uint64_t t = ((r & tm) << lT) | (r >> lT);
+    const uint64_t t = traversal_tile(order, r, lT);
     const uint64_t sz = tile_ptr[t + 1] - tile_ptr[t];
     size[r] = (uint32_t)sz;
     cnt[r] = (uint32_t)((sz + TS_P - 1) / TS_P);
@@ -627,7 +666,7 @@ __global__ void xs_count_kernel(const unsigned long long* __restrict__ tile_ptr,
 }
 
 __global__ void xs_write_kernel(const unsigned long long* __restrict__ tile_ptr, uint32_t lT, uint64_t ntiles,
-                                const uint32_t* __restrict__ cnt, const uint32_t* __restrict__ off,
+                                uint32_t order, const uint32_t* __restrict__ cnt, const uint32_t* __restrict__ off,
                                 const uint32_t* __restrict__ size, const uint32_t* __restrict__ ecm,
                                 const uint32_t* __restrict__ nst, TileStage* __restrict__ st,
                                 unsigned long long* __restrict__ cum, unsigned long long* __restrict__ colcum,
@@ -635,10 +674,10 @@ __global__ void xs_write_kernel(const unsigned long long* __restrict__ tile_ptr,
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const uint64_t tm = (1ULL << lT) - 1ULL;
   for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < ntiles; r += stride) {
-    const uint64_t t = ((r & tm) << lT) | (r >> lT);
+    const uint64_t t = traversal_tile(order, r, lT);
     const uint32_t n = cnt[r], o = off[r], sz = size[r];
     const unsigned long long wbase = (unsigned long long)ecm[r] + (unsigned long long)o * TS_STAGE_COST;
-    if ((r & tm) == 0) colcum[r >> lT] = wbase;
+    if ((r & tm) == 0) colcum[r >> lT] = wbase;  // row-first: the first tile of column r >> lT
     const unsigned long long e0 = tile_ptr[t];
     for (uint32_t k = 0; k < n; ++k) {
       TileStage s;
@@ -703,13 +742,14 @@ int build_tile_stages(Ctx* c) {
   uint32_t* ecm = size + nt;
   int slot = prof_begin(c, KC_MERGE);
   xs_count_kernel<<<std::max(1, std::min<int>(grid_persistent(c, 8), (int)((nt + 255) / 256))), 256, 0, c->stream>>>(
-      c->tile_ptr, c->lT, nt, cnt, size);
+      c->tile_ptr, c->lT, nt, (uint32_t)c->cfg.traversal, cnt, size);
   c->launches++;
   int rc = exclusive_scan_u32(c, cnt, off, nt, nst);
   if (!rc) rc = exclusive_scan_u32(c, size, ecm, nt, tot);
   if (rc) return rc;
   xs_write_kernel<<<std::max(1, std::min<int>(grid_persistent(c, 8), (int)((nt + 255) / 256))), 256, 0, c->stream>>>(
-      c->tile_ptr, c->lT, nt, cnt, off, size, ecm, nst, c->xs_stage, c->xs_cum, c->xs_colcum, c->E);
+      c->tile_ptr, c->lT, nt, (uint32_t)c->cfg.traversal, cnt, off, size, ecm, nst, c->xs_stage, c->xs_cum,
+      c->xs_colcum, c->E);
   c->launches++;
   prof_end(c, slot, (double)nt * 28.0 + (double)need * 24.0);
   cudaError_t e = cudaGetLastError();
@@ -1337,15 +1377,65 @@ __global__ void tune_state_kernel(JobDesc* jd, const StoreDesc* __restrict__ sd,
   }
 }
 
+// Frontier of the sparse-threshold tuning: word i is non-zero with probability 1/div,
+// with one vertex chosen by a hash of i; next = current = vertex id; a fresh loop state.
+// The seeding apply (apply_minprop_kernel, initial) then lists the words and flags rows.
+__global__ void tune_frontier_kernel(JobDesc* jd, const StoreDesc* __restrict__ sd, LoopState* ls, uint32_t div) {
+  const uint64_t n = sd->n, nwords = (n + 31) >> 5, T = sd->T;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (uint64_t v = tid; v < n; v += stride) {
+    jd->cur[v] = (uint32_t)v;
+    jd->next[v] = (uint32_t)v;
+  }
+  for (uint64_t i = tid; i < nwords; i += stride) {
+    uint32_t h = (uint32_t)i * 0x9E3779B9u + 0x7F4A7C15u;
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    jd->ch[i] = (h % div == 0) ? (1u << ((h >> 20) & 31u)) : 0u;
+  }
+  for (uint64_t x = tid; x < 2 * T; x += stride) jd->rows[x] = 0;
+  if (tid == 0) {
+    ls->iter = 0;
+    ls->max_iter = 1000;
+    ls->cont = 1;
+    ls->err = 0;
+    ls->active[0] = ls->active[1] = 0;
+    ls->nact_words[0] = ls->nact_words[1] = 0;
+    ls->teps[0] = ls->teps[1] = 0;
+    ls->spq_count = 0;
+    ls->apply_done = 0;
+    ls->sel_rounds = 0;
+  }
+}
+
+__global__ void tune_mode_kernel(LoopState* ls, unsigned mode) {
+  ls->mode = mode;
+  ls->cont = 1;
+  ls->spq_count = 0;
+}
+
+static const uint32_t kDivCandidates[6] = {128, 64, 32, 16, 8, 4};
+
+static bool sparse_div_from_env() {
+  static int v = -1;
+  if (v < 0) v = getenv("CYTOM_SPARSE_DIV") ? 1 : 0;
+  return v == 1;
+}
+
 int minprop_autotune(Ctx* c) {
-  int brc = build_tile_stages(c);
+  int brc = build_directory(c);
+  if (!brc) brc = build_tile_stages(c);
   if (brc) return brc;
   const uint64_t n = c->n, nwords = (n + 31) / 32;
   JobDesc h{};
   LoopState* ls = nullptr;
   JobDesc* d = nullptr;
   char* buf = nullptr;
-  const size_t bytes = n * 8 + nwords * 8 + 2 * c->T * 4 + nwords * 4 + sizeof(LoopState) + sizeof(JobDesc) + 4096;
+  const uint64_t qcap = c->E / 32 + c->E / 256 + 1024;
+  const size_t bytes = n * 8 + nwords * 8 + 2 * c->T * 4 + nwords * 4 + sizeof(LoopState) + sizeof(JobDesc) +
+                       qcap * sizeof(uint2) + 8 * 256;
   if (cy_malloc_async((void**)&buf, bytes, c->stream) != cudaSuccess) {
     cudaGetLastError();
     return CYTOM_OK;  // no memory to tune with: keep the current shapes
@@ -1364,6 +1454,8 @@ int minprop_autotune(Ctx* c) {
   h.aw = (uint32_t*)take(nwords * 4);
   ls = (LoopState*)take(sizeof(LoopState));
   d = (JobDesc*)take(sizeof(JobDesc));
+  h.spq = (uint2*)take(qcap * sizeof(uint2));
+  h.spq_cap = qcap;
   h.ls = ls;
   cudaMemsetAsync(ls, 0, sizeof(LoopState), c->stream);
   cudaMemcpyAsync(d, &h, sizeof(JobDesc), cudaMemcpyHostToDevice, c->stream);
@@ -1402,6 +1494,46 @@ int minprop_autotune(Ctx* c) {
       }
     }
     if (e == cudaSuccess) c->sg_variant[cls] = best;
+    // sparse-round threshold of this class: dense (the chosen kernel) against sparse
+    // (directory walk + chunk pass) rounds on frontiers of growing density
+    c->tune_div[cls] = 0;
+    if (e == cudaSuccess && c->hsd.dir_ok && c->cfg.enable_adaptive_scheduling && !sparse_div_from_env()) {
+      GatherLaunch gd = stream_launch(c, algo, best);
+      const int g_apply = resident_grid(c, (void*)apply_minprop_kernel, APPLY_T);
+      const int g_sparse = resident_grid(c, sparse_fn(algo), 256);
+      const int g_chunks = resident_grid(c, chunks_fn(algo), 256);
+      void* a_q[] = {(void*)&jd, (void*)&sd};
+      uint32_t div = 0;
+      bool losing = false;
+      for (int k = 0; k < 6 && e == cudaSuccess; ++k) {
+        double t_mode[2] = {1e300, 1e300};
+        for (unsigned mode = 0; mode < 2 && e == cudaSuccess; ++mode) {
+          for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep) {
+            tune_frontier_kernel<<<grid_persistent(c, 4), 256, 0, c->stream>>>(d, sd, ls, kDivCandidates[k]);
+            apply_minprop_kernel<<<g_apply, APPLY_T, 0, c->stream>>>(d, sd, 1, 0, 0);
+            tune_mode_kernel<<<1, 1, 0, c->stream>>>(ls, mode);
+            cudaEventRecord(a, c->stream);
+            if (mode == 0) {
+              e = cudaLaunchKernel(gd.fn, gd.grid, gd.block, args, gd.smem, c->stream);
+            } else {
+              e = cudaLaunchKernel(sparse_fn(algo), dim3(g_sparse), dim3(256), args, 0, c->stream);
+              if (e == cudaSuccess) e = cudaLaunchKernel(chunks_fn(algo), dim3(g_chunks), dim3(256), a_q, 0, c->stream);
+            }
+            cudaEventRecord(b, c->stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(b);
+            float ms = 0.f;
+            if (e == cudaSuccess) cudaEventElapsedTime(&ms, a, b);
+            t_mode[mode] = std::min(t_mode[mode], (double)ms * 1e3);
+            c->launches += 5;
+          }
+        }
+        c->tune_dense_us[cls][k] = t_mode[0];
+        c->tune_sparse_us[cls][k] = t_mode[1];
+        if (!losing && t_mode[1] < t_mode[0]) div = kDivCandidates[k];
+        else losing = true;
+      }
+      if (e == cudaSuccess) c->tune_div[cls] = div ? div : 1024;
+    }
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);

@@ -224,7 +224,8 @@ __device__ __forceinline__ unsigned control_step(const JobDesc* __restrict__ jd,
     ls->active_total = ls->active_total + a;
     ls->cont = (a > 0 && iter < ls->max_iter && ls->err == 0) ? 1u : 0u;
     const uint64_t nwords = (sd->n + 31) >> 5;
-    ls->mode = (sd->dir_ok && sd->adaptive && (uint64_t)ls->nact_words[p] * sd->sparse_div <= nwords) ? 1u : 0u;
+    const uint32_t div = jd->sparse_div ? jd->sparse_div : sd->sparse_div;
+    ls->mode = (sd->dir_ok && sd->adaptive && (uint64_t)ls->nact_words[p] * div <= nwords) ? 1u : 0u;
     ls->spq_count = 0;
   }
   return ls->cont;

@@ -74,6 +74,18 @@ extern "C" {
 #define CYTOM_ALGO_BFS_ASYNC 7
 #define CYTOM_ALGO_CC_ASYNC 8
 
+/* Tile visiting order of the column-ordered dense round (dense-round variant 4, see
+ * cytom_tune_report), the reference's --traversal (src/include/util/config.h traversal_t;
+ * src/lib/traversal/row_first.cc, column_first.cc, hilbert.cc; default row-first,
+ * src/scripts/config.py:62). x = source tile, y = target tile, T tiles per dimension.
+ * The work of a round is this sequence of tiles cut into equal contiguous ranges, one
+ * per SM (the reference's meta-tiles of consecutive tiles, src/include/core/tile-distributor.h). */
+#define CYTOM_TRAVERSAL_ROW_FIRST 0    /* d = y * T + x: all sources of a target tile column in a
+                                          row; only this order reduces a column's targets in
+                                          shared memory */
+#define CYTOM_TRAVERSAL_COLUMN_FIRST 1 /* d = x * T + y: the store's tile-major order */
+#define CYTOM_TRAVERSAL_HILBERT 2      /* d along the Hilbert curve over (x, y) (hilbert.cc) */
+
 /* Context configuration: the subset of ConfigContext (src/include/util/config.h:529-567)
  * and its command-line flags (src/include/core/jobs.h:176-216) that the hot path uses. */
 typedef struct cytom_config {
@@ -84,6 +96,8 @@ typedef struct cytom_config {
   int32_t enable_adaptive_scheduling; /* --enable-adaptive-scheduling (skip inactive tile rows) */
   uint64_t edge_capacity_hint;   /* initial edge capacity; the store grows on demand */
   void* stream;                  /* cudaStream_t to run on; NULL = the context's own stream */
+  int32_t traversal;             /* --traversal: CYTOM_TRAVERSAL_* (default row-first) */
+  int32_t reserved;
 } cytom_config;
 
 /* Fills *cfg with the reference defaults (src/scripts/config.py:45-109). */
@@ -366,6 +380,16 @@ typedef struct cytom_tune_report {
   int32_t reserved;
   double us[2][8];       /* best of three timed rounds; 0 = not measured */
   uint64_t tuned_edges;  /* edge count the choice was made at (0 = never tuned) */
+  /* Sparse-round threshold: a round walks only the listed frontier words (the source
+   * directory) while at most 1/sparse_div of the frontier words are non-zero, else it
+   * streams every active tile row. Tuned per program class by timing both kinds of
+   * round on frontiers with 1/div_candidates[k] of the words non-zero (one active
+   * vertex each); sparse_div = the largest such density at which the sparse round was
+   * faster. 0 = not tuned (the default 8, or CYTOM_SPARSE_DIV, applies). */
+  int32_t sparse_div[2];
+  int32_t div_candidates[6];
+  double dense_round_us[2][6];
+  double sparse_round_us[2][6];
 } cytom_tune_report;
 /* Times every shape on the current graph (compacting first) and keeps the fastest.
  * Runs by itself once per context, on a job's first run at >= 2^20 edges (environment

@@ -34,13 +34,24 @@ def test_bindings_cover_header(cg):
     assert set(declared_symbols()) <= bound
 
 
-def test_struct_layouts(cg):
+def test_struct_layouts(cg, tmp_path):
+    # every struct of the header has the same size in C (gcc) and in the ctypes binding
     import ctypes as C
     L = cg._lib
-    assert C.sizeof(L.Config) == 40
-    assert C.sizeof(L.RmatParams) == 56
-    assert C.sizeof(L.JobParams) == 48
-    assert C.sizeof(L.RunStats) == 56
+    pairs = {"cytom_config": L.Config, "cytom_rmat_params": L.RmatParams, "cytom_job_params": L.JobParams,
+             "cytom_run_stats": L.RunStats, "cytom_tune_report": L.TuneReport, "cytom_kernel_stats": L.KernelStats,
+             "cytom_fault_injection": L.FaultInjection}
+    src = tmp_path / "sizes.c"
+    src.write_text('#include <stdio.h>\n#include "cytom_gpu.h"\nint main(void) {\n' +
+                   "".join(f'  printf("{k} %zu\\n", sizeof({k}));\n' for k in pairs) + "  return 0;\n}\n")
+    exe = tmp_path / "sizes"
+    r = subprocess.run(["gcc", "-std=c11", "-I", str(ROOT / "include"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    sizes = dict(zip(out[0::2], map(int, out[1::2])))
+    for k, cls in pairs.items():
+        assert C.sizeof(cls) == sizes[k], (k, C.sizeof(cls), sizes[k])
 
 
 def test_cpp_header_compiles():

@@ -167,9 +167,11 @@ print(json.dumps(out))
         assert all(checks), (mode, name, checks)
 
 
-@pytest.mark.parametrize("sparse", ["0", "1"])
-def test_sparse_and_dense_rounds_agree(cg, orc, sparse, tmp_path):
-    # incremental runs on a growing graph, with sparse (directory) rounds allowed or not
+@pytest.mark.parametrize("sparse,div", [("0", None), ("1", None), ("1", "2"), ("1", "64")])
+def test_sparse_and_dense_rounds_agree(cg, orc, sparse, div, tmp_path):
+    # incremental runs on a growing graph, with sparse (directory) rounds allowed or not,
+    # at the tuned threshold and at fixed thresholds the tuner may choose from (a sparse
+    # round while at most 1/div of the frontier words are non-zero)
     import json
     import os
     import subprocess
@@ -202,10 +204,12 @@ with cg.Engine(n, vpt, weight_type=cg.WEIGHT_U32) as eng:
 print(json.dumps(ok))
 """
     env = dict(os.environ, CYTOM_SPARSE=sparse)
+    if div:
+        env["CYTOM_SPARSE_DIV"] = div
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=900)
     assert r.returncode == 0, r.stderr[-2000:]
     ok = json.loads(r.stdout.strip().splitlines()[-1])
-    assert all(ok), (sparse, ok)
+    assert all(ok), (sparse, div, ok)
 
 
 @pytest.mark.parametrize("variant", ["0", "1", "2", "3", "4"])
@@ -274,13 +278,36 @@ def test_autotune_report(cg, orc):
         assert k >= 2 and all(x > 0 for x in rep["round_us"]["bfs_cc"]) and all(x > 0 for x in rep["round_us"]["sssp"])
         best = rep["chosen"]["sssp"]
         assert rep["round_us"]["sssp"][best] == min(rep["round_us"]["sssp"])
-        p = cg.SSSP(eng, start_vertex=0, max_iterations=1000)
-        p.execute_algorithm()
+        # the sparse-round threshold: one of the candidates (1024 = sparse rounds lost
+        # at every tried density), with both round kinds timed at every density
+        cands = rep["sparse_threshold_table"]["div_candidates"]
+        for cls in ("bfs_cc", "sssp"):
+            assert rep["sparse_div"][cls] in cands + [1024], rep["sparse_div"]
+            tab = rep["sparse_threshold_table"][cls]
+            assert all(x > 0 for x in tab["dense_us"]) and all(x > 0 for x in tab["sparse_us"])
         st = orc.Store(n, vpt, True)
         st.insert(s, t, w)
         st.compact()
-        ref, _ = st.run_minprop(2, start=0, max_iter=1000)
-        assert np.array_equal(p.result(), ref)
+        for prog, algo in ((cg.BFS, 0), (cg.CC, 1), (cg.SSSP, 2)):
+            p = prog(eng, start_vertex=0, max_iterations=1000)
+            stt = p.execute_algorithm()
+            ref, info = st.run_minprop(algo, start=0, max_iter=1000)
+            assert np.array_equal(p.result(), ref)
+            assert stt["iterations"] == info["iterations"] and stt["count_edges"] == info["count_edges"]
+        # incremental runs after further batches use the tuned threshold on small frontiers
+        progs = [cg.BFS(eng, start_vertex=0, max_iterations=1000), cg.SSSP(eng, start_vertex=0, max_iterations=1000)]
+        for p in progs:
+            p.execute_algorithm()
+        for b in range(3):
+            s2, t2 = orc.rmat(scale, 16 * n + b * 20000, 20000, 9)
+            w2 = orc.edge_weights(s2, t2, 10)
+            eng.insert_edges(s2, t2, w2)
+            st.insert(s2, t2, w2)
+            st.compact()
+            for p, algo in zip(progs, (0, 2)):
+                p.execute_algorithm()
+                ref, _ = st.run_minprop(algo, start=0, max_iter=1000)
+                assert np.array_equal(p.result(), ref), (b, algo)
 
 
 @pytest.mark.parametrize("name,algo", [("BFSAsync", 0), ("CCAsync", 1)])
@@ -353,3 +380,52 @@ def test_run_many_concurrent_jobs(cg, orc):
         assert len(out) == 2 and out[1]["iterations"] > 0
         with pytest.raises(cg.CytomError):
             ea.run_many([pa[0], pa[0]])
+
+
+def test_traversal_orders_agree(cg, orc):
+    # the column-ordered dense round (variant 4) visits the tiles in each of the
+    # reference's traversal orders (row-first, column-first, Hilbert): the same values,
+    # rounds, processed-edge counts and scanned edges as the oracle / each other
+    import json
+    import os
+    import subprocess
+    import sys
+    code = f"""
+import sys, json, numpy as np
+sys.path.insert(0, {str(__import__('pathlib').Path(__file__).resolve().parents[1])!r})
+import cytom_gb300 as cg
+from oracle import oracle as orc
+out = []
+for scale, vpt in ((16, 4096), (17, 1024)):
+    n = 1 << scale
+    s, t = orc.rmat(scale, 0, 16 * n, 13)
+    w = orc.edge_weights(s, t, 14)
+    st = orc.Store(n, vpt, True)
+    st.insert(s, t, w); st.compact()
+    scans = []
+    for order in (cg.TRAVERSAL_ROW_FIRST, cg.TRAVERSAL_COLUMN_FIRST, cg.TRAVERSAL_HILBERT):
+        with cg.Engine(n, vpt, weight_type=cg.WEIGHT_U32, traversal=order) as eng:
+            eng.insert_edges(s, t, w)
+            sc = []
+            for prog, algo in ((cg.BFS, 0), (cg.CC, 1), (cg.SSSP, 2), (cg.SSWP, 3)):
+                p = prog(eng, start_vertex=0, max_iterations=1000)
+                stt = p.execute_algorithm()
+                ref, info = st.run_minprop(algo, start=0, max_iter=1000)
+                out.append(bool(np.array_equal(p.result(), ref)) and stt["iterations"] == info["iterations"]
+                           and stt["count_edges"] == info["count_edges"])
+                sc.append(stt["edges_scanned"])
+            scans.append(sc)
+    out.append(scans[0] == scans[1] == scans[2])
+print(json.dumps(out))
+"""
+    env = dict(os.environ, CYTOM_SG_VARIANT="4", CYTOM_SPARSE="0", CYTOM_AUTOTUNE="0")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=900)
+    assert r.returncode == 0, r.stderr[-2000:]
+    ok = json.loads(r.stdout.strip().splitlines()[-1])
+    assert all(ok), ok
+
+
+def test_engine_rejects_unknown_traversal(cg):
+    with pytest.raises(cg.CytomError) as ei:
+        cg.Engine(1 << 12, 1024, traversal=7)
+    assert ei.value.code == -1

@@ -208,7 +208,8 @@ def batching(args) -> dict:
     4 further insert batches of 5% of its edges with a job round after each. The batched
     arm runs each job round as ONE persistent launch (cytom_run_batch); the plain arm
     runs each job by itself (cytom_run: one CUDA-graph launch per BFS/CC/SSSP run and per
-    PageRank run). Inserts and compactions are untimed and identical in both arms; a job
+    PageRank run); the batched launch pairs the two PageRank jobs of a snapshot (one pass
+    per round for both). Inserts and compactions are untimed and identical in both arms; a job
     round is timed from the first call to the readback of the last job's statistics.
     BFS/CC/SSSP results of the two arms are compared bit for bit after every round."""
     import torch
@@ -274,6 +275,12 @@ def batching(args) -> dict:
     run_arm(False)  # warm-up passes (allocations, graph builds)
     run_arm(True)
     tp, rp, sp, lp, _ = run_arm(False)
+    # the batched arm with every job on passes of its own (no PageRank pairs), for the record
+    os.environ["CYTOM_BATCH_PAIR"] = "0"
+    try:
+        tu, _, _, _, _ = run_arm(True)
+    finally:
+        del os.environ["CYTOM_BATCH_PAIR"]
     tb, rb, sb, lb, Es = run_arm(True)
     exact = all(np.array_equal(x, y) for ra, rb_ in zip(rp, rb) for x, y in zip(ra, rb_))
     njobs = len(sb[0])
@@ -323,6 +330,9 @@ def batching(args) -> dict:
                        "jobs": njobs, "job_rounds": rounds + 1, "snapshot_scales": scales,
                        "vertices_per_tile": "min(65536, vertices / 4)"},
             "batched_jobs_per_s": jobs_b, "plain_jobs_per_s": jobs_p, "batched_over_plain": jobs_b / jobs_p,
+            "batched_unpaired_jobs_per_s": njobs * (rounds + 1) / sum(tu),
+            "pairing": "the two PageRank jobs of each snapshot share one pass per round (cytom_run_batch pairs "
+                       "PageRank jobs of one context and form); unpaired = every job on passes of its own",
             "round_ms_batched": [1e3 * x for x in tb], "round_ms_plain": [1e3 * x for x in tp],
             "integer_results_bit_exact": bool(exact), "rounds_and_counts_equal": bool(counts_equal),
             "batched_device_ms_per_round": [st[0]["elapsed_ms"] for st in sb],

@@ -227,6 +227,8 @@ struct Ctx {
   uint64_t pr_deg_mult_version = ~0ULL;
   void* pr_csc = nullptr;
   void* pr_wgraph = nullptr;  // weighted PageRank: CSC + CSR with weights
+  void* pr_pair = nullptr;    // batched executor: interleaved contributions of paired PageRank jobs
+  size_t pr_pair_bytes = 0;
   void* edge_log = nullptr;   // open edge log (cytom_persist_edges)
   // column-ordered stage list of the dense round, rebuilt when the store version changes
   TileStage* xs_stage = nullptr;

@@ -23,6 +23,7 @@
 // Values written during the launch are read through L2 (the PERSIST load policy).
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -68,9 +69,13 @@ struct BJob {
   const JobDesc* jd;
   const StoreDesc* sd;
   PrArgs pr;
+  PrArgs pr2;                      // paired PAGERANK job (paired = 1): its arguments
+  void* cpair;                     // paired jobs: interleaved contributions {job, pr2 job}
   unsigned long long nb[kPrBins];  // PageRank target bins
   int algo;
   int adaptive;
+  int paired;
+  int pad_bj;
 };
 
 struct __align__(128) BSched {
@@ -236,6 +241,266 @@ __device__ void unit_pr_pull(const BJob* J, uint32_t unit) {
   pr_tally_flush<MODE>(ls, p, t);
 }
 
+// ---- two PAGERANK jobs of one snapshot in one pass ---------------------------------
+// Jobs of one context and form (FP32 compensated, or FP64 plain) share a round's passes:
+// the contribution pass writes both jobs' contributions interleaved per source, so the
+// pull loads each in-edge's source id once and one pair of contributions for both jobs
+// (one L2 sector where two jobs apart take two). Each job keeps its own ranks, loop
+// state, parameters and summation order: its sums are those of a pass of its own, bit
+// for bit. A job that converges first stops updating; the pair runs until both have.
+template <int MODE>
+struct PrPairT;
+template <>
+struct PrPairT<PR_NORM32> {
+  using T = float2;
+};
+template <>
+struct PrPairT<PR_NORM64> {
+  using T = double2;
+};
+template <int MODE>
+using pr_pair_t = typename PrPairT<MODE>::T;
+
+__device__ __forceinline__ bool pr_on(const LoopState* ls) { return __ldcg(&ls->cont) != 0u; }
+
+// One job's contribution of source u and its dangling share, as pr_contrib_range computes
+// them (NORM32: FP32 quotient of the rank's high word; NORM64: FP64 quotient).
+template <int MODE>
+__device__ __forceinline__ pr_val_t<MODE> pr_pair_contrib(const PrArgs& a, unsigned p, uint64_t u, uint32_t d,
+                                                          double& dangling) {
+  if constexpr (MODE == PR_NORM32) {
+    const float* r = (p == 0) ? a.rank : a.comp;
+    const float* rl = (p == 0) ? a.lo0 : a.lo1;
+    const float rh = __ldcg(r + u);
+    if (!d) dangling += (double)rh + (double)__ldcg(rl + u);
+    return d ? rh / (float)d : 0.f;
+  } else {
+    const double* r = (p == 0) ? a.r64 : a.r64n;
+    const double rv = __ldcg(r + u);
+    if (!d) dangling += rv;
+    return d ? rv / (double)d : 0.0;
+  }
+}
+
+template <int MODE>
+__device__ void unit_pr_contrib_pair(const BJob* J, uint32_t unit) {
+  const PrArgs& a0 = J->pr;
+  const PrArgs& a1 = J->pr2;
+  const bool on0 = pr_on(a0.ls), on1 = pr_on(a1.ls);
+  const unsigned p0 = ls_iter(a0.ls) & 1u, p1 = ls_iter(a1.ls) & 1u;
+  pr_pair_t<MODE>* cw = reinterpret_cast<pr_pair_t<MODE>*>(J->cpair);
+  const uint64_t lo = (uint64_t)unit * BU_PR_VERTS;
+  const uint64_t hi = std::min<uint64_t>(lo + BU_PR_VERTS, a0.n);
+  double d0 = 0.0, d1 = 0.0;
+  for (uint64_t u = lo + threadIdx.x; u < hi; u += BT) {
+    const uint32_t d = a0.deg[u];  // the snapshot's out-degrees, shared by both jobs
+    pr_pair_t<MODE> c;
+    c.x = on0 ? pr_pair_contrib<MODE>(a0, p0, u, d, d0) : (pr_val_t<MODE>)0;
+    c.y = on1 ? pr_pair_contrib<MODE>(a1, p1, u, d, d1) : (pr_val_t<MODE>)0;
+    cw[u] = c;
+  }
+  pr_dangling_flush<MODE>(a0.ls, p0, d0);
+  pr_dangling_flush<MODE>(a1.ls, p1, d1);
+}
+
+// pr_lane_sum over the interleaved pairs: the same edges in the same order for each job.
+template <int MODE, int B, class Acc>
+__device__ __forceinline__ void pr_lane_sum_pair(const PrArgs& a, const pr_pair_t<MODE>* cp, uint32_t e0, uint32_t hi,
+                                                 uint32_t stride, Acc& acc0, Acc& acc1) {
+  uint32_t id[B];
+#pragma unroll
+  for (int k = 0; k < B; ++k) {
+    const uint32_t e = e0 + (uint32_t)k * stride;
+    id[k] = e < hi ? a.csc_src[e] : 0u;
+  }
+  for (uint32_t e = e0; e < hi; e += (uint32_t)B * stride) {
+    pr_pair_t<MODE> c[B];
+#pragma unroll
+    for (int k = 0; k < B; ++k) {
+      const uint32_t ek = e + (uint32_t)k * stride;
+      if (ek < hi) {
+        c[k] = __ldcg(cp + id[k]);
+      } else {
+        c[k].x = 0;
+        c[k].y = 0;
+      }
+    }
+    const uint32_t en = e + (uint32_t)B * stride;
+#pragma unroll
+    for (int k = 0; k < B; ++k) {
+      const uint32_t ek = en + (uint32_t)k * stride;
+      id[k] = ek < hi ? a.csc_src[ek] : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < B; ++k)
+      if (e + (uint32_t)k * stride < hi) {
+        acc0.add(c[k].x);
+        acc1.add(c[k].y);
+      }
+  }
+}
+
+template <int MODE>
+using pr_acc_t = typename std::conditional<pr_is64<MODE>(), Acc64, Acc32>::type;
+
+template <int MODE>
+__device__ __forceinline__ double pr_acc_value(const Acc32& a) {
+  return (double)a.s + (double)a.e;
+}
+template <int MODE>
+__device__ __forceinline__ double pr_acc_value(const Acc64& a) {
+  return a.s;
+}
+
+// A group of VW lanes merges its lanes by an xor tree, as pr_sum_group does.
+template <int VW>
+__device__ __forceinline__ void pr_group_merge(Acc32& acc) {
+#pragma unroll
+  for (int o = VW / 2; o > 0; o >>= 1) {
+    const float s2 = __shfl_xor_sync(0xFFFFFFFFu, acc.s, o, VW);
+    const float e2 = __shfl_xor_sync(0xFFFFFFFFu, acc.e, o, VW);
+    acc.merge(s2, e2);
+  }
+}
+template <int VW>
+__device__ __forceinline__ void pr_group_merge(Acc64& acc) {
+#pragma unroll
+  for (int o = VW / 2; o > 0; o >>= 1) acc.s += __shfl_xor_sync(0xFFFFFFFFu, acc.s, o, VW);
+}
+
+// Whole-block sum (pr_sum_block's reduction) of both jobs; thread 0 holds the sums.
+template <int MODE>
+__device__ __forceinline__ void pr_block_pair(const PrArgs& a, const pr_pair_t<MODE>* cp, uint32_t v, double& s0,
+                                              double& s1) {
+  __shared__ float s_s[2][BT / 32], s_e[2][BT / 32];
+  __shared__ double s_d[2][BT / 32];
+  const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const uint32_t lo = a.csc_ptr[v], hi = a.csc_ptr[v + 1];
+  pr_acc_t<MODE> acc0, acc1;
+  acc0.init();
+  acc1.init();
+  pr_lane_sum_pair<MODE, 4>(a, cp, lo + threadIdx.x, hi, BT, acc0, acc1);
+  pr_group_merge<32>(acc0);
+  pr_group_merge<32>(acc1);
+  if constexpr (pr_is64<MODE>()) {
+    if (lane == 0) {
+      s_d[0][wid] = acc0.s;
+      s_d[1][wid] = acc1.s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      s0 = 0.0;
+      s1 = 0.0;
+      for (int k = 0; k < BT / 32; ++k) {
+        s0 += s_d[0][k];
+        s1 += s_d[1][k];
+      }
+    }
+  } else {
+    if (lane == 0) {
+      s_s[0][wid] = acc0.s;
+      s_e[0][wid] = acc0.e;
+      s_s[1][wid] = acc1.s;
+      s_e[1][wid] = acc1.e;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      Acc32 t0, t1;
+      t0.init();
+      t1.init();
+      for (int k = 0; k < BT / 32; ++k) {
+        t0.merge(s_s[0][k], s_e[0][k]);
+        t1.merge(s_s[1][k], s_e[1][k]);
+      }
+      s0 = (double)t0.s + (double)t0.e;
+      s1 = (double)t1.s + (double)t1.e;
+    }
+  }
+  __syncthreads();
+}
+
+template <int MODE>
+__device__ void unit_pr_pull_pair(const BJob* J, uint32_t unit) {
+  const PrArgs& a0 = J->pr;
+  const PrArgs& a1 = J->pr2;
+  const bool on0 = pr_on(a0.ls), on1 = pr_on(a1.ls);
+  const unsigned p0 = ls_iter(a0.ls) & 1u, p1 = ls_iter(a1.ls) & 1u;
+  const double dang0 = pr_dang_arg<MODE, true>(a0.ls, p0, a0.n);
+  const double dang1 = pr_dang_arg<MODE, true>(a1.ls, p1, a1.n);
+  int k = 0;
+  uint64_t off = 0;
+  uint32_t u = unit;
+  for (; k < kPrBins - 1; ++k) {
+    const uint32_t units_k = ceil_div(J->nb[k], pr_bin_unit(k));
+    if (u < units_k) break;
+    u -= units_k;
+    off += J->nb[k];
+  }
+  const uint64_t cnt = J->nb[k];
+  const uint64_t first = (uint64_t)u * pr_bin_unit(k);
+  const pr_pair_t<MODE>* cp = reinterpret_cast<const pr_pair_t<MODE>*>(J->cpair);
+  PrTally t0, t1;
+  t0.init();
+  t1.init();
+  auto finish = [&](uint32_t v, double s0, double s1) {
+    if (on0) pr_finish<MODE, true>(a0, v, s0, p0, dang0, t0);
+    if (on1) pr_finish<MODE, true>(a1, v, s1, p1, dang1, t1);
+  };
+  const int vw = pr_bin_vw(k);
+  if (vw == 1) {
+#pragma unroll 1
+    for (uint32_t r = 0; r < 4; ++r) {
+      const uint64_t i = first + (uint64_t)r * BT + threadIdx.x;
+      if (i < cnt) {
+        const uint32_t v = a0.bins[off + i];
+        pr_acc_t<MODE> acc0, acc1;
+        acc0.init();
+        acc1.init();
+        pr_lane_sum_pair<MODE, 4>(a0, cp, a0.csc_ptr[v], a0.csc_ptr[v + 1], 1u, acc0, acc1);
+        finish(v, pr_acc_value<MODE>(acc0), pr_acc_value<MODE>(acc1));
+      }
+    }
+  } else if (vw == 0) {
+    const uint32_t v = a0.bins[off + first];
+    double s0 = 0.0, s1 = 0.0;
+    pr_block_pair<MODE>(a0, cp, v, s0, s1);
+    if (threadIdx.x == 0) finish(v, s0, s1);
+  } else {
+    // groups of VW lanes, four targets per group (pull_groups)
+    const unsigned VW = (unsigned)vw;
+    const uint32_t GPB = BT / VW;
+    const unsigned gl = threadIdx.x & (VW - 1);
+    const uint32_t g = threadIdx.x / VW;
+#pragma unroll 1
+    for (uint32_t r = 0; r < 4; ++r) {
+      const uint64_t i = first + (uint64_t)r * GPB + g;
+      uint32_t v = 0, lo = 0, hi = 0;
+      if (i < cnt) {
+        v = a0.bins[off + i];
+        lo = a0.csc_ptr[v];
+        hi = a0.csc_ptr[v + 1];
+      }
+      pr_acc_t<MODE> acc0, acc1;
+      acc0.init();
+      acc1.init();
+      pr_lane_sum_pair<MODE, 4>(a0, cp, lo + gl, hi, VW, acc0, acc1);
+      if (VW == 4) {
+        pr_group_merge<4>(acc0);
+        pr_group_merge<4>(acc1);
+      } else if (VW == 8) {
+        pr_group_merge<8>(acc0);
+        pr_group_merge<8>(acc1);
+      } else {
+        pr_group_merge<32>(acc0);
+        pr_group_merge<32>(acc1);
+      }
+      if (gl == 0 && i < cnt) finish(v, pr_acc_value<MODE>(acc0), pr_acc_value<MODE>(acc1));
+    }
+  }
+  if (on0) pr_tally_flush<MODE>(a0.ls, p0, t0);
+  if (on1) pr_tally_flush<MODE>(a1.ls, p1, t1);
+}
+
 __device__ __forceinline__ uint32_t pr_pull_units(const BJob* J) {
   uint32_t t = 0;
   for (int k = 0; k < kPrBins; ++k) t += ceil_div(J->nb[k], pr_bin_unit(k));
@@ -261,6 +526,7 @@ __device__ void advance(const BJob* J, BSched* S, BCtl* ctl, unsigned phase) {
         s_total = pr_pull_units(J);
       } else {
         s_cont = pr_control_step(J->pr.ls, s_mode);
+        if (J->paired) s_cont |= pr_control_step(J->pr2.ls, s_mode);
         if (s_cont) {
           if (s_mode == PR_DELTA_RESIDUAL || s_mode == PR_DELTA_PUSH) {
             // PageRank-delta: the pull wrote the next round's contributions
@@ -351,6 +617,11 @@ __device__ void run_unit(const BJob* J, unsigned phase, uint32_t unit, int prmod
       else unit_chunks<2>(J, unit);
       break;
     case PH_PR_CONTRIB:
+      if (J->paired) {
+        if (prmode == PR_NORM32) unit_pr_contrib_pair<PR_NORM32>(J, unit);
+        else unit_pr_contrib_pair<PR_NORM64>(J, unit);
+        break;
+      }
       // PageRank-delta: its residual round only (the delta rounds take the previous
       // pull's contributions)
       if (prmode == PR_DELTA_RESIDUAL) unit_pr_contrib<PR_DELTA_RESIDUAL>(J, unit);
@@ -358,6 +629,11 @@ __device__ void run_unit(const BJob* J, unsigned phase, uint32_t unit, int prmod
       else unit_pr_contrib<PR_NORM64>(J, unit);
       break;
     case PH_PR_PULL:
+      if (J->paired) {
+        if (prmode == PR_NORM32) unit_pr_pull_pair<PR_NORM32>(J, unit);
+        else unit_pr_pull_pair<PR_NORM64>(J, unit);
+        break;
+      }
       if (prmode == PR_DELTA_RESIDUAL) unit_pr_pull<PR_DELTA_RESIDUAL>(J, unit);
       else if (prmode == PR_DELTA_PUSH) unit_pr_pull<PR_DELTA_PUSH>(J, unit);
       else if (prmode == PR_NORM32) unit_pr_pull<PR_NORM32>(J, unit);
@@ -519,6 +795,39 @@ static int batch_run(Ctx* const* ctxs, const int* job_ids, int count, cytom_run_
       hs[k].claim = pack_claim(PH_APPLY0, (unsigned)units);
     }
     hj[k] = b;
+  }
+  // PAGERANK jobs of one context and form run in pairs: one pass per round for both
+  // (CYTOM_BATCH_PAIR=0 keeps every job on passes of its own)
+  const char* pair_env = getenv("CYTOM_BATCH_PAIR");
+  if (!(pair_env && pair_env[0] == '0')) {
+    std::vector<char> used(count, 0);
+    for (int k1 = 0; k1 < count; ++k1) {
+      if (used[k1] || jobs[k1]->algo != CYTOM_ALGO_PAGERANK || (unsigned)(hs[k1].claim >> 56) == PH_DONE) continue;
+      for (int k2 = k1 + 1; k2 < count; ++k2) {
+        if (used[k2] || ctxs[k2] != ctxs[k1] || jobs[k2]->algo != CYTOM_ALGO_PAGERANK ||
+            (unsigned)(hs[k2].claim >> 56) == PH_DONE || jobs[k2]->params.kahan != jobs[k1]->params.kahan ||
+            hj[k2].pr.csc_src != hj[k1].pr.csc_src)
+          continue;
+        Ctx* c = ctxs[k1];
+        const size_t need = (size_t)c->n * 16;  // double2 per vertex covers both forms
+        if (c->pr_pair_bytes < need) {
+          cudaFree(c->pr_pair);
+          c->pr_pair = nullptr;
+          c->pr_pair_bytes = 0;
+          if (cy_malloc(&c->pr_pair, need) != cudaSuccess) {
+            cudaGetLastError();
+            break;  // no pair buffer: the jobs run on passes of their own
+          }
+          c->pr_pair_bytes = need;
+        }
+        hj[k1].paired = 1;
+        hj[k1].pr2 = hj[k2].pr;
+        hj[k1].cpair = c->pr_pair;
+        hs[k2].claim = pack_claim(PH_DONE, 0);
+        used[k1] = used[k2] = 1;
+        break;
+      }
+    }
   }
   unsigned left = 0;
   for (int k = 0; k < count; ++k)

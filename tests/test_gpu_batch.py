@@ -139,3 +139,47 @@ def test_batch_rejects_bad_calls(cg):
         p = cg.BFS(e, start_vertex=0)
         with pytest.raises(cg.CytomError):
             cg.run_batch([p, p])  # the same job twice
+
+
+@pytest.mark.parametrize("kahan", [True, False])
+def test_paired_pagerank_jobs_share_passes(cg, orc, kahan):
+    # PageRank jobs of one snapshot and form run as pairs in the batched executor (one
+    # pass per round for both): each job ends where it ends alone -- same rounds, values
+    # equal up to the order of the FP64 dangling-mass atomics, and within the tolerance of
+    # the FP64 oracle -- also when the two jobs differ in damping and tolerance, when an
+    # odd job is left over, fresh and after a further batch
+    import os
+    scale, vpt = 13, 1024
+    n = 1 << scale
+    s, t = orc.rmat(scale, 0, 16 * n, 41)
+    st = orc.Store(n, vpt)
+    st.insert(s, t)
+    st.compact()
+    specs = [(0.85, 1e-10), (0.85, 1e-10), (0.80, 1e-9)]
+    rtol = 1e-6 if kahan else 1e-12
+    with cg.Engine(n, vpt) as ea, cg.Engine(n, vpt) as eb:
+        ea.insert_edges(s.copy(), t.copy())
+        eb.insert_edges(s.copy(), t.copy())
+        pa = [cg.PageRank(ea, max_iterations=500, alpha=alpha, tolerance=tol, kahan=kahan) for alpha, tol in specs]
+        pb = [cg.PageRank(eb, max_iterations=500, alpha=alpha, tolerance=tol, kahan=kahan) for alpha, tol in specs]
+        for rnd in range(2):
+            sa = cg.run_batch(pa)  # paired: jobs 0 and 1; job 2 on its own passes
+            os.environ["CYTOM_BATCH_PAIR"] = "0"
+            try:
+                sb = cg.run_batch(pb)
+            finally:
+                del os.environ["CYTOM_BATCH_PAIR"]
+            for x, y, xs, ys in zip(pa, pb, sa, sb):
+                assert xs["iterations"] == ys["iterations"], (rnd, xs, ys)
+                gx = x.result64() if not kahan else x.result().astype(np.float64)
+                gy = y.result64() if not kahan else y.result().astype(np.float64)
+                assert np.allclose(gx, gy, rtol=rtol, atol=0), (rnd, np.abs(gx - gy).max())
+            ref, _ = st.pagerank_norm(tol=1e-15)
+            got = pa[0].result64() if not kahan else pa[0].result()
+            l1, mr = rel_errors(got, ref)
+            assert l1 <= L1_TOL and mr <= MAXREL_TOL, (rnd, l1, mr)
+            s2, t2 = orc.rmat(scale, 16 * n + rnd * 4096, 4096, 41)
+            for e in (ea, eb):
+                e.insert_edges(s2.copy(), t2.copy())
+            st.insert(s2, t2)
+            st.compact()

@@ -246,9 +246,9 @@ static int job_prepare(Ctx* c, Job* j) {
   if (rc) return rc;
   if (is_minprop(j->algo)) {
     rc = build_directory(c);
-    if (!rc) rc = build_tile_stages(c);
     if (!rc) rc = ensure_job_queue(c, j);
     if (!rc && autotune_due(c)) rc = minprop_autotune(c);
+    if (!rc && tiles_in_use(c, j->algo)) rc = build_tile_stages(c);
     if (rc) return rc;
     // the tuned sparse-round threshold of the job's class, read by its control step
     const uint32_t div = c->tune_div[(j->algo == CYTOM_ALGO_SSSP || j->algo == CYTOM_ALGO_SSWP) ? 1 : 0];

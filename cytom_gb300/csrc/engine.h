@@ -290,6 +290,7 @@ int compact(Ctx* c);
 int compute_compact_flags(Ctx* c, uint8_t* dflags);
 int build_directory(Ctx* c);
 int build_tile_stages(Ctx* c);
+bool tiles_in_use(Ctx* c, int algo);
 int ensure_app_capacity(Ctx* c, uint64_t need);
 
 // device-wide utilities

@@ -261,51 +261,61 @@ __global__ void __launch_bounds__(SG_T, MINB) gather_stream_kernel(const JobDesc
   }
   __syncthreads();
 
-  // stq[k]: the stage in slot (slot + k) % NST, k = 0 the one consumed next
+  // Thread 0 walks the block's stage sequence (skipping inactive stages) and keeps its
+  // queue: stq[k] = the stage in slot (slot + k) % NST, k = 0 the one consumed next. The
+  // stage of each slot is published in s_stage when it is issued; every thread reads it
+  // there after the block barrier that follows (NST >= 2 barriers later).
+  __shared__ unsigned long long s_stage[NST];
   uint64_t stq[NST];
-  {
+  uint64_t s_next = nst;
+  if (threadIdx.x == 0) {
     const uint64_t first = (uint64_t)blockIdx.x * SG_GROUP;
     uint64_t s0 = next_active(first < nst ? first : nst);
 #pragma unroll
     for (int k = 0; k < NST; ++k) {
       stq[k] = s0;
+      s_stage[k] = s0;
       if (s0 < nst) s0 = next_active(advance(s0));
     }
-    if (threadIdx.x == 0) {
 #pragma unroll
-      for (int k = 0; k < NST; ++k)
-        if (stq[k] < nst) issue(k, stq[k]);
-    }
+    for (int k = 0; k < NST; ++k)
+      if (stq[k] < nst) issue(k, stq[k]);
+    s_next = s0;
   }
-  uint64_t s_next = (stq[NST - 1] < nst) ? next_active(advance(stq[NST - 1])) : nst;
+  __syncthreads();
   uint32_t phases = 0;  // bit k: parity to wait for on slot k
   int slot = 0;
   unsigned long long scanned = 0;
   bool failed = false;
 
-  while (stq[0] < nst) {
+  for (;;) {
+    const uint64_t cur = s_stage[slot];
+    if (cur >= nst) break;
     // one block barrier per stage: a thread whose bounded wait gave up skips the stage
     // and the barrier after it ends the block
     const bool ok = mbar_wait(&bar[slot], (phases >> slot) & 1u);
     phases ^= 1u << slot;
     if (ok) {
       if (threadIdx.x == 0) {
-        const uint64_t rem = E - stq[0] * SE;
+        const uint64_t rem = E - cur * SE;
         scanned += rem < (uint64_t)SE ? rem : (uint64_t)SE;
       }
-      dense_stage<ALGO, false, false, EPT>(jd, sd, ebuf + slot * SE, wbuf + slot * SE, stq[0], p, adaptive);
+      dense_stage<ALGO, false, false, EPT>(jd, sd, ebuf + slot * SE, wbuf + slot * SE, cur, p, adaptive);
     }
     if (__syncthreads_or(!ok)) {  // every thread is done with this slot
       failed = true;
       phases ^= 1u << slot;  // the slot's copy is still owed: the cleanup waits on it
       break;
     }
-    // refill the slot with the next stage of this block
-    if (threadIdx.x == 0 && s_next < nst) issue(slot, s_next);
+    if (threadIdx.x == 0) {
+      // refill the slot with the next stage of this block
+      if (s_next < nst) issue(slot, s_next);
+      s_stage[slot] = s_next;
 #pragma unroll
-    for (int k = 0; k + 1 < NST; ++k) stq[k] = stq[k + 1];
-    stq[NST - 1] = s_next;
-    if (s_next < nst) s_next = next_active(advance(s_next));
+      for (int k = 0; k + 1 < NST; ++k) stq[k] = stq[k + 1];
+      stq[NST - 1] = s_next;
+      if (s_next < nst) s_next = next_active(advance(s_next));
+    }
     slot = (slot + 1 == NST) ? 0 : slot + 1;
   }
   if (failed) {
@@ -1093,6 +1103,10 @@ static int sg_variant(Ctx* c, int algo) {
   if (v == kTilesVariant && !tiles_usable(c)) v = 0;
   return v;
 }
+
+// Whether the runs of program `algo` use the column-ordered tiles kernel (its stage list
+// is built only then).
+bool tiles_in_use(Ctx* c, int algo) { return gather_mode() != 0 && sg_variant(c, algo) == kTilesVariant; }
 
 static GatherLaunch gather_launch(Ctx* c, int algo) {
   GatherLaunch g{};

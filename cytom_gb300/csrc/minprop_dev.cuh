@@ -57,8 +57,8 @@ __device__ __forceinline__ uint32_t mp_cand(uint32_t c, uint32_t w) {
   if (ALGO == 0) return c + 1;
   if (ALGO == 1) return c;
   if (ALGO == 2) {
-    const unsigned long long sum = (unsigned long long)c + w;
-    return sum >= kInf ? kInf : (uint32_t)sum;
+    const uint32_t sum = c + w;  // c < kInf; a carry out or kInf itself means unreachable
+    return (sum < c || sum == kInf) ? kInf : sum;
   }
   return max(c, ~w);
 }
@@ -302,9 +302,12 @@ __device__ __forceinline__ void dense_stage(const JobDesc* __restrict__ jd, cons
     ww[4 * k + 1] = wq.y;
     ww[4 * k + 2] = wq.z;
     ww[4 * k + 3] = wq.w;
+    if (cnt != SE) {
 #pragma unroll
-    for (int j = 0; j < 4; ++j) vmask |= ((i0 + j) < cnt) ? (1u << (4 * k + j)) : 0u;
+      for (int j = 0; j < 4; ++j) vmask |= ((i0 + j) < cnt) ? (1u << (4 * k + j)) : 0u;
+    }
   }
+  if (cnt == SE) vmask = (EPT == 32) ? 0xFFFFFFFFu : ((1u << EPT) - 1u);  // a full stage
   if (single_row) {
     const uint32_t xb = (tf >> lT) << lvpt;
 #pragma unroll

@@ -60,7 +60,7 @@ def parse(argv=None):
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-workloads", action="store_true", help="headline stream only")
-    ap.add_argument("--profile-steps", type=int, default=4,
+    ap.add_argument("--profile-steps", type=int, default=16,
                     help="batches at the end of the stream timed launch by launch for the roofline")
     ap.add_argument("--precision-scale", type=int, default=26)
     ap.add_argument("--profile-only", action="store_true",

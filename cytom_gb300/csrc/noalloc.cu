@@ -14,7 +14,8 @@
 // the GPU (other streams, other host threads) race; serialise them. Host code
 // cannot use the array's name as a device address: the first call on each device,
 // with that device current, looks the address up with cudaGetSymbolAddress and
-// caches it; make that first call before any stream capture.
+// caches it. Every call ends by synchronising its stream (it reads the kept-edge
+// count back), so no call can be captured in a CUDA graph.
 #include <cuda_runtime.h>
 #include <stdint.h>
 

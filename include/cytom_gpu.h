@@ -353,8 +353,8 @@ int cytom_write_results(cytom_ctx* ctx, int job_id, const char* path);
  * is CYTOM_ERR_RANGE and leaves the outputs undefined. Scratch lives in one static device
  * array of CYTOM_NOALLOC_SCRATCH_BYTES per GPU, held until exit and shared by every
  * call: calls that overlap on the GPU race. The first call on a device looks the
- * array up (cudaGetSymbolAddress) with that device current; make it before any
- * stream capture. The call synchronises `stream` before it returns. */
+ * array up (cudaGetSymbolAddress) with that device current. Every call synchronises
+ * `stream` before it returns, so no call can be captured in a CUDA graph. */
 #define CYTOM_NOALLOC_MAX_EDGES (1u << 18)
 #define CYTOM_NOALLOC_SCRATCH_BYTES ((size_t)9 << 20)
 int cytom_tile_batch_noalloc(const uint32_t* src, const uint32_t* tgt, const uint32_t* w,

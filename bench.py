@@ -221,6 +221,15 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+
+def dense_kernel_names(tune) -> str:
+    """The dense gather kernels the tuned jobs run (gather_stream_kernel or gather_tiles_kernel)."""
+    try:
+        kinds = sorted({tune["shapes"][k]["kernel"] for k in tune["chosen"].values()})
+    except (TypeError, KeyError, IndexError):
+        kinds = ["stream"]
+    return " + ".join(f"gather_{k}_kernel" for k in kinds)
+
 def main(argv=None):
     args = parse(argv)
     rank, world, local = dist_env()
@@ -478,7 +487,8 @@ def main(argv=None):
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": (achieved / hbm_peak) if achieved else None, "traffic": traffic,
-                         "kernel": "executor gather, dense + sparse rounds (gather_tiles_kernel / gather_sparse_*)",
+                         "kernel": "executor gather, dense + sparse rounds (" + dense_kernel_names(tune)
+                                   + " / gather_sparse_kernel + gather_sparse_chunks)",
                          "launches": g_launches,
                          "avg_launch_us": (g_ms * 1e3 / g_launches) if g_launches else None,
                          "bytes_per_launch": (g_bytes / g_launches) if g_launches else None,

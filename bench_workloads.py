@@ -210,7 +210,9 @@ def batching(args) -> dict:
     runs each job by itself (cytom_run: one CUDA-graph launch per BFS/CC/SSSP run and per
     PageRank run); the batched launch pairs the two PageRank jobs of a snapshot (one pass
     per round for both). Inserts and compactions are untimed and identical in both arms; a job
-    round is timed from the first call to the readback of the last job's statistics.
+    round is timed from the first call to the readback of the last job's statistics. One-time
+    setup (autotuning, loop capture, the first PageRank CSC) runs before the timed rounds
+    in both arms: every job once by itself, then reset to start from scratch.
     BFS/CC/SSSP results of the two arms are compared bit for bit after every round."""
     import torch
     import cytom_gb300 as cg
@@ -242,6 +244,13 @@ def batching(args) -> dict:
                       cg.SSSP(e, start_vertex=0, max_iterations=100), cg.SSSP(e, start_vertex=1, max_iterations=100),
                       cg.PageRank(e, max_iterations=100, tolerance=1e-8, kahan=True),
                       cg.PageRank(e, max_iterations=100, tolerance=1e-8, kahan=True)]
+        # one-time setup outside the timed rounds, the same for both arms: every job runs
+        # once by itself (autotuning, captured loops, the first PageRank CSC), then is reset
+        # so that job round 0 computes from scratch
+        for p in progs:
+            p.execute_algorithm()
+        for p in progs:
+            p.init_algorithm()
         return engs, progs
 
     def insert_round(engs, r):

@@ -226,6 +226,13 @@ struct Ctx {
   uint32_t* pr_deg_mult = nullptr;
   uint64_t pr_deg_mult_version = ~0ULL;
   void* pr_csc = nullptr;
+  // The kept edges of the last compaction as renumbered (target, source) keys, saved
+  // while the PageRank CSC was current, so that its next build merges them in instead of
+  // re-sorting every edge (pr_delta_version: the store version they lead to).
+  uint64_t* pr_delta_keys = nullptr;
+  uint64_t pr_delta_cap = 0;
+  uint64_t pr_delta_count = 0;
+  uint64_t pr_delta_version = ~0ULL;
   void* pr_wgraph = nullptr;  // weighted PageRank: CSC + CSR with weights
   void* pr_pair = nullptr;    // batched executor: interleaved contributions of paired PageRank jobs
   size_t pr_pair_bytes = 0;
@@ -305,6 +312,7 @@ int job_init_state(Ctx* c, Job* j);
 int job_seed(Ctx* c, Job* j, const uint32_t* src, const uint32_t* tgt, const uint32_t* w,
              uint64_t count);
 int job_seed_keys(Ctx* c, Job* j, const uint64_t* K, const uint32_t* W, uint64_t count);
+int pagerank_note_kept(Ctx* c, const uint32_t* nloc, const uint32_t* ntile, uint64_t kept);
 // The context's stream waits for runs launched asynchronously (no host wait); every
 // operation that touches the installed snapshot or job state comes after it.
 void join_runs(Ctx* c);

@@ -72,6 +72,7 @@ struct BJob {
   PrArgs pr2;                      // paired PAGERANK job (paired = 1): its arguments
   void* cpair;                     // paired jobs: interleaved contributions {job, pr2 job}
   unsigned long long nb[kPrBins];  // PageRank target bins
+  LoopState* ls;                   // the job's loop state (statistics read back after the launch)
   int algo;
   int adaptive;
   int paired;
@@ -172,13 +173,13 @@ __device__ void unit_pr_contrib(const BJob* J, uint32_t unit) {
   const unsigned p = ls_iter(a.ls) & 1u;
   const uint64_t lo = (uint64_t)unit * BU_PR_VERTS;
   const uint64_t hi = std::min<uint64_t>(lo + BU_PR_VERTS, a.n);
-  const double dangling = pr_contrib_range<MODE, true>(a, p, lo, hi, threadIdx.x, BT);
+  const pr_ff_t<MODE> dangling = pr_contrib_range<MODE, true>(a, p, lo, hi, threadIdx.x, BT);
   pr_dangling_flush<MODE>(a.ls, p, dangling);
 }
 
 template <int MODE, int VW>
 __device__ __forceinline__ void pull_groups(const PrArgs& a, const pr_val_t<MODE>* cr, uint64_t off, uint64_t cnt,
-                                            uint64_t first, unsigned p, double dang, PrTally& t) {
+                                            uint64_t first, unsigned p, pr_ff_t<MODE> dang, PrTally& t) {
   constexpr uint32_t GPB = BT / VW;  // groups per block
   const unsigned gl = threadIdx.x & (VW - 1);
   const uint32_t g = threadIdx.x / VW;
@@ -191,7 +192,7 @@ __device__ __forceinline__ void pull_groups(const PrArgs& a, const pr_val_t<MODE
       lo = a.csc_ptr[v];
       hi = a.csc_ptr[v + 1];
     }
-    const double sum = pr_sum_group<MODE, true, VW>(a, cr, lo, hi, gl);
+    const pr_ff_t<MODE> sum = pr_sum_group<MODE, true, VW>(a, cr, lo, hi, gl);
     if (gl == 0 && i < cnt) pr_finish<MODE, true>(a, v, sum, p, dang, t);
   }
 }
@@ -201,7 +202,7 @@ __device__ void unit_pr_pull(const BJob* J, uint32_t unit) {
   const PrArgs& a = J->pr;
   LoopState* ls = a.ls;
   const unsigned p = ls_iter(ls) & 1u;
-  const double dang = pr_dang_arg<MODE, true>(ls, p, a.n);
+  const pr_ff_t<MODE> dang = pr_dang_arg<MODE, true>(a, ls, p);
   // the bin this unit belongs to
   int k = 0;
   uint64_t off = 0;
@@ -224,7 +225,7 @@ __device__ void unit_pr_pull(const BJob* J, uint32_t unit) {
         const uint64_t i = first + (uint64_t)r * BT + threadIdx.x;
         if (i < cnt) {
           const uint32_t v = a.bins[off + i];
-          const double sum = pr_sum_thread<MODE, true>(a, cr, v);
+          const pr_ff_t<MODE> sum = pr_sum_thread<MODE, true>(a, cr, v);
           pr_finish<MODE, true>(a, v, sum, p, dang, t);
         }
       }
@@ -234,7 +235,7 @@ __device__ void unit_pr_pull(const BJob* J, uint32_t unit) {
     case 32: pull_groups<MODE, 32>(a, cr, off, cnt, first, p, dang, t); break;
     default: {
       const uint32_t v = a.bins[off + first];
-      const double sum = pr_sum_block<MODE, true>(a, cr, v);
+      const pr_ff_t<MODE> sum = pr_sum_block<MODE, true>(a, cr, v);
       if (threadIdx.x == 0) pr_finish<MODE, true>(a, v, sum, p, dang, t);
     }
   }
@@ -263,41 +264,65 @@ using pr_pair_t = typename PrPairT<MODE>::T;
 
 __device__ __forceinline__ bool pr_on(const LoopState* ls) { return __ldcg(&ls->cont) != 0u; }
 
-// One job's contribution of source u and its dangling share, as pr_contrib_range computes
-// them (NORM32: FP32 quotient of the rank's high word; NORM64: FP64 quotient).
-template <int MODE>
-__device__ __forceinline__ pr_val_t<MODE> pr_pair_contrib(const PrArgs& a, unsigned p, uint64_t u, uint32_t d,
-                                                          double& dangling) {
-  if constexpr (MODE == PR_NORM32) {
-    const float* r = (p == 0) ? a.rank : a.comp;
-    const float* rl = (p == 0) ? a.lo0 : a.lo1;
-    const float rh = __ldcg(r + u);
-    if (!d) dangling += (double)rh + (double)__ldcg(rl + u);
-    return d ? rh / (float)d : 0.f;
-  } else {
-    const double* r = (p == 0) ? a.r64 : a.r64n;
-    const double rv = __ldcg(r + u);
-    if (!d) dangling += rv;
-    return d ? rv / (double)d : 0.0;
-  }
-}
-
+// Both jobs' contributions of sources [unit * BU_PR_VERTS, ...), as pr_contrib_range
+// computes them (NORM32: FP32 quotient of the rank's high word, the low word entering the
+// dangling mass; NORM64: FP64 quotient). A thread loads the degrees and ranks of four
+// sources before it uses any (one round trip per four sources); the dangling sums add up
+// in source order as in pr_contrib_range.
 template <int MODE>
 __device__ void unit_pr_contrib_pair(const BJob* J, uint32_t unit) {
+  using V = pr_val_t<MODE>;
+  constexpr bool k32 = MODE == PR_NORM32;
   const PrArgs& a0 = J->pr;
   const PrArgs& a1 = J->pr2;
   const bool on0 = pr_on(a0.ls), on1 = pr_on(a1.ls);
   const unsigned p0 = ls_iter(a0.ls) & 1u, p1 = ls_iter(a1.ls) & 1u;
+  const V* r0 = k32 ? (const V*)((p0 == 0) ? a0.rank : a0.comp) : (const V*)((p0 == 0) ? a0.r64 : a0.r64n);
+  const V* r1 = k32 ? (const V*)((p1 == 0) ? a1.rank : a1.comp) : (const V*)((p1 == 0) ? a1.r64 : a1.r64n);
+  const float* l0 = (p0 == 0) ? a0.lo0 : a0.lo1;
+  const float* l1 = (p1 == 0) ? a1.lo0 : a1.lo1;
   pr_pair_t<MODE>* cw = reinterpret_cast<pr_pair_t<MODE>*>(J->cpair);
   const uint64_t lo = (uint64_t)unit * BU_PR_VERTS;
   const uint64_t hi = std::min<uint64_t>(lo + BU_PR_VERTS, a0.n);
-  double d0 = 0.0, d1 = 0.0;
-  for (uint64_t u = lo + threadIdx.x; u < hi; u += BT) {
-    const uint32_t d = a0.deg[u];  // the snapshot's out-degrees, shared by both jobs
-    pr_pair_t<MODE> c;
-    c.x = on0 ? pr_pair_contrib<MODE>(a0, p0, u, d, d0) : (pr_val_t<MODE>)0;
-    c.y = on1 ? pr_pair_contrib<MODE>(a1, p1, u, d, d1) : (pr_val_t<MODE>)0;
-    cw[u] = c;
+  pr_ff_t<MODE> d0{}, d1{};
+  for (uint64_t ub = lo + threadIdx.x; ub < hi; ub += 4 * BT) {
+    uint32_t dg[4];
+    V h0[4], h1[4];
+    float w0[4], w1[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const uint64_t u = ub + (uint64_t)k * BT;
+      const bool in = u < hi;
+      dg[k] = in ? a0.deg[u] : 1u;  // the snapshot's out-degrees, shared by both jobs
+      h0[k] = (in && on0) ? __ldcg(r0 + u) : (V)0;
+      h1[k] = (in && on1) ? __ldcg(r1 + u) : (V)0;
+      w0[k] = (k32 && in && on0) ? __ldcg(l0 + u) : 0.f;
+      w1[k] = (k32 && in && on1) ? __ldcg(l1 + u) : 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const uint64_t u = ub + (uint64_t)k * BT;
+      if (u < hi) {
+        pr_pair_t<MODE> c;
+        c.x = (V)0;
+        c.y = (V)0;
+        if (on0) {
+          if (!dg[k]) {
+            if constexpr (k32) d0 = ff_add(d0, FF{(float)h0[k], w0[k]});
+            else d0 += h0[k];
+          }
+          c.x = dg[k] ? h0[k] / (V)dg[k] : (V)0;
+        }
+        if (on1) {
+          if (!dg[k]) {
+            if constexpr (k32) d1 = ff_add(d1, FF{(float)h1[k], w1[k]});
+            else d1 += h1[k];
+          }
+          c.y = dg[k] ? h1[k] / (V)dg[k] : (V)0;
+        }
+        cw[u] = c;
+      }
+    }
   }
   pr_dangling_flush<MODE>(a0.ls, p0, d0);
   pr_dangling_flush<MODE>(a1.ls, p1, d1);
@@ -344,8 +369,8 @@ template <int MODE>
 using pr_acc_t = typename std::conditional<pr_is64<MODE>(), Acc64, Acc32>::type;
 
 template <int MODE>
-__device__ __forceinline__ double pr_acc_value(const Acc32& a) {
-  return (double)a.s + (double)a.e;
+__device__ __forceinline__ pr_ff_t<MODE> pr_acc_value(const Acc32& a) {
+  return pr_acc32_out<MODE>(a.s, a.e);
 }
 template <int MODE>
 __device__ __forceinline__ double pr_acc_value(const Acc64& a) {
@@ -370,8 +395,8 @@ __device__ __forceinline__ void pr_group_merge(Acc64& acc) {
 
 // Whole-block sum (pr_sum_block's reduction) of both jobs; thread 0 holds the sums.
 template <int MODE>
-__device__ __forceinline__ void pr_block_pair(const PrArgs& a, const pr_pair_t<MODE>* cp, uint32_t v, double& s0,
-                                              double& s1) {
+__device__ __forceinline__ void pr_block_pair(const PrArgs& a, const pr_pair_t<MODE>* cp, uint32_t v,
+                                              pr_ff_t<MODE>& s0, pr_ff_t<MODE>& s1) {
   __shared__ float s_s[2][BT / 32], s_e[2][BT / 32];
   __shared__ double s_d[2][BT / 32];
   const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -412,21 +437,141 @@ __device__ __forceinline__ void pr_block_pair(const PrArgs& a, const pr_pair_t<M
         t0.merge(s_s[0][k], s_e[0][k]);
         t1.merge(s_s[1][k], s_e[1][k]);
       }
-      s0 = (double)t0.s + (double)t0.e;
-      s1 = (double)t1.s + (double)t1.e;
+      s0 = pr_acc32_out<MODE>(t0.s, t0.e);
+      s1 = pr_acc32_out<MODE>(t1.s, t1.e);
     }
   }
   __syncthreads();
+}
+
+// Both jobs' updates of target v from their sums and preloaded ranks (pr_finish).
+template <int MODE>
+struct PairFinish {
+  const PrArgs& a0;
+  const PrArgs& a1;
+  bool on0, on1;
+  unsigned p0, p1;
+  pr_ff_t<MODE> dang0, dang1;
+  PrTally t0, t1;
+  __device__ __forceinline__ void old(uint32_t v, PrOld& o0, PrOld& o1) const {
+    if (on0) o0 = pr_load_old<MODE, true>(a0, v, p0);
+    if (on1) o1 = pr_load_old<MODE, true>(a1, v, p1);
+  }
+  __device__ __forceinline__ void operator()(uint32_t v, pr_ff_t<MODE> s0, pr_ff_t<MODE> s1, PrOld o0, PrOld o1) {
+    if (on0) pr_apply_norm<MODE>(a0, v, s0, p0, dang0, o0, t0);
+    if (on1) pr_apply_norm<MODE>(a1, v, s1, p1, dang1, o1, t1);
+  }
+};
+
+// Targets of in-degree <= 4, one thread each, four per thread: the thread loads the
+// four targets' ids and offsets up front, then handles two targets at a time with their
+// in-edge ids, then their contributions and ranks, in flight together. Each target's
+// edges add up in edge order, as pr_sum_thread adds them.
+template <int MODE>
+__device__ __forceinline__ void pair_small(const PrArgs& a0, const pr_pair_t<MODE>* cp, uint64_t off, uint64_t cnt,
+                                           uint64_t first, PairFinish<MODE>& fin) {
+  using Acc = pr_acc_t<MODE>;
+  uint32_t v[4], lo[4], hi[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const uint64_t i = first + (uint64_t)r * BT + threadIdx.x;
+    v[r] = i < cnt ? a0.bins[off + i] : 0xFFFFFFFFu;
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    lo[r] = v[r] != 0xFFFFFFFFu ? a0.csc_ptr[v[r]] : 0u;
+    hi[r] = v[r] != 0xFFFFFFFFu ? a0.csc_ptr[v[r] + 1] : 0u;
+  }
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    uint32_t id[2][4];
+#pragma unroll
+    for (int t = 0; t < 2; ++t)
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const uint32_t e = lo[2 * h + t] + (uint32_t)k;
+        id[t][k] = e < hi[2 * h + t] ? a0.csc_src[e] : 0u;
+      }
+    pr_pair_t<MODE> c[2][4];
+    PrOld o0[2] = {}, o1[2] = {};
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (lo[2 * h + t] + (uint32_t)k < hi[2 * h + t]) {
+          c[t][k] = __ldcg(cp + id[t][k]);
+        } else {
+          c[t][k].x = 0;
+          c[t][k].y = 0;
+        }
+      }
+      if (v[2 * h + t] != 0xFFFFFFFFu) fin.old(v[2 * h + t], o0[t], o1[t]);
+    }
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      if (v[2 * h + t] == 0xFFFFFFFFu) continue;
+      Acc acc0, acc1;
+      acc0.init();
+      acc1.init();
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (lo[2 * h + t] + (uint32_t)k < hi[2 * h + t]) {
+          acc0.add(c[t][k].x);
+          acc1.add(c[t][k].y);
+        }
+      fin(v[2 * h + t], pr_acc_value<MODE>(acc0), pr_acc_value<MODE>(acc1), o0[t], o1[t]);
+    }
+  }
+}
+
+// Targets of one group bin, VW lanes each, four per group (pull_groups): the group loads
+// its four targets' ids and offsets up front; the first lane loads each target's ranks
+// before the target's sum. Lane order and merge tree as pr_sum_group.
+template <int MODE, int VW>
+__device__ __forceinline__ void pair_groups(const PrArgs& a0, const pr_pair_t<MODE>* cp, uint64_t off,
+                                            uint64_t cnt, uint64_t first, PairFinish<MODE>& fin) {
+  constexpr uint32_t GPB = BT / VW;
+  const unsigned gl = threadIdx.x & (VW - 1);
+  const uint32_t g = threadIdx.x / VW;
+  uint32_t v[4], lo[4], hi[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const uint64_t i = first + (uint64_t)r * GPB + g;
+    v[r] = i < cnt ? a0.bins[off + i] : 0xFFFFFFFFu;
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    lo[r] = v[r] != 0xFFFFFFFFu ? a0.csc_ptr[v[r]] : 0u;
+    hi[r] = v[r] != 0xFFFFFFFFu ? a0.csc_ptr[v[r] + 1] : 0u;
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    PrOld o0 = {}, o1 = {};
+    if (gl == 0 && v[r] != 0xFFFFFFFFu) fin.old(v[r], o0, o1);
+    pr_acc_t<MODE> acc0, acc1;
+    acc0.init();
+    acc1.init();
+    pr_lane_sum_pair<MODE, 4>(a0, cp, lo[r] + gl, hi[r], VW, acc0, acc1);
+    pr_group_merge<VW>(acc0);
+    pr_group_merge<VW>(acc1);
+    if (gl == 0 && v[r] != 0xFFFFFFFFu)
+      fin(v[r], pr_acc_value<MODE>(acc0), pr_acc_value<MODE>(acc1), o0, o1);
+  }
 }
 
 template <int MODE>
 __device__ void unit_pr_pull_pair(const BJob* J, uint32_t unit) {
   const PrArgs& a0 = J->pr;
   const PrArgs& a1 = J->pr2;
-  const bool on0 = pr_on(a0.ls), on1 = pr_on(a1.ls);
-  const unsigned p0 = ls_iter(a0.ls) & 1u, p1 = ls_iter(a1.ls) & 1u;
-  const double dang0 = pr_dang_arg<MODE, true>(a0.ls, p0, a0.n);
-  const double dang1 = pr_dang_arg<MODE, true>(a1.ls, p1, a1.n);
+  PairFinish<MODE> fin{a0, a1};
+  fin.on0 = pr_on(a0.ls);
+  fin.on1 = pr_on(a1.ls);
+  fin.p0 = ls_iter(a0.ls) & 1u;
+  fin.p1 = ls_iter(a1.ls) & 1u;
+  fin.dang0 = pr_dang_arg<MODE, true>(a0, a0.ls, fin.p0);
+  fin.dang1 = pr_dang_arg<MODE, true>(a1, a1.ls, fin.p1);
+  fin.t0.init();
+  fin.t1.init();
   int k = 0;
   uint64_t off = 0;
   uint32_t u = unit;
@@ -439,66 +584,22 @@ __device__ void unit_pr_pull_pair(const BJob* J, uint32_t unit) {
   const uint64_t cnt = J->nb[k];
   const uint64_t first = (uint64_t)u * pr_bin_unit(k);
   const pr_pair_t<MODE>* cp = reinterpret_cast<const pr_pair_t<MODE>*>(J->cpair);
-  PrTally t0, t1;
-  t0.init();
-  t1.init();
-  auto finish = [&](uint32_t v, double s0, double s1) {
-    if (on0) pr_finish<MODE, true>(a0, v, s0, p0, dang0, t0);
-    if (on1) pr_finish<MODE, true>(a1, v, s1, p1, dang1, t1);
-  };
-  const int vw = pr_bin_vw(k);
-  if (vw == 1) {
-#pragma unroll 1
-    for (uint32_t r = 0; r < 4; ++r) {
-      const uint64_t i = first + (uint64_t)r * BT + threadIdx.x;
-      if (i < cnt) {
-        const uint32_t v = a0.bins[off + i];
-        pr_acc_t<MODE> acc0, acc1;
-        acc0.init();
-        acc1.init();
-        pr_lane_sum_pair<MODE, 4>(a0, cp, a0.csc_ptr[v], a0.csc_ptr[v + 1], 1u, acc0, acc1);
-        finish(v, pr_acc_value<MODE>(acc0), pr_acc_value<MODE>(acc1));
-      }
-    }
-  } else if (vw == 0) {
-    const uint32_t v = a0.bins[off + first];
-    double s0 = 0.0, s1 = 0.0;
-    pr_block_pair<MODE>(a0, cp, v, s0, s1);
-    if (threadIdx.x == 0) finish(v, s0, s1);
-  } else {
-    // groups of VW lanes, four targets per group (pull_groups)
-    const unsigned VW = (unsigned)vw;
-    const uint32_t GPB = BT / VW;
-    const unsigned gl = threadIdx.x & (VW - 1);
-    const uint32_t g = threadIdx.x / VW;
-#pragma unroll 1
-    for (uint32_t r = 0; r < 4; ++r) {
-      const uint64_t i = first + (uint64_t)r * GPB + g;
-      uint32_t v = 0, lo = 0, hi = 0;
-      if (i < cnt) {
-        v = a0.bins[off + i];
-        lo = a0.csc_ptr[v];
-        hi = a0.csc_ptr[v + 1];
-      }
-      pr_acc_t<MODE> acc0, acc1;
-      acc0.init();
-      acc1.init();
-      pr_lane_sum_pair<MODE, 4>(a0, cp, lo + gl, hi, VW, acc0, acc1);
-      if (VW == 4) {
-        pr_group_merge<4>(acc0);
-        pr_group_merge<4>(acc1);
-      } else if (VW == 8) {
-        pr_group_merge<8>(acc0);
-        pr_group_merge<8>(acc1);
-      } else {
-        pr_group_merge<32>(acc0);
-        pr_group_merge<32>(acc1);
-      }
-      if (gl == 0 && i < cnt) finish(v, pr_acc_value<MODE>(acc0), pr_acc_value<MODE>(acc1));
+  switch (pr_bin_vw(k)) {
+    case 1: pair_small<MODE>(a0, cp, off, cnt, first, fin); break;
+    case 4: pair_groups<MODE, 4>(a0, cp, off, cnt, first, fin); break;
+    case 8: pair_groups<MODE, 8>(a0, cp, off, cnt, first, fin); break;
+    case 32: pair_groups<MODE, 32>(a0, cp, off, cnt, first, fin); break;
+    default: {
+      const uint32_t v = a0.bins[off + first];
+      PrOld o0 = {}, o1 = {};
+      if (threadIdx.x == 0) fin.old(v, o0, o1);
+      pr_ff_t<MODE> s0{}, s1{};
+      pr_block_pair<MODE>(a0, cp, v, s0, s1);
+      if (threadIdx.x == 0) fin(v, s0, s1, o0, o1);
     }
   }
-  if (on0) pr_tally_flush<MODE>(a0.ls, p0, t0);
-  if (on1) pr_tally_flush<MODE>(a1.ls, p1, t1);
+  if (fin.on0) pr_tally_flush<MODE>(a0.ls, fin.p0, fin.t0);
+  if (fin.on1) pr_tally_flush<MODE>(a1.ls, fin.p1, fin.t1);
 }
 
 __device__ __forceinline__ uint32_t pr_pull_units(const BJob* J) {
@@ -656,42 +757,64 @@ __global__ void __launch_bounds__(BT, 4) batch_kernel(const BJob* __restrict__ j
   unsigned idle = 0;
   unsigned long long done_units = 0;
   for (;;) {
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < 32) {
+      // warp 0 reads 32 claim words at a time (one L2 round trip), in cyclic order from
+      // the job this block worked on last, and claims a unit of the first open one
+      const unsigned lane = threadIdx.x;
       int found = -1;
       unsigned unit = 0, total = 0, phase = 0;
-      for (int k = 0; k < njobs && found < 0; ++k) {
+      for (int base = 0; base < njobs && found < 0; base += 32) {
+        const int k = base + (int)lane;
         int jj = cursor + k;
         if (jj >= njobs) jj -= njobs;
-        const unsigned long long cw = *(volatile unsigned long long*)&sched[jj].claim;
-        if ((unsigned)cw >= ((unsigned)(cw >> 32) & 0xFFFFFFu)) continue;
-        const unsigned long long old = atomicAdd(&sched[jj].claim, 1ULL);
-        const unsigned tot = (unsigned)(old >> 32) & 0xFFFFFFu;
-        if ((unsigned)old < tot) {
-          found = jj;
-          unit = (unsigned)old;
-          total = tot;
-          phase = (unsigned)(old >> 56);
+        bool open = false;
+        if (k < njobs) {
+          const unsigned long long cw = *(volatile unsigned long long*)&sched[jj].claim;
+          open = (unsigned)cw < ((unsigned)(cw >> 32) & 0xFFFFFFu);
+        }
+        unsigned m = __ballot_sync(0xFFFFFFFFu, open);
+        while (m) {
+          const int l = __ffs(m) - 1;
+          m &= m - 1;
+          int got = 0;
+          unsigned long long old = 0;
+          if ((int)lane == l) {
+            old = atomicAdd(&sched[jj].claim, 1ULL);
+            got = (unsigned)old < ((unsigned)(old >> 32) & 0xFFFFFFu) ? 1 : 0;
+            if (got) __threadfence();  // the phase's state was published before the claim word
+          }
+          got = __shfl_sync(0xFFFFFFFFu, got, l);
+          if (got) {
+            old = __shfl_sync(0xFFFFFFFFu, old, l);
+            found = __shfl_sync(0xFFFFFFFFu, jj, l);
+            unit = (unsigned)old;
+            total = (unsigned)(old >> 32) & 0xFFFFFFu;
+            phase = (unsigned)(old >> 56);
+            break;
+          }
         }
       }
-      int state = 0;
-      if (found >= 0) {
-        __threadfence();  // the phase's state was published before the claim word
-        s_mode = *(volatile int*)&sched[found].prmode;
-        idle = 0;
-      } else if (*(volatile unsigned*)&ctl->jobs_left == 0 || *(volatile unsigned*)&ctl->err != 0) {
-        state = 2;
-      } else if (++idle > ctl->idle_limit) {
-        atomicExch(&ctl->err, 1u);
-        state = 2;
-      } else {
-        state = 1;
-        __nanosleep(200);
+      if (lane == 0) {
+        int state = 0;
+        if (found >= 0) {
+          __threadfence();
+          s_mode = *(volatile int*)&sched[found].prmode;
+          idle = 0;
+        } else if (*(volatile unsigned*)&ctl->jobs_left == 0 || *(volatile unsigned*)&ctl->err != 0) {
+          state = 2;
+        } else if (++idle > ctl->idle_limit) {
+          atomicExch(&ctl->err, 1u);
+          state = 2;
+        } else {
+          state = 1;
+          __nanosleep(idle < 16 ? 100u : 800u);  // back off once the block has polled a while
+        }
+        s_job = found;
+        s_unit = unit;
+        s_total = total;
+        s_phase = phase;
+        s_state = state;
       }
-      s_job = found;
-      s_unit = unit;
-      s_total = total;
-      s_phase = phase;
-      s_state = state;
     }
     __syncthreads();
     const int state = s_state;
@@ -720,6 +843,15 @@ __global__ void __launch_bounds__(BT, 4) batch_kernel(const BJob* __restrict__ j
   if (threadIdx.x == 0 && done_units) atomicAdd(&ctl->units, done_units);
 }
 
+// Copies every job's loop state into one array, read back with a single copy.
+__global__ void batch_stats_kernel(const BJob* __restrict__ jobs, int count, LoopState* __restrict__ out) {
+  const int k = blockIdx.x;
+  if (k >= count) return;
+  const unsigned* src = reinterpret_cast<const unsigned*>(jobs[k].ls);
+  unsigned* dst = reinterpret_cast<unsigned*>(out + k);
+  for (unsigned i = threadIdx.x; i < sizeof(LoopState) / 4; i += blockDim.x) dst[i] = __ldcg(src + i);
+}
+
 // ---- host ---------------------------------------------------------------------
 
 static bool is_pr(int algo) { return algo == CYTOM_ALGO_PR_DELTA || algo == CYTOM_ALGO_PAGERANK; }
@@ -729,6 +861,8 @@ struct BatchBuffers {
   BJob* jobs = nullptr;
   BSched* sched = nullptr;
   BCtl* ctl = nullptr;
+  LoopState* d_ls = nullptr;  // the jobs' loop states after the launch
+  LoopState* h_ls = nullptr;  // pinned copy
   int cap = 0;
   cudaEvent_t a = nullptr, b = nullptr;
 };
@@ -771,6 +905,7 @@ static int batch_run(Ctx* const* ctxs, const int* job_ids, int count, cytom_run_
     BJob b{};
     b.jd = j->d;
     b.sd = c->dsd;
+    b.ls = j->ls;
     b.algo = j->algo;
     b.adaptive = c->cfg.enable_adaptive_scheduling;
     memset(&hs[k], 0, sizeof(BSched));
@@ -848,11 +983,17 @@ static int batch_run(Ctx* const* ctxs, const int* job_ids, int count, cytom_run_
   if (bb->cap < count) {
     cudaFree(bb->jobs);
     cudaFree(bb->sched);
+    cudaFree(bb->d_ls);
+    cudaFreeHost(bb->h_ls);
     bb->jobs = nullptr;
     bb->sched = nullptr;
+    bb->d_ls = nullptr;
+    bb->h_ls = nullptr;
     bb->cap = 0;
     if (cy_malloc(&bb->jobs, sizeof(BJob) * count) != cudaSuccess ||
-        cy_malloc(&bb->sched, sizeof(BSched) * count) != cudaSuccess) {
+        cy_malloc(&bb->sched, sizeof(BSched) * count) != cudaSuccess ||
+        cy_malloc(&bb->d_ls, sizeof(LoopState) * count) != cudaSuccess ||
+        cy_malloc_host(&bb->h_ls, sizeof(LoopState) * count) != cudaSuccess) {
       cudaGetLastError();
       return set_err(c0, CYTOM_ERR_OOM, "batch tables");
     }
@@ -882,8 +1023,14 @@ static int batch_run(Ctx* const* ctxs, const int* job_ids, int count, cytom_run_
     c0->launches++;
   }
   cudaEventRecord(bb->b, st);
+  if (stats) {
+    batch_stats_kernel<<<count, 64, 0, st>>>(bb->jobs, count, bb->d_ls);
+    c0->launches++;
+  }
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpyAsync(&hctl, bb->ctl, sizeof(BCtl), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && stats)
+    e = cudaMemcpyAsync(bb->h_ls, bb->d_ls, sizeof(LoopState) * count, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_err(c0, e, "batch run");
   float ms = 0.f;
@@ -896,13 +1043,10 @@ static int batch_run(Ctx* const* ctxs, const int* job_ids, int count, cytom_run_
     return set_err(c0, CYTOM_ERR_RANGE, "batched executor: a phase exceeds the unit limit");
   }
   for (int k = 0; k < count; ++k) {
-    Ctx* c = ctxs[k];
     Job* j = jobs[k];
     j->last_run_graph = false;
     if (!stats) continue;
-    LoopState ls;
-    e = cudaMemcpy(&ls, j->ls, sizeof(LoopState), cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return cuda_err(c, e, "batch stats");
+    const LoopState& ls = bb->h_ls[k];
     cytom_run_stats& s = stats[k];
     memset(&s, 0, sizeof(s));
     s.iterations = ls.iter;
@@ -922,6 +1066,8 @@ void batch_free(Ctx* c) {
   if (bb->jobs) cudaFree(bb->jobs);
   if (bb->sched) cudaFree(bb->sched);
   if (bb->ctl) cudaFree(bb->ctl);
+  if (bb->d_ls) cudaFree(bb->d_ls);
+  if (bb->h_ls) cudaFreeHost(bb->h_ls);
   if (bb->a) cudaEventDestroy(bb->a);
   if (bb->b) cudaEventDestroy(bb->b);
   delete bb;

@@ -55,6 +55,8 @@ struct PrBinLaunch {
 // CSC of the compacted store, per job (PageRank family).
 struct Csc {
   uint32_t* src = nullptr;       // E: global source of each in-edge, grouped by target
+  uint32_t* src_alt = nullptr;   // the merge's output (merge_csc), swapped with src
+  uint64_t cap_alt = 0;
   uint32_t* ptr = nullptr;       // n+1
   uint32_t* deg_out = nullptr;   // n: distinct out-degree (stored edges)
   uint32_t* bins = nullptr;      // n: targets, small | medium | large
@@ -175,6 +177,98 @@ __global__ void csc_cnt_bins_kernel(const uint32_t* seg_lo, const uint32_t* __re
   if (threadIdx.x < kPrBins && s_tot[threadIdx.x]) atomicAdd(&tot[threadIdx.x], s_tot[threadIdx.x]);
 }
 
+// ---- incremental CSC: one compaction's kept edges merged in ------------------------
+// Renumbered (target, source) keys of the kept edges (csc_keys_kernel's key, by target).
+__global__ void csc_delta_keys_kernel(const uint32_t* __restrict__ nloc, const uint32_t* __restrict__ ntile,
+                                      uint64_t kept, const uint32_t* __restrict__ perm, uint32_t lg_n, uint32_t lT,
+                                      uint32_t lvpt, uint64_t* __restrict__ keys) {
+  const uint32_t ymask = (1u << lT) - 1u;
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < kept; i += stride) {
+    const uint32_t t = ntile[i], p = nloc[i];
+    const uint32_t u = perm[((t >> lT) << lvpt) | (p >> 16)];
+    const uint32_t v = perm[((t & ymask) << lvpt) | (p & 0xFFFFu)];
+    keys[i] = ((uint64_t)v << lg_n) | u;
+  }
+}
+
+// Per target: the new keys it receives (cnt), and each new key's source gains an
+// out-edge (deg_out, one atomic per source and warp).
+__global__ void csc_delta_count_kernel(const uint64_t* __restrict__ keys, uint64_t kept, uint32_t lg_n,
+                                       uint32_t* __restrict__ cnt, uint32_t* __restrict__ deg_out) {
+  const uint64_t mask = (1ULL << lg_n) - 1ULL;
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < kept; i += stride) {
+    const uint64_t k = keys[i];
+    atomicAdd(&cnt[k >> lg_n], 1u);
+    const uint32_t u = (uint32_t)(k & mask);
+    const unsigned m = __match_any_sync(__activemask(), u);
+    if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) atomicAdd(&deg_out[u], (unsigned)__popc(m));
+  }
+}
+
+// np[v] = ptr[v] + dx[v]: the merged segment offsets (dx = new keys before target v).
+__global__ void csc_new_ptr_kernel(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ dx, uint64_t n,
+                                   uint32_t* __restrict__ np) {
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v <= n; v += stride) np[v] = ptr[v] + dx[v];
+}
+
+// Every target's old in-edges [ptr[v], ptr[v+1]) and new ones (sorted keys
+// [dx[v], dx[v+1])) written ascending by source at ptr[v] + dx[v] of nsrc: an entry's
+// place is its index in its own list plus the number of the other list's sources below
+// it (the lists share no source: the store keeps every edge once). Targets are taken by
+// the old bin layout, pr_bin_vw(k) lanes each (a whole block for the largest bin).
+__global__ void __launch_bounds__(PR_T) csc_merge_kernel(const PrBinLaunch* __restrict__ blp,
+                                                         const uint32_t* __restrict__ bins,
+                                                         const uint32_t* __restrict__ ptr,
+                                                         const uint32_t* __restrict__ src,
+                                                         const uint64_t* __restrict__ keys,
+                                                         const uint32_t* __restrict__ dx, uint32_t lg_n,
+                                                         uint32_t* __restrict__ nsrc) {
+  const uint64_t mask = (1ULL << lg_n) - 1ULL;
+  const uint32_t total = blp->blocks;
+  for (uint32_t vb = blockIdx.x; vb < total; vb += gridDim.x) {
+    int k = 0;
+    while (k < kPrBins && !(vb >= blp->first[k] && vb - blp->first[k] < blp->nblk[k])) ++k;
+    if (k == kPrBins) continue;
+    const uint64_t bid = vb - blp->first[k], nblk = blp->nblk[k];
+    const uint64_t off = blp->off[k], cnt = blp->count[k];
+    const unsigned G = pr_bin_vw(k) == 0 ? blockDim.x : (unsigned)pr_bin_vw(k);
+    const uint64_t gpb = blockDim.x / G;
+    const unsigned gl = threadIdx.x % G;
+    for (uint64_t i = bid * gpb + threadIdx.x / G; i < cnt; i += nblk * gpb) {
+      const uint32_t v = bins[off + i];
+      const uint32_t olo = ptr[v], ohi = ptr[v + 1], dlo = dx[v], dhi = dx[v + 1];
+      const uint32_t out = olo + dlo;
+      if (dlo == dhi) {
+        for (uint32_t e = olo + gl; e < ohi; e += G) nsrc[out + (e - olo)] = src[e];
+        continue;
+      }
+      for (uint32_t e = olo + gl; e < ohi; e += G) {
+        const uint32_t sv = src[e];
+        uint32_t a = dlo, b = dhi;
+        while (a < b) {
+          const uint32_t m = (a + b) >> 1;
+          if ((uint32_t)(keys[m] & mask) < sv) a = m + 1;
+          else b = m;
+        }
+        nsrc[out + (e - olo) + (a - dlo)] = sv;
+      }
+      for (uint32_t j = dlo + gl; j < dhi; j += G) {
+        const uint32_t sv = (uint32_t)(keys[j] & mask);
+        uint32_t a = olo, b = ohi;
+        while (a < b) {
+          const uint32_t m = (a + b) >> 1;
+          if (src[m] < sv) a = m + 1;
+          else b = m;
+        }
+        nsrc[out + (j - dlo) + (a - olo)] = sv;
+      }
+    }
+  }
+}
+
 static int grid_n(Ctx* c, uint64_t work, int threads = 256, int per_sm = 8) {
   uint64_t b = (work + threads - 1) / threads;
   uint64_t cap = (uint64_t)c->num_sms * per_sm;
@@ -268,6 +362,117 @@ static int build_csx(Ctx* c, Csc& q, int by_source, float** w, uint64_t* wcap) {
 
 static int build_csc(Ctx* c, Csc& q) { return build_csx(c, q, 0, nullptr, nullptr); }
 
+// Called by the compaction once it knows its kept edges (nloc / ntile, `kept` of them):
+// while the context's CSC matches the store before this compaction, the edges are saved
+// as CSC keys for merge_csc. Without room for them the next build re-sorts.
+int pagerank_note_kept(Ctx* c, const uint32_t* nloc, const uint32_t* ntile, uint64_t kept) {
+  c->pr_delta_version = ~0ULL;
+  const Csc* q = reinterpret_cast<const Csc*>(c->pr_csc);
+  if (!q || !q->src || !c->pr_perm || q->built_version != c->version) return CYTOM_OK;
+  if (kept > c->pr_delta_cap || !c->pr_delta_keys) {
+    cudaFree(c->pr_delta_keys);
+    c->pr_delta_keys = nullptr;
+    c->pr_delta_cap = 0;
+    const uint64_t cap = std::max<uint64_t>(kept + kept / 2, 1024);
+    if (cy_malloc(&c->pr_delta_keys, cap * 8) != cudaSuccess) {
+      cudaGetLastError();
+      return CYTOM_OK;
+    }
+    c->pr_delta_cap = cap;
+  }
+  uint32_t lg_n = 0;
+  while ((1ULL << lg_n) < c->n) ++lg_n;
+  if (kept) {
+    csc_delta_keys_kernel<<<grid_n(c, kept), 256, 0, c->stream>>>(nloc, ntile, kept, c->pr_perm, lg_n, c->lT, c->lvpt,
+                                                                  c->pr_delta_keys);
+    c->launches++;
+  }
+  c->pr_delta_count = kept;
+  c->pr_delta_version = c->version + 1;
+  return cuda_err(c, cudaGetLastError(), "CSC delta keys");
+}
+
+// The CSC after one compaction that only added edges: the saved keys sorted, counted
+// per target and merged into the old segments (csc_merge_kernel) -- the same CSC,
+// offsets, out-degrees and bins a full build of the new store gives, without re-sorting
+// the old edges.
+static int merge_csc(Ctx* c, Csc& q) {
+  const uint64_t n = c->n, K = c->pr_delta_count, E = q.E + K;
+  if (E != c->E || E > 0xFFFFFFFFULL - (1ULL << 20)) return build_csc(c, q);
+  uint32_t lg_n = 0;
+  while ((1ULL << lg_n) < n) ++lg_n;
+  if (E > q.cap_alt || !q.src_alt) {
+    cudaFree(q.src_alt);
+    q.src_alt = nullptr;
+    q.cap_alt = 0;
+    const uint64_t cap = std::max<uint64_t>(E + E / 4, 1024);
+    if (cy_malloc(&q.src_alt, cap * 4) != cudaSuccess) {
+      cudaGetLastError();
+      return build_csc(c, q);
+    }
+    q.cap_alt = cap;
+  }
+  const size_t kb = std::max<uint64_t>(K, 1) * 8, nb8 = std::max<uint64_t>(n, 1) * 8, n4 = (n + 1) * 4;
+  char* tmp = nullptr;
+  if (cy_malloc_async((void**)&tmp, kb + 2 * nb8 + 4 * n4 + 64, c->stream) != cudaSuccess)
+    return set_err(c, CYTOM_ERR_OOM, "CSC merge temporaries");
+  uint64_t* kalt = (uint64_t*)tmp;
+  uint64_t* bk0 = (uint64_t*)(tmp + kb);
+  uint64_t* bk1 = (uint64_t*)(tmp + kb + nb8);
+  uint32_t* cnt = (uint32_t*)(tmp + kb + 2 * nb8);
+  uint32_t* dx = cnt + (n + 1);
+  uint32_t* np = dx + (n + 1);
+  uint32_t* vid = np + (n + 1);
+  uint32_t* tot = vid + (n + 1);
+  bool alt = false;
+  int rc = radix_sort_pairs(c, c->pr_delta_keys, kalt, nullptr, nullptr, K, (int)(2 * lg_n), &alt);
+  if (rc) return rc;
+  const uint64_t* keys = alt ? kalt : c->pr_delta_keys;
+  cudaMemsetAsync(cnt, 0, n4, c->stream);
+  cudaMemsetAsync(tot, 0, 64, c->stream);
+  if (K) {
+    csc_delta_count_kernel<<<grid_n(c, K), 256, 0, c->stream>>>(keys, K, lg_n, cnt, q.deg_out);
+    c->launches++;
+  }
+  rc = exclusive_scan_u32(c, cnt, dx, n, dx + n);
+  if (rc) return rc;
+  csc_new_ptr_kernel<<<grid_n(c, n + 1), 256, 0, c->stream>>>(q.ptr, dx, n, np);
+  const PrBinLaunch old_bl = bin_launch(c, q.nb);
+  csc_merge_kernel<<<std::max<uint32_t>(1, std::min<uint32_t>(old_bl.blocks, (uint32_t)c->num_sms * 8)), PR_T, 0,
+                     c->stream>>>(q.dbl, q.bins, q.ptr, q.src, keys, dx, lg_n, q.src_alt);
+  c->launches += 2;
+  // bins of the new in-degrees, as build_csx makes them
+  csc_cnt_bins_kernel<<<grid_n(c, n), 256, 0, c->stream>>>(np, np + 1, n, cnt, bk0, vid, tot);
+  c->launches++;
+  bool balt = false;
+  rc = radix_sort_pairs(c, bk0, bk1, vid, q.bins, n, 3, &balt);
+  if (rc) return rc;
+  if (!balt) cudaMemcpyAsync(q.bins, vid, n * 4, cudaMemcpyDeviceToDevice, c->stream);
+  cudaMemcpyAsync(q.ptr, np, n4, cudaMemcpyDeviceToDevice, c->stream);
+  uint32_t ht[kPrBins];
+  cudaMemcpyAsync(ht, tot, sizeof(ht), cudaMemcpyDeviceToHost, c->stream);
+  cudaFreeAsync(tmp, c->stream);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "CSC merge");
+  std::swap(q.src, q.src_alt);
+  std::swap(q.cap, q.cap_alt);
+  for (int k = 0; k < kPrBins; ++k) q.nb[k] = ht[k];
+  q.E = E;
+  const PrBinLaunch hb = bin_launch(c, q.nb);
+  // pageable source: the call returns once the bytes are staged
+  e = cudaMemcpyAsync(q.dbl, &hb, sizeof(hb), cudaMemcpyHostToDevice, c->stream);
+  return e == cudaSuccess ? CYTOM_OK : cuda_err(c, e, "CSC bins");
+}
+
+// The CSC for the current store: merged from the previous one when exactly one
+// compaction (that saved its kept edges) lies between them, rebuilt otherwise.
+static int update_csc(Ctx* c, Csc& q) {
+  if (q.src && q.dbl && q.built_version != ~0ULL && q.built_version + 1 == c->version &&
+      c->pr_delta_version == c->version)
+    return merge_csc(c, q);
+  return build_csc(c, q);
+}
+
 // ---- renumbering by out-degree ---------------------------------------------------
 __global__ void perm_keys_kernel(const uint32_t* __restrict__ deg, uint64_t n, uint32_t lg_n,
                                  uint64_t* __restrict__ keys) {
@@ -347,27 +552,27 @@ __global__ void pr_contrib_kernel(PrArgs a) {
   LoopState* ls = a.ls;
   if (!ls->cont) return;
   const unsigned p = ls->iter & 1u;
-  const double dangling = pr_contrib_range<MODE, false>(a, p, 0, a.n, (uint64_t)blockIdx.x * blockDim.x + threadIdx.x,
+  const pr_ff_t<MODE> dangling = pr_contrib_range<MODE, false>(a, p, 0, a.n, (uint64_t)blockIdx.x * blockDim.x + threadIdx.x,
                                                         (uint64_t)gridDim.x * blockDim.x);
   pr_dangling_flush<MODE>(ls, p, dangling);
 }
 
 template <int MODE>
-__device__ __forceinline__ void pull_small_body(const PrArgs& a, const pr_val_t<MODE>* cr, unsigned p, double dang,
+__device__ __forceinline__ void pull_small_body(const PrArgs& a, const pr_val_t<MODE>* cr, unsigned p, pr_ff_t<MODE> dang,
                                                 uint64_t bid, uint64_t nblk, PrTally& t) {
   const uint64_t stride = nblk * blockDim.x;
   for (uint64_t base = bid * blockDim.x; base < a.bin_count; base += stride) {
     const uint64_t i = base + threadIdx.x;
     if (i < a.bin_count) {
       const uint32_t v = a.bins[a.bin_off + i];
-      const double sum = pr_sum_thread<MODE, false>(a, cr, v);
+      const pr_ff_t<MODE> sum = pr_sum_thread<MODE, false>(a, cr, v);
       pr_finish<MODE, false>(a, v, sum, p, dang, t);
     }
   }
 }
 
 template <int MODE, int VW>
-__device__ __forceinline__ void pull_group_body(const PrArgs& a, const pr_val_t<MODE>* cr, unsigned p, double dang,
+__device__ __forceinline__ void pull_group_body(const PrArgs& a, const pr_val_t<MODE>* cr, unsigned p, pr_ff_t<MODE> dang,
                                                 uint64_t bid, uint64_t nblk, PrTally& t) {
   constexpr uint64_t GPW = 32 / VW;  // groups per warp
   const unsigned gl = threadIdx.x & (VW - 1);
@@ -383,17 +588,17 @@ __device__ __forceinline__ void pull_group_body(const PrArgs& a, const pr_val_t<
       lo = a.csc_ptr[v];
       hi = a.csc_ptr[v + 1];
     }
-    const double sum = pr_sum_group<MODE, false, VW>(a, cr, lo, hi, gl);
+    const pr_ff_t<MODE> sum = pr_sum_group<MODE, false, VW>(a, cr, lo, hi, gl);
     if (gl == 0 && i < a.bin_count) pr_finish<MODE, false>(a, v, sum, p, dang, t);
   }
 }
 
 template <int MODE>
-__device__ __forceinline__ void pull_large_body(const PrArgs& a, const pr_val_t<MODE>* cr, unsigned p, double dang,
+__device__ __forceinline__ void pull_large_body(const PrArgs& a, const pr_val_t<MODE>* cr, unsigned p, pr_ff_t<MODE> dang,
                                                 uint64_t bid, uint64_t nblk, PrTally& t) {
   for (uint64_t i = bid; i < a.bin_count; i += nblk) {
     const uint32_t v = a.bins[a.bin_off + i];
-    const double sum = pr_sum_block<MODE, false>(a, cr, v);
+    const pr_ff_t<MODE> sum = pr_sum_block<MODE, false>(a, cr, v);
     if (threadIdx.x == 0) pr_finish<MODE, false>(a, v, sum, p, dang, t);
   }
 }
@@ -443,7 +648,7 @@ __global__ void __launch_bounds__(PR_T) pr_pull_kernel(PrArgs a, const PrBinLaun
   PrTally t;
   t.init();
   const uint32_t total = live ? blp->blocks : 0u;
-  const double dang = pr_dang_arg<MODE, false>(ls, p, a.n);
+  const pr_ff_t<MODE> dang = pr_dang_arg<MODE, false>(a, ls, p);
   const pr_val_t<MODE>* cr = pr_cread<MODE>(a, p);
   for (uint32_t vb = blockIdx.x; vb < total; vb += gridDim.x) {
     int k = 0;
@@ -527,7 +732,7 @@ static Csc* ctx_csc(Ctx* c) {
 }
 
 static void csc_free(Csc* q) {
-  void* ptrs[] = {q->src, q->ptr, q->deg_out, q->bins, q->dbl};
+  void* ptrs[] = {q->src, q->src_alt, q->ptr, q->deg_out, q->bins, q->dbl};
   for (void* p : ptrs)
     if (p) cudaFree(p);
 }
@@ -538,10 +743,13 @@ static WGraph* ctx_wgraph(Ctx* c) {
 }
 
 void pagerank_ctx_free(Ctx* c) {
-  void* pp[] = {c->pr_perm, c->pr_inv, c->pr_deg_mult};
+  void* pp[] = {c->pr_perm, c->pr_inv, c->pr_deg_mult, c->pr_delta_keys};
   for (void* p : pp)
     if (p) cudaFree(p);
   c->pr_perm = c->pr_inv = c->pr_deg_mult = nullptr;
+  c->pr_delta_keys = nullptr;
+  c->pr_delta_cap = 0;
+  c->pr_delta_version = ~0ULL;
   Csc* q = reinterpret_cast<Csc*>(c->pr_csc);
   if (q) {
     csc_free(q);
@@ -839,7 +1047,7 @@ int pagerank_run(Ctx* c, Job* j) {
   PrState* s = prs(j);
   const uint64_t ver = store_version(c);
   if (s->csc->built_version != ver) {
-    int rc = build_csc(c, *s->csc);
+    int rc = update_csc(c, *s->csc);
     if (rc) return rc;
     s->csc->built_version = ver;
   }
@@ -866,6 +1074,7 @@ int pagerank_run(Ctx* c, Job* j) {
   a.alpha = j->params.alpha;
   a.delta_param = j->params.delta;
   a.base = (1.0 - j->params.alpha) / (double)n;
+  pr_args_ff(a);
   unsigned max_iter = (unsigned)std::min<uint64_t>(j->params.max_iterations, 0xFFFFFFFFu);
   pr_begin_kernel<<<1, 1, 0, c->stream>>>(j->ls, max_iter, j->params.tolerance, (unsigned long long)s->csc->E);
   c->launches++;
@@ -901,7 +1110,7 @@ int pagerank_batch_prep(Ctx* c, Job* j, PrArgs* out, uint64_t* nb, int* first_mo
   PrState* s = prs(j);
   const uint64_t ver = store_version(c);
   if (s->csc->built_version != ver) {
-    int rc = build_csc(c, *s->csc);
+    int rc = update_csc(c, *s->csc);
     if (rc) return rc;
     s->csc->built_version = ver;
   }
@@ -925,6 +1134,7 @@ int pagerank_batch_prep(Ctx* c, Job* j, PrArgs* out, uint64_t* nb, int* first_mo
   a.alpha = j->params.alpha;
   a.delta_param = j->params.delta;
   a.base = (1.0 - j->params.alpha) / (double)n;
+  pr_args_ff(a);
   unsigned max_iter = (unsigned)std::min<uint64_t>(j->params.max_iterations, 0xFFFFFFFFu);
   pr_begin_kernel<<<1, 1, 0, c->stream>>>(j->ls, max_iter, j->params.tolerance, (unsigned long long)s->csc->E);
   c->launches++;
@@ -1067,6 +1277,7 @@ static PrArgs wargs(Ctx* c, Job* j, const WGraph& g) {
   a.ls = j->ls;
   a.n = c->n;
   a.alpha = j->params.alpha;
+  pr_args_ff(a);
   return a;
 }
 
@@ -1245,6 +1456,7 @@ int pagerank_adjoint(Ctx* c, Job* j, const double* cv, int cwhere, float* d_w, f
   a.ls = s->adj_ls;
   a.n = n;
   a.alpha = j->params.alpha;
+  pr_args_ff(a);
   int rc = f32 ? run_rounds<PR_ADJ32>(c, j, a, max_iter, g->out) : run_rounds<PR_ADJ64>(c, j, a, max_iter, g->out);
   if (rc) return rc;
   LoopState als;

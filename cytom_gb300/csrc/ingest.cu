@@ -927,6 +927,11 @@ int compact(Ctx* c) {
   }
   uint64_t Kn = *(uint32_t*)c->h_pinned;
   prof_end(c, slot, (double)A * (wt ? 44.0 : 36.0) + (double)(c->E + Kn) * (wt ? 16.0 : 8.0));
+  rc = pagerank_note_kept(c, nloc, ntile, Kn);  // the PageRank CSC's next build merges these in
+  if (rc) {
+    cudaFreeAsync(tmp, c->stream);
+    return rc;
+  }
   // Installing the merged snapshot: runs on the previous one must have finished. The jobs
   // are then seeded by the merged edges (edgeChanged(INSERT)) and lowered weights of
   // stored edges are applied to the merged copy.

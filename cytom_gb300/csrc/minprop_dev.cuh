@@ -468,15 +468,15 @@ __device__ __forceinline__ void sp_batch(const JobDesc* __restrict__ jd, const S
   const bool async = jd->async != 0;
   uint32_t pk[SP_ILP], wv[SP_ILP], cand[SP_ILP], nv[SP_ILP];
 #pragma unroll
-  for (int k = 0; k < SP_ILP; ++k) {
-    pk[k] = ((valid >> k) & 1u) ? sd->edges[pos[k]] : 0u;
-    wv[k] = (mp_weighted<ALGO>() && ((valid >> k) & 1u)) ? sd->wts[pos[k]] : 0u;
-  }
+  for (int k = 0; k < SP_ILP; ++k) pk[k] = ((valid >> k) & 1u) ? sd->edges[pos[k]] : 0u;
+  // the weight is read only for an edge whose source is in the frontier, beside its
+  // source value (one dependent step, as before; most listed edges have inactive sources)
 #pragma unroll
   for (int k = 0; k < SP_ILP; ++k) {
     const uint32_t sl = pk[k] >> 16;
     const bool act = ((valid >> k) & 1u) && ((bits[k] >> (sl & 31)) & 1u);
     cand[k] = act ? ld_src<PERSIST>(jd, async, (xs[k] << lvpt) | sl) : kInf;
+    wv[k] = (mp_weighted<ALGO>() && act) ? sd->wts[pos[k]] : 0u;
   }
 #pragma unroll
   for (int k = 0; k < SP_ILP; ++k)

@@ -97,6 +97,41 @@ struct Acc64 {
   __device__ __forceinline__ double value() const { return s; }
 };
 
+// Float-float numbers: an unevaluated pair hi + lo of FP32 values (about 44 significant
+// bits), built from error-free transformations -- Knuth's two-sum, Dekker's fast two-sum
+// (|a| >= |b|) and the FMA-exact product. GB300 runs FP64 at a small fraction of its FP32
+// rate, so the FP32-compensated PageRank keeps its per-target arithmetic (update, change,
+// dangling mass) in this form instead of FP64. The _rn intrinsics keep the compiler from
+// contracting the transformations' products and sums into FMAs.
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ FF ff_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ FF ff_fast_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const FF s = ff_two_sum(a.hi, b.hi);
+  const FF t = ff_two_sum(a.lo, b.lo);
+  const FF u = ff_fast_two_sum(s.hi, __fadd_rn(s.lo, t.hi));
+  return ff_fast_two_sum(u.hi, __fadd_rn(u.lo, t.lo));
+}
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  const float e = __fmaf_rn(a.hi, b.hi, -p);
+  return ff_fast_two_sum(p, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e)));
+}
+__device__ __forceinline__ FF ff_abs(FF a) { return a.hi < 0.f ? FF{-a.hi, -a.lo} : a; }
+__host__ __device__ inline FF ff_from_double(double x) {
+  const float hi = (float)x;
+  return {hi, (float)(x - (double)hi)};
+}
+
 struct PrArgs {
   const uint32_t* csc_src;
   const uint32_t* csc_ptr;
@@ -121,7 +156,20 @@ struct PrArgs {
   LoopState* ls;
   uint64_t n;
   double alpha, delta_param, base;
+  FF alpha_ff, base_ff, inv_n_ff;  // alpha, base and 1/n as float-float (pr_args_ff)
 };
+
+// Fills the float-float copies of alpha, base and 1/n (host, after those are set).
+inline void pr_args_ff(PrArgs& a) {
+  a.alpha_ff = ff_from_double(a.alpha);
+  a.base_ff = ff_from_double(a.base);
+  a.inv_n_ff = ff_from_double(a.n ? 1.0 / (double)a.n : 0.0);
+}
+
+// A round's sums and the dangling term: float-float in the FP32-compensated form, FP64
+// in the others.
+template <int MODE>
+using pr_ff_t = typename std::conditional<MODE == PR_NORM32, FF, double>::type;
 
 template <bool PERSIST, class T>
 __device__ __forceinline__ T pr_ld(const T* p) {
@@ -152,16 +200,16 @@ __device__ __forceinline__ pr_val_t<MODE> pr_cval(const PrArgs& a, const pr_val_
 // other forms.
 // Returns the thread's share of the dangling mass (PAGERANK).
 template <int MODE, bool PERSIST>
-__device__ __forceinline__ double pr_contrib_range(const PrArgs& a, unsigned p, uint64_t lo, uint64_t hi,
-                                                   uint64_t tid, uint64_t nthr) {
-  double dangling = 0.0;
-  if (MODE == PR_DELTA_RESIDUAL || MODE == PR_DELTA_PUSH) {
+__device__ __forceinline__ pr_ff_t<MODE> pr_contrib_range(const PrArgs& a, unsigned p, uint64_t lo, uint64_t hi,
+                                                          uint64_t tid, uint64_t nthr) {
+  pr_ff_t<MODE> dangling{};
+  if constexpr (MODE == PR_DELTA_RESIDUAL || MODE == PR_DELTA_PUSH) {
     float* cw = a.contrib + (uint64_t)p * a.n;
     for (uint64_t u = lo + tid; u < hi; u += nthr) {
       const uint32_t d = a.deg[u];
       cw[u] = d ? pr_ld<PERSIST>(a.rank + u) / (float)d : 0.f;
     }
-  } else if (MODE == PR_NORM32) {
+  } else if constexpr (MODE == PR_NORM32) {
     const float* r = (p == 0) ? a.rank : a.comp;
     const float* rl = (p == 0) ? a.lo0 : a.lo1;
     float* cw = a.contrib;
@@ -171,9 +219,9 @@ __device__ __forceinline__ double pr_contrib_range(const PrArgs& a, unsigned p, 
       const uint32_t d = a.deg[u];
       const float rh = pr_ld<PERSIST>(r + u);
       cw[u] = d ? rh / (float)d : 0.f;
-      if (!d) dangling += (double)rh + (double)pr_ld<PERSIST>(rl + u);
+      if (!d) dangling = ff_add(dangling, FF{rh, pr_ld<PERSIST>(rl + u)});
     }
-  } else if (MODE == PR_W32) {
+  } else if constexpr (MODE == PR_W32) {
     const float* r = (p == 0) ? a.rank : a.comp;
     const float* rl = (p == 0) ? a.lo0 : a.lo1;
     for (uint64_t u = lo + tid; u < hi; u += nthr) {
@@ -182,7 +230,7 @@ __device__ __forceinline__ double pr_contrib_range(const PrArgs& a, unsigned p, 
       a.contrib[u] = s > 0.0 ? rh / (float)s : 0.f;
       if (!(s > 0.0)) dangling += (double)rh + (double)pr_ld<PERSIST>(rl + u);
     }
-  } else if (MODE == PR_W64) {
+  } else if constexpr (MODE == PR_W64) {
     const double* r = (p == 0) ? a.r64 : a.r64n;
     for (uint64_t u = lo + tid; u < hi; u += nthr) {
       const double s = a.wsum[u];
@@ -190,7 +238,7 @@ __device__ __forceinline__ double pr_contrib_range(const PrArgs& a, unsigned p, 
       a.contrib64[u] = s > 0.0 ? rv / s : 0.0;
       if (!(s > 0.0)) dangling += rv;
     }
-  } else if (MODE == PR_ADJ32) {
+  } else if constexpr (MODE == PR_ADJ32) {
     // gather source = lambda itself; the returned sum is t . lambda
     const float* l = (p == 0) ? a.rank : a.comp;
     const double tu = 1.0 / (double)a.n;
@@ -199,7 +247,7 @@ __device__ __forceinline__ double pr_contrib_range(const PrArgs& a, unsigned p, 
       a.contrib[u] = lv;
       dangling += (a.tele ? a.tele[u] : tu) * (double)lv;
     }
-  } else if (MODE == PR_ADJ64) {
+  } else if constexpr (MODE == PR_ADJ64) {
     const double* l = (p == 0) ? a.r64 : a.r64n;
     const double tu = 1.0 / (double)a.n;
     for (uint64_t u = lo + tid; u < hi; u += nthr) {
@@ -222,8 +270,16 @@ __device__ __forceinline__ double pr_contrib_range(const PrArgs& a, unsigned p, 
 
 // Warp-reduced dangling mass into the loop state (every lane calls it).
 template <int MODE>
-__device__ __forceinline__ void pr_dangling_flush(LoopState* ls, unsigned p, double dangling) {
-  if (MODE >= PR_NORM32) {
+__device__ __forceinline__ void pr_dangling_flush(LoopState* ls, unsigned p, pr_ff_t<MODE> dangling) {
+  if constexpr (MODE == PR_NORM32) {
+    // float-float warp sum; one conversion per warp
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      dangling = ff_add(dangling, FF{__shfl_xor_sync(0xFFFFFFFFu, dangling.hi, o),
+                                     __shfl_xor_sync(0xFFFFFFFFu, dangling.lo, o)});
+    if ((threadIdx.x & 31) == 0 && dangling.hi != 0.f)
+      atomicAdd(&ls->dangling[p], (double)dangling.hi + (double)dangling.lo);
+  } else if constexpr (MODE >= PR_NORM32) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) dangling += __shfl_xor_sync(0xFFFFFFFFu, dangling, o);
     if ((threadIdx.x & 31) == 0 && dangling != 0.0) atomicAdd(&ls->dangling[p], dangling);
@@ -233,37 +289,39 @@ __device__ __forceinline__ void pr_dangling_flush(LoopState* ls, unsigned p, dou
 // The round's dangling term as pr_finish takes it: D / n (normalised PageRank), D
 // (weighted: scaled by t_v in pr_finish), t . lambda (adjoint), none (PageRank-delta).
 template <int MODE, bool PERSIST>
-__device__ __forceinline__ double pr_dang_arg(const LoopState* ls, unsigned p, uint64_t n) {
-  if (MODE < PR_NORM32) return 0.0;
-  const double d = pr_ld<PERSIST>(&ls->dangling[p]);
-  return (MODE == PR_NORM32 || MODE == PR_NORM64) ? d / (double)n : d;
+__device__ __forceinline__ pr_ff_t<MODE> pr_dang_arg(const PrArgs& a, const LoopState* ls, unsigned p) {
+  if constexpr (MODE == PR_NORM32) {
+    return ff_mul(ff_from_double(pr_ld<PERSIST>(&ls->dangling[p])), a.inv_n_ff);
+  } else {
+    if (MODE < PR_NORM32) return 0.0;
+    const double d = pr_ld<PERSIST>(&ls->dangling[p]);
+    return MODE == PR_NORM64 ? d / (double)a.n : d;
+  }
+}
+
+// The normalised forms' rank of v before the round (FP32: high and low word; FP64: d),
+// loaded ahead of the sum by the batched executor's pulls.
+struct PrOld {
+  double d;
+  float hi, lo;
+};
+template <int MODE, bool PERSIST>
+__device__ __forceinline__ PrOld pr_load_old(const PrArgs& a, uint64_t v, unsigned p) {
+  PrOld o{};
+  if constexpr (MODE == PR_NORM32) {
+    o.hi = pr_ld<PERSIST>(((p == 0) ? a.rank : a.comp) + v);
+    o.lo = pr_ld<PERSIST>(((p == 0) ? a.lo0 : a.lo1) + v);
+  } else {
+    o.d = pr_ld<PERSIST>(((p == 0) ? a.r64 : a.r64n) + v);
+  }
+  return o;
 }
 
 // The update of target v (pr_finish); returns |change| for the FP64 residual.
 template <int MODE, bool PERSIST>
 __device__ __forceinline__ double pr_apply(const PrArgs& a, uint64_t v, double sum, unsigned p, double dang,
                                            double* rsum, unsigned* nact) {
-  if (MODE == PR_NORM32) {
-    const float* r = (p == 0) ? a.rank : a.comp;
-    const float* rl = (p == 0) ? a.lo0 : a.lo1;
-    float* rn = (p == 0) ? a.comp : a.rank;
-    float* rnl = (p == 0) ? a.lo1 : a.lo0;
-    const double nv = a.base + a.alpha * (sum + dang);
-    const float hi = (float)nv;
-    const double d = fabs(nv - ((double)pr_ld<PERSIST>(r + v) + (double)pr_ld<PERSIST>(rl + v)));
-    rn[v] = hi;
-    rnl[v] = (float)(nv - (double)hi);
-    *rsum += nv;
-    return d;
-  } else if (MODE == PR_NORM64) {
-    const double* r = (p == 0) ? a.r64 : a.r64n;
-    double* rn = (p == 0) ? a.r64n : a.r64;
-    const double nv = a.base + a.alpha * (sum + dang);
-    const double d = fabs(nv - pr_ld<PERSIST>(r + v));
-    rn[v] = nv;
-    *rsum += nv;
-    return d;
-  } else if (MODE == PR_W32 || MODE == PR_W64) {
+  if (MODE == PR_W32 || MODE == PR_W64) {
     const double tv = a.tele ? a.tele[v] : 1.0 / (double)a.n;
     const double nv = tv * ((1.0 - a.alpha) + a.alpha * dang) + a.alpha * sum;
     if (MODE == PR_W32) {
@@ -335,17 +393,43 @@ __device__ __forceinline__ double pr_apply(const PrArgs& a, uint64_t v, double s
 // (pr_tally_flush).
 struct PrTally {
   double resid, rsum;
+  FF fres;  // FP32-compensated form: the residual in float-float
   unsigned nact;
-  __device__ __forceinline__ void init() { resid = rsum = 0.0, nact = 0u; }
+  __device__ __forceinline__ void init() { resid = rsum = 0.0, fres = FF{0.f, 0.f}, nact = 0u; }
 };
+
+// The normalised forms' update of v from its sum and its rank before the round; the
+// residual share goes to the tally (the rank sum is not kept: their control step does
+// not read it). FP32-compensated: nv = base + alpha (sum + D/n) in float-float, stored as
+// its high and low words; FP64: the same in FP64.
+template <int MODE>
+__device__ __forceinline__ void pr_apply_norm(const PrArgs& a, uint64_t v, pr_ff_t<MODE> sum, unsigned p,
+                                              pr_ff_t<MODE> dang, PrOld o, PrTally& t) {
+  if constexpr (MODE == PR_NORM32) {
+    float* rn = (p == 0) ? a.comp : a.rank;
+    float* rnl = (p == 0) ? a.lo1 : a.lo0;
+    const FF nv = ff_add(a.base_ff, ff_mul(a.alpha_ff, ff_add(sum, dang)));
+    rn[v] = nv.hi;
+    rnl[v] = nv.lo;
+    t.fres = ff_add(t.fres, ff_abs(ff_add(nv, FF{-o.hi, -o.lo})));
+  } else {
+    double* rn = (p == 0) ? a.r64n : a.r64;
+    const double nv = a.base + a.alpha * (sum + dang);
+    rn[v] = nv;
+    t.resid += fabs(nv - o.d);
+  }
+}
 
 // Applies the finished sum of target v and adds its share to the tally. The fused form
 // also writes v's contribution to the next round (half p^1), exactly as the
 // contribution pass would compute it from the new delta.
 template <int MODE, bool PERSIST>
-__device__ __forceinline__ void pr_finish(const PrArgs& a, uint64_t v, double sum, unsigned p, double dang,
-                                          PrTally& t) {
-  t.resid += pr_apply<MODE, PERSIST>(a, v, sum, p, dang, &t.rsum, &t.nact);
+__device__ __forceinline__ void pr_finish(const PrArgs& a, uint64_t v, pr_ff_t<MODE> sum, unsigned p,
+                                          pr_ff_t<MODE> dang, PrTally& t) {
+  if constexpr (MODE == PR_NORM32 || MODE == PR_NORM64)
+    pr_apply_norm<MODE>(a, v, sum, p, dang, pr_load_old<MODE, PERSIST>(a, v, p), t);
+  else
+    t.resid += pr_apply<MODE, PERSIST>(a, v, sum, p, dang, &t.rsum, &t.nact);
 }
 
 // The block's tally into the loop state: one atomic per quantity and block (every
@@ -356,11 +440,21 @@ __device__ __forceinline__ void pr_tally_flush(LoopState* ls, unsigned p, PrTall
   __shared__ double s_r[32], s_s[32];
   __shared__ unsigned s_n[32];
   constexpr bool kN = pr_fused<MODE>();  // activations (PageRank-delta)
+  constexpr bool kS = MODE != PR_NORM32 && MODE != PR_NORM64;  // rank sum kept
   if (!kN) t.nact = 0u;
+  if constexpr (MODE == PR_NORM32) {
+    // float-float warp sum of the residual; one conversion per warp
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      t.fres = ff_add(t.fres, FF{__shfl_xor_sync(0xFFFFFFFFu, t.fres.hi, o), __shfl_xor_sync(0xFFFFFFFFu, t.fres.lo, o)});
+    t.resid = (double)t.fres.hi + (double)t.fres.lo;
+  } else {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t.resid += __shfl_xor_sync(0xFFFFFFFFu, t.resid, o);
+  }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    t.resid += __shfl_xor_sync(0xFFFFFFFFu, t.resid, o);
-    t.rsum += __shfl_xor_sync(0xFFFFFFFFu, t.rsum, o);
+    if (kS) t.rsum += __shfl_xor_sync(0xFFFFFFFFu, t.rsum, o);
     if (kN) t.nact += __shfl_xor_sync(0xFFFFFFFFu, t.nact, o);
   }
   const unsigned w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
@@ -418,9 +512,17 @@ __device__ __forceinline__ void pr_lane_sum(const PrArgs& a, const pr_val_t<MODE
   }
 }
 
+// A compensated FP32 sum as the update takes it: the float pair itself in the
+// FP32-compensated form, s + e in FP64 in the other FP32 forms.
+template <int MODE>
+__device__ __forceinline__ pr_ff_t<MODE> pr_acc32_out(float s, float e) {
+  if constexpr (MODE == PR_NORM32) return FF{s, e};
+  else return (double)s + (double)e;
+}
+
 // Sum of target v's in-edge contributions by one thread (in-degree <= 4), in edge order.
 template <int MODE, bool PERSIST>
-__device__ __forceinline__ double pr_sum_thread(const PrArgs& a, const pr_val_t<MODE>* cr, uint32_t v) {
+__device__ __forceinline__ pr_ff_t<MODE> pr_sum_thread(const PrArgs& a, const pr_val_t<MODE>* cr, uint32_t v) {
   const uint32_t lo = a.csc_ptr[v], hi = a.csc_ptr[v + 1];
   if constexpr (pr_is64<MODE>()) {
     Acc64 acc;
@@ -431,7 +533,7 @@ __device__ __forceinline__ double pr_sum_thread(const PrArgs& a, const pr_val_t<
     Acc32 acc;
     acc.init();
     pr_lane_sum<MODE, PERSIST, 4>(a, cr, lo, hi, 1u, acc);
-    return (double)acc.s + (double)acc.e;
+    return pr_acc32_out<MODE>(acc.s, acc.e);
   }
 }
 
@@ -440,7 +542,7 @@ __device__ __forceinline__ double pr_sum_thread(const PrArgs& a, const pr_val_t<
 // group sums edges lo+gl, lo+gl+VW, ... in order, then the group merges its lanes by an
 // xor tree. Every lane of the group returns the sum.
 template <int MODE, bool PERSIST, int VW>
-__device__ __forceinline__ double pr_sum_group(const PrArgs& a, const pr_val_t<MODE>* cr, uint32_t lo, uint32_t hi,
+__device__ __forceinline__ pr_ff_t<MODE> pr_sum_group(const PrArgs& a, const pr_val_t<MODE>* cr, uint32_t lo, uint32_t hi,
                                                unsigned gl) {
   constexpr int B = 4;
   if constexpr (pr_is64<MODE>()) {
@@ -461,19 +563,19 @@ __device__ __forceinline__ double pr_sum_group(const PrArgs& a, const pr_val_t<M
       const float e2 = __shfl_xor_sync(0xFFFFFFFFu, acc.e, o, VW);
       acc.merge(s2, e2);
     }
-    return (double)acc.s + (double)acc.e;
+    return pr_acc32_out<MODE>(acc.s, acc.e);
   }
 }
 
 // The same by a block of PR_BLOCK_T threads (in-degree > 4096: RMAT hubs); thread 0
 // returns the sum. Every thread of the block calls it.
 template <int MODE, bool PERSIST>
-__device__ __forceinline__ double pr_sum_block(const PrArgs& a, const pr_val_t<MODE>* cr, uint32_t v) {
+__device__ __forceinline__ pr_ff_t<MODE> pr_sum_block(const PrArgs& a, const pr_val_t<MODE>* cr, uint32_t v) {
   __shared__ float s_s[PR_BLOCK_T / 32], s_e[PR_BLOCK_T / 32];
   __shared__ double s_d[PR_BLOCK_T / 32];
   const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const uint32_t lo = a.csc_ptr[v], hi = a.csc_ptr[v + 1];
-  double sum = 0.0;
+  pr_ff_t<MODE> sum{};
   if constexpr (pr_is64<MODE>()) {
     Acc64 acc;
     acc.init();
@@ -505,7 +607,7 @@ __device__ __forceinline__ double pr_sum_block(const PrArgs& a, const pr_val_t<M
       Acc32 t;
       t.init();
       for (int k = 0; k < PR_BLOCK_T / 32; ++k) t.merge(s_s[k], s_e[k]);
-      sum = (double)t.s + (double)t.e;
+      sum = pr_acc32_out<MODE>(t.s, t.e);
     }
   }
   __syncthreads();

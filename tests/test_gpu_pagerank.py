@@ -89,3 +89,60 @@ def test_pagerank_normalised(cg, orc, kahan):
         else:
             assert l1 <= 1e-10, (l1, mr, stats)
         assert abs(np.asarray(got, np.float64).sum() - 1.0) < 1e-5
+
+
+@pytest.mark.parametrize("kahan", [True, False])
+def test_incremental_csc_matches_full_build(cg, orc, kahan):
+    # A context whose PageRank job runs after every batch merges the compaction's kept
+    # edges into its CSC (no re-sort); a context that runs PageRank only at the end sorts
+    # once. Fresh jobs on the two end in the same round with the same ranks up to the
+    # order of the FP64 dangling-mass atomics (a wrong or missing in-edge moves its
+    # target's rank by far more) -- after six batches with duplicates (within and across
+    # batches), after a deletion (a full rebuild on both) and after one more batch merged
+    # on top of the rebuilt CSC -- and the FP32 form stays within the tolerance of the
+    # FP64 oracle.
+    scale, vpt = 13, 1024
+    n = 1 << scale
+    st = orc.Store(n, vpt)
+
+    def fresh_pair(ea, eb):
+        fa = cg.PageRank(ea, max_iterations=300, tolerance=1e-10, kahan=kahan)
+        fb = cg.PageRank(eb, max_iterations=300, tolerance=1e-10, kahan=kahan)
+        sa, sb = fa.execute_algorithm(), fb.execute_algorithm()
+        assert sa["iterations"] == sb["iterations"]
+        ra = fa.result().astype(np.float64) if kahan else fa.result64()
+        rb = fb.result().astype(np.float64) if kahan else fb.result64()
+        assert np.allclose(ra, rb, rtol=1e-6 if kahan else 1e-12, atol=0), np.abs(ra - rb).max()
+        fa.destroy()
+        fb.destroy()
+        return ra
+
+    with cg.Engine(n, vpt) as ea, cg.Engine(n, vpt) as eb, cg.Engine(n, vpt) as ec:
+        pa = cg.PageRank(ea, max_iterations=300, tolerance=1e-10, kahan=kahan)
+        for b in range(6):
+            s, t = orc.rmat(scale, b * 2 * n, 2 * n, 77)
+            s = np.concatenate([s, s[:100]])  # duplicates inside the batch
+            t = np.concatenate([t, t[:100]])
+            for e in (ea, eb, ec):
+                e.insert_edges(s.copy(), t.copy())
+                e.do_global_compaction()
+            st.insert(s, t)
+            st.compact()
+            pa.execute_algorithm()
+        r = fresh_pair(ea, eb)
+        ref, _ = st.pagerank_norm(tol=1e-15)
+        l1, mr = rel_errors(r, ref)
+        assert l1 <= L1_TOL and mr <= MAXREL_TOL, (l1, mr)
+        ds, dt = orc.rmat(scale, 0, 500, 77)
+        for e in (ea, eb, ec):
+            e.delete_edges(ds.copy(), dt.copy())
+        pa.execute_algorithm()
+        fresh_pair(ea, eb)
+        s, t = orc.rmat(scale, 12 * n, 2 * n, 78)
+        for e in (ea, eb, ec):
+            e.insert_edges(s.copy(), t.copy())
+            e.do_global_compaction()
+        pa.execute_algorithm()
+        # ea merged the last batch into the CSC rebuilt after the deletion; ec, which ran
+        # no PageRank before, sorts once
+        fresh_pair(ea, ec)

@@ -313,6 +313,7 @@ int job_seed(Ctx* c, Job* j, const uint32_t* src, const uint32_t* tgt, const uin
              uint64_t count);
 int job_seed_keys(Ctx* c, Job* j, const uint64_t* K, const uint32_t* W, uint64_t count);
 int pagerank_note_kept(Ctx* c, const uint32_t* nloc, const uint32_t* ntile, uint64_t kept);
+int pagerank_csc_stage(Ctx* c);
 // The context's stream waits for runs launched asynchronously (no host wait); every
 // operation that touches the installed snapshot or job state comes after it.
 void join_runs(Ctx* c);

@@ -98,6 +98,19 @@ __host__ __device__ constexpr unsigned long long pack_claim(unsigned phase, unsi
 
 __device__ __forceinline__ uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
 
+// Units of a pull phase: every bin's targets in units of pr_bin_unit(k).
+__device__ __forceinline__ uint32_t pr_pull_units(const BJob* J) {
+  uint32_t t = 0;
+  for (int k = 0; k < kPrBins; ++k) t += ceil_div(J->nb[k], pr_bin_unit(k));
+  return t;
+}
+
+// Pull units are handed out from the largest in-degree bin down (unit 0 = the last unit
+// of the hub bin), so the longest units start first and the short ones fill the phase's
+// tail.
+__device__ __forceinline__ uint32_t pr_pull_order(const BJob* J, uint32_t unit) { return pr_pull_units(J) - 1u - unit; }
+
+
 // ---- units -----------------------------------------------------------------
 
 __device__ __forceinline__ unsigned ls_iter(const LoopState* ls) { return *(const volatile unsigned*)&ls->iter; }
@@ -206,7 +219,7 @@ __device__ void unit_pr_pull(const BJob* J, uint32_t unit) {
   // the bin this unit belongs to
   int k = 0;
   uint64_t off = 0;
-  uint32_t u = unit;
+  uint32_t u = pr_pull_order(J, unit);
   for (; k < kPrBins - 1; ++k) {
     const uint32_t units_k = ceil_div(J->nb[k], pr_bin_unit(k));
     if (u < units_k) break;
@@ -574,7 +587,7 @@ __device__ void unit_pr_pull_pair(const BJob* J, uint32_t unit) {
   fin.t1.init();
   int k = 0;
   uint64_t off = 0;
-  uint32_t u = unit;
+  uint32_t u = pr_pull_order(J, unit);
   for (; k < kPrBins - 1; ++k) {
     const uint32_t units_k = ceil_div(J->nb[k], pr_bin_unit(k));
     if (u < units_k) break;
@@ -602,11 +615,6 @@ __device__ void unit_pr_pull_pair(const BJob* J, uint32_t unit) {
   if (fin.on1) pr_tally_flush<MODE>(a1.ls, fin.p1, fin.t1);
 }
 
-__device__ __forceinline__ uint32_t pr_pull_units(const BJob* J) {
-  uint32_t t = 0;
-  for (int k = 0; k < kPrBins; ++k) t += ceil_div(J->nb[k], pr_bin_unit(k));
-  return t;
-}
 
 // ---- phase transitions (whole block, after the last unit of `phase`) --------
 
@@ -882,12 +890,21 @@ static int batch_run(Ctx* const* ctxs, const int* job_ids, int count, cytom_run_
       if (ctxs[m] == c && job_ids[m] == job_ids[k]) return set_err(c0, CYTOM_ERR_INVAL, "job listed twice in batch");
     if (std::find(uniq.begin(), uniq.end(), c) == uniq.end()) uniq.push_back(c);
   }
-  // per snapshot: merge pending edges, refresh the source directory
+  // per snapshot: merge pending edges, refresh the source directory, then enqueue every
+  // snapshot's PageRank CSC update before any is waited for (they run side by side)
   for (Ctx* c : uniq) {
     int rc = compact(c);
     if (!rc) rc = build_directory(c);
     if (rc) {
       if (c != c0) c0->err = c->err;
+      return rc;
+    }
+  }
+  for (int k = 0; k < count; ++k) {
+    if (!is_pr(jobs[k]->algo)) continue;
+    int rc = pagerank_csc_stage(ctxs[k]);
+    if (rc) {
+      if (ctxs[k] != c0) c0->err = ctxs[k]->err;
       return rc;
     }
   }

@@ -55,7 +55,7 @@ struct PrBinLaunch {
 // CSC of the compacted store, per job (PageRank family).
 struct Csc {
   uint32_t* src = nullptr;       // E: global source of each in-edge, grouped by target
-  uint32_t* src_alt = nullptr;   // the merge's output (merge_csc), swapped with src
+  uint32_t* src_alt = nullptr;   // the merge's output (merge_csc_stage), swapped with src
   uint64_t cap_alt = 0;
   uint32_t* ptr = nullptr;       // n+1
   uint32_t* deg_out = nullptr;   // n: distinct out-degree (stored edges)
@@ -65,6 +65,10 @@ struct Csc {
   uint64_t E = 0;
   uint64_t cap = 0;
   uint64_t built_version = ~0ULL;
+  // A build or merge in flight on the context's stream writes its bin sizes here (pinned)
+  // and sets `pending`; csc_settle waits for it and takes nb and the bin layout from them.
+  uint32_t* htot = nullptr;
+  bool pending = false;
 };
 
 struct PrState {
@@ -192,18 +196,18 @@ __global__ void csc_delta_keys_kernel(const uint32_t* __restrict__ nloc, const u
   }
 }
 
-// Per target: the new keys it receives (cnt), and each new key's source gains an
-// out-edge (deg_out, one atomic per source and warp).
+// Per target: the new keys it receives (cnt; the keys are sorted by target, so a warp
+// adds each target's run with one atomic), and each new key's source gains an out-edge.
 __global__ void csc_delta_count_kernel(const uint64_t* __restrict__ keys, uint64_t kept, uint32_t lg_n,
                                        uint32_t* __restrict__ cnt, uint32_t* __restrict__ deg_out) {
   const uint64_t mask = (1ULL << lg_n) - 1ULL;
   uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < kept; i += stride) {
     const uint64_t k = keys[i];
-    atomicAdd(&cnt[k >> lg_n], 1u);
-    const uint32_t u = (uint32_t)(k & mask);
-    const unsigned m = __match_any_sync(__activemask(), u);
-    if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) atomicAdd(&deg_out[u], (unsigned)__popc(m));
+    const uint32_t t = (uint32_t)(k >> lg_n);
+    const unsigned m = __match_any_sync(__activemask(), t);
+    if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) atomicAdd(&cnt[t], (unsigned)__popc(m));
+    atomicAdd(&deg_out[(uint32_t)(k & mask)], 1u);
   }
 }
 
@@ -214,58 +218,72 @@ __global__ void csc_new_ptr_kernel(const uint32_t* __restrict__ ptr, const uint3
   for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v <= n; v += stride) np[v] = ptr[v] + dx[v];
 }
 
-// Every target's old in-edges [ptr[v], ptr[v+1]) and new ones (sorted keys
-// [dx[v], dx[v+1])) written ascending by source at ptr[v] + dx[v] of nsrc: an entry's
-// place is its index in its own list plus the number of the other list's sources below
-// it (the lists share no source: the store keeps every edge once). Targets are taken by
-// the old bin layout, pr_bin_vw(k) lanes each (a whole block for the largest bin).
-__global__ void __launch_bounds__(PR_T) csc_merge_kernel(const PrBinLaunch* __restrict__ blp,
-                                                         const uint32_t* __restrict__ bins,
-                                                         const uint32_t* __restrict__ ptr,
-                                                         const uint32_t* __restrict__ src,
-                                                         const uint64_t* __restrict__ keys,
-                                                         const uint32_t* __restrict__ dx, uint32_t lg_n,
-                                                         uint32_t* __restrict__ nsrc) {
+// New keys: key j of target t lands at ptr[t] + j plus the number of t's old in-edges
+// with a smaller source (ptr[t] + dx[t] + (j - dx[t]) + that count); at[j] = ptr[t] + that
+// count, the old edge the key is placed before. The keys are sorted by (target, source),
+// so at[] ascends.
+__global__ void csc_merge_new_kernel(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ src,
+                                     const uint64_t* __restrict__ keys, uint64_t kept, uint32_t lg_n,
+                                     uint32_t* __restrict__ nsrc, uint32_t* __restrict__ at) {
   const uint64_t mask = (1ULL << lg_n) - 1ULL;
-  const uint32_t total = blp->blocks;
-  for (uint32_t vb = blockIdx.x; vb < total; vb += gridDim.x) {
-    int k = 0;
-    while (k < kPrBins && !(vb >= blp->first[k] && vb - blp->first[k] < blp->nblk[k])) ++k;
-    if (k == kPrBins) continue;
-    const uint64_t bid = vb - blp->first[k], nblk = blp->nblk[k];
-    const uint64_t off = blp->off[k], cnt = blp->count[k];
-    const unsigned G = pr_bin_vw(k) == 0 ? blockDim.x : (unsigned)pr_bin_vw(k);
-    const uint64_t gpb = blockDim.x / G;
-    const unsigned gl = threadIdx.x % G;
-    for (uint64_t i = bid * gpb + threadIdx.x / G; i < cnt; i += nblk * gpb) {
-      const uint32_t v = bins[off + i];
-      const uint32_t olo = ptr[v], ohi = ptr[v + 1], dlo = dx[v], dhi = dx[v + 1];
-      const uint32_t out = olo + dlo;
-      if (dlo == dhi) {
-        for (uint32_t e = olo + gl; e < ohi; e += G) nsrc[out + (e - olo)] = src[e];
-        continue;
-      }
-      for (uint32_t e = olo + gl; e < ohi; e += G) {
-        const uint32_t sv = src[e];
-        uint32_t a = dlo, b = dhi;
-        while (a < b) {
-          const uint32_t m = (a + b) >> 1;
-          if ((uint32_t)(keys[m] & mask) < sv) a = m + 1;
-          else b = m;
-        }
-        nsrc[out + (e - olo) + (a - dlo)] = sv;
-      }
-      for (uint32_t j = dlo + gl; j < dhi; j += G) {
-        const uint32_t sv = (uint32_t)(keys[j] & mask);
-        uint32_t a = olo, b = ohi;
-        while (a < b) {
-          const uint32_t m = (a + b) >> 1;
-          if (src[m] < sv) a = m + 1;
-          else b = m;
-        }
-        nsrc[out + (j - dlo) + (a - olo)] = sv;
-      }
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < kept; j += stride) {
+    const uint64_t k = keys[j];
+    const uint32_t t = (uint32_t)(k >> lg_n), sv = (uint32_t)(k & mask);
+    uint32_t a = ptr[t], b = ptr[t + 1];
+    while (a < b) {
+      const uint32_t m = (a + b) >> 1;
+      if (src[m] < sv) a = m + 1;
+      else b = m;
     }
+    nsrc[(uint64_t)a + j] = sv;
+    at[j] = a;
+  }
+}
+
+// The old edges move in blocks of CSC_MB; jb[b] = the new keys placed before block b's
+// first edge (at[j] < b * CSC_MB).
+constexpr uint32_t CSC_MB = 2048;
+__global__ void csc_block_keys_kernel(const uint32_t* __restrict__ at, uint64_t kept, uint32_t nblk,
+                                      uint32_t* __restrict__ jb) {
+  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b > nblk) return;
+  const uint64_t e = (uint64_t)b * CSC_MB;
+  uint64_t lo = 0, hi = kept;
+  while (lo < hi) {
+    const uint64_t m = (lo + hi) >> 1;
+    if ((uint64_t)at[m] < e) lo = m + 1;
+    else hi = m;
+  }
+  jb[b] = (uint32_t)lo;
+}
+
+// Old edge e moves up by the new keys placed at or before it: jb[b] plus those of the
+// block's keys with at <= e, counted by a search of the block's at[] (staged in shared
+// memory when it fits). Consecutive threads take consecutive edges.
+__global__ void __launch_bounds__(256) csc_merge_old_kernel(const uint32_t* __restrict__ src, uint64_t E,
+                                                            const uint32_t* __restrict__ at,
+                                                            const uint32_t* __restrict__ jb,
+                                                            uint32_t* __restrict__ nsrc) {
+  __shared__ uint32_t s_at[CSC_MB];
+  const uint64_t base = (uint64_t)blockIdx.x * CSC_MB;
+  const uint32_t jlo = jb[blockIdx.x], jhi = jb[blockIdx.x + 1];
+  const uint32_t nk = jhi - jlo;
+  const bool staged = nk <= CSC_MB;
+  if (staged)
+    for (uint32_t i = threadIdx.x; i < nk; i += blockDim.x) s_at[i] = at[jlo + i];
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < CSC_MB; i += blockDim.x) {
+    const uint64_t e = base + i;
+    if (e >= E) break;
+    uint32_t a = 0, b = nk;  // keys of the block with at <= e
+    while (a < b) {
+      const uint32_t m = (a + b) >> 1;
+      const uint32_t v = staged ? s_at[m] : at[jlo + m];
+      if ((uint64_t)v <= e) a = m + 1;
+      else b = m;
+    }
+    nsrc[e + jlo + a] = src[e];
   }
 }
 
@@ -286,7 +304,9 @@ static uint64_t store_version(Ctx* c) { return c->version; }
 static int pr_ensure_perm(Ctx* c);
 static PrBinLaunch bin_launch(Ctx* c, const uint64_t* nb);
 
-static int build_csx(Ctx* c, Csc& q, int by_source, float** w, uint64_t* wcap) {
+static int csc_settle(Ctx* c, Csc& q);
+
+static int build_csx_stage(Ctx* c, Csc& q, int by_source, float** w, uint64_t* wcap) {
   int prc = pr_ensure_perm(c);
   if (prc) return prc;
   const uint64_t n = c->n, E = c->E;
@@ -308,6 +328,9 @@ static int build_csx(Ctx* c, Csc& q, int by_source, float** w, uint64_t* wcap) {
         cy_malloc(&q.bins, n * 4) != cudaSuccess)
       return set_err(c, CYTOM_ERR_OOM, "CSC index");
   }
+  if ((!q.htot && cy_malloc_host(&q.htot, 64) != cudaSuccess) ||
+      (!q.dbl && cy_malloc(&q.dbl, sizeof(PrBinLaunch)) != cudaSuccess))
+    return set_err(c, CYTOM_ERR_OOM, "CSC bins");
   char* tmp = nullptr;
   const size_t kbytes = std::max<uint64_t>(std::max<uint64_t>(E, n), 1) * 8;
   const size_t vbytes = w ? std::max<uint64_t>(E, 1) * 4 : 0;
@@ -346,25 +369,36 @@ static int build_csx(Ctx* c, Csc& q, int by_source, float** w, uint64_t* wcap) {
   rc = radix_sort_pairs(c, k0, k1, seg_lo, q.bins, n, 3, &balt);
   if (rc) return rc;
   if (!balt) cudaMemcpyAsync(q.bins, seg_lo, nbytes, cudaMemcpyDeviceToDevice, c->stream);
-  uint32_t ht[kPrBins];
-  cudaMemcpyAsync(ht, tot, sizeof(ht), cudaMemcpyDeviceToHost, c->stream);
+  cudaMemcpyAsync(q.htot, tot, kPrBins * 4, cudaMemcpyDeviceToHost, c->stream);
   cudaFreeAsync(tmp, c->stream);
+  q.E = E;
+  q.pending = true;
+  return cuda_err(c, cudaGetLastError(), "CSC build");
+}
+
+// Waits for the build or merge in flight (if any) and installs its bin sizes and layout.
+static int csc_settle(Ctx* c, Csc& q) {
+  if (!q.pending) return CYTOM_OK;
   cudaError_t e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_err(c, e, "CSC build");
-  for (int k = 0; k < kPrBins; ++k) q.nb[k] = ht[k];
-  q.E = E;
-  if (!q.dbl && cy_malloc(&q.dbl, sizeof(PrBinLaunch)) != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "CSC bins");
+  q.pending = false;
+  for (int k = 0; k < kPrBins; ++k) q.nb[k] = q.htot[k];
   const PrBinLaunch hb = bin_launch(c, q.nb);
   // pageable source: the call returns once the bytes are staged
   e = cudaMemcpyAsync(q.dbl, &hb, sizeof(hb), cudaMemcpyHostToDevice, c->stream);
   return e == cudaSuccess ? CYTOM_OK : cuda_err(c, e, "CSC bins");
 }
 
-static int build_csc(Ctx* c, Csc& q) { return build_csx(c, q, 0, nullptr, nullptr); }
+static int build_csx(Ctx* c, Csc& q, int by_source, float** w, uint64_t* wcap) {
+  int rc = build_csx_stage(c, q, by_source, w, wcap);
+  return rc ? rc : csc_settle(c, q);
+}
+
+static int build_csc_stage(Ctx* c, Csc& q) { return build_csx_stage(c, q, 0, nullptr, nullptr); }
 
 // Called by the compaction once it knows its kept edges (nloc / ntile, `kept` of them):
 // while the context's CSC matches the store before this compaction, the edges are saved
-// as CSC keys for merge_csc. Without room for them the next build re-sorts.
+// as CSC keys for merge_csc_stage. Without room for them the next build re-sorts.
 int pagerank_note_kept(Ctx* c, const uint32_t* nloc, const uint32_t* ntile, uint64_t kept) {
   c->pr_delta_version = ~0ULL;
   const Csc* q = reinterpret_cast<const Csc*>(c->pr_csc);
@@ -393,12 +427,12 @@ int pagerank_note_kept(Ctx* c, const uint32_t* nloc, const uint32_t* ntile, uint
 }
 
 // The CSC after one compaction that only added edges: the saved keys sorted, counted
-// per target and merged into the old segments (csc_merge_kernel) -- the same CSC,
+// per target and merged into the old segments (csc_merge_old_kernel, csc_merge_new_kernel) -- the same CSC,
 // offsets, out-degrees and bins a full build of the new store gives, without re-sorting
 // the old edges.
-static int merge_csc(Ctx* c, Csc& q) {
+static int merge_csc_stage(Ctx* c, Csc& q) {
   const uint64_t n = c->n, K = c->pr_delta_count, E = q.E + K;
-  if (E != c->E || E > 0xFFFFFFFFULL - (1ULL << 20)) return build_csc(c, q);
+  if (E != c->E || E > 0xFFFFFFFFULL - (1ULL << 20)) return build_csc_stage(c, q);
   uint32_t lg_n = 0;
   while ((1ULL << lg_n) < n) ++lg_n;
   if (E > q.cap_alt || !q.src_alt) {
@@ -408,13 +442,14 @@ static int merge_csc(Ctx* c, Csc& q) {
     const uint64_t cap = std::max<uint64_t>(E + E / 4, 1024);
     if (cy_malloc(&q.src_alt, cap * 4) != cudaSuccess) {
       cudaGetLastError();
-      return build_csc(c, q);
+      return build_csc_stage(c, q);
     }
     q.cap_alt = cap;
   }
   const size_t kb = std::max<uint64_t>(K, 1) * 8, nb8 = std::max<uint64_t>(n, 1) * 8, n4 = (n + 1) * 4;
+  const size_t ab = std::max<uint64_t>(K, 1) * 4 + ((q.E + CSC_MB - 1) / CSC_MB + 2) * 4;
   char* tmp = nullptr;
-  if (cy_malloc_async((void**)&tmp, kb + 2 * nb8 + 4 * n4 + 64, c->stream) != cudaSuccess)
+  if (cy_malloc_async((void**)&tmp, kb + 2 * nb8 + 4 * n4 + 64 + ab, c->stream) != cudaSuccess)
     return set_err(c, CYTOM_ERR_OOM, "CSC merge temporaries");
   uint64_t* kalt = (uint64_t*)tmp;
   uint64_t* bk0 = (uint64_t*)(tmp + kb);
@@ -424,6 +459,8 @@ static int merge_csc(Ctx* c, Csc& q) {
   uint32_t* np = dx + (n + 1);
   uint32_t* vid = np + (n + 1);
   uint32_t* tot = vid + (n + 1);
+  uint32_t* at = tot + 16;  // the old edge each new key is placed before
+  uint32_t* jb = at + std::max<uint64_t>(K, 1);  // new keys before each block of the merge
   bool alt = false;
   int rc = radix_sort_pairs(c, c->pr_delta_keys, kalt, nullptr, nullptr, K, (int)(2 * lg_n), &alt);
   if (rc) return rc;
@@ -437,10 +474,12 @@ static int merge_csc(Ctx* c, Csc& q) {
   rc = exclusive_scan_u32(c, cnt, dx, n, dx + n);
   if (rc) return rc;
   csc_new_ptr_kernel<<<grid_n(c, n + 1), 256, 0, c->stream>>>(q.ptr, dx, n, np);
-  const PrBinLaunch old_bl = bin_launch(c, q.nb);
-  csc_merge_kernel<<<std::max<uint32_t>(1, std::min<uint32_t>(old_bl.blocks, (uint32_t)c->num_sms * 8)), PR_T, 0,
-                     c->stream>>>(q.dbl, q.bins, q.ptr, q.src, keys, dx, lg_n, q.src_alt);
-  c->launches += 2;
+  const uint64_t Eo = q.E;
+  const uint32_t mblk = (uint32_t)((Eo + CSC_MB - 1) / CSC_MB);
+  if (K) csc_merge_new_kernel<<<grid_n(c, K), 256, 0, c->stream>>>(q.ptr, q.src, keys, K, lg_n, q.src_alt, at);
+  csc_block_keys_kernel<<<(mblk + 1 + 255) / 256, 256, 0, c->stream>>>(at, K, mblk, jb);
+  if (mblk) csc_merge_old_kernel<<<mblk, 256, 0, c->stream>>>(q.src, Eo, at, jb, q.src_alt);
+  c->launches += 4;
   // bins of the new in-degrees, as build_csx makes them
   csc_cnt_bins_kernel<<<grid_n(c, n), 256, 0, c->stream>>>(np, np + 1, n, cnt, bk0, vid, tot);
   c->launches++;
@@ -449,28 +488,45 @@ static int merge_csc(Ctx* c, Csc& q) {
   if (rc) return rc;
   if (!balt) cudaMemcpyAsync(q.bins, vid, n * 4, cudaMemcpyDeviceToDevice, c->stream);
   cudaMemcpyAsync(q.ptr, np, n4, cudaMemcpyDeviceToDevice, c->stream);
-  uint32_t ht[kPrBins];
-  cudaMemcpyAsync(ht, tot, sizeof(ht), cudaMemcpyDeviceToHost, c->stream);
+  cudaMemcpyAsync(q.htot, tot, kPrBins * 4, cudaMemcpyDeviceToHost, c->stream);
   cudaFreeAsync(tmp, c->stream);
-  cudaError_t e = cudaStreamSynchronize(c->stream);
-  if (e != cudaSuccess) return cuda_err(c, e, "CSC merge");
-  std::swap(q.src, q.src_alt);
+  std::swap(q.src, q.src_alt);  // later work on the stream reads the merged array
   std::swap(q.cap, q.cap_alt);
-  for (int k = 0; k < kPrBins; ++k) q.nb[k] = ht[k];
   q.E = E;
-  const PrBinLaunch hb = bin_launch(c, q.nb);
-  // pageable source: the call returns once the bytes are staged
-  e = cudaMemcpyAsync(q.dbl, &hb, sizeof(hb), cudaMemcpyHostToDevice, c->stream);
-  return e == cudaSuccess ? CYTOM_OK : cuda_err(c, e, "CSC bins");
+  q.pending = true;
+  return cuda_err(c, cudaGetLastError(), "CSC merge");
 }
 
-// The CSC for the current store: merged from the previous one when exactly one
-// compaction (that saved its kept edges) lies between them, rebuilt otherwise.
-static int update_csc(Ctx* c, Csc& q) {
+constexpr uint64_t kCscMergeMinEdges = 1ULL << 21;
+
+// The CSC for the current store, enqueued on the context's stream: merged from the
+// previous one when exactly one compaction (that saved its kept edges) lies between
+// them, rebuilt otherwise. csc_settle completes it.
+static int update_csc_stage(Ctx* c, Csc& q) {
+  int rc = csc_settle(c, q);  // the merge reads the previous bins
+  if (rc) return rc;
+  // below about 2 M edges a full sort is as fast as the merge's extra passes (RMAT-16
+  // PageRank-delta stream: 1.30 ms per update with full builds, 1.37 with merges)
   if (q.src && q.dbl && q.built_version != ~0ULL && q.built_version + 1 == c->version &&
-      c->pr_delta_version == c->version)
-    return merge_csc(c, q);
-  return build_csc(c, q);
+      c->pr_delta_version == c->version && q.E >= kCscMergeMinEdges)
+    rc = merge_csc_stage(c, q);
+  else
+    rc = build_csc_stage(c, q);
+  if (!rc) q.built_version = c->version;
+  return rc;
+}
+
+static int update_csc(Ctx* c, Csc& q) {
+  int rc = q.built_version == c->version ? CYTOM_OK : update_csc_stage(c, q);
+  return rc ? rc : csc_settle(c, q);
+}
+
+// The batched executor enqueues every snapshot's CSC update before it waits for any, so
+// the updates of several contexts run side by side.
+int pagerank_csc_stage(Ctx* c) {
+  Csc* q = reinterpret_cast<Csc*>(c->pr_csc);
+  if (!q || q->built_version == c->version) return CYTOM_OK;
+  return update_csc_stage(c, *q);
 }
 
 // ---- renumbering by out-degree ---------------------------------------------------
@@ -735,6 +791,7 @@ static void csc_free(Csc* q) {
   void* ptrs[] = {q->src, q->src_alt, q->ptr, q->deg_out, q->bins, q->dbl};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  if (q->htot) cudaFreeHost(q->htot);
 }
 
 static WGraph* ctx_wgraph(Ctx* c) {
@@ -1046,10 +1103,9 @@ int pagerank_run(Ctx* c, Job* j) {
   if (j->algo == CYTOM_ALGO_WPAGERANK) return wpagerank_run(c, j);
   PrState* s = prs(j);
   const uint64_t ver = store_version(c);
-  if (s->csc->built_version != ver) {
+  {
     int rc = update_csc(c, *s->csc);
     if (rc) return rc;
-    s->csc->built_version = ver;
   }
   if (s->seen_version != ver) {
     s->need_residual = true;
@@ -1109,10 +1165,9 @@ int pagerank_batch_prep(Ctx* c, Job* j, PrArgs* out, uint64_t* nb, int* first_mo
     return set_err(c, CYTOM_ERR_UNIMPLEMENTED, "weighted PageRank runs through cytom_run only");
   PrState* s = prs(j);
   const uint64_t ver = store_version(c);
-  if (s->csc->built_version != ver) {
+  {
     int rc = update_csc(c, *s->csc);
     if (rc) return rc;
-    s->csc->built_version = ver;
   }
   s->seen_version = ver;
   const uint64_t n = c->n;

@@ -94,14 +94,14 @@ def test_pagerank_normalised(cg, orc, kahan):
 @pytest.mark.parametrize("kahan", [True, False])
 def test_incremental_csc_matches_full_build(cg, orc, kahan):
     # A context whose PageRank job runs after every batch merges the compaction's kept
-    # edges into its CSC (no re-sort); a context that runs PageRank only at the end sorts
-    # once. Fresh jobs on the two end in the same round with the same ranks up to the
+    # edges into its CSC (no re-sort) once the CSC holds 2 M edges; a context that runs
+    # PageRank only at the end sorts once. Fresh jobs on the two end in the same round with the same ranks up to the
     # order of the FP64 dangling-mass atomics (a wrong or missing in-edge moves its
     # target's rank by far more) -- after six batches with duplicates (within and across
     # batches), after a deletion (a full rebuild on both) and after one more batch merged
     # on top of the rebuilt CSC -- and the FP32 form stays within the tolerance of the
     # FP64 oracle.
-    scale, vpt = 13, 1024
+    scale, vpt = 17, 4096
     n = 1 << scale
     st = orc.Store(n, vpt)
 
@@ -120,7 +120,7 @@ def test_incremental_csc_matches_full_build(cg, orc, kahan):
     with cg.Engine(n, vpt) as ea, cg.Engine(n, vpt) as eb, cg.Engine(n, vpt) as ec:
         pa = cg.PageRank(ea, max_iterations=300, tolerance=1e-10, kahan=kahan)
         for b in range(6):
-            s, t = orc.rmat(scale, b * 2 * n, 2 * n, 77)
+            s, t = orc.rmat(scale, b * 4 * n, 4 * n, 77)  # past 2 M stored edges after the fifth
             s = np.concatenate([s, s[:100]])  # duplicates inside the batch
             t = np.concatenate([t, t[:100]])
             for e in (ea, eb, ec):
@@ -138,7 +138,7 @@ def test_incremental_csc_matches_full_build(cg, orc, kahan):
             e.delete_edges(ds.copy(), dt.copy())
         pa.execute_algorithm()
         fresh_pair(ea, eb)
-        s, t = orc.rmat(scale, 12 * n, 2 * n, 78)
+        s, t = orc.rmat(scale, 24 * n, 4 * n, 78)
         for e in (ea, eb, ec):
             e.insert_edges(s.copy(), t.copy())
             e.do_global_compaction()

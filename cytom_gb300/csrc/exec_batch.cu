@@ -349,7 +349,7 @@ __device__ __forceinline__ void pr_lane_sum_pair(const PrArgs& a, const pr_pair_
 #pragma unroll
   for (int k = 0; k < B; ++k) {
     const uint32_t e = e0 + (uint32_t)k * stride;
-    id[k] = e < hi ? a.csc_src[e] : 0u;
+    id[k] = e < hi ? __ldcs(a.csc_src + e) : 0u;  // streamed: keep L1 for the gathered contributions
   }
   for (uint32_t e = e0; e < hi; e += (uint32_t)B * stride) {
     pr_pair_t<MODE> c[B];
@@ -367,7 +367,7 @@ __device__ __forceinline__ void pr_lane_sum_pair(const PrArgs& a, const pr_pair_
 #pragma unroll
     for (int k = 0; k < B; ++k) {
       const uint32_t ek = en + (uint32_t)k * stride;
-      id[k] = ek < hi ? a.csc_src[ek] : 0u;
+      id[k] = ek < hi ? __ldcs(a.csc_src + ek) : 0u;
     }
 #pragma unroll
     for (int k = 0; k < B; ++k)

@@ -694,18 +694,10 @@ __device__ __forceinline__ void pr_round_end(LoopState* ls, int mode, cudaGraphC
 
 // Every block takes part in the round end of the fused forms, whether or not the run
 // still continues (a captured loop's condition is only set here).
+// The virtual blocks of the bin layout from blockIdx.x on, gridDim.x apart.
 template <int MODE>
-__global__ void __launch_bounds__(PR_T) pr_pull_kernel(PrArgs a, const PrBinLaunch* __restrict__ blp,
-                                                       cudaGraphConditionalHandle h, int use_handle) {
-  LoopState* ls = a.ls;
-  const bool live = ls->cont != 0;
-  if (!live && !pr_fused<MODE>()) return;
-  const unsigned p = ls->iter & 1u;
-  PrTally t;
-  t.init();
-  const uint32_t total = live ? blp->blocks : 0u;
-  const pr_ff_t<MODE> dang = pr_dang_arg<MODE, false>(a, ls, p);
-  const pr_val_t<MODE>* cr = pr_cread<MODE>(a, p);
+__device__ __forceinline__ void pull_vblocks(PrArgs& a, const pr_val_t<MODE>* cr, unsigned p, pr_ff_t<MODE> dang,
+                                             const PrBinLaunch* __restrict__ blp, uint32_t total, PrTally& t) {
   for (uint32_t vb = blockIdx.x; vb < total; vb += gridDim.x) {
     int k = 0;
     while (k < kPrBins && !(vb >= blp->first[k] && vb - blp->first[k] < blp->nblk[k])) ++k;
@@ -721,9 +713,26 @@ __global__ void __launch_bounds__(PR_T) pr_pull_kernel(PrArgs a, const PrBinLaun
       default: pull_large_body<MODE>(a, cr, p, dang, bid, nblk, t);
     }
   }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(PR_T) pr_pull_kernel(PrArgs a, const PrBinLaunch* __restrict__ blp,
+                                                       cudaGraphConditionalHandle h, int use_handle) {
+  LoopState* ls = a.ls;
+  const bool live = ls->cont != 0;
+  if (!live && !pr_fused<MODE>()) return;
+  const unsigned p = ls->iter & 1u;
+  PrTally t;
+  t.init();
+  const uint32_t total = live ? blp->blocks : 0u;
+  const pr_ff_t<MODE> dang = pr_dang_arg<MODE, false>(a, ls, p);
+  const pr_val_t<MODE>* cr = pr_cread<MODE>(a, p);
+  pull_vblocks<MODE>(a, cr, p, dang, blp, total, t);
   if (live) pr_tally_flush<MODE>(ls, p, t);
   if constexpr (pr_fused<MODE>()) pr_round_end(ls, MODE, h, use_handle);
 }
+
+
 
 // The control step as its own launch (the forms without a fused round end).
 __global__ void pr_control_kernel(LoopState* ls, int mode, cudaGraphConditionalHandle h, int use_handle) {

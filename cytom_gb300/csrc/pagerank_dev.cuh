@@ -567,31 +567,31 @@ __device__ __forceinline__ pr_ff_t<MODE> pr_sum_group(const PrArgs& a, const pr_
   }
 }
 
-// The same by a block of PR_BLOCK_T threads (in-degree > 4096: RMAT hubs); thread 0
+// The same by a whole block (in-degree > 4096: RMAT hubs; up to 1024 threads); thread 0
 // returns the sum. Every thread of the block calls it.
 template <int MODE, bool PERSIST>
 __device__ __forceinline__ pr_ff_t<MODE> pr_sum_block(const PrArgs& a, const pr_val_t<MODE>* cr, uint32_t v) {
-  __shared__ float s_s[PR_BLOCK_T / 32], s_e[PR_BLOCK_T / 32];
-  __shared__ double s_d[PR_BLOCK_T / 32];
-  const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __shared__ float s_s[32], s_e[32];
+  __shared__ double s_d[32];
+  const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const uint32_t lo = a.csc_ptr[v], hi = a.csc_ptr[v + 1];
   pr_ff_t<MODE> sum{};
   if constexpr (pr_is64<MODE>()) {
     Acc64 acc;
     acc.init();
-    pr_lane_sum<MODE, PERSIST, 4>(a, cr, lo + threadIdx.x, hi, PR_BLOCK_T, acc);
+    pr_lane_sum<MODE, PERSIST, 4>(a, cr, lo + threadIdx.x, hi, blockDim.x, acc);
     double s = acc.s;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
     if (lane == 0) s_d[wid] = s;
     __syncthreads();
     if (threadIdx.x == 0) {
-      for (int k = 0; k < PR_BLOCK_T / 32; ++k) sum += s_d[k];
+      for (unsigned k = 0; k < nw; ++k) sum += s_d[k];
     }
   } else {
     Acc32 acc;
     acc.init();
-    pr_lane_sum<MODE, PERSIST, 4>(a, cr, lo + threadIdx.x, hi, PR_BLOCK_T, acc);
+    pr_lane_sum<MODE, PERSIST, 4>(a, cr, lo + threadIdx.x, hi, blockDim.x, acc);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       const float s2 = __shfl_xor_sync(0xFFFFFFFFu, acc.s, o);
@@ -606,7 +606,7 @@ __device__ __forceinline__ pr_ff_t<MODE> pr_sum_block(const PrArgs& a, const pr_
     if (threadIdx.x == 0) {
       Acc32 t;
       t.init();
-      for (int k = 0; k < PR_BLOCK_T / 32; ++k) t.merge(s_s[k], s_e[k]);
+      for (unsigned k = 0; k < nw; ++k) t.merge(s_s[k], s_e[k]);
       sum = pr_acc32_out<MODE>(t.s, t.e);
     }
   }

@@ -753,11 +753,11 @@ __device__ void run_unit(const BJob* J, unsigned phase, uint32_t unit, int prmod
   }
 }
 
-// Four blocks per SM (64 registers, a few hundred bytes spilled): the job rounds are
+// Five blocks per SM (48 registers, about 1.9 KB spilled per thread): the job rounds are
 // latency-bound gathers, and warps in flight matter more than the spills (64 jobs over
-// RMAT-14..21 snapshots: 29 ms device time per job round at two blocks per SM, 22.7
-// at three, 19.6 at four; five spill 1.4 KB per thread).
-__global__ void __launch_bounds__(BT, 4) batch_kernel(const BJob* __restrict__ jobs, BSched* sched, BCtl* ctl,
+// RMAT-14..21 snapshots, incremental job round: 10.9-11.3 ms device time at four blocks
+// per SM, 10.4-11.1 at five).
+__global__ void __launch_bounds__(BT, 5) batch_kernel(const BJob* __restrict__ jobs, BSched* sched, BCtl* ctl,
                                                         int njobs) {
   __shared__ int s_job, s_state, s_last, s_mode;
   __shared__ unsigned s_unit, s_total, s_phase;
@@ -1032,7 +1032,7 @@ static int batch_run(Ctx* const* ctxs, const int* job_ids, int count, cytom_run_
   if (e != cudaSuccess) return cuda_err(c0, e, "batch upload");
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, BT, 0);
-  per_sm = std::max(1, std::min(per_sm, 4));
+  per_sm = std::max(1, std::min(per_sm, 5));
   const int grid = c0->num_sms * per_sm;
   cudaEventRecord(bb->a, st);
   if (launch_left) {

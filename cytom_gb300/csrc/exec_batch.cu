@@ -36,8 +36,7 @@
 
 namespace cytom {
 
-int minprop_batch_prep(Ctx* c, Job* j);
-int pagerank_batch_prep(Ctx* c, Job* j, PrArgs* out, uint64_t* nb, int* first_mode);
+int pagerank_batch_prep(Ctx* c, Job* j, PrArgs* out, uint64_t* nb, int* first_mode, uint64_t* begin_edges);
 
 constexpr int BT = 256;  // threads of a batch block (every unit kind is written for 256)
 static_assert(BT == APPLY_T && BT == SG_T && BT == PR_BLOCK_T, "one block shape for every unit");
@@ -76,7 +75,11 @@ struct BJob {
   int algo;
   int adaptive;
   int paired;
-  int pad_bj;
+  unsigned begin;                  // batch_begin_kernel: 1 BFS / CC / SSSP reset, 2 PageRank reset, 0 none
+  unsigned max_iter;
+  unsigned pad_bj;
+  double tol;
+  unsigned long long begin_edges;  // PageRank: edges a round reads
 };
 
 struct __align__(128) BSched {
@@ -851,6 +854,24 @@ __global__ void __launch_bounds__(BT, 5) batch_kernel(const BJob* __restrict__ j
   if (threadIdx.x == 0 && done_units) atomicAdd(&ctl->units, done_units);
 }
 
+// Every job's loop state reset for its run, one block per job, in one launch: BFS / CC /
+// SSSP / SSWP clear both parities of their row flags; PageRank-delta jobs were reset by
+// their preparation (their rank sum follows the reset).
+__global__ void batch_begin_kernel(const BJob* __restrict__ jobs, int count) {
+  const int k = blockIdx.x;
+  if (k >= count) return;
+  const BJob& J = jobs[k];
+  if (J.begin == 1) {
+    const JobDesc* jd = J.jd;
+    const uint64_t T = J.sd->T;
+    uint32_t* rows = jd->rows;
+    for (uint64_t i = threadIdx.x; i < 2 * T; i += blockDim.x) rows[i] = 0;
+    if (threadIdx.x == 0) minprop_begin_state(jd->ls, J.max_iter);
+  } else if (J.begin == 2 && threadIdx.x == 0) {
+    pr_begin_state(J.ls, J.max_iter, J.tol, J.begin_edges);
+  }
+}
+
 // Copies every job's loop state into one array, read back with a single copy.
 __global__ void batch_stats_kernel(const BJob* __restrict__ jobs, int count, LoopState* __restrict__ out) {
   const int k = blockIdx.x;
@@ -908,6 +929,7 @@ static int batch_run(Ctx* const* ctxs, const int* job_ids, int count, cytom_run_
       return rc;
     }
   }
+
   std::vector<BJob> hj(count);
   std::vector<BSched> hs(count);
   for (int k = 0; k < count; ++k) {
@@ -926,11 +948,16 @@ static int batch_run(Ctx* const* ctxs, const int* job_ids, int count, cytom_run_
     b.algo = j->algo;
     b.adaptive = c->cfg.enable_adaptive_scheduling;
     memset(&hs[k], 0, sizeof(BSched));
+    b.max_iter = (unsigned)std::min<uint64_t>(j->params.max_iterations, 0xFFFFFFFFu);
+    b.tol = j->params.tolerance;
     if (is_pr(j->algo)) {
       uint64_t nb[kPrBins];
       int mode = 0;
-      rc = pagerank_batch_prep(c, j, &b.pr, nb, &mode);
+      uint64_t edges = 0;
+      rc = pagerank_batch_prep(c, j, &b.pr, nb, &mode, &edges);
       if (rc) return rc;
+      b.begin = j->algo == CYTOM_ALGO_PAGERANK ? 2u : 0u;
+      b.begin_edges = edges;
       for (int bi = 0; bi < kPrBins; ++bi) b.nb[bi] = nb[bi];
       hs[k].prmode = mode;
       const uint64_t units = (c->n + BU_PR_VERTS - 1) / BU_PR_VERTS;
@@ -938,8 +965,7 @@ static int batch_run(Ctx* const* ctxs, const int* job_ids, int count, cytom_run_
       hs[k].claim = (j->params.max_iterations > 0) ? pack_claim(PH_PR_CONTRIB, (unsigned)units)
                                                    : pack_claim(PH_DONE, 0);
     } else {
-      rc = minprop_batch_prep(c, j);
-      if (rc) return rc;
+      b.begin = 1;
       const uint64_t units = (((c->n + 31) >> 5) + BU_APPLY_WORDS - 1) / BU_APPLY_WORDS;
       const uint64_t stages = (c->E + SG_E - 1) / SG_E;
       if (units > kMaxUnits || stages > kMaxUnits)
@@ -1034,6 +1060,8 @@ static int batch_run(Ctx* const* ctxs, const int* job_ids, int count, cytom_run_
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, BT, 0);
   per_sm = std::max(1, std::min(per_sm, 5));
   const int grid = c0->num_sms * per_sm;
+  batch_begin_kernel<<<count, 256, 0, st>>>(bb->jobs, count);
+  c0->launches++;
   cudaEventRecord(bb->a, st);
   if (launch_left) {
     batch_kernel<<<grid, BT, 0, st>>>(bb->jobs, bb->sched, bb->ctl, count);

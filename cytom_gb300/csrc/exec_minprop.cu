@@ -43,22 +43,7 @@ __global__ void begin_kernel(const JobDesc* __restrict__ jd, const StoreDesc* __
   uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < 2 * T; i += stride)
     jd->rows[i] = 0;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    ls->iter = 0;
-    ls->max_iter = max_iter;
-    ls->cont = 1;
-    ls->err = 0;
-    ls->active[0] = ls->active[1] = 0;
-    ls->nact_words[0] = ls->nact_words[1] = 0;
-    ls->mode = 0;
-    ls->spq_count = 0;
-    ls->teps[0] = ls->teps[1] = 0;
-    ls->count_edges = 0;
-    ls->edges_scanned = 0;
-    ls->active_total = 0;
-    ls->apply_done = 0;
-    ls->sel_rounds = 0;
-  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) minprop_begin_state(ls, max_iter);
 }
 
 // Apply over every frontier word (apply_step), then the block's counters (apply_flush);
@@ -1252,15 +1237,6 @@ static double round_bytes(const Ctx* c, const LoopState& a, const LoopState& b, 
   if (a.mode == 0) bytes += (double)c->n / 8.0;
   else bytes += (double)a.nact_words[p] * (8.0 + 16.0 * (double)c->T);
   return bytes;
-}
-
-// Prepares a run of the batched executor: clears the loop state and the row flags
-// (the persistent kernel starts with the seeding apply).
-int minprop_batch_prep(Ctx* c, Job* j) {
-  unsigned max_iter = (unsigned)std::min<uint64_t>(j->params.max_iterations, 0xFFFFFFFFu);
-  begin_kernel<<<std::max(1, c->num_sms), 256, 0, c->stream>>>(j->d, c->dsd, max_iter);
-  c->launches++;
-  return cuda_err(c, cudaGetLastError(), "batch prep");
 }
 
 int minprop_run(Ctx* c, Job* j) {

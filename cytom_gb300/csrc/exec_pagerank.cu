@@ -764,27 +764,7 @@ __global__ void pr_rank_sum_kernel(const float* r, uint64_t n, LoopState* ls) {
   if ((threadIdx.x & 31) == 0 && s != 0.0) atomicAdd(&ls->base_sum, s);
 }
 __global__ void pr_begin_kernel(LoopState* ls, unsigned max_iter, double tol, unsigned long long edges) {
-  ls->iter = 0;
-  ls->sel_rounds = 0;
-  ls->apply_done = 0;
-  ls->max_iter = max_iter;
-  ls->cont = max_iter > 0 ? 1u : 0u;
-  ls->err = 0;
-  ls->active[0] = ls->active[1] = 0;
-  ls->teps[0] = edges;  // every round reads every stored edge once
-  ls->teps[1] = 0;
-  ls->count_edges = 0;
-  ls->edges_scanned = 0;
-  ls->active_total = 0;
-  ls->resid[0] = ls->resid[1] = 0.0;
-  ls->rank_sum[0] = ls->rank_sum[1] = 0.0;
-  ls->dangling[0] = ls->dangling[1] = 0.0;
-  ls->tol = tol;
-  ls->resid_final = 0.0;
-  ls->base_sum = 0.0;
-  ls->change_sum = 0.0;
-  ls->best_resid = 1.0e300;
-  ls->stall = 0;
+  pr_begin_state(ls, max_iter, tol, edges);
 }
 
 static PrState* prs(Job* j) { return reinterpret_cast<PrState*>(j->ext); }
@@ -1169,7 +1149,10 @@ int pagerank_run(Ctx* c, Job* j) {
 // Prepares a run of the batched executor: the snapshot's CSC, the loop state (and for
 // PageRank-delta the rank sum before the run), the round arguments, the bin sizes and
 // the mode of the first round.
-int pagerank_batch_prep(Ctx* c, Job* j, PrArgs* out, uint64_t* nb, int* first_mode) {
+// Prepares a PageRank-family job of the batched executor. A PAGERANK job's loop state is
+// reset by the batch's begin kernel (*begin_edges = the edges a round reads); a
+// PageRank-delta job's here, before its rank sum.
+int pagerank_batch_prep(Ctx* c, Job* j, PrArgs* out, uint64_t* nb, int* first_mode, uint64_t* begin_edges) {
   if (j->algo == CYTOM_ALGO_WPAGERANK)
     return set_err(c, CYTOM_ERR_UNIMPLEMENTED, "weighted PageRank runs through cytom_run only");
   PrState* s = prs(j);
@@ -1200,9 +1183,10 @@ int pagerank_batch_prep(Ctx* c, Job* j, PrArgs* out, uint64_t* nb, int* first_mo
   a.base = (1.0 - j->params.alpha) / (double)n;
   pr_args_ff(a);
   unsigned max_iter = (unsigned)std::min<uint64_t>(j->params.max_iterations, 0xFFFFFFFFu);
-  pr_begin_kernel<<<1, 1, 0, c->stream>>>(j->ls, max_iter, j->params.tolerance, (unsigned long long)s->csc->E);
-  c->launches++;
+  *begin_edges = s->csc->E;
   if (j->algo == CYTOM_ALGO_PR_DELTA) {
+    pr_begin_kernel<<<1, 1, 0, c->stream>>>(j->ls, max_iter, j->params.tolerance, (unsigned long long)s->csc->E);
+    c->launches++;
     int drc = pr_deg_mult(c);
     if (drc) return drc;
     a.deg = c->pr_deg_mult;

@@ -231,6 +231,24 @@ __device__ __forceinline__ unsigned control_step(const JobDesc* __restrict__ jd,
   return ls->cont;
 }
 
+// The loop state of a BFS / CC / SSSP / SSWP run before its first round (one thread).
+__device__ __forceinline__ void minprop_begin_state(LoopState* ls, unsigned max_iter) {
+  ls->iter = 0;
+  ls->max_iter = max_iter;
+  ls->cont = 1;
+  ls->err = 0;
+  ls->active[0] = ls->active[1] = 0;
+  ls->nact_words[0] = ls->nact_words[1] = 0;
+  ls->mode = 0;
+  ls->spq_count = 0;
+  ls->teps[0] = ls->teps[1] = 0;
+  ls->count_edges = 0;
+  ls->edges_scanned = 0;
+  ls->active_total = 0;
+  ls->apply_done = 0;
+  ls->sel_rounds = 0;
+}
+
 // ---- dense gather: one stage of SG_T * EPT edges ---------------------------
 // Processes stage `st` (EPT edges per thread, a multiple of 4) whose edges (and weights) are at eb / wb: shared memory for the
 // bulk-copy pipeline, global memory (FROM_GLOBAL, guarded loads) for the persistent

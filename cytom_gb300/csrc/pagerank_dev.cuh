@@ -614,6 +614,32 @@ __device__ __forceinline__ pr_ff_t<MODE> pr_sum_block(const PrArgs& a, const pr_
   return sum;
 }
 
+// The loop state of a PageRank-family run before its first round (one thread); every
+// round reads every stored edge once (teps[0] = edges).
+__device__ __forceinline__ void pr_begin_state(LoopState* ls, unsigned max_iter, double tol, unsigned long long edges) {
+  ls->iter = 0;
+  ls->sel_rounds = 0;
+  ls->apply_done = 0;
+  ls->max_iter = max_iter;
+  ls->cont = max_iter > 0 ? 1u : 0u;
+  ls->err = 0;
+  ls->active[0] = ls->active[1] = 0;
+  ls->teps[0] = edges;
+  ls->teps[1] = 0;
+  ls->count_edges = 0;
+  ls->edges_scanned = 0;
+  ls->active_total = 0;
+  ls->resid[0] = ls->resid[1] = 0.0;
+  ls->rank_sum[0] = ls->rank_sum[1] = 0.0;
+  ls->dangling[0] = ls->dangling[1] = 0.0;
+  ls->tol = tol;
+  ls->resid_final = 0.0;
+  ls->base_sum = 0.0;
+  ls->change_sum = 0.0;
+  ls->best_resid = 1.0e300;
+  ls->stall = 0;
+}
+
 // Ends a round: records the FP64 residual, decides whether to continue (one thread).
 // Every value the step reads is loaded from L2 up front (one round trip; the other
 // blocks' totals are complete and visible when it runs), then the new state is stored.

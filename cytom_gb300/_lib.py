@@ -34,7 +34,7 @@ class Config(C.Structure):
         ("edge_capacity_hint", C.c_uint64),
         ("stream", C.c_void_p),
         ("traversal", C.c_int32),
-        ("reserved", C.c_int32),
+        ("use_dynamic_compaction", C.c_int32),
     ]
 
 

@@ -544,7 +544,7 @@ int cytom_destroy(cytom_ctx* ctx) {
   void* ptrs[] = {c->dir, c->dir_alt, c->edges, c->wts, c->edges_alt, c->wts_alt, c->tile_ptr, c->tile_ptr_alt,
                   c->chunk_tile, c->chunk_tile_alt, c->app_keys, c->app_keys_alt, c->app_w, c->app_w_alt,
                   c->out_deg, c->in_deg, c->dsd, c->scratch, c->d_flag, c->xs_stage, c->xs_cum,
-                  c->xs_colcum, c->xs_tmp, c->pr_pair};
+                  c->xs_colcum, c->xs_tmp, c->pr_pair, c->dyn_pending, c->dyn_next};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->h_pinned) cudaFreeHost(c->h_pinned);
@@ -737,6 +737,12 @@ int cytom_clear(cytom_ctx* ctx) {
   if (e != cudaSuccess) return cuda_err(c, e, "clear");
   c->E = 0;
   c->A = 0;
+  if (c->dyn_pending) {  // dynamic compaction starts over: no appended edges, thresholds 4096
+    cudaFree(c->dyn_pending);
+    cudaFree(c->dyn_next);
+    c->dyn_pending = nullptr;
+    c->dyn_next = nullptr;
+  }
   c->version++;  // directory, PageRank structures and degree copies are rebuilt on use
   for (Job* j : c->jobs)
     if (j) j->fresh = true;

@@ -182,6 +182,11 @@ struct Ctx {
   uint64_t dir_entries = 0;
   uint64_t dir_version = ~0ULL;
   bool dir_disabled = false;
+  // dynamic compaction (cfg.use_dynamic_compaction): appended edges per tile since the
+  // last compaction and each tile's next threshold (4096, doubling)
+  uint32_t* dyn_pending = nullptr;
+  unsigned long long* dyn_next = nullptr;
+  uint64_t dyn_compactions = 0;
   uint64_t *app_keys = nullptr, *app_keys_alt = nullptr;
   uint32_t *app_w = nullptr, *app_w_alt = nullptr;
   uint64_t A = 0, app_cap = 0;

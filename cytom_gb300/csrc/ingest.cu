@@ -234,6 +234,69 @@ __global__ void append_kernel(const uint32_t* __restrict__ src, const uint32_t* 
   }
 }
 
+// ---- dynamic compaction (TileManager::insertEdge, tile-manager.h:117, 150-161) ----
+// Appended edges per tile (one atomic per tile and warp).
+__global__ void dyn_count_kernel(const uint64_t* __restrict__ keys, uint64_t count, uint32_t lvpt,
+                                 uint32_t* __restrict__ pending) {
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+    const uint32_t t = (uint32_t)(keys[i] >> (2 * lvpt));
+    const unsigned m = __match_any_sync(__activemask(), t);
+    if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) atomicAdd(&pending[t], (unsigned)__popc(m));
+  }
+}
+// A tile whose edges (stored + appended) reached its threshold raises the flag; the
+// threshold doubles past the count, as one doubling per crossing would leave it.
+__global__ void dyn_check_kernel(const unsigned long long* __restrict__ tile_ptr, const uint32_t* __restrict__ pending,
+                                 uint64_t ntiles, unsigned long long* __restrict__ next, unsigned* __restrict__ flag) {
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += stride) {
+    const unsigned long long total = (tile_ptr[t + 1] - tile_ptr[t]) + pending[t];
+    unsigned long long nx = next[t];
+    if (total >= nx) {
+      while (nx <= total) nx *= 2;
+      next[t] = nx;
+      atomicOr(flag, 1u);
+    }
+  }
+}
+__global__ void dyn_init_kernel(unsigned long long* __restrict__ next, uint64_t ntiles) {
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += stride) next[t] = 4096;
+}
+
+// After an insert with dynamic compaction on: counts the batch's edges per tile and
+// compacts the store when some tile reached its threshold.
+static int dynamic_compaction(Ctx* c, uint64_t first, uint64_t count) {
+  const uint64_t nt = c->ntiles;
+  if (!c->dyn_pending) {
+    if (cy_malloc(&c->dyn_pending, nt * 4) != cudaSuccess || cy_malloc(&c->dyn_next, nt * 8) != cudaSuccess) {
+      cudaGetLastError();
+      return set_err(c, CYTOM_ERR_OOM, "dynamic compaction counters");
+    }
+    cudaMemsetAsync(c->dyn_pending, 0, nt * 4, c->stream);
+    dyn_init_kernel<<<grid_for(c, nt, 256), 256, 0, c->stream>>>(c->dyn_next, nt);
+    c->launches++;
+    // edges appended before the counters existed
+    if (first) {
+      dyn_count_kernel<<<grid_for(c, first, 256), 256, 0, c->stream>>>(c->app_keys, first, c->lvpt, c->dyn_pending);
+      c->launches++;
+    }
+  }
+  dyn_count_kernel<<<grid_for(c, count, 256), 256, 0, c->stream>>>(c->app_keys + first, count, c->lvpt,
+                                                                    c->dyn_pending);
+  cudaMemsetAsync(c->d_flag, 0, sizeof(unsigned int), c->stream);
+  dyn_check_kernel<<<grid_for(c, nt, 256), 256, 0, c->stream>>>(c->tile_ptr, c->dyn_pending, nt, c->dyn_next,
+                                                                c->d_flag);
+  c->launches += 2;
+  cudaError_t e = cudaMemcpyAsync(c->h_pinned, c->d_flag, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "dynamic compaction check");
+  if (!*(unsigned int*)c->h_pinned) return CYTOM_OK;
+  c->dyn_compactions++;
+  return compact(c);
+}
+
 int insert_device(Ctx* c, const uint32_t* src, const uint32_t* tgt, const uint32_t* w,
                   uint64_t count) {
   if (count == 0) return CYTOM_OK;
@@ -265,6 +328,7 @@ int insert_device(Ctx* c, const uint32_t* src, const uint32_t* tgt, const uint32
   if (e != cudaSuccess) return cuda_err(c, e, "append_kernel");
   // the jobs are seeded by these edges when the compaction installs them
   c->A += count;
+  if (c->cfg.use_dynamic_compaction) return dynamic_compaction(c, c->A - count, count);
   return CYTOM_OK;
 }
 
@@ -958,6 +1022,7 @@ int compact(Ctx* c) {
     c->launches++;
   }
   cudaFreeAsync(tmp, c->stream);
+  if (c->dyn_pending) cudaMemsetAsync(c->dyn_pending, 0, c->ntiles * 4, c->stream);  // nothing appended now
   std::swap(c->edges, c->edges_alt);
   std::swap(c->wts, c->wts_alt);
   std::swap(c->tile_ptr, c->tile_ptr_alt);

@@ -72,7 +72,8 @@ class TileView:
 class Engine:
     def __init__(self, max_vertices: int, vertices_per_tile: int = 65536,
                  weight_type: int = L.UNWEIGHTED, adaptive_scheduling: bool = True,
-                 stream: int | None = None, lib=None, traversal: int = L.TRAVERSAL_ROW_FIRST):
+                 stream: int | None = None, lib=None, traversal: int = L.TRAVERSAL_ROW_FIRST,
+                 dynamic_compaction: bool = False):
         self.lib = lib or L.load()
         cfg = L.Config()
         self.lib.cytom_config_default(C.byref(cfg))
@@ -82,6 +83,7 @@ class Engine:
         cfg.enable_adaptive_scheduling = 1 if adaptive_scheduling else 0
         cfg.stream = stream
         cfg.traversal = traversal
+        cfg.use_dynamic_compaction = 1 if dynamic_compaction else 0
         h = C.c_void_p()
         rc = self.lib.cytom_create(C.byref(cfg), C.byref(h))
         if rc != L.CYTOM_OK:

@@ -97,7 +97,12 @@ typedef struct cytom_config {
   uint64_t edge_capacity_hint;   /* initial edge capacity; the store grows on demand */
   void* stream;                  /* cudaStream_t to run on; NULL = the context's own stream */
   int32_t traversal;             /* --traversal: CYTOM_TRAVERSAL_* (default row-first) */
-  int32_t reserved;
+  int32_t use_dynamic_compaction; /* --use-dynamic-compaction (default 0, src/scripts/config.py:95):
+                                     after an insert, when some tile holds at least its next
+                                     threshold of edges (stored + appended; 4096 at first,
+                                     doubling past each crossing, TileManager::insertEdge,
+                                     tile-manager.h:117, 150-161), the store compacts -- every
+                                     tile at once, one merge pass */
 } cytom_config;
 
 /* Fills *cfg with the reference defaults (src/scripts/config.py:45-109). */

@@ -180,3 +180,42 @@ def test_gpu_matches_reference_golden(cg, path):
             st = prog.execute_algorithm()
             assert np.array_equal(prog.result(), g[f"{name}_values"]), name
             assert st["count_edges"] == int(g[f"{name}_count_edges"]), name
+
+
+def test_dynamic_compaction(cg, orc):
+    # use_dynamic_compaction (TileManager::insertEdge, tile-manager.h:117, 150-161): after an
+    # insert, once some tile holds 4096 edges (then 8192, 16384, ...; stored + appended) the
+    # store compacts by itself. RMAT-12 over 4 x 4 tiles puts about a third of the edges in
+    # tile (0, 0), so 2,000-edge batches cross 4096 and 8192 there. The store then equals,
+    # tile for tile, one compacted only when asked, and so do the runs over it.
+    scale, vpt, nb, b = 12, 1024, 20, 2000
+    n = 1 << scale
+    s, t = orc.rmat(scale, 0, nb * b, 5)
+    w = orc.edge_weights(s, t, 9)
+    autos = 0
+    with cg.Engine(n, vpt, weight_type=cg.WEIGHT_U32, dynamic_compaction=True) as ea, \
+            cg.Engine(n, vpt, weight_type=cg.WEIGHT_U32) as eb:
+        for k in range(nb):
+            sl = slice(k * b, (k + 1) * b)
+            for e in (ea, eb):
+                e.insert_edges(s[sl].copy(), t[sl].copy(), w[sl].copy())
+            ca, pa = ea.count_edges()
+            cb, pb = eb.count_edges()
+            assert cb == 0 and pb == (k + 1) * b  # no compaction unless asked
+            if pa == 0:
+                autos += 1  # this insert compacted the store
+        assert autos >= 2, autos
+        for e in (ea, eb):
+            e.do_global_compaction()
+        ta, tb = ea.dump_tiles(weights=True), eb.dump_tiles(weights=True)
+        for x, y in zip(ta, tb):
+            assert np.array_equal(x, y)
+        st = orc.Store(n, vpt, True)
+        st.insert(s, t, w)
+        st.compact()
+        ot = st.dump()
+        assert np.array_equal(ta[0], ot[0]) and np.array_equal(ta[1], ot[1])
+        pa_, pb_ = cg.SSSP(ea, start_vertex=0, max_iterations=1000), cg.SSSP(eb, start_vertex=0, max_iterations=1000)
+        pa_.execute_algorithm()
+        pb_.execute_algorithm()
+        assert np.array_equal(pa_.result(), pb_.result())

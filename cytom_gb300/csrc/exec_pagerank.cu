@@ -463,7 +463,10 @@ static int merge_csc_stage(Ctx* c, Csc& q) {
   uint32_t* jb = at + std::max<uint64_t>(K, 1);  // new keys before each block of the merge
   bool alt = false;
   int rc = radix_sort_pairs(c, c->pr_delta_keys, kalt, nullptr, nullptr, K, (int)(2 * lg_n), &alt);
-  if (rc) return rc;
+  if (rc) {
+    cudaFreeAsync(tmp, c->stream);
+    return rc;
+  }
   const uint64_t* keys = alt ? kalt : c->pr_delta_keys;
   cudaMemsetAsync(cnt, 0, n4, c->stream);
   cudaMemsetAsync(tot, 0, 64, c->stream);
@@ -472,7 +475,10 @@ static int merge_csc_stage(Ctx* c, Csc& q) {
     c->launches++;
   }
   rc = exclusive_scan_u32(c, cnt, dx, n, dx + n);
-  if (rc) return rc;
+  if (rc) {
+    cudaFreeAsync(tmp, c->stream);
+    return rc;
+  }
   csc_new_ptr_kernel<<<grid_n(c, n + 1), 256, 0, c->stream>>>(q.ptr, dx, n, np);
   const uint64_t Eo = q.E;
   const uint32_t mblk = (uint32_t)((Eo + CSC_MB - 1) / CSC_MB);
@@ -485,7 +491,10 @@ static int merge_csc_stage(Ctx* c, Csc& q) {
   c->launches++;
   bool balt = false;
   rc = radix_sort_pairs(c, bk0, bk1, vid, q.bins, n, 3, &balt);
-  if (rc) return rc;
+  if (rc) {
+    cudaFreeAsync(tmp, c->stream);
+    return rc;
+  }
   if (!balt) cudaMemcpyAsync(q.bins, vid, n * 4, cudaMemcpyDeviceToDevice, c->stream);
   cudaMemcpyAsync(q.ptr, np, n4, cudaMemcpyDeviceToDevice, c->stream);
   cudaMemcpyAsync(q.htot, tot, kPrBins * 4, cudaMemcpyDeviceToHost, c->stream);

@@ -653,9 +653,7 @@ int cytom_insert_batch(cytom_ctx* ctx, const uint32_t* src, const uint32_t* tgt,
   if (!c || (count && (!src || !tgt))) return CYTOM_ERR_INVAL;
   if (count == 0) return CYTOM_OK;
   if (where == CYTOM_PTR_DEVICE) {
-    int rc = insert_device(c, src, tgt, w, count);
-    if (rc) return rc;
-    rc = cuda_err(c, cudaStreamSynchronize(c->stream), "insert");
+    int rc = insert_device(c, src, tgt, w, count);  // returns once the batch is appended
     if (rc) return rc;
     return edge_log_append(c, src, tgt, w, count, CYTOM_PTR_DEVICE);
   }
@@ -670,9 +668,7 @@ int cytom_insert_batch(cytom_ctx* ctx, const uint32_t* src, const uint32_t* tgt,
   cudaMemcpyAsync(ds, src, count * 4, cudaMemcpyHostToDevice, c->stream);
   cudaMemcpyAsync(dt, tgt, count * 4, cudaMemcpyHostToDevice, c->stream);
   if (dw) cudaMemcpyAsync(dw, w, count * 4, cudaMemcpyHostToDevice, c->stream);
-  int rc = insert_device(c, ds, dt, dw, count);
-  if (rc) return rc;
-  rc = cuda_err(c, cudaStreamSynchronize(c->stream), "insert");
+  int rc = insert_device(c, ds, dt, dw, count);  // returns once the batch is appended
   if (rc) return rc;
   return edge_log_append(c, src, tgt, w, count, CYTOM_PTR_HOST);
 }

@@ -212,11 +212,15 @@ __device__ __forceinline__ uint64_t make_key(uint32_t s, uint32_t t, uint32_t lv
 // Appends one batch to the append region and counts degrees. Degree increments
 // are warp-aggregated: lanes holding the same vertex elect one leader that adds
 // the group's size (RMAT hubs repeat often within a warp).
+// Appends the batch and counts its degrees -- unless validate_kernel, earlier on the same
+// stream, found an endpoint out of range: then the whole batch is rejected and nothing
+// is written, so the host reads the verdict once, after both kernels.
 __global__ void append_kernel(const uint32_t* __restrict__ src, const uint32_t* __restrict__ tgt,
                               const uint32_t* __restrict__ w, uint64_t count,
                               uint64_t* __restrict__ keys, uint32_t* __restrict__ kw,
                               uint32_t* __restrict__ out_deg, uint32_t* __restrict__ in_deg,
-                              uint32_t lvpt, uint32_t lT) {
+                              uint32_t lvpt, uint32_t lT, const unsigned int* __restrict__ bad) {
+  if (*bad) return;
   uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const unsigned lane = threadIdx.x & 31;
   for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < count; base += stride) {
@@ -304,28 +308,27 @@ int insert_device(Ctx* c, const uint32_t* src, const uint32_t* tgt, const uint32
     return set_err(c, CYTOM_ERR_INVAL, "weighted store needs a weight per edge");
   cudaError_t e = cudaMemsetAsync(c->d_flag, 0, sizeof(unsigned int), c->stream);
   if (e != cudaSuccess) return cuda_err(c, e, "memset");
+  int rc = ensure_app_capacity(c, c->A + count);
+  if (rc) return rc;
   int slot = prof_begin(c, KC_INSERT);
   validate_kernel<<<grid_for(c, count, 256), 256, 0, c->stream>>>(src, tgt, count, c->n, c->d_flag);
   c->launches++;
   prof_end(c, slot, (double)count * 8.0);
-  e = cudaMemcpyAsync(c->h_pinned, c->d_flag, sizeof(unsigned int), cudaMemcpyDeviceToHost,
-                      c->stream);
-  if (e != cudaSuccess) return cuda_err(c, e, "memcpy");
-  e = cudaStreamSynchronize(c->stream);
-  if (e != cudaSuccess) return cuda_err(c, e, "validate");
-  if (*(unsigned int*)c->h_pinned)
-    return set_err(c, CYTOM_ERR_RANGE, "edge endpoint >= vertex count; batch rejected");
-  int rc = ensure_app_capacity(c, c->A + count);
-  if (rc) return rc;
   const uint32_t* wuse = (c->wtype != CYTOM_UNWEIGHTED) ? w : nullptr;
   slot = prof_begin(c, KC_INSERT);
   append_kernel<<<grid_for(c, count, 256), 256, 0, c->stream>>>(
       src, tgt, wuse, count, c->app_keys + c->A, wuse ? c->app_w + c->A : nullptr, c->out_deg,
-      c->in_deg, c->lvpt, c->lT);
+      c->in_deg, c->lvpt, c->lT, c->d_flag);
   c->launches++;
   prof_end(c, slot, (double)count * (wuse ? 28.0 : 24.0));
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_err(c, e, "append_kernel");
+  // one wait: the batch's copies (host path), validation and append
+  e = cudaMemcpyAsync(c->h_pinned, c->d_flag, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "insert");
+  if (*(unsigned int*)c->h_pinned)
+    return set_err(c, CYTOM_ERR_RANGE, "edge endpoint >= vertex count; batch rejected");
   // the jobs are seeded by these edges when the compaction installs them
   c->A += count;
   if (c->cfg.use_dynamic_compaction) return dynamic_compaction(c, c->A - count, count);

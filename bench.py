@@ -60,8 +60,9 @@ def parse(argv=None):
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-workloads", action="store_true", help="headline stream only")
-    ap.add_argument("--profile-steps", type=int, default=16,
-                    help="batches at the end of the stream timed launch by launch for the roofline")
+    ap.add_argument("--profile-steps", type=int, default=63,
+                    help="batches at the end of the stream timed launch by launch for the roofline "
+                         "(default: every batch after the first)")
     ap.add_argument("--precision-scale", type=int, default=26)
     ap.add_argument("--profile-only", action="store_true",
                     help="run --batches batches once with every launch timed and its algorithmic bytes recorded "
@@ -267,7 +268,7 @@ def main(argv=None):
     # device-resident inputs of one stream (generated by the library's RMAT kernel)
     eng, progs = make_engine()
     total_edges_in = (args.preload + NB) * B
-    d_src = torch.empty(total_edges_in + args.profile_steps * B, dtype=torch.int32, device=dev)
+    d_src = torch.empty(total_edges_in, dtype=torch.int32, device=dev)
     d_tgt = torch.empty_like(d_src)
     d_w = torch.empty_like(d_src)
     with torch.cuda.stream(stream):

@@ -450,10 +450,13 @@ constexpr uint32_t SP_HEAVY = 256;
 constexpr uint32_t SP_CHUNK = 256;
 constexpr uint32_t SP_LIGHT = 32;
 constexpr uint32_t SP_WARP_MAX = 2048;
+// A light item longer than this is first narrowed to the edges of its word's active
+// sources (sp_narrow).
+constexpr uint32_t SP_NARROW = 16;
 constexpr int SP_ILP = 8;
 
 struct SpItem {
-  uint32_t x, y, bits, lo, hi;
+  uint32_t x, y, bits, lo, hi, b;  // b: the word's 32-source block in its tile row
   unsigned long long base;
 };
 
@@ -467,6 +470,7 @@ __device__ __forceinline__ SpItem sp_item(const JobDesc* __restrict__ jd, const 
   r.y = (uint32_t)(it & (T - 1));
   r.x = w >> lnbw;
   const uint32_t b = w & (nbw - 1);
+  r.b = b;
   r.bits = ld_state<PERSIST>(jd->fa + w);
   const uint64_t dbase = (((uint64_t)r.x << lT) + r.y) * (nbw + 1) + b;
   r.lo = sd->dir[dbase];
@@ -512,6 +516,36 @@ __device__ __forceinline__ void sp_batch(const JobDesc* __restrict__ jd, const S
   }
 }
 
+// Narrows item m to the edges whose sources lie between the lowest and the highest
+// active source of its word: an item's edges are sorted by (source, target) and packed
+// as source << 16 | target, so two lower-bound searches (run side by side) on
+// (source << 16) find the span. Sources outside it are inactive; their edges would only
+// be read and dropped.
+__device__ __forceinline__ void sp_narrow(const StoreDesc* __restrict__ sd, SpItem& m) {
+  const uint32_t smin = (m.b << 5) + (uint32_t)(__ffs(m.bits) - 1);
+  const uint32_t smax = (m.b << 5) + (31u - (uint32_t)__clz(m.bits));
+  const uint32_t klo = smin << 16;
+  const bool top = smax == 0xFFFFu;  // the tile's last source: the span runs to the end
+  const uint32_t khi = top ? 0u : (smax + 1u) << 16;
+  const uint32_t* e = sd->edges + m.base;
+  uint32_t a0 = m.lo, a1 = m.hi, c0 = m.lo, c1 = top ? m.lo : m.hi;
+  while (a0 < a1 || c0 < c1) {
+    const uint32_t ma = (a0 + a1) >> 1, mc = (c0 + c1) >> 1;
+    const uint32_t va = a0 < a1 ? e[ma] : 0u;
+    const uint32_t vc = c0 < c1 ? e[mc] : 0u;
+    if (a0 < a1) {
+      if (va < klo) a0 = ma + 1;
+      else a1 = ma;
+    }
+    if (c0 < c1) {
+      if (vc < khi) c0 = mc + 1;
+      else c1 = mc;
+    }
+  }
+  m.lo = a0;
+  m.hi = top ? m.hi : c0;
+}
+
 // One group of 32 items [g, g + 32) for the calling warp; returns the light edges walked.
 // With nslice > 1 several warps share the group: each reads the group's items, slice 0
 // alone queues the heavy ones, and the light edges are dealt out in steps of 32 * SP_ILP
@@ -530,6 +564,10 @@ __device__ __forceinline__ uint32_t sparse_group(const JobDesc* __restrict__ jd,
   if (it < items) {
     m = sp_item<PERSIST>(jd, sd, it);
     len = m.hi > m.lo ? m.hi - m.lo : 0u;
+    if (len > SP_NARROW && len <= SP_HEAVY) {
+      sp_narrow(sd, m);
+      len = m.hi > m.lo ? m.hi - m.lo : 0u;
+    }
   }
   uint32_t tot = len;
 #pragma unroll
@@ -598,7 +636,12 @@ __device__ __forceinline__ uint32_t sparse_chunk(const JobDesc* __restrict__ jd,
   const unsigned lane = threadIdx.x & 31;
   const uint2 c = ld_plain<PERSIST>(jd->spq + q);
   if (c.x >= items) return 0;  // never indexes outside this round's items
-  const SpItem m = sp_item<PERSIST>(jd, sd, c.x);
+  SpItem m = sp_item<PERSIST>(jd, sd, c.x);
+  {
+    // the item as sparse_group cut it into chunks: narrowed by the same rule
+    const uint32_t len = m.hi > m.lo ? m.hi - m.lo : 0u;
+    if (len > SP_NARROW && len <= SP_HEAVY) sp_narrow(sd, m);
+  }
   const uint32_t e0 = m.lo + c.y * SP_CHUNK;
   const uint32_t e1 = min(m.hi, e0 + SP_CHUNK);
   if (e0 >= e1) return 0;

@@ -338,9 +338,9 @@ def main(argv=None):
     teps_edges, scanned = 0, 0
     per_algo = [0] * len(progs)
     per_algo_ms = [0.0] * len(progs)
-    t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    t_start.record(stream)
-    for _ in range(args.steps):
+    t_marks = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    t_marks[0].record(stream)
+    for k_ in range(args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()
         for stats in run_stream(eng, progs):
@@ -349,11 +349,12 @@ def main(argv=None):
                 scanned += s["edges_scanned"]
                 per_algo[i] += s["count_edges"]
                 per_algo_ms[i] += s["elapsed_ms"]
-    t_end.record(stream)
+        t_marks[k_ + 1].record(stream)
     torch.cuda.synchronize()
     launches = eng.launch_count() - launches0
     clk = clocks.stop()
-    total_ms = t_start.elapsed_time(t_end)
+    total_ms = t_marks[0].elapsed_time(t_marks[-1])
+    step_ms = [round(t_marks[k_].elapsed_time(t_marks[k_ + 1]), 2) for k_ in range(args.steps)]
     if world > 1:
         torch.distributed.barrier()
     total_ms, teps_all = reduce_over_ranks(total_ms, teps_edges, dev, world)
@@ -447,18 +448,23 @@ def main(argv=None):
             run_stream(eng2, progs2, host)
         torch.cuda.synchronize()
         e_edges = 0
-        e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e_start.record(stream)
-        for _ in range(args.steps):
+        e_clocks = Clocks(local)
+        e_clocks.start()
+        e_marks = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+        e_marks[0].record(stream)
+        for k_ in range(args.steps):
             with torch.cuda.stream(stream):
                 flush.zero_()
             e_edges += sum(s["count_edges"] for stats in run_stream(eng2, progs2, host) for s in stats)
-        e_end.record(stream)
+            e_marks[k_ + 1].record(stream)
         torch.cuda.synchronize()
-        e_ms = e_start.elapsed_time(e_end)
+        e_clk = e_clocks.stop()
+        e_ms = e_marks[0].elapsed_time(e_marks[-1])
+        e_step_ms = [round(e_marks[k_].elapsed_time(e_marks[k_ + 1]), 2) for k_ in range(args.steps)]
         e_ms, e_all = reduce_over_ranks(e_ms, e_edges, dev, world)
         e2e = {"value": e_all / (e_ms / 1e3) / 1e9, "unit": "GTEPS",
-               "h2d_bytes_per_step": NB * B * 12, "d2h_bytes_per_step": NB * len(progs) * 56}
+               "h2d_bytes_per_step": NB * B * 12, "d2h_bytes_per_step": NB * len(progs) * 56,
+               "ms_per_step": e_ms / args.steps, "step_ms": e_step_ms, "clocks": e_clk}
     eng.close()
     del d_src, d_tgt, d_w, flush
     torch.cuda.empty_cache()
@@ -498,6 +504,7 @@ def main(argv=None):
             "run_profile": run_profile,
             "autotune": tune,
             "clocks": clk,
+            "step_ms": step_ms,
             "e2e": e2e,
             "cpu_baseline": cpu,
         }

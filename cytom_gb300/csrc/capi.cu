@@ -127,6 +127,8 @@ int upload_store_desc(Ctx* c) {
   h.dir = c->dir;
   h.nbw = c->lvpt >= 5 ? (uint32_t)(c->vpt / 32) : 0u;
   h.dir_ok = (c->dir && c->dir_version == c->version && !c->dir_disabled) ? 1 : 0;
+  h.cmask = h.dir_ok ? c->cmask : nullptr;
+  h.cshift = c->lT > 6 ? c->lT - 6 : 0u;
   h.traversal = (uint32_t)c->cfg.traversal;
   h.xst = c->xs_stage;
   h.xcum = c->xs_cum;
@@ -180,7 +182,7 @@ void job_free(Ctx* c, Job* j) {
   (void)c;
   if (j->loop_exec) cudaGraphExecDestroy(j->loop_exec);
   if (j->ext) pagerank_free(j);
-  void* ptrs[] = {j->h.spq, j->h.aw, j->h.cur, j->h.next, j->h.fa, j->h.ch, j->h.rows, j->h.rank, j->h.rank_c,
+  void* ptrs[] = {j->h.spq, j->h.aw, j->h.awm, j->h.cur, j->h.next, j->h.fa, j->h.ch, j->h.rows, j->h.rank, j->h.rank_c,
                   j->h.delta, j->h.dsum, j->h.contrib, j->h.rank64, j->h.dsum64, j->h.deg_distinct,
                   j->ls, j->d};
   for (void* p : ptrs)
@@ -541,7 +543,7 @@ int cytom_destroy(cytom_ctx* ctx) {
   batch_free(c);
   pagerank_ctx_free(c);
   edge_log_close(c);
-  void* ptrs[] = {c->dir, c->dir_alt, c->edges, c->wts, c->edges_alt, c->wts_alt, c->tile_ptr, c->tile_ptr_alt,
+  void* ptrs[] = {c->dir, c->dir_alt, c->cmask, c->edges, c->wts, c->edges_alt, c->wts_alt, c->tile_ptr, c->tile_ptr_alt,
                   c->chunk_tile, c->chunk_tile_alt, c->app_keys, c->app_keys_alt, c->app_w, c->app_w_alt,
                   c->out_deg, c->in_deg, c->dsd, c->scratch, c->d_flag, c->xs_stage, c->xs_cum,
                   c->xs_colcum, c->xs_tmp, c->pr_pair, c->dyn_pending, c->dyn_next};
@@ -730,6 +732,7 @@ int cytom_clear(cytom_ctx* ctx) {
   if (e == cudaSuccess) e = cudaMemsetAsync(c->tile_ptr, 0, (c->ntiles + 1) * 8, c->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(c->tile_ptr_alt, 0, (c->ntiles + 1) * 8, c->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(c->chunk_tile, 0, 2 * 4, c->stream);
+  if (e == cudaSuccess && c->cmask) e = cudaMemsetAsync(c->cmask, 0, c->n * 8, c->stream);
   if (e != cudaSuccess) return cuda_err(c, e, "clear");
   c->E = 0;
   c->A = 0;

@@ -67,6 +67,12 @@ struct StoreDesc {
   const unsigned long long* xcum;
   const unsigned long long* xcolcum;
   const uint32_t* xnst;
+  // source column masks: bit (y >> cshift) of cmask[u] is set when source u may have an
+  // edge in tile column y (a superset: set for every stored edge, never cleared by
+  // deletions); NULL when the context keeps none. Current whenever dir_ok is.
+  const unsigned long long* cmask;
+  uint32_t cshift;             // log2(T) - 6 above 64 tile columns, else 0
+  uint32_t pad_cm;
 };
 
 // Loop state of one job run, in device memory. Kernels index the double-buffered
@@ -105,6 +111,7 @@ struct JobDesc {
   uint32_t* ch;       // changed bitmap
   uint32_t* rows;     // 2 x T tile-row activity flags (by parity)
   uint32_t* aw;       // indices of the non-zero frontier words (sparse rounds)
+  unsigned long long* awm;  // per listed word: OR of its active sources' column masks
   uint2* spq;         // sparse rounds: queue of (item, chunk) of heavy items
   unsigned long long spq_cap;
   float* rank;        // PageRank family
@@ -178,6 +185,7 @@ struct Ctx {
   std::vector<Job*> sync_jobs;     // an asynchronous request that ran synchronously
   std::vector<cytom_run_stats> sync_stats;
   uint32_t* dir = nullptr;  // source directory (sparse rounds)
+  unsigned long long* cmask = nullptr;  // per-source tile-column masks (StoreDesc::cmask)
   uint32_t* dir_alt = nullptr;  // written by the merge, swapped in with the store
   uint64_t dir_entries = 0;
   uint64_t dir_version = ~0ULL;

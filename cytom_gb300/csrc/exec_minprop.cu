@@ -962,6 +962,7 @@ int minprop_alloc(Ctx* c, Job* j) {
   if (e == cudaSuccess) e = cy_malloc(&h.ch, nwords * 4);
   if (e == cudaSuccess) e = cy_malloc(&h.rows, 2 * c->T * 4);
   if (e == cudaSuccess) e = cy_malloc(&h.aw, nwords * 4);
+  if (e == cudaSuccess) e = cy_malloc(&h.awm, nwords * 8);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return set_err(c, CYTOM_ERR_OOM, "job state");
@@ -1424,8 +1425,8 @@ int minprop_autotune(Ctx* c) {
   JobDesc* d = nullptr;
   char* buf = nullptr;
   const uint64_t qcap = c->E / 32 + c->E / 256 + 1024;
-  const size_t bytes = n * 8 + nwords * 8 + 2 * c->T * 4 + nwords * 4 + sizeof(LoopState) + sizeof(JobDesc) +
-                       qcap * sizeof(uint2) + 8 * 256;
+  const size_t bytes = n * 8 + nwords * 8 + 2 * c->T * 4 + nwords * 12 + sizeof(LoopState) + sizeof(JobDesc) +
+                       qcap * sizeof(uint2) + 9 * 256;
   if (cy_malloc_async((void**)&buf, bytes, c->stream) != cudaSuccess) {
     cudaGetLastError();
     return CYTOM_OK;  // no memory to tune with: keep the current shapes
@@ -1442,6 +1443,7 @@ int minprop_autotune(Ctx* c) {
   h.ch = (uint32_t*)take(nwords * 4);
   h.rows = (uint32_t*)take(2 * c->T * 4);
   h.aw = (uint32_t*)take(nwords * 4);
+  h.awm = (unsigned long long*)take(nwords * 8);
   ls = (LoopState*)take(sizeof(LoopState));
   d = (JobDesc*)take(sizeof(JobDesc));
   h.spq = (uint2*)take(qcap * sizeof(uint2));

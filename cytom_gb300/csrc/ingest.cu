@@ -545,15 +545,27 @@ __global__ void dedupe_lookup_kernel(const uint64_t* __restrict__ K, const uint3
   }
 }
 
+// Also sets the column-mask bit (StoreDesc::cmask) of every appended key's source and
+// tile column, once per run of keys with the same (tile, source); duplicates and dropped
+// corner edges only add bits that are allowed to be spare.
 __global__ void pack_kept_kernel(const uint64_t* __restrict__ K, uint64_t A,
                                  const uint32_t* __restrict__ keep, const uint32_t* __restrict__ P,
                                  const unsigned long long* __restrict__ lb,
                                  const uint32_t* __restrict__ wsel, uint32_t lvpt,
                                  unsigned long long* __restrict__ q, uint32_t* __restrict__ nloc,
-                                 uint32_t* __restrict__ nw, uint32_t* __restrict__ ntile) {
+                                 uint32_t* __restrict__ nw, uint32_t* __restrict__ ntile,
+                                 unsigned long long* __restrict__ cmask, uint32_t lT, uint32_t cshift) {
   uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const uint64_t m = (1ULL << lvpt) - 1ULL;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A; i += stride) {
+    if (cmask) {
+      const uint64_t ts = K[i] >> lvpt;  // (tile, local source)
+      if (i == 0 || (K[i - 1] >> lvpt) != ts) {
+        const uint64_t tile = ts >> lvpt;
+        const uint64_t u = ((tile >> lT) << lvpt) | (ts & m);
+        atomicOr(cmask + u, 1ULL << ((tile & ((1ULL << lT) - 1ULL)) >> cshift));
+      }
+    }
     if (!keep[i]) continue;
     uint64_t key = K[i];
     uint32_t p = P[i];
@@ -963,7 +975,8 @@ int compact(Ctx* c) {
   rc = exclusive_scan_u32(c, keep, P, A, Kdev);
   if (rc) return rc;
   pack_kept_kernel<<<grid_for(c, A, 256), 256, 0, c->stream>>>(K, A, keep, P, lb, wsel, c->lvpt, q,
-                                                               nloc, wt ? nw : nullptr, ntile);
+                                                               nloc, wt ? nw : nullptr, ntile, c->cmask, c->lT,
+                                                               c->lT > 6 ? c->lT - 6 : 0u);
   c->launches++;
   new_tile_ptr_kernel<<<grid_for(c, c->ntiles + 1, 256), 256, 0, c->stream>>>(
       c->tile_ptr, c->ntiles, ntile, Kdev, c->tile_ptr_alt);
@@ -1130,6 +1143,22 @@ __global__ void dir_tiles_kernel(const StoreDesc* __restrict__ sd, uint32_t* __r
   }
 }
 
+// Column-mask bits of every stored edge (a full directory build): one atomic per run of
+// edges with the same source in a tile.
+__global__ void cmask_all_kernel(const StoreDesc* __restrict__ sd, unsigned long long* __restrict__ cmask,
+                                 uint32_t cshift) {
+  const uint64_t E = sd->E, T = sd->T;
+  const uint32_t lT = sd->lT, lvpt = sd->lvpt;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += stride) {
+    uint64_t t = sd->chunk_tile[e / kChunk];
+    while (sd->tile_ptr[t + 1] <= e) ++t;
+    const uint32_t src = sd->edges[e] >> 16;
+    if (e > sd->tile_ptr[t] && (sd->edges[e - 1] >> 16) == src) continue;
+    atomicOr(cmask + (((t >> lT) << lvpt) | src), 1ULL << ((t & (T - 1)) >> cshift));
+  }
+}
+
 int build_directory(Ctx* c) {
   if (c->dir_version == c->version || c->dir_disabled) return CYTOM_OK;
   const char* env = getenv("CYTOM_SPARSE");  // "0": dense rounds only
@@ -1152,10 +1181,23 @@ int build_directory(Ctx* c) {
     }
     c->dir_entries = entries;
   }
+  // column masks: without memory for them sparse rounds read every item's directory entry
+  if (!c->cmask) {
+    if (cy_malloc(&c->cmask, c->n * 8) != cudaSuccess) {
+      cudaGetLastError();
+      c->cmask = nullptr;
+    } else {
+      cudaMemsetAsync(c->cmask, 0, c->n * 8, c->stream);
+    }
+  }
   int slot = prof_begin(c, KC_MERGE);
   if (c->E) {
     dir_edges_kernel<<<grid_for(c, (c->E + 3) / 4, 256), 256, 0, c->stream>>>(c->dsd, c->dir, (uint32_t)nbw);
     c->launches++;
+    if (c->cmask) {
+      cmask_all_kernel<<<grid_for(c, c->E, 256), 256, 0, c->stream>>>(c->dsd, c->cmask, c->lT > 6 ? c->lT - 6 : 0u);
+      c->launches++;
+    }
   }
   dir_tiles_kernel<<<grid_for(c, c->ntiles * 32, 256), 256, 0, c->stream>>>(c->dsd, c->dir, (uint32_t)nbw);
   c->launches++;

@@ -104,6 +104,25 @@ __device__ __forceinline__ void round_open(const JobDesc* __restrict__ jd, const
   }
 }
 
+// Tile columns in which the active sources of frontier word i (bits w) may have edges:
+// the OR of their column masks, read for words with at most four active sources (the
+// sparse rounds' words hold about one); all columns for denser words or without masks.
+__device__ __forceinline__ unsigned long long word_columns(const StoreDesc* __restrict__ sd, uint64_t i,
+                                                           uint32_t w) {
+  const unsigned long long* cm = sd->cmask;
+  if (!cm || __popc(w) > 4) return ~0ULL;
+  unsigned long long m = 0;
+  const unsigned long long* row = cm + (i << 5);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if (w) {
+      m |= row[__ffs(w) - 1];
+      w &= w - 1;
+    }
+  }
+  return m;
+}
+
 // ---- apply ---------------------------------------------------------------
 // One apply step of a block: thread t handles frontier word base + t (base a multiple
 // of 32). `initial` apply = the seeding apply before round 0 (writes parity 0).
@@ -149,7 +168,11 @@ __device__ __forceinline__ void apply_step(const JobDesc* __restrict__ jd, const
       unsigned slot0 = 0;
       if (lane == 0) slot0 = atomicAdd(&ls->nact_words[pw], (unsigned)__popc(nz));
       slot0 = __shfl_sync(0xFFFFFFFFu, slot0, 0);
-      if (w) jd->aw[slot0 + __popc(nz & ((1u << lane) - 1u))] = (uint32_t)i;
+      if (w) {
+        const unsigned slot = slot0 + __popc(nz & ((1u << lane) - 1u));
+        jd->aw[slot] = (uint32_t)i;
+        jd->awm[slot] = word_columns(sd, i, w);
+      }
     }
   }
   if (lvpt >= 10) {
@@ -463,14 +486,13 @@ struct SpItem {
   unsigned long long base;
 };
 
+// Item (word w, tile column y): its frontier bits, directory range and tile base.
 template <bool PERSIST>
-__device__ __forceinline__ SpItem sp_item(const JobDesc* __restrict__ jd, const StoreDesc* __restrict__ sd,
-                                          uint64_t it) {
+__device__ __forceinline__ SpItem sp_item_at(const JobDesc* __restrict__ jd, const StoreDesc* __restrict__ sd,
+                                             uint32_t w, uint32_t y) {
   const uint32_t lT = sd->lT, lnbw = sd->lvpt - 5, nbw = sd->nbw;
-  const uint64_t T = sd->T;
   SpItem r;
-  const uint32_t w = ld_plain<PERSIST>(jd->aw + (it >> lT));
-  r.y = (uint32_t)(it & (T - 1));
+  r.y = y;
   r.x = w >> lnbw;
   const uint32_t b = w & (nbw - 1);
   r.b = b;
@@ -480,6 +502,13 @@ __device__ __forceinline__ SpItem sp_item(const JobDesc* __restrict__ jd, const 
   r.hi = sd->dir[dbase + 1];
   r.base = sd->tile_ptr[((uint64_t)r.x << lT) | r.y];
   return r;
+}
+
+template <bool PERSIST>
+__device__ __forceinline__ SpItem sp_item(const JobDesc* __restrict__ jd, const StoreDesc* __restrict__ sd,
+                                          uint64_t it) {
+  const uint32_t w = ld_plain<PERSIST>(jd->aw + (it >> sd->lT));
+  return sp_item_at<PERSIST>(jd, sd, w, (uint32_t)(it & (sd->T - 1)));
 }
 
 // Relaxes SP_ILP edges per lane whose sources are in their item's frontier word; the
@@ -565,11 +594,19 @@ __device__ __forceinline__ uint32_t sparse_group(const JobDesc* __restrict__ jd,
   SpItem m{};
   uint32_t len = 0;
   if (it < items) {
-    m = sp_item<PERSIST>(jd, sd, it);
-    len = m.hi > m.lo ? m.hi - m.lo : 0u;
-    if (len > SP_NARROW && len <= SP_HEAVY) {
-      sp_narrow(sd, m);
+    // an item whose column no active source of its word reaches holds none of their
+    // edges: it is left empty without reading the directory
+    const uint64_t li = it >> sd->lT;
+    const uint32_t y = (uint32_t)(it & (sd->T - 1));
+    const uint32_t w = ld_plain<PERSIST>(jd->aw + li);
+    const unsigned long long cols = ld_plain<PERSIST>(jd->awm + li);
+    if ((cols >> (y >> sd->cshift)) & 1ULL) {
+      m = sp_item_at<PERSIST>(jd, sd, w, y);
       len = m.hi > m.lo ? m.hi - m.lo : 0u;
+      if (len > SP_NARROW && len <= SP_HEAVY) {
+        sp_narrow(sd, m);
+        len = m.hi > m.lo ? m.hi - m.lo : 0u;
+      }
     }
   }
   uint32_t tot = len;

@@ -102,6 +102,7 @@ struct LoopState {
   unsigned int apply_done;  // blocks of the running apply that finished (last one runs control)
   unsigned int sel_rounds;  // rounds started by the captured loop (bounds it independently)
   unsigned int pad2;
+  unsigned long long items_read;  // sparse rounds: (word, column) items whose directory was read
 };
 
 struct JobDesc {

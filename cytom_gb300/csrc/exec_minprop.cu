@@ -768,16 +768,21 @@ __global__ void __launch_bounds__(256, 4) gather_sparse_kernel(const JobDesc* __
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   const uint64_t items = (uint64_t)ls->nact_words[p] << sd->lT;
   unsigned long long scanned = 0;
+  uint32_t nread = 0;
   // few groups: up to 8 warps share each group's light edges
   const uint64_t groups = (items + 31) / 32;
   uint32_t nslice = 1;
   while (nslice < 8 && groups * nslice * 2 <= nwarps) nslice *= 2;
   const uint32_t slice = (uint32_t)(warp % nslice);
   for (uint64_t g = (warp / nslice) * 32; g < items; g += (nwarps / nslice) * 32)
-    scanned += sparse_group<ALGO, false>(jd, sd, g, items, slice, nslice);
+    scanned += sparse_group<ALGO, false>(jd, sd, g, items, nread, slice, nslice);
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) scanned += __shfl_xor_sync(0xFFFFFFFFu, scanned, o);
+  for (int o = 16; o > 0; o >>= 1) {
+    scanned += __shfl_xor_sync(0xFFFFFFFFu, scanned, o);
+    nread += __shfl_xor_sync(0xFFFFFFFFu, nread, o);
+  }
   if (lane == 0 && scanned) atomicAdd(&ls->edges_scanned, scanned);
+  if (lane == 0 && nread) atomicAdd(&ls->items_read, (unsigned long long)nread);
 }
 
 template <int ALGO>
@@ -1228,7 +1233,8 @@ static bool use_graphs() {
 // (`b`) it: every scanned edge (+ its weight), one value per active source, a read and a
 // reduction per changed target (bounded by the vertices the round activates), and the
 // frontier: the whole bitmap for a dense round; for a sparse round the listed words
-// (index + word) and per (word, tile column) item its two directory entries and tile offset.
+// (index, word and column mask) and, per (word, tile column) item that a source of the
+// word reaches, its two directory entries and tile offset.
 static double round_bytes(const Ctx* c, const LoopState& a, const LoopState& b, double wbytes) {
   const unsigned p = a.iter & 1u;
   const double scanned = (double)(b.edges_scanned - a.edges_scanned);
@@ -1236,7 +1242,7 @@ static double round_bytes(const Ctx* c, const LoopState& a, const LoopState& b, 
   const double changed = (double)b.active[p ^ 1u];
   double bytes = scanned * (4.0 + wbytes) + act * 4.0 + changed * 8.0;
   if (a.mode == 0) bytes += (double)c->n / 8.0;
-  else bytes += (double)a.nact_words[p] * (8.0 + 16.0 * (double)c->T);
+  else bytes += (double)a.nact_words[p] * 16.0 + (double)(b.items_read - a.items_read) * 16.0;
   return bytes;
 }
 

@@ -270,6 +270,7 @@ __device__ __forceinline__ void minprop_begin_state(LoopState* ls, unsigned max_
   ls->active_total = 0;
   ls->apply_done = 0;
   ls->sel_rounds = 0;
+  ls->items_read = 0;
 }
 
 // ---- dense gather: one stage of SG_T * EPT edges ---------------------------
@@ -578,15 +579,16 @@ __device__ __forceinline__ void sp_narrow(const StoreDesc* __restrict__ sd, SpIt
   m.hi = top ? m.hi : c0;
 }
 
-// One group of 32 items [g, g + 32) for the calling warp; returns the light edges walked.
+// One group of 32 items [g, g + 32) for the calling warp; returns the light edges walked
+// and adds the items whose directory entries it read to `nread` (slice 0 only).
 // With nslice > 1 several warps share the group: each reads the group's items, slice 0
 // alone queues the heavy ones, and the light edges are dealt out in steps of 32 * SP_ILP
 // (slice k takes steps k, k + nslice, ...); if the queue overflowed, slice 0 walks every
 // light edge itself (the others' share is then walked twice, which changes nothing).
 template <int ALGO, bool PERSIST>
 __device__ __forceinline__ uint32_t sparse_group(const JobDesc* __restrict__ jd, const StoreDesc* __restrict__ sd,
-                                                 uint64_t g, uint64_t items, uint32_t slice = 0,
-                                                 uint32_t nslice = 1) {
+                                                 uint64_t g, uint64_t items, uint32_t& nread,
+                                                 uint32_t slice = 0, uint32_t nslice = 1) {
   LoopState* ls = jd->ls;
   const unsigned lane = threadIdx.x & 31;
   const uint64_t qcap = jd->spq_cap;
@@ -601,6 +603,7 @@ __device__ __forceinline__ uint32_t sparse_group(const JobDesc* __restrict__ jd,
     const uint32_t w = ld_plain<PERSIST>(jd->aw + li);
     const unsigned long long cols = ld_plain<PERSIST>(jd->awm + li);
     if ((cols >> (y >> sd->cshift)) & 1ULL) {
+      nread += slice == 0 ? 1u : 0u;
       m = sp_item_at<PERSIST>(jd, sd, w, y);
       len = m.hi > m.lo ? m.hi - m.lo : 0u;
       if (len > SP_NARROW && len <= SP_HEAVY) {

@@ -163,15 +163,11 @@ __device__ void unit_sparse(const BJob* J, uint32_t unit) {
   const uint64_t items = (uint64_t)__ldcg(&jd->ls->nact_words[p]) << sd->lT;
   const uint64_t g = (uint64_t)unit * BU_SPARSE_ITEMS + (threadIdx.x >> 5) * 32;
   unsigned long long scanned = 0;
-  uint32_t nread = 0;
+  uint32_t nread = 0;  // items read: the one-job kernels' byte accounting, not kept here
   if (g < items) scanned = sparse_group<ALGO, true>(jd, sd, g, items, nread);
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    scanned += __shfl_xor_sync(0xFFFFFFFFu, scanned, o);
-    nread += __shfl_xor_sync(0xFFFFFFFFu, nread, o);
-  }
+  for (int o = 16; o > 0; o >>= 1) scanned += __shfl_xor_sync(0xFFFFFFFFu, scanned, o);
   if ((threadIdx.x & 31) == 0 && scanned) atomicAdd(&jd->ls->edges_scanned, scanned);
-  if ((threadIdx.x & 31) == 0 && nread) atomicAdd(&jd->ls->items_read, (unsigned long long)nread);
 }
 
 template <int ALGO>

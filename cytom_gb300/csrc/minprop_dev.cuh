@@ -151,12 +151,26 @@ __device__ __forceinline__ void apply_step(const JobDesc* __restrict__ jd, const
     fa[i] = w;
     if (w) {
       ch[i] = 0;
-      uint32_t bits = w;
-      while (bits) {
-        const int b = __ffs(bits) - 1;
-        bits &= bits - 1;
-        const uint64_t v = (i << 5) + b;
-        cur[v] = ld_plain<PERSIST>(next + v);
+      if (!PERSIST && __popc(w) > 2 && ((i + 1) << 5) <= n) {
+        // many changed vertices: the whole word's 32 values in one round trip. A vertex
+        // without its changed bit holds next == current (every lowering of next sets
+        // the bit), so copying it is a no-op. (Not in the persistent kernel, whose
+        // register budget would spill the eight vectors.)
+        const uint4* src = reinterpret_cast<const uint4*>(next + (i << 5));
+        uint4* dst = reinterpret_cast<uint4*>(cur + (i << 5));
+        uint4 q[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) q[k] = ld_plain<PERSIST>(src + k);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) dst[k] = q[k];
+      } else {
+        uint32_t bits = w;
+        while (bits) {
+          const int b = __ffs(bits) - 1;
+          bits &= bits - 1;
+          const uint64_t v = (i << 5) + b;
+          cur[v] = ld_plain<PERSIST>(next + v);
+        }
       }
     }
   }

@@ -23,6 +23,7 @@ FP32-vs-FP64 PageRank, the 64-job batched executor and the RMAT-20 PageRank adjo
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -332,6 +333,11 @@ def main(argv=None):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
+    # the timed regions run with Python's cyclic garbage collector paused (as timeit
+    # does): a full collection of the interpreter's heap is tens of milliseconds of host
+    # time that would otherwise land in a random step
+    gc.collect()
+    gc.disable()
     clocks = Clocks(local)
     clocks.start()
     launches0 = eng.launch_count()
@@ -351,6 +357,7 @@ def main(argv=None):
                 per_algo_ms[i] += s["elapsed_ms"]
         t_marks[k_ + 1].record(stream)
     torch.cuda.synchronize()
+    gc.enable()
     launches = eng.launch_count() - launches0
     clk = clocks.stop()
     total_ms = t_marks[0].elapsed_time(t_marks[-1])
@@ -448,6 +455,8 @@ def main(argv=None):
             run_stream(eng2, progs2, host)
         torch.cuda.synchronize()
         e_edges = 0
+        gc.collect()
+        gc.disable()
         e_clocks = Clocks(local)
         e_clocks.start()
         e_marks = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
@@ -458,6 +467,7 @@ def main(argv=None):
             e_edges += sum(s["count_edges"] for stats in run_stream(eng2, progs2, host) for s in stats)
             e_marks[k_ + 1].record(stream)
         torch.cuda.synchronize()
+        gc.enable()
         e_clk = e_clocks.stop()
         e_ms = e_marks[0].elapsed_time(e_marks[-1])
         e_step_ms = [round(e_marks[k_].elapsed_time(e_marks[k_ + 1]), 2) for k_ in range(args.steps)]

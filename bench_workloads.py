@@ -22,6 +22,7 @@ adjoint: weighted PageRank RMAT-20 forward to L1 1e-8 and its adjoint, checked a
 """
 from __future__ import annotations
 
+import gc
 import json
 import os
 import time
@@ -446,6 +447,18 @@ KEYS = {"prdelta": "prdelta_rmat16", "precision": "precision_rmat26", "batching"
         "adjoint": "adjoint_rmat20"}
 
 
+def _gc_paused(fn, args):
+    """Runs a workload with Python's cyclic garbage collector paused (as timeit does), so
+    that no full collection of the interpreter's heap lands in a timed region of either
+    arm."""
+    gc.collect()
+    gc.disable()
+    try:
+        return fn(args)
+    finally:
+        gc.enable()
+
+
 def all_workloads(args, rank, world, local) -> dict:
     """Every secondary workload in turn; a workload that fails reports its error and the
     others still run."""
@@ -455,7 +468,7 @@ def all_workloads(args, rank, world, local) -> dict:
     for name, fn in WORKLOADS.items():
         t0 = time.time()
         try:
-            r = fn(args)
+            r = _gc_paused(fn, args)
         except Exception as e:  # reported in the line, not hidden
             r = {"error": f"{type(e).__name__}: {e}", "trace": traceback.format_exc()[-1500:]}
         r["wall_s"] = time.time() - t0
@@ -472,7 +485,7 @@ def run_workload(args, rank, world, local):
         return
     import torch
     torch.cuda.set_device(local)
-    r = WORKLOADS[args.workload](args)
+    r = _gc_paused(WORKLOADS[args.workload], args)
     if rank == 0:
         line = {"metric": METRIC, "value": r["value"], "unit": r["unit"], "n_gpus": world, "steps": r.get("steps"),
                 "warmup": 1, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",

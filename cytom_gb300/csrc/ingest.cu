@@ -409,27 +409,43 @@ __global__ void scan_down_kernel(const uint32_t* __restrict__ in, uint32_t* __re
   if (total_out && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *total_out = boff + t;
 }
 
-int exclusive_scan_u32(Ctx* c, const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* total_dev) {
+// Words of scratch a scan of n values needs for its per-tile sums and their offsets,
+// every recursion level together.
+static uint64_t scan_scratch_words(uint64_t n) {
+  const uint64_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+  return nb <= 1 ? 0 : 2 * nb + scan_scratch_words(nb);
+}
+
+// The scan on scratch the caller provides (scan_scratch_words(n) words): launches only.
+static int scan_into(Ctx* c, const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* total_dev,
+                     uint32_t* scratch) {
   if (n == 0) return CYTOM_OK;
-  uint64_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
-  cudaError_t e;
+  const uint64_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
   if (nb == 1) {
     scan_down_kernel<<<1, SCAN_T, 0, c->stream>>>(in, out, n, nullptr, total_dev);
     c->launches++;
     return cuda_err(c, cudaGetLastError(), "scan_down");
   }
-  uint32_t *sums = nullptr, *soffs = nullptr;
-  e = cy_malloc_async((void**)&sums, nb * 4 * 2, c->stream);
-  if (e != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "scan temp");
-  soffs = sums + nb;
+  uint32_t* sums = scratch;
+  uint32_t* soffs = scratch + nb;
   scan_reduce_kernel<<<(unsigned)nb, SCAN_T, 0, c->stream>>>(in, n, sums);
   c->launches++;
-  int rc = exclusive_scan_u32(c, sums, soffs, nb, nullptr);
+  int rc = scan_into(c, sums, soffs, nb, nullptr, scratch + 2 * nb);
   if (rc) return rc;
   scan_down_kernel<<<(unsigned)nb, SCAN_T, 0, c->stream>>>(in, out, n, soffs, total_dev);
   c->launches++;
-  cudaFreeAsync(sums, c->stream);
   return cuda_err(c, cudaGetLastError(), "scan");
+}
+
+int exclusive_scan_u32(Ctx* c, const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* total_dev) {
+  const uint64_t words = scan_scratch_words(n);
+  if (words == 0) return scan_into(c, in, out, n, total_dev, nullptr);
+  uint32_t* scratch = nullptr;
+  if (cy_malloc_async((void**)&scratch, words * 4, c->stream) != cudaSuccess)
+    return set_err(c, CYTOM_ERR_OOM, "scan temp");
+  const int rc = scan_into(c, in, out, n, total_dev, scratch);
+  cudaFreeAsync(scratch, c->stream);
+  return rc;
 }
 
 // --------------------------------------------------------------------------
@@ -446,9 +462,12 @@ int radix_sort_pairs(Ctx* c, uint64_t* keys, uint64_t* keys_alt, uint32_t* vals,
   const uint64_t tile = (uint64_t)RS_T * (small ? RS_IPT_SMALL : RS_IPT_LARGE);
   uint64_t nb = (n + tile - 1) / tile;
   uint32_t* hist = nullptr;
-  cudaError_t e = cy_malloc_async((void**)&hist, nb * 256 * 4 * 2, c->stream);
+  // histogram, its scan and the scan's scratch in one allocation for every pass
+  const uint64_t sw = scan_scratch_words(nb * 256);
+  cudaError_t e = cy_malloc_async((void**)&hist, (nb * 256 * 2 + sw) * 4, c->stream);
   if (e != cudaSuccess) return set_err(c, CYTOM_ERR_OOM, "radix histogram");
   uint32_t* offs = hist + nb * 256;
+  uint32_t* sscr = offs + nb * 256;
   uint64_t *kin = keys, *kout = keys_alt;
   uint32_t *vin = vals, *vout = vals_alt;
   bool alt = false;
@@ -457,8 +476,11 @@ int radix_sort_pairs(Ctx* c, uint64_t* keys, uint64_t* keys_alt, uint32_t* vals,
     if (small) radix_upsweep_kernel<RS_IPT_SMALL><<<(unsigned)nb, RS_T, 0, c->stream>>>(kin, n, shift, hist, (uint32_t)nb);
     else radix_upsweep_kernel<RS_IPT_LARGE><<<(unsigned)nb, RS_T, 0, c->stream>>>(kin, n, shift, hist, (uint32_t)nb);
     c->launches++;
-    int rc = exclusive_scan_u32(c, hist, offs, nb * 256, nullptr);
-    if (rc) return rc;
+    int rc = scan_into(c, hist, offs, nb * 256, nullptr, sscr);
+    if (rc) {
+      cudaFreeAsync(hist, c->stream);
+      return rc;
+    }
     if (small)
       radix_downsweep_kernel<RS_IPT_SMALL><<<(unsigned)nb, RS_T, 0, c->stream>>>(kin, vin, n, shift, offs, (uint32_t)nb,
                                                                                kout, vout);
@@ -468,7 +490,10 @@ int radix_sort_pairs(Ctx* c, uint64_t* keys, uint64_t* keys_alt, uint32_t* vals,
     c->launches++;
     prof_end(c, slot, (double)n * (vals ? 12.0 : 8.0) * 3.0);
     e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_err(c, e, "radix");
+    if (e != cudaSuccess) {
+      cudaFreeAsync(hist, c->stream);
+      return cuda_err(c, e, "radix");
+    }
     std::swap(kin, kout);
     std::swap(vin, vout);
     alt = !alt;
